@@ -1,0 +1,358 @@
+"""Benchmark: Cayley/Crank-Nicolson propagation steps per second on one GB300.
+
+Workload (one step = one Crank-Nicolson step of the whole wavefunction): hydrogen,
+lmax 40 (41 channels), 600 B-splines of order 7 on an exponential-linear grid r in
+[0, 400], Coulomb + length-gauge dipole of an 800 nm sin^2 pulse (peak 0.05 a.u.,
+50 a.u. long), dt = 0.01, GMRES (basis 20) left-preconditioned by the block-diagonal
+banded LU. The measured path is the mixed-precision one: FP64 residual, complex64
+operator and Krylov basis, FP64 Gram-Schmidt sums, Hessenberg least squares, norms and
+true residual (refined until the preconditioned residual is below 1e-12). The same steps
+are also run on the plain FP64 GPU path, and the final-state infidelity between the two
+is reported.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Rank 0 prints one JSON line. ``--impl reference`` times the CPU oracle port of the
+reference algorithm (numpy/scipy complex128, one process per host core, bounded sample).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Cayley propagation steps/s (hydrogen lmax40 N600, mixed FP32/FP64, vs plain FP64 GPU path)"
+WORKLOAD = dict(lmax=40, nbsplines=600, rmax=400.0, timestep=0.01, pulse_duration=50.0, amplitude=0.05,
+                wavelength_nm=800.0, krylov_basis_size=20, gmres_tolerance=1e-12)
+
+
+def _config(precision):
+    from pyprop_gb300.workloads import hydrogen
+    return hydrogen(propagator="CayleyPropagatorGPU", precision=precision, duration=50.0, **WORKLOAD)
+
+
+def initial_state(prob):
+    """Field-free 1s state of the l = 0 channel (host generalized eigenproblem, setup only)."""
+    import scipy.linalg as sl
+    repr_ = prob.psi.GetRepresentation()
+    nang, N = repr_.GetFullShape()
+    bp = prob.Propagator.BasePropagator
+    h0 = bp.PotentialList[0].PotentialData[0]
+    kb = repr_.kb
+    b = 2 * kb + 1
+    H = np.zeros((N, N), dtype=complex)
+    S = np.zeros((N, N))
+    for i in range(N):
+        for j in range(max(0, i - kb), min(N, i + kb + 1)):
+            H[i, j] = h0[j * b + (kb + i - j)]
+            S[i, j] = repr_.overlap_rows[i, kb + j - i]
+    w, v = sl.eigh(H.real, S)
+    psi = np.zeros((nang, N), dtype=complex)
+    psi[0] = v[:, 0] / np.sqrt(v[:, 0] @ S @ v[:, 0])
+    return psi, w[0]
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = [l.split(", ") for l in self.lines if l.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def l2_flush_buffer(torch):
+    return torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def time_matvec(torch, prob, flush, reps=50):
+    """Average duration of the complex64 H matvec kernel (events on the launching stream,
+    L2 flushed before every launch) and its algorithmic bytes per launch."""
+    from pyprop_gb300 import _native as nat
+    bp = prob.Propagator.BasePropagator
+    op = bp.device_operator(nat.PG_FP32)
+    nang, N = prob.psi.GetRepresentation().GetFullShape()
+    src = torch.randn((nang, N), dtype=torch.complex64, device="cuda")
+    dst = torch.empty_like(src)
+    sc = op.scales(5.0)
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        op.matvec(sc, src, dst)
+    total = 0.0
+    for _ in range(reps):
+        flush.fill_(1.0)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        op.matvec(sc, src, dst)
+        e.record(stream)
+        e.synchronize()
+        total += s.elapsed_time(e) * 1e-3
+    avg = total / reps
+    elems = op.stored_elements()
+    bytes_per = 8 * (elems + 2 * nang * N)
+    return avg, bytes_per, elems
+
+
+def run_ours(args):
+    import torch
+    import pyprop_gb300 as pp
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    probs = {}
+    for prec in ("fp32", "fp64"):
+        p = pp.Problem(pp.LoadString(_config(prec)))
+        p.SetupStep(skipWavefunctionSetup=True)
+        probs[prec] = p
+    psi0, e0 = initial_state(probs["fp32"])
+    flush = l2_flush_buffer(torch)
+    stream = torch.cuda.current_stream()
+
+    def run(prob, K, W, timed=True):
+        prob.psi.GetData().copy_(torch.as_tensor(psi0, device="cuda"))
+        prob.PropagatedTime = 0.0
+        for _ in range(W):
+            prob.AdvanceStep()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        total = 0.0
+        iters = 0
+        ctx = prob.Propagator.op64.ctx
+        l0 = ctx.launches()
+        for _ in range(K):
+            flush.fill_(1.0)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            prob.AdvanceStep()
+            e.record(stream)
+            e.synchronize()
+            total += s.elapsed_time(e) * 1e-3
+            iters += prob.Propagator.LastStats.Iterations
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        return total, iters / max(K, 1), ctx.launches() - l0
+
+    with ClockSampler(local) as clk:
+        t_mixed, it_mixed, launches = run(probs["fp32"], args.steps, args.warmup)
+    t_fp64, it_fp64, _ = run(probs["fp64"], args.steps, args.warmup)
+    if dist:
+        tt = torch.tensor([t_mixed, t_fp64], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_mixed, t_fp64 = tt.tolist()
+    psi_m = probs["fp32"].psi.numpy()
+    psi_d = probs["fp64"].psi.numpy()
+    repr_ = probs["fp32"].psi.GetRepresentation()
+    S = repr_.radial.BSplineObject.dense(repr_.overlap_rows)
+    Sm, Sd = psi_m @ S.T, psi_d @ S.T
+    fid = abs(np.vdot(psi_d, Sm)) ** 2 / (np.vdot(psi_m, Sm).real * np.vdot(psi_d, Sd).real)
+    infid = float(1.0 - fid)
+
+    # end to end through the public API with host buffers: H2D + step + D2H per step
+    prob = probs["fp32"]
+    host = torch.empty(psi0.shape, dtype=torch.complex128).pin_memory()
+    host.copy_(torch.as_tensor(psi0))
+    dev = prob.psi.GetData()
+    prob.PropagatedTime = 0.0
+    for _ in range(args.warmup):
+        dev.copy_(host, non_blocking=True)
+        prob.AdvanceStep()
+        host.copy_(dev, non_blocking=True)
+        torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dev.copy_(host, non_blocking=True)
+        prob.AdvanceStep()
+        host.copy_(dev, non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_t = time.perf_counter() - t0
+    nbytes = psi0.size * 16
+
+    avg_mv, bytes_mv, elems = time_matvec(torch, prob, flush)
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_mv / avg_mv / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "matvec_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            traffic = json.load(fh).get("bytes_per_launch")
+
+    cpu = cpu_baseline_sample() if (rank == 0 and world == 1 and not args.no_cpu) else None
+    if rank == 0:
+        steps_per_s = world * args.steps / t_mixed
+        line = {
+            "metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_mixed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64 matvec/basis, f64 reductions+residual",
+            "data": "synthetic (hydrogen model built from the config; initial state = field-free 1s)",
+            "config": {"workload": "hydrogen lmax=40 N=600 rmax=400 Cayley-GMRES(20) block-diag LU, dt=0.01, "
+                                   "800nm sin2 pulse 0.05au", "global_batch": world, "seq_len": None,
+                       "parallelism": "replicas" if world > 1 else "single", "l2": "flushed before every step"},
+            "plain_fp64": {"steps_per_s": world * args.steps / t_fp64, "gmres_iterations_per_step": it_fp64},
+            "speedup_vs_plain_fp64": t_fp64 / t_mixed,
+            "infidelity_vs_fp64_gpu": infid,
+            "gmres_iterations_per_step": it_mixed,
+            "e2e": {"value": world * args.steps / e2e_t, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": nbytes},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "kernel": "op_matvec_kernel<float,6>", "avg_launch_us": 1e6 * avg_mv,
+                         "algorithmic_bytes": bytes_mv, "peak_kind": peak_kind,
+                         "note": "working set (%.1f MB) is L2 resident between launches only without the flush" %
+                                 (bytes_mv / 1e6)},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+            "ground_energy": e0,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------------------
+# CPU reference (oracle port of the reference algorithm)
+# ---------------------------------------------------------------------------------------
+
+def _oracle_setup():
+    import pyprop_gb300 as pp
+    from oracle.propagators import OracleCayley, OracleHamiltonian
+    prob = pp.Problem(pp.LoadString(_config("fp64")))
+    repr_ = prob.psi.GetRepresentation()
+    nang, N = repr_.GetFullShape()
+    bp = prob.Propagator.BasePropagator
+    terms = [("_".join(g.GetStorageId() for g in p.GeometryList), p.PotentialData, p.GeometryList[0].GetBasisPairs(),
+              p.TimeFunction) for p in bp.PotentialList]
+    ham = OracleHamiltonian(terms, repr_.overlap_rows, nang, N)
+    cay = OracleCayley(ham, WORKLOAD["timestep"], [0], WORKLOAD["krylov_basis_size"], WORKLOAD["gmres_tolerance"])
+    psi0, _ = initial_state(prob)
+    return cay, psi0
+
+
+def _oracle_worker(nsteps, q):
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    cay, psi = _oracle_setup()
+    dt = WORKLOAD["timestep"]
+    t0 = time.perf_counter()
+    t = 0.0
+    for _ in range(nsteps):
+        psi = cay.step(psi, t, dt)
+        t += dt
+    q.put(time.perf_counter() - t0)
+
+
+def cpu_baseline_sample(nsteps=20, procs=1):
+    """Oracle Cayley steps on the host, `procs` processes each stepping its own copy."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_oracle_worker, args=(nsteps, q)) for _ in range(procs)]
+    for p in ps:
+        p.start()
+    times = [q.get() for _ in ps]
+    for p in ps:
+        p.join()
+    return {"value": procs * nsteps / max(times), "unit": "steps/s", "cores": procs, "kind": "port",
+            "sample": "%d Cayley steps from t=0 per process, numpy/scipy complex128 oracle of the reference "
+                      "algorithm (OPENBLAS_NUM_THREADS=1)" % nsteps}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    procs = os.cpu_count() or 1
+    nsteps = max(1, min(args.steps, 10))
+    base = cpu_baseline_sample(nsteps=nsteps, procs=procs)
+    line = {"metric": METRIC, "value": base["value"], "unit": "steps/s", "n_gpus": 0, "steps": nsteps * procs,
+            "warmup": 0, "ms_per_step": 1e3 / base["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "hydrogen lmax=40 N=600 rmax=400 Cayley-GMRES(20) block-diag LU, dt=0.01"},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    from pyprop_gb300 import build_native
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        build_native.build()
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,240 @@
+/*
+ * pyprop_gpu.h - C ABI of the GB300 propagation hot path.
+ *
+ * One shared library, libpyprop_gpu.so, built for sm_103a. Plain C types only: device
+ * buffers are passed as pointers, complex numbers as interleaved (re, im) pairs of double
+ * or float, streams as cudaStream_t cast to void*. Every entry point returns 0 on success
+ * or a negative PG_ERR_* code; pg_error_string() names it. Nothing here falls back to the
+ * CPU: without a usable CUDA device the calls fail with PG_ERR_CUDA.
+ *
+ * Wavefunction layout is the reference's C order: rank 2 (one electron) is [Nang][N]
+ * (angular channel, B-spline); rank 3 (two electrons) is [Nang][N][N].
+ */
+#ifndef PYPROP_GPU_H
+#define PYPROP_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------------- */
+/* status codes, precision, context                                                   */
+/* ---------------------------------------------------------------------------------- */
+
+enum {
+    PG_OK = 0,
+    PG_ERR_ARG = -1,           /* bad argument (null pointer, size out of range) */
+    PG_ERR_CUDA = -2,          /* a CUDA runtime call failed or no device */
+    PG_ERR_STORAGE = -3,       /* storage id combination not supported */
+    PG_ERR_SHAPE = -4,         /* extents disagree with the operator or wavefunction */
+    PG_ERR_NONFINITE = -5,     /* NaN/Inf detected by a checking kernel */
+    PG_ERR_BREAKDOWN = -6,     /* Krylov breakdown that the method cannot absorb */
+    PG_ERR_NOT_CONVERGED = -7, /* iterative solve stopped at its iteration cap */
+    PG_ERR_ALLOC = -8,         /* device allocation failed */
+    PG_ERR_STATE = -9          /* object used before setup / after destroy */
+};
+
+enum { PG_FP64 = 0, PG_FP32 = 1 };
+
+typedef struct pg_ctx pg_ctx;
+
+/* Error name for a status code (static string). */
+const char *pg_error_string(int code);
+
+/* Library build string: compiler, arch, build flags. */
+const char *pg_version(void);
+
+/* Create a context on CUDA device `device` with its own non-blocking stream. */
+int pg_ctx_create(int device, pg_ctx **out);
+int pg_ctx_destroy(pg_ctx *ctx);
+/* The context's stream (cudaStream_t as void*). */
+void *pg_ctx_stream(pg_ctx *ctx);
+/* Use the caller's stream for all later work of this context (NULL = own stream). */
+int pg_ctx_set_stream(pg_ctx *ctx, void *stream);
+/* Count of kernels this context launched since creation (own kernels only). */
+long long pg_ctx_kernel_launches(pg_ctx *ctx);
+int pg_ctx_synchronize(pg_ctx *ctx);
+
+/* ---------------------------------------------------------------------------------- */
+/* reference-layout tensor multiply                                                   */
+/* ---------------------------------------------------------------------------------- */
+/*
+ * Device twins of the generated Fortran kernels tensorpotentialmultiply_<ids>_ for rank 2
+ * (pyprop: core/tensorpotential/tensorpotentialmultiply_generator.py:1391-1495, storage
+ * snippets Diag :403-432, Simp :302-363, Ident :436-462, BandNH :622-762). Same argument
+ * order and meaning, all pointers on the device, complex128 interleaved:
+ *     dest += scaling * V * source
+ * The potential is in the reference's layout [pairs0][N*(2k+1)], BandNH slot
+ * j*(2k+1) + (k+i-j) holding V(i, j). `bandCount` is k (super diagonals).
+ */
+int pg_tensor_multiply_diag_bandnh(const double *potential, int potExtent0, int potExtent1,
+                                   double scaling,
+                                   const double *source, int srcExtent0, int srcExtent1,
+                                   double *dest, int dstExtent0, int dstExtent1,
+                                   int bandCount, void *stream);
+int pg_tensor_multiply_simp_bandnh(const double *potential, int potExtent0, int potExtent1,
+                                   double scaling,
+                                   const double *source, int srcExtent0, int srcExtent1,
+                                   double *dest, int dstExtent0, int dstExtent1,
+                                   const int *pair0, int pair0Extent0, int pair0Extent1,
+                                   int bandCount, void *stream);
+int pg_tensor_multiply_ident_bandnh(const double *potential, int potExtent0, int potExtent1,
+                                    double scaling,
+                                    const double *source, int srcExtent0, int srcExtent1,
+                                    double *dest, int dstExtent0, int dstExtent1,
+                                    int bandCount, void *stream);
+
+/* ---------------------------------------------------------------------------------- */
+/* fused device operator: sum over terms of scale[slot] * V_term                       */
+/* ---------------------------------------------------------------------------------- */
+/*
+ * Replaces the Python loop over consolidated TensorPotentials
+ * (pyprop/tensorpotential/BasisPropagator.py:116-159, TensorPotential.py:92-112) by one
+ * resident operator applied in one launch. Terms are added in the reference layout and
+ * converted once to the device layout (per-pair bands stored diagonal-major).
+ */
+typedef struct pg_op pg_op;
+
+/* shape: rank-2 {Nang, N}. bandCount k: the radial band has 2k+1 diagonals. */
+int pg_op_create(pg_ctx *ctx, int rank, const int *shape, int bandCount, int precision, pg_op **out);
+int pg_op_destroy(pg_op *op);
+/*
+ * Add one term. storage: "Diag_BandNH", "Simp_BandNH" or "Ident_BandNH".
+ * potential: host complex128 [potExtent0][potExtent1] in the reference layout.
+ * pairs0: host int32 [npairs0][2] (row, col) for Simp (ignored otherwise).
+ * slot: which scale multiplies this term (0 <= slot < 16).
+ */
+int pg_op_add_term(pg_op *op, const char *storage, const double *potential, int potExtent0,
+                   int potExtent1, const int *pairs0, int npairs0, int slot);
+/* Upload. Must be called once after the last add_term. */
+int pg_op_finalize(pg_op *op);
+/* Number of complex band elements the operator stores (for roofline bookkeeping). */
+long long pg_op_stored_elements(const pg_op *op);
+/*
+ * dst = (accumulate ? dst : 0) + sum_t scales[slot_t] * V_t * src
+ * scales: host complex128 array [nscales] (interleaved), nscales <= 16.
+ * src/dst: device arrays in the operator's precision (complex128 or complex64).
+ */
+int pg_op_matvec(pg_op *op, const double *scales, int nscales, const void *src, void *dst,
+                 int accumulate);
+
+/* ---------------------------------------------------------------------------------- */
+/* banded fibre operators: overlap S = U^T U and block-diagonal preconditioner LU      */
+/* ---------------------------------------------------------------------------------- */
+/*
+ * Replaces OverlapMatrix multiply/solve along the B-spline rank
+ * (core/representation/overlapmatrix.cpp:123-229, zpbtrf factor :35-37) and the
+ * per-channel banded LU of BSplineSolver (core/transform/bspline/bsplinesolver.h:43-162).
+ * A fibre is one radial vector psi[a][:] (rank 2). Solves run one warp per fibre over
+ * 32-row blocks with precomputed inverse diagonal blocks.
+ */
+typedef struct pg_banded pg_banded;
+
+/*
+ * Overlap: `overlap_rows` is host float64 [N][2k+1], row i column k+(j-i) = S(i, j).
+ * The Cholesky factor is computed on the host in float64.
+ */
+int pg_overlap_create(pg_op *op, const double *overlap_rows, pg_banded **out);
+/*
+ * Block-diagonal preconditioner M_a = cS * S + cH * H_a for every angular channel a,
+ * H_a from the Diag_BandNH terms of `op` with the given slots weighted by slot_weights
+ * (complex128). Factored M = L U without pivoting (M has a positive definite Hermitian part).
+ */
+int pg_prec_blockdiag_create(pg_op *op, const double *overlap_rows, const double *cS,
+                             const double *cH, const int *slots, const double *slot_weights,
+                             int nslots, pg_banded **out);
+int pg_banded_destroy(pg_banded *b);
+
+enum {
+    PG_BAND_MUL_U = 0,     /* x <- U x            (MultiplySqrtOverlap(false)) */
+    PG_BAND_MUL_UT = 1,    /* x <- U^H x          (MultiplySqrtOverlap(true)) */
+    PG_BAND_SOLVE_U = 2,   /* x <- U^-1 x         (SolveSqrtOverlap(false)) */
+    PG_BAND_SOLVE_UT = 3,  /* x <- U^-H x         (SolveSqrtOverlap(true)) */
+    PG_BAND_MUL_S = 4,     /* x <- S x            (MultiplyOverlap) */
+    PG_BAND_SOLVE_S = 5,   /* x <- S^-1 x         (SolveOverlap) */
+    PG_BAND_PREC_SOLVE = 6 /* x <- M_a^-1 x per channel (preconditioner Solve) */
+};
+/* In place on a device wavefunction in the operator's precision. */
+int pg_banded_apply(pg_banded *b, int which, void *x);
+
+/* ---------------------------------------------------------------------------------- */
+/* Krylov propagators and solvers                                                     */
+/* ---------------------------------------------------------------------------------- */
+
+typedef struct pg_krylov_stats {
+    long long OpCount;           /* operator applications */
+    long long InnerProductCount; /* block inner products (one per Gram-Schmidt pass) */
+    long long ReOrthoCount;      /* second Gram-Schmidt passes */
+    long long RestartCount;      /* pIRAM restarts */
+    long long Iterations;        /* GMRES iterations in the last solve */
+    double ErrorEstimate;        /* pAMP |last Krylov coefficient|^2 or GMRES residual */
+    double TrueResidual;         /* GMRES: ||b - A x|| recomputed after the solve */
+} pg_krylov_stats;
+
+typedef struct pg_pamp pg_pamp;
+/*
+ * pAMP exp(-i dt H) psi (core/krylov/pamp/pamp/pamp.h:613-670) in the balanced-overlap
+ * form of PamPropagator.AdvanceStep (pyprop/propagator/PamPropagator.py:50-75):
+ * psi <- U psi; Krylov with U^-H H(t) U^-1; psi <- U^-1 psi. H is frozen at t.
+ * basis_precision: PG_FP64 or PG_FP32 Arnoldi basis (psi itself is always complex128).
+ * double_ortho: 1 always runs a second Gram-Schmidt pass (CGS2).
+ */
+int pg_pamp_create(pg_op *op64, pg_op *op_basis, pg_banded *ovl64, pg_banded *ovl_basis,
+                   int basis_size, int basis_precision, int double_ortho, pg_pamp **out);
+int pg_pamp_destroy(pg_pamp *p);
+/* One step. scales: host complex128 [nscales], H(t) slot values. psi: device complex128. */
+int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scales, int nscales,
+                 pg_krylov_stats *stats);
+
+typedef struct pg_cayley pg_cayley;
+/*
+ * Cayley / Crank-Nicolson step (pyprop/propagator/CayleyPropagator.py:71-150):
+ * (S + i dt/2 H) psi' = (S - i dt/2 H) psi with GMRES (core/krylov/gmres/gmres.h:433-505),
+ * left-preconditioned by the block-diagonal LU. FP64 mode: the reference's scheme with
+ * x0 = 0. Mixed mode (basis_precision PG_FP32): the residual r = b - A psi is formed in
+ * FP64, GMRES in FP32 solves A d = r, psi' = psi + d, and the FP64 true residual is
+ * checked (refinement repeats while it is above `tolerance`).
+ */
+int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64, pg_banded *prec_basis,
+                     int basis_size, int basis_precision, double tolerance, pg_cayley **out);
+int pg_cayley_destroy(pg_cayley *c);
+/* scales: host complex128 [nscales]: slot values of H(t + dt/2). Slot 0 must be the S term
+ * weight-free slot reserved by the caller (see pg_cayley_create docs in the host layer). */
+int pg_cayley_step(pg_cayley *c, void *psi, double dt, const double *scales, int nscales,
+                   pg_krylov_stats *stats);
+
+/* Arnoldi expansion used by pIRAM (core/krylov/piram/piram/piram.h:346-442), Euclidean
+ * inner product, re-orthogonalisation on. Operator: S^-1 H(slot scales) or, when
+ * shift_invert (a pg_prec_blockdiag_create object for M = H0 - sigma S) is given,
+ * M^-1 S - the shift-invert operator of GMRESShiftInvertSolver
+ * (pyprop/solver/GMRESShiftInvertSolver.py:103-131) for an H diagonal in the angular rank.
+ * On entry V[0..j0] (device complex128 [m][Npsi]) hold the basis and f the residual; the
+ * call fills V[j0+1..m-1], the Hessenberg columns of H (host complex128 [m][m], row
+ * major) and leaves the last residual in f. If ||f|| < breakdown_tol before a new
+ * vector, it stops with *steps_done = that vector's index so the caller can put a random
+ * vector into f and call again with inject = 1 (f is then orthogonalised against the basis
+ * and the subdiagonal entry set to 0). *steps_done = m when the expansion completed. */
+int pg_arnoldi_expand(pg_op *op64, pg_banded *ovl64, pg_banded *shift_invert, const double *scales,
+                      int nscales, void *V, int m, int j0, void *f, double *H, double breakdown_tol,
+                      int inject, int *steps_done, double *residual_norm_out, pg_krylov_stats *stats);
+
+/* ---------------------------------------------------------------------------------- */
+/* vector utilities on device wavefunctions                                           */
+/* ---------------------------------------------------------------------------------- */
+
+/* out = sum conj(x) y over n complex elements, FP64 accumulation. precision selects the
+ * element type. out: host complex128. */
+int pg_vec_dot(pg_ctx *ctx, int precision, const void *x, const void *y, long long n, double *out);
+/* y (precision) <- convert(x (other precision)); n complex elements. */
+int pg_vec_convert(pg_ctx *ctx, int src_precision, const void *x, int dst_precision, void *y, long long n);
+/* V (complex128 [k][n]) <- V (complex128 [m][n]) * Q (host complex128 [m][k], row major) */
+int pg_vec_combine(pg_ctx *ctx, void *V, long long n, int m, const double *Q, int k);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYPROP_GPU_H */

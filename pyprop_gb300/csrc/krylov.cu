@@ -1,0 +1,634 @@
+// Krylov drivers: pAMP exp(-i dt H) psi, Cayley/Crank-Nicolson GMRES, Arnoldi expansion
+// for pIRAM. Host C++ orchestrates device kernels; the small dense problems (Hessenberg
+// exponential, least squares by Givens rotations) run on the host in FP64.
+//
+// Reference algorithms:
+//   pAMP  core/krylov/pamp/pamp/pamp.h:270-351 (Arnoldi), :430-565 (scaling and squaring,
+//         diagonal Pade of order 6 evaluated by Horner in A^2), :613-670 (PropagateVector)
+//   GMRES core/krylov/gmres/gmres.h:260-354 (Arnoldi with double Gram-Schmidt),
+//         :433-505 (SolveVector: x0 = 0, least squares each iteration, tolerance floor 1e-13)
+//   pIRAM core/krylov/piram/piram/piram.h:346-442 (Arnoldi steps)
+// Gram-Schmidt here is always classical with a second pass (CGS2); the reference's
+// DGKS test (0.717) only decides whether the second pass runs, which changes results at
+// the rounding level.
+#include "pg_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <limits>
+
+typedef std::complex<double> zd;
+
+template <typename Rd, typename Rs>
+int pg_scale_copy(pg_ctx *ctx, const cx<Rs> *src, cx<Rd> *dst, cx<Rd> *dst2, long long n, const double *inv_scale_dev,
+                  double mul);
+template <typename R>
+int pg_combine(pg_ctx *ctx, const cx<R> *V, long long ldv, int k, const double *c_dev, double alpha, cxd *out,
+               long long n, int accumulate);
+int pg_axpy(pg_ctx *ctx, cxd a, const cxd *x, cxd *y, long long n);
+
+// ------------------------------------------------------------------------------------
+// small dense FP64 helpers (row-major)
+// ------------------------------------------------------------------------------------
+namespace dense {
+
+void matmul(int n, const zd *A, const zd *B, zd *C)
+{
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            zd s(0.0, 0.0);
+            for (int k = 0; k < n; ++k) s += A[i * n + k] * B[k * n + j];
+            C[i * n + j] = s;
+        }
+}
+
+// Solve A X = B (n x n, nrhs columns) by LU with partial pivoting. Returns false if singular.
+bool solve(int n, std::vector<zd> A, zd *B, int nrhs)
+{
+    std::vector<int> piv(n);
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        double best = std::abs(A[k * n + k]);
+        for (int i = k + 1; i < n; ++i)
+            if (std::abs(A[i * n + k]) > best) { best = std::abs(A[i * n + k]); p = i; }
+        if (best == 0.0) return false;
+        piv[k] = p;
+        if (p != k) {
+            for (int j = 0; j < n; ++j) std::swap(A[k * n + j], A[p * n + j]);
+            for (int j = 0; j < nrhs; ++j) std::swap(B[k * nrhs + j], B[p * nrhs + j]);
+        }
+        for (int i = k + 1; i < n; ++i) {
+            const zd l = A[i * n + k] / A[k * n + k];
+            A[i * n + k] = l;
+            for (int j = k + 1; j < n; ++j) A[i * n + j] -= l * A[k * n + j];
+            for (int j = 0; j < nrhs; ++j) B[i * nrhs + j] -= l * B[k * nrhs + j];
+        }
+    }
+    for (int j = 0; j < nrhs; ++j)
+        for (int i = n - 1; i >= 0; --i) {
+            zd s = B[i * nrhs + j];
+            for (int q = i + 1; q < n; ++q) s -= A[i * n + q] * B[q * nrhs + j];
+            B[i * nrhs + j] = s / A[i * n + i];
+        }
+    return true;
+}
+
+// exp(A) by scaling and squaring with the diagonal Pade approximant of `order`:
+// N(x) = sum c_i x^i, c_0 = 1, c_{i+1} = c_i (p-i) / ((i+1)(2p-i)); D(x) = N(-x);
+// N/D = I + 2 (E - O)^-1 O with E, O the even and odd parts (sign flips for odd p).
+bool expm_pade(int n, const zd *Ain, zd *E, int order)
+{
+    double maxabs = 0.0;
+    for (int k = 0; k < n * n; ++k) maxabs = std::max(maxabs, std::abs(Ain[k]));
+    int s = maxabs > 0.0 ? (int)std::ceil(std::log2(maxabs)) : 0;
+    s = std::max(0, s);
+    const double scale = std::ldexp(1.0, -s);
+    std::vector<zd> A(n * n), A2(n * n), P(n * n, 0.0), Q(n * n, 0.0), T(n * n);
+    for (int k = 0; k < n * n; ++k) A[k] = Ain[k] * scale;
+    matmul(n, A.data(), A.data(), A2.data());
+    std::vector<double> c(order + 1);
+    c[0] = 1.0;
+    for (int i = 0; i < order; ++i) c[i + 1] = c[i] * (double)(order - i) / (double)((i + 1) * (2 * order - i));
+    for (int i = 0; i < n; ++i) {
+        Q[i * n + i] = c[order];
+        P[i * n + i] = c[order - 1];
+    }
+    bool odd = true;
+    for (int i = order - 2; i >= 0; --i) {
+        std::vector<zd> &M = odd ? Q : P;
+        matmul(n, M.data(), A2.data(), T.data());
+        M.swap(T);
+        for (int r = 0; r < n; ++r) M[r * n + r] += c[i];
+        odd = !odd;
+    }
+    {
+        std::vector<zd> &M = odd ? Q : P;
+        matmul(n, M.data(), A.data(), T.data());
+        M.swap(T);
+    }
+    std::vector<zd> D(n * n);
+    for (int k = 0; k < n * n; ++k) D[k] = Q[k] - P[k];
+    if (!solve(n, D, P.data(), n)) return false;
+    for (int k = 0; k < n * n; ++k) E[k] = 2.0 * P[k];
+    for (int i = 0; i < n; ++i) E[i * n + i] += 1.0;
+    if (odd)
+        for (int k = 0; k < n * n; ++k) E[k] = -E[k];
+    for (int q = 0; q < s; ++q) {
+        matmul(n, E, E, T.data());
+        std::copy(T.begin(), T.end(), E);
+    }
+    return true;
+}
+
+}  // namespace dense
+
+// ------------------------------------------------------------------------------------
+// shared Arnoldi machinery
+// ------------------------------------------------------------------------------------
+// Column buffers on the device: for Arnoldi step j, three reduction outputs of
+// 2*(m+2) doubles each: pass-1 dots, pass-2 dots, final norm.
+struct ArnoldiBuf {
+    double *d_cols = nullptr;  // [m][3][2*(m+2)]
+    double *h_cols = nullptr;  // pinned mirror
+    int m = 0;
+    size_t col_doubles() const { return 2 * (size_t)(m + 2); }
+    double *dcol(int j, int pass) { return d_cols + ((size_t)j * 3 + pass) * col_doubles(); }
+    double *hcol(int j, int pass) { return h_cols + ((size_t)j * 3 + pass) * col_doubles(); }
+    int alloc(int m_)
+    {
+        m = m_;
+        const size_t bytes = sizeof(double) * (size_t)m * 3 * col_doubles();
+        PG_CUDA_TRY(cudaMalloc(&d_cols, bytes));
+        PG_CUDA_TRY(cudaMemset(d_cols, 0, bytes));
+        PG_CUDA_TRY(cudaMallocHost(&h_cols, bytes));
+        return PG_OK;
+    }
+    void release()
+    {
+        cudaFree(d_cols);
+        if (h_cols) cudaFreeHost(h_cols);
+        d_cols = nullptr;
+        h_cols = nullptr;
+    }
+};
+
+// Orthogonalise w against V[0..J) with CGS2. Results: pass0 col = h1 (J) + ||w0||,
+// pass1 col = h2 (J) + ..., pass2 col = final ||w||^2, ||w||.
+template <typename R>
+static int cgs2(pg_ctx *ctx, const cx<R> *V, long long n, int J, cx<R> *w, ArnoldiBuf &ab, int j, int double_ortho,
+                pg_krylov_stats *st)
+{
+    PG_TRY(pg_multidot<R>(ctx, V, n, J, w, n, ab.dcol(j, 0)));
+    if (double_ortho) {
+        PG_TRY(pg_gs_update<R>(ctx, V, n, J, ab.dcol(j, 0), w, n, 1, ab.dcol(j, 1)));
+        PG_TRY(pg_gs_update<R>(ctx, V, n, J, ab.dcol(j, 1), w, n, 0, ab.dcol(j, 2)));
+        if (st) { st->InnerProductCount += 2; st->ReOrthoCount += 1; }
+    } else {
+        PG_TRY(pg_gs_update<R>(ctx, V, n, J, ab.dcol(j, 0), w, n, 0, ab.dcol(j, 2)));
+        if (st) st->InnerProductCount += 1;
+    }
+    return PG_OK;
+}
+
+// host: Hessenberg column j (entries 0..J-1) and subdiagonal beta from the pinned mirror
+static void read_column(ArnoldiBuf &ab, int j, int J, int double_ortho, zd *hcol, double *beta)
+{
+    const double *p0 = ab.hcol(j, 0), *p1 = ab.hcol(j, 1), *p2 = ab.hcol(j, 2);
+    for (int i = 0; i < J; ++i) {
+        zd h(p0[2 * i], p0[2 * i + 1]);
+        if (double_ortho) h += zd(p1[2 * i], p1[2 * i + 1]);
+        hcol[i] = h;
+    }
+    *beta = p2[2 * J + 1];
+}
+
+static int fetch_columns(pg_ctx *ctx, ArnoldiBuf &ab, int j0, int j1)
+{
+    if (j1 <= j0) return PG_OK;
+    const size_t off = (size_t)j0 * 3 * ab.col_doubles();
+    const size_t cnt = (size_t)(j1 - j0) * 3 * ab.col_doubles();
+    PG_CUDA_TRY(cudaMemcpyAsync(ab.h_cols + off, ab.d_cols + off, cnt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return PG_OK;
+}
+
+static pg_scales to_scales(const double *s, int n)
+{
+    pg_scales sc;
+    for (int k = 0; k < PG_MAX_SLOTS; ++k) sc.s[k] = mk<double>(k < n ? s[2 * k] : 0.0, k < n ? s[2 * k + 1] : 0.0);
+    return sc;
+}
+
+// ------------------------------------------------------------------------------------
+// pAMP
+// ------------------------------------------------------------------------------------
+struct pg_pamp {
+    pg_op *op64 = nullptr, *opb = nullptr;
+    pg_banded *ovl64 = nullptr, *ovlb = nullptr;
+    int m = 0, prec = PG_FP64, double_ortho = 1;
+    long long n = 0;
+    void *V = nullptr;    // [m][n] basis precision
+    void *w = nullptr;    // [n] basis precision
+    void *tmp = nullptr;  // [n] basis precision
+    double *d_c = nullptr;
+    double *h_c = nullptr;
+    double *d_norm = nullptr;  // 2 doubles: ||psi||^2, ||psi||
+    ArnoldiBuf ab;
+    double tolerance = std::sqrt(std::numeric_limits<double>::epsilon());
+};
+
+extern "C" int pg_pamp_create(pg_op *op64, pg_op *op_basis, pg_banded *ovl64, pg_banded *ovl_basis, int basis_size,
+                              int basis_precision, int double_ortho, pg_pamp **out)
+{
+    if (!op64 || !op_basis || !ovl64 || !ovl_basis || !out) return PG_ERR_ARG;
+    if (basis_size < 2 || basis_size > PG_RED_COLS - 2) return PG_ERR_ARG;
+    if (op64->precision != PG_FP64 || op_basis->precision != basis_precision) return PG_ERR_ARG;
+    if (ovl64->op->precision != PG_FP64 || ovl_basis->op->precision != basis_precision) return PG_ERR_ARG;
+    if (!op64->finalized || !op_basis->finalized) return PG_ERR_STATE;
+    pg_pamp *p = new pg_pamp();
+    p->op64 = op64;
+    p->opb = op_basis;
+    p->ovl64 = ovl64;
+    p->ovlb = ovl_basis;
+    p->m = basis_size;
+    p->prec = basis_precision;
+    p->double_ortho = double_ortho ? 1 : 0;
+    p->n = (long long)op64->nrows * op64->N;
+    const size_t esz = basis_precision == PG_FP64 ? sizeof(cxd) : sizeof(cxf);
+    PG_CUDA_TRY(cudaMalloc(&p->V, esz * (size_t)p->m * p->n));
+    PG_CUDA_TRY(cudaMalloc(&p->w, esz * (size_t)p->n));
+    PG_CUDA_TRY(cudaMalloc(&p->tmp, esz * (size_t)p->n));
+    PG_CUDA_TRY(cudaMalloc(&p->d_c, sizeof(double) * 2 * p->m));
+    PG_CUDA_TRY(cudaMallocHost(&p->h_c, sizeof(double) * 2 * p->m));
+    PG_CUDA_TRY(cudaMalloc(&p->d_norm, sizeof(double) * 2 * (PG_RED_COLS)));
+    PG_TRY(p->ab.alloc(p->m));
+    *out = p;
+    return PG_OK;
+}
+
+extern "C" int pg_pamp_destroy(pg_pamp *p)
+{
+    if (!p) return PG_ERR_ARG;
+    cudaFree(p->V);
+    cudaFree(p->w);
+    cudaFree(p->tmp);
+    cudaFree(p->d_c);
+    if (p->h_c) cudaFreeHost(p->h_c);
+    cudaFree(p->d_norm);
+    p->ab.release();
+    delete p;
+    return PG_OK;
+}
+
+template <typename R>
+static int pamp_arnoldi(pg_pamp *p, const pg_scales &sc, pg_krylov_stats *st)
+{
+    pg_ctx *ctx = p->op64->ctx;
+    const long long n = p->n;
+    cx<R> *V = (cx<R> *)p->V;
+    cx<R> *w = (cx<R> *)p->w;
+    cx<R> *tmp = (cx<R> *)p->tmp;
+    for (int j = 0; j < p->m; ++j) {
+        if (j > 0) {
+            // V[j] = f / beta_{j-1}; tmp = V[j]
+            PG_TRY((pg_scale_copy<R, R>(ctx, w, V + (size_t)j * n, tmp, n, p->ab.dcol(j - 1, 2) + 2 * j + 1, 1.0)));
+        } else {
+            PG_CUDA_TRY(cudaMemcpyAsync(tmp, V, sizeof(cx<R>) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+        }
+        // w = U^-H H U^-1 V[j]
+        PG_TRY(pg_banded_apply_dev(p->ovlb, PG_BAND_SOLVE_U, tmp));
+        PG_TRY(pg_op_matvec_dev(p->opb, sc, nullptr, tmp, w, 0, nullptr, nullptr));
+        PG_TRY(pg_banded_apply_dev(p->ovlb, PG_BAND_SOLVE_UT, w));
+        if (st) st->OpCount++;
+        PG_TRY(cgs2<R>(ctx, V, n, j + 1, w, p->ab, j, p->double_ortho, st));
+    }
+    return PG_OK;
+}
+
+extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scales, int nscales, pg_krylov_stats *st)
+{
+    if (!p || !psi || nscales < 0 || nscales > PG_MAX_SLOTS) return PG_ERR_ARG;
+    pg_ctx *ctx = p->op64->ctx;
+    const long long n = p->n;
+    const int m = p->m;
+    const pg_scales sc = to_scales(scales, nscales);
+    cxd *x = (cxd *)psi;
+    // psi <- U psi; ||psi||
+    PG_TRY(pg_banded_apply_dev(p->ovl64, PG_BAND_MUL_U, x));
+    PG_TRY(pg_multidot<double>(ctx, x, n, 0, x, n, p->d_norm));
+    // V[0] = psi / ||psi||
+    if (p->prec == PG_FP64) {
+        PG_TRY((pg_scale_copy<double, double>(ctx, x, (cxd *)p->V, nullptr, n, p->d_norm + 1, 1.0)));
+        PG_TRY(pamp_arnoldi<double>(p, sc, st));
+    } else {
+        PG_TRY((pg_scale_copy<float, double>(ctx, x, (cxf *)p->V, nullptr, n, p->d_norm + 1, 1.0)));
+        PG_TRY(pamp_arnoldi<float>(p, sc, st));
+    }
+    PG_TRY(fetch_columns(ctx, p->ab, 0, m));
+    PG_CUDA_TRY(cudaMemcpyAsync(ctx->h_pinned, p->d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    const double norm_h = ctx->h_pinned[1];
+    // Hessenberg (row-major), truncated at a happy breakdown
+    std::vector<zd> H((size_t)m * m, zd(0.0, 0.0));
+    int k = m;
+    for (int j = 0; j < m; ++j) {
+        std::vector<zd> col(j + 1);
+        double beta = 0.0;
+        read_column(p->ab, j, j + 1, p->double_ortho, col.data(), &beta);
+        for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = col[i];
+        if (j + 1 < m) {
+            if (beta < p->tolerance) { k = j + 1; break; }
+            H[(size_t)(j + 1) * m + j] = beta;
+        }
+    }
+    std::vector<zd> A((size_t)k * k), E((size_t)k * k);
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j) A[(size_t)i * k + j] = zd(0.0, -dt) * H[(size_t)i * m + j];
+    if (!dense::expm_pade(k, A.data(), E.data(), 6)) return PG_ERR_BREAKDOWN;
+    for (int i = 0; i < k; ++i) {
+        p->h_c[2 * i] = E[(size_t)i * k].real();
+        p->h_c[2 * i + 1] = E[(size_t)i * k].imag();
+    }
+    if (st) st->ErrorEstimate = std::norm(E[(size_t)(k - 1) * k]);
+    PG_CUDA_TRY(cudaMemcpyAsync(p->d_c, p->h_c, sizeof(double) * 2 * k, cudaMemcpyHostToDevice, ctx->stream));
+    if (p->prec == PG_FP64) PG_TRY(pg_combine<double>(ctx, (const cxd *)p->V, n, k, p->d_c, norm_h, x, n, 0));
+    else PG_TRY(pg_combine<float>(ctx, (const cxf *)p->V, n, k, p->d_c, norm_h, x, n, 0));
+    PG_TRY(pg_banded_apply_dev(p->ovl64, PG_BAND_SOLVE_U, x));
+    return PG_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// GMRES (left-preconditioned) and the Cayley step
+// ------------------------------------------------------------------------------------
+struct pg_cayley {
+    pg_op *op64 = nullptr, *opb = nullptr;
+    pg_banded *prec64 = nullptr, *precb = nullptr;
+    int m = 0, prec = PG_FP64;
+    long long n = 0;
+    double tolerance = 1e-13;
+    void *V = nullptr, *w = nullptr;     // basis precision
+    cxd *b64 = nullptr, *r64 = nullptr, *d64 = nullptr, *e64 = nullptr;  // FP64 work vectors
+    double *d_y = nullptr, *h_y = nullptr;
+    double *d_norm = nullptr;
+    ArnoldiBuf ab;
+};
+
+extern "C" int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64, pg_banded *prec_basis, int basis_size,
+                                int basis_precision, double tolerance, pg_cayley **out)
+{
+    if (!op64 || !op_basis || !prec64 || !prec_basis || !out) return PG_ERR_ARG;
+    if (basis_size < 2 || basis_size > PG_RED_COLS - 2) return PG_ERR_ARG;
+    if (op64->precision != PG_FP64 || op_basis->precision != basis_precision) return PG_ERR_ARG;
+    if (prec64->kind != 1 || prec_basis->kind != 1) return PG_ERR_ARG;
+    pg_cayley *c = new pg_cayley();
+    c->op64 = op64;
+    c->opb = op_basis;
+    c->prec64 = prec64;
+    c->precb = prec_basis;
+    c->m = basis_size;
+    c->prec = basis_precision;
+    c->tolerance = tolerance;
+    c->n = (long long)op64->nrows * op64->N;
+    const size_t esz = basis_precision == PG_FP64 ? sizeof(cxd) : sizeof(cxf);
+    PG_CUDA_TRY(cudaMalloc(&c->V, esz * (size_t)c->m * c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->w, esz * (size_t)c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->b64, sizeof(cxd) * (size_t)c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->r64, sizeof(cxd) * (size_t)c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->d64, sizeof(cxd) * (size_t)c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->e64, sizeof(cxd) * (size_t)c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->d_y, sizeof(double) * 2 * c->m));
+    PG_CUDA_TRY(cudaMallocHost(&c->h_y, sizeof(double) * 2 * c->m));
+    PG_CUDA_TRY(cudaMalloc(&c->d_norm, sizeof(double) * 2 * PG_RED_COLS));
+    PG_TRY(c->ab.alloc(c->m));
+    *out = c;
+    return PG_OK;
+}
+
+extern "C" int pg_cayley_destroy(pg_cayley *c)
+{
+    if (!c) return PG_ERR_ARG;
+    cudaFree(c->V);
+    cudaFree(c->w);
+    cudaFree(c->b64);
+    cudaFree(c->r64);
+    cudaFree(c->d64);
+    cudaFree(c->e64);
+    cudaFree(c->d_y);
+    if (c->h_y) cudaFreeHost(c->h_y);
+    cudaFree(c->d_norm);
+    c->ab.release();
+    delete c;
+    return PG_OK;
+}
+
+// GMRES on A = M^-1 (S + i dt/2 H): V[0] holds rhs (already preconditioned) scaled by
+// 1/beta0. Writes the solution combination into out (complex128, overwritten).
+// Stops when the least-squares residual is <= tol or after m matvecs.
+template <typename R>
+static int gmres_solve(pg_cayley *c, const pg_scales &scA, double beta0, double tol, cxd *out, pg_krylov_stats *st)
+{
+    pg_ctx *ctx = c->op64->ctx;
+    const long long n = c->n;
+    const int m = c->m;
+    cx<R> *V = (cx<R> *)c->V;
+    cx<R> *w = (cx<R> *)c->w;
+    // Givens state
+    std::vector<zd> Rm((size_t)(m + 1) * m, zd(0.0, 0.0));  // R[i][j] row-major (m+1) x m
+    std::vector<zd> cs(m), sn(m), g(m + 1, zd(0.0, 0.0));
+    g[0] = beta0;
+    int kdone = 0;
+    double resid = beta0;
+    for (int j = 0; j < m; ++j) {
+        if (j > 0) PG_TRY((pg_scale_copy<R, R>(ctx, w, V + (size_t)j * n, nullptr, n, c->ab.dcol(j - 1, 2) + 2 * j + 1, 1.0)));
+        PG_TRY(pg_op_matvec_dev(c->opb, scA, nullptr, V + (size_t)j * n, w, 0, nullptr, nullptr));
+        PG_TRY(pg_banded_apply_dev(c->precb, PG_BAND_PREC_SOLVE, w));
+        if (st) st->OpCount++;
+        PG_TRY(cgs2<R>(ctx, V, n, j + 1, w, c->ab, j, 1, st));
+        PG_TRY(fetch_columns(ctx, c->ab, j, j + 1));
+        std::vector<zd> h(j + 2);
+        double beta = 0.0;
+        read_column(c->ab, j, j + 1, 1, h.data(), &beta);
+        h[j + 1] = beta;
+        // apply previous rotations
+        for (int i = 0; i < j; ++i) {
+            const zd t = cs[i] * h[i] + sn[i] * h[i + 1];
+            h[i + 1] = -std::conj(sn[i]) * h[i] + std::conj(cs[i]) * h[i + 1];
+            h[i] = t;
+        }
+        // new rotation zeroing h[j+1]
+        const double a = std::abs(h[j]), bb = std::abs(h[j + 1]);
+        const double r = std::hypot(a, bb);
+        if (r == 0.0) { cs[j] = 1.0; sn[j] = 0.0; }
+        else if (a == 0.0) { cs[j] = 0.0; sn[j] = std::conj(h[j + 1]) / bb; }
+        else {
+            cs[j] = a / r;
+            sn[j] = (h[j] / a) * std::conj(h[j + 1]) / r;
+        }
+        const zd hj = cs[j] * h[j] + sn[j] * h[j + 1];
+        h[j] = hj;
+        h[j + 1] = 0.0;
+        g[j + 1] = -std::conj(sn[j]) * g[j];
+        g[j] = cs[j] * g[j];
+        for (int i = 0; i <= j; ++i) Rm[(size_t)i * m + j] = h[i];
+        kdone = j + 1;
+        resid = std::abs(g[j + 1]);
+        if (resid <= tol || beta < 1e-300) break;
+    }
+    // back substitution R y = g
+    std::vector<zd> y(kdone);
+    for (int i = kdone - 1; i >= 0; --i) {
+        zd s = g[i];
+        for (int q = i + 1; q < kdone; ++q) s -= Rm[(size_t)i * m + q] * y[q];
+        y[i] = s / Rm[(size_t)i * m + i];
+    }
+    for (int i = 0; i < kdone; ++i) {
+        c->h_y[2 * i] = y[i].real();
+        c->h_y[2 * i + 1] = y[i].imag();
+    }
+    PG_CUDA_TRY(cudaMemcpyAsync(c->d_y, c->h_y, sizeof(double) * 2 * kdone, cudaMemcpyHostToDevice, ctx->stream));
+    PG_TRY(pg_combine<R>(ctx, V, n, kdone, c->d_y, 1.0, out, n, 0));
+    if (st) {
+        st->Iterations = kdone;
+        st->ErrorEstimate = resid;
+    }
+    return PG_OK;
+}
+
+// scales layout for the Cayley step: slot 0 = the overlap term S (weight 1), slots >= 1 the
+// terms of H. sc_in gives the H(t+dt/2) slot values; this builds A-scales (S + f H) for a
+// complex factor f.
+static pg_scales cayley_scales(const double *scales, int nscales, zd f, zd s_weight)
+{
+    pg_scales sc;
+    for (int k = 0; k < PG_MAX_SLOTS; ++k) {
+        zd v(0.0, 0.0);
+        if (k == 0) v = s_weight;
+        else if (k < nscales) v = f * zd(scales[2 * k], scales[2 * k + 1]);
+        sc.s[k] = mk<double>(v.real(), v.imag());
+    }
+    return sc;
+}
+
+static int norm64(pg_ctx *ctx, const cxd *x, long long n, double *d_norm, double *out)
+{
+    PG_TRY(pg_multidot<double>(ctx, x, n, 0, x, n, d_norm));
+    PG_CUDA_TRY(cudaMemcpyAsync(ctx->h_pinned, d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    *out = ctx->h_pinned[1];
+    return PG_OK;
+}
+
+extern "C" int pg_cayley_step(pg_cayley *c, void *psi, double dt, const double *scales, int nscales, pg_krylov_stats *st)
+{
+    if (!c || !psi || !scales || nscales < 1 || nscales > PG_MAX_SLOTS) return PG_ERR_ARG;
+    pg_ctx *ctx = c->op64->ctx;
+    const long long n = c->n;
+    cxd *x = (cxd *)psi;
+    const zd half(0.0, dt / 2.0);
+    const pg_scales scPlus = cayley_scales(scales, nscales, half, 1.0);    // S + i dt/2 H
+    const pg_scales scMinus = cayley_scales(scales, nscales, -half, 1.0);  // S - i dt/2 H
+    const pg_scales scDiff = cayley_scales(scales, nscales, zd(0.0, -dt), 0.0);  // -i dt H
+    if (c->prec == PG_FP64) {
+        // reference scheme: b = (S - i dt/2 H) psi, rhs = M^-1 b, GMRES from x0 = 0
+        PG_TRY(pg_op_matvec_dev(c->op64, scMinus, nullptr, x, c->b64, 0, nullptr, nullptr));
+        PG_CUDA_TRY(cudaMemcpyAsync(c->d64, c->b64, sizeof(cxd) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+        PG_TRY(pg_banded_apply_dev(c->prec64, PG_BAND_PREC_SOLVE, c->d64));
+        double beta0 = 0.0;
+        PG_TRY(norm64(ctx, c->d64, n, c->d_norm, &beta0));
+        if (beta0 == 0.0) return PG_OK;
+        PG_TRY((pg_scale_copy<double, double>(ctx, c->d64, (cxd *)c->V, nullptr, n, nullptr, 1.0 / beta0)));
+        PG_TRY(gmres_solve<double>(c, scPlus, beta0, c->tolerance, x, st));
+        if (st) {
+            // true residual || (S + i dt/2 H) x - b ||
+            PG_TRY(pg_op_matvec_dev(c->op64, scPlus, nullptr, x, c->r64, 0, nullptr, nullptr));
+            PG_TRY(pg_axpy(ctx, mk<double>(-1.0, 0.0), c->b64, c->r64, n));
+            PG_TRY(norm64(ctx, c->r64, n, c->d_norm, &st->TrueResidual));
+        }
+        return PG_OK;
+    }
+    // mixed precision: r = b - A psi = -i dt H psi (FP64); correction d from FP32 GMRES on
+    // M^-1 A d = M^-1 r; psi += d; r -= A d in FP64; repeat while ||M^-1 r|| > tolerance.
+    PG_TRY(pg_op_matvec_dev(c->op64, scDiff, nullptr, x, c->r64, 0, nullptr, nullptr));
+    long long iters = 0;
+    double rn = 0.0;
+    for (int pass = 0; pass < 4; ++pass) {
+        PG_CUDA_TRY(cudaMemcpyAsync(c->d64, c->r64, sizeof(cxd) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+        PG_TRY(pg_banded_apply_dev(c->prec64, PG_BAND_PREC_SOLVE, c->d64));
+        PG_TRY(norm64(ctx, c->d64, n, c->d_norm, &rn));
+        if (rn <= c->tolerance || rn == 0.0) break;
+        PG_TRY((pg_scale_copy<float, double>(ctx, c->d64, (cxf *)c->V, nullptr, n, nullptr, 1.0 / rn)));
+        const double inner_tol = std::max(c->tolerance, 2e-6 * rn);
+        PG_TRY(gmres_solve<float>(c, scPlus, rn, inner_tol, c->e64, st));
+        if (st) iters += st->Iterations;
+        PG_TRY(pg_axpy(ctx, mk<double>(1.0, 0.0), c->e64, x, n));
+        PG_TRY(pg_op_matvec_dev(c->op64, scPlus, nullptr, c->e64, c->b64, 0, nullptr, nullptr));
+        PG_TRY(pg_axpy(ctx, mk<double>(-1.0, 0.0), c->b64, c->r64, n));
+    }
+    if (st) {
+        st->Iterations = iters;
+        st->ErrorEstimate = rn;
+        PG_TRY(norm64(ctx, c->r64, n, c->d_norm, &st->TrueResidual));
+    }
+    return PG_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// Arnoldi expansion for pIRAM: operator S^-1 H, Euclidean inner product, CGS2
+// ------------------------------------------------------------------------------------
+extern "C" int pg_arnoldi_expand(pg_op *op64, pg_banded *ovl64, pg_banded *shift_invert, const double *scales,
+                                 int nscales, void *Vv, int m, int j0, void *fv, double *Hio, double breakdown_tol,
+                                 int inject, int *steps_done, double *residual_norm_out, pg_krylov_stats *st)
+{
+    if (!op64 || !ovl64 || !Vv || !fv || !Hio || !steps_done || m < 1 || j0 < -1 || j0 >= m || m > PG_RED_COLS - 2)
+        return PG_ERR_ARG;
+    if (op64->precision != PG_FP64 || ovl64->kind != 0) return PG_ERR_ARG;
+    if (shift_invert && shift_invert->kind != 1) return PG_ERR_ARG;
+    if (nscales < 0 || nscales > PG_MAX_SLOTS || (nscales > 0 && !scales)) return PG_ERR_ARG;
+    pg_ctx *ctx = op64->ctx;
+    const long long n = (long long)op64->nrows * op64->N;
+    const pg_scales sc = to_scales(scales, nscales);
+    cxd *V = (cxd *)Vv;
+    cxd *f = (cxd *)fv;
+    ArnoldiBuf ab;
+    PG_TRY(ab.alloc(m));
+    double *d_norm = nullptr;
+    cxd *w = nullptr;
+    int code = PG_OK;
+    *steps_done = m;
+    auto fail = [&](int c) { code = c; };
+    if (cudaMalloc(&d_norm, sizeof(double) * 2 * PG_RED_COLS) != cudaSuccess ||
+        cudaMalloc(&w, sizeof(cxd) * n) != cudaSuccess) {
+        fail(PG_ERR_ALLOC);
+    }
+    auto Hset = [&](int r, int c, double re, double im) {
+        Hio[2 * ((size_t)r * m + c)] = re;
+        Hio[2 * ((size_t)r * m + c) + 1] = im;
+    };
+    for (int j = j0 + 1; j < m && code == PG_OK; ++j) {
+        const bool injected = inject && j == j0 + 1 && j > 0;
+        if (injected) {
+            // random continuation vector supplied in f: orthogonalise it against V[0..j)
+            if ((code = cgs2<double>(ctx, V, n, j, f, ab, j, 1, nullptr)) != PG_OK) break;
+        }
+        if ((code = pg_multidot<double>(ctx, f, n, 0, f, n, d_norm)) != PG_OK) break;
+        if (cudaMemcpyAsync(ctx->h_pinned, d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+            cudaStreamSynchronize(ctx->stream) != cudaSuccess) { fail(PG_ERR_CUDA); break; }
+        const double beta = ctx->h_pinned[1];
+        if (j > 0) {
+            if (!injected && beta < breakdown_tol) { *steps_done = j; break; }
+            if (beta == 0.0) { fail(PG_ERR_BREAKDOWN); break; }
+            Hset(j, j - 1, injected ? 0.0 : beta, 0.0);
+        }
+        if ((code = pg_scale_copy<double, double>(ctx, f, V + (size_t)j * n, nullptr, n, d_norm + 1, 1.0)) != PG_OK) break;
+        if (shift_invert) {
+            // w = (H - sigma S)^-1 S V[j]
+            if (cudaMemcpyAsync(w, V + (size_t)j * n, sizeof(cxd) * n, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess) {
+                fail(PG_ERR_CUDA); break;
+            }
+            if ((code = pg_banded_apply_dev(ovl64, PG_BAND_MUL_S, w)) != PG_OK) break;
+            if ((code = pg_banded_apply_dev(shift_invert, PG_BAND_PREC_SOLVE, w)) != PG_OK) break;
+        } else {
+            // w = S^-1 H V[j]
+            if ((code = pg_op_matvec_dev(op64, sc, nullptr, V + (size_t)j * n, w, 0, nullptr, nullptr)) != PG_OK) break;
+            if ((code = pg_banded_apply_dev(ovl64, PG_BAND_SOLVE_S, w)) != PG_OK) break;
+        }
+        if (st) st->OpCount++;
+        if ((code = cgs2<double>(ctx, V, n, j + 1, w, ab, j, 1, st)) != PG_OK) break;
+        if ((code = fetch_columns(ctx, ab, j, j + 1)) != PG_OK) break;
+        std::vector<zd> h(j + 1);
+        double b2 = 0.0;
+        read_column(ab, j, j + 1, 1, h.data(), &b2);
+        for (int i = 0; i <= j; ++i) Hset(i, j, h[i].real(), h[i].imag());
+        if (cudaMemcpyAsync(f, w, sizeof(cxd) * n, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess) {
+            fail(PG_ERR_CUDA); break;
+        }
+        if (residual_norm_out) *residual_norm_out = b2;
+    }
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(w);
+    cudaFree(d_norm);
+    ab.release();
+    return code;
+}

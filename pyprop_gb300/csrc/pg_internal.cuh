@@ -1,0 +1,188 @@
+// Internal definitions shared by the libpyprop_gpu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+#include <complex>
+#include <string>
+
+#include "../../include/pyprop_gpu.h"
+
+// ------------------------------------------------------------------------------------
+// complex arithmetic on interleaved pairs
+// ------------------------------------------------------------------------------------
+template <typename R> struct __align__(2 * sizeof(R)) cx {
+    R x, y;
+};
+typedef cx<double> cxd;
+typedef cx<float> cxf;
+
+template <typename R> __host__ __device__ __forceinline__ cx<R> mk(R a, R b) { cx<R> c; c.x = a; c.y = b; return c; }
+template <typename R> __host__ __device__ __forceinline__ cx<R> operator+(cx<R> a, cx<R> b) { return mk<R>(a.x + b.x, a.y + b.y); }
+template <typename R> __host__ __device__ __forceinline__ cx<R> operator-(cx<R> a, cx<R> b) { return mk<R>(a.x - b.x, a.y - b.y); }
+template <typename R> __host__ __device__ __forceinline__ cx<R> operator*(cx<R> a, cx<R> b) {
+    return mk<R>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename R> __host__ __device__ __forceinline__ cx<R> operator*(R s, cx<R> a) { return mk<R>(s * a.x, s * a.y); }
+template <typename R> __host__ __device__ __forceinline__ cx<R> conjx(cx<R> a) { return mk<R>(a.x, -a.y); }
+// acc += a * b
+template <typename R> __device__ __forceinline__ void cfma(cx<R> &acc, cx<R> a, cx<R> b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+// acc += conj(a) * b
+template <typename R> __device__ __forceinline__ void cfma_conj(cx<R> &acc, cx<R> a, cx<R> b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(-a.y, b.x, acc.y);
+}
+template <typename R, typename S> __host__ __device__ __forceinline__ cx<R> cvt(cx<S> a) { return mk<R>((R)a.x, (R)a.y); }
+
+template <typename R> struct prec_of;
+template <> struct prec_of<double> { static const int value = PG_FP64; };
+template <> struct prec_of<float> { static const int value = PG_FP32; };
+
+// ------------------------------------------------------------------------------------
+// context
+// ------------------------------------------------------------------------------------
+struct pg_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    long long launches = 0;
+    int num_sms = 0;
+    // scratch for reductions: per-block partials and an arrival counter
+    double *red_partial = nullptr;   // [max_blocks * max_cols] complex -> 2 doubles each
+    unsigned int *red_counter = nullptr;
+    double *red_out = nullptr;       // [max_cols] complex + extra
+    double *h_pinned = nullptr;      // pinned host mirror of red_out
+    int red_max_blocks = 0;
+    int red_max_cols = 0;
+};
+
+#define PG_CUDA_TRY(...)                                                                     \
+    do {                                                                                     \
+        cudaError_t _e = (__VA_ARGS__);                                                             \
+        if (_e != cudaSuccess) {                                                             \
+            pg_set_last_error(_e, #__VA_ARGS__, __FILE__, __LINE__);                                \
+            return PG_ERR_CUDA;                                                              \
+        }                                                                                    \
+    } while (0)
+
+#define PG_TRY(...)                                                                          \
+    do {                                                                                     \
+        int _s = (__VA_ARGS__);                                                                     \
+        if (_s != PG_OK) return _s;                                                          \
+    } while (0)
+
+void pg_set_last_error(cudaError_t e, const char *what, const char *file, int line);
+int pg_check_launch(pg_ctx *ctx);
+
+// reduction scratch sizes
+static const int PG_RED_BLOCKS = 304;   // 2 x 152 SMs
+static const int PG_RED_COLS = 130;     // up to 128 Krylov vectors + norm + spare
+int pg_ctx_ensure_reduction(pg_ctx *ctx);
+
+// ------------------------------------------------------------------------------------
+// device operator
+// ------------------------------------------------------------------------------------
+static const int PG_MAX_SLOTS = 16;
+
+struct pg_scales {
+    cxd s[PG_MAX_SLOTS];
+};
+
+struct OpDev {
+    int nrows;        // angular rows (Nang)
+    int N;            // radial length
+    int kb;           // super diagonals
+    int b;            // 2kb+1
+    const int *row_ptr;
+    const int *ent_col;
+    const int *ent_band;
+    const int *ent_slot;
+    const void *bands;  // [nbands][b][N] complex<R>
+};
+
+struct HostTerm {
+    std::string storage;
+    std::vector<double> pot;  // complex interleaved, reference layout
+    int e0 = 0, e1 = 0;
+    std::vector<int> pairs;   // (row, col) for Simp
+    int slot = 0;
+};
+
+struct pg_op {
+    pg_ctx *ctx = nullptr;
+    int rank = 2;
+    int nrows = 0, N = 0, kb = 0, b = 0;
+    int precision = PG_FP64;
+    std::vector<HostTerm> terms;
+    bool finalized = false;
+    // device arrays
+    int *d_row_ptr = nullptr, *d_ent_col = nullptr, *d_ent_band = nullptr, *d_ent_slot = nullptr;
+    void *d_bands = nullptr;
+    int nbands = 0;
+    long long nentries = 0;
+    OpDev dev() const {
+        OpDev o;
+        o.nrows = nrows; o.N = N; o.kb = kb; o.b = b;
+        o.row_ptr = d_row_ptr; o.ent_col = d_ent_col; o.ent_band = d_ent_band; o.ent_slot = d_ent_slot;
+        o.bands = d_bands;
+        return o;
+    }
+    // host copy of bands in diagonal-major form (complex128), kept for preconditioner setup
+    std::vector<std::complex<double>> h_bands;   // [nbands][b][N]
+    std::vector<int> h_row_ptr, h_ent_col, h_ent_band, h_ent_slot;
+};
+
+// matvec launcher shared by the drivers: dst = acc*dst + sum scales * V src
+// scales_dev (optional) overrides `scales` when non-null.
+int pg_op_matvec_dev(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src,
+                     void *dst, int accumulate, const double *src_inv_scale_dev, void *src_copy_out);
+
+// ------------------------------------------------------------------------------------
+// banded fibre operators
+// ------------------------------------------------------------------------------------
+// One blocked triangular matrix set: for each matrix, nblk blocks of 32 rows:
+//   inv[m][blk][s][t] = (T_blk^-1)[t][s]     (t = output row within block, s = input row)
+//   cpl[m][blk][j][t] = T(row, row -/+ j) coupling to the neighbouring block, j = 1..w
+struct TriDev {
+    int N, nblk, w;
+    int lower;           // 1: forward (lower) solve, 0: backward (upper)
+    int complex_coef;    // 1: complex coefficients, 0: real
+    const void *inv;     // real: double/float [nmat][nblk][32][32]; complex: cx
+    const void *cpl;     // [nmat][nblk][w][32]
+};
+
+struct pg_banded {
+    pg_op *op = nullptr;
+    int kind = 0;            // 0 overlap, 1 preconditioner
+    int N = 0, kb = 0, nmat = 0;
+    // overlap: U upper Cholesky factor rows (real) for multiplies, lower = U^T
+    void *d_U = nullptr;     // [N][kb+1]  U(i, i+j) at [i][j]   (real, precision of op)
+    void *d_S = nullptr;     // [N][2kb+1] S rows (real)
+    // blocked solves
+    void *d_lo_inv = nullptr, *d_lo_cpl = nullptr;   // lower factor (U^T or L)
+    void *d_up_inv = nullptr, *d_up_cpl = nullptr;   // upper factor (U)
+    int complex_coef = 0;
+};
+
+int pg_banded_apply_dev(pg_banded *b, int which, void *x);
+
+// ------------------------------------------------------------------------------------
+// vector kernels (vector.cu)
+// ------------------------------------------------------------------------------------
+// h[j] = sum_i conj(V[j][i]) w[i] for j < J; nrm2 = sum |w|^2. Results FP64 in ctx->red_out:
+// red_out[2j], red_out[2j+1] = h[j]; red_out[2J] = ||w||^2.
+template <typename R>
+int pg_multidot(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const cx<R> *w, long long n, double *out_dev);
+// w -= sum_j V[j] h[j] with h complex128 on device; then, if J2 > 0, out2 = V[0..J2)^H w and ||w||^2
+template <typename R>
+int pg_gs_update(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const double *h_dev, cx<R> *w, long long n,
+                 int want_dots, double *out_dev);

@@ -1,0 +1,344 @@
+// Krylov vector kernels: block inner products (Gram-Schmidt), updates, norms, basis
+// combinations, precision conversion.
+//
+// Reductions: every CTA reduces its contiguous chunk in the element precision (warp
+// shuffles, then shared memory), stores one complex128 partial per column, and the last
+// CTA to arrive (threadfence + atomic ticket, no waiting) sums the partials in FP64 and
+// resets the ticket. The block inner product <V_j, w> for all j replaces the reference's
+// conjugate-transpose zgemv + MPI_Allreduce (core/krylov/piram/piram/functors.h:197-240).
+#include "pg_internal.cuh"
+
+#include <algorithm>
+
+static const int RED_THREADS = 256;
+static const int RED_ELEMS = 4;  // elements per thread per chunk pass
+
+static inline int red_blocks(pg_ctx *ctx, long long n)
+{
+    long long per = (long long)RED_THREADS * RED_ELEMS;
+    long long nb = (n + per - 1) / per;
+    int cap = std::min(ctx->red_max_blocks, 2 * std::max(1, ctx->num_sms));
+    return (int)std::max<long long>(1, std::min<long long>(nb, cap));
+}
+
+template <typename R> __device__ __forceinline__ R warp_sum(R v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-reduce two values; result valid in thread 0.
+template <typename R> __device__ __forceinline__ void block_sum2(R &a, R &b, R *sm)
+{
+    a = warp_sum(a);
+    b = warp_sum(b);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) { sm[2 * wid] = a; sm[2 * wid + 1] = b; }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        a = lane < nw ? sm[2 * lane] : (R)0;
+        b = lane < nw ? sm[2 * lane + 1] : (R)0;
+        a = warp_sum(a);
+        b = warp_sum(b);
+    }
+}
+
+// Final cross-block reduction by the last CTA. partial: [nblocks][ncols] complex128.
+__device__ void finish_reduction(double *partial, int ncols, unsigned int *counter, double *out, bool last)
+{
+    if (!last) return;
+    __threadfence();
+    for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
+        double sx = 0.0, sy = 0.0;
+        for (int blk = 0; blk < (int)gridDim.x; ++blk) {
+            sx += partial[2 * ((size_t)blk * ncols + c)];
+            sy += partial[2 * ((size_t)blk * ncols + c) + 1];
+        }
+        out[2 * c] = sx;
+        out[2 * c + 1] = sy;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // column ncols-1 holds ||w||^2 in its real part: publish sqrt next to it
+        *counter = 0;
+    }
+}
+
+__device__ __forceinline__ bool arrive_last(unsigned int *counter)
+{
+    __shared__ bool is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int ticket = atomicAdd(counter, 1u);
+        is_last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    return is_last;
+}
+
+// out[2j..2j+1] = <V_j, w> (j < J); out[2J] = ||w||^2, out[2J+1] = ||w||.
+template <typename R>
+__global__ void __launch_bounds__(RED_THREADS) multidot_kernel(const cx<R> *__restrict__ V, long long ldv, int J,
+                                                               const cx<R> *__restrict__ w, long long n,
+                                                               double *partial, unsigned int *counter, double *out)
+{
+    __shared__ R sm[64];
+    const long long chunk = (n + gridDim.x - 1) / gridDim.x;
+    const long long lo = (long long)blockIdx.x * chunk;
+    const long long hi = min(n, lo + chunk);
+    const int ncols = J + 1;
+    for (int j = 0; j <= J; ++j) {
+        R ax = 0, ay = 0;
+        if (j < J) {
+            const cx<R> *v = V + (size_t)j * ldv;
+            for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+                const cx<R> a = v[i], b = w[i];
+                ax = fma(a.x, b.x, ax); ax = fma(a.y, b.y, ax);
+                ay = fma(a.x, b.y, ay); ay = fma(-a.y, b.x, ay);
+            }
+        } else {
+            for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+                const cx<R> b = w[i];
+                ax = fma(b.x, b.x, ax); ax = fma(b.y, b.y, ax);
+            }
+        }
+        block_sum2(ax, ay, sm);
+        if (threadIdx.x == 0) {
+            partial[2 * ((size_t)blockIdx.x * ncols + j)] = (double)ax;
+            partial[2 * ((size_t)blockIdx.x * ncols + j) + 1] = (double)ay;
+        }
+    }
+    const bool last = arrive_last(counter);
+    finish_reduction(partial, ncols, counter, out, last);
+    if (last && threadIdx.x == 0) out[2 * J + 1] = sqrt(out[2 * J]);
+}
+
+// w -= sum_j V_j h_j (h complex128 on device); then optional dots <V_j, w> (j < J) and
+// ||w||^2 into out exactly as multidot_kernel.
+template <typename R>
+__global__ void __launch_bounds__(RED_THREADS) gs_update_kernel(const cx<R> *__restrict__ V, long long ldv, int J,
+                                                                const double *__restrict__ h, cx<R> *__restrict__ w,
+                                                                long long n, int want_dots, double *partial,
+                                                                unsigned int *counter, double *out)
+{
+    __shared__ R sm[64];
+    __shared__ cx<R> hs[PG_RED_COLS];
+    for (int j = threadIdx.x; j < J; j += blockDim.x) hs[j] = mk<R>((R)h[2 * j], (R)h[2 * j + 1]);
+    __syncthreads();
+    const long long chunk = (n + gridDim.x - 1) / gridDim.x;
+    const long long lo = (long long)blockIdx.x * chunk;
+    const long long hi = min(n, lo + chunk);
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        cx<R> acc = w[i];
+        for (int j = 0; j < J; ++j) {
+            const cx<R> v = V[(size_t)j * ldv + i];
+            const cx<R> c = hs[j];
+            acc.x = fma(-v.x, c.x, acc.x); acc.x = fma(v.y, c.y, acc.x);
+            acc.y = fma(-v.x, c.y, acc.y); acc.y = fma(-v.y, c.x, acc.y);
+        }
+        w[i] = acc;
+    }
+    __syncthreads();
+    const int ncols = J + 1;
+    for (int j = want_dots ? 0 : J; j <= J; ++j) {
+        R ax = 0, ay = 0;
+        if (j < J) {
+            const cx<R> *v = V + (size_t)j * ldv;
+            for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+                const cx<R> a = v[i], b = w[i];
+                ax = fma(a.x, b.x, ax); ax = fma(a.y, b.y, ax);
+                ay = fma(a.x, b.y, ay); ay = fma(-a.y, b.x, ay);
+            }
+        } else {
+            for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+                const cx<R> b = w[i];
+                ax = fma(b.x, b.x, ax); ax = fma(b.y, b.y, ax);
+            }
+        }
+        block_sum2(ax, ay, sm);
+        if (threadIdx.x == 0) {
+            partial[2 * ((size_t)blockIdx.x * ncols + j)] = (double)ax;
+            partial[2 * ((size_t)blockIdx.x * ncols + j) + 1] = (double)ay;
+        }
+    }
+    if (!want_dots) {
+        // columns < J untouched: zero them so the final sum is well defined
+        if (threadIdx.x < J) {
+            partial[2 * ((size_t)blockIdx.x * ncols + threadIdx.x)] = 0.0;
+            partial[2 * ((size_t)blockIdx.x * ncols + threadIdx.x) + 1] = 0.0;
+        }
+    }
+    const bool last = arrive_last(counter);
+    finish_reduction(partial, ncols, counter, out, last);
+    if (last && threadIdx.x == 0) out[2 * J + 1] = sqrt(out[2 * J]);
+}
+
+template <typename R>
+int pg_multidot(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const cx<R> *w, long long n, double *out_dev)
+{
+    if (J + 1 > ctx->red_max_cols) return PG_ERR_ARG;
+    const int nb = red_blocks(ctx, n);
+    multidot_kernel<R><<<nb, RED_THREADS, 0, ctx->stream>>>(V, ldv, J, w, n, ctx->red_partial, ctx->red_counter, out_dev);
+    ctx->launches++;
+    return pg_check_launch(ctx);
+}
+
+template <typename R>
+int pg_gs_update(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const double *h_dev, cx<R> *w, long long n,
+                 int want_dots, double *out_dev)
+{
+    if (J + 1 > ctx->red_max_cols) return PG_ERR_ARG;
+    const int nb = red_blocks(ctx, n);
+    gs_update_kernel<R><<<nb, RED_THREADS, 0, ctx->stream>>>(V, ldv, J, h_dev, w, n, want_dots, ctx->red_partial,
+                                                            ctx->red_counter, out_dev);
+    ctx->launches++;
+    return pg_check_launch(ctx);
+}
+
+template int pg_multidot<double>(pg_ctx *, const cxd *, long long, int, const cxd *, long long, double *);
+template int pg_multidot<float>(pg_ctx *, const cxf *, long long, int, const cxf *, long long, double *);
+template int pg_gs_update<double>(pg_ctx *, const cxd *, long long, int, const double *, cxd *, long long, int, double *);
+template int pg_gs_update<float>(pg_ctx *, const cxf *, long long, int, const double *, cxf *, long long, int, double *);
+
+// ------------------------------------------------------------------------------------
+// elementwise helpers
+// ------------------------------------------------------------------------------------
+// dst (Rd) = src (Rs) * (1/scale_dev[0]) (or * mul when scale_dev is null); dst2 gets a copy
+template <typename Rd, typename Rs>
+__global__ void scale_copy_kernel(const cx<Rs> *__restrict__ src, cx<Rd> *__restrict__ dst, cx<Rd> *__restrict__ dst2,
+                                  long long n, const double *__restrict__ inv_scale_dev, double mul)
+{
+    const double s = inv_scale_dev ? 1.0 / inv_scale_dev[0] : mul;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const cx<Rs> a = src[i];
+        const cx<Rd> v = mk<Rd>((Rd)((double)a.x * s), (Rd)((double)a.y * s));
+        dst[i] = v;
+        if (dst2) dst2[i] = v;
+    }
+}
+
+template <typename Rd, typename Rs>
+int pg_scale_copy(pg_ctx *ctx, const cx<Rs> *src, cx<Rd> *dst, cx<Rd> *dst2, long long n, const double *inv_scale_dev,
+                  double mul)
+{
+    int nb = (int)std::min<long long>((n + 255) / 256, 4LL * std::max(1, ctx->num_sms));
+    if (nb < 1) nb = 1;
+    scale_copy_kernel<Rd, Rs><<<nb, 256, 0, ctx->stream>>>(src, dst, dst2, n, inv_scale_dev, mul);
+    ctx->launches++;
+    return pg_check_launch(ctx);
+}
+template int pg_scale_copy<double, double>(pg_ctx *, const cxd *, cxd *, cxd *, long long, const double *, double);
+template int pg_scale_copy<float, double>(pg_ctx *, const cxd *, cxf *, cxf *, long long, const double *, double);
+template int pg_scale_copy<double, float>(pg_ctx *, const cxf *, cxd *, cxd *, long long, const double *, double);
+template int pg_scale_copy<float, float>(pg_ctx *, const cxf *, cxf *, cxf *, long long, const double *, double);
+
+// out (complex128) = alpha * sum_{j<k} V_j c_j (+ beta_acc * out); c complex128 on device.
+template <typename R>
+__global__ void combine_kernel(const cx<R> *__restrict__ V, long long ldv, int k, const double *__restrict__ c,
+                               double alpha, cxd *__restrict__ out, long long n, int accumulate)
+{
+    __shared__ cxd cs[PG_RED_COLS];
+    for (int j = threadIdx.x; j < k; j += blockDim.x) cs[j] = mk<double>(c[2 * j], c[2 * j + 1]);
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double ax = 0, ay = 0;
+        for (int j = 0; j < k; ++j) {
+            const cx<R> v = V[(size_t)j * ldv + i];
+            const cxd q = cs[j];
+            ax = fma((double)v.x, q.x, ax); ax = fma(-(double)v.y, q.y, ax);
+            ay = fma((double)v.x, q.y, ay); ay = fma((double)v.y, q.x, ay);
+        }
+        cxd o = mk<double>(alpha * ax, alpha * ay);
+        if (accumulate) o = o + out[i];
+        out[i] = o;
+    }
+}
+
+template <typename R>
+int pg_combine(pg_ctx *ctx, const cx<R> *V, long long ldv, int k, const double *c_dev, double alpha, cxd *out,
+               long long n, int accumulate)
+{
+    if (k > PG_RED_COLS) return PG_ERR_ARG;
+    int nb = (int)std::min<long long>((n + 255) / 256, 4LL * std::max(1, ctx->num_sms));
+    if (nb < 1) nb = 1;
+    combine_kernel<R><<<nb, 256, 0, ctx->stream>>>(V, ldv, k, c_dev, alpha, out, n, accumulate);
+    ctx->launches++;
+    return pg_check_launch(ctx);
+}
+template int pg_combine<double>(pg_ctx *, const cxd *, long long, int, const double *, double, cxd *, long long, int);
+template int pg_combine<float>(pg_ctx *, const cxf *, long long, int, const double *, double, cxd *, long long, int);
+
+// y = a*x + y with complex a (host value), complex128 vectors
+__global__ void axpy_kernel(cxd a, const cxd *__restrict__ x, cxd *__restrict__ y, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        cfma(y[i], a, x[i]);
+}
+int pg_axpy(pg_ctx *ctx, cxd a, const cxd *x, cxd *y, long long n)
+{
+    int nb = (int)std::min<long long>((n + 255) / 256, 4LL * std::max(1, ctx->num_sms));
+    if (nb < 1) nb = 1;
+    axpy_kernel<<<nb, 256, 0, ctx->stream>>>(a, x, y, n);
+    ctx->launches++;
+    return pg_check_launch(ctx);
+}
+
+// ------------------------------------------------------------------------------------
+// ABI
+// ------------------------------------------------------------------------------------
+extern "C" int pg_vec_dot(pg_ctx *ctx, int precision, const void *x, const void *y, long long n, double *out)
+{
+    if (!ctx || !x || !y || !out || n < 0) return PG_ERR_ARG;
+    int st;
+    if (precision == PG_FP64) st = pg_multidot<double>(ctx, (const cxd *)x, 0, 1, (const cxd *)y, n, ctx->red_out);
+    else if (precision == PG_FP32) st = pg_multidot<float>(ctx, (const cxf *)x, 0, 1, (const cxf *)y, n, ctx->red_out);
+    else return PG_ERR_ARG;
+    if (st != PG_OK) return st;
+    PG_CUDA_TRY(cudaMemcpyAsync(ctx->h_pinned, ctx->red_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    out[0] = ctx->h_pinned[0];
+    out[1] = ctx->h_pinned[1];
+    return PG_OK;
+}
+
+extern "C" int pg_vec_convert(pg_ctx *ctx, int src_precision, const void *x, int dst_precision, void *y, long long n)
+{
+    if (!ctx || !x || !y || n < 0) return PG_ERR_ARG;
+    if (src_precision == PG_FP64 && dst_precision == PG_FP32)
+        return pg_scale_copy<float, double>(ctx, (const cxd *)x, (cxf *)y, nullptr, n, nullptr, 1.0);
+    if (src_precision == PG_FP32 && dst_precision == PG_FP64)
+        return pg_scale_copy<double, float>(ctx, (const cxf *)x, (cxd *)y, nullptr, n, nullptr, 1.0);
+    if (src_precision == PG_FP64 && dst_precision == PG_FP64)
+        return pg_scale_copy<double, double>(ctx, (const cxd *)x, (cxd *)y, nullptr, n, nullptr, 1.0);
+    if (src_precision == PG_FP32 && dst_precision == PG_FP32)
+        return pg_scale_copy<float, float>(ctx, (const cxf *)x, (cxf *)y, nullptr, n, nullptr, 1.0);
+    return PG_ERR_ARG;
+}
+
+extern "C" int pg_vec_combine(pg_ctx *ctx, void *V, long long n, int m, const double *Q, int k)
+{
+    // V[:k] <- V[:m] Q  (column q of Q gives new vector q); done through a temporary
+    if (!ctx || !V || !Q || m <= 0 || k <= 0 || k > m || m > PG_RED_COLS) return PG_ERR_ARG;
+    cxd *tmp = nullptr;
+    double *dQ = nullptr;
+    PG_CUDA_TRY(cudaMalloc(&tmp, sizeof(cxd) * (size_t)n * k));
+    PG_CUDA_TRY(cudaMalloc(&dQ, sizeof(double) * 2 * (size_t)m * k));
+    std::vector<double> colmaj(2 * (size_t)m * k);
+    for (int q = 0; q < k; ++q)
+        for (int j = 0; j < m; ++j) {
+            colmaj[2 * ((size_t)q * m + j)] = Q[2 * ((size_t)j * k + q)];
+            colmaj[2 * ((size_t)q * m + j) + 1] = Q[2 * ((size_t)j * k + q) + 1];
+        }
+    PG_CUDA_TRY(cudaMemcpyAsync(dQ, colmaj.data(), colmaj.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    for (int q = 0; q < k; ++q)
+        PG_TRY(pg_combine<double>(ctx, (const cxd *)V, n, m, dQ + 2 * (size_t)q * m, 1.0, tmp + (size_t)q * n, n, 0));
+    PG_CUDA_TRY(cudaMemcpyAsync(V, tmp, sizeof(cxd) * (size_t)n * k, cudaMemcpyDeviceToDevice, ctx->stream));
+    PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    cudaFree(tmp);
+    cudaFree(dQ);
+    return PG_OK;
+}

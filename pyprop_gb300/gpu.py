@@ -1,0 +1,268 @@
+"""Python handles over the C ABI: context, fused operator, banded fibre operators and the
+Krylov steppers. Device buffers are torch tensors on the current CUDA device; the library
+runs on torch's current stream so its kernels are ordered with torch's.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as nat
+from ._native import check
+
+_TORCH = None
+
+
+def torch():
+    global _TORCH
+    if _TORCH is None:
+        import torch as _t
+        _TORCH = _t
+    return _TORCH
+
+
+def require_cuda():
+    t = torch()
+    if not t.cuda.is_available():
+        raise RuntimeError("pyprop_gb300 needs a CUDA device: the GPU path has no CPU fallback")
+
+
+def ptr(tensor):
+    return C.c_void_p(tensor.data_ptr())
+
+
+class Context:
+    """One pg_ctx per CUDA device, bound to torch's current stream at each use."""
+
+    _instances: dict = {}
+
+    def __init__(self, device=0):
+        require_cuda()
+        self.lib = nat.load()
+        h = C.c_void_p()
+        check(self.lib.pg_ctx_create(device, C.byref(h)), "pg_ctx_create")
+        self.h = h
+        self.device = device
+
+    @classmethod
+    def get(cls, device=None):
+        t = torch()
+        if device is None:
+            device = t.cuda.current_device()
+        if device not in cls._instances:
+            cls._instances[device] = Context(device)
+        ctx = cls._instances[device]
+        ctx.bind_stream()
+        return ctx
+
+    def bind_stream(self):
+        s = torch().cuda.current_stream(self.device).cuda_stream
+        check(self.lib.pg_ctx_set_stream(self.h, C.c_void_p(s)), "pg_ctx_set_stream")
+
+    def launches(self):
+        return int(self.lib.pg_ctx_kernel_launches(self.h))
+
+    def synchronize(self):
+        check(self.lib.pg_ctx_synchronize(self.h), "pg_ctx_synchronize")
+
+
+def complex_dtype(precision):
+    t = torch()
+    return t.complex128 if precision == nat.PG_FP64 else t.complex64
+
+
+def precision_of(name):
+    name = (name or "fp64").lower()
+    if name in ("fp64", "double", "complex128"):
+        return nat.PG_FP64
+    if name in ("fp32", "single", "complex64", "mixed"):
+        return nat.PG_FP32
+    raise ValueError("unknown precision %r" % (name,))
+
+
+def bandnh_from_rows(rows, kb):
+    """(N, 2kb+1) row-oriented band -> reference BandNH layout (N*(2kb+1),), complex128."""
+    N = rows.shape[0]
+    b = 2 * kb + 1
+    out = np.zeros(N * b, dtype=np.complex128)
+    for d in range(-kb, kb + 1):
+        i = np.arange(max(0, -d), min(N, N - d))
+        j = i + d
+        out[j * b + (kb + i - j)] = rows[i, kb + d]
+    return out
+
+
+class DeviceOperator:
+    """Fused sum of tensor potentials (and optionally S) resident on the device.
+
+    Slots: 0 is the overlap S when ``overlap_rows`` is given; potential ``p`` uses slot
+    ``1 + p``. ``scales(t)`` gives the slot values of H(t) (time functions evaluated on
+    the host, as the reference does per matvec).
+    """
+
+    def __init__(self, ctx, potentials, shape, kb, precision, overlap_rows=None):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.shape = tuple(shape)
+        self.kb = kb
+        self.precision = precision
+        self.potentials = list(potentials)
+        if 1 + len(self.potentials) > 16:
+            raise ValueError("at most 15 consolidated potentials per operator")
+        h = C.c_void_p()
+        shp, shp_p = nat.iptr(np.asarray(shape, dtype=np.int32))
+        check(self.lib.pg_op_create(ctx.h, len(shape), shp_p, kb, precision, C.byref(h)), "pg_op_create")
+        self.h = h
+        self.has_overlap = overlap_rows is not None
+        if overlap_rows is not None:
+            band = bandnh_from_rows(np.asarray(overlap_rows, dtype=np.float64), kb)[None, :]
+            self._add("Ident_BandNH", band, None, 0)
+        for p, pot in enumerate(self.potentials):
+            ids = "_".join(g.GetStorageId() for g in pot.GeometryList)
+            pairs = pot.GeometryList[0].GetBasisPairs() if ids.startswith("Simp") else None
+            self._add(ids, pot.PotentialData, pairs, 1 + p)
+        check(self.lib.pg_op_finalize(self.h), "pg_op_finalize")
+
+    def _add(self, ids, data, pairs, slot):
+        data = np.ascontiguousarray(data, dtype=np.complex128)
+        _, dp = nat.dptr(data.view(np.float64))
+        if pairs is not None:
+            pa, pp = nat.iptr(pairs)
+            npairs = pa.shape[0]
+        else:
+            pp, npairs = None, 0
+        check(self.lib.pg_op_add_term(self.h, ids.encode(), dp, data.shape[0], data.shape[1], pp, npairs, slot),
+              "pg_op_add_term(%s)" % ids)
+
+    @property
+    def nslots(self):
+        return 1 + len(self.potentials)
+
+    def scales(self, t, h_factor=1.0, s_weight=0.0):
+        sc = np.zeros(self.nslots, dtype=np.complex128)
+        sc[0] = s_weight
+        for p, pot in enumerate(self.potentials):
+            sc[1 + p] = h_factor * pot.GetTimeScaling(t)
+        return sc
+
+    def stored_elements(self):
+        return int(self.lib.pg_op_stored_elements(self.h))
+
+    def matvec(self, scales, src, dst, accumulate=False):
+        sc = np.ascontiguousarray(scales, dtype=np.complex128)
+        _, sp = nat.dptr(sc.view(np.float64))
+        self.ctx.bind_stream()
+        check(self.lib.pg_op_matvec(self.h, sp, len(sc), ptr(src), ptr(dst), int(accumulate)), "pg_op_matvec")
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.lib.pg_op_destroy(self.h)
+        except Exception:
+            pass
+
+
+class Banded:
+    """Overlap factor or block-diagonal preconditioner on the device (pg_banded)."""
+
+    def __init__(self, op: DeviceOperator, h):
+        self.op = op
+        self.h = h
+        self.lib = op.lib
+
+    @classmethod
+    def overlap(cls, op, overlap_rows):
+        rows, rp = nat.dptr(np.asarray(overlap_rows, dtype=np.float64))
+        h = C.c_void_p()
+        check(op.lib.pg_overlap_create(op.h, rp, C.byref(h)), "pg_overlap_create")
+        return cls(op, h)
+
+    @classmethod
+    def blockdiag(cls, op, overlap_rows, cS, cH, slots, weights):
+        rows, rp = nat.dptr(np.asarray(overlap_rows, dtype=np.float64))
+        cs, csp = nat.dptr(np.array([cS], dtype=np.complex128).view(np.float64))
+        ch, chp = nat.dptr(np.array([cH], dtype=np.complex128).view(np.float64))
+        sl, slp = nat.iptr(np.asarray(slots, dtype=np.int32))
+        wt, wtp = nat.dptr(np.asarray(weights, dtype=np.complex128).view(np.float64))
+        h = C.c_void_p()
+        check(op.lib.pg_prec_blockdiag_create(op.h, rp, csp, chp, slp, wtp, len(sl), C.byref(h)),
+              "pg_prec_blockdiag_create")
+        return cls(op, h)
+
+    def apply(self, which, x):
+        self.op.ctx.bind_stream()
+        check(self.lib.pg_banded_apply(self.h, which, ptr(x)), "pg_banded_apply")
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.lib.pg_banded_destroy(self.h)
+        except Exception:
+            pass
+
+
+class PampStepper:
+    """pg_pamp: one pAMP step per call on a complex128 device wavefunction."""
+
+    def __init__(self, op64, opb, ovl64, ovlb, basis_size, precision, double_ortho=True):
+        self.lib = op64.lib
+        self.ctx = op64.ctx
+        self.op64 = op64
+        self._keep = (op64, opb, ovl64, ovlb)
+        h = C.c_void_p()
+        check(self.lib.pg_pamp_create(op64.h, opb.h, ovl64.h, ovlb.h, basis_size, precision, int(double_ortho),
+                                      C.byref(h)), "pg_pamp_create")
+        self.h = h
+        self.stats = nat.KrylovStats()
+
+    def step(self, psi, dt, scales):
+        sc = np.ascontiguousarray(scales, dtype=np.complex128)
+        _, sp = nat.dptr(sc.view(np.float64))
+        self.ctx.bind_stream()
+        check(self.lib.pg_pamp_step(self.h, ptr(psi), float(dt), sp, len(sc), C.byref(self.stats)), "pg_pamp_step")
+        return self.stats
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.lib.pg_pamp_destroy(self.h)
+        except Exception:
+            pass
+
+
+class CayleyStepper:
+    """pg_cayley: one Crank-Nicolson step per call (GMRES + block-diagonal preconditioner)."""
+
+    def __init__(self, op64, opb, prec64, precb, basis_size, precision, tolerance):
+        self.lib = op64.lib
+        self.ctx = op64.ctx
+        self._keep = (op64, opb, prec64, precb)
+        h = C.c_void_p()
+        check(self.lib.pg_cayley_create(op64.h, opb.h, prec64.h, precb.h, basis_size, precision, float(tolerance),
+                                        C.byref(h)), "pg_cayley_create")
+        self.h = h
+        self.stats = nat.KrylovStats()
+
+    def step(self, psi, dt, scales):
+        sc = np.ascontiguousarray(scales, dtype=np.complex128)
+        _, sp = nat.dptr(sc.view(np.float64))
+        self.ctx.bind_stream()
+        check(self.lib.pg_cayley_step(self.h, ptr(psi), float(dt), sp, len(sc), C.byref(self.stats)),
+              "pg_cayley_step")
+        return self.stats
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.lib.pg_cayley_destroy(self.h)
+        except Exception:
+            pass
+
+
+def vec_dot(ctx, x, y, precision=nat.PG_FP64):
+    out = np.zeros(2)
+    _, op = nat.dptr(out)
+    ctx.bind_stream()
+    check(ctx.lib.pg_vec_dot(ctx.h, precision, ptr(x), ptr(y), x.numel(), op), "pg_vec_dot")
+    return complex(out[0], out[1])

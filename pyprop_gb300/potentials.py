@@ -1,0 +1,174 @@
+"""Potential evaluators and laser time functions used by the tensor-potential generator.
+
+Each evaluator mirrors a C++ ``GetPotentialValue(pos)`` class of the reference examples
+(``examples/tensor/helium_stabilization_sae/potential.cpp``) but is evaluated on the whole
+tensor grid at once: ``pos`` is a tuple with one broadcastable numpy array per rank. A rank
+represented in its basis (geometry "Diagonal") passes basis values (the l of each
+channel); a rank on its grid passes grid points (theta, r).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+class PotentialBase:
+    def ApplyConfigSection(self, conf):
+        for key in getattr(self, "_keys", ()):
+            if conf.Exists(key):
+                setattr(self, key, conf.Get(key))
+
+    def __call__(self, pos, t=0.0):
+        return self.GetPotentialValue(pos)
+
+
+class KineticEnergyPotential(PotentialBase):
+    """Constant ``-1/(2 mass)``, used with ``differentiation=2`` (potential.cpp:6-35)."""
+    _keys = ("mass",)
+    mass = 1.0
+
+    def GetPotentialValue(self, pos):
+        shape = np.broadcast(*pos).shape
+        return np.full(shape, -1.0 / (2.0 * self.mass))
+
+
+class AngularKineticEnergyPotential(PotentialBase):
+    """``l(l+1) / (2 mass r^2)`` with l from the angular rank's basis values
+    (potential.cpp:219-253)."""
+    _keys = ("mass", "angular_rank", "radial_rank")
+    mass = 1.0
+    angular_rank = 0
+    radial_rank = 1
+
+    def GetPotentialValue(self, pos):
+        l = pos[self.angular_rank]
+        r = pos[self.radial_rank]
+        return l * (l + 1.0) / (2.0 * self.mass * r * r)
+
+
+class CoulombPotential(PotentialBase):
+    """Nuclear attraction ``-z / sqrt(r^2 + soft^2)``; ``soft = 0`` gives the pure ``-z/r``."""
+    _keys = ("z", "soft", "radial_rank", "charge")
+    z = 1.0
+    soft = 0.0
+    radial_rank = 1
+
+    def GetPotentialValue(self, pos):
+        r = pos[self.radial_rank]
+        return -self.z / np.sqrt(r * r + self.soft * self.soft) + 0.0 * np.broadcast_to(0.0, np.broadcast(*pos).shape)
+
+
+class SingleActiveElectronPotential(PotentialBase):
+    """Model potential ``-(Z + a1 e^{-a2 r} + a3 r e^{-a4 r} + a5 e^{-a6 r}) / sqrt(r^2+soft^2)``
+    (potential.cpp:256-314)."""
+    _keys = ("z", "a1", "a2", "a3", "a4", "a5", "a6", "soft", "radial_rank")
+    z = 1.0
+    a1 = a2 = a3 = a4 = a5 = a6 = 0.0
+    soft = 0.0
+    radial_rank = 1
+
+    def GetPotentialValue(self, pos):
+        r = np.abs(pos[self.radial_rank])
+        V = -(self.z + self.a1 * np.exp(-self.a2 * r) + self.a3 * r * np.exp(-self.a4 * r)
+              + self.a5 * np.exp(-self.a6 * r)) / np.sqrt(r * r + self.soft * self.soft)
+        return V + 0.0 * np.broadcast_to(0.0, np.broadcast(*pos).shape)
+
+
+class DipoleLaserPotentialLength(PotentialBase):
+    """Length-gauge dipole ``-charge * r * cos(theta)`` (potential.cpp:75-109)."""
+    _keys = ("angular_rank", "radial_rank", "charge")
+    angular_rank = 0
+    radial_rank = 1
+    charge = -1.0
+
+    def GetPotentialValue(self, pos):
+        theta = pos[self.angular_rank]
+        r = pos[self.radial_rank]
+        return -self.charge * r * np.cos(theta)
+
+
+class OverlapPotential(PotentialBase):
+    """Constant 1 with ``differentiation=0``: represents S itself in a rank."""
+
+    def GetPotentialValue(self, pos):
+        return np.ones(np.broadcast(*pos).shape)
+
+
+class ComplexAbsorbingPotential(PotentialBase):
+    """Complex absorber ``factor_real x^scaling_real + i factor_imag x^scaling_imag`` with
+    ``x = (r - absorber_start)/absorber_length`` on ``start < r <= start + length``, zero
+    elsewhere (potential.cpp ``ComplexAbsorbingPotential``)."""
+    _keys = ("radial_rank", "scaling_real", "scaling_imag", "factor_real", "factor_imag",
+             "absorber_start", "absorber_length")
+    radial_rank = 1
+    scaling_real = 1.0
+    scaling_imag = 1.0
+    factor_real = 0.0
+    factor_imag = -1.0
+    absorber_start = 0.0
+    absorber_length = 1.0
+
+    def GetPotentialValue(self, pos):
+        r = pos[self.radial_rank]
+        inside = (self.absorber_start < r) & (r <= self.absorber_start + self.absorber_length)
+        x = np.where(inside, (r - self.absorber_start) / self.absorber_length, 0.0)
+        val = np.where(inside, self.factor_real * x ** self.scaling_real
+                       + 1j * self.factor_imag * x ** self.scaling_imag, 0.0)
+        return np.broadcast_to(val, np.broadcast(*pos).shape).astype(np.complex128)
+
+
+# ---------------------------------------------------------------------------------------
+# laser time functions (examples/tensor/helium_stabilization_sae/example.py:220-273)
+# ---------------------------------------------------------------------------------------
+
+
+def LaserFunctionSimpleLength(conf, t):
+    """``E0 sin^2(pi t / T) cos(w t)`` for 0 <= t < T, else 0."""
+    if 0 <= t < conf.pulse_duration:
+        return conf.amplitude * np.sin(t * np.pi / conf.pulse_duration) ** 2 * np.cos(t * conf.frequency)
+    return 0.0
+
+
+def LaserFunctionVelocity(conf, t):
+    """``-E0 sin^2(pi t / T) cos(w t + phase)`` for 0 <= t < T, else 0."""
+    phase = getattr(conf, "phase", 0.0)
+    if 0 <= t < conf.pulse_duration:
+        return -conf.amplitude * np.sin(t * np.pi / conf.pulse_duration) ** 2 * np.cos(t * conf.frequency + phase)
+    return 0.0
+
+
+def LaserFunctionLength(conf, t):
+    """Time derivative of the velocity-gauge sin^2 pulse (example.py:243-252)."""
+    if 0 <= t < conf.pulse_duration:
+        T = conf.pulse_duration
+        w = conf.frequency
+        return conf.amplitude * np.sin(np.pi * t / T) * (
+            -2 * np.pi / T * np.cos(np.pi * t / T) * np.cos(w * t) + w * np.sin(np.pi * t / T) * np.sin(w * t))
+    return 0.0
+
+
+def LaserFunctionFlatTop(conf, t):
+    """Flat-top pulse with sin^2 ramps (example.py:254-273)."""
+    start = getattr(conf, "pulse_start", 0.0)
+    field = conf.amplitude * np.cos(t * conf.frequency)
+    if t > conf.pulse_duration or t < start:
+        return 0.0
+    if 0 <= t < conf.ramp_on_time:
+        return field * np.sin(t * np.pi / (2 * conf.ramp_on_time)) ** 2
+    if t > conf.pulse_duration - conf.ramp_off_time:
+        return field * np.sin((conf.pulse_duration - t) * np.pi / (2 * conf.ramp_off_time)) ** 2
+    return field
+
+
+POTENTIAL_CLASSES = {cls.__name__: cls for cls in (
+    KineticEnergyPotential, AngularKineticEnergyPotential, CoulombPotential,
+    SingleActiveElectronPotential, DipoleLaserPotentialLength, OverlapPotential,
+    ComplexAbsorbingPotential)}
+
+TIME_FUNCTIONS = {f.__name__: f for f in (
+    LaserFunctionSimpleLength, LaserFunctionVelocity, LaserFunctionLength, LaserFunctionFlatTop)}
+
+
+def register_potential(cls):
+    """Make a user evaluator class available to ``classname = "..."`` in configs."""
+    POTENTIAL_CLASSES[cls.__name__] = cls
+    return cls

@@ -1,0 +1,279 @@
+"""GPU propagators behind the reference's propagator interface.
+
+* ``BasisPropagatorGPU`` - generates and consolidates the tensor potentials
+  (``pyprop/tensorpotential/BasisPropagator.py:1-168``) and owns the device operators.
+* ``PamPropagatorGPU`` - ``pyprop/propagator/PamPropagator.py``: pAMP with the balanced
+  overlap (psi <- U psi, Krylov on U^-H H U^-1, psi <- U^-1 psi), H frozen at the step start.
+* ``CayleyPropagatorGPU`` - ``pyprop/propagator/CayleyPropagator.py``: Crank-Nicolson at
+  t + |dt|/2 solved by GMRES, left-preconditioned by the block-diagonal radial LU
+  (``BSplinePreconditioner``, ``examples/tensor/helium_stabilization_sae/example.py:275-318``).
+
+A config switches to these by naming them: ``propagator = PamPropagatorGPU`` or
+``CayleyPropagatorGPU``, ``base_propagator = BasisPropagatorGPU`` (``BasisPropagator`` is
+accepted as the same class). GPU-only keys in [Propagation]: ``gpu_precision``
+("fp64" or "fp32": precision of the Krylov basis and of the operator it multiplies).
+"""
+from __future__ import annotations
+
+import logging
+
+import numpy as np
+
+from . import _native as nat
+from .gpu import Banded, CayleyStepper, Context, DeviceOperator, PampStepper, precision_of, torch
+from .tensorpotential import TensorPotential
+
+_log = logging.getLogger("pyprop_gb300.propagator")
+
+
+class PropagatorBase:
+    """``pyprop/propagator/Propagator.py``: config plumbing shared by the propagators."""
+
+    def __init__(self, psi):
+        self.psi = psi
+        self.Rank = psi.GetRank()
+        self.PotentialList = []
+        self.RenormalizeActive = False
+
+    def ApplyConfig(self, config):
+        self.Config = config
+        config.Propagation.Apply(self)
+
+    def ApplyConfigSection(self, conf):
+        self.RenormalizeActive = bool(getattr(conf, "renormalization", False))
+        self.PropagationSection = conf
+
+    def SetupStep(self, dt):
+        pass
+
+    def RestartPropagation(self, timestep, startTime, propagationTime):
+        pass
+
+
+class BasisPropagatorGPU(PropagatorBase):
+    """Holds the consolidated tensor potentials and applies H on the device."""
+
+    def ApplyConfig(self, config):
+        PropagatorBase.ApplyConfig(self, config)
+        self.GeneratePotentials(config)
+        self.ConsolidatePotentials()
+
+    def GeneratePotential(self, conf):
+        pot = TensorPotential(self.psi)
+        conf.Apply(pot)
+        return pot
+
+    def GeneratePotentials(self, config):
+        names = getattr(config.Propagation, "grid_potential_list", [])
+        for name in names:
+            pot = self.GeneratePotential(config.GetSection(name))
+            for existing in self.PotentialList:
+                if existing.CanConsolidate(pot):
+                    existing.PotentialData = existing.PotentialData + pot.PotentialData
+                    existing.Name += "+" + pot.Name
+                    pot = None
+                    break
+            if pot is not None:
+                self.PotentialList.append(pot)
+
+    def ConsolidatePotentials(self):
+        """Merge potentials with equal storage, pairs and time dependence (BasisPropagator.py:68-105)."""
+        pots = list(self.PotentialList)
+        i = 0
+        while i < len(pots) - 1:
+            cur = pots[i]
+            for other in list(pots[i + 1:]):
+                if cur.CanConsolidate(other):
+                    cur.PotentialData = cur.PotentialData + other.PotentialData
+                    cur.Name += "+" + other.Name
+                    pots.remove(other)
+            i += 1
+        self.PotentialList = pots
+
+    def SetupStep(self, dt):
+        for pot in self.PotentialList:
+            pot.SetupStep(dt)
+        self._ops = {}
+
+    # device operators, built on first use
+    def device_operator(self, precision, with_overlap=False):
+        key = (precision, with_overlap)
+        if key not in getattr(self, "_ops", {}):
+            if not hasattr(self, "_ops"):
+                self._ops = {}
+            repr_ = self.psi.GetRepresentation()
+            self._ops[key] = DeviceOperator(Context.get(), self.PotentialList, repr_.GetFullShape(), repr_.kb,
+                                            precision, repr_.overlap_rows if with_overlap else None)
+        return self._ops[key]
+
+    def MultiplyPotential(self, srcPsi, destPsi, t, dt):
+        op = self.device_operator(nat.PG_FP64)
+        op.matvec(op.scales(t), srcPsi.GetData(), destPsi.GetData(), accumulate=True)
+
+    def MultiplyHamiltonianNoOverlap(self, srcPsi, destPsi, t, dt):
+        op = self.device_operator(nat.PG_FP64)
+        op.matvec(op.scales(t), srcPsi.GetData(), destPsi.GetData(), accumulate=False)
+
+    def MultiplyHamiltonian(self, srcPsi, destPsi, t, dt):
+        """dest = S^-1 H src (BasisPropagator.py:116-124)."""
+        self.MultiplyHamiltonianNoOverlap(srcPsi, destPsi, t, dt)
+        destPsi.GetRepresentation().SolveOverlap(destPsi)
+
+    def MultiplyHamiltonianBalancedOverlap(self, srcPsi, destPsi, t, dt):
+        """dest = U^-H H U^-1 src, src unchanged (BasisPropagator.py:131-159)."""
+        tmp = srcPsi.Copy()
+        repr_ = srcPsi.GetRepresentation()
+        repr_.SolveSqrtOverlap(False, tmp)
+        self.MultiplyHamiltonianNoOverlap(tmp, destPsi, t, dt)
+        repr_.SolveSqrtOverlap(True, destPsi)
+
+
+BasisPropagator = BasisPropagatorGPU
+
+
+def _basis_propagator(config, psi):
+    cls = getattr(config.Propagation, "base_propagator", BasisPropagatorGPU)
+    if cls not in (BasisPropagatorGPU,):
+        cls = BasisPropagatorGPU
+    bp = cls(psi)
+    config.Apply(bp)
+    return bp
+
+
+class PamPropagatorGPU(PropagatorBase):
+    def ApplyConfig(self, config):
+        PropagatorBase.ApplyConfig(self, config)
+        self.BasePropagator = _basis_propagator(config, self.psi)
+        conf = config.Propagation
+        self.BasisSize = int(getattr(conf, "krylov_basis_size", 20))
+        self.DoubleOrthogonalization = bool(getattr(conf, "krylov_double_orthogonalization", True))
+        self.Precision = precision_of(getattr(conf, "gpu_precision", "fp64"))
+        method = getattr(conf, "krylov_exponentiation_method", 0)
+        if method not in (0, "pade", "Pade"):
+            _log.warning("krylov_exponentiation_method=%r: the GPU path uses the Pade exponential", method)
+
+    def SetupStep(self, dt):
+        self.BasePropagator.SetupStep(dt)
+        repr_ = self.psi.GetRepresentation()
+        bp = self.BasePropagator
+        self.op64 = bp.device_operator(nat.PG_FP64)
+        self.opb = bp.device_operator(self.Precision)
+        self.ovl64 = Banded.overlap(self.op64, repr_.overlap_rows)
+        self.ovlb = self.ovl64 if self.Precision == nat.PG_FP64 else Banded.overlap(self.opb, repr_.overlap_rows)
+        self.stepper = PampStepper(self.op64, self.opb, self.ovl64, self.ovlb, self.BasisSize, self.Precision,
+                                   self.DoubleOrthogonalization)
+
+    def AdvanceStep(self, t, dt):
+        scales = self.op64.scales(t)
+        self.LastStats = self.stepper.step(self.psi.GetData(), dt, scales)
+
+    def MultiplyHamiltonian(self, srcPsi, destPsi, t, dt):
+        self.BasePropagator.MultiplyHamiltonian(srcPsi, destPsi, t, dt)
+
+    def GetErrorEstimate(self):
+        return self.LastStats.ErrorEstimate
+
+
+class BSplinePreconditioner:
+    """Block-diagonal radial preconditioner M_l = cS S + cH H_l (example.py:275-318):
+    the potentials listed in ``potential_evaluation`` (diagonal in the angular rank) are
+    summed per channel and each band is factored on the host, solved on the device."""
+
+    def __init__(self, psi):
+        self.psi = psi
+        self.PotentialSections = []
+
+    def ApplyConfigSection(self, conf):
+        self.PreconditionRank = getattr(conf, "rank", 1)
+        names = getattr(conf, "potential_evaluation", [])
+        self.PotentialSections = [conf.Config.GetSection(s) for s in names]
+
+    def SetHamiltonianScaling(self, scalingH):
+        self.HamiltonianScaling = scalingH
+
+    def SetOverlapScaling(self, scalingS):
+        self.OverlapScaling = scalingS
+
+    def Setup(self, prop, precision=nat.PG_FP64):
+        pots = []
+        for conf in self.PotentialSections:
+            pot = prop.BasePropagator.GeneratePotential(conf)
+            ids = [g.GetStorageId() for g in pot.GeometryList]
+            if ids[-1] != "BandNH" or any(i != "Diag" for i in ids[:-1]):
+                raise ValueError("preconditioner potentials must be Diag in the angular rank and BandNH radially")
+            pots.append(pot)
+        repr_ = self.psi.GetRepresentation()
+        self.ops = {}
+        self.solvers = {}
+        for prec in (nat.PG_FP64, precision):
+            if prec in self.solvers:
+                continue
+            op = DeviceOperator(Context.get(), pots, repr_.GetFullShape(), repr_.kb, prec)
+            self.ops[prec] = op
+            self.solvers[prec] = Banded.blockdiag(op, repr_.overlap_rows, self.OverlapScaling, self.HamiltonianScaling,
+                                                  list(range(1, 1 + len(pots))), [1.0] * len(pots))
+
+    def Solve(self, psi):
+        self.solvers[nat.PG_FP64].apply(nat.PG_BAND_PREC_SOLVE, psi.GetData())
+
+
+RadialPreconditioner = BSplinePreconditioner
+
+
+class CayleyPropagatorGPU(PropagatorBase):
+    def ApplyConfig(self, config):
+        PropagatorBase.ApplyConfig(self, config)
+        self.BasePropagator = _basis_propagator(config, self.psi)
+        conf = config.Propagation
+        self.BasisSize = int(getattr(conf, "krylov_basis_size", 20))
+        tol = float(getattr(conf, "krylov_tolerance", 0.0) or 0.0)
+        self.Tolerance = max(tol, 1e-13)  # gmres.h:223-229 floor
+        self.Precision = precision_of(getattr(conf, "gpu_precision", "fp64"))
+        name = getattr(conf, "preconditioner", None)
+        self.Preconditioner = None
+        if name:
+            sec = config.GetSection(name)
+            ptype = getattr(sec, "type", BSplinePreconditioner)
+            if not isinstance(ptype, type) or not issubclass(ptype, BSplinePreconditioner):
+                ptype = BSplinePreconditioner
+            pre = ptype(self.psi)
+            sec.Apply(pre)
+            self.Preconditioner = pre
+
+    def SetupStep(self, dt):
+        self.BasePropagator.SetupStep(dt)
+        if self.Preconditioner is None:
+            raise ValueError("CayleyPropagatorGPU needs a block-diagonal preconditioner section")
+        self.Preconditioner.SetHamiltonianScaling(1.0j * dt / 2.0)
+        self.Preconditioner.SetOverlapScaling(1.0)
+        self.Preconditioner.Setup(self, self.Precision)
+        bp = self.BasePropagator
+        self.op64 = bp.device_operator(nat.PG_FP64, with_overlap=True)
+        self.opb = bp.device_operator(self.Precision, with_overlap=True)
+        self.stepper = CayleyStepper(self.op64, self.opb, self.Preconditioner.solvers[nat.PG_FP64],
+                                     self.Preconditioner.solvers[self.Precision], self.BasisSize, self.Precision,
+                                     self.Tolerance)
+
+    def AdvanceStep(self, t, dt):
+        scales = self.op64.scales(t + abs(dt / 2.0))
+        self.LastStats = st = self.stepper.step(self.psi.GetData(), dt, scales)
+        if st.ErrorEstimate > 1e-4:
+            _log.warning("GMRES error estimate %g", st.ErrorEstimate)
+
+    def MultiplyHamiltonian(self, srcPsi, destPsi, t, dt):
+        self.BasePropagator.MultiplyHamiltonian(srcPsi, destPsi, t, dt)
+
+    def GetErrorEstimate(self):
+        return self.LastStats.ErrorEstimate
+
+
+class PamPropagator:
+    """Name of the reference's CPU propagator: this package has no CPU path."""
+
+    def __init__(self, psi):
+        raise RuntimeError("PamPropagator is the reference CPU propagator; name PamPropagatorGPU in the config")
+
+
+class CayleyPropagator:
+    def __init__(self, psi):
+        raise RuntimeError("CayleyPropagator is the reference CPU propagator; name CayleyPropagatorGPU in the config")

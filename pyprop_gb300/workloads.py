@@ -1,0 +1,132 @@
+"""Config files for the hydrogen-in-a-laser workloads the hot path is measured on.
+
+One electron, reduced spherical harmonics (m = 0) x B-splines of order 7 on an
+exponential-linear grid with 'zero' continuity, potentials kinetic (d^2/dr^2),
+centrifugal l(l+1)/2r^2, Coulomb -1/r (no softening) and the length-gauge dipole
+E(t) r cos(theta) with a sin^2 envelope (``LaserFunctionSimpleLength``). Each potential
+section uses the reference's geometry and differentiation keys
+(``examples/tensor/helium_stabilization_sae/config.ini``).
+
+* ``hydrogen(lmax=10, nbsplines=150, rmax=100)``: N = 150 B-splines from 147 breakpoints.
+* ``hydrogen(lmax=40, nbsplines=600, rmax=400)``: N = 600 from 597 breakpoints.
+The inner exponential part starts at ``xpartition`` 10 with gamma 2; the inner point count
+(and, when no count hits the total, ``xpartition`` in steps of 0.25) is searched so the
+breakpoint total is exact. The chosen values are written into the config text.
+"""
+from __future__ import annotations
+
+import math
+
+from .bspline import exponential_linear_params_for
+
+C_AU = 137.035999084
+BOHR_NM = 0.0529177210903
+
+
+def omega_for_wavelength(nm):
+    """Photon angular frequency (a.u.) for a wavelength in nm: 2 pi c / lambda."""
+    return 2.0 * math.pi * C_AU / (nm / BOHR_NM)
+
+
+def hydrogen(lmax=10, nbsplines=150, rmax=100.0, propagator="PamPropagatorGPU", precision="fp64",
+             timestep=0.01, duration=10.0, krylov_basis_size=20, amplitude=0.05, wavelength_nm=800.0,
+             pulse_duration=10.0, gmres_tolerance=1e-12, order=7):
+    total = nbsplines - 3 if order == 7 else nbsplines - (order - 4)
+    rpart, xsize = exponential_linear_params_for(0.0, rmax, total, gamma=2.0, rpartition=10.0)
+    omega = omega_for_wavelength(wavelength_nm)
+    return f"""
+[Representation]
+rank = 2
+type = core.CombinedRepresentation_2
+representation0 = "AngularRepresentation"
+representation1 = "RadialRepresentation"
+
+[AngularRepresentation]
+type = core.ReducedSphericalHarmonicRepresentation
+maxl = {lmax}
+m = 0
+
+[RadialRepresentation]
+type = core.BSplineRepresentation
+init_function = InitBSpline
+xmin = 0.0
+xmax = {rmax!r}
+xsize = {xsize}
+gamma = 2.0
+xpartition = {rpart!r}
+bpstype = 'exponentiallinear'
+continuity = 'zero'
+order = {order}
+quad_order_additional = 0
+projection_algorithm = 0
+
+[InitialCondition]
+type = InitialConditionType.Function
+function = lambda conf, x: 1.0 * (x[0] == 0)
+
+[PulseParameters]
+frequency = {omega!r}
+amplitude = {amplitude!r}
+pulse_duration = {pulse_duration!r}
+
+[Propagation]
+base = "PulseParameters"
+grid_potential_list = ["RadialKineticEnergy", "AngularKineticEnergy", "CoulombPotential", "LaserPotential"]
+propagator = {propagator}
+base_propagator = BasisPropagatorGPU
+preconditioner = "RadialPreconditioner"
+timestep = {timestep!r}
+duration = {duration!r}
+renormalization = False
+krylov_basis_size = {krylov_basis_size}
+krylov_tolerance = {gmres_tolerance!r}
+krylov_double_orthogonalization = True
+gpu_precision = "{precision}"
+silent = True
+
+[RadialPreconditioner]
+type = BSplinePreconditioner
+rank = 1
+potential_evaluation = ["RadialKineticEnergy", "AngularKineticEnergy", "CoulombPotential"]
+
+[Arpack]
+krylov_basis_size = 20
+krylov_tolerance = 1e-12
+krylov_eigenvalue_count = 2
+krylov_max_iteration_count = 50
+krylov_use_random_start = True
+
+[RadialKineticEnergy]
+classname = "KineticEnergyPotential"
+geometry0 = "Diagonal"
+geometry1 = "banded-nonhermitian"
+differentiation0 = 0
+differentiation1 = 2
+mass = 1
+
+[AngularKineticEnergy]
+classname = "AngularKineticEnergyPotential"
+geometry0 = "Diagonal"
+geometry1 = "banded-nonhermitian"
+mass = 1
+angular_rank = 0
+radial_rank = 1
+
+[CoulombPotential]
+classname = "CoulombPotential"
+geometry0 = "Diagonal"
+geometry1 = "banded-nonhermitian"
+radial_rank = 1
+z = 1.0
+soft = 0.0
+
+[LaserPotential]
+base = "PulseParameters"
+classname = "DipoleLaserPotentialLength"
+geometry0 = "dipoleselectionrule"
+geometry1 = "banded-nonhermitian"
+angular_rank = 0
+radial_rank = 1
+charge = -1.0
+time_function = LaserFunctionSimpleLength
+"""

@@ -1,0 +1,130 @@
+"""GPU parity of the Krylov propagators and solvers against the oracle."""
+import numpy as np
+import pytest
+
+from pyprop_gb300 import _native as nat
+from tests.helpers import golden, hydrogen_problem, infidelity, oracle_hamiltonian, relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _set_psi(prob, psi):
+    t = _torch()
+    prob.psi.GetData().copy_(t.as_tensor(psi, device="cuda"))
+
+
+def test_pamp_step_fp64_matches_golden(gpu):
+    g = golden("hydrogen_small.npz")
+    prob = hydrogen_problem(propagator="PamPropagatorGPU", precision="fp64")
+    prob.SetupStep(skipWavefunctionSetup=True)
+    _set_psi(prob, g["psi"])
+    prob.Propagator.AdvanceStep(float(g["t"]), float(g["dt"]))
+    out = prob.psi.numpy()
+    assert relerr(out, g["pamp"]) < 1e-12
+    st = prob.Propagator.LastStats
+    assert st.OpCount == 20 and st.ErrorEstimate < 1e-20
+
+
+def test_pamp_steps_against_oracle_fp64_and_fp32(gpu):
+    from oracle.propagators import OraclePam
+    g = golden("hydrogen_small.npz")
+    ref = hydrogen_problem()
+    ham = oracle_hamiltonian(ref)
+    pam = OraclePam(ham, 20, True)
+    psi_ref = g["psi"].copy()
+    t0, dt, nsteps = 1.0, 0.01, 10
+    for n in range(nsteps):
+        psi_ref = pam.step(psi_ref, t0 + n * dt, dt)
+    S = ham.overlap.S
+    for prec, tol_rel, tol_inf in [("fp64", 1e-11, 1e-20), ("fp32", 5e-5, 1e-9)]:
+        prob = hydrogen_problem(propagator="PamPropagatorGPU", precision=prec)
+        prob.SetupStep(skipWavefunctionSetup=True)
+        _set_psi(prob, g["psi"])
+        for n in range(nsteps):
+            prob.Propagator.AdvanceStep(t0 + n * dt, dt)
+        out = prob.psi.numpy()
+        assert relerr(out, psi_ref) < tol_rel, prec
+        assert infidelity(psi_ref, out, S) < tol_inf, prec
+        assert abs(ham.norm(out) - ham.norm(psi_ref)) < 10 * tol_rel
+
+
+def test_cayley_step_fp64_matches_golden(gpu):
+    g = golden("hydrogen_small.npz")
+    prob = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp64", gmres_tolerance=1e-13)
+    prob.SetupStep(skipWavefunctionSetup=True)
+    _set_psi(prob, g["psi"])
+    prob.Propagator.AdvanceStep(float(g["t"]), float(g["dt"]))
+    out = prob.psi.numpy()
+    assert relerr(out, g["cayley"]) < 1e-11
+    st = prob.Propagator.LastStats
+    assert st.TrueResidual < 1e-10 and 1 <= st.Iterations <= 20
+
+
+def test_cayley_mixed_precision_against_oracle(gpu):
+    from oracle.propagators import OracleCayley
+    g = golden("hydrogen_small.npz")
+    ham = oracle_hamiltonian(hydrogen_problem())
+    cay = OracleCayley(ham, 0.01, [0], 20, 1e-13)
+    psi_ref = g["psi"].copy()
+    t0, dt, nsteps = 1.0, 0.01, 10
+    for n in range(nsteps):
+        psi_ref = cay.step(psi_ref, t0 + n * dt, dt)
+    prob = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp32", gmres_tolerance=1e-12)
+    prob.SetupStep(skipWavefunctionSetup=True)
+    _set_psi(prob, g["psi"])
+    for n in range(nsteps):
+        prob.Propagator.AdvanceStep(t0 + n * dt, dt)
+        assert prob.Propagator.LastStats.ErrorEstimate < 1e-12
+    out = prob.psi.numpy()
+    assert relerr(out, psi_ref) < 1e-9
+    assert infidelity(psi_ref, out, ham.overlap.S) < 1e-16
+
+
+def test_piram_ground_state_shift_invert(gpu):
+    """Config-1 model (lmax 10, N 150): shift-invert pIRAM ground state E = -1/2."""
+    import pyprop_gb300 as pp
+    prob = hydrogen_problem(lmax=10, nbsplines=150, rmax=100.0)
+    prob.Config.Arpack.inverse_iterations = True
+    prob.Config.Arpack.krylov_eigenvalue_shift = -0.7
+    solver = pp.PiramSolverGPU(prob, seed=1234)
+    solver.Solve()
+    ev = solver.GetEigenvalues()
+    assert abs(ev[0] + 0.5) < 1e-10 and abs(ev[1] + 0.125) < 1e-9
+    solver.SetEigenvector(prob.psi, 0)
+    E = prob.GetEnergyExpectationValue()
+    assert abs(E + 0.5) < 1e-10
+    assert abs(prob.psi.GetNorm() - 1.0) < 1e-12
+
+
+def test_piram_plain_mode_small_operator(gpu):
+    """Plain pIRAM (S^-1 H, smallest real parts) on lmax 0: matches the oracle's pIRAM."""
+    import pyprop_gb300 as pp
+    from oracle.krylov import piram_solve
+    prob = hydrogen_problem(lmax=0, nbsplines=30, rmax=30.0)
+    prob.Config.Arpack.krylov_basis_size = 29
+    prob.Config.Arpack.krylov_max_iteration_count = 5
+    solver = pp.PiramSolverGPU(prob, seed=1234)
+    solver.Solve()
+    ham = oracle_hamiltonian(prob)
+    op = lambda v: ham.overlap.solve(ham.apply_H(v.reshape(1, -1), 0.0)).ravel()
+    start = np.random.default_rng(1234).uniform(0.0, 1.0, 30).astype(complex)
+    vals, vecs, rs, conv = piram_solve(op, start, 29, 2, 1e-12, 5)
+    assert np.max(np.abs(solver.GetEigenvalues() - vals.real)) < 1e-9
+    assert abs(solver.GetEigenvalues()[0] + 0.5) < 1e-6
+
+
+def test_problem_energy_and_norm(gpu):
+    """Problem API: energy <H> of a state and S-norm, GPU vs oracle."""
+    g = golden("hydrogen_small.npz")
+    prob = hydrogen_problem()
+    prob.SetupStep(skipWavefunctionSetup=True)
+    _set_psi(prob, g["psi"])
+    ham = oracle_hamiltonian(prob)
+    assert abs(prob.psi.GetNorm() - ham.norm(g["psi"])) < 1e-13
+    E = prob.GetEnergyExpectationValue()
+    assert abs(E - ham.energy(g["psi"], 0.0)) < 1e-10 * abs(E)
