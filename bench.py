@@ -165,6 +165,7 @@ def run_ours(args):
     probs = {}
     for prec in ("fp32", "fp64"):
         p = pp.Problem(pp.LoadString(_config(prec)))
+        p.Propagator.StepStats = False  # steps only enqueue; stats are read after the end event
         p.SetupStep(skipWavefunctionSetup=True)
         probs[prec] = p
     psi0, e0 = initial_state(probs["fp32"])

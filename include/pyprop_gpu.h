@@ -52,8 +52,11 @@ int pg_ctx_create(int device, pg_ctx **out);
 int pg_ctx_destroy(pg_ctx *ctx);
 /* The context's stream (cudaStream_t as void*). */
 void *pg_ctx_stream(pg_ctx *ctx);
-/* Use the caller's stream for all later work of this context (NULL = own stream). */
+/* Use the caller's stream for all later work of this context (NULL = the legacy default
+ * stream, so that work stays ordered with the caller's default-stream work). */
 int pg_ctx_set_stream(pg_ctx *ctx, void *stream);
+/* Go back to the context's own non-blocking stream. */
+int pg_ctx_use_own_stream(pg_ctx *ctx);
 /* Count of kernels this context launched since creation (own kernels only). */
 long long pg_ctx_kernel_launches(pg_ctx *ctx);
 int pg_ctx_synchronize(pg_ctx *ctx);
@@ -192,19 +195,32 @@ int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scales, int nsc
 typedef struct pg_cayley pg_cayley;
 /*
  * Cayley / Crank-Nicolson step (pyprop/propagator/CayleyPropagator.py:71-150):
- * (S + i dt/2 H) psi' = (S - i dt/2 H) psi with GMRES (core/krylov/gmres/gmres.h:433-505),
- * left-preconditioned by the block-diagonal LU. FP64 mode: the reference's scheme with
- * x0 = 0. Mixed mode (basis_precision PG_FP32): the residual r = b - A psi is formed in
- * FP64, GMRES in FP32 solves A d = r, psi' = psi + d, and the FP64 true residual is
- * checked (refinement repeats while it is above `tolerance`).
+ * (S + i dt/2 H) psi' = (S - i dt/2 H) psi with H at t + dt/2, GMRES
+ * (core/krylov/gmres/gmres.h:433-505) left-preconditioned by the block-diagonal LU.
+ * The step is one CUDA graph launch: GMRES iterations are a conditional WHILE node whose
+ * last kernel applies the Givens rotations and sets the loop condition on the device.
+ * basis_precision PG_FP64: the reference scheme (x0 = 0) in complex128. PG_FP32: the FP64
+ * residual r = b - A psi, a complex64 GMRES for the correction (2e-6 relative), psi += d,
+ * r -= A d in FP64, repeated while ||M^-1 r|| > tolerance (at most 4 passes).
+ * op64/op_basis must contain the overlap as slot 0 (Ident_BandNH term) and the terms of H
+ * in slots >= 1. tolerance is floored at 1e-13 (gmres.h:223-229). basis_size <= 64.
  */
 int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64, pg_banded *prec_basis,
                      int basis_size, int basis_precision, double tolerance, pg_cayley **out);
 int pg_cayley_destroy(pg_cayley *c);
-/* scales: host complex128 [nscales]: slot values of H(t + dt/2). Slot 0 must be the S term
- * weight-free slot reserved by the caller (see pg_cayley_create docs in the host layer). */
+/* One step. scales: host complex128 [nscales] slot values of H(t + dt/2) (slot 0 is
+ * ignored: the overlap weight is fixed). With stats non-NULL the call waits for the step and
+ * fills them (Iterations, ErrorEstimate = last least-squares residual, TrueResidual); with
+ * NULL it returns after enqueueing. */
 int pg_cayley_step(pg_cayley *c, void *psi, double dt, const double *scales, int nscales,
                    pg_krylov_stats *stats);
+/* nsteps steps; scales_table: host complex128 [nsteps][nscales]. */
+int pg_cayley_advance(pg_cayley *c, void *psi, double dt, int nsteps, const double *scales_table,
+                      int nscales, pg_krylov_stats *stats);
+/* Statistics of the last completed step (waits for the stream). */
+int pg_cayley_last_stats(pg_cayley *c, pg_krylov_stats *stats);
+/* FP64 mode: also compute ||(S + i dt/2 H) psi' - b|| every step (one extra matvec). */
+int pg_cayley_set_true_residual(pg_cayley *c, int on);
 
 /* Arnoldi expansion used by pIRAM (core/krylov/piram/piram/piram.h:346-442), Euclidean
  * inner product, re-orthogonalisation on. Operator: S^-1 H(slot scales) or, when

@@ -59,6 +59,7 @@ _SIGS = {
     "pg_ctx_destroy": (_I, [_P]),
     "pg_ctx_stream": (_P, [_P]),
     "pg_ctx_set_stream": (_I, [_P, _P]),
+    "pg_ctx_use_own_stream": (_I, [_P]),
     "pg_ctx_kernel_launches": (_LL, [_P]),
     "pg_ctx_synchronize": (_I, [_P]),
     "pg_tensor_multiply_diag_bandnh": (_I, [_P, _I, _I, _D, _P, _I, _I, _P, _I, _I, _I, _P]),
@@ -80,6 +81,9 @@ _SIGS = {
     "pg_cayley_create": (_I, [_P, _P, _P, _P, _I, _I, _D, C.POINTER(_P)]),
     "pg_cayley_destroy": (_I, [_P]),
     "pg_cayley_step": (_I, [_P, _P, _D, _DP, _I, C.POINTER(KrylovStats)]),
+    "pg_cayley_advance": (_I, [_P, _P, _D, _I, _DP, _I, C.POINTER(KrylovStats)]),
+    "pg_cayley_last_stats": (_I, [_P, C.POINTER(KrylovStats)]),
+    "pg_cayley_set_true_residual": (_I, [_P, _I]),
     "pg_arnoldi_expand": (_I, [_P, _P, _P, _DP, _I, _P, _I, _I, _P, _DP, _D, _I, _IP, _DP,
                                C.POINTER(KrylovStats)]),
     "pg_vec_dot": (_I, [_P, _I, _P, _P, _LL, _DP]),

@@ -1,0 +1,637 @@
+// Cayley / Crank-Nicolson step with a device-resident GMRES, captured in a CUDA graph.
+//
+// Reference: pyprop/propagator/CayleyPropagator.py:71-150 (b = (S - i dt/2 H) psi with H at
+// t + |dt|/2, left preconditioner M, GMRES on M^-1 (S + i dt/2 H)) and
+// core/krylov/gmres/gmres.h:433-505 (x0 = 0, least squares each iteration, stop when the
+// residual estimate is below max(tol, 1e-13) or the basis is full).
+//
+// Here the whole step is one graph launch: the GMRES iterations form a conditional WHILE
+// node whose body ends in a one-thread kernel that applies the Givens rotations to the new
+// Hessenberg column, updates the residual estimate and sets the loop condition on the
+// device (cudaGraphSetConditional). No host round trip per iteration.
+//
+// Precision modes:
+//   FP64  - the reference scheme in complex128 throughout.
+//   mixed - r = b - A psi = -i dt H psi in FP64; a complex64 GMRES (Givens and back
+//           substitution in FP32, Gram-Schmidt sums in FP64 across CTAs) solves
+//           M^-1 A d = M^-1 r to 2e-6 relative; psi += d and r -= A d in FP64; the outer
+//           WHILE node repeats while ||M^-1 r|| > tol (at most 4 passes). ||r|| in FP64 is
+//           the true residual reported.
+#include "pg_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+template <typename Rd, typename Rs>
+int pg_scale_copy(pg_ctx *ctx, const cx<Rs> *src, cx<Rd> *dst, cx<Rd> *dst2, long long n, const double *inv_scale_dev,
+                  double mul);
+int pg_axpy(pg_ctx *ctx, cxd a, const cxd *x, cxd *y, long long n);
+
+static const int GM_MAXM = 64;
+static const int RING = 64;
+
+struct GmresStats {
+    long long iterations;  // GMRES iterations of the step (all refinement passes)
+    int k;                 // basis vectors used by the last solve
+    int passes;            // refinement passes (mixed) / 1
+    double resid;          // least-squares residual estimate of the last solve
+    double true_resid;     // ||(S + i dt/2 H) psi' - b|| in FP64 (mixed; FP64 mode when requested)
+    double beta0;          // norm of the preconditioned right-hand side of the last solve
+};
+
+struct GmresState {
+    GmresStats stats;
+    int j;            // Krylov vector being expanded in this iteration
+    int pad;
+    double tol_eff;
+    double beta_last;
+    double cs[GM_MAXM];
+    double sn[2 * GM_MAXM];
+    double g[2 * (GM_MAXM + 1)];
+    double R[2 * GM_MAXM * GM_MAXM];  // column-major R[col * GM_MAXM + row]
+    double y[2 * GM_MAXM];
+};
+
+struct StepParams {
+    double dt;
+    double pad;
+    cxd h[PG_MAX_SLOTS];  // slot values of H(t + dt/2); slot 0 is the overlap slot
+};
+
+// scale sets derived on the device from StepParams
+enum { SC_PLUS = 0, SC_MINUS = 1, SC_DIFF = 2, SC_NEGPLUS = 3, SC_COUNT = 4 };
+
+// ------------------------------------------------------------------------------------
+// kernels
+// ------------------------------------------------------------------------------------
+__global__ void cay_scales_kernel(const StepParams *__restrict__ p, cxd *__restrict__ sc, GmresState *st)
+{
+    const int k = threadIdx.x;
+    if (k < PG_MAX_SLOTS) {
+        const double hdt = 0.5 * p->dt;
+        const cxd h = p->h[k];
+        // i*a*h = (-a h.y, a h.x)
+        cxd plus, minus, diff;
+        if (k == 0) {
+            plus = mk<double>(1.0, 0.0);
+            minus = mk<double>(1.0, 0.0);
+            diff = mk<double>(0.0, 0.0);
+        } else {
+            plus = mk<double>(-hdt * h.y, hdt * h.x);
+            minus = mk<double>(hdt * h.y, -hdt * h.x);
+            diff = mk<double>(2.0 * hdt * h.y, -2.0 * hdt * h.x);
+        }
+        sc[SC_PLUS * PG_MAX_SLOTS + k] = plus;
+        sc[SC_MINUS * PG_MAX_SLOTS + k] = minus;
+        sc[SC_DIFF * PG_MAX_SLOTS + k] = diff;
+        sc[SC_NEGPLUS * PG_MAX_SLOTS + k] = mk<double>(-plus.x, -plus.y);
+    }
+    if (k == 0) {
+        st->stats.iterations = 0;
+        st->stats.passes = 0;
+        st->stats.true_resid = -1.0;
+    }
+}
+
+// V[0] = d / ||d||, vcur = V[0]; reset the Givens state; decide whether GMRES runs.
+template <typename R>
+__global__ void cay_gmres_init_kernel(GmresState *st, const double *__restrict__ nrm, const cx<R> *__restrict__ d,
+                                      cx<R> *__restrict__ V0, cx<R> *__restrict__ vcur, long long n, double tol,
+                                      double rel_tol, int maxpass, cudaGraphConditionalHandle inner,
+                                      cudaGraphConditionalHandle outer, int has_outer)
+{
+    const double b = nrm[1];
+    const double s = b > 0.0 ? 1.0 / b : 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const cx<R> a = d[i];
+        const cx<R> v = mk<R>((R)((double)a.x * s), (R)((double)a.y * s));
+        V0[i] = v;
+        vcur[i] = v;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->j = 0;
+        st->stats.k = 0;
+        st->stats.beta0 = b;
+        st->stats.resid = b;
+        st->beta_last = b;
+        st->tol_eff = fmax(tol, rel_tol * b);
+        st->g[0] = b;
+        st->g[1] = 0.0;
+        st->stats.passes += 1;
+        const bool run = has_outer ? (b > tol) : (b > 0.0);
+        cudaGraphSetConditional(inner, run ? 1u : 0u);
+        if (has_outer) cudaGraphSetConditional(outer, (run && st->stats.passes < maxpass) ? 1u : 0u);
+    }
+}
+
+// V[j] = w / beta_{j-1} and vcur = V[j] for j > 0 (V[0] comes from the init kernel)
+template <typename R>
+__global__ void cay_next_vector_kernel(const GmresState *__restrict__ st, cx<R> *__restrict__ V, const cx<R> *__restrict__ w,
+                                       cx<R> *__restrict__ vcur, long long n)
+{
+    const int j = st->j;
+    if (j == 0) return;
+    const double b = st->beta_last;
+    const R s = (R)(b > 0.0 ? 1.0 / b : 0.0);
+    cx<R> *Vj = V + (size_t)j * n;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const cx<R> a = w[i];
+        const cx<R> v = mk<R>(a.x * s, a.y * s);
+        Vj[i] = v;
+        vcur[i] = v;
+    }
+}
+
+// One thread: Hessenberg column j = h1 + h2, subdiagonal ||w||; apply the previous Givens
+// rotations, form the new one, update g, store the R column, set the loop condition.
+// T is the arithmetic precision of the rotations (float for the complex64 inner solve).
+template <typename T>
+__global__ void cay_gmres_finalize_kernel(GmresState *st, const double *__restrict__ h1, const double *__restrict__ h2,
+                                          const double *__restrict__ h3, int m, cudaGraphConditionalHandle inner)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int j = st->j;
+    const int J = j + 1;
+    T hx[GM_MAXM + 1], hy[GM_MAXM + 1];
+    for (int i = 0; i < J; ++i) {
+        hx[i] = (T)(h1[2 * i] + h2[2 * i]);
+        hy[i] = (T)(h1[2 * i + 1] + h2[2 * i + 1]);
+    }
+    const double beta = h3[2 * J + 1];
+    hx[J] = (T)beta;
+    hy[J] = (T)0;
+    for (int i = 0; i < j; ++i) {
+        const T c = (T)st->cs[i];
+        const T sx = (T)st->sn[2 * i], sy = (T)st->sn[2 * i + 1];
+        // t = c h_i + s h_{i+1};  h_{i+1} = -conj(s) h_i + c h_{i+1}
+        const T tx = c * hx[i] + (sx * hx[i + 1] - sy * hy[i + 1]);
+        const T ty = c * hy[i] + (sx * hy[i + 1] + sy * hx[i + 1]);
+        const T ux = -(sx * hx[i] + sy * hy[i]) + c * hx[i + 1];
+        const T uy = -(sx * hy[i] - sy * hx[i]) + c * hy[i + 1];
+        hx[i] = tx; hy[i] = ty;
+        hx[i + 1] = ux; hy[i + 1] = uy;
+    }
+    const T a = hypot(hx[j], hy[j]);
+    const T bb = hypot(hx[j + 1], hy[j + 1]);
+    const T r = hypot(a, bb);
+    T c, sx, sy;
+    if (r == (T)0) { c = (T)1; sx = (T)0; sy = (T)0; }
+    else if (a == (T)0) { c = (T)0; sx = hx[j + 1] / bb; sy = -hy[j + 1] / bb; }
+    else {
+        c = a / r;
+        // s = (h_j / |h_j|) conj(h_{j+1}) / r
+        const T px = hx[j] / a, py = hy[j] / a;
+        sx = (px * hx[j + 1] + py * hy[j + 1]) / r;
+        sy = (py * hx[j + 1] - px * hy[j + 1]) / r;
+    }
+    const T rjx = c * hx[j] + (sx * hx[j + 1] - sy * hy[j + 1]);
+    const T rjy = c * hy[j] + (sx * hy[j + 1] + sy * hx[j + 1]);
+    hx[j] = rjx; hy[j] = rjy;
+    st->cs[j] = (double)c;
+    st->sn[2 * j] = (double)sx;
+    st->sn[2 * j + 1] = (double)sy;
+    // g_{j+1} = -conj(s) g_j ; g_j = c g_j
+    const T gx = (T)st->g[2 * j], gy = (T)st->g[2 * j + 1];
+    const T g1x = -(sx * gx + sy * gy), g1y = -(sx * gy - sy * gx);
+    st->g[2 * j] = (double)(c * gx);
+    st->g[2 * j + 1] = (double)(c * gy);
+    st->g[2 * (j + 1)] = (double)g1x;
+    st->g[2 * (j + 1) + 1] = (double)g1y;
+    for (int i = 0; i <= j; ++i) {
+        st->R[2 * (j * GM_MAXM + i)] = (double)hx[i];
+        st->R[2 * (j * GM_MAXM + i) + 1] = (double)hy[i];
+    }
+    const double resid = (double)hypot(g1x, g1y);
+    st->stats.k = J;
+    st->stats.resid = resid;
+    st->stats.iterations += 1;
+    st->beta_last = beta;
+    const bool bad = !(resid == resid);
+    const bool conv = bad || resid <= st->tol_eff || J >= m || !(beta > 1e-300);
+    if (!conv) st->j = j + 1;
+    cudaGraphSetConditional(inner, conv ? 0u : 1u);
+}
+
+// y = R^-1 g over the k completed columns (one thread, precision T)
+template <typename T>
+__global__ void cay_backsolve_kernel(GmresState *st)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int k = st->stats.k;
+    T yx[GM_MAXM], yy[GM_MAXM];
+    for (int i = k - 1; i >= 0; --i) {
+        T sx = (T)st->g[2 * i], sy = (T)st->g[2 * i + 1];
+        for (int q = i + 1; q < k; ++q) {
+            const T rx = (T)st->R[2 * (q * GM_MAXM + i)], ry = (T)st->R[2 * (q * GM_MAXM + i) + 1];
+            sx -= rx * yx[q] - ry * yy[q];
+            sy -= rx * yy[q] + ry * yx[q];
+        }
+        const T dx = (T)st->R[2 * (i * GM_MAXM + i)], dy = (T)st->R[2 * (i * GM_MAXM + i) + 1];
+        const T den = dx * dx + dy * dy;
+        if (den > (T)0) {
+            yx[i] = (sx * dx + sy * dy) / den;
+            yy[i] = (sy * dx - sx * dy) / den;
+        } else {
+            yx[i] = (T)0;
+            yy[i] = (T)0;
+        }
+    }
+    for (int i = 0; i < k; ++i) {
+        st->y[2 * i] = (double)yx[i];
+        st->y[2 * i + 1] = (double)yy[i];
+    }
+}
+
+// out = V y over k = st->stats.k vectors (complex128 result); out2 += same when given
+template <typename R>
+__global__ void cay_combine_kernel(const cx<R> *__restrict__ V, long long n, const GmresState *__restrict__ st,
+                                   cxd *__restrict__ out, cxd *__restrict__ out2)
+{
+    __shared__ cxd ys[GM_MAXM];
+    const int k = st->stats.k;
+    for (int j = threadIdx.x; j < k; j += blockDim.x) ys[j] = mk<double>(st->y[2 * j], st->y[2 * j + 1]);
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double ax = 0.0, ay = 0.0;
+        for (int j = 0; j < k; ++j) {
+            const cx<R> v = V[(size_t)j * n + i];
+            const cxd q = ys[j];
+            ax = fma((double)v.x, q.x, ax); ax = fma(-(double)v.y, q.y, ax);
+            ay = fma((double)v.x, q.y, ay); ay = fma((double)v.y, q.x, ay);
+        }
+        out[i] = mk<double>(ax, ay);
+        if (out2) out2[i] = out2[i] + mk<double>(ax, ay);
+    }
+}
+
+__global__ void cay_true_resid_kernel(GmresState *st, const double *__restrict__ nrm)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) st->stats.true_resid = nrm[1];
+}
+
+// ------------------------------------------------------------------------------------
+// host object
+// ------------------------------------------------------------------------------------
+struct pg_cayley {
+    pg_op *op64 = nullptr, *opb = nullptr;
+    pg_banded *prec64 = nullptr, *precb = nullptr;
+    pg_ctx *ctx = nullptr;
+    int m = 0, prec = PG_FP64;
+    long long n = 0;
+    double tol = 1e-13;
+    int true_residual = 0;
+    void *V = nullptr, *w = nullptr, *vcur = nullptr, *dconv = nullptr;
+    cxd *b64 = nullptr, *r64 = nullptr, *d64 = nullptr, *e64 = nullptr;
+    double *h1 = nullptr, *h2 = nullptr, *h3 = nullptr, *nrm = nullptr, *nrm2 = nullptr;
+    GmresState *st = nullptr;
+    GmresStats *h_stats = nullptr;
+    StepParams *d_params = nullptr;
+    StepParams *h_ring = nullptr;
+    cudaEvent_t ring_ev[RING];
+    bool ring_used[RING];
+    int ring_pos = 0;
+    cxd *d_sc = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void *built_psi = nullptr;
+    cudaStream_t cap[3] = {nullptr, nullptr, nullptr};
+};
+
+static int nblocks_for(pg_ctx *ctx, long long n)
+{
+    return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4LL * std::max(1, ctx->num_sms)));
+}
+
+// Conditional handle on the graph being captured by stream s.
+static int capture_handle(cudaStream_t s, cudaGraphConditionalHandle *handle, unsigned def, unsigned flags)
+{
+    cudaStreamCaptureStatus status;
+    cudaGraph_t g;
+    PG_CUDA_TRY(cudaStreamGetCaptureInfo(s, &status, nullptr, &g, nullptr, nullptr, nullptr));
+    if (status != cudaStreamCaptureStatusActive) return PG_ERR_STATE;
+    PG_CUDA_TRY(cudaGraphConditionalHandleCreate(handle, g, def, flags));
+    return PG_OK;
+}
+
+// WHILE node on `handle` appended to the capture of stream s; its body graph in *body.
+static int capture_while(cudaStream_t s, cudaGraphConditionalHandle handle, cudaGraph_t *body)
+{
+    cudaStreamCaptureStatus status;
+    cudaGraph_t g;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    PG_CUDA_TRY(cudaStreamGetCaptureInfo(s, &status, nullptr, &g, &deps, nullptr, &ndeps));
+    if (status != cudaStreamCaptureStatusActive) return PG_ERR_STATE;
+    cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
+    p.conditional.handle = handle;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    PG_CUDA_TRY(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p));
+    *body = p.conditional.phGraph_out[0];
+    PG_CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    return PG_OK;
+}
+
+// kernels of one GMRES iteration, captured on ctx->stream
+template <typename R, typename T>
+static int capture_iteration(pg_cayley *c, pg_op *op, pg_banded *pre, cudaGraphConditionalHandle inner)
+{
+    pg_ctx *ctx = c->ctx;
+    cudaStream_t s = ctx->stream;
+    const long long n = c->n;
+    const int nb = nblocks_for(ctx, n);
+    cx<R> *V = (cx<R> *)c->V, *w = (cx<R> *)c->w, *vcur = (cx<R> *)c->vcur;
+    cay_next_vector_kernel<R><<<nb, 256, 0, s>>>(c->st, V, w, vcur, n);
+    PG_TRY(pg_check_launch(ctx));
+    pg_scales dummy;
+    memset(&dummy, 0, sizeof(dummy));
+    PG_TRY(pg_op_matvec_dev(op, dummy, c->d_sc + SC_PLUS * PG_MAX_SLOTS, vcur, w, 0, nullptr, nullptr));
+    PG_TRY(pg_banded_apply_dev(pre, PG_BAND_PREC_SOLVE, w));
+    PG_TRY(pg_multidot<R>(ctx, V, n, c->m, w, n, c->h1, &c->st->j));
+    PG_TRY(pg_gs_update<R>(ctx, V, n, c->m, c->h1, w, n, 1, c->h2, &c->st->j));
+    PG_TRY(pg_gs_update<R>(ctx, V, n, c->m, c->h2, w, n, 0, c->h3, &c->st->j));
+    cay_gmres_finalize_kernel<T><<<1, 32, 0, s>>>(c->st, c->h1, c->h2, c->h3, c->m, inner);
+    return pg_check_launch(ctx);
+}
+
+// Capture a nested body: begin capture of stream s into `body`, run fn with ctx->stream = s.
+template <typename F>
+static int capture_body(pg_cayley *c, cudaStream_t s, cudaGraph_t body, F fn)
+{
+    pg_ctx *ctx = c->ctx;
+    PG_CUDA_TRY(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    cudaStream_t saved = ctx->stream;
+    ctx->stream = s;
+    int code = fn();
+    ctx->stream = saved;
+    cudaGraph_t out = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &out);
+    if (code == PG_OK && e != cudaSuccess) {
+        pg_set_last_error(e, "cudaStreamEndCapture(body)", __FILE__, __LINE__);
+        code = PG_ERR_CUDA;
+    }
+    return code;
+}
+
+// plain FP64 step (the reference scheme)
+static int record_fp64(pg_cayley *c, cxd *psi)
+{
+    pg_ctx *ctx = c->ctx;
+    cudaStream_t s0 = ctx->stream;
+    const long long n = c->n;
+    const int nb = nblocks_for(ctx, n);
+    pg_scales dummy;
+    memset(&dummy, 0, sizeof(dummy));
+    cay_scales_kernel<<<1, 32, 0, s0>>>(c->d_params, c->d_sc, c->st);
+    PG_TRY(pg_check_launch(ctx));
+    PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_MINUS * PG_MAX_SLOTS, psi, c->b64, 0, nullptr, nullptr));
+    PG_CUDA_TRY(cudaMemcpyAsync(c->d64, c->b64, sizeof(cxd) * n, cudaMemcpyDeviceToDevice, s0));
+    PG_TRY(pg_banded_apply_dev(c->prec64, PG_BAND_PREC_SOLVE, c->d64));
+    PG_TRY(pg_multidot<double>(ctx, c->d64, n, 0, c->d64, n, c->nrm));
+    cudaGraphConditionalHandle inner;
+    PG_TRY(capture_handle(s0, &inner, 0, 0));
+    cay_gmres_init_kernel<double><<<nb, 256, 0, s0>>>(c->st, c->nrm, c->d64, (cxd *)c->V, (cxd *)c->vcur, n, c->tol,
+                                                      0.0, 1, inner, inner, 0);
+    PG_TRY(pg_check_launch(ctx));
+    cudaGraph_t body;
+    PG_TRY(capture_while(s0, inner, &body));
+    PG_TRY(capture_body(c, c->cap[1], body, [&]() { return capture_iteration<double, double>(c, c->op64, c->prec64, inner); }));
+    cay_backsolve_kernel<double><<<1, 32, 0, s0>>>(c->st);
+    PG_TRY(pg_check_launch(ctx));
+    cay_combine_kernel<double><<<nb, 256, 0, s0>>>((const cxd *)c->V, n, c->st, psi, nullptr);
+    PG_TRY(pg_check_launch(ctx));
+    if (c->true_residual) {
+        // ||(S + i dt/2 H) psi' - b||
+        PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_PLUS * PG_MAX_SLOTS, psi, c->r64, 0, nullptr, nullptr));
+        PG_TRY(pg_axpy(ctx, mk<double>(-1.0, 0.0), c->b64, c->r64, n));
+        PG_TRY(pg_multidot<double>(ctx, c->r64, n, 0, c->r64, n, c->nrm2));
+        cay_true_resid_kernel<<<1, 32, 0, s0>>>(c->st, c->nrm2);
+        PG_TRY(pg_check_launch(ctx));
+    }
+    PG_CUDA_TRY(cudaMemcpyAsync(c->h_stats, &c->st->stats, sizeof(GmresStats), cudaMemcpyDeviceToHost, s0));
+    return PG_OK;
+}
+
+// mixed step: FP64 residual, complex64 GMRES correction, refinement WHILE loop
+static int record_mixed(pg_cayley *c, cxd *psi)
+{
+    pg_ctx *ctx = c->ctx;
+    cudaStream_t s0 = ctx->stream;
+    const long long n = c->n;
+    const int nb = nblocks_for(ctx, n);
+    pg_scales dummy;
+    memset(&dummy, 0, sizeof(dummy));
+    cay_scales_kernel<<<1, 32, 0, s0>>>(c->d_params, c->d_sc, c->st);
+    PG_TRY(pg_check_launch(ctx));
+    PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_DIFF * PG_MAX_SLOTS, psi, c->r64, 0, nullptr, nullptr));
+    cudaGraphConditionalHandle outer;
+    PG_TRY(capture_handle(s0, &outer, 1, cudaGraphCondAssignDefault));
+    cudaGraph_t obody;
+    PG_TRY(capture_while(s0, outer, &obody));
+    PG_TRY(capture_body(c, c->cap[1], obody, [&]() -> int {
+        cudaStream_t s1 = ctx->stream;
+        cxf *dconv = (cxf *)c->dconv;
+        PG_TRY((pg_scale_copy<float, double>(ctx, c->r64, dconv, nullptr, n, nullptr, 1.0)));
+        PG_TRY(pg_banded_apply_dev(c->precb, PG_BAND_PREC_SOLVE, dconv));
+        PG_TRY(pg_multidot<float>(ctx, dconv, n, 0, dconv, n, c->nrm));
+        cudaGraphConditionalHandle inner;
+        PG_TRY(capture_handle(s1, &inner, 0, 0));
+        cay_gmres_init_kernel<float><<<nb, 256, 0, s1>>>(c->st, c->nrm, dconv, (cxf *)c->V, (cxf *)c->vcur, n, c->tol,
+                                                         2e-6, 4, inner, outer, 1);
+        PG_TRY(pg_check_launch(ctx));
+        cudaGraph_t ibody;
+        PG_TRY(capture_while(s1, inner, &ibody));
+        PG_TRY(capture_body(c, c->cap[2], ibody, [&]() { return capture_iteration<float, float>(c, c->opb, c->precb, inner); }));
+        cay_backsolve_kernel<float><<<1, 32, 0, s1>>>(c->st);
+        PG_TRY(pg_check_launch(ctx));
+        cay_combine_kernel<float><<<nb, 256, 0, s1>>>((const cxf *)c->V, n, c->st, c->e64, psi);
+        PG_TRY(pg_check_launch(ctx));
+        // r -= (S + i dt/2 H) e   in FP64
+        return pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_NEGPLUS * PG_MAX_SLOTS, c->e64, c->r64, 1, nullptr, nullptr);
+    }));
+    PG_TRY(pg_multidot<double>(ctx, c->r64, n, 0, c->r64, n, c->nrm2));
+    cay_true_resid_kernel<<<1, 32, 0, s0>>>(c->st, c->nrm2);
+    PG_TRY(pg_check_launch(ctx));
+    PG_CUDA_TRY(cudaMemcpyAsync(c->h_stats, &c->st->stats, sizeof(GmresStats), cudaMemcpyDeviceToHost, s0));
+    return PG_OK;
+}
+
+static int build_graph(pg_cayley *c, cxd *psi)
+{
+    pg_ctx *ctx = c->ctx;
+    if (c->exec) { cudaGraphExecDestroy(c->exec); c->exec = nullptr; }
+    if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+    cudaStream_t saved = ctx->stream;
+    PG_CUDA_TRY(cudaStreamBeginCapture(c->cap[0], cudaStreamCaptureModeThreadLocal));
+    ctx->stream = c->cap[0];
+    int code = (c->prec == PG_FP64) ? record_fp64(c, psi) : record_mixed(c, psi);
+    ctx->stream = saved;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->cap[0], &g);
+    if (code != PG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return code;
+    }
+    if (e != cudaSuccess) {
+        pg_set_last_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+        return PG_ERR_CUDA;
+    }
+    c->graph = g;
+    PG_CUDA_TRY(cudaGraphInstantiate(&c->exec, g, 0));
+    c->built_psi = psi;
+    return PG_OK;
+}
+
+extern "C" int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64, pg_banded *prec_basis, int basis_size,
+                                int basis_precision, double tolerance, pg_cayley **out)
+{
+    if (!op64 || !op_basis || !prec64 || !prec_basis || !out) return PG_ERR_ARG;
+    if (basis_size < 2 || basis_size > GM_MAXM || basis_size > PG_RED_COLS - 2) return PG_ERR_ARG;
+    if (op64->precision != PG_FP64 || op_basis->precision != basis_precision) return PG_ERR_ARG;
+    if (prec64->kind != 1 || prec_basis->kind != 1) return PG_ERR_ARG;
+    if (prec64->op->precision != PG_FP64 || prec_basis->op->precision != basis_precision) return PG_ERR_ARG;
+    if (basis_precision != PG_FP64 && basis_precision != PG_FP32) return PG_ERR_ARG;
+    pg_cayley *c = new pg_cayley();
+    c->op64 = op64;
+    c->opb = op_basis;
+    c->prec64 = prec64;
+    c->precb = prec_basis;
+    c->ctx = op64->ctx;
+    c->m = basis_size;
+    c->prec = basis_precision;
+    c->tol = std::max(tolerance, 1e-13);
+    c->n = (long long)op64->nrows * op64->N;
+    const size_t esz = basis_precision == PG_FP64 ? sizeof(cxd) : sizeof(cxf);
+    PG_CUDA_TRY(cudaMalloc(&c->V, esz * (size_t)c->m * c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->w, esz * (size_t)c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->vcur, esz * (size_t)c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->dconv, esz * (size_t)c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->b64, sizeof(cxd) * (size_t)c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->r64, sizeof(cxd) * (size_t)c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->d64, sizeof(cxd) * (size_t)c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->e64, sizeof(cxd) * (size_t)c->n));
+    const size_t cols = sizeof(double) * 2 * (PG_RED_COLS + 2);
+    PG_CUDA_TRY(cudaMalloc(&c->h1, cols));
+    PG_CUDA_TRY(cudaMalloc(&c->h2, cols));
+    PG_CUDA_TRY(cudaMalloc(&c->h3, cols));
+    PG_CUDA_TRY(cudaMalloc(&c->nrm, cols));
+    PG_CUDA_TRY(cudaMalloc(&c->nrm2, cols));
+    PG_CUDA_TRY(cudaMalloc(&c->st, sizeof(GmresState)));
+    PG_CUDA_TRY(cudaMemset(c->st, 0, sizeof(GmresState)));
+    PG_CUDA_TRY(cudaMallocHost(&c->h_stats, sizeof(GmresStats)));
+    memset(c->h_stats, 0, sizeof(GmresStats));
+    PG_CUDA_TRY(cudaMalloc(&c->d_params, sizeof(StepParams)));
+    PG_CUDA_TRY(cudaMallocHost(&c->h_ring, sizeof(StepParams) * RING));
+    PG_CUDA_TRY(cudaMalloc(&c->d_sc, sizeof(cxd) * SC_COUNT * PG_MAX_SLOTS));
+    for (int k = 0; k < RING; ++k) {
+        PG_CUDA_TRY(cudaEventCreateWithFlags(&c->ring_ev[k], cudaEventDisableTiming));
+        c->ring_used[k] = false;
+    }
+    for (int k = 0; k < 3; ++k) PG_CUDA_TRY(cudaStreamCreateWithFlags(&c->cap[k], cudaStreamNonBlocking));
+    *out = c;
+    return PG_OK;
+}
+
+extern "C" int pg_cayley_destroy(pg_cayley *c)
+{
+    if (!c) return PG_ERR_ARG;
+    cudaStreamSynchronize(c->ctx->stream);
+    if (c->exec) cudaGraphExecDestroy(c->exec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    for (int k = 0; k < 3; ++k)
+        if (c->cap[k]) cudaStreamDestroy(c->cap[k]);
+    for (int k = 0; k < RING; ++k) cudaEventDestroy(c->ring_ev[k]);
+    void *bufs[] = {c->V, c->w, c->vcur, c->dconv, c->b64, c->r64, c->d64, c->e64, c->h1, c->h2, c->h3, c->nrm,
+                    c->nrm2, c->st, c->d_params, c->d_sc};
+    for (void *b : bufs) cudaFree(b);
+    if (c->h_stats) cudaFreeHost(c->h_stats);
+    if (c->h_ring) cudaFreeHost(c->h_ring);
+    delete c;
+    return PG_OK;
+}
+
+// one step: upload this step's H(t+dt/2) slot values, launch the graph
+static int cayley_launch(pg_cayley *c, cxd *psi, double dt, const double *scales, int nscales)
+{
+    pg_ctx *ctx = c->ctx;
+    if (!c->exec || c->built_psi != psi) PG_TRY(build_graph(c, psi));
+    const int slot = c->ring_pos;
+    c->ring_pos = (c->ring_pos + 1) % RING;
+    if (c->ring_used[slot]) PG_CUDA_TRY(cudaEventSynchronize(c->ring_ev[slot]));
+    StepParams &p = c->h_ring[slot];
+    memset(&p, 0, sizeof(p));
+    p.dt = dt;
+    for (int k = 0; k < PG_MAX_SLOTS; ++k) p.h[k] = mk<double>(k < nscales ? scales[2 * k] : 0.0, k < nscales ? scales[2 * k + 1] : 0.0);
+    PG_CUDA_TRY(cudaMemcpyAsync(c->d_params, &p, sizeof(StepParams), cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA_TRY(cudaEventRecord(c->ring_ev[slot], ctx->stream));
+    c->ring_used[slot] = true;
+    PG_CUDA_TRY(cudaGraphLaunch(c->exec, ctx->stream));
+    return PG_OK;
+}
+
+// Kernels one graph launch ran, from its iteration and pass counts:
+// FP64 8 + 8k (+4 with the true residual); mixed 4 + 8 passes + 8 iterations.
+static long long step_kernels(const pg_cayley *c, const GmresStats &g)
+{
+    if (c->prec == PG_FP64) return 8 + 8 * g.iterations + (c->true_residual ? 4 : 0);
+    return 4 + 8LL * g.passes + 8 * g.iterations;
+}
+
+static void fill_stats(pg_cayley *c, pg_krylov_stats *st)
+{
+    const GmresStats &g = *c->h_stats;
+    st->Iterations = g.iterations;
+    st->OpCount = g.iterations;
+    st->InnerProductCount = 2 * g.iterations;
+    st->ReOrthoCount = g.iterations;
+    st->RestartCount = g.passes;
+    st->ErrorEstimate = g.resid;
+    st->TrueResidual = g.true_resid;
+}
+
+extern "C" int pg_cayley_step(pg_cayley *c, void *psi, double dt, const double *scales, int nscales, pg_krylov_stats *st)
+{
+    if (!c || !psi || !scales || nscales < 1 || nscales > PG_MAX_SLOTS) return PG_ERR_ARG;
+    PG_TRY(cayley_launch(c, (cxd *)psi, dt, scales, nscales));
+    if (st) {
+        PG_CUDA_TRY(cudaStreamSynchronize(c->ctx->stream));
+        fill_stats(c, st);
+        c->ctx->launches += step_kernels(c, *c->h_stats);
+    }
+    return PG_OK;
+}
+
+extern "C" int pg_cayley_set_true_residual(pg_cayley *c, int on)
+{
+    if (!c) return PG_ERR_ARG;
+    if ((on != 0) != (c->true_residual != 0)) {
+        c->true_residual = on ? 1 : 0;
+        c->built_psi = nullptr;  // rebuild the graph on the next step
+    }
+    return PG_OK;
+}
+
+extern "C" int pg_cayley_advance(pg_cayley *c, void *psi, double dt, int nsteps, const double *scales_table,
+                                 int nscales, pg_krylov_stats *st)
+{
+    if (!c || !psi || !scales_table || nsteps < 0 || nscales < 1 || nscales > PG_MAX_SLOTS) return PG_ERR_ARG;
+    long long iters = 0;
+    for (int k = 0; k < nsteps; ++k)
+        PG_TRY(cayley_launch(c, (cxd *)psi, dt, scales_table + 2 * (size_t)k * nscales, nscales));
+    if (st) {
+        PG_CUDA_TRY(cudaStreamSynchronize(c->ctx->stream));
+        fill_stats(c, st);
+        (void)iters;
+    }
+    return PG_OK;
+}
+
+extern "C" int pg_cayley_last_stats(pg_cayley *c, pg_krylov_stats *st)
+{
+    if (!c || !st) return PG_ERR_ARG;
+    PG_CUDA_TRY(cudaStreamSynchronize(c->ctx->stream));
+    fill_stats(c, st);
+    return PG_OK;
+}

@@ -103,7 +103,16 @@ extern "C" void *pg_ctx_stream(pg_ctx *ctx) { return ctx ? (void *)ctx->stream :
 extern "C" int pg_ctx_set_stream(pg_ctx *ctx, void *stream)
 {
     if (!ctx) return PG_ERR_ARG;
-    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    // NULL is the legacy default stream (what torch reports as stream 0), so the library's
+    // kernels stay ordered with the caller's work on that stream
+    ctx->stream = (cudaStream_t)stream;
+    return PG_OK;
+}
+
+extern "C" int pg_ctx_use_own_stream(pg_ctx *ctx)
+{
+    if (!ctx) return PG_ERR_ARG;
+    ctx->stream = ctx->own_stream;
     return PG_OK;
 }
 

@@ -340,221 +340,6 @@ extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scal
 }
 
 // ------------------------------------------------------------------------------------
-// GMRES (left-preconditioned) and the Cayley step
-// ------------------------------------------------------------------------------------
-struct pg_cayley {
-    pg_op *op64 = nullptr, *opb = nullptr;
-    pg_banded *prec64 = nullptr, *precb = nullptr;
-    int m = 0, prec = PG_FP64;
-    long long n = 0;
-    double tolerance = 1e-13;
-    void *V = nullptr, *w = nullptr;     // basis precision
-    cxd *b64 = nullptr, *r64 = nullptr, *d64 = nullptr, *e64 = nullptr;  // FP64 work vectors
-    double *d_y = nullptr, *h_y = nullptr;
-    double *d_norm = nullptr;
-    ArnoldiBuf ab;
-};
-
-extern "C" int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64, pg_banded *prec_basis, int basis_size,
-                                int basis_precision, double tolerance, pg_cayley **out)
-{
-    if (!op64 || !op_basis || !prec64 || !prec_basis || !out) return PG_ERR_ARG;
-    if (basis_size < 2 || basis_size > PG_RED_COLS - 2) return PG_ERR_ARG;
-    if (op64->precision != PG_FP64 || op_basis->precision != basis_precision) return PG_ERR_ARG;
-    if (prec64->kind != 1 || prec_basis->kind != 1) return PG_ERR_ARG;
-    pg_cayley *c = new pg_cayley();
-    c->op64 = op64;
-    c->opb = op_basis;
-    c->prec64 = prec64;
-    c->precb = prec_basis;
-    c->m = basis_size;
-    c->prec = basis_precision;
-    c->tolerance = tolerance;
-    c->n = (long long)op64->nrows * op64->N;
-    const size_t esz = basis_precision == PG_FP64 ? sizeof(cxd) : sizeof(cxf);
-    PG_CUDA_TRY(cudaMalloc(&c->V, esz * (size_t)c->m * c->n));
-    PG_CUDA_TRY(cudaMalloc(&c->w, esz * (size_t)c->n));
-    PG_CUDA_TRY(cudaMalloc(&c->b64, sizeof(cxd) * (size_t)c->n));
-    PG_CUDA_TRY(cudaMalloc(&c->r64, sizeof(cxd) * (size_t)c->n));
-    PG_CUDA_TRY(cudaMalloc(&c->d64, sizeof(cxd) * (size_t)c->n));
-    PG_CUDA_TRY(cudaMalloc(&c->e64, sizeof(cxd) * (size_t)c->n));
-    PG_CUDA_TRY(cudaMalloc(&c->d_y, sizeof(double) * 2 * c->m));
-    PG_CUDA_TRY(cudaMallocHost(&c->h_y, sizeof(double) * 2 * c->m));
-    PG_CUDA_TRY(cudaMalloc(&c->d_norm, sizeof(double) * 2 * PG_RED_COLS));
-    PG_TRY(c->ab.alloc(c->m));
-    *out = c;
-    return PG_OK;
-}
-
-extern "C" int pg_cayley_destroy(pg_cayley *c)
-{
-    if (!c) return PG_ERR_ARG;
-    cudaFree(c->V);
-    cudaFree(c->w);
-    cudaFree(c->b64);
-    cudaFree(c->r64);
-    cudaFree(c->d64);
-    cudaFree(c->e64);
-    cudaFree(c->d_y);
-    if (c->h_y) cudaFreeHost(c->h_y);
-    cudaFree(c->d_norm);
-    c->ab.release();
-    delete c;
-    return PG_OK;
-}
-
-// GMRES on A = M^-1 (S + i dt/2 H): V[0] holds rhs (already preconditioned) scaled by
-// 1/beta0. Writes the solution combination into out (complex128, overwritten).
-// Stops when the least-squares residual is <= tol or after m matvecs.
-template <typename R>
-static int gmres_solve(pg_cayley *c, const pg_scales &scA, double beta0, double tol, cxd *out, pg_krylov_stats *st)
-{
-    pg_ctx *ctx = c->op64->ctx;
-    const long long n = c->n;
-    const int m = c->m;
-    cx<R> *V = (cx<R> *)c->V;
-    cx<R> *w = (cx<R> *)c->w;
-    // Givens state
-    std::vector<zd> Rm((size_t)(m + 1) * m, zd(0.0, 0.0));  // R[i][j] row-major (m+1) x m
-    std::vector<zd> cs(m), sn(m), g(m + 1, zd(0.0, 0.0));
-    g[0] = beta0;
-    int kdone = 0;
-    double resid = beta0;
-    for (int j = 0; j < m; ++j) {
-        if (j > 0) PG_TRY((pg_scale_copy<R, R>(ctx, w, V + (size_t)j * n, nullptr, n, c->ab.dcol(j - 1, 2) + 2 * j + 1, 1.0)));
-        PG_TRY(pg_op_matvec_dev(c->opb, scA, nullptr, V + (size_t)j * n, w, 0, nullptr, nullptr));
-        PG_TRY(pg_banded_apply_dev(c->precb, PG_BAND_PREC_SOLVE, w));
-        if (st) st->OpCount++;
-        PG_TRY(cgs2<R>(ctx, V, n, j + 1, w, c->ab, j, 1, st));
-        PG_TRY(fetch_columns(ctx, c->ab, j, j + 1));
-        std::vector<zd> h(j + 2);
-        double beta = 0.0;
-        read_column(c->ab, j, j + 1, 1, h.data(), &beta);
-        h[j + 1] = beta;
-        // apply previous rotations
-        for (int i = 0; i < j; ++i) {
-            const zd t = cs[i] * h[i] + sn[i] * h[i + 1];
-            h[i + 1] = -std::conj(sn[i]) * h[i] + std::conj(cs[i]) * h[i + 1];
-            h[i] = t;
-        }
-        // new rotation zeroing h[j+1]
-        const double a = std::abs(h[j]), bb = std::abs(h[j + 1]);
-        const double r = std::hypot(a, bb);
-        if (r == 0.0) { cs[j] = 1.0; sn[j] = 0.0; }
-        else if (a == 0.0) { cs[j] = 0.0; sn[j] = std::conj(h[j + 1]) / bb; }
-        else {
-            cs[j] = a / r;
-            sn[j] = (h[j] / a) * std::conj(h[j + 1]) / r;
-        }
-        const zd hj = cs[j] * h[j] + sn[j] * h[j + 1];
-        h[j] = hj;
-        h[j + 1] = 0.0;
-        g[j + 1] = -std::conj(sn[j]) * g[j];
-        g[j] = cs[j] * g[j];
-        for (int i = 0; i <= j; ++i) Rm[(size_t)i * m + j] = h[i];
-        kdone = j + 1;
-        resid = std::abs(g[j + 1]);
-        if (resid <= tol || beta < 1e-300) break;
-    }
-    // back substitution R y = g
-    std::vector<zd> y(kdone);
-    for (int i = kdone - 1; i >= 0; --i) {
-        zd s = g[i];
-        for (int q = i + 1; q < kdone; ++q) s -= Rm[(size_t)i * m + q] * y[q];
-        y[i] = s / Rm[(size_t)i * m + i];
-    }
-    for (int i = 0; i < kdone; ++i) {
-        c->h_y[2 * i] = y[i].real();
-        c->h_y[2 * i + 1] = y[i].imag();
-    }
-    PG_CUDA_TRY(cudaMemcpyAsync(c->d_y, c->h_y, sizeof(double) * 2 * kdone, cudaMemcpyHostToDevice, ctx->stream));
-    PG_TRY(pg_combine<R>(ctx, V, n, kdone, c->d_y, 1.0, out, n, 0));
-    if (st) {
-        st->Iterations = kdone;
-        st->ErrorEstimate = resid;
-    }
-    return PG_OK;
-}
-
-// scales layout for the Cayley step: slot 0 = the overlap term S (weight 1), slots >= 1 the
-// terms of H. sc_in gives the H(t+dt/2) slot values; this builds A-scales (S + f H) for a
-// complex factor f.
-static pg_scales cayley_scales(const double *scales, int nscales, zd f, zd s_weight)
-{
-    pg_scales sc;
-    for (int k = 0; k < PG_MAX_SLOTS; ++k) {
-        zd v(0.0, 0.0);
-        if (k == 0) v = s_weight;
-        else if (k < nscales) v = f * zd(scales[2 * k], scales[2 * k + 1]);
-        sc.s[k] = mk<double>(v.real(), v.imag());
-    }
-    return sc;
-}
-
-static int norm64(pg_ctx *ctx, const cxd *x, long long n, double *d_norm, double *out)
-{
-    PG_TRY(pg_multidot<double>(ctx, x, n, 0, x, n, d_norm));
-    PG_CUDA_TRY(cudaMemcpyAsync(ctx->h_pinned, d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    *out = ctx->h_pinned[1];
-    return PG_OK;
-}
-
-extern "C" int pg_cayley_step(pg_cayley *c, void *psi, double dt, const double *scales, int nscales, pg_krylov_stats *st)
-{
-    if (!c || !psi || !scales || nscales < 1 || nscales > PG_MAX_SLOTS) return PG_ERR_ARG;
-    pg_ctx *ctx = c->op64->ctx;
-    const long long n = c->n;
-    cxd *x = (cxd *)psi;
-    const zd half(0.0, dt / 2.0);
-    const pg_scales scPlus = cayley_scales(scales, nscales, half, 1.0);    // S + i dt/2 H
-    const pg_scales scMinus = cayley_scales(scales, nscales, -half, 1.0);  // S - i dt/2 H
-    const pg_scales scDiff = cayley_scales(scales, nscales, zd(0.0, -dt), 0.0);  // -i dt H
-    if (c->prec == PG_FP64) {
-        // reference scheme: b = (S - i dt/2 H) psi, rhs = M^-1 b, GMRES from x0 = 0
-        PG_TRY(pg_op_matvec_dev(c->op64, scMinus, nullptr, x, c->b64, 0, nullptr, nullptr));
-        PG_CUDA_TRY(cudaMemcpyAsync(c->d64, c->b64, sizeof(cxd) * n, cudaMemcpyDeviceToDevice, ctx->stream));
-        PG_TRY(pg_banded_apply_dev(c->prec64, PG_BAND_PREC_SOLVE, c->d64));
-        double beta0 = 0.0;
-        PG_TRY(norm64(ctx, c->d64, n, c->d_norm, &beta0));
-        if (beta0 == 0.0) return PG_OK;
-        PG_TRY((pg_scale_copy<double, double>(ctx, c->d64, (cxd *)c->V, nullptr, n, nullptr, 1.0 / beta0)));
-        PG_TRY(gmres_solve<double>(c, scPlus, beta0, c->tolerance, x, st));
-        if (st) {
-            // true residual || (S + i dt/2 H) x - b ||
-            PG_TRY(pg_op_matvec_dev(c->op64, scPlus, nullptr, x, c->r64, 0, nullptr, nullptr));
-            PG_TRY(pg_axpy(ctx, mk<double>(-1.0, 0.0), c->b64, c->r64, n));
-            PG_TRY(norm64(ctx, c->r64, n, c->d_norm, &st->TrueResidual));
-        }
-        return PG_OK;
-    }
-    // mixed precision: r = b - A psi = -i dt H psi (FP64); correction d from FP32 GMRES on
-    // M^-1 A d = M^-1 r; psi += d; r -= A d in FP64; repeat while ||M^-1 r|| > tolerance.
-    PG_TRY(pg_op_matvec_dev(c->op64, scDiff, nullptr, x, c->r64, 0, nullptr, nullptr));
-    long long iters = 0;
-    double rn = 0.0;
-    for (int pass = 0; pass < 4; ++pass) {
-        PG_CUDA_TRY(cudaMemcpyAsync(c->d64, c->r64, sizeof(cxd) * n, cudaMemcpyDeviceToDevice, ctx->stream));
-        PG_TRY(pg_banded_apply_dev(c->prec64, PG_BAND_PREC_SOLVE, c->d64));
-        PG_TRY(norm64(ctx, c->d64, n, c->d_norm, &rn));
-        if (rn <= c->tolerance || rn == 0.0) break;
-        PG_TRY((pg_scale_copy<float, double>(ctx, c->d64, (cxf *)c->V, nullptr, n, nullptr, 1.0 / rn)));
-        const double inner_tol = std::max(c->tolerance, 2e-6 * rn);
-        PG_TRY(gmres_solve<float>(c, scPlus, rn, inner_tol, c->e64, st));
-        if (st) iters += st->Iterations;
-        PG_TRY(pg_axpy(ctx, mk<double>(1.0, 0.0), c->e64, x, n));
-        PG_TRY(pg_op_matvec_dev(c->op64, scPlus, nullptr, c->e64, c->b64, 0, nullptr, nullptr));
-        PG_TRY(pg_axpy(ctx, mk<double>(-1.0, 0.0), c->b64, c->r64, n));
-    }
-    if (st) {
-        st->Iterations = iters;
-        st->ErrorEstimate = rn;
-        PG_TRY(norm64(ctx, c->r64, n, c->d_norm, &st->TrueResidual));
-    }
-    return PG_OK;
-}
-
-// ------------------------------------------------------------------------------------
 // Arnoldi expansion for pIRAM: operator S^-1 H, Euclidean inner product, CGS2
 // ------------------------------------------------------------------------------------
 extern "C" int pg_arnoldi_expand(pg_op *op64, pg_banded *ovl64, pg_banded *shift_invert, const double *scales,

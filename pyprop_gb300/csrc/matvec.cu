@@ -44,6 +44,7 @@ __global__ void ref_bandnh_kernel(int mode, const cxd *__restrict__ pot, int npa
         for (int p = 0; p < npairs; ++p) {
             if (pairs[2 * p] != r) continue;
             const int c = pairs[2 * p + 1];
+            if (c < 0 || c >= nrows) continue;  // pair lists come from device memory: never index past psi
             acc = acc + band_row(pot + (size_t)p * potStride, src + (size_t)c * N);
         }
     }

@@ -180,9 +180,12 @@ int pg_banded_apply_dev(pg_banded *b, int which, void *x);
 // ------------------------------------------------------------------------------------
 // h[j] = sum_i conj(V[j][i]) w[i] for j < J; nrm2 = sum |w|^2. Results FP64 in ctx->red_out:
 // red_out[2j], red_out[2j+1] = h[j]; red_out[2J] = ||w||^2.
+// With Jdev non-null the column count is *Jdev + 1 (read on the device; J is then the
+// host-side upper bound used for the scratch check).
 template <typename R>
-int pg_multidot(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const cx<R> *w, long long n, double *out_dev);
+int pg_multidot(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const cx<R> *w, long long n, double *out_dev,
+                const int *Jdev = nullptr);
 // w -= sum_j V[j] h[j] with h complex128 on device; then, if J2 > 0, out2 = V[0..J2)^H w and ||w||^2
 template <typename R>
 int pg_gs_update(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const double *h_dev, cx<R> *w, long long n,
-                 int want_dots, double *out_dev);
+                 int want_dots, double *out_dev, const int *Jdev = nullptr);

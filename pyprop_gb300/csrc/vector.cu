@@ -51,11 +51,12 @@ __device__ void finish_reduction(double *partial, int ncols, unsigned int *count
 {
     if (!last) return;
     __threadfence();
+    const volatile double *vp = partial;  // other CTAs' partials: read past L1
     for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
         double sx = 0.0, sy = 0.0;
         for (int blk = 0; blk < (int)gridDim.x; ++blk) {
-            sx += partial[2 * ((size_t)blk * ncols + c)];
-            sy += partial[2 * ((size_t)blk * ncols + c) + 1];
+            sx += vp[2 * ((size_t)blk * ncols + c)];
+            sy += vp[2 * ((size_t)blk * ncols + c) + 1];
         }
         out[2 * c] = sx;
         out[2 * c + 1] = sy;
@@ -83,10 +84,12 @@ __device__ __forceinline__ bool arrive_last(unsigned int *counter)
 // out[2j..2j+1] = <V_j, w> (j < J); out[2J] = ||w||^2, out[2J+1] = ||w||.
 template <typename R>
 __global__ void __launch_bounds__(RED_THREADS) multidot_kernel(const cx<R> *__restrict__ V, long long ldv, int J,
-                                                               const cx<R> *__restrict__ w, long long n,
-                                                               double *partial, unsigned int *counter, double *out)
+                                                               const int *__restrict__ Jdev, const cx<R> *__restrict__ w,
+                                                               long long n, double *partial, unsigned int *counter,
+                                                               double *out)
 {
     __shared__ R sm[64];
+    if (Jdev) J = min(*Jdev + 1, J);  // device count, bounded by the host-checked maximum
     const long long chunk = (n + gridDim.x - 1) / gridDim.x;
     const long long lo = (long long)blockIdx.x * chunk;
     const long long hi = min(n, lo + chunk);
@@ -121,11 +124,13 @@ __global__ void __launch_bounds__(RED_THREADS) multidot_kernel(const cx<R> *__re
 // ||w||^2 into out exactly as multidot_kernel.
 template <typename R>
 __global__ void __launch_bounds__(RED_THREADS) gs_update_kernel(const cx<R> *__restrict__ V, long long ldv, int J,
+                                                                const int *__restrict__ Jdev,
                                                                 const double *__restrict__ h, cx<R> *__restrict__ w,
                                                                 long long n, int want_dots, double *partial,
                                                                 unsigned int *counter, double *out)
 {
     __shared__ R sm[64];
+    if (Jdev) J = min(*Jdev + 1, J);  // device count, bounded by the host-checked maximum
     __shared__ cx<R> hs[PG_RED_COLS];
     for (int j = threadIdx.x; j < J; j += blockDim.x) hs[j] = mk<R>((R)h[2 * j], (R)h[2 * j + 1]);
     __syncthreads();
@@ -178,31 +183,35 @@ __global__ void __launch_bounds__(RED_THREADS) gs_update_kernel(const cx<R> *__r
 }
 
 template <typename R>
-int pg_multidot(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const cx<R> *w, long long n, double *out_dev)
+int pg_multidot(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const cx<R> *w, long long n, double *out_dev,
+                const int *Jdev)
 {
     if (J + 1 > ctx->red_max_cols) return PG_ERR_ARG;
     const int nb = red_blocks(ctx, n);
-    multidot_kernel<R><<<nb, RED_THREADS, 0, ctx->stream>>>(V, ldv, J, w, n, ctx->red_partial, ctx->red_counter, out_dev);
+    multidot_kernel<R><<<nb, RED_THREADS, 0, ctx->stream>>>(V, ldv, J, Jdev, w, n, ctx->red_partial, ctx->red_counter,
+                                                            out_dev);
     ctx->launches++;
     return pg_check_launch(ctx);
 }
 
 template <typename R>
 int pg_gs_update(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const double *h_dev, cx<R> *w, long long n,
-                 int want_dots, double *out_dev)
+                 int want_dots, double *out_dev, const int *Jdev)
 {
     if (J + 1 > ctx->red_max_cols) return PG_ERR_ARG;
     const int nb = red_blocks(ctx, n);
-    gs_update_kernel<R><<<nb, RED_THREADS, 0, ctx->stream>>>(V, ldv, J, h_dev, w, n, want_dots, ctx->red_partial,
+    gs_update_kernel<R><<<nb, RED_THREADS, 0, ctx->stream>>>(V, ldv, J, Jdev, h_dev, w, n, want_dots, ctx->red_partial,
                                                             ctx->red_counter, out_dev);
     ctx->launches++;
     return pg_check_launch(ctx);
 }
 
-template int pg_multidot<double>(pg_ctx *, const cxd *, long long, int, const cxd *, long long, double *);
-template int pg_multidot<float>(pg_ctx *, const cxf *, long long, int, const cxf *, long long, double *);
-template int pg_gs_update<double>(pg_ctx *, const cxd *, long long, int, const double *, cxd *, long long, int, double *);
-template int pg_gs_update<float>(pg_ctx *, const cxf *, long long, int, const double *, cxf *, long long, int, double *);
+template int pg_multidot<double>(pg_ctx *, const cxd *, long long, int, const cxd *, long long, double *, const int *);
+template int pg_multidot<float>(pg_ctx *, const cxf *, long long, int, const cxf *, long long, double *, const int *);
+template int pg_gs_update<double>(pg_ctx *, const cxd *, long long, int, const double *, cxd *, long long, int, double *,
+                                  const int *);
+template int pg_gs_update<float>(pg_ctx *, const cxf *, long long, int, const double *, cxf *, long long, int, double *,
+                                 const int *);
 
 // ------------------------------------------------------------------------------------
 // elementwise helpers
@@ -212,7 +221,11 @@ template <typename Rd, typename Rs>
 __global__ void scale_copy_kernel(const cx<Rs> *__restrict__ src, cx<Rd> *__restrict__ dst, cx<Rd> *__restrict__ dst2,
                                   long long n, const double *__restrict__ inv_scale_dev, double mul)
 {
-    const double s = inv_scale_dev ? 1.0 / inv_scale_dev[0] : mul;
+    double s = mul;
+    if (inv_scale_dev) {
+        const double b = inv_scale_dev[0];
+        s = b > 0.0 ? 1.0 / b : 0.0;  // a zero norm gives a zero vector, never inf/NaN
+    }
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const cx<Rs> a = src[i];
         const cx<Rd> v = mk<Rd>((Rd)((double)a.x * s), (Rd)((double)a.y * s));

@@ -232,9 +232,10 @@ class PampStepper:
 
 
 class CayleyStepper:
-    """pg_cayley: one Crank-Nicolson step per call (GMRES + block-diagonal preconditioner)."""
+    """pg_cayley: one Crank-Nicolson step per call (GMRES + block-diagonal preconditioner),
+    executed as one CUDA graph launch."""
 
-    def __init__(self, op64, opb, prec64, precb, basis_size, precision, tolerance):
+    def __init__(self, op64, opb, prec64, precb, basis_size, precision, tolerance, true_residual=False):
         self.lib = op64.lib
         self.ctx = op64.ctx
         self._keep = (op64, opb, prec64, precb)
@@ -242,14 +243,20 @@ class CayleyStepper:
         check(self.lib.pg_cayley_create(op64.h, opb.h, prec64.h, precb.h, basis_size, precision, float(tolerance),
                                         C.byref(h)), "pg_cayley_create")
         self.h = h
+        check(self.lib.pg_cayley_set_true_residual(h, int(bool(true_residual))), "pg_cayley_set_true_residual")
         self.stats = nat.KrylovStats()
 
-    def step(self, psi, dt, scales):
+    def step(self, psi, dt, scales, want_stats=True):
         sc = np.ascontiguousarray(scales, dtype=np.complex128)
         _, sp = nat.dptr(sc.view(np.float64))
         self.ctx.bind_stream()
-        check(self.lib.pg_cayley_step(self.h, ptr(psi), float(dt), sp, len(sc), C.byref(self.stats)),
-              "pg_cayley_step")
+        check(self.lib.pg_cayley_step(self.h, ptr(psi), float(dt), sp, len(sc),
+                                      C.byref(self.stats) if want_stats else None), "pg_cayley_step")
+        return self.stats if want_stats else None
+
+    def last_stats(self):
+        self.ctx.bind_stream()
+        check(self.lib.pg_cayley_last_stats(self.h, C.byref(self.stats)), "pg_cayley_last_stats")
         return self.stats
 
     def __del__(self):

@@ -229,6 +229,8 @@ class CayleyPropagatorGPU(PropagatorBase):
         tol = float(getattr(conf, "krylov_tolerance", 0.0) or 0.0)
         self.Tolerance = max(tol, 1e-13)  # gmres.h:223-229 floor
         self.Precision = precision_of(getattr(conf, "gpu_precision", "fp64"))
+        self.StepStats = bool(getattr(conf, "gpu_step_stats", True))
+        self.TrueResidual = bool(getattr(conf, "gpu_true_residual", False))
         name = getattr(conf, "preconditioner", None)
         self.Preconditioner = None
         if name:
@@ -252,13 +254,29 @@ class CayleyPropagatorGPU(PropagatorBase):
         self.opb = bp.device_operator(self.Precision, with_overlap=True)
         self.stepper = CayleyStepper(self.op64, self.opb, self.Preconditioner.solvers[nat.PG_FP64],
                                      self.Preconditioner.solvers[self.Precision], self.BasisSize, self.Precision,
-                                     self.Tolerance)
+                                     self.Tolerance, self.TrueResidual)
 
     def AdvanceStep(self, t, dt):
+        """One step at H(t + |dt|/2). With ``gpu_step_stats`` (default) the call waits for the
+        step and warns when the GMRES estimate exceeds 1e-4 (CayleyPropagator.py:103-111);
+        otherwise it only enqueues and ``GetErrorEstimate`` waits."""
         scales = self.op64.scales(t + abs(dt / 2.0))
-        self.LastStats = st = self.stepper.step(self.psi.GetData(), dt, scales)
-        if st.ErrorEstimate > 1e-4:
-            _log.warning("GMRES error estimate %g", st.ErrorEstimate)
+        self._last_stats = None
+        st = self.stepper.step(self.psi.GetData(), dt, scales, want_stats=self.StepStats)
+        if st is not None:
+            self.LastStats = st
+            if st.ErrorEstimate > 1e-4:
+                _log.warning("GMRES error estimate %g", st.ErrorEstimate)
+
+    @property
+    def LastStats(self):
+        if getattr(self, "_last_stats", None) is None:
+            self._last_stats = self.stepper.last_stats()
+        return self._last_stats
+
+    @LastStats.setter
+    def LastStats(self, value):
+        self._last_stats = value
 
     def MultiplyHamiltonian(self, srcPsi, destPsi, t, dt):
         self.BasePropagator.MultiplyHamiltonian(srcPsi, destPsi, t, dt)

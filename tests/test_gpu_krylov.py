@@ -56,13 +56,20 @@ def test_pamp_steps_against_oracle_fp64_and_fp32(gpu):
 def test_cayley_step_fp64_matches_golden(gpu):
     g = golden("hydrogen_small.npz")
     prob = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp64", gmres_tolerance=1e-13)
+    prob.Propagator.TrueResidual = True
     prob.SetupStep(skipWavefunctionSetup=True)
     _set_psi(prob, g["psi"])
     prob.Propagator.AdvanceStep(float(g["t"]), float(g["dt"]))
     out = prob.psi.numpy()
     assert relerr(out, g["cayley"]) < 1e-11
     st = prob.Propagator.LastStats
-    assert st.TrueResidual < 1e-10 and 1 <= st.Iterations <= 20
+    assert 0 <= st.TrueResidual < 1e-10 and 1 <= st.Iterations <= 20
+    # the same step enqueued without waiting gives the same state (graph replay)
+    prob.Propagator.StepStats = False
+    _set_psi(prob, g["psi"])
+    prob.Propagator.AdvanceStep(float(g["t"]), float(g["dt"]))
+    assert relerr(prob.psi.numpy(), out) < 1e-15
+    assert prob.Propagator.LastStats.Iterations == st.Iterations
 
 
 def test_cayley_mixed_precision_against_oracle(gpu):
@@ -114,8 +121,12 @@ def test_piram_plain_mode_small_operator(gpu):
     op = lambda v: ham.overlap.solve(ham.apply_H(v.reshape(1, -1), 0.0)).ravel()
     start = np.random.default_rng(1234).uniform(0.0, 1.0, 30).astype(complex)
     vals, vecs, rs, conv = piram_solve(op, start, 29, 2, 1e-12, 5)
-    assert np.max(np.abs(solver.GetEigenvalues() - vals.real)) < 1e-9
-    assert abs(solver.GetEigenvalues()[0] + 0.5) < 1e-6
+    ev = solver.GetEigenvalues()
+    # the lowest Ritz value is converged in both; the second is not yet, so the two runs
+    # (CGS2 on the GPU, DGKS in the oracle) agree only to the Ritz error bound
+    assert abs(ev[0] - vals[0].real) < 1e-9
+    assert abs(ev[1] - vals[1].real) < 1e-3
+    assert abs(ev[0] + 0.5) < 1e-6
 
 
 def test_problem_energy_and_norm(gpu):
