@@ -249,6 +249,29 @@ int pg_vec_convert(pg_ctx *ctx, int src_precision, const void *x, int dst_precis
 /* V (complex128 [k][n]) <- V (complex128 [m][n]) * Q (host complex128 [m][k], row major) */
 int pg_vec_combine(pg_ctx *ctx, void *V, long long n, int m, const double *Q, int k);
 
+/* ---------------------------------------------------------------------------------- */
+/* allocation-free entry point                                                        */
+/* ---------------------------------------------------------------------------------- */
+/*
+ * pg_vec_multidot_noalloc: the block inner product of the Krylov Gram-Schmidt step,
+ *     out[2j], out[2j+1] = sum_i conj(V[j][i]) w[i]   (j < J, complex128 result)
+ *     out[2J] = ||w||^2, out[2J+1] = ||w||
+ * for complex128 (PG_FP64) or complex64 (PG_FP32) device vectors, written to the caller's
+ * device buffer `out` (2J+2 doubles), on `stream` (NULL = legacy default stream). No
+ * counterpart in the reference: it serves callers that must not allocate device memory -
+ * code recorded into a CUDA graph under global stream capture (where cudaMalloc is not
+ * permitted), and hosts that give the library a fixed memory budget at start-up. It needs no
+ * pg_ctx and calls no cudaMalloc, cudaFree or allocating library routine: its scratch
+ * (per-CTA partial sums and the arrival ticket) is a static device array of about 320 KB that
+ * every GPU loading the library keeps until the process exits, so J is limited to 64 vectors
+ * (PG_ERR_ARG above that). The first call on a device looks up the array's address on that
+ * device (cudaGetSymbolAddress); make that first call before any stream capture. All calls
+ * share the one array: calls that overlap on the GPU (two streams, two threads) race and give
+ * wrong sums - serialize them.
+ */
+int pg_vec_multidot_noalloc(int precision, const void *V, long long ldv, int J, const void *w,
+                            long long n, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,6 +89,7 @@ _SIGS = {
     "pg_vec_dot": (_I, [_P, _I, _P, _P, _LL, _DP]),
     "pg_vec_convert": (_I, [_P, _I, _P, _I, _P, _LL]),
     "pg_vec_combine": (_I, [_P, _P, _LL, _I, _DP, _I]),
+    "pg_vec_multidot_noalloc": (_I, [_I, _P, _LL, _I, _P, _LL, _P, _P]),
 }
 
 _lib = None

@@ -9,6 +9,7 @@
 #include "pg_internal.cuh"
 
 #include <algorithm>
+#include <mutex>
 
 static const int RED_THREADS = 256;
 static const int RED_ELEMS = 4;  // elements per thread per chunk pass
@@ -353,5 +354,75 @@ extern "C" int pg_vec_combine(pg_ctx *ctx, void *V, long long n, int m, const do
     PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     cudaFree(tmp);
     cudaFree(dQ);
+    return PG_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// allocation-free block inner product
+// ------------------------------------------------------------------------------------
+// Same multidot kernel, but its per-CTA partials, arrival ticket and nothing else live in
+// file-scope device arrays instead of memory from cudaMalloc. Every GPU that loads this
+// library holds these ~320 KB until the process exits. Host code cannot use the arrays'
+// names as device addresses, so their addresses are looked up once per device with
+// cudaGetSymbolAddress (on the first call on that device) and passed to the kernel.
+static const int NOALLOC_MAX_VECTORS = 64;
+static const int NOALLOC_BLOCKS = PG_RED_BLOCKS;
+static const int NOALLOC_MAX_DEVICES = 64;
+
+static __device__ __align__(256) double g_noalloc_partial[2 * NOALLOC_BLOCKS * (NOALLOC_MAX_VECTORS + 1)];
+static __device__ __align__(256) unsigned int g_noalloc_ticket[64];
+
+namespace {
+struct NoallocDevice {
+    bool ready = false;
+    double *partial = nullptr;
+    unsigned int *ticket = nullptr;
+    int max_blocks = 1;
+};
+NoallocDevice g_noalloc_dev[NOALLOC_MAX_DEVICES];
+std::mutex g_noalloc_mutex;
+}  // namespace
+
+// First call on a device: resolve the scratch addresses with that device current.
+static int noalloc_setup(int device, NoallocDevice **out)
+{
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    NoallocDevice &d = g_noalloc_dev[device];
+    if (!d.ready) {
+        PG_CUDA_TRY(cudaGetSymbolAddress((void **)&d.partial, g_noalloc_partial));
+        PG_CUDA_TRY(cudaGetSymbolAddress((void **)&d.ticket, g_noalloc_ticket));
+        int sms = 0;
+        PG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        d.max_blocks = std::max(1, std::min(NOALLOC_BLOCKS, 2 * std::max(1, sms)));
+        d.ready = true;
+    }
+    *out = &d;
+    return PG_OK;
+}
+
+extern "C" int pg_vec_multidot_noalloc(int precision, const void *V, long long ldv, int J, const void *w, long long n,
+                                       double *out, void *stream)
+{
+    if (!w || !out || n < 0 || J < 0 || (J > 0 && !V)) return PG_ERR_ARG;
+    if (J > NOALLOC_MAX_VECTORS) return PG_ERR_ARG;  // more columns than the static scratch holds
+    if (J > 1 && ldv < n) return PG_ERR_ARG;
+    if (precision != PG_FP64 && precision != PG_FP32) return PG_ERR_ARG;
+    int device = 0;
+    PG_CUDA_TRY(cudaGetDevice(&device));
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES) return PG_ERR_ARG;
+    NoallocDevice *d = nullptr;
+    PG_TRY(noalloc_setup(device, &d));
+    cudaStream_t s = (cudaStream_t)stream;
+    // the ticket must start at zero; the last CTA leaves it at zero, this clears any leftover
+    PG_CUDA_TRY(cudaMemsetAsync(d->ticket, 0, sizeof(unsigned int), s));
+    const long long per = (long long)RED_THREADS * RED_ELEMS;
+    const int nb = (int)std::max<long long>(1, std::min<long long>((n + per - 1) / per, d->max_blocks));
+    if (precision == PG_FP64)
+        multidot_kernel<double><<<nb, RED_THREADS, 0, s>>>((const cxd *)V, ldv, J, nullptr, (const cxd *)w, n,
+                                                           d->partial, d->ticket, out);
+    else
+        multidot_kernel<float><<<nb, RED_THREADS, 0, s>>>((const cxf *)V, ldv, J, nullptr, (const cxf *)w, n,
+                                                          d->partial, d->ticket, out);
+    PG_CUDA_TRY(cudaGetLastError());
     return PG_OK;
 }
