@@ -60,6 +60,9 @@ int pg_ctx_use_own_stream(pg_ctx *ctx);
 /* Count of kernels this context launched since creation (own kernels only). */
 long long pg_ctx_kernel_launches(pg_ctx *ctx);
 int pg_ctx_synchronize(pg_ctx *ctx);
+/* Device error word: non-zero when a kernel's bounded wait on an asynchronous copy ran out
+ * (the kernel then skipped its work). Waits for the context's stream. */
+int pg_ctx_device_error(pg_ctx *ctx, int *flag);
 
 /* ---------------------------------------------------------------------------------- */
 /* reference-layout tensor multiply                                                   */

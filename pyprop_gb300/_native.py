@@ -62,6 +62,7 @@ _SIGS = {
     "pg_ctx_use_own_stream": (_I, [_P]),
     "pg_ctx_kernel_launches": (_LL, [_P]),
     "pg_ctx_synchronize": (_I, [_P]),
+    "pg_ctx_device_error": (_I, [_P, _IP]),
     "pg_tensor_multiply_diag_bandnh": (_I, [_P, _I, _I, _D, _P, _I, _I, _P, _I, _I, _I, _P]),
     "pg_tensor_multiply_simp_bandnh": (_I, [_P, _I, _I, _D, _P, _I, _I, _P, _I, _I, _P, _I, _I, _I, _P]),
     "pg_tensor_multiply_ident_bandnh": (_I, [_P, _I, _I, _D, _P, _I, _I, _P, _I, _I, _I, _P]),

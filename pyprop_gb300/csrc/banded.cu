@@ -44,47 +44,81 @@ template <typename R> __device__ __forceinline__ void coef_fms(cx<R> &acc, R c, 
 }
 template <typename R> __device__ __forceinline__ void coef_fms(cx<R> &acc, cx<R> c, cx<R> v) { cfma(acc, mk<R>(-c.x, -c.y), v); }
 
+// Asynchronous 16-byte global->shared copies (cp.async, completion by group wait).
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// One warp (one CTA) per fibre. Per 32-row block the inverse diagonal block and the
+// coupling rows are copied to shared memory with cp.async one block ahead (double
+// buffer), so the solve reads only shared memory. Four accumulators shorten the FMA chain.
 // C: coefficient type (R or cx<R>). inv: [nmat][nblk][32 s][32 t], cpl: [nmat][nblk][w][32 t]
 template <typename R, typename C, bool LOWER>
-__global__ void __launch_bounds__(128) tri_solve_kernel(int N, int nblk, int w, const C *__restrict__ inv,
-                                                        const C *__restrict__ cpl, int per_fibre_matrix,
-                                                        cx<R> *__restrict__ x, int nfib)
+__global__ void __launch_bounds__(32) tri_solve_kernel(int N, int nblk, int w, const C *__restrict__ inv,
+                                                       const C *__restrict__ cpl, int per_fibre_matrix,
+                                                       cx<R> *__restrict__ x, int nfib)
 {
-    const int lane = threadIdx.x & 31;
-    const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (f >= nfib) return;  // whole warp exits together
+    extern __shared__ __align__(16) unsigned char tri_smem[];
+    const int lane = threadIdx.x;
+    const int f = blockIdx.x;
+    if (f >= nfib) return;
+    const int per_blk = 1024 + w * 32;  // coefficients staged per block
+    C *buf = (C *)tri_smem;
     const size_t m = per_fibre_matrix ? (size_t)f : 0;
     cx<R> *xf = x + (size_t)f * N;
-    const C *invm = inv + m * (size_t)nblk * 32 * 32;
+    const C *invm = inv + m * (size_t)nblk * 1024;
     const C *cplm = cpl + m * (size_t)nblk * w * 32;
+    const int chunks_inv = (int)(1024 * sizeof(C) / 16);
+    const int chunks_cpl = (int)(w * 32 * sizeof(C) / 16);
+    auto prefetch = [&](int step) {
+        const int blk = LOWER ? step : (nblk - 1 - step);
+        C *dst = buf + (size_t)(step & 1) * per_blk;
+        const unsigned char *gi = (const unsigned char *)(invm + (size_t)blk * 1024);
+        const unsigned char *gc = (const unsigned char *)(cplm + (size_t)blk * w * 32);
+        unsigned char *si = (unsigned char *)dst;
+        unsigned char *sc = (unsigned char *)(dst + 1024);
+        for (int c = lane; c < chunks_inv; c += 32) cp_async16(si + 16 * c, gi + 16 * c);
+        for (int c = lane; c < chunks_cpl; c += 32) cp_async16(sc + 16 * c, gc + 16 * c);
+        cp_async_commit();
+    };
+    prefetch(0);
     cx<R> yprev = mk<R>((R)0, (R)0);
     for (int step = 0; step < nblk; ++step) {
+        if (step + 1 < nblk) {
+            prefetch(step + 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncwarp();
+        const C *ib = buf + (size_t)(step & 1) * per_blk;
+        const C *cb = ib + 1024;
         const int blk = LOWER ? step : (nblk - 1 - step);
         const int row = blk * 32 + lane;
         cx<R> r = (row < N) ? xf[row] : mk<R>((R)0, (R)0);
         if (step > 0) {
-            const C *cb = cplm + (size_t)blk * w * 32;
             for (int j = 1; j <= w; ++j) {
                 // LOWER: row couples to row-j in the previous block when lane < j
                 // UPPER: row couples to row+j in the next block when lane >= 32-j
                 const int src_lane = LOWER ? (32 - j + lane) & 31 : (lane + j - 32) & 31;
                 const cx<R> yp = shfl_cx(yprev, src_lane);
                 const bool use = LOWER ? (lane < j) : (lane >= 32 - j);
-                if (use) coef_fms(r, cb[(size_t)(j - 1) * 32 + lane], yp);
+                if (use) coef_fms(r, cb[(j - 1) * 32 + lane], yp);
             }
         }
-        const C *ib = invm + (size_t)blk * 32 * 32;
-        cx<R> y0 = mk<R>((R)0, (R)0), y1 = mk<R>((R)0, (R)0);
+        cx<R> acc[4];
 #pragma unroll
-        for (int s = 0; s < 32; s += 2) {
-            const cx<R> rs0 = shfl_cx(r, s);
-            const cx<R> rs1 = shfl_cx(r, s + 1);
-            coef_fma(y0, ib[(size_t)s * 32 + lane], rs0);
-            coef_fma(y1, ib[(size_t)(s + 1) * 32 + lane], rs1);
-        }
-        const cx<R> y = y0 + y1;
+        for (int a = 0; a < 4; ++a) acc[a] = mk<R>((R)0, (R)0);
+#pragma unroll
+        for (int s = 0; s < 32; ++s) coef_fma(acc[s & 3], ib[s * 32 + lane], shfl_cx(r, s));
+        const cx<R> y = (acc[0] + acc[1]) + (acc[2] + acc[3]);
         if (row < N) xf[row] = y;
         yprev = y;
+        __syncwarp();  // the buffer is refilled by the next prefetch
     }
 }
 
@@ -384,13 +418,13 @@ static int launch_tri(pg_banded *b, bool lower, void *x)
     pg_ctx *ctx = b->op->ctx;
     const int N = b->N, nblk = (N + 31) / 32, w = b->kb;
     const int nfib = b->op->nrows;
-    const int warps = 4;
-    dim3 grid((nfib + warps - 1) / warps);
+    if (w > 32 || (w * 32 * sizeof(C)) % 16 != 0) return PG_ERR_ARG;
+    const size_t smem = 2 * (size_t)(1024 + w * 32) * sizeof(C);
     if (lower)
-        tri_solve_kernel<R, C, true><<<grid, 32 * warps, 0, ctx->stream>>>(
+        tri_solve_kernel<R, C, true><<<nfib, 32, smem, ctx->stream>>>(
             N, nblk, w, (const C *)b->d_lo_inv, (const C *)b->d_lo_cpl, b->nmat > 1, (cx<R> *)x, nfib);
     else
-        tri_solve_kernel<R, C, false><<<grid, 32 * warps, 0, ctx->stream>>>(
+        tri_solve_kernel<R, C, false><<<nfib, 32, smem, ctx->stream>>>(
             N, nblk, w, (const C *)b->d_up_inv, (const C *)b->d_up_cpl, b->nmat > 1, (cx<R> *)x, nfib);
     ctx->launches++;
     return pg_check_launch(ctx);

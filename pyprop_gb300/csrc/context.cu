@@ -82,6 +82,8 @@ int pg_ctx_ensure_reduction(pg_ctx *ctx)
     PG_CUDA_TRY(cudaMemset(ctx->red_counter, 0, sizeof(unsigned int) * 64));
     PG_CUDA_TRY(cudaMalloc(&ctx->red_out, sizeof(double) * 2 * PG_RED_COLS));
     PG_CUDA_TRY(cudaMallocHost(&ctx->h_pinned, sizeof(double) * 2 * PG_RED_COLS));
+    PG_CUDA_TRY(cudaMalloc(&ctx->d_err, sizeof(int) * 4));
+    PG_CUDA_TRY(cudaMemset(ctx->d_err, 0, sizeof(int) * 4));
     return PG_OK;
 }
 
@@ -92,6 +94,7 @@ extern "C" int pg_ctx_destroy(pg_ctx *ctx)
     cudaFree(ctx->red_partial);
     cudaFree(ctx->red_counter);
     cudaFree(ctx->red_out);
+    cudaFree(ctx->d_err);
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
@@ -117,6 +120,15 @@ extern "C" int pg_ctx_use_own_stream(pg_ctx *ctx)
 }
 
 extern "C" long long pg_ctx_kernel_launches(pg_ctx *ctx) { return ctx ? ctx->launches : -1; }
+
+extern "C" int pg_ctx_device_error(pg_ctx *ctx, int *flag)
+{
+    if (!ctx || !flag) return PG_ERR_ARG;
+    PG_CUDA_TRY(cudaMemcpyAsync(ctx->h_pinned, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    *flag = *(int *)ctx->h_pinned;
+    return PG_OK;
+}
 
 extern "C" int pg_ctx_synchronize(pg_ctx *ctx)
 {

@@ -128,19 +128,19 @@ __global__ void __launch_bounds__(128) op_matvec_kernel(OpDev op, pg_scales scal
     const int e_begin = op.row_ptr[r], e_end = op.row_ptr[r + 1];
     for (int e = e_begin; e < e_end; ++e) {
         const int col = op.ent_col[e];
-        const cx<R> *__restrict__ V = bands + (size_t)op.ent_band[e] * b * N;
+        const cx<R> *__restrict__ V = bands + (size_t)op.ent_band[e] * b * op.ld;
         const cx<R> *__restrict__ x = src + (size_t)col * N;
         cx<R> t = mk<R>((R)0, (R)0);
         if (KB >= 0) {
 #pragma unroll
             for (int d = 0; d < 2 * KB + 1; ++d) {
                 const int j = i + d - KB;
-                if (j >= 0 && j < N) cfma(t, V[(size_t)d * N + i], x[j]);
+                if (j >= 0 && j < N) cfma(t, V[(size_t)d * op.ld + i], x[j]);
             }
         } else {
             for (int d = 0; d < b; ++d) {
                 const int j = i + d - kb;
-                if (j >= 0 && j < N) cfma(t, V[(size_t)d * N + i], x[j]);
+                if (j >= 0 && j < N) cfma(t, V[(size_t)d * op.ld + i], x[j]);
             }
         }
         const int slot = op.ent_slot[e];
@@ -154,6 +154,146 @@ __global__ void __launch_bounds__(128) op_matvec_kernel(OpDev op, pg_scales scal
     }
     if (accumulate) acc = acc + dst[o];
     dst[o] = acc;
+}
+
+// ------------------------------------------------------------------------------------
+// fused operator, bulk-copy staged variant
+// ------------------------------------------------------------------------------------
+// One CTA = BT radial rows of one angular row. Thread 0 issues one cp.async.bulk per
+// (entry, diagonal) band slab [d][i0 .. i0+BT) into shared memory, all completing on one
+// mbarrier (expected bytes), while all threads load the source slabs x[col][i0-kb .. i0+BT+kb)
+// with ordinary coalesced loads. The whole CTA's operator tile is in flight at once, so the
+// kernel is bound by HBM rather than by load latency. Entries of a row are processed in
+// groups of BMAXE. Requires band leading dimension ld (>= N) with 16-byte aligned slabs.
+static const int BT = 64;
+static const int BMAXE = 4;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// bounded wait: gives up after `limit` polls and reports through *err
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, int *err)
+{
+    for (long long it = 0; it < (1LL << 26); ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    if (err) atomicExch(err, 1);
+    return false;
+}
+
+template <typename R, int KB>
+__global__ void __launch_bounds__(BT) op_matvec_bulk_kernel(OpDev op, pg_scales scales, const cxd *__restrict__ scales_dev,
+                                                            const cx<R> *__restrict__ src, cx<R> *__restrict__ dst,
+                                                            int accumulate, int *err)
+{
+    constexpr int B = 2 * KB + 1;
+    extern __shared__ __align__(128) unsigned char mv_smem[];
+    unsigned long long *bar = (unsigned long long *)mv_smem;
+    cx<R> *bs = (cx<R> *)(mv_smem + 128);            // [BMAXE][B][BT]
+    cx<R> *xs = bs + (size_t)BMAXE * B * BT;          // [BMAXE][BT + 2KB]
+    const int r = blockIdx.y;
+    const int i0 = blockIdx.x * BT;
+    const int t = threadIdx.x;
+    const int N = op.N;
+    const int ld = op.ld;
+    const int cnt = min(BT, N - i0);
+    const unsigned slab_bytes = (unsigned)(((size_t)cnt * sizeof(cx<R>) + 15) & ~(size_t)15);
+    const cx<R> *bands = (const cx<R> *)op.bands;
+    if (t == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    cx<R> acc = mk<R>((R)0, (R)0);
+    const int e_begin = op.row_ptr[r], e_end = op.row_ptr[r + 1];
+    unsigned phase = 0;
+    for (int e0 = e_begin; e0 < e_end; e0 += BMAXE) {
+        const int ne = min(BMAXE, e_end - e0);
+        if (t == 0) {
+            mbar_arrive_expect_tx(bar, slab_bytes * (unsigned)(ne * B));
+            for (int q = 0; q < ne; ++q) {
+                const cx<R> *V = bands + (size_t)op.ent_band[e0 + q] * B * ld + i0;
+                for (int d = 0; d < B; ++d)
+                    bulk_g2s(bs + ((size_t)q * B + d) * BT, V + (size_t)d * ld, slab_bytes, bar);
+            }
+        }
+        for (int q = 0; q < ne; ++q) {
+            const cx<R> *x = src + (size_t)op.ent_col[e0 + q] * N;
+            for (int u = t; u < BT + 2 * KB; u += BT) {
+                const int j = i0 - KB + u;
+                xs[q * (BT + 2 * KB) + u] = (j >= 0 && j < N) ? x[j] : mk<R>((R)0, (R)0);
+            }
+        }
+        __syncthreads();
+        const bool ok = mbar_wait_bounded(bar, phase, err);
+        // CTA-uniform decision: a thread whose wait ran out waits once more (bounded) for the
+        // copies still in flight, then the whole CTA leaves without computing
+        if (__syncthreads_or(ok ? 0 : 1)) {
+            if (!ok) mbar_wait_bounded(bar, phase, err);
+            return;
+        }
+        phase ^= 1u;
+        if (t < cnt) {
+            for (int q = 0; q < ne; ++q) {
+                const cx<R> *Vb = bs + (size_t)q * B * BT;
+                const cx<R> *xb = xs + q * (BT + 2 * KB) + t;
+                cx<R> tq = mk<R>((R)0, (R)0);
+#pragma unroll
+                for (int d = 0; d < B; ++d) cfma(tq, Vb[d * BT + t], xb[d]);
+                const int slot = op.ent_slot[e0 + q];
+                const cx<R> sc = scales_dev ? cvt<R>(scales_dev[slot]) : cvt<R>(scales.s[slot]);
+                cfma(acc, sc, tq);
+            }
+        }
+        __syncthreads();  // shared slabs are refilled by the next group
+    }
+    if (t < cnt) {
+        const size_t o = (size_t)r * N + i0 + t;
+        if (accumulate) acc = acc + dst[o];
+        dst[o] = acc;
+    }
+}
+
+template <typename R, int KB>
+static int launch_bulk(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
+                       int accumulate)
+{
+    constexpr int B = 2 * KB + 1;
+    const size_t smem = 128 + sizeof(cx<R>) * ((size_t)BMAXE * B * BT + (size_t)BMAXE * (BT + 2 * KB));
+    static bool configured[2] = {false, false};
+    const int which = sizeof(R) == 8 ? 1 : 0;
+    if (!configured[which]) {
+        PG_CUDA_TRY(cudaFuncSetAttribute(op_matvec_bulk_kernel<R, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+        configured[which] = true;
+    }
+    dim3 grid((op->N + BT - 1) / BT, op->nrows);
+    op_matvec_bulk_kernel<R, KB><<<grid, BT, smem, op->ctx->stream>>>(op->dev(), scales, scales_dev, (const cx<R> *)src,
+                                                                       (cx<R> *)dst, accumulate, op->ctx->d_err);
+    op->ctx->launches++;
+    return pg_check_launch(op->ctx);
 }
 
 template <typename R>
@@ -181,6 +321,10 @@ int pg_op_matvec_dev(pg_op *op, const pg_scales &scales, const cxd *scales_dev, 
                      int accumulate, const double *src_inv_scale_dev, void *src_copy_out)
 {
     if (!op || !op->finalized) return PG_ERR_STATE;
+    if (op->kb == 6 && !src_inv_scale_dev && !src_copy_out && op->use_bulk) {
+        if (op->precision == PG_FP64) return launch_bulk<double, 6>(op, scales, scales_dev, src, dst, accumulate);
+        return launch_bulk<float, 6>(op, scales, scales_dev, src, dst, accumulate);
+    }
     if (op->precision == PG_FP64)
         return launch_op_matvec<double>(op, scales, scales_dev, src, dst, accumulate, src_inv_scale_dev, src_copy_out);
     return launch_op_matvec<float>(op, scales, scales_dev, src, dst, accumulate, src_inv_scale_dev, src_copy_out);
@@ -199,6 +343,8 @@ extern "C" int pg_op_create(pg_ctx *ctx, int rank, const int *shape, int bandCou
     op->N = shape[1];
     op->kb = bandCount;
     op->b = 2 * bandCount + 1;
+    op->ld = (op->N + 3) & ~3;
+    op->use_bulk = 1;
     op->precision = precision;
     *out = op;
     return PG_OK;
@@ -247,9 +393,15 @@ extern "C" int pg_op_add_term(pg_op *op, const char *storage, const double *pote
 template <typename R>
 static int upload_bands(pg_op *op)
 {
-    const size_t n = op->h_bands.size();
-    std::vector<cx<R>> tmp(n);
-    for (size_t k = 0; k < n; ++k) tmp[k] = mk<R>((R)op->h_bands[k].real(), (R)op->h_bands[k].imag());
+    // device rows of length ld (>= N, multiple of 4): every slab starts 16-byte aligned
+    const size_t rows = op->h_bands.size() / (size_t)op->N;
+    const size_t n = rows * (size_t)op->ld;
+    std::vector<cx<R>> tmp(n, mk<R>((R)0, (R)0));
+    for (size_t q = 0; q < rows; ++q)
+        for (int i = 0; i < op->N; ++i) {
+            const std::complex<double> v = op->h_bands[q * op->N + i];
+            tmp[q * op->ld + i] = mk<R>((R)v.real(), (R)v.imag());
+        }
     PG_CUDA_TRY(cudaMalloc(&op->d_bands, std::max<size_t>(1, n) * sizeof(cx<R>)));
     PG_CUDA_TRY(cudaMemcpy(op->d_bands, tmp.data(), n * sizeof(cx<R>), cudaMemcpyHostToDevice));
     return PG_OK;

@@ -63,6 +63,7 @@ struct pg_ctx {
     double *h_pinned = nullptr;      // pinned host mirror of red_out
     int red_max_blocks = 0;
     int red_max_cols = 0;
+    int *d_err = nullptr;            // set to non-zero by a kernel whose bounded wait ran out
 };
 
 #define PG_CUDA_TRY(...)                                                                     \
@@ -100,6 +101,7 @@ struct pg_scales {
 struct OpDev {
     int nrows;        // angular rows (Nang)
     int N;            // radial length
+    int ld;           // band row length on the device (N rounded up to a multiple of 4)
     int kb;           // super diagonals
     int b;            // 2kb+1
     const int *row_ptr;
@@ -129,9 +131,11 @@ struct pg_op {
     void *d_bands = nullptr;
     int nbands = 0;
     long long nentries = 0;
+    int ld = 0;
+    int use_bulk = 1;
     OpDev dev() const {
         OpDev o;
-        o.nrows = nrows; o.N = N; o.kb = kb; o.b = b;
+        o.nrows = nrows; o.N = N; o.ld = ld; o.kb = kb; o.b = b;
         o.row_ptr = d_row_ptr; o.ent_col = d_ent_col; o.ent_band = d_ent_band; o.ent_slot = d_ent_slot;
         o.bands = d_bands;
         return o;
