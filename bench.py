@@ -242,6 +242,7 @@ def run_ours(args):
         with open(tpath) as fh:
             traffic = json.load(fh).get("bytes_per_launch")
 
+    ens = run_ensemble(args, torch, flush) if args.ensemble > 0 else None
     cpu = cpu_baseline_sample() if (rank == 0 and world == 1 and not args.no_cpu) else None
     if rank == 0:
         steps_per_s = world * args.steps / t_mixed
@@ -265,6 +266,7 @@ def run_ours(args):
                          "note": "working set (%.1f MB) is L2 resident between launches only without the flush" %
                                  (bytes_mv / 1e6)},
             "cpu_baseline": cpu,
+            "ensemble": ens,
             "clocks": clk.summary(),
             "gpu_launches": launches,
             "ground_energy": e0,
@@ -272,6 +274,77 @@ def run_ours(args):
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
+
+
+def run_ensemble(args, torch, flush):
+    """Batched ensemble: member-steps/s of one graph launch per ensemble step (mixed
+    precision), against the same members stepped one at a time on the plain FP64 path."""
+    import pyprop_gb300 as pp
+    from pyprop_gb300.ensemble import CayleyEnsembleGPU, hydrogen_ensemble_params
+    from pyprop_gb300.workloads import hydrogen
+    t_setup = time.perf_counter()
+    params = hydrogen_ensemble_params(args.ensemble)
+
+    def member(prm, precision):
+        p = pp.Problem(pp.LoadString(hydrogen(propagator="CayleyPropagatorGPU", precision=precision, rmax=100.0,
+                                              timestep=0.01, pulse_duration=10.0, duration=10.0,
+                                              krylov_basis_size=20, gmres_tolerance=1e-12, **prm)))
+        p.Propagator.StepStats = False
+        p.SetupStep(skipWavefunctionSetup=True)
+        psi, _ = initial_state(p)
+        p.psi.SetData(psi)
+        return p, psi
+
+    members = [member(prm, "fp32") for prm in params]
+    probs = [m[0] for m in members]
+    ens = CayleyEnsembleGPU(probs)
+    setup_s = time.perf_counter() - t_setup
+    for _ in range(args.warmup):
+        ens.AdvanceStep()
+    torch.cuda.synchronize()
+    K = max(1, min(args.steps, 20))
+    table = ens.scale_table(K)
+    stream = torch.cuda.current_stream()
+    total = 0.0
+    iters = 0
+    for k in range(K):
+        flush.fill_(1.0)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        ens.AdvanceStep(table[k])
+        e.record(stream)
+        e.synchronize()
+        total += s.elapsed_time(e) * 1e-3
+        iters += sum(st["Iterations"] for st in ens.Stats())
+    member_steps = K * len(probs)
+    # plain FP64 path on a sample of the same members, one member step at a time
+    sample = list(range(0, len(params), max(1, len(params) // 16)))[:16]
+    t64 = 0.0
+    n64 = 0
+    for i in sample:
+        p64, psi = member(params[i], "fp64")
+        for _ in range(3):
+            p64.AdvanceStep()
+        torch.cuda.synchronize()
+        for _ in range(5):
+            flush.fill_(1.0)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            p64.AdvanceStep()
+            e.record(stream)
+            e.synchronize()
+            t64 += s.elapsed_time(e) * 1e-3
+            n64 += 1
+        del p64
+    fp64_rate = n64 / t64
+    rate = member_steps / total
+    return {"members": len(probs), "member_steps_per_s": rate, "ms_per_ensemble_step": 1e3 * total / K,
+            "gmres_iterations_per_member_step": iters / member_steps,
+            "plain_fp64_single_member_steps_per_s": fp64_rate, "speedup_vs_plain_fp64": rate / fp64_rate,
+            "workload": "%d hydrogen members, lmax U{8..32}, N U{100..400} on r in [0,100], E0 U[0.01,0.1], "
+                        "lambda U[400,1600] nm (rng seed 20261203), Cayley mixed precision, one graph launch per "
+                        "ensemble step, L2 flushed between steps" % len(probs),
+            "setup_s": setup_s}
 
 
 # ---------------------------------------------------------------------------------------
@@ -344,6 +417,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ensemble", type=int, default=256, help="members of the batched leg (0 = skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -204,7 +204,7 @@ typedef struct pg_cayley pg_cayley;
  * last kernel applies the Givens rotations and sets the loop condition on the device.
  * basis_precision PG_FP64: the reference scheme (x0 = 0) in complex128. PG_FP32: the FP64
  * residual r = b - A psi, a complex64 GMRES for the correction (2e-6 relative), psi += d,
- * r -= A d in FP64, repeated while ||M^-1 r|| > tolerance (at most 4 passes).
+ * r -= A d in FP64, repeated while the true residual ||r|| > tolerance (at most 4 passes).
  * op64/op_basis must contain the overlap as slot 0 (Ident_BandNH term) and the terms of H
  * in slots >= 1. tolerance is floored at 1e-13 (gmres.h:223-229). basis_size <= 64.
  */
@@ -224,6 +224,19 @@ int pg_cayley_advance(pg_cayley *c, void *psi, double dt, int nsteps, const doub
 int pg_cayley_last_stats(pg_cayley *c, pg_krylov_stats *stats);
 /* FP64 mode: also compute ||(S + i dt/2 H) psi' - b|| every step (one extra matvec). */
 int pg_cayley_set_true_residual(pg_cayley *c, int on);
+
+/* Ensembles: many pg_cayley members (each with its own operator, basis size, field) advanced
+ * together by one CUDA graph launch whose branches (one per member) run concurrently. The
+ * members keep their own buffers; the batch owns the graph. While a batch exists, stepping a
+ * member alone rebuilds that member's graph. */
+typedef struct pg_cayley_batch pg_cayley_batch;
+int pg_cayley_batch_create(pg_cayley **members, int nmembers, pg_cayley_batch **out);
+int pg_cayley_batch_destroy(pg_cayley_batch *b);
+/* One step of every member: psis[k] device complex128 wavefunction of member k,
+ * scales host complex128 [nmembers][nscales] slot values of H_k(t + dt/2). Enqueues only. */
+int pg_cayley_batch_step(pg_cayley_batch *b, void **psis, double dt, const double *scales, int nscales);
+/* Per-member statistics of the last step (waits): stats[nmembers]. */
+int pg_cayley_batch_stats(pg_cayley_batch *b, pg_krylov_stats *stats);
 
 /* Arnoldi expansion used by pIRAM (core/krylov/piram/piram/piram.h:346-442), Euclidean
  * inner product, re-orthogonalisation on. Operator: S^-1 H(slot scales) or, when

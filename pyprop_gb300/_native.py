@@ -85,6 +85,10 @@ _SIGS = {
     "pg_cayley_advance": (_I, [_P, _P, _D, _I, _DP, _I, C.POINTER(KrylovStats)]),
     "pg_cayley_last_stats": (_I, [_P, C.POINTER(KrylovStats)]),
     "pg_cayley_set_true_residual": (_I, [_P, _I]),
+    "pg_cayley_batch_create": (_I, [C.POINTER(_P), _I, C.POINTER(_P)]),
+    "pg_cayley_batch_destroy": (_I, [_P]),
+    "pg_cayley_batch_step": (_I, [_P, C.POINTER(_P), _D, _DP, _I]),
+    "pg_cayley_batch_stats": (_I, [_P, C.POINTER(KrylovStats)]),
     "pg_arnoldi_expand": (_I, [_P, _P, _P, _DP, _I, _P, _I, _I, _P, _DP, _D, _I, _IP, _DP,
                                C.POINTER(KrylovStats)]),
     "pg_vec_dot": (_I, [_P, _I, _P, _P, _LL, _DP]),

@@ -220,34 +220,113 @@ class BSplineBasis:
         return np.tensordot(coeffs, B, axes=([-1], [0]))
 
     # -- matrix elements ------------------------------------------------------------------
+    def _local(self):
+        """Per breakpoint interval m: the k splines nonzero there (index, -1 if dropped) and
+        their values and first/second derivatives at the interval's quadrature points.
+
+        Values come from de Boor's triangular recursion (BSPLVB) run on all intervals and
+        points at once; the derivatives use the same lower-order formulas as the dense
+        tables (bspline.cpp:82-165)."""
+        if getattr(self, "_local_cache", None) is None:
+            k = self.MaxSplineOrder
+            N = self.NumberOfBSplines
+            q = self.quad_order
+            t = self.knots
+            bps = self.breakpoints
+            nint = len(bps) - 1
+            s_idx = np.searchsorted(t, bps[:-1], side="right") - 1  # knot index of each interval
+            x = self.grid.reshape(nint, q)
+            # b[p][r]: order-(p+1) splines s-p+r, r = 0..p, at every (interval, point)
+            orders = {}
+            b = [np.ones_like(x)]
+            orders[1] = b
+            left = [None] + [x - t[np.clip(s_idx + 1 - j, 0, len(t) - 1)][:, None] for j in range(1, k)]
+            right = [None] + [t[np.clip(s_idx + j, 0, len(t) - 1)][:, None] - x for j in range(1, k)]
+            for p in range(1, k):
+                nb = []
+                saved = np.zeros_like(x)
+                for r in range(p):
+                    den = right[r + 1] + left[p - r]
+                    temp = np.divide(b[r], den, out=np.zeros_like(x), where=den != 0)
+                    nb.append(saved + right[r + 1] * temp)
+                    saved = left[p - r] * temp
+                nb.append(saved)
+                b = nb
+                orders[p + 1] = b
+
+            def deriv(vals_lower, order, first):
+                # d/dx of order-`order` splines i = first + r from order-1 splines (same indexing)
+                out = []
+                for r in range(order):
+                    i = first + r
+                    acc = np.zeros_like(x)
+                    if r - 1 >= 0:  # B_{order-1, i} is index r-1 among order-1 splines starting at first+1
+                        den = (t[np.clip(i + order - 1, 0, len(t) - 1)] - t[np.clip(i, 0, len(t) - 1)])
+                        c = np.divide(order - 1.0, den, out=np.zeros_like(den, dtype=float), where=den != 0)
+                        acc = acc + c[:, None] * vals_lower[r - 1]
+                    if r < order - 1:
+                        den = (t[np.clip(i + order, 0, len(t) - 1)] - t[np.clip(i + 1, 0, len(t) - 1)])
+                        c = np.divide(order - 1.0, den, out=np.zeros_like(den, dtype=float), where=den != 0)
+                        acc = acc - c[:, None] * vals_lower[r]
+                    out.append(acc)
+                return out
+
+            first_k = s_idx - (k - 1)          # first nonzero order-k spline
+            vals_k = orders[k]                 # splines first_k + r
+            d1 = deriv(orders[k - 1], k, first_k)
+            # second derivative: derivative of the order-(k-1) derivatives
+            d1_km1 = deriv(orders[k - 2], k - 1, first_k + 1)
+            d2 = deriv(d1_km1, k, first_k)
+            idx = first_k[:, None] + np.arange(k)[None, :]
+            valid = (idx >= 0) & (idx < N)
+            idx = np.where(valid, idx, -1)
+            loc = []
+            for vals in (vals_k, d1, d2):
+                L = np.stack(vals, axis=1)  # (nint, k, q)
+                L[~valid] = 0.0
+                loc.append(L)
+            cols = np.arange(nint)[:, None] * q + np.arange(q)[None, :]
+            self._local_cache = (idx, valid, cols, loc)
+        return self._local_cache
+
     def band_elements(self, func_values, derivative=0):
         """Matrix elements ``M[i, j] = <B_i | f | d^d B_j>`` for |i - j| < k.
 
         ``func_values`` is f on the global quadrature grid; a leading batch shape is
         allowed, ``(..., nquad)``. Returns ``(..., N, 2k-1)`` where ``[..., i, (k-1) + (j-i)]``
         holds M[i, j] (zero outside the matrix). For i > j the reference integrates
-        ``(-1)^d <B_j| f |d^d B_i>`` (bspline.cpp:379-393); this does the same.
+        ``(-1)^d <B_j| f |d^d B_i>`` (bspline.cpp:379-393); this does the same. The sums run
+        interval by interval over the k splines that are nonzero there.
         """
-        B, d1, d2 = self.tables()
-        D = {0: B, 1: d1, 2: d2}[derivative]
         k = self.MaxSplineOrder
         N = self.NumberOfBSplines
+        idx, valid, cols, loc = self._local()
+        BL = loc[0]
+        DL = loc[derivative]
         f = np.asarray(func_values)
-        fw = f * self.weights
+        fw = (f * self.weights)[..., cols]  # (..., nint, q)
+        blocks = np.einsum("...mq,maq,mbq->...mab", fw, BL, DL, optimize=True)  # (..., nint, k, k)
         out = np.zeros(f.shape[:-1] + (N, 2 * k - 1), dtype=np.result_type(f, np.float64))
         sign = (-1.0) ** derivative
-        for off in range(-(k - 1), k):
-            if off >= 0:
-                i = np.arange(0, N - off)
-                j = i + off
-                # sum_q w f B_i D_j
-                vals = np.einsum("...q,iq,iq->...i", fw, B[i], D[j], optimize=True)
-                out[..., i, (k - 1) + off] = vals
-            else:
-                i = np.arange(-off, N)
-                j = i + off
-                vals = sign * np.einsum("...q,iq,iq->...i", fw, B[j], D[i], optimize=True)
-                out[..., i, (k - 1) + off] = vals
+        # i <= j: <B_i f D_j>; i > j: sign * <B_j f D_i> (the transposed block entry)
+        m_i, a_i, b_i = np.meshgrid(np.arange(idx.shape[0]), np.arange(k), np.arange(k), indexing="ij")
+        ok = valid[m_i, a_i] & valid[m_i, b_i]
+        m_i, a_i, b_i = m_i[ok], a_i[ok], b_i[ok]
+        lo = np.minimum(a_i, b_i)
+        hi = np.maximum(a_i, b_i)
+        vals = blocks[..., m_i, lo, hi]
+        vals = np.where(a_i <= b_i, vals, sign * vals)
+        rows = idx[m_i, a_i]
+        diag = (k - 1) + idx[m_i, b_i] - rows
+        flat = rows * (2 * k - 1) + diag
+        out2 = out.reshape(f.shape[:-1] + (N * (2 * k - 1),))
+        if out2.ndim == 1:
+            np.add.at(out2, flat, vals)
+        else:
+            lead = out2.reshape(-1, out2.shape[-1])
+            v2 = vals.reshape(-1, vals.shape[-1])
+            for r in range(lead.shape[0]):
+                np.add.at(lead[r], flat, v2[r])
         return out
 
     def overlap_band(self):

@@ -53,21 +53,38 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-// One warp (one CTA) per fibre. Per 32-row block the inverse diagonal block and the
-// coupling rows are copied to shared memory with cp.async one block ahead (double
-// buffer), so the solve reads only shared memory. Four accumulators shorten the FMA chain.
+// One CTA of NW warps per fibre. Per 32-row block the inverse diagonal block and the
+// coupling rows are copied to shared memory with cp.async TRI_STAGES-1 blocks ahead, so the
+// solve reads only shared memory. Lane t of every warp owns row 32*blk + t; warp w forms the
+// partial product of the inverse block over columns s in [w*32/NW, (w+1)*32/NW) and warp 0
+// sums the partials. NW > 1 spreads FP64 work over the SM's sub-partitions (one warp runs on
+// one sub-partition, which has a quarter of the SM's FP64 rate).
 // C: coefficient type (R or cx<R>). inv: [nmat][nblk][32 s][32 t], cpl: [nmat][nblk][w][32 t]
-template <typename R, typename C, bool LOWER>
-__global__ void __launch_bounds__(32) tri_solve_kernel(int N, int nblk, int w, const C *__restrict__ inv,
-                                                       const C *__restrict__ cpl, int per_fibre_matrix,
-                                                       cx<R> *__restrict__ x, int nfib)
+static const int TRI_STAGES = 4;
+
+__device__ __forceinline__ void cp_async_wait_dyn(int pending)
+{
+    // pending groups allowed to remain in flight (0 .. TRI_STAGES-1)
+    if (pending >= 3) cp_async_wait<3>();
+    else if (pending == 2) cp_async_wait<2>();
+    else if (pending == 1) cp_async_wait<1>();
+    else cp_async_wait<0>();
+}
+
+template <typename R, typename C, bool LOWER, int NW>
+__global__ void __launch_bounds__(32 * NW) tri_solve_kernel(int N, int nblk, int w, const C *__restrict__ inv,
+                                                            const C *__restrict__ cpl, int per_fibre_matrix,
+                                                            cx<R> *__restrict__ x, int nfib)
 {
     extern __shared__ __align__(16) unsigned char tri_smem[];
-    const int lane = threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
     const int f = blockIdx.x;
     if (f >= nfib) return;
     const int per_blk = 1024 + w * 32;  // coefficients staged per block
     C *buf = (C *)tri_smem;
+    cx<R> *part = (cx<R> *)(buf + (size_t)TRI_STAGES * per_blk);  // [NW][32]
+    cx<R> *ybuf = part + NW * 32;                                   // [32] solution of the previous block
     const size_t m = per_fibre_matrix ? (size_t)f : 0;
     cx<R> *xf = x + (size_t)f * N;
     const C *invm = inv + m * (size_t)nblk * 1024;
@@ -76,26 +93,23 @@ __global__ void __launch_bounds__(32) tri_solve_kernel(int N, int nblk, int w, c
     const int chunks_cpl = (int)(w * 32 * sizeof(C) / 16);
     auto prefetch = [&](int step) {
         const int blk = LOWER ? step : (nblk - 1 - step);
-        C *dst = buf + (size_t)(step & 1) * per_blk;
+        C *dst = buf + (size_t)(step % TRI_STAGES) * per_blk;
         const unsigned char *gi = (const unsigned char *)(invm + (size_t)blk * 1024);
         const unsigned char *gc = (const unsigned char *)(cplm + (size_t)blk * w * 32);
         unsigned char *si = (unsigned char *)dst;
         unsigned char *sc = (unsigned char *)(dst + 1024);
-        for (int c = lane; c < chunks_inv; c += 32) cp_async16(si + 16 * c, gi + 16 * c);
-        for (int c = lane; c < chunks_cpl; c += 32) cp_async16(sc + 16 * c, gc + 16 * c);
+        for (int c = threadIdx.x; c < chunks_inv; c += 32 * NW) cp_async16(si + 16 * c, gi + 16 * c);
+        for (int c = threadIdx.x; c < chunks_cpl; c += 32 * NW) cp_async16(sc + 16 * c, gc + 16 * c);
         cp_async_commit();
     };
-    prefetch(0);
-    cx<R> yprev = mk<R>((R)0, (R)0);
+    for (int k = 0; k < TRI_STAGES - 1 && k < nblk; ++k) prefetch(k);
+    if (threadIdx.x < 32) ybuf[lane] = mk<R>((R)0, (R)0);
+    constexpr int SPW = 32 / NW;  // inverse columns per warp
     for (int step = 0; step < nblk; ++step) {
-        if (step + 1 < nblk) {
-            prefetch(step + 1);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
-        __syncwarp();
-        const C *ib = buf + (size_t)(step & 1) * per_blk;
+        if (step + TRI_STAGES - 1 < nblk) prefetch(step + TRI_STAGES - 1);
+        cp_async_wait_dyn(min(TRI_STAGES - 1, nblk - 1 - step));
+        __syncthreads();
+        const C *ib = buf + (size_t)(step % TRI_STAGES) * per_blk;
         const C *cb = ib + 1024;
         const int blk = LOWER ? step : (nblk - 1 - step);
         const int row = blk * 32 + lane;
@@ -105,20 +119,33 @@ __global__ void __launch_bounds__(32) tri_solve_kernel(int N, int nblk, int w, c
                 // LOWER: row couples to row-j in the previous block when lane < j
                 // UPPER: row couples to row+j in the next block when lane >= 32-j
                 const int src_lane = LOWER ? (32 - j + lane) & 31 : (lane + j - 32) & 31;
-                const cx<R> yp = shfl_cx(yprev, src_lane);
                 const bool use = LOWER ? (lane < j) : (lane >= 32 - j);
-                if (use) coef_fms(r, cb[(j - 1) * 32 + lane], yp);
+                if (use) coef_fms(r, cb[(j - 1) * 32 + lane], ybuf[src_lane]);
             }
         }
         cx<R> acc[4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) acc[a] = mk<R>((R)0, (R)0);
 #pragma unroll
-        for (int s = 0; s < 32; ++s) coef_fma(acc[s & 3], ib[s * 32 + lane], shfl_cx(r, s));
-        const cx<R> y = (acc[0] + acc[1]) + (acc[2] + acc[3]);
-        if (row < N) xf[row] = y;
-        yprev = y;
-        __syncwarp();  // the buffer is refilled by the next prefetch
+        for (int q = 0; q < SPW; ++q) {
+            const int s = warp * SPW + q;
+            coef_fma(acc[q & 3], ib[s * 32 + lane], shfl_cx(r, s));
+        }
+        cx<R> y = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+        if (NW > 1) {
+            part[warp * 32 + lane] = y;
+            __syncthreads();
+            if (warp == 0) {
+                y = part[lane];
+#pragma unroll
+                for (int q = 1; q < NW; ++q) y = y + part[q * 32 + lane];
+            }
+        }
+        if (warp == 0) {
+            if (row < N) xf[row] = y;
+            ybuf[lane] = y;
+        }
+        __syncthreads();  // ybuf ready; the stage buffer may be refilled
     }
 }
 
@@ -419,12 +446,23 @@ static int launch_tri(pg_banded *b, bool lower, void *x)
     const int N = b->N, nblk = (N + 31) / 32, w = b->kb;
     const int nfib = b->op->nrows;
     if (w > 32 || (w * 32 * sizeof(C)) % 16 != 0) return PG_ERR_ARG;
-    const size_t smem = 2 * (size_t)(1024 + w * 32) * sizeof(C);
+    // FP64 spreads each block product over 4 warps, FP32 keeps one warp per fibre
+    constexpr int NW = sizeof(R) == 8 ? 4 : 1;
+    const size_t smem = (size_t)TRI_STAGES * (1024 + w * 32) * sizeof(C) + (size_t)(NW + 1) * 32 * sizeof(cx<R>);
+    static bool configured[2][2] = {{false, false}, {false, false}};
+    bool &cfg = configured[lower ? 1 : 0][sizeof(C) == sizeof(R) ? 0 : 1];
+    if (!cfg) {
+        PG_CUDA_TRY(cudaFuncSetAttribute(tri_solve_kernel<R, C, true, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem + 4096));
+        PG_CUDA_TRY(cudaFuncSetAttribute(tri_solve_kernel<R, C, false, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem + 4096));
+        cfg = true;
+    }
     if (lower)
-        tri_solve_kernel<R, C, true><<<nfib, 32, smem, ctx->stream>>>(
+        tri_solve_kernel<R, C, true, NW><<<nfib, 32 * NW, smem, ctx->stream>>>(
             N, nblk, w, (const C *)b->d_lo_inv, (const C *)b->d_lo_cpl, b->nmat > 1, (cx<R> *)x, nfib);
     else
-        tri_solve_kernel<R, C, false><<<nfib, 32, smem, ctx->stream>>>(
+        tri_solve_kernel<R, C, false, NW><<<nfib, 32 * NW, smem, ctx->stream>>>(
             N, nblk, w, (const C *)b->d_up_inv, (const C *)b->d_up_cpl, b->nmat > 1, (cx<R> *)x, nfib);
     ctx->launches++;
     return pg_check_launch(ctx);

@@ -15,8 +15,8 @@
 //   mixed - r = b - A psi = -i dt H psi in FP64; a complex64 GMRES (Givens and back
 //           substitution in FP32, Gram-Schmidt sums in FP64 across CTAs) solves
 //           M^-1 A d = M^-1 r to 2e-6 relative; psi += d and r -= A d in FP64; the outer
-//           WHILE node repeats while ||M^-1 r|| > tol (at most 4 passes). ||r|| in FP64 is
-//           the true residual reported.
+//           WHILE node repeats while the true residual ||r|| (FP64) is above tol (at most
+//           4 passes).
 #include "pg_internal.cuh"
 
 #include <algorithm>
@@ -119,9 +119,8 @@ __global__ void cay_gmres_init_kernel(GmresState *st, const double *__restrict__
         st->g[0] = b;
         st->g[1] = 0.0;
         st->stats.passes += 1;
-        const bool run = has_outer ? (b > tol) : (b > 0.0);
-        cudaGraphSetConditional(inner, run ? 1u : 0u);
-        if (has_outer) cudaGraphSetConditional(outer, (run && st->stats.passes < maxpass) ? 1u : 0u);
+        cudaGraphSetConditional(inner, b > 0.0 ? 1u : 0u);
+        (void)outer; (void)has_outer; (void)maxpass;
     }
 }
 
@@ -270,6 +269,17 @@ __global__ void cay_true_resid_kernel(GmresState *st, const double *__restrict__
     if (threadIdx.x == 0 && blockIdx.x == 0) st->stats.true_resid = nrm[1];
 }
 
+// end of a refinement pass: record ||r|| (FP64) and repeat while it is above tol
+__global__ void cay_refine_decide_kernel(GmresState *st, const double *__restrict__ nrm, double tol, int maxpass,
+                                         cudaGraphConditionalHandle outer)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double r = nrm[1];
+    st->stats.true_resid = r;
+    const bool again = (r > tol) && (r == r) && st->stats.passes < maxpass;
+    cudaGraphSetConditional(outer, again ? 1u : 0u);
+}
+
 // ------------------------------------------------------------------------------------
 // host object
 // ------------------------------------------------------------------------------------
@@ -277,6 +287,8 @@ struct pg_cayley {
     pg_op *op64 = nullptr, *opb = nullptr;
     pg_banded *prec64 = nullptr, *precb = nullptr;
     pg_ctx *ctx = nullptr;
+    pg_ctx rctx;                      // private reduction scratch: steppers may run concurrently
+    StepParams *params_dev = nullptr; // where the graph reads this step's parameters
     int m = 0, prec = PG_FP64;
     long long n = 0;
     double tol = 1e-13;
@@ -349,9 +361,11 @@ static int capture_iteration(pg_cayley *c, pg_op *op, pg_banded *pre, cudaGraphC
     memset(&dummy, 0, sizeof(dummy));
     PG_TRY(pg_op_matvec_dev(op, dummy, c->d_sc + SC_PLUS * PG_MAX_SLOTS, vcur, w, 0, nullptr, nullptr));
     PG_TRY(pg_banded_apply_dev(pre, PG_BAND_PREC_SOLVE, w));
-    PG_TRY(pg_multidot<R>(ctx, V, n, c->m, w, n, c->h1, &c->st->j));
-    PG_TRY(pg_gs_update<R>(ctx, V, n, c->m, c->h1, w, n, 1, c->h2, &c->st->j));
-    PG_TRY(pg_gs_update<R>(ctx, V, n, c->m, c->h2, w, n, 0, c->h3, &c->st->j));
+    pg_ctx *rc = &c->rctx;
+    rc->stream = s;
+    PG_TRY(pg_multidot<R>(rc, V, n, c->m, w, n, c->h1, &c->st->j));
+    PG_TRY(pg_gs_update<R>(rc, V, n, c->m, c->h1, w, n, 1, c->h2, &c->st->j));
+    PG_TRY(pg_gs_update<R>(rc, V, n, c->m, c->h2, w, n, 0, c->h3, &c->st->j));
     cay_gmres_finalize_kernel<T><<<1, 32, 0, s>>>(c->st, c->h1, c->h2, c->h3, c->m, inner);
     return pg_check_launch(ctx);
 }
@@ -384,12 +398,14 @@ static int record_fp64(pg_cayley *c, cxd *psi)
     const int nb = nblocks_for(ctx, n);
     pg_scales dummy;
     memset(&dummy, 0, sizeof(dummy));
-    cay_scales_kernel<<<1, 32, 0, s0>>>(c->d_params, c->d_sc, c->st);
+    pg_ctx *rc = &c->rctx;
+    rc->stream = s0;
+    cay_scales_kernel<<<1, 32, 0, s0>>>(c->params_dev, c->d_sc, c->st);
     PG_TRY(pg_check_launch(ctx));
     PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_MINUS * PG_MAX_SLOTS, psi, c->b64, 0, nullptr, nullptr));
     PG_CUDA_TRY(cudaMemcpyAsync(c->d64, c->b64, sizeof(cxd) * n, cudaMemcpyDeviceToDevice, s0));
     PG_TRY(pg_banded_apply_dev(c->prec64, PG_BAND_PREC_SOLVE, c->d64));
-    PG_TRY(pg_multidot<double>(ctx, c->d64, n, 0, c->d64, n, c->nrm));
+    PG_TRY(pg_multidot<double>(rc, c->d64, n, 0, c->d64, n, c->nrm));
     cudaGraphConditionalHandle inner;
     PG_TRY(capture_handle(s0, &inner, 0, 0));
     cay_gmres_init_kernel<double><<<nb, 256, 0, s0>>>(c->st, c->nrm, c->d64, (cxd *)c->V, (cxd *)c->vcur, n, c->tol,
@@ -406,7 +422,8 @@ static int record_fp64(pg_cayley *c, cxd *psi)
         // ||(S + i dt/2 H) psi' - b||
         PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_PLUS * PG_MAX_SLOTS, psi, c->r64, 0, nullptr, nullptr));
         PG_TRY(pg_axpy(ctx, mk<double>(-1.0, 0.0), c->b64, c->r64, n));
-        PG_TRY(pg_multidot<double>(ctx, c->r64, n, 0, c->r64, n, c->nrm2));
+        rc->stream = s0;
+        PG_TRY(pg_multidot<double>(rc, c->r64, n, 0, c->r64, n, c->nrm2));
         cay_true_resid_kernel<<<1, 32, 0, s0>>>(c->st, c->nrm2);
         PG_TRY(pg_check_launch(ctx));
     }
@@ -414,7 +431,8 @@ static int record_fp64(pg_cayley *c, cxd *psi)
     return PG_OK;
 }
 
-// mixed step: FP64 residual, complex64 GMRES correction, refinement WHILE loop
+// mixed step: FP64 residual, complex64 GMRES correction, refinement WHILE loop that
+// repeats while the FP64 true residual ||b - A psi|| is above tol (at most 4 passes)
 static int record_mixed(pg_cayley *c, cxd *psi)
 {
     pg_ctx *ctx = c->ctx;
@@ -423,7 +441,8 @@ static int record_mixed(pg_cayley *c, cxd *psi)
     const int nb = nblocks_for(ctx, n);
     pg_scales dummy;
     memset(&dummy, 0, sizeof(dummy));
-    cay_scales_kernel<<<1, 32, 0, s0>>>(c->d_params, c->d_sc, c->st);
+    pg_ctx *rc = &c->rctx;
+    cay_scales_kernel<<<1, 32, 0, s0>>>(c->params_dev, c->d_sc, c->st);
     PG_TRY(pg_check_launch(ctx));
     PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_DIFF * PG_MAX_SLOTS, psi, c->r64, 0, nullptr, nullptr));
     cudaGraphConditionalHandle outer;
@@ -435,7 +454,8 @@ static int record_mixed(pg_cayley *c, cxd *psi)
         cxf *dconv = (cxf *)c->dconv;
         PG_TRY((pg_scale_copy<float, double>(ctx, c->r64, dconv, nullptr, n, nullptr, 1.0)));
         PG_TRY(pg_banded_apply_dev(c->precb, PG_BAND_PREC_SOLVE, dconv));
-        PG_TRY(pg_multidot<float>(ctx, dconv, n, 0, dconv, n, c->nrm));
+        rc->stream = s1;
+        PG_TRY(pg_multidot<float>(rc, dconv, n, 0, dconv, n, c->nrm));
         cudaGraphConditionalHandle inner;
         PG_TRY(capture_handle(s1, &inner, 0, 0));
         cay_gmres_init_kernel<float><<<nb, 256, 0, s1>>>(c->st, c->nrm, dconv, (cxf *)c->V, (cxf *)c->vcur, n, c->tol,
@@ -448,12 +468,13 @@ static int record_mixed(pg_cayley *c, cxd *psi)
         PG_TRY(pg_check_launch(ctx));
         cay_combine_kernel<float><<<nb, 256, 0, s1>>>((const cxf *)c->V, n, c->st, c->e64, psi);
         PG_TRY(pg_check_launch(ctx));
-        // r -= (S + i dt/2 H) e   in FP64
-        return pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_NEGPLUS * PG_MAX_SLOTS, c->e64, c->r64, 1, nullptr, nullptr);
+        // r -= (S + i dt/2 H) e   in FP64, then ||r|| decides whether another pass runs
+        PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_NEGPLUS * PG_MAX_SLOTS, c->e64, c->r64, 1, nullptr, nullptr));
+        rc->stream = s1;
+        PG_TRY(pg_multidot<double>(rc, c->r64, n, 0, c->r64, n, c->nrm2));
+        cay_refine_decide_kernel<<<1, 32, 0, s1>>>(c->st, c->nrm2, c->tol, 4, outer);
+        return pg_check_launch(ctx);
     }));
-    PG_TRY(pg_multidot<double>(ctx, c->r64, n, 0, c->r64, n, c->nrm2));
-    cay_true_resid_kernel<<<1, 32, 0, s0>>>(c->st, c->nrm2);
-    PG_TRY(pg_check_launch(ctx));
     PG_CUDA_TRY(cudaMemcpyAsync(c->h_stats, &c->st->stats, sizeof(GmresStats), cudaMemcpyDeviceToHost, s0));
     return PG_OK;
 }
@@ -523,6 +544,11 @@ extern "C" int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64,
     PG_CUDA_TRY(cudaMallocHost(&c->h_stats, sizeof(GmresStats)));
     memset(c->h_stats, 0, sizeof(GmresStats));
     PG_CUDA_TRY(cudaMalloc(&c->d_params, sizeof(StepParams)));
+    c->params_dev = c->d_params;
+    c->rctx.device = c->ctx->device;
+    c->rctx.num_sms = c->ctx->num_sms;
+    c->rctx.stream = c->ctx->stream;
+    PG_TRY(pg_ctx_ensure_reduction(&c->rctx));
     PG_CUDA_TRY(cudaMallocHost(&c->h_ring, sizeof(StepParams) * RING));
     PG_CUDA_TRY(cudaMalloc(&c->d_sc, sizeof(cxd) * SC_COUNT * PG_MAX_SLOTS));
     for (int k = 0; k < RING; ++k) {
@@ -544,8 +570,10 @@ extern "C" int pg_cayley_destroy(pg_cayley *c)
         if (c->cap[k]) cudaStreamDestroy(c->cap[k]);
     for (int k = 0; k < RING; ++k) cudaEventDestroy(c->ring_ev[k]);
     void *bufs[] = {c->V, c->w, c->vcur, c->dconv, c->b64, c->r64, c->d64, c->e64, c->h1, c->h2, c->h3, c->nrm,
-                    c->nrm2, c->st, c->d_params, c->d_sc};
+                    c->nrm2, c->st, c->d_params, c->d_sc, c->rctx.red_partial, c->rctx.red_counter,
+                    c->rctx.red_out, c->rctx.d_err};
     for (void *b : bufs) cudaFree(b);
+    if (c->rctx.h_pinned) cudaFreeHost(c->rctx.h_pinned);
     if (c->h_stats) cudaFreeHost(c->h_stats);
     if (c->h_ring) cudaFreeHost(c->h_ring);
     delete c;
@@ -576,7 +604,7 @@ static int cayley_launch(pg_cayley *c, cxd *psi, double dt, const double *scales
 static long long step_kernels(const pg_cayley *c, const GmresStats &g)
 {
     if (c->prec == PG_FP64) return 8 + 8 * g.iterations + (c->true_residual ? 4 : 0);
-    return 4 + 8LL * g.passes + 8 * g.iterations;
+    return 2 + 10LL * g.passes + 8 * g.iterations;
 }
 
 static void fill_stats(pg_cayley *c, pg_krylov_stats *st)
@@ -633,5 +661,146 @@ extern "C" int pg_cayley_last_stats(pg_cayley *c, pg_krylov_stats *st)
     if (!c || !st) return PG_ERR_ARG;
     PG_CUDA_TRY(cudaStreamSynchronize(c->ctx->stream));
     fill_stats(c, st);
+    return PG_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// ensembles: many independent Cayley steppers advanced by one graph launch
+// ------------------------------------------------------------------------------------
+// Each member keeps its own operator, preconditioner, Krylov basis, reduction scratch and
+// conditional loops; the batch graph forks one branch per member from a common origin and
+// joins them, so the members' kernels run concurrently and the whole ensemble step is a
+// single cudaGraphLaunch. Step parameters of all members travel in one host-to-device copy.
+struct pg_cayley_batch {
+    std::vector<pg_cayley *> members;
+    std::vector<void *> psis;
+    pg_ctx *ctx = nullptr;
+    StepParams *d_params = nullptr;
+    StepParams *h_params = nullptr;
+    cudaEvent_t params_done = nullptr;
+    bool params_pending = false;
+    cudaStream_t origin = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" int pg_cayley_batch_create(pg_cayley **members, int nmembers, pg_cayley_batch **out)
+{
+    if (!members || nmembers < 1 || !out) return PG_ERR_ARG;
+    pg_cayley_batch *b = new pg_cayley_batch();
+    b->ctx = members[0]->ctx;
+    for (int k = 0; k < nmembers; ++k) {
+        if (!members[k] || members[k]->ctx != b->ctx) { delete b; return PG_ERR_ARG; }
+        b->members.push_back(members[k]);
+    }
+    PG_CUDA_TRY(cudaMalloc(&b->d_params, sizeof(StepParams) * nmembers));
+    PG_CUDA_TRY(cudaMallocHost(&b->h_params, sizeof(StepParams) * nmembers));
+    memset(b->h_params, 0, sizeof(StepParams) * nmembers);
+    PG_CUDA_TRY(cudaEventCreateWithFlags(&b->params_done, cudaEventDisableTiming));
+    PG_CUDA_TRY(cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking));
+    PG_CUDA_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    b->join.resize(nmembers);
+    for (int k = 0; k < nmembers; ++k) PG_CUDA_TRY(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
+    *out = b;
+    return PG_OK;
+}
+
+extern "C" int pg_cayley_batch_destroy(pg_cayley_batch *b)
+{
+    if (!b) return PG_ERR_ARG;
+    cudaStreamSynchronize(b->ctx->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (auto e : b->join) cudaEventDestroy(e);
+    cudaEventDestroy(b->fork);
+    cudaEventDestroy(b->params_done);
+    cudaStreamDestroy(b->origin);
+    cudaFree(b->d_params);
+    cudaFreeHost(b->h_params);
+    for (pg_cayley *c : b->members) {
+        c->params_dev = c->d_params;
+        c->built_psi = nullptr;  // a member stepped alone again rebuilds its own graph
+    }
+    delete b;
+    return PG_OK;
+}
+
+static int batch_build(pg_cayley_batch *b, void **psis)
+{
+    pg_ctx *ctx = b->ctx;
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    const int n = (int)b->members.size();
+    cudaStream_t saved = ctx->stream;
+    PG_CUDA_TRY(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
+    int code = PG_OK;
+    if (cudaEventRecord(b->fork, b->origin) != cudaSuccess) code = PG_ERR_CUDA;
+    for (int k = 0; k < n && code == PG_OK; ++k) {
+        pg_cayley *c = b->members[k];
+        c->params_dev = b->d_params + k;
+        if (cudaStreamWaitEvent(c->cap[0], b->fork, 0) != cudaSuccess) { code = PG_ERR_CUDA; break; }
+        ctx->stream = c->cap[0];
+        code = (c->prec == PG_FP64) ? record_fp64(c, (cxd *)psis[k]) : record_mixed(c, (cxd *)psis[k]);
+        ctx->stream = saved;
+        if (code != PG_OK) break;
+        if (cudaEventRecord(b->join[k], c->cap[0]) != cudaSuccess ||
+            cudaStreamWaitEvent(b->origin, b->join[k], 0) != cudaSuccess)
+            code = PG_ERR_CUDA;
+    }
+    ctx->stream = saved;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->origin, &g);
+    if (code != PG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return code;
+    }
+    if (e != cudaSuccess) {
+        pg_set_last_error(e, "cudaStreamEndCapture(batch)", __FILE__, __LINE__);
+        return PG_ERR_CUDA;
+    }
+    b->graph = g;
+    PG_CUDA_TRY(cudaGraphInstantiate(&b->exec, g, 0));
+    b->psis.assign(psis, psis + n);
+    for (pg_cayley *c : b->members) c->built_psi = nullptr;  // their own graphs no longer match
+    return PG_OK;
+}
+
+// One ensemble step: member k's wavefunction psis[k], slot values scales[k][0..nscales).
+extern "C" int pg_cayley_batch_step(pg_cayley_batch *b, void **psis, double dt, const double *scales, int nscales)
+{
+    if (!b || !psis || !scales || nscales < 1 || nscales > PG_MAX_SLOTS) return PG_ERR_ARG;
+    const int n = (int)b->members.size();
+    bool same = b->exec && (int)b->psis.size() == n;
+    for (int k = 0; same && k < n; ++k) same = (b->psis[k] == psis[k]);
+    if (!same) PG_TRY(batch_build(b, psis));
+    if (b->params_pending) PG_CUDA_TRY(cudaEventSynchronize(b->params_done));
+    for (int k = 0; k < n; ++k) {
+        StepParams &p = b->h_params[k];
+        p.dt = dt;
+        for (int q = 0; q < PG_MAX_SLOTS; ++q)
+            p.h[q] = mk<double>(q < nscales ? scales[2 * ((size_t)k * nscales + q)] : 0.0,
+                                q < nscales ? scales[2 * ((size_t)k * nscales + q) + 1] : 0.0);
+    }
+    cudaStream_t s = b->ctx->stream;
+    PG_CUDA_TRY(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(StepParams) * n, cudaMemcpyHostToDevice, s));
+    PG_CUDA_TRY(cudaEventRecord(b->params_done, s));
+    b->params_pending = true;
+    PG_CUDA_TRY(cudaGraphLaunch(b->exec, s));
+    return PG_OK;
+}
+
+// Per-member statistics of the last completed ensemble step (waits for the stream).
+extern "C" int pg_cayley_batch_stats(pg_cayley_batch *b, pg_krylov_stats *stats)
+{
+    if (!b || !stats) return PG_ERR_ARG;
+    PG_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+    long long kernels = 0;
+    for (size_t k = 0; k < b->members.size(); ++k) {
+        fill_stats(b->members[k], &stats[k]);
+        kernels += step_kernels(b->members[k], *b->members[k]->h_stats);
+    }
+    b->ctx->launches += kernels;
     return PG_OK;
 }

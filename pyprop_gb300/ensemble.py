@@ -1,0 +1,102 @@
+"""Ensembles of independent hydrogen-like propagations advanced together on one GPU.
+
+Each member is an ordinary ``Problem`` with ``CayleyPropagatorGPU`` (its own basis size,
+angular size and laser parameters). ``CayleyEnsembleGPU`` binds their device steppers into a
+``pg_cayley_batch``: one CUDA graph launch per ensemble step, one branch per member, the
+branches running concurrently. This is the ensemble mode the reference runs as separate
+processes (one job per field parameter set, ``pyprop/utilities/submitpbs*.py``).
+
+``partition_members`` splits an ensemble over ranks for multi-GPU runs (members are
+independent: no collective on the data path).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as nat
+from ._native import check
+
+
+def partition_members(nmembers, world_size, rank):
+    """Contiguous, balanced member ranges: rank r gets [start, stop)."""
+    base, extra = divmod(nmembers, world_size)
+    start = rank * base + min(rank, extra)
+    stop = start + base + (1 if rank < extra else 0)
+    return start, stop
+
+
+def hydrogen_ensemble_params(nmembers=256, seed=20261203, lmax_range=(8, 32), n_range=(100, 400),
+                             e0_range=(0.01, 0.1), wavelength_range=(400.0, 1600.0)):
+    """Member parameters drawn from numpy's default_rng(seed): lmax ~ U{8..32}, B-splines
+    ~ U{100..400}, peak field ~ U[0.01, 0.1] a.u., wavelength ~ U[400, 1600] nm."""
+    rng = np.random.default_rng(seed)
+    lmax = rng.integers(lmax_range[0], lmax_range[1] + 1, nmembers)
+    nb = rng.integers(n_range[0], n_range[1] + 1, nmembers)
+    e0 = rng.uniform(e0_range[0], e0_range[1], nmembers)
+    lam = rng.uniform(wavelength_range[0], wavelength_range[1], nmembers)
+    return [dict(lmax=int(a), nbsplines=int(b), amplitude=float(c), wavelength_nm=float(d))
+            for a, b, c, d in zip(lmax, nb, e0, lam)]
+
+
+class CayleyEnsembleGPU:
+    """Advance many ``Problem`` objects (CayleyPropagatorGPU, same dt) with one launch per step."""
+
+    def __init__(self, problems):
+        self.problems = list(problems)
+        if not self.problems:
+            raise ValueError("empty ensemble")
+        props = [p.Propagator for p in self.problems]
+        for pr in props:
+            if not hasattr(pr, "stepper"):
+                raise ValueError("call SetupStep() on every member first")
+        self.lib = props[0].stepper.lib
+        self.ctx = props[0].stepper.ctx
+        n = len(props)
+        arr = (C.c_void_p * n)(*[pr.stepper.h.value for pr in props])
+        h = C.c_void_p()
+        check(self.lib.pg_cayley_batch_create(arr, n, C.byref(h)), "pg_cayley_batch_create")
+        self.h = h
+        self._keep = props
+        self.nslots = props[0].op64.nslots
+        if any(pr.op64.nslots != self.nslots for pr in props):
+            raise ValueError("ensemble members must have the same number of potential slots")
+        self.dt = self.problems[0].TimeStep
+        self._psis = (C.c_void_p * n)(*[p.psi.GetData().data_ptr() for p in self.problems])
+        self.stats = (nat.KrylovStats * n)()
+
+    def scales(self):
+        """(n, nslots) slot values of each member's H(t + dt/2) at its current time."""
+        dt = self.dt
+        return np.stack([p.Propagator.op64.scales(p.PropagatedTime + abs(dt / 2.0)) for p in self.problems])
+
+    def AdvanceStep(self, scales=None):
+        sc = np.ascontiguousarray(self.scales() if scales is None else scales, dtype=np.complex128)
+        self.ctx.bind_stream()
+        check(self.lib.pg_cayley_batch_step(self.h, self._psis, float(self.dt), sc.view(np.float64).ctypes.data_as(
+            nat._DP), self.nslots), "pg_cayley_batch_step")
+        for p in self.problems:
+            p.PropagatedTime += self.dt
+
+    def scale_table(self, nsteps):
+        """Slot values for the next ``nsteps`` steps of every member: (nsteps, n, nslots)."""
+        dt = self.dt
+        out = np.empty((nsteps, len(self.problems), self.nslots), dtype=np.complex128)
+        for k, p in enumerate(self.problems):
+            op = p.Propagator.op64
+            for s in range(nsteps):
+                out[s, k] = op.scales(p.PropagatedTime + s * dt + abs(dt / 2.0))
+        return out
+
+    def Stats(self):
+        self.ctx.bind_stream()
+        check(self.lib.pg_cayley_batch_stats(self.h, self.stats), "pg_cayley_batch_stats")
+        return [s.as_dict() for s in self.stats]
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.lib.pg_cayley_batch_destroy(self.h)
+        except Exception:
+            pass

@@ -1,0 +1,57 @@
+"""Ensemble stepping (one graph launch for many members) against members stepped alone."""
+import numpy as np
+import pytest
+
+from tests.helpers import hydrogen_problem, oracle_hamiltonian, relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def _members(precision):
+    specs = [dict(lmax=3, nbsplines=40, rmax=40.0, amplitude=0.05),
+             dict(lmax=5, nbsplines=33, rmax=30.0, amplitude=0.08, wavelength_nm=400.0),
+             dict(lmax=2, nbsplines=55, rmax=50.0, amplitude=0.02, wavelength_nm=1600.0)]
+    probs = []
+    for k, sp in enumerate(specs):
+        p = hydrogen_problem(propagator="CayleyPropagatorGPU", precision=precision, gmres_tolerance=1e-12, **sp)
+        p.SetupStep(skipWavefunctionSetup=True)
+        rng = np.random.default_rng(100 + k)
+        shape = p.psi.GetRepresentation().GetFullShape()
+        psi = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+        p.psi.SetData(psi / np.linalg.norm(psi))
+        p.PropagatedTime = 1.0
+        probs.append(p)
+    return probs
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_ensemble_matches_single_members(gpu, precision):
+    from pyprop_gb300.ensemble import CayleyEnsembleGPU
+    alone = _members(precision)
+    together = _members(precision)
+    for _ in range(3):
+        for p in alone:
+            p.AdvanceStep()
+    ens = CayleyEnsembleGPU(together)
+    for _ in range(3):
+        ens.AdvanceStep()
+    stats = ens.Stats()
+    for a, b, st in zip(alone, together, stats):
+        assert relerr(b.psi.numpy(), a.psi.numpy()) < 1e-13
+        assert st["Iterations"] >= 1
+        assert abs(a.PropagatedTime - b.PropagatedTime) < 1e-12
+
+
+def test_ensemble_member_against_oracle(gpu):
+    from pyprop_gb300.ensemble import CayleyEnsembleGPU
+    from oracle.propagators import OracleCayley
+    together = _members("fp64")
+    psi0 = [p.psi.numpy() for p in together]
+    ens = CayleyEnsembleGPU(together)
+    for _ in range(2):
+        ens.AdvanceStep()
+    for p, start in zip(together, psi0):
+        ham = oracle_hamiltonian(p)
+        cay = OracleCayley(ham, 0.01, [0], 20, 1e-13)
+        ref = cay.step(cay.step(start, 1.0, 0.01), 1.01, 0.01)
+        assert relerr(p.psi.numpy(), ref) < 1e-10
