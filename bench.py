@@ -166,6 +166,7 @@ def run_ours(args):
     for prec in ("fp32", "fp64"):
         p = pp.Problem(pp.LoadString(_config(prec)))
         p.Propagator.StepStats = False  # steps only enqueue; stats are read after the end event
+        p.Propagator.Eager = args.eager
         p.SetupStep(skipWavefunctionSetup=True)
         probs[prec] = p
     psi0, e0 = initial_state(probs["fp32"])
@@ -183,6 +184,7 @@ def run_ours(args):
         total = 0.0
         iters = 0
         ctx = prob.Propagator.op64.ctx
+        prob.Propagator.LastStats  # settles the device kernel count of the warm-up steps
         l0 = ctx.launches()
         for _ in range(K):
             flush.fill_(1.0)
@@ -243,7 +245,7 @@ def run_ours(args):
             traffic = json.load(fh).get("bytes_per_launch")
 
     ens = run_ensemble(args, torch, flush) if args.ensemble > 0 else None
-    cpu = cpu_baseline_sample() if (rank == 0 and world == 1 and not args.no_cpu) else None
+    cpu = cpu_baseline_sample(nsteps=args.cpu_steps) if (rank == 0 and world == 1 and args.cpu_steps > 0) else None
     if rank == 0:
         steps_per_s = world * args.steps / t_mixed
         line = {
@@ -399,7 +401,7 @@ def run_reference(args):
     if rank != 0:
         return
     procs = os.cpu_count() or 1
-    nsteps = max(1, min(args.steps, 10))
+    nsteps = max(10, min(args.steps, 300))
     base = cpu_baseline_sample(nsteps=nsteps, procs=procs)
     line = {"metric": METRIC, "value": base["value"], "unit": "steps/s", "n_gpus": 0, "steps": nsteps * procs,
             "warmup": 0, "ms_per_step": 1e3 / base["value"], "higher_is_better": True, "scaling": "weak",
@@ -416,7 +418,10 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=300,
+                    help="oracle Cayley steps timed on one host core for cpu_baseline (0 = skip)")
+    ap.add_argument("--eager", action="store_true",
+                    help="host-driven GMRES loops (same kernels, visible one by one to a profiler)")
     ap.add_argument("--ensemble", type=int, default=256, help="members of the batched leg (0 = skip)")
     args = ap.parse_args()
     if args.warmup < 3:

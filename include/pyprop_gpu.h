@@ -224,6 +224,10 @@ int pg_cayley_advance(pg_cayley *c, void *psi, double dt, int nsteps, const doub
 int pg_cayley_last_stats(pg_cayley *c, pg_krylov_stats *stats);
 /* FP64 mode: also compute ||(S + i dt/2 H) psi' - b|| every step (one extra matvec). */
 int pg_cayley_set_true_residual(pg_cayley *c, int on);
+/* Eager mode: the same kernels launched one by one with the GMRES/refinement loops driven
+ * from the host (one wait per iteration). For profilers that cannot look inside
+ * conditional graph nodes; results are identical to the graph mode. */
+int pg_cayley_set_eager(pg_cayley *c, int on);
 
 /* Ensembles: many pg_cayley members (each with its own operator, basis size, field) advanced
  * together by one CUDA graph launch whose branches (one per member) run concurrently. The

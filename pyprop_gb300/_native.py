@@ -85,6 +85,7 @@ _SIGS = {
     "pg_cayley_advance": (_I, [_P, _P, _D, _I, _DP, _I, C.POINTER(KrylovStats)]),
     "pg_cayley_last_stats": (_I, [_P, C.POINTER(KrylovStats)]),
     "pg_cayley_set_true_residual": (_I, [_P, _I]),
+    "pg_cayley_set_eager": (_I, [_P, _I]),
     "pg_cayley_batch_create": (_I, [C.POINTER(_P), _I, C.POINTER(_P)]),
     "pg_cayley_batch_destroy": (_I, [_P]),
     "pg_cayley_batch_step": (_I, [_P, C.POINTER(_P), _D, _DP, _I]),

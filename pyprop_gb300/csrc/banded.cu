@@ -9,10 +9,9 @@
 //    Hermitian part Re(cS) S (cS = 1, cH = i dt/2 in the Cayley step), for which
 //    elimination without pivoting is stable.
 //
-// Triangular solves: one warp per fibre, 32-row blocks. Lane t owns row 32*blk + t. The
-// coupling to the neighbouring block (at most kb rows) is subtracted with warp shuffles,
-// then the precomputed inverse of the 32x32 diagonal block is applied (32 shuffles + FMAs).
-// The sequential dependency is one block (not one row) per step.
+// Triangular solves: one CTA per fibre, 32-row blocks. The diagonal-block products of all
+// blocks run in parallel; the only sequential part is a recurrence on the kb boundary values
+// of consecutive blocks (tri_solve_kernel).
 #include "pg_internal.cuh"
 
 #include <algorithm>
@@ -44,109 +43,109 @@ template <typename R> __device__ __forceinline__ void coef_fms(cx<R> &acc, R c, 
 }
 template <typename R> __device__ __forceinline__ void coef_fms(cx<R> &acc, cx<R> c, cx<R> v) { cfma(acc, mk<R>(-c.x, -c.y), v); }
 
-// Asynchronous 16-byte global->shared copies (cp.async, completion by group wait).
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
-
-// One CTA of NW warps per fibre. Per 32-row block the inverse diagonal block and the
-// coupling rows are copied to shared memory with cp.async TRI_STAGES-1 blocks ahead, so the
-// solve reads only shared memory. Lane t of every warp owns row 32*blk + t; warp w forms the
-// partial product of the inverse block over columns s in [w*32/NW, (w+1)*32/NW) and warp 0
-// sums the partials. NW > 1 spreads FP64 work over the SM's sub-partitions (one warp runs on
-// one sub-partition, which has a quarter of the SM's FP64 rate).
-// C: coefficient type (R or cx<R>). inv: [nmat][nblk][32 s][32 t], cpl: [nmat][nblk][w][32 t]
-static const int TRI_STAGES = 4;
-
-__device__ __forceinline__ void cp_async_wait_dyn(int pending)
-{
-    // pending groups allowed to remain in flight (0 .. TRI_STAGES-1)
-    if (pending >= 3) cp_async_wait<3>();
-    else if (pending == 2) cp_async_wait<2>();
-    else if (pending == 1) cp_async_wait<1>();
-    else cp_async_wait<0>();
-}
-
-template <typename R, typename C, bool LOWER, int NW>
-__global__ void __launch_bounds__(32 * NW) tri_solve_kernel(int N, int nblk, int w, const C *__restrict__ inv,
-                                                            const C *__restrict__ cpl, int per_fibre_matrix,
-                                                            cx<R> *__restrict__ x, int nfib)
+// Blocked triangular solves, parallel over the blocks of a fibre. With T_b the 32x32 diagonal
+// block of block b and C_b its coupling to the w boundary values s of the neighbouring block
+// (lower sweep: the last w values of block b-1; upper sweep: the first w values of block
+// b+1), the solution of block b is
+//     y_b = z_b - G_b s,   z_b = T_b^-1 f_b,   G_b = T_b^-1 C_b   (G_b: 32 x w, precomputed).
+// So every z_b and every correction G_b s is independent work, spread over the CTA's warps
+// (lane t owns row 32b + t), and only the w-wide boundary recurrence
+//     s_b = z_b[boundary rows] - G_b[boundary rows] s_{b-1 or b+1}
+// is sequential: one step per block, w lanes of one warp, operands in shared memory.
+// The fibre stays in shared memory for both sweeps.
+// C: coefficient type (R or cx<R>). inv: [nmat][nblk][32 s][32 t] = T^-1[t][s],
+// g: [nmat][nblk][w c][32 t] = G[t][c].
+template <typename R, typename C, int NW>
+__global__ void __launch_bounds__(32 * NW, 1)
+    tri_solve_kernel(int N, int nblk, int w, const C *__restrict__ lo_inv, const C *__restrict__ lo_g,
+                     const C *__restrict__ up_inv, const C *__restrict__ up_g, int do_lower, int do_upper,
+                     int per_fibre_matrix, int g_in_smem, cx<R> *__restrict__ x, int nfib)
 {
     extern __shared__ __align__(16) unsigned char tri_smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int f = blockIdx.x;
     if (f >= nfib) return;
-    const int per_blk = 1024 + w * 32;  // coefficients staged per block
-    C *buf = (C *)tri_smem;
-    cx<R> *part = (cx<R> *)(buf + (size_t)TRI_STAGES * per_blk);  // [NW][32]
-    cx<R> *ybuf = part + NW * 32;                                   // [32] solution of the previous block
+    cx<R> *xs = (cx<R> *)tri_smem;              // [nblk*32] the fibre: f, then z, then y
+    cx<R> *sb = xs + (size_t)nblk * 32;          // [nblk][w] boundary values s_b
+    C *gt = (C *)(sb + (size_t)nblk * w);        // [nblk][w c][w r] boundary rows of G_b
+    C *sg = gt + (size_t)nblk * w * w;           // [nblk][w][32] G_b (when g_in_smem)
     const size_t m = per_fibre_matrix ? (size_t)f : 0;
+    const size_t gstride = (size_t)w * 32;
     cx<R> *xf = x + (size_t)f * N;
-    const C *invm = inv + m * (size_t)nblk * 1024;
-    const C *cplm = cpl + m * (size_t)nblk * w * 32;
-    const int chunks_inv = (int)(1024 * sizeof(C) / 16);
-    const int chunks_cpl = (int)(w * 32 * sizeof(C) / 16);
-    auto prefetch = [&](int step) {
-        const int blk = LOWER ? step : (nblk - 1 - step);
-        C *dst = buf + (size_t)(step % TRI_STAGES) * per_blk;
-        const unsigned char *gi = (const unsigned char *)(invm + (size_t)blk * 1024);
-        const unsigned char *gc = (const unsigned char *)(cplm + (size_t)blk * w * 32);
-        unsigned char *si = (unsigned char *)dst;
-        unsigned char *sc = (unsigned char *)(dst + 1024);
-        for (int c = threadIdx.x; c < chunks_inv; c += 32 * NW) cp_async16(si + 16 * c, gi + 16 * c);
-        for (int c = threadIdx.x; c < chunks_cpl; c += 32 * NW) cp_async16(sc + 16 * c, gc + 16 * c);
-        cp_async_commit();
-    };
-    for (int k = 0; k < TRI_STAGES - 1 && k < nblk; ++k) prefetch(k);
-    if (threadIdx.x < 32) ybuf[lane] = mk<R>((R)0, (R)0);
-    constexpr int SPW = 32 / NW;  // inverse columns per warp
-    for (int step = 0; step < nblk; ++step) {
-        if (step + TRI_STAGES - 1 < nblk) prefetch(step + TRI_STAGES - 1);
-        cp_async_wait_dyn(min(TRI_STAGES - 1, nblk - 1 - step));
-        __syncthreads();
-        const C *ib = buf + (size_t)(step % TRI_STAGES) * per_blk;
-        const C *cb = ib + 1024;
-        const int blk = LOWER ? step : (nblk - 1 - step);
-        const int row = blk * 32 + lane;
-        cx<R> r = (row < N) ? xf[row] : mk<R>((R)0, (R)0);
-        if (step > 0) {
-            for (int j = 1; j <= w; ++j) {
-                // LOWER: row couples to row-j in the previous block when lane < j
-                // UPPER: row couples to row+j in the next block when lane >= 32-j
-                const int src_lane = LOWER ? (32 - j + lane) & 31 : (lane + j - 32) & 31;
-                const bool use = LOWER ? (lane < j) : (lane >= 32 - j);
-                if (use) coef_fms(r, cb[(j - 1) * 32 + lane], ybuf[src_lane]);
-            }
-        }
+    for (int i = threadIdx.x; i < nblk * 32; i += 32 * NW) xs[i] = (i < N) ? xf[i] : mk<R>((R)0, (R)0);
+    __syncthreads();
+
+    // z_b = T_b^-1 r for lane's row; G_b staged for the boundary recurrence and the correction
+    auto solve_block = [&](int blk, cx<R> r, const C *inv, const C *g, bool lower) {
+        const C *ib = inv + (m * nblk + blk) * 1024;
+        const C *gb = g + (m * nblk + blk) * gstride;
         cx<R> acc[4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) acc[a] = mk<R>((R)0, (R)0);
 #pragma unroll
-        for (int q = 0; q < SPW; ++q) {
-            const int s = warp * SPW + q;
-            coef_fma(acc[q & 3], ib[s * 32 + lane], shfl_cx(r, s));
+        for (int q = 0; q < 32; ++q) coef_fma(acc[q & 3], ib[q * 32 + lane], shfl_cx(r, q));
+        xs[blk * 32 + lane] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+        const int r0 = lower ? 32 - w : 0;  // boundary rows of this block
+        for (int c = 0; c < w; ++c) {
+            const C v = gb[c * 32 + lane];
+            if (g_in_smem) sg[((size_t)blk * w + c) * 32 + lane] = v;
+            if (lane >= r0 && lane < r0 + w) gt[((size_t)blk * w + c) * w + (lane - r0)] = v;
         }
-        cx<R> y = (acc[0] + acc[1]) + (acc[2] + acc[3]);
-        if (NW > 1) {
-            part[warp * 32 + lane] = y;
-            __syncthreads();
-            if (warp == 0) {
-                y = part[lane];
-#pragma unroll
-                for (int q = 1; q < NW; ++q) y = y + part[q * 32 + lane];
-            }
+    };
+    // w-wide recurrence over the blocks (warp 0; lanes >= w mirror lane w-1 to keep shuffles whole)
+    auto scan = [&](bool lower) {
+        if (warp != 0) return;
+        const int r = min(lane, w - 1);
+        const int r0 = lower ? 32 - w : 0;
+        int blk = lower ? 0 : nblk - 1;
+        cx<R> s = xs[blk * 32 + r0 + r];
+        if (lane < w) sb[blk * w + lane] = s;
+        for (int step = 1; step < nblk; ++step) {
+            blk = lower ? step : nblk - 1 - step;
+            cx<R> acc = xs[blk * 32 + r0 + r];
+            const C *gtb = gt + (size_t)blk * w * w;
+            for (int c = 0; c < w; ++c) coef_fms(acc, gtb[c * w + r], shfl_cx(s, c));
+            s = acc;
+            if (lane < w) sb[blk * w + lane] = s;
         }
-        if (warp == 0) {
-            if (row < N) xf[row] = y;
-            ybuf[lane] = y;
+    };
+    // y_b = z_b - G_b s (returns the corrected row)
+    auto correct = [&](int blk, const C *g, bool lower) -> cx<R> {
+        cx<R> y = xs[blk * 32 + lane];
+        const int nb = lower ? blk - 1 : blk + 1;
+        if (nb >= 0 && nb < nblk) {
+            const C *gb = g_in_smem ? sg + (size_t)blk * gstride : g + (m * nblk + blk) * gstride;
+            for (int c = 0; c < w; ++c) coef_fms(y, gb[c * 32 + lane], sb[nb * w + c]);
         }
-        __syncthreads();  // ybuf ready; the stage buffer may be refilled
+        return y;
+    };
+
+    if (do_lower) {
+        for (int blk = warp; blk < nblk; blk += NW) solve_block(blk, xs[blk * 32 + lane], lo_inv, lo_g, true);
+        __syncthreads();
+        scan(true);
+        __syncthreads();
+        for (int blk = warp; blk < nblk; blk += NW) {
+            const cx<R> y = correct(blk, lo_g, true);
+            if (do_upper) solve_block(blk, y, up_inv, up_g, false);  // same rows, same warp
+            else xs[blk * 32 + lane] = y;
+        }
+        __syncthreads();
+    } else if (do_upper) {
+        for (int blk = warp; blk < nblk; blk += NW) solve_block(blk, xs[blk * 32 + lane], up_inv, up_g, false);
+        __syncthreads();
     }
+    if (do_upper) {
+        scan(false);
+        __syncthreads();
+        for (int blk = warp; blk < nblk; blk += NW) {
+            const cx<R> y = correct(blk, up_g, false);
+            xs[blk * 32 + lane] = y;
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < N; i += 32 * NW) xf[i] = xs[i];
 }
 
 // U x (up=1) or U^T x (up=0), U real upper with kb super diagonals, rows [N][kb+1]
@@ -212,15 +211,17 @@ void invert_triangular_32(const zd *T, bool lower, zd *Tinv)
     }
 }
 
-// Build block data for a triangular matrix given by accessor A(i, j) (band width w).
-// inv[blk][s][t] = Tinv[t][s]; cpl[blk][j-1][t] = A(row, row -/+ j) for the cross-block part.
+// Build block data for a triangular matrix given by accessor A(i, j) (band width w):
+// inv[blk][s][t] = T^-1[t][s] for the diagonal block T, and g[blk][c][t] = (T^-1 C)[t][c] for
+// the coupling C[t][c] = A(32 blk + t, col_c) to the neighbouring block's boundary columns
+// col_c = 32 blk - w + c (lower) or 32 (blk + 1) + c (upper), c < w.
 template <typename Acc>
-void build_blocks(int N, int w, bool lower, Acc A, std::vector<zd> &inv, std::vector<zd> &cpl)
+void build_blocks(int N, int w, bool lower, Acc A, std::vector<zd> &inv, std::vector<zd> &g)
 {
     const int nblk = (N + 31) / 32;
     inv.assign((size_t)nblk * 1024, zd(0.0, 0.0));
-    cpl.assign((size_t)nblk * w * 32, zd(0.0, 0.0));
-    std::vector<zd> T(1024), Ti(1024);
+    g.assign((size_t)nblk * w * 32, zd(0.0, 0.0));
+    std::vector<zd> T(1024), Ti(1024), Cm((size_t)32 * w);
     for (int blk = 0; blk < nblk; ++blk) {
         const int r0 = blk * 32;
         for (int t = 0; t < 32; ++t)
@@ -237,12 +238,19 @@ void build_blocks(int N, int w, bool lower, Acc A, std::vector<zd> &inv, std::ve
         invert_triangular_32(T.data(), lower, Ti.data());
         for (int s = 0; s < 32; ++s)
             for (int t = 0; t < 32; ++t) inv[(size_t)blk * 1024 + s * 32 + t] = Ti[t * 32 + s];
-        for (int j = 1; j <= w; ++j)
-            for (int t = 0; t < 32; ++t) {
+        for (int t = 0; t < 32; ++t)
+            for (int c = 0; c < w; ++c) {
                 const int i = r0 + t;
-                const int col = lower ? i - j : i + j;
-                const bool cross = lower ? (t < j) : (t >= 32 - j);
-                if (i < N && cross && col >= 0 && col < N) cpl[(size_t)blk * w * 32 + (j - 1) * 32 + t] = A(i, col);
+                const int col = lower ? r0 - w + c : r0 + 32 + c;
+                zd v(0.0, 0.0);
+                if (i < N && col >= 0 && col < N && std::abs(i - col) <= w) v = A(i, col);
+                Cm[(size_t)t * w + c] = v;
+            }
+        for (int t = 0; t < 32; ++t)
+            for (int c = 0; c < w; ++c) {
+                zd acc(0.0, 0.0);
+                for (int s = 0; s < 32; ++s) acc += Ti[t * 32 + s] * Cm[(size_t)s * w + c];
+                g[(size_t)blk * w * 32 + (size_t)c * 32 + t] = acc;
             }
     }
 }
@@ -440,30 +448,31 @@ extern "C" int pg_banded_destroy(pg_banded *b)
 }
 
 template <typename R, typename C>
-static int launch_tri(pg_banded *b, bool lower, void *x)
+static int launch_tri(pg_banded *b, bool do_lower, bool do_upper, void *x)
 {
     pg_ctx *ctx = b->op->ctx;
     const int N = b->N, nblk = (N + 31) / 32, w = b->kb;
     const int nfib = b->op->nrows;
-    if (w > 32 || (w * 32 * sizeof(C)) % 16 != 0) return PG_ERR_ARG;
-    // FP64 spreads each block product over 4 warps, FP32 keeps one warp per fibre
-    constexpr int NW = sizeof(R) == 8 ? 4 : 1;
-    const size_t smem = (size_t)TRI_STAGES * (1024 + w * 32) * sizeof(C) + (size_t)(NW + 1) * 32 * sizeof(cx<R>);
-    static bool configured[2][2] = {{false, false}, {false, false}};
-    bool &cfg = configured[lower ? 1 : 0][sizeof(C) == sizeof(R) ? 0 : 1];
-    if (!cfg) {
-        PG_CUDA_TRY(cudaFuncSetAttribute(tri_solve_kernel<R, C, true, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem + 4096));
-        PG_CUDA_TRY(cudaFuncSetAttribute(tri_solve_kernel<R, C, false, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem + 4096));
-        cfg = true;
+    if (w < 1 || w > 32) return PG_ERR_ARG;
+    // FP64 (a quarter of the SM's FP64 rate per sub-partition) wants more warps in flight
+    constexpr int NW = sizeof(R) == 8 ? 16 : 8;
+    const size_t base = (size_t)nblk * 32 * sizeof(cx<R>) + (size_t)nblk * w * sizeof(cx<R>) +
+                        (size_t)nblk * w * w * sizeof(C);
+    const size_t full = base + (size_t)nblk * w * 32 * sizeof(C);
+    const size_t limit = 200 * 1024;
+    if (base > limit) return PG_ERR_SHAPE;  // fibre too long for the shared-memory solve
+    const bool g_in_smem = full <= limit;
+    const size_t smem = g_in_smem ? full : base;
+    static size_t configured[2] = {0, 0};
+    size_t &cfg = configured[sizeof(C) == sizeof(R) ? 0 : 1];
+    if (cfg < smem) {
+        PG_CUDA_TRY(cudaFuncSetAttribute(tri_solve_kernel<R, C, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+        cfg = smem;
     }
-    if (lower)
-        tri_solve_kernel<R, C, true, NW><<<nfib, 32 * NW, smem, ctx->stream>>>(
-            N, nblk, w, (const C *)b->d_lo_inv, (const C *)b->d_lo_cpl, b->nmat > 1, (cx<R> *)x, nfib);
-    else
-        tri_solve_kernel<R, C, false, NW><<<nfib, 32 * NW, smem, ctx->stream>>>(
-            N, nblk, w, (const C *)b->d_up_inv, (const C *)b->d_up_cpl, b->nmat > 1, (cx<R> *)x, nfib);
+    tri_solve_kernel<R, C, NW><<<nfib, 32 * NW, smem, ctx->stream>>>(
+        N, nblk, w, (const C *)b->d_lo_inv, (const C *)b->d_lo_cpl, (const C *)b->d_up_inv, (const C *)b->d_up_cpl,
+        do_lower ? 1 : 0, do_upper ? 1 : 0, b->nmat > 1, g_in_smem ? 1 : 0, (cx<R> *)x, nfib);
     ctx->launches++;
     return pg_check_launch(ctx);
 }
@@ -496,18 +505,16 @@ static int banded_apply_t(pg_banded *bb, int which, void *x)
         return PG_OK;
     case PG_BAND_SOLVE_U:
         if (b->kind != 0) return PG_ERR_STATE;
-        return launch_tri<R, R>(b, false, x);
+        return launch_tri<R, R>(b, false, true, x);
     case PG_BAND_SOLVE_UT:
         if (b->kind != 0) return PG_ERR_STATE;
-        return launch_tri<R, R>(b, true, x);
+        return launch_tri<R, R>(b, true, false, x);
     case PG_BAND_SOLVE_S:
         if (b->kind != 0) return PG_ERR_STATE;
-        PG_TRY(launch_tri<R, R>(b, true, x));
-        return launch_tri<R, R>(b, false, x);
+        return launch_tri<R, R>(b, true, true, x);
     case PG_BAND_PREC_SOLVE:
         if (b->kind != 1) return PG_ERR_STATE;
-        PG_TRY((launch_tri<R, cx<R>>(b, true, x)));
-        return launch_tri<R, cx<R>>(b, false, x);
+        return launch_tri<R, cx<R>>(b, true, true, x);
     default:
         return PG_ERR_ARG;
     }

@@ -38,11 +38,22 @@ struct GmresStats {
     double resid;          // least-squares residual estimate of the last solve
     double true_resid;     // ||(S + i dt/2 H) psi' - b|| in FP64 (mixed; FP64 mode when requested)
     double beta0;          // norm of the preconditioned right-hand side of the last solve
+    long long kernels;     // kernels run by all steps so far (never reset; see the K_* counts)
 };
+
+// Kernels a step runs, counted on the device as the loops decide (one graph launch hides them):
+// FP64 step: scales, matvec, preconditioner solve, norm, init, back-substitution, combine;
+//            + matvec, axpy, norm, record when the true residual is requested;
+// mixed step: scales, matvec; per refinement pass: convert, preconditioner solve, norm, init,
+//            back-substitution, combine, matvec, norm, decide;
+// per GMRES iteration: next vector, matvec, preconditioner solve, multidot, 2 GS updates, Givens.
+static const int K_FP64_BASE = 7, K_TRUE_RESID = 4, K_MIXED_BASE = 2, K_MIXED_PASS = 9, K_ITER = 7;
 
 struct GmresState {
     GmresStats stats;
     int j;            // Krylov vector being expanded in this iteration
+    int cont_inner;   // loop decisions, mirrored for the eager (host-driven) mode
+    int cont_outer;
     int pad;
     double tol_eff;
     double beta_last;
@@ -65,7 +76,7 @@ enum { SC_PLUS = 0, SC_MINUS = 1, SC_DIFF = 2, SC_NEGPLUS = 3, SC_COUNT = 4 };
 // ------------------------------------------------------------------------------------
 // kernels
 // ------------------------------------------------------------------------------------
-__global__ void cay_scales_kernel(const StepParams *__restrict__ p, cxd *__restrict__ sc, GmresState *st)
+__global__ void cay_scales_kernel(const StepParams *__restrict__ p, cxd *__restrict__ sc, GmresState *st, int kernels)
 {
     const int k = threadIdx.x;
     if (k < PG_MAX_SLOTS) {
@@ -91,6 +102,7 @@ __global__ void cay_scales_kernel(const StepParams *__restrict__ p, cxd *__restr
         st->stats.iterations = 0;
         st->stats.passes = 0;
         st->stats.true_resid = -1.0;
+        st->stats.kernels += kernels;
     }
 }
 
@@ -98,7 +110,7 @@ __global__ void cay_scales_kernel(const StepParams *__restrict__ p, cxd *__restr
 template <typename R>
 __global__ void cay_gmres_init_kernel(GmresState *st, const double *__restrict__ nrm, const cx<R> *__restrict__ d,
                                       cx<R> *__restrict__ V0, cx<R> *__restrict__ vcur, long long n, double tol,
-                                      double rel_tol, int maxpass, cudaGraphConditionalHandle inner,
+                                      double rel_tol, int kernels, cudaGraphConditionalHandle inner,
                                       cudaGraphConditionalHandle outer, int has_outer)
 {
     const double b = nrm[1];
@@ -119,8 +131,10 @@ __global__ void cay_gmres_init_kernel(GmresState *st, const double *__restrict__
         st->g[0] = b;
         st->g[1] = 0.0;
         st->stats.passes += 1;
-        cudaGraphSetConditional(inner, b > 0.0 ? 1u : 0u);
-        (void)outer; (void)has_outer; (void)maxpass;
+        st->stats.kernels += kernels;
+        st->cont_inner = b > 0.0 ? 1 : 0;
+        if (has_outer >= 0) cudaGraphSetConditional(inner, st->cont_inner ? 1u : 0u);
+        (void)outer;
     }
 }
 
@@ -147,7 +161,8 @@ __global__ void cay_next_vector_kernel(const GmresState *__restrict__ st, cx<R> 
 // T is the arithmetic precision of the rotations (float for the complex64 inner solve).
 template <typename T>
 __global__ void cay_gmres_finalize_kernel(GmresState *st, const double *__restrict__ h1, const double *__restrict__ h2,
-                                          const double *__restrict__ h3, int m, cudaGraphConditionalHandle inner)
+                                          const double *__restrict__ h3, int m, cudaGraphConditionalHandle inner,
+                                          int use_cond)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int j = st->j;
@@ -205,11 +220,13 @@ __global__ void cay_gmres_finalize_kernel(GmresState *st, const double *__restri
     st->stats.k = J;
     st->stats.resid = resid;
     st->stats.iterations += 1;
+    st->stats.kernels += K_ITER;
     st->beta_last = beta;
     const bool bad = !(resid == resid);
     const bool conv = bad || resid <= st->tol_eff || J >= m || !(beta > 1e-300);
     if (!conv) st->j = j + 1;
-    cudaGraphSetConditional(inner, conv ? 0u : 1u);
+    st->cont_inner = conv ? 0 : 1;
+    if (use_cond) cudaGraphSetConditional(inner, conv ? 0u : 1u);
 }
 
 // y = R^-1 g over the k completed columns (one thread, precision T)
@@ -271,13 +288,14 @@ __global__ void cay_true_resid_kernel(GmresState *st, const double *__restrict__
 
 // end of a refinement pass: record ||r|| (FP64) and repeat while it is above tol
 __global__ void cay_refine_decide_kernel(GmresState *st, const double *__restrict__ nrm, double tol, int maxpass,
-                                         cudaGraphConditionalHandle outer)
+                                         cudaGraphConditionalHandle outer, int use_cond)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double r = nrm[1];
     st->stats.true_resid = r;
     const bool again = (r > tol) && (r == r) && st->stats.passes < maxpass;
-    cudaGraphSetConditional(outer, again ? 1u : 0u);
+    st->cont_outer = again ? 1 : 0;
+    if (use_cond) cudaGraphSetConditional(outer, again ? 1u : 0u);
 }
 
 // ------------------------------------------------------------------------------------
@@ -308,6 +326,9 @@ struct pg_cayley {
     cudaGraphExec_t exec = nullptr;
     void *built_psi = nullptr;
     cudaStream_t cap[3] = {nullptr, nullptr, nullptr};
+    bool eager = false;  // host-driven loops (same kernels; for profilers that cannot see graph loops)
+    int h_flag = 0;
+    long long kernels_counted = 0;  // device kernel count already added to ctx->launches
 };
 
 static int nblocks_for(pg_ctx *ctx, long long n)
@@ -366,8 +387,30 @@ static int capture_iteration(pg_cayley *c, pg_op *op, pg_banded *pre, cudaGraphC
     PG_TRY(pg_multidot<R>(rc, V, n, c->m, w, n, c->h1, &c->st->j));
     PG_TRY(pg_gs_update<R>(rc, V, n, c->m, c->h1, w, n, 1, c->h2, &c->st->j));
     PG_TRY(pg_gs_update<R>(rc, V, n, c->m, c->h2, w, n, 0, c->h3, &c->st->j));
-    cay_gmres_finalize_kernel<T><<<1, 32, 0, s>>>(c->st, c->h1, c->h2, c->h3, c->m, inner);
+    cay_gmres_finalize_kernel<T><<<1, 32, 0, s>>>(c->st, c->h1, c->h2, c->h3, c->m, inner, c->eager ? 0 : 1);
     return pg_check_launch(ctx);
+}
+
+// WHILE loop: a conditional graph node whose body `fn` records on `body_stream`, or, in the
+// eager mode, a host loop on the current stream reading the device flag `flag`.
+template <typename F>
+static int loop_while(pg_cayley *c, cudaGraphConditionalHandle handle, cudaStream_t body_stream, const int *flag, F fn)
+{
+    pg_ctx *ctx = c->ctx;
+    if (!c->eager) {
+        cudaGraph_t body;
+        PG_TRY(capture_while(ctx->stream, handle, &body));
+        return capture_body(c, body_stream, body, fn);
+    }
+    for (int guard = 0; guard < 1000; ++guard) {
+        int v = 0;
+        PG_CUDA_TRY(cudaMemcpyAsync(&c->h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        v = c->h_flag;
+        if (!v) return PG_OK;
+        PG_TRY(fn());
+    }
+    return PG_ERR_NOT_CONVERGED;
 }
 
 // Capture a nested body: begin capture of stream s into `body`, run fn with ctx->stream = s.
@@ -400,20 +443,20 @@ static int record_fp64(pg_cayley *c, cxd *psi)
     memset(&dummy, 0, sizeof(dummy));
     pg_ctx *rc = &c->rctx;
     rc->stream = s0;
-    cay_scales_kernel<<<1, 32, 0, s0>>>(c->params_dev, c->d_sc, c->st);
+    cay_scales_kernel<<<1, 32, 0, s0>>>(c->params_dev, c->d_sc, c->st,
+                                        K_FP64_BASE + (c->true_residual ? K_TRUE_RESID : 0));
     PG_TRY(pg_check_launch(ctx));
     PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_MINUS * PG_MAX_SLOTS, psi, c->b64, 0, nullptr, nullptr));
     PG_CUDA_TRY(cudaMemcpyAsync(c->d64, c->b64, sizeof(cxd) * n, cudaMemcpyDeviceToDevice, s0));
     PG_TRY(pg_banded_apply_dev(c->prec64, PG_BAND_PREC_SOLVE, c->d64));
     PG_TRY(pg_multidot<double>(rc, c->d64, n, 0, c->d64, n, c->nrm));
-    cudaGraphConditionalHandle inner;
-    PG_TRY(capture_handle(s0, &inner, 0, 0));
+    cudaGraphConditionalHandle inner = 0;
+    if (!c->eager) PG_TRY(capture_handle(s0, &inner, 0, 0));
     cay_gmres_init_kernel<double><<<nb, 256, 0, s0>>>(c->st, c->nrm, c->d64, (cxd *)c->V, (cxd *)c->vcur, n, c->tol,
-                                                      0.0, 1, inner, inner, 0);
+                                                      0.0, 0, inner, inner, c->eager ? -1 : 0);
     PG_TRY(pg_check_launch(ctx));
-    cudaGraph_t body;
-    PG_TRY(capture_while(s0, inner, &body));
-    PG_TRY(capture_body(c, c->cap[1], body, [&]() { return capture_iteration<double, double>(c, c->op64, c->prec64, inner); }));
+    PG_TRY(loop_while(c, inner, c->cap[1], &c->st->cont_inner,
+                      [&]() { return capture_iteration<double, double>(c, c->op64, c->prec64, inner); }));
     cay_backsolve_kernel<double><<<1, 32, 0, s0>>>(c->st);
     PG_TRY(pg_check_launch(ctx));
     cay_combine_kernel<double><<<nb, 256, 0, s0>>>((const cxd *)c->V, n, c->st, psi, nullptr);
@@ -442,28 +485,29 @@ static int record_mixed(pg_cayley *c, cxd *psi)
     pg_scales dummy;
     memset(&dummy, 0, sizeof(dummy));
     pg_ctx *rc = &c->rctx;
-    cay_scales_kernel<<<1, 32, 0, s0>>>(c->params_dev, c->d_sc, c->st);
+    cay_scales_kernel<<<1, 32, 0, s0>>>(c->params_dev, c->d_sc, c->st, K_MIXED_BASE);
     PG_TRY(pg_check_launch(ctx));
     PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_DIFF * PG_MAX_SLOTS, psi, c->r64, 0, nullptr, nullptr));
-    cudaGraphConditionalHandle outer;
-    PG_TRY(capture_handle(s0, &outer, 1, cudaGraphCondAssignDefault));
-    cudaGraph_t obody;
-    PG_TRY(capture_while(s0, outer, &obody));
-    PG_TRY(capture_body(c, c->cap[1], obody, [&]() -> int {
+    cudaGraphConditionalHandle outer = 0;
+    if (!c->eager) {
+        PG_TRY(capture_handle(s0, &outer, 1, cudaGraphCondAssignDefault));
+    } else {
+        PG_CUDA_TRY(cudaMemsetAsync(&c->st->cont_outer, 0xff, sizeof(int), s0));  // first pass always runs
+    }
+    PG_TRY(loop_while(c, outer, c->cap[1], &c->st->cont_outer, [&]() -> int {
         cudaStream_t s1 = ctx->stream;
         cxf *dconv = (cxf *)c->dconv;
         PG_TRY((pg_scale_copy<float, double>(ctx, c->r64, dconv, nullptr, n, nullptr, 1.0)));
         PG_TRY(pg_banded_apply_dev(c->precb, PG_BAND_PREC_SOLVE, dconv));
         rc->stream = s1;
         PG_TRY(pg_multidot<float>(rc, dconv, n, 0, dconv, n, c->nrm));
-        cudaGraphConditionalHandle inner;
-        PG_TRY(capture_handle(s1, &inner, 0, 0));
+        cudaGraphConditionalHandle inner = 0;
+        if (!c->eager) PG_TRY(capture_handle(s1, &inner, 0, 0));
         cay_gmres_init_kernel<float><<<nb, 256, 0, s1>>>(c->st, c->nrm, dconv, (cxf *)c->V, (cxf *)c->vcur, n, c->tol,
-                                                         2e-6, 4, inner, outer, 1);
+                                                         2e-6, K_MIXED_PASS, inner, outer, c->eager ? -1 : 1);
         PG_TRY(pg_check_launch(ctx));
-        cudaGraph_t ibody;
-        PG_TRY(capture_while(s1, inner, &ibody));
-        PG_TRY(capture_body(c, c->cap[2], ibody, [&]() { return capture_iteration<float, float>(c, c->opb, c->precb, inner); }));
+        PG_TRY(loop_while(c, inner, c->cap[2], &c->st->cont_inner,
+                          [&]() { return capture_iteration<float, float>(c, c->opb, c->precb, inner); }));
         cay_backsolve_kernel<float><<<1, 32, 0, s1>>>(c->st);
         PG_TRY(pg_check_launch(ctx));
         cay_combine_kernel<float><<<nb, 256, 0, s1>>>((const cxf *)c->V, n, c->st, c->e64, psi);
@@ -472,7 +516,7 @@ static int record_mixed(pg_cayley *c, cxd *psi)
         PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_NEGPLUS * PG_MAX_SLOTS, c->e64, c->r64, 1, nullptr, nullptr));
         rc->stream = s1;
         PG_TRY(pg_multidot<double>(rc, c->r64, n, 0, c->r64, n, c->nrm2));
-        cay_refine_decide_kernel<<<1, 32, 0, s1>>>(c->st, c->nrm2, c->tol, 4, outer);
+        cay_refine_decide_kernel<<<1, 32, 0, s1>>>(c->st, c->nrm2, c->tol, 4, outer, c->eager ? 0 : 1);
         return pg_check_launch(ctx);
     }));
     PG_CUDA_TRY(cudaMemcpyAsync(c->h_stats, &c->st->stats, sizeof(GmresStats), cudaMemcpyDeviceToHost, s0));
@@ -580,11 +624,18 @@ extern "C" int pg_cayley_destroy(pg_cayley *c)
     return PG_OK;
 }
 
-// one step: upload this step's H(t+dt/2) slot values, launch the graph
+// one step: upload this step's H(t+dt/2) slot values, launch the graph (or, in the eager
+// mode, run the same kernels with the loops on the host)
 static int cayley_launch(pg_cayley *c, cxd *psi, double dt, const double *scales, int nscales)
 {
     pg_ctx *ctx = c->ctx;
-    if (!c->exec || c->built_psi != psi) PG_TRY(build_graph(c, psi));
+    // kernels are counted on the device (GmresStats::kernels), not while recording
+    const long long launches = ctx->launches;
+    if (!c->eager && (!c->exec || c->built_psi != psi)) {
+        const int code = build_graph(c, psi);
+        ctx->launches = launches;
+        PG_TRY(code);
+    }
     const int slot = c->ring_pos;
     c->ring_pos = (c->ring_pos + 1) % RING;
     if (c->ring_used[slot]) PG_CUDA_TRY(cudaEventSynchronize(c->ring_ev[slot]));
@@ -595,21 +646,23 @@ static int cayley_launch(pg_cayley *c, cxd *psi, double dt, const double *scales
     PG_CUDA_TRY(cudaMemcpyAsync(c->d_params, &p, sizeof(StepParams), cudaMemcpyHostToDevice, ctx->stream));
     PG_CUDA_TRY(cudaEventRecord(c->ring_ev[slot], ctx->stream));
     c->ring_used[slot] = true;
+    if (c->eager) {
+        c->rctx.stream = ctx->stream;
+        const int code = (c->prec == PG_FP64) ? record_fp64(c, psi) : record_mixed(c, psi);
+        ctx->launches = launches;
+        return code;
+    }
     PG_CUDA_TRY(cudaGraphLaunch(c->exec, ctx->stream));
     return PG_OK;
 }
 
-// Kernels one graph launch ran, from its iteration and pass counts:
-// FP64 8 + 8k (+4 with the true residual); mixed 4 + 8 passes + 8 iterations.
-static long long step_kernels(const pg_cayley *c, const GmresStats &g)
-{
-    if (c->prec == PG_FP64) return 8 + 8 * g.iterations + (c->true_residual ? 4 : 0);
-    return 2 + 10LL * g.passes + 8 * g.iterations;
-}
-
+// statistics of the last completed step; adds the kernels run since the last call to the
+// context's launch count
 static void fill_stats(pg_cayley *c, pg_krylov_stats *st)
 {
     const GmresStats &g = *c->h_stats;
+    c->ctx->launches += g.kernels - c->kernels_counted;
+    c->kernels_counted = g.kernels;
     st->Iterations = g.iterations;
     st->OpCount = g.iterations;
     st->InnerProductCount = 2 * g.iterations;
@@ -626,8 +679,14 @@ extern "C" int pg_cayley_step(pg_cayley *c, void *psi, double dt, const double *
     if (st) {
         PG_CUDA_TRY(cudaStreamSynchronize(c->ctx->stream));
         fill_stats(c, st);
-        c->ctx->launches += step_kernels(c, *c->h_stats);
     }
+    return PG_OK;
+}
+
+extern "C" int pg_cayley_set_eager(pg_cayley *c, int on)
+{
+    if (!c) return PG_ERR_ARG;
+    c->eager = on != 0;
     return PG_OK;
 }
 
@@ -774,7 +833,12 @@ extern "C" int pg_cayley_batch_step(pg_cayley_batch *b, void **psis, double dt, 
     const int n = (int)b->members.size();
     bool same = b->exec && (int)b->psis.size() == n;
     for (int k = 0; same && k < n; ++k) same = (b->psis[k] == psis[k]);
-    if (!same) PG_TRY(batch_build(b, psis));
+    if (!same) {
+        const long long launches = b->ctx->launches;  // counted on the device, not while recording
+        const int code = batch_build(b, psis);
+        b->ctx->launches = launches;
+        PG_TRY(code);
+    }
     if (b->params_pending) PG_CUDA_TRY(cudaEventSynchronize(b->params_done));
     for (int k = 0; k < n; ++k) {
         StepParams &p = b->h_params[k];
@@ -796,11 +860,6 @@ extern "C" int pg_cayley_batch_stats(pg_cayley_batch *b, pg_krylov_stats *stats)
 {
     if (!b || !stats) return PG_ERR_ARG;
     PG_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
-    long long kernels = 0;
-    for (size_t k = 0; k < b->members.size(); ++k) {
-        fill_stats(b->members[k], &stats[k]);
-        kernels += step_kernels(b->members[k], *b->members[k]->h_stats);
-    }
-    b->ctx->launches += kernels;
+    for (size_t k = 0; k < b->members.size(); ++k) fill_stats(b->members[k], &stats[k]);
     return PG_OK;
 }

@@ -204,19 +204,137 @@ static pg_scales to_scales(const double *s, int n)
 // ------------------------------------------------------------------------------------
 // pAMP
 // ------------------------------------------------------------------------------------
+// A step is two CUDA graphs and one host round trip:
+//   graph 1: psi <- U psi, ||psi||, V[0] = psi/||psi||, then m Arnoldi steps on
+//            U^-H H(t) U^-1 (solve, matvec, solve, CGS2), Hessenberg columns to pinned memory;
+//   host:    exp(-i dt H_m) e1 in FP64 (Hermitian tridiagonal H_m: eigen-decomposition by
+//            implicit QL; otherwise the reference's scaled Pade of order 6);
+//   graph 2: coefficients to the device, psi = ||psi|| V c, psi <- U^-1 psi.
+// A happy breakdown (beta < sqrt(eps), pamp.h:306-313) truncates the basis on the host; the
+// device normalisation maps a zero norm to a zero vector, so the extra rows stay finite and
+// get zero coefficients.
+namespace dense {
+
+// symmetric tridiagonal eigen-decomposition (implicit QL with Wilkinson shifts):
+// d (diagonal), e (sub-diagonal, e[n-1] unused); on return d holds the eigenvalues and
+// z (row-major n x n, column k = eigenvector k). Returns false if it did not converge.
+bool tridiag_ql(int n, std::vector<double> &d, std::vector<double> &e, std::vector<double> &z)
+{
+    z.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) z[(size_t)i * n + i] = 1.0;
+    e.resize(n);
+    e[n - 1] = 0.0;
+    for (int l = 0; l < n; ++l) {
+        int iter = 0;
+        int mm;
+        do {
+            for (mm = l; mm < n - 1; ++mm) {
+                const double dd = std::fabs(d[mm]) + std::fabs(d[mm + 1]);
+                if (std::fabs(e[mm]) <= 1e-16 * dd) break;
+            }
+            if (mm != l) {
+                if (++iter > 60) return false;
+                // Wilkinson shift from the 2x2 block at l
+                double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+                double r = std::hypot(g, 1.0);
+                g = d[mm] - d[l] + e[l] / (g + (g >= 0 ? r : -r));
+                double sn = 1.0, cn = 1.0, p = 0.0;
+                int i;
+                for (i = mm - 1; i >= l; --i) {
+                    double f = sn * e[i];
+                    const double b = cn * e[i];
+                    r = std::hypot(f, g);
+                    e[i + 1] = r;
+                    if (r == 0.0) {
+                        d[i + 1] -= p;
+                        e[mm] = 0.0;
+                        break;
+                    }
+                    sn = f / r;
+                    cn = g / r;
+                    g = d[i + 1] - p;
+                    r = (d[i] - g) * sn + 2.0 * cn * b;
+                    p = sn * r;
+                    d[i + 1] = g + p;
+                    g = cn * r - b;
+                    for (int k = 0; k < n; ++k) {
+                        f = z[(size_t)k * n + i + 1];
+                        z[(size_t)k * n + i + 1] = sn * z[(size_t)k * n + i] + cn * f;
+                        z[(size_t)k * n + i] = cn * z[(size_t)k * n + i] - sn * f;
+                    }
+                }
+                if (r == 0.0 && i >= l) continue;
+                d[l] -= p;
+                e[l] = g;
+                e[mm] = 0.0;
+            }
+        } while (mm != l);
+    }
+    return true;
+}
+
+// first column of exp(-i dt H) for a k x k upper Hessenberg H (row-major)
+bool expm_first_column(int k, const std::vector<zd> &H, double dt, std::vector<zd> &c, bool *hermitian_used)
+{
+    double hmax = 0.0;
+    for (const zd &v : H) hmax = std::max(hmax, std::abs(v));
+    const double tol = 1e-10 * std::max(hmax, 1e-300);
+    bool herm = true;
+    for (int i = 0; i < k && herm; ++i) {
+        if (std::fabs(H[(size_t)i * k + i].imag()) > tol) herm = false;
+        for (int j = i + 2; j < k && herm; ++j)
+            if (std::abs(H[(size_t)i * k + j]) > tol) herm = false;
+        if (i + 1 < k) {
+            const zd up = H[(size_t)i * k + i + 1], lo = H[(size_t)(i + 1) * k + i];
+            if (std::abs(up - std::conj(lo)) > tol || std::fabs(lo.imag()) > tol) herm = false;
+        }
+    }
+    c.assign(k, zd(0.0, 0.0));
+    if (herm) {
+        std::vector<double> d(k), e(k, 0.0), z;
+        for (int i = 0; i < k; ++i) d[i] = H[(size_t)i * k + i].real();
+        for (int i = 0; i + 1 < k; ++i) e[i] = 0.5 * (H[(size_t)(i + 1) * k + i].real() + H[(size_t)i * k + i + 1].real());
+        if (tridiag_ql(k, d, e, z)) {
+            for (int q = 0; q < k; ++q) {
+                const zd ph = std::exp(zd(0.0, -dt * d[q])) * z[q];  // z[0][q] = first component
+                for (int i = 0; i < k; ++i) c[i] += z[(size_t)i * k + q] * ph;
+            }
+            if (hermitian_used) *hermitian_used = true;
+            return true;
+        }
+    }
+    if (hermitian_used) *hermitian_used = false;
+    std::vector<zd> A((size_t)k * k), E((size_t)k * k);
+    for (size_t q = 0; q < A.size(); ++q) A[q] = zd(0.0, -dt) * H[q];
+    if (!expm_pade(k, A.data(), E.data(), 6)) return false;
+    for (int i = 0; i < k; ++i) c[i] = E[(size_t)i * k];
+    return true;
+}
+
+}  // namespace dense
+
 struct pg_pamp {
     pg_op *op64 = nullptr, *opb = nullptr;
     pg_banded *ovl64 = nullptr, *ovlb = nullptr;
+    pg_ctx *ctx = nullptr;
+    pg_ctx rctx;  // private reduction scratch
     int m = 0, prec = PG_FP64, double_ortho = 1;
     long long n = 0;
     void *V = nullptr;    // [m][n] basis precision
     void *w = nullptr;    // [n] basis precision
     void *tmp = nullptr;  // [n] basis precision
     double *d_c = nullptr;
-    double *h_c = nullptr;
-    double *d_norm = nullptr;  // 2 doubles: ||psi||^2, ||psi||
+    double *h_c = nullptr;       // pinned [2m]
+    double *d_norm = nullptr;    // ||psi||^2, ||psi||
+    cxd *d_scales = nullptr;     // [PG_MAX_SLOTS]
+    cxd *h_scales = nullptr;     // pinned
     ArnoldiBuf ab;
     double tolerance = std::sqrt(std::numeric_limits<double>::epsilon());
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t g1 = nullptr, g2 = nullptr;
+    void *built_psi = nullptr;
+    bool last_hermitian = false;
+    long long kernels_per_step = 0;  // kernel nodes of the two graphs
 };
 
 extern "C" int pg_pamp_create(pg_op *op64, pg_op *op_basis, pg_banded *ovl64, pg_banded *ovl_basis, int basis_size,
@@ -232,18 +350,26 @@ extern "C" int pg_pamp_create(pg_op *op64, pg_op *op_basis, pg_banded *ovl64, pg
     p->opb = op_basis;
     p->ovl64 = ovl64;
     p->ovlb = ovl_basis;
+    p->ctx = op64->ctx;
     p->m = basis_size;
     p->prec = basis_precision;
     p->double_ortho = double_ortho ? 1 : 0;
     p->n = (long long)op64->nrows * op64->N;
     const size_t esz = basis_precision == PG_FP64 ? sizeof(cxd) : sizeof(cxf);
     PG_CUDA_TRY(cudaMalloc(&p->V, esz * (size_t)p->m * p->n));
+    PG_CUDA_TRY(cudaMemset(p->V, 0, esz * (size_t)p->m * p->n));
     PG_CUDA_TRY(cudaMalloc(&p->w, esz * (size_t)p->n));
     PG_CUDA_TRY(cudaMalloc(&p->tmp, esz * (size_t)p->n));
     PG_CUDA_TRY(cudaMalloc(&p->d_c, sizeof(double) * 2 * p->m));
     PG_CUDA_TRY(cudaMallocHost(&p->h_c, sizeof(double) * 2 * p->m));
     PG_CUDA_TRY(cudaMalloc(&p->d_norm, sizeof(double) * 2 * (PG_RED_COLS)));
+    PG_CUDA_TRY(cudaMalloc(&p->d_scales, sizeof(cxd) * PG_MAX_SLOTS));
+    PG_CUDA_TRY(cudaMallocHost(&p->h_scales, sizeof(cxd) * PG_MAX_SLOTS));
     PG_TRY(p->ab.alloc(p->m));
+    p->rctx.device = p->ctx->device;
+    p->rctx.num_sms = p->ctx->num_sms;
+    PG_TRY(pg_ctx_ensure_reduction(&p->rctx));
+    PG_CUDA_TRY(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking));
     *out = p;
     return PG_OK;
 }
@@ -251,65 +377,120 @@ extern "C" int pg_pamp_create(pg_op *op64, pg_op *op_basis, pg_banded *ovl64, pg
 extern "C" int pg_pamp_destroy(pg_pamp *p)
 {
     if (!p) return PG_ERR_ARG;
+    cudaStreamSynchronize(p->ctx->stream);
+    if (p->g1) cudaGraphExecDestroy(p->g1);
+    if (p->g2) cudaGraphExecDestroy(p->g2);
+    if (p->cap) cudaStreamDestroy(p->cap);
     cudaFree(p->V);
     cudaFree(p->w);
     cudaFree(p->tmp);
     cudaFree(p->d_c);
     if (p->h_c) cudaFreeHost(p->h_c);
     cudaFree(p->d_norm);
+    cudaFree(p->d_scales);
+    if (p->h_scales) cudaFreeHost(p->h_scales);
+    cudaFree(p->rctx.red_partial);
+    cudaFree(p->rctx.red_counter);
+    cudaFree(p->rctx.red_out);
+    cudaFree(p->rctx.d_err);
+    if (p->rctx.h_pinned) cudaFreeHost(p->rctx.h_pinned);
     p->ab.release();
     delete p;
     return PG_OK;
 }
 
 template <typename R>
-static int pamp_arnoldi(pg_pamp *p, const pg_scales &sc, pg_krylov_stats *st)
+static int pamp_record_arnoldi(pg_pamp *p, cxd *x)
 {
-    pg_ctx *ctx = p->op64->ctx;
+    pg_ctx *ctx = p->ctx;
+    pg_ctx *rc = &p->rctx;
+    rc->stream = ctx->stream;
     const long long n = p->n;
     cx<R> *V = (cx<R> *)p->V;
     cx<R> *w = (cx<R> *)p->w;
     cx<R> *tmp = (cx<R> *)p->tmp;
+    pg_scales dummy;
+    memset(&dummy, 0, sizeof(dummy));
+    PG_TRY(pg_banded_apply_dev(p->ovl64, PG_BAND_MUL_U, x));
+    PG_TRY(pg_multidot<double>(rc, x, n, 0, x, n, p->d_norm));
+    PG_TRY((pg_scale_copy<R, double>(ctx, x, V, tmp, n, p->d_norm + 1, 1.0)));
     for (int j = 0; j < p->m; ++j) {
-        if (j > 0) {
-            // V[j] = f / beta_{j-1}; tmp = V[j]
-            PG_TRY((pg_scale_copy<R, R>(ctx, w, V + (size_t)j * n, tmp, n, p->ab.dcol(j - 1, 2) + 2 * j + 1, 1.0)));
-        } else {
-            PG_CUDA_TRY(cudaMemcpyAsync(tmp, V, sizeof(cx<R>) * n, cudaMemcpyDeviceToDevice, ctx->stream));
-        }
+        if (j > 0) PG_TRY((pg_scale_copy<R, R>(ctx, w, V + (size_t)j * n, tmp, n, p->ab.dcol(j - 1, 2) + 2 * j + 1, 1.0)));
         // w = U^-H H U^-1 V[j]
         PG_TRY(pg_banded_apply_dev(p->ovlb, PG_BAND_SOLVE_U, tmp));
-        PG_TRY(pg_op_matvec_dev(p->opb, sc, nullptr, tmp, w, 0, nullptr, nullptr));
+        PG_TRY(pg_op_matvec_dev(p->opb, dummy, p->d_scales, tmp, w, 0, nullptr, nullptr));
         PG_TRY(pg_banded_apply_dev(p->ovlb, PG_BAND_SOLVE_UT, w));
-        if (st) st->OpCount++;
-        PG_TRY(cgs2<R>(ctx, V, n, j + 1, w, p->ab, j, p->double_ortho, st));
+        PG_TRY(cgs2<R>(rc, V, n, j + 1, w, p->ab, j, p->double_ortho, nullptr));
+    }
+    const size_t cnt = (size_t)p->m * 3 * p->ab.col_doubles();
+    PG_CUDA_TRY(cudaMemcpyAsync(p->ab.h_cols, p->ab.d_cols, cnt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA_TRY(cudaMemcpyAsync(rc->h_pinned, p->d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    return PG_OK;
+}
+
+template <typename R>
+static int pamp_record_finish(pg_pamp *p, cxd *x)
+{
+    pg_ctx *ctx = p->ctx;
+    PG_CUDA_TRY(cudaMemcpyAsync(p->d_c, p->h_c, sizeof(double) * 2 * p->m, cudaMemcpyHostToDevice, ctx->stream));
+    PG_TRY(pg_combine<R>(ctx, (const cx<R> *)p->V, p->n, p->m, p->d_c, 1.0, x, p->n, 0));
+    return pg_banded_apply_dev(p->ovl64, PG_BAND_SOLVE_U, x);
+}
+
+static int pamp_capture(pg_pamp *p, cxd *x, bool first, cudaGraphExec_t *out)
+{
+    pg_ctx *ctx = p->ctx;
+    cudaStream_t saved = ctx->stream;
+    // the helpers count the kernels they record; keep that count per step instead
+    const long long l0 = ctx->launches, r0 = p->rctx.launches;
+    PG_CUDA_TRY(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
+    ctx->stream = p->cap;
+    int code;
+    if (first) code = (p->prec == PG_FP64) ? pamp_record_arnoldi<double>(p, x) : pamp_record_arnoldi<float>(p, x);
+    else code = (p->prec == PG_FP64) ? pamp_record_finish<double>(p, x) : pamp_record_finish<float>(p, x);
+    ctx->stream = saved;
+    p->kernels_per_step += (ctx->launches - l0) + (p->rctx.launches - r0);
+    ctx->launches = l0;
+    p->rctx.launches = r0;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(p->cap, &g);
+    if (code != PG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return code;
+    }
+    if (e != cudaSuccess) {
+        pg_set_last_error(e, "cudaStreamEndCapture(pamp)", __FILE__, __LINE__);
+        return PG_ERR_CUDA;
+    }
+    cudaError_t ie = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        pg_set_last_error(ie, "cudaGraphInstantiate(pamp)", __FILE__, __LINE__);
+        return PG_ERR_CUDA;
     }
     return PG_OK;
 }
 
 extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scales, int nscales, pg_krylov_stats *st)
 {
-    if (!p || !psi || nscales < 0 || nscales > PG_MAX_SLOTS) return PG_ERR_ARG;
-    pg_ctx *ctx = p->op64->ctx;
-    const long long n = p->n;
+    if (!p || !psi || nscales < 0 || nscales > PG_MAX_SLOTS || (nscales > 0 && !scales)) return PG_ERR_ARG;
+    pg_ctx *ctx = p->ctx;
     const int m = p->m;
-    const pg_scales sc = to_scales(scales, nscales);
     cxd *x = (cxd *)psi;
-    // psi <- U psi; ||psi||
-    PG_TRY(pg_banded_apply_dev(p->ovl64, PG_BAND_MUL_U, x));
-    PG_TRY(pg_multidot<double>(ctx, x, n, 0, x, n, p->d_norm));
-    // V[0] = psi / ||psi||
-    if (p->prec == PG_FP64) {
-        PG_TRY((pg_scale_copy<double, double>(ctx, x, (cxd *)p->V, nullptr, n, p->d_norm + 1, 1.0)));
-        PG_TRY(pamp_arnoldi<double>(p, sc, st));
-    } else {
-        PG_TRY((pg_scale_copy<float, double>(ctx, x, (cxf *)p->V, nullptr, n, p->d_norm + 1, 1.0)));
-        PG_TRY(pamp_arnoldi<float>(p, sc, st));
+    if (p->built_psi != psi) {
+        if (p->g1) { cudaGraphExecDestroy(p->g1); p->g1 = nullptr; }
+        if (p->g2) { cudaGraphExecDestroy(p->g2); p->g2 = nullptr; }
+        p->kernels_per_step = 0;
+        PG_TRY(pamp_capture(p, x, true, &p->g1));
+        PG_TRY(pamp_capture(p, x, false, &p->g2));
+        p->built_psi = psi;
     }
-    PG_TRY(fetch_columns(ctx, p->ab, 0, m));
-    PG_CUDA_TRY(cudaMemcpyAsync(ctx->h_pinned, p->d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    for (int k = 0; k < PG_MAX_SLOTS; ++k)
+        p->h_scales[k] = mk<double>(k < nscales ? scales[2 * k] : 0.0, k < nscales ? scales[2 * k + 1] : 0.0);
+    PG_CUDA_TRY(cudaMemcpyAsync(p->d_scales, p->h_scales, sizeof(cxd) * PG_MAX_SLOTS, cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA_TRY(cudaGraphLaunch(p->g1, ctx->stream));
     PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    const double norm_h = ctx->h_pinned[1];
+    const double norm_h = p->rctx.h_pinned[1];
     // Hessenberg (row-major), truncated at a happy breakdown
     std::vector<zd> H((size_t)m * m, zd(0.0, 0.0));
     int k = m;
@@ -323,19 +504,24 @@ extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scal
             H[(size_t)(j + 1) * m + j] = beta;
         }
     }
-    std::vector<zd> A((size_t)k * k), E((size_t)k * k);
+    std::vector<zd> Hk((size_t)k * k), c;
     for (int i = 0; i < k; ++i)
-        for (int j = 0; j < k; ++j) A[(size_t)i * k + j] = zd(0.0, -dt) * H[(size_t)i * m + j];
-    if (!dense::expm_pade(k, A.data(), E.data(), 6)) return PG_ERR_BREAKDOWN;
-    for (int i = 0; i < k; ++i) {
-        p->h_c[2 * i] = E[(size_t)i * k].real();
-        p->h_c[2 * i + 1] = E[(size_t)i * k].imag();
+        for (int j = 0; j < k; ++j) Hk[(size_t)i * k + j] = H[(size_t)i * m + j];
+    if (!dense::expm_first_column(k, Hk, dt, c, &p->last_hermitian)) return PG_ERR_BREAKDOWN;
+    for (int i = 0; i < m; ++i) {
+        const zd v = i < k ? c[i] * norm_h : zd(0.0, 0.0);
+        p->h_c[2 * i] = v.real();
+        p->h_c[2 * i + 1] = v.imag();
     }
-    if (st) st->ErrorEstimate = std::norm(E[(size_t)(k - 1) * k]);
-    PG_CUDA_TRY(cudaMemcpyAsync(p->d_c, p->h_c, sizeof(double) * 2 * k, cudaMemcpyHostToDevice, ctx->stream));
-    if (p->prec == PG_FP64) PG_TRY(pg_combine<double>(ctx, (const cxd *)p->V, n, k, p->d_c, norm_h, x, n, 0));
-    else PG_TRY(pg_combine<float>(ctx, (const cxf *)p->V, n, k, p->d_c, norm_h, x, n, 0));
-    PG_TRY(pg_banded_apply_dev(p->ovl64, PG_BAND_SOLVE_U, x));
+    PG_CUDA_TRY(cudaGraphLaunch(p->g2, ctx->stream));
+    ctx->launches += p->kernels_per_step;
+    if (st) {
+        st->OpCount += m;
+        st->InnerProductCount += (p->double_ortho ? 2 : 1) * m;
+        st->ReOrthoCount += p->double_ortho ? m : 0;
+        st->ErrorEstimate = std::norm(c[k - 1]);
+        st->Iterations = k;
+    }
     return PG_OK;
 }
 

@@ -171,7 +171,8 @@ struct pg_banded {
     // overlap: U upper Cholesky factor rows (real) for multiplies, lower = U^T
     void *d_U = nullptr;     // [N][kb+1]  U(i, i+j) at [i][j]   (real, precision of op)
     void *d_S = nullptr;     // [N][2kb+1] S rows (real)
-    // blocked solves
+    // blocked solves: inverse 32x32 diagonal blocks and the coupling G = T^-1 C to the
+    // neighbouring block's kb boundary values
     void *d_lo_inv = nullptr, *d_lo_cpl = nullptr;   // lower factor (U^T or L)
     void *d_up_inv = nullptr, *d_up_cpl = nullptr;   // upper factor (U)
     int complex_coef = 0;

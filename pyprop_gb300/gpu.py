@@ -259,6 +259,10 @@ class CayleyStepper:
         check(self.lib.pg_cayley_last_stats(self.h, C.byref(self.stats)), "pg_cayley_last_stats")
         return self.stats
 
+    def set_eager(self, on):
+        """Host-driven loops instead of the graph's conditional nodes (for profilers)."""
+        check(self.lib.pg_cayley_set_eager(self.h, int(bool(on))), "pg_cayley_set_eager")
+
     def __del__(self):
         try:
             if getattr(self, "h", None):

@@ -231,6 +231,7 @@ class CayleyPropagatorGPU(PropagatorBase):
         self.Precision = precision_of(getattr(conf, "gpu_precision", "fp64"))
         self.StepStats = bool(getattr(conf, "gpu_step_stats", True))
         self.TrueResidual = bool(getattr(conf, "gpu_true_residual", False))
+        self.Eager = bool(getattr(conf, "gpu_eager", False))
         name = getattr(conf, "preconditioner", None)
         self.Preconditioner = None
         if name:
@@ -255,6 +256,8 @@ class CayleyPropagatorGPU(PropagatorBase):
         self.stepper = CayleyStepper(self.op64, self.opb, self.Preconditioner.solvers[nat.PG_FP64],
                                      self.Preconditioner.solvers[self.Precision], self.BasisSize, self.Precision,
                                      self.Tolerance, self.TrueResidual)
+        if self.Eager:
+            self.stepper.set_eager(True)
 
     def AdvanceStep(self, t, dt):
         """One step at H(t + |dt|/2). With ``gpu_step_stats`` (default) the call waits for the
