@@ -104,17 +104,34 @@ int pg_tensor_multiply_ident_bandnh(const double *potential, int potExtent0, int
  */
 typedef struct pg_op pg_op;
 
-/* shape: rank-2 {Nang, N}. bandCount k: the radial band has 2k+1 diagonals. */
+/* shape: rank-2 {Nang, N} or rank-3 {Nang, N, N}. bandCount k: the band of the last
+ * (fibre) rank has 2k+1 diagonals. */
 int pg_op_create(pg_ctx *ctx, int rank, const int *shape, int bandCount, int precision, pg_op **out);
 int pg_op_destroy(pg_op *op);
 /*
- * Add one term. storage: "Diag_BandNH", "Simp_BandNH" or "Ident_BandNH".
+ * Add one term. storage: "<angular>_<radial>" as in the names of the reference's generated
+ * kernels (core/tensorpotential/tensorpotentialmultiply_generator.py:1336-1346):
+ *   angular Simp, Herm, Diag, Ident, Band, BandNH, Dense; radial BandNH, Band, Dense,
+ *   Diag, Ident. Extents: potExtent0 = npairs (Simp, Herm), Nang (Diag), 1 (Ident),
+ *   Nang*bandCount (Band, BandNH), Nang^2 (Dense); potExtent1 = N(2k+1) (BandNH), N(k+1)
+ *   (Band), N^2 (Dense), N (Diag), 1 (Ident).
  * potential: host complex128 [potExtent0][potExtent1] in the reference layout.
- * pairs0: host int32 [npairs0][2] (row, col) for Simp (ignored otherwise).
+ * pairs0: host int32 [npairs0][2] (row, col) for Simp and Herm (ignored otherwise).
  * slot: which scale multiplies this term (0 <= slot < 16).
+ * Returns PG_ERR_STORAGE for other ids and PG_ERR_SHAPE for extents that do not match.
  */
 int pg_op_add_term(pg_op *op, const char *storage, const double *potential, int potExtent0,
                    int potExtent1, const int *pairs0, int npairs0, int slot);
+/*
+ * Rank-general form (rank-2 and rank-3 operators; rank 3 is the two-electron layout
+ * [Nang][N][N] of core/tensorpotential/tensorpotentialmultiply_generator.py's rank-3
+ * kernels such as Diag_Simp_BandNH and Simp_Simp_BandNH). storage "<r0>_<r1>[_<r2>]";
+ * extents[rank] as pg_op_add_term (Simp on the last rank: a pair list within or beyond the
+ * band); pairs: the (row, col) lists of all Simp/Herm ranks concatenated in rank order,
+ * npairs[rank] their lengths (0 for other ranks).
+ */
+int pg_op_add_term_ranks(pg_op *op, const char *storage, const double *potential, const int *extents,
+                         const int *pairs, const int *npairs, int slot);
 /* Upload. Must be called once after the last add_term. */
 int pg_op_finalize(pg_op *op);
 /* Number of complex band elements the operator stores (for roofline bookkeeping). */

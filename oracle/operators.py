@@ -1,10 +1,10 @@
 """Oracle operators (complex128, CPU) - test infrastructure only.
 
-* ``tensor_multiply``: the generated TensorPotentialMultiply_<Diag|Simp|Ident>_BandNH
-  (core/tensorpotential/tensorpotentialmultiply_generator.py:302-462 storage loops,
-  :622-762 BandNH body calling zgbmv at :702-724): for each angular pair
-  dest[row, :] += scaling * A_pair @ src[col, :], A_pair general banded with the BLAS
-  layout slot j*(2k+1) + (k+i-j) (GeometryInfo.py:437-456).
+* ``tensor_multiply``: the generated TensorPotentialMultiply_<angular>_<radial> kernels
+  (core/tensorpotential/tensorpotentialmultiply_generator.py: angular storage loops
+  :302-462, :467-618, :622-762, :1227-1330; radial bodies zgbmv :702-724, zhbmv :585-600,
+  dense loop :1268-1275): for each angular block dest[row, :] += scaling * A @ src[col, :],
+  BandNH blocks in the BLAS layout slot j*(2k+1) + (k+i-j) (GeometryInfo.py:437-456).
 * ``Overlap``: OverlapMatrix (core/representation/overlapmatrix.cpp): upper banded Cholesky
   S = U^H U (zpbtrf, :35-37) and the vector operations (:123-149) on every radial fibre.
 * ``BandLU``: BSplineSolver's banded LU with partial pivoting (zgbtrf/zgbtrs,
@@ -30,42 +30,135 @@ def bandnh_rows(potential_row, N, kb):
     return out
 
 
+def outer_blocks(kind, e0, pairs, nang):
+    """Angular-rank loops of the generated multiply kernels: list of (row, col, index, conj).
+
+    Simp (tensorpotentialmultiply_generator.py:326-333), Herm (:380-386, second pass with
+    row/col swapped and the potential conjugated), Diag (:416-421), Ident (:448-453, index 0
+    for every row), Band (:507-552: (row, col >= row) at row*bc + col - row, then the mirrored
+    (col, row) conjugated), BandNH (:662-694: (row, col) at col*bc + sub + row - col), Dense
+    (:1268-1275: row*n + col)."""
+    out = []
+    if kind in ("Simp", "Herm"):
+        pairs = np.asarray(pairs).reshape(-1, 2)
+        out += [(int(r), int(c), p, False) for p, (r, c) in enumerate(pairs)]
+        if kind == "Herm":
+            out += [(int(c), int(r), p, True) for p, (r, c) in enumerate(pairs)]
+    elif kind == "Diag":
+        out += [(a, a, a, False) for a in range(nang)]
+    elif kind == "Ident":
+        out += [(a, a, 0, False) for a in range(nang)]
+    elif kind == "Dense":
+        out += [(r, c, r * nang + c, False) for r in range(nang) for c in range(nang)]
+    elif kind == "Band":
+        bc = e0 // nang
+        i = 0
+        for row in range(nang):  # first pass: upper part, row-major, bc slots per row
+            for col in range(row, row + bc):
+                if col < nang:
+                    out.append((row, col, i, False))
+                i += 1
+        i = 0
+        for herm_row in range(nang):  # mirrored part, diagonal slot skipped
+            i += 1
+            for herm_col in range(herm_row + 1, herm_row + bc):
+                if herm_col < nang:
+                    out.append((herm_col, herm_row, i, True))
+                i += 1
+    elif kind == "BandNH":
+        bc = e0 // nang
+        sub = (bc - 1) // 2
+        for col in range(nang):
+            for row in range(max(0, col - sub), min(nang, col + sub + 1)):
+                out.append((row, col, col * bc + sub + row - col, False))
+    else:
+        raise ValueError(kind)
+    return out
+
+
+def radial_rows(kind, pot, N, kb, conj):
+    """Radial block of one angular pair as band rows (N, 2kb+1), [i, kb + j - i] = A(i, j).
+
+    BandNH: zgbmv layout j*(2kb+1) + kb + i - j (:700-723); conjugated through the explicit
+    loop when the outer rank asks (:653-690). Band: zhbmv('L') (:585-600), lower triangle
+    column-major with lda = kb + 1, upper = conjugate, diagonal real; the reference calls
+    zhbmv whatever the conjugate flag. Diag: A(i, i) = pot[i]. Ident: A(i, i) = pot[0]."""
+    b = 2 * kb + 1
+    out = np.zeros((N, b), dtype=np.complex128)
+    if kind == "BandNH":
+        out[:] = bandnh_rows(pot, N, kb)
+        if conj:
+            out = out.conj()
+    elif kind == "Band":
+        k1 = kb + 1
+        for i in range(N):
+            for j in range(max(0, i - kb), min(N, i + kb + 1)):
+                if i > j:
+                    v = pot[j * k1 + (i - j)]
+                elif i < j:
+                    v = np.conj(pot[i * k1 + (j - i)])
+                else:
+                    v = complex(pot[j * k1].real, 0.0)
+                out[i, kb + j - i] = v
+    elif kind == "Diag":
+        out[:, kb] = np.conj(pot[:N]) if conj else pot[:N]
+    elif kind == "Ident":
+        out[:, kb] = np.conj(pot[0]) if conj else pot[0]
+    else:
+        raise ValueError(kind)
+    return out
+
+
 class TermOracle:
-    """One consolidated tensor potential in the reference layout, ready to multiply."""
+    """One consolidated tensor potential in the reference layout, ready to multiply.
+
+    ``storage`` is "<angular>_<radial>"; banded radial blocks are kept as band rows
+    (``rows``, ``cols``, ``bands``), dense radial blocks (:1227-1330) as matrices
+    (``drows``, ``dcols``, ``dense``)."""
 
     def __init__(self, storage, potential, pairs, nang, N, kb, time_function=None):
         self.storage = storage
         self.nang, self.N, self.kb = nang, N, kb
         self.time_function = time_function
+        outer, inner = storage.split("_")
         pot = np.asarray(potential, dtype=np.complex128)
-        if storage == "Diag_BandNH":
-            self.rows = np.arange(nang)
-            self.cols = np.arange(nang)
-            self.bands = np.stack([bandnh_rows(pot[a], N, kb) for a in range(nang)])
-        elif storage == "Ident_BandNH":
-            self.rows = np.arange(nang)
-            self.cols = np.arange(nang)
-            self.bands = np.repeat(bandnh_rows(pot[0], N, kb)[None], nang, axis=0)
-        elif storage == "Simp_BandNH":
-            pairs = np.asarray(pairs)
-            self.rows = pairs[:, 0]
-            self.cols = pairs[:, 1]
-            self.bands = np.stack([bandnh_rows(pot[p], N, kb) for p in range(len(pairs))]) if len(pairs) else \
-                np.zeros((0, N, 2 * kb + 1), dtype=np.complex128)
+        if pot.ndim == 1:
+            pot = pot.reshape(1, -1)
+        blocks = outer_blocks(outer, pot.shape[0], pairs, nang)
+        b = 2 * kb + 1
+        self.rows = np.zeros(0, dtype=np.int64)
+        self.cols = np.zeros(0, dtype=np.int64)
+        self.bands = np.zeros((0, N, b), dtype=np.complex128)
+        self.drows = np.zeros(0, dtype=np.int64)
+        self.dcols = np.zeros(0, dtype=np.int64)
+        self.dense = np.zeros((0, N, N), dtype=np.complex128)
+        if not blocks:
+            return
+        rows = np.array([r for r, _, _, _ in blocks])
+        cols = np.array([c for _, c, _, _ in blocks])
+        if inner == "Dense":
+            mats = [pot[i].reshape(N, N) for _, _, i, _ in blocks]
+            self.dense = np.stack([m.conj() if cj else m for m, (_, _, _, cj) in zip(mats, blocks)])
+            self.drows, self.dcols = rows, cols
         else:
-            raise ValueError(storage)
+            self.bands = np.stack([radial_rows(inner, pot[i], N, kb, cj) for _, _, i, cj in blocks])
+            self.rows, self.cols = rows, cols
 
     def scaling(self, t):
         return 1.0 if self.time_function is None else float(self.time_function(t))
 
     def multiply(self, src, dest, scaling):
-        """dest += scaling * V src (loop over pairs, each a general band product)."""
+        """dest += scaling * V src (loop over the angular blocks)."""
         kb = self.kb
-        pad = np.zeros((src.shape[0], src.shape[1] + 2 * kb), dtype=np.complex128)
-        pad[:, kb:kb + src.shape[1]] = src
-        win = sliding_window_view(pad, 2 * kb + 1, axis=1)  # (nang, N, b): win[c, i, d] = src[c, i+d-kb]
-        y = np.einsum("pid,pid->pi", self.bands, win[self.cols])
-        np.add.at(dest, self.rows, scaling * y)
+        if len(self.rows):
+            pad = np.zeros((src.shape[0], src.shape[1] + 2 * kb), dtype=np.complex128)
+            pad[:, kb:kb + src.shape[1]] = src
+            win = sliding_window_view(pad, 2 * kb + 1, axis=1)  # win[c, i, d] = src[c, i+d-kb]
+            y = np.einsum("pid,pid->pi", self.bands, win[self.cols])
+            np.add.at(dest, self.rows, scaling * y)
+        if len(self.drows):
+            y = np.einsum("pij,pj->pi", self.dense, src[self.dcols])
+            np.add.at(dest, self.drows, scaling * y)
 
 
 def tensor_multiply(terms, scalings, src, dest):
@@ -82,6 +175,8 @@ def dense_operator(terms, scalings, nang, N):
             for d in range(-kb, kb + 1):
                 i = np.arange(max(0, -d), min(N, N - d))
                 M[r * N + i, c * N + i + d] += s * term.bands[p, i, kb + d]
+        for p, (r, c) in enumerate(zip(term.drows, term.dcols)):
+            M[r * N:(r + 1) * N, c * N:(c + 1) * N] += s * term.dense[p]
     return M
 
 

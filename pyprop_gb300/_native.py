@@ -69,6 +69,7 @@ _SIGS = {
     "pg_op_create": (_I, [_P, _I, _IP, _I, _I, C.POINTER(_P)]),
     "pg_op_destroy": (_I, [_P]),
     "pg_op_add_term": (_I, [_P, C.c_char_p, _DP, _I, _I, _IP, _I, _I]),
+    "pg_op_add_term_ranks": (_I, [_P, C.c_char_p, _DP, _IP, _IP, _IP, _I]),
     "pg_op_finalize": (_I, [_P]),
     "pg_op_stored_elements": (_LL, [_P]),
     "pg_op_matvec": (_I, [_P, _DP, _I, _P, _P, _I]),

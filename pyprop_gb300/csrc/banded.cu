@@ -83,8 +83,11 @@ __global__ void __launch_bounds__(32 * NW, 1)
         cx<R> acc[4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) acc[a] = mk<R>((R)0, (R)0);
+#pragma unroll 1
+        for (int q0 = 0; q0 < 32; q0 += 16) {
 #pragma unroll
-        for (int q = 0; q < 32; ++q) coef_fma(acc[q & 3], ib[q * 32 + lane], shfl_cx(r, q));
+            for (int q = 0; q < 16; ++q) coef_fma(acc[q & 3], ib[(q0 + q) * 32 + lane], shfl_cx(r, q0 + q));
+        }
         xs[blk * 32 + lane] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
         const int r0 = lower ? 32 - w : 0;  // boundary rows of this block
         for (int c = 0; c < w; ++c) {
@@ -93,7 +96,9 @@ __global__ void __launch_bounds__(32 * NW, 1)
             if (lane >= r0 && lane < r0 + w) gt[((size_t)blk * w + c) * w + (lane - r0)] = v;
         }
     };
-    // w-wide recurrence over the blocks (warp 0; lanes >= w mirror lane w-1 to keep shuffles whole)
+    // w-wide recurrence over the blocks (warp 0; lanes >= w mirror lane w-1 to keep shuffles
+    // whole). For w <= 8 the next block's operands are loaded while the current step's
+    // dependent chain runs, and the chain is split in two partial sums.
     auto scan = [&](bool lower) {
         if (warp != 0) return;
         const int r = min(lane, w - 1);
@@ -101,13 +106,42 @@ __global__ void __launch_bounds__(32 * NW, 1)
         int blk = lower ? 0 : nblk - 1;
         cx<R> s = xs[blk * 32 + r0 + r];
         if (lane < w) sb[blk * w + lane] = s;
-        for (int step = 1; step < nblk; ++step) {
-            blk = lower ? step : nblk - 1 - step;
-            cx<R> acc = xs[blk * 32 + r0 + r];
-            const C *gtb = gt + (size_t)blk * w * w;
-            for (int c = 0; c < w; ++c) coef_fms(acc, gtb[c * w + r], shfl_cx(s, c));
-            s = acc;
-            if (lane < w) sb[blk * w + lane] = s;
+        if (w <= 8) {
+            C gn[8];
+            cx<R> zn = mk<R>((R)0, (R)0);
+            auto load = [&](int b) {
+                zn = xs[b * 32 + r0 + r];
+                const C *gtb = gt + (size_t)b * w * w;
+#pragma unroll
+                for (int c = 0; c < 8; ++c) gn[c] = (c < w) ? gtb[c * w + r] : C{};
+            };
+            if (nblk > 1) load(lower ? 1 : nblk - 2);
+            for (int step = 1; step < nblk; ++step) {
+                blk = lower ? step : nblk - 1 - step;
+                C g[8];
+#pragma unroll
+                for (int c = 0; c < 8; ++c) g[c] = gn[c];
+                cx<R> acc0 = zn, acc1 = mk<R>((R)0, (R)0);
+                if (step + 1 < nblk) load(lower ? step + 1 : nblk - 2 - step);
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    if (c < w) {
+                        const cx<R> sc = shfl_cx(s, c);
+                        if (c & 1) coef_fms(acc1, g[c], sc);
+                        else coef_fms(acc0, g[c], sc);
+                    }
+                s = acc0 + acc1;
+                if (lane < w) sb[blk * w + lane] = s;
+            }
+        } else {
+            for (int step = 1; step < nblk; ++step) {
+                blk = lower ? step : nblk - 1 - step;
+                cx<R> acc = xs[blk * 32 + r0 + r];
+                const C *gtb = gt + (size_t)blk * w * w;
+                for (int c = 0; c < w; ++c) coef_fms(acc, gtb[c * w + r], shfl_cx(s, c));
+                s = acc;
+                if (lane < w) sb[blk * w + lane] = s;
+            }
         }
     };
     // y_b = z_b - G_b s (returns the corrected row)
@@ -377,6 +411,7 @@ extern "C" int pg_prec_blockdiag_create(pg_op *op, const double *overlap_rows, c
     if (!op || !overlap_rows || !cS || !cH || !out || nslots < 0 || (nslots > 0 && (!slots || !slot_weights)))
         return PG_ERR_ARG;
     if (!op->finalized) return PG_ERR_STATE;
+    if (op->rank != 2) return PG_ERR_STORAGE;  // blocks are angular channels of a rank-2 operator
     const int N = op->N, kb = op->kb, b = 2 * kb + 1, na = op->nrows;
     const zd zS(cS[0], cS[1]), zH(cH[0], cH[1]);
     std::vector<zd> all_lo_inv, all_lo_cpl, all_up_inv, all_up_cpl;
@@ -447,15 +482,14 @@ extern "C" int pg_banded_destroy(pg_banded *b)
     return PG_OK;
 }
 
-template <typename R, typename C>
-static int launch_tri(pg_banded *b, bool do_lower, bool do_upper, void *x)
+// One CTA of NW warps per fibre; NW covers the blocks of a fibre (one block per warp where
+// possible), bounded by the registers of the unrolled block product.
+template <typename R, typename C, int NW>
+static int launch_tri_nw(pg_banded *b, bool do_lower, bool do_upper, void *x)
 {
     pg_ctx *ctx = b->op->ctx;
     const int N = b->N, nblk = (N + 31) / 32, w = b->kb;
     const int nfib = b->op->nrows;
-    if (w < 1 || w > 32) return PG_ERR_ARG;
-    // FP64 (a quarter of the SM's FP64 rate per sub-partition) wants more warps in flight
-    constexpr int NW = sizeof(R) == 8 ? 16 : 8;
     const size_t base = (size_t)nblk * 32 * sizeof(cx<R>) + (size_t)nblk * w * sizeof(cx<R>) +
                         (size_t)nblk * w * w * sizeof(C);
     const size_t full = base + (size_t)nblk * w * 32 * sizeof(C);
@@ -463,18 +497,32 @@ static int launch_tri(pg_banded *b, bool do_lower, bool do_upper, void *x)
     if (base > limit) return PG_ERR_SHAPE;  // fibre too long for the shared-memory solve
     const bool g_in_smem = full <= limit;
     const size_t smem = g_in_smem ? full : base;
-    static size_t configured[2] = {0, 0};
-    size_t &cfg = configured[sizeof(C) == sizeof(R) ? 0 : 1];
-    if (cfg < smem) {
+    static size_t configured = 0;
+    if (configured < smem) {
         PG_CUDA_TRY(cudaFuncSetAttribute(tri_solve_kernel<R, C, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem));
-        cfg = smem;
+        configured = smem;
     }
     tri_solve_kernel<R, C, NW><<<nfib, 32 * NW, smem, ctx->stream>>>(
         N, nblk, w, (const C *)b->d_lo_inv, (const C *)b->d_lo_cpl, (const C *)b->d_up_inv, (const C *)b->d_up_cpl,
         do_lower ? 1 : 0, do_upper ? 1 : 0, b->nmat > 1, g_in_smem ? 1 : 0, (cx<R> *)x, nfib);
     ctx->launches++;
     return pg_check_launch(ctx);
+}
+
+template <typename R, typename C>
+static int launch_tri(pg_banded *b, bool do_lower, bool do_upper, void *x)
+{
+    const int nblk = (b->N + 31) / 32;
+    if (b->kb < 1 || b->kb > 32) return PG_ERR_ARG;
+    if (nblk <= 8) return launch_tri_nw<R, C, 8>(b, do_lower, do_upper, x);
+    // FP64 stays at 16 warps (register budget of the complex128 block product)
+    if constexpr (sizeof(R) == 8) {
+        return launch_tri_nw<R, C, 16>(b, do_lower, do_upper, x);
+    } else {
+        if (nblk <= 16) return launch_tri_nw<R, C, 16>(b, do_lower, do_upper, x);
+        return launch_tri_nw<R, C, 24>(b, do_lower, do_upper, x);
+    }
 }
 
 template <typename R>

@@ -47,6 +47,8 @@ struct GmresStats {
 // mixed step: scales, matvec; per refinement pass: convert, preconditioner solve, norm, init,
 //            back-substitution, combine, matvec, norm, decide;
 // per GMRES iteration: next vector, matvec, preconditioner solve, multidot, 2 GS updates, Givens.
+// Each count has one matvec kernel per operator product; an operator with dense radial blocks
+// launches one more (pg_op_matvec_kernels).
 static const int K_FP64_BASE = 7, K_TRUE_RESID = 4, K_MIXED_BASE = 2, K_MIXED_PASS = 9, K_ITER = 7;
 
 struct GmresState {
@@ -113,7 +115,7 @@ __global__ void cay_gmres_init_kernel(GmresState *st, const double *__restrict__
                                       double rel_tol, int kernels, cudaGraphConditionalHandle inner,
                                       cudaGraphConditionalHandle outer, int has_outer)
 {
-    const double b = nrm[1];
+    const double b = sqrt(fmax(nrm[0], 0.0));  // nrm: FP64 atomic sum of |d|^2 (cleared by backsolve)
     const double s = b > 0.0 ? 1.0 / b : 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const cx<R> a = d[i];
@@ -160,9 +162,9 @@ __global__ void cay_next_vector_kernel(const GmresState *__restrict__ st, cx<R> 
 // rotations, form the new one, update g, store the R column, set the loop condition.
 // T is the arithmetic precision of the rotations (float for the complex64 inner solve).
 template <typename T>
-__global__ void cay_gmres_finalize_kernel(GmresState *st, const double *__restrict__ h1, const double *__restrict__ h2,
-                                          const double *__restrict__ h3, int m, cudaGraphConditionalHandle inner,
-                                          int use_cond)
+__global__ void cay_gmres_finalize_kernel(GmresState *st, double *h1, double *h2, double *h3, int m,
+                                          cudaGraphConditionalHandle inner,
+                                          int use_cond, int kernels)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int j = st->j;
@@ -172,9 +174,15 @@ __global__ void cay_gmres_finalize_kernel(GmresState *st, const double *__restri
         hx[i] = (T)(h1[2 * i] + h2[2 * i]);
         hy[i] = (T)(h1[2 * i + 1] + h2[2 * i + 1]);
     }
-    const double beta = h3[2 * J + 1];
+    const double beta = sqrt(fmax(h3[2 * J], 0.0));
     hx[J] = (T)beta;
     hy[J] = (T)0;
+    // the three reductions were FP64 atomic sums: clear them for the next iteration
+    for (int i = 0; i < 2 * J + 2; ++i) {
+        ((double *)h1)[i] = 0.0;
+        ((double *)h2)[i] = 0.0;
+        ((double *)h3)[i] = 0.0;
+    }
     for (int i = 0; i < j; ++i) {
         const T c = (T)st->cs[i];
         const T sx = (T)st->sn[2 * i], sy = (T)st->sn[2 * i + 1];
@@ -220,7 +228,7 @@ __global__ void cay_gmres_finalize_kernel(GmresState *st, const double *__restri
     st->stats.k = J;
     st->stats.resid = resid;
     st->stats.iterations += 1;
-    st->stats.kernels += K_ITER;
+    st->stats.kernels += kernels;
     st->beta_last = beta;
     const bool bad = !(resid == resid);
     const bool conv = bad || resid <= st->tol_eff || J >= m || !(beta > 1e-300);
@@ -231,9 +239,11 @@ __global__ void cay_gmres_finalize_kernel(GmresState *st, const double *__restri
 
 // y = R^-1 g over the k completed columns (one thread, precision T)
 template <typename T>
-__global__ void cay_backsolve_kernel(GmresState *st)
+__global__ void cay_backsolve_kernel(GmresState *st, double *nrm)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    nrm[0] = 0.0;  // the init kernel's atomic norm sum, read by then
+    nrm[1] = 0.0;
     const int k = st->stats.k;
     T yx[GM_MAXM], yy[GM_MAXM];
     for (int i = k - 1; i >= 0; --i) {
@@ -281,17 +291,23 @@ __global__ void cay_combine_kernel(const cx<R> *__restrict__ V, long long n, con
     }
 }
 
-__global__ void cay_true_resid_kernel(GmresState *st, const double *__restrict__ nrm)
+__global__ void cay_true_resid_kernel(GmresState *st, double *nrm)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0) st->stats.true_resid = nrm[1];
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        st->stats.true_resid = sqrt(fmax(nrm[0], 0.0));
+        nrm[0] = 0.0;
+        nrm[1] = 0.0;
+    }
 }
 
 // end of a refinement pass: record ||r|| (FP64) and repeat while it is above tol
-__global__ void cay_refine_decide_kernel(GmresState *st, const double *__restrict__ nrm, double tol, int maxpass,
+__global__ void cay_refine_decide_kernel(GmresState *st, double *nrm, double tol, int maxpass,
                                          cudaGraphConditionalHandle outer, int use_cond)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const double r = nrm[1];
+    const double r = sqrt(fmax(nrm[0], 0.0));
+    nrm[0] = 0.0;
+    nrm[1] = 0.0;
     st->stats.true_resid = r;
     const bool again = (r > tol) && (r == r) && st->stats.passes < maxpass;
     st->cont_outer = again ? 1 : 0;
@@ -384,10 +400,12 @@ static int capture_iteration(pg_cayley *c, pg_op *op, pg_banded *pre, cudaGraphC
     PG_TRY(pg_banded_apply_dev(pre, PG_BAND_PREC_SOLVE, w));
     pg_ctx *rc = &c->rctx;
     rc->stream = s;
-    PG_TRY(pg_multidot<R>(rc, V, n, c->m, w, n, c->h1, &c->st->j));
-    PG_TRY(pg_gs_update<R>(rc, V, n, c->m, c->h1, w, n, 1, c->h2, &c->st->j));
-    PG_TRY(pg_gs_update<R>(rc, V, n, c->m, c->h2, w, n, 0, c->h3, &c->st->j));
-    cay_gmres_finalize_kernel<T><<<1, 32, 0, s>>>(c->st, c->h1, c->h2, c->h3, c->m, inner, c->eager ? 0 : 1);
+    // reductions add into h1/h2/h3 with FP64 atomics; the Givens kernel reads and clears them
+    PG_TRY(pg_multidot<R>(rc, V, n, c->m, w, n, c->h1, &c->st->j, 1));
+    PG_TRY(pg_gs_update<R>(rc, V, n, c->m, c->h1, w, n, 1, c->h2, &c->st->j, 1));
+    PG_TRY(pg_gs_update<R>(rc, V, n, c->m, c->h2, w, n, 0, c->h3, &c->st->j, 1));
+    cay_gmres_finalize_kernel<T><<<1, 32, 0, s>>>(c->st, c->h1, c->h2, c->h3, c->m, inner, c->eager ? 0 : 1,
+                                                   K_ITER - 1 + pg_op_matvec_kernels(op));
     return pg_check_launch(ctx);
 }
 
@@ -443,13 +461,14 @@ static int record_fp64(pg_cayley *c, cxd *psi)
     memset(&dummy, 0, sizeof(dummy));
     pg_ctx *rc = &c->rctx;
     rc->stream = s0;
+    const int mv = pg_op_matvec_kernels(c->op64) - 1;
     cay_scales_kernel<<<1, 32, 0, s0>>>(c->params_dev, c->d_sc, c->st,
-                                        K_FP64_BASE + (c->true_residual ? K_TRUE_RESID : 0));
+                                        K_FP64_BASE + mv + (c->true_residual ? K_TRUE_RESID + mv : 0));
     PG_TRY(pg_check_launch(ctx));
     PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_MINUS * PG_MAX_SLOTS, psi, c->b64, 0, nullptr, nullptr));
     PG_CUDA_TRY(cudaMemcpyAsync(c->d64, c->b64, sizeof(cxd) * n, cudaMemcpyDeviceToDevice, s0));
     PG_TRY(pg_banded_apply_dev(c->prec64, PG_BAND_PREC_SOLVE, c->d64));
-    PG_TRY(pg_multidot<double>(rc, c->d64, n, 0, c->d64, n, c->nrm));
+    PG_TRY(pg_multidot<double>(rc, c->d64, n, 0, c->d64, n, c->nrm, nullptr, 1));
     cudaGraphConditionalHandle inner = 0;
     if (!c->eager) PG_TRY(capture_handle(s0, &inner, 0, 0));
     cay_gmres_init_kernel<double><<<nb, 256, 0, s0>>>(c->st, c->nrm, c->d64, (cxd *)c->V, (cxd *)c->vcur, n, c->tol,
@@ -457,7 +476,7 @@ static int record_fp64(pg_cayley *c, cxd *psi)
     PG_TRY(pg_check_launch(ctx));
     PG_TRY(loop_while(c, inner, c->cap[1], &c->st->cont_inner,
                       [&]() { return capture_iteration<double, double>(c, c->op64, c->prec64, inner); }));
-    cay_backsolve_kernel<double><<<1, 32, 0, s0>>>(c->st);
+    cay_backsolve_kernel<double><<<1, 32, 0, s0>>>(c->st, c->nrm);
     PG_TRY(pg_check_launch(ctx));
     cay_combine_kernel<double><<<nb, 256, 0, s0>>>((const cxd *)c->V, n, c->st, psi, nullptr);
     PG_TRY(pg_check_launch(ctx));
@@ -466,7 +485,7 @@ static int record_fp64(pg_cayley *c, cxd *psi)
         PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_PLUS * PG_MAX_SLOTS, psi, c->r64, 0, nullptr, nullptr));
         PG_TRY(pg_axpy(ctx, mk<double>(-1.0, 0.0), c->b64, c->r64, n));
         rc->stream = s0;
-        PG_TRY(pg_multidot<double>(rc, c->r64, n, 0, c->r64, n, c->nrm2));
+        PG_TRY(pg_multidot<double>(rc, c->r64, n, 0, c->r64, n, c->nrm2, nullptr, 1));
         cay_true_resid_kernel<<<1, 32, 0, s0>>>(c->st, c->nrm2);
         PG_TRY(pg_check_launch(ctx));
     }
@@ -485,7 +504,8 @@ static int record_mixed(pg_cayley *c, cxd *psi)
     pg_scales dummy;
     memset(&dummy, 0, sizeof(dummy));
     pg_ctx *rc = &c->rctx;
-    cay_scales_kernel<<<1, 32, 0, s0>>>(c->params_dev, c->d_sc, c->st, K_MIXED_BASE);
+    const int mv = pg_op_matvec_kernels(c->op64) - 1;
+    cay_scales_kernel<<<1, 32, 0, s0>>>(c->params_dev, c->d_sc, c->st, K_MIXED_BASE + mv);
     PG_TRY(pg_check_launch(ctx));
     PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_DIFF * PG_MAX_SLOTS, psi, c->r64, 0, nullptr, nullptr));
     cudaGraphConditionalHandle outer = 0;
@@ -500,22 +520,22 @@ static int record_mixed(pg_cayley *c, cxd *psi)
         PG_TRY((pg_scale_copy<float, double>(ctx, c->r64, dconv, nullptr, n, nullptr, 1.0)));
         PG_TRY(pg_banded_apply_dev(c->precb, PG_BAND_PREC_SOLVE, dconv));
         rc->stream = s1;
-        PG_TRY(pg_multidot<float>(rc, dconv, n, 0, dconv, n, c->nrm));
+        PG_TRY(pg_multidot<float>(rc, dconv, n, 0, dconv, n, c->nrm, nullptr, 1));
         cudaGraphConditionalHandle inner = 0;
         if (!c->eager) PG_TRY(capture_handle(s1, &inner, 0, 0));
         cay_gmres_init_kernel<float><<<nb, 256, 0, s1>>>(c->st, c->nrm, dconv, (cxf *)c->V, (cxf *)c->vcur, n, c->tol,
-                                                         2e-6, K_MIXED_PASS, inner, outer, c->eager ? -1 : 1);
+                                                         2e-6, K_MIXED_PASS + mv, inner, outer, c->eager ? -1 : 1);
         PG_TRY(pg_check_launch(ctx));
         PG_TRY(loop_while(c, inner, c->cap[2], &c->st->cont_inner,
                           [&]() { return capture_iteration<float, float>(c, c->opb, c->precb, inner); }));
-        cay_backsolve_kernel<float><<<1, 32, 0, s1>>>(c->st);
+        cay_backsolve_kernel<float><<<1, 32, 0, s1>>>(c->st, c->nrm);
         PG_TRY(pg_check_launch(ctx));
         cay_combine_kernel<float><<<nb, 256, 0, s1>>>((const cxf *)c->V, n, c->st, c->e64, psi);
         PG_TRY(pg_check_launch(ctx));
         // r -= (S + i dt/2 H) e   in FP64, then ||r|| decides whether another pass runs
         PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_NEGPLUS * PG_MAX_SLOTS, c->e64, c->r64, 1, nullptr, nullptr));
         rc->stream = s1;
-        PG_TRY(pg_multidot<double>(rc, c->r64, n, 0, c->r64, n, c->nrm2));
+        PG_TRY(pg_multidot<double>(rc, c->r64, n, 0, c->r64, n, c->nrm2, nullptr, 1));
         cay_refine_decide_kernel<<<1, 32, 0, s1>>>(c->st, c->nrm2, c->tol, 4, outer, c->eager ? 0 : 1);
         return pg_check_launch(ctx);
     }));
@@ -583,6 +603,8 @@ extern "C" int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64,
     PG_CUDA_TRY(cudaMalloc(&c->h3, cols));
     PG_CUDA_TRY(cudaMalloc(&c->nrm, cols));
     PG_CUDA_TRY(cudaMalloc(&c->nrm2, cols));
+    // atomic reduction targets start (and are left by their consumers) at zero
+    for (double *z : {c->h1, c->h2, c->h3, c->nrm, c->nrm2}) PG_CUDA_TRY(cudaMemset(z, 0, cols));
     PG_CUDA_TRY(cudaMalloc(&c->st, sizeof(GmresState)));
     PG_CUDA_TRY(cudaMemset(c->st, 0, sizeof(GmresState)));
     PG_CUDA_TRY(cudaMallocHost(&c->h_stats, sizeof(GmresStats)));

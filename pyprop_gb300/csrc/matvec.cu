@@ -11,6 +11,8 @@
 //    consecutive addresses for every diagonal d, complex64 or complex128.
 #include "pg_internal.cuh"
 
+#include <map>
+
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -154,6 +156,47 @@ __global__ void __launch_bounds__(128) op_matvec_kernel(OpDev op, pg_scales scal
     }
     if (accumulate) acc = acc + dst[o];
     dst[o] = acc;
+}
+
+// ------------------------------------------------------------------------------------
+// dense radial blocks (radial storage "Dense"): dst[r][i] += sum_e s_e sum_j D_e[i][j] x_e[j],
+// x_e = src[col_e] (times 1/src_inv_scale when given). One CTA = 128 radial rows of one
+// angular row; the source row is staged through shared memory in tiles of 128, and D is
+// stored transposed ([j][i]) so the threads of a warp read consecutive i.
+template <typename R>
+__global__ void __launch_bounds__(128) op_dense_kernel(int N, const int *__restrict__ row_ptr,
+                                                       const int *__restrict__ ent_col, const int *__restrict__ ent_mat,
+                                                       const int *__restrict__ ent_slot, const cx<R> *__restrict__ dense,
+                                                       pg_scales scales, const cxd *__restrict__ scales_dev,
+                                                       const cx<R> *__restrict__ src, cx<R> *__restrict__ dst,
+                                                       const double *__restrict__ src_inv_scale)
+{
+    __shared__ cx<R> xs[128];
+    const int r = blockIdx.y;
+    const int i = blockIdx.x * 128 + threadIdx.x;
+    const R sc = src_inv_scale ? (R)(1.0 / *src_inv_scale) : (R)1;
+    cx<R> acc = mk<R>((R)0, (R)0);
+    for (int e = row_ptr[r]; e < row_ptr[r + 1]; ++e) {
+        const cx<R> *__restrict__ D = dense + (size_t)ent_mat[e] * N * N;
+        const cx<R> *__restrict__ x = src + (size_t)ent_col[e] * N;
+        cx<R> t = mk<R>((R)0, (R)0);
+        for (int j0 = 0; j0 < N; j0 += 128) {
+            __syncthreads();
+            const int jj = j0 + threadIdx.x;
+            xs[threadIdx.x] = jj < N ? x[jj] : mk<R>((R)0, (R)0);
+            __syncthreads();
+            const int jn = min(128, N - j0);
+            if (i < N)
+                for (int q = 0; q < jn; ++q) cfma(t, D[(size_t)(j0 + q) * N + i], xs[q]);
+        }
+        const int slot = ent_slot[e];
+        const cx<R> s = scales_dev ? cvt<R>(scales_dev[slot]) : cvt<R>(scales.s[slot]);
+        cfma(acc, s, t);
+    }
+    if (i < N) {
+        const size_t o = (size_t)r * N + i;
+        dst[o] = dst[o] + sc * acc;
+    }
 }
 
 // ------------------------------------------------------------------------------------
@@ -317,30 +360,57 @@ static int launch_op_matvec(pg_op *op, const pg_scales &scales, const cxd *scale
     return pg_check_launch(op->ctx);
 }
 
+template <typename R>
+static int launch_dense(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
+                        const double *inv_scale)
+{
+    dim3 grid((op->N + 127) / 128, op->nrows);
+    op_dense_kernel<R><<<grid, 128, 0, op->ctx->stream>>>(op->N, op->d_drow_ptr, op->d_dent_col, op->d_dent_mat,
+                                                          op->d_dent_slot, (const cx<R> *)op->d_dense, scales,
+                                                          scales_dev, (const cx<R> *)src, (cx<R> *)dst, inv_scale);
+    op->ctx->launches++;
+    return pg_check_launch(op->ctx);
+}
+
+int pg_op_matvec_kernels(const pg_op *op) { return op->ndense_entries > 0 ? 2 : 1; }
+
 int pg_op_matvec_dev(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
                      int accumulate, const double *src_inv_scale_dev, void *src_copy_out)
 {
     if (!op || !op->finalized) return PG_ERR_STATE;
+    const bool fp64 = op->precision == PG_FP64;
     if (op->kb == 6 && !src_inv_scale_dev && !src_copy_out && op->use_bulk) {
-        if (op->precision == PG_FP64) return launch_bulk<double, 6>(op, scales, scales_dev, src, dst, accumulate);
-        return launch_bulk<float, 6>(op, scales, scales_dev, src, dst, accumulate);
+        PG_TRY(fp64 ? launch_bulk<double, 6>(op, scales, scales_dev, src, dst, accumulate)
+                    : launch_bulk<float, 6>(op, scales, scales_dev, src, dst, accumulate));
+    } else {
+        PG_TRY(fp64 ? launch_op_matvec<double>(op, scales, scales_dev, src, dst, accumulate, src_inv_scale_dev,
+                                               src_copy_out)
+                    : launch_op_matvec<float>(op, scales, scales_dev, src, dst, accumulate, src_inv_scale_dev,
+                                              src_copy_out));
     }
-    if (op->precision == PG_FP64)
-        return launch_op_matvec<double>(op, scales, scales_dev, src, dst, accumulate, src_inv_scale_dev, src_copy_out);
-    return launch_op_matvec<float>(op, scales, scales_dev, src, dst, accumulate, src_inv_scale_dev, src_copy_out);
+    if (op->ndense_entries == 0) return PG_OK;
+    return fp64 ? launch_dense<double>(op, scales, scales_dev, src, dst, src_inv_scale_dev)
+                : launch_dense<float>(op, scales, scales_dev, src, dst, src_inv_scale_dev);
 }
 
 extern "C" int pg_op_create(pg_ctx *ctx, int rank, const int *shape, int bandCount, int precision, pg_op **out)
 {
     if (!ctx || !shape || !out || bandCount < 0) return PG_ERR_ARG;
-    if (rank != 2) return PG_ERR_STORAGE;
+    if (rank != 2 && rank != 3) return PG_ERR_STORAGE;
     if (precision != PG_FP64 && precision != PG_FP32) return PG_ERR_ARG;
-    if (shape[0] <= 0 || shape[1] <= 2 * bandCount) return PG_ERR_SHAPE;
+    long long rows = 1;
+    for (int r = 0; r < rank - 1; ++r) {
+        if (shape[r] <= 0) return PG_ERR_SHAPE;
+        rows *= shape[r];
+    }
+    if (rows > (1LL << 30) || shape[rank - 1] <= 2 * bandCount) return PG_ERR_SHAPE;
     pg_op *op = new pg_op();
     op->ctx = ctx;
     op->rank = rank;
-    op->nrows = shape[0];
-    op->N = shape[1];
+    op->shape.assign(shape, shape + rank);
+    // the last rank is the banded fibre; all other ranks together index the fibres
+    op->nrows = (int)rows;
+    op->N = shape[rank - 1];
     op->kb = bandCount;
     op->b = 2 * bandCount + 1;
     op->ld = (op->N + 3) & ~3;
@@ -358,36 +428,102 @@ extern "C" int pg_op_destroy(pg_op *op)
     cudaFree(op->d_ent_band);
     cudaFree(op->d_ent_slot);
     cudaFree(op->d_bands);
+    cudaFree(op->d_drow_ptr);
+    cudaFree(op->d_dent_col);
+    cudaFree(op->d_dent_mat);
+    cudaFree(op->d_dent_slot);
+    cudaFree(op->d_dense);
     delete op;
+    return PG_OK;
+}
+
+// Storage ids "<rank 0>_<rank 1>[_<rank 2>]" of the reference's generated multiply kernels
+// (core/tensorpotential/tensorpotentialmultiply_generator.py): every rank but the last is
+// Simp, Herm, Diag, Ident, Band, BandNH or Dense (:302-462, :467-618, :622-762, :1227-1330);
+// the last (fibre) rank is BandNH, Band, Dense, Diag, Ident or Simp. potential holds
+// prod(extents) complex128 in the reference's layout; pairs lists (row, col) of every Simp or
+// Herm rank, in rank order.
+static bool outer_kind(const std::string &s)
+{
+    return s == "Simp" || s == "Herm" || s == "Diag" || s == "Ident" || s == "Band" || s == "BandNH" || s == "Dense";
+}
+static bool inner_kind(const std::string &s)
+{
+    return s == "BandNH" || s == "Band" || s == "Dense" || s == "Diag" || s == "Ident" || s == "Simp";
+}
+static bool has_pairs(const std::string &s) { return s == "Simp" || s == "Herm"; }
+
+static int add_term(pg_op *op, const char *storage, const double *potential, const int *extents, const int *pairs,
+                    const int *npairs, int slot)
+{
+    if (!op || !storage || !extents) return PG_ERR_ARG;
+    if (op->finalized) return PG_ERR_STATE;
+    if (slot < 0 || slot >= PG_MAX_SLOTS) return PG_ERR_ARG;
+    const int R = op->rank;
+    HostTerm t;
+    t.storage = storage;
+    size_t start = 0;
+    for (;;) {
+        const size_t us = t.storage.find('_', start);
+        t.kinds.push_back(t.storage.substr(start, us == std::string::npos ? std::string::npos : us - start));
+        if (us == std::string::npos) break;
+        start = us + 1;
+    }
+    if ((int)t.kinds.size() != R) return PG_ERR_STORAGE;
+    for (int r = 0; r < R - 1; ++r)
+        if (!outer_kind(t.kinds[r])) return PG_ERR_STORAGE;
+    if (!inner_kind(t.kinds[R - 1])) return PG_ERR_STORAGE;
+    size_t total = 1;
+    const int *pp = pairs;
+    t.pairs.resize(R);
+    for (int r = 0; r < R; ++r) {
+        const std::string &k = t.kinds[r];
+        const int e = extents[r], n = op->shape[r];
+        if (e < 0) return PG_ERR_SHAPE;
+        total *= (size_t)e;
+        if (has_pairs(k)) {
+            if (!npairs || npairs[r] != e || (e > 0 && !pp)) return PG_ERR_SHAPE;
+            if (r == R - 1 && k == "Herm") return PG_ERR_STORAGE;
+            for (int q = 0; q < e; ++q)
+                if (pp[2 * q] < 0 || pp[2 * q] >= n || pp[2 * q + 1] < 0 || pp[2 * q + 1] >= n) return PG_ERR_SHAPE;
+            t.pairs[r].assign(pp, pp + 2 * (size_t)e);
+            pp += 2 * (size_t)e;
+        } else if (k == "Diag") {
+            if (e != n) return PG_ERR_SHAPE;
+        } else if (k == "Ident") {
+            if (e != 1) return PG_ERR_SHAPE;
+        } else if (k == "Dense") {
+            if (e != n * n) return PG_ERR_SHAPE;
+        } else if (r == R - 1) {  // banded fibre storage
+            if (k == "BandNH" && e != n * op->b) return PG_ERR_SHAPE;
+            if (k == "Band" && e != n * (op->kb + 1)) return PG_ERR_SHAPE;
+        } else {  // Band / BandNH outer: extent n * bandCount
+            if (e <= 0 || e % n != 0) return PG_ERR_SHAPE;
+            if (k == "BandNH" && (e / n) % 2 == 0) return PG_ERR_SHAPE;
+        }
+    }
+    if (total > 0 && !potential) return PG_ERR_ARG;
+    t.ext.assign(extents, extents + R);
+    if (total > 0) t.pot.assign(potential, potential + 2 * total);
+    t.slot = slot;
+    op->terms.push_back(std::move(t));
     return PG_OK;
 }
 
 extern "C" int pg_op_add_term(pg_op *op, const char *storage, const double *potential, int potExtent0,
                               int potExtent1, const int *pairs0, int npairs0, int slot)
 {
-    if (!op || !storage || (!potential && potExtent0 > 0)) return PG_ERR_ARG;
-    if (op->finalized) return PG_ERR_STATE;
-    if (slot < 0 || slot >= PG_MAX_SLOTS) return PG_ERR_ARG;
-    HostTerm t;
-    t.storage = storage;
-    if (t.storage != "Diag_BandNH" && t.storage != "Simp_BandNH" && t.storage != "Ident_BandNH") return PG_ERR_STORAGE;
-    if (potExtent1 != op->N * op->b) return PG_ERR_SHAPE;
-    if (t.storage == "Diag_BandNH" && potExtent0 != op->nrows) return PG_ERR_SHAPE;
-    if (t.storage == "Ident_BandNH" && potExtent0 != 1) return PG_ERR_SHAPE;
-    if (t.storage == "Simp_BandNH") {
-        if (npairs0 != potExtent0 || (npairs0 > 0 && !pairs0)) return PG_ERR_SHAPE;
-        for (int p = 0; p < npairs0; ++p) {
-            const int rr = pairs0[2 * p], cc = pairs0[2 * p + 1];
-            if (rr < 0 || rr >= op->nrows || cc < 0 || cc >= op->nrows) return PG_ERR_SHAPE;
-        }
-        t.pairs.assign(pairs0, pairs0 + 2 * npairs0);
-    }
-    t.e0 = potExtent0;
-    t.e1 = potExtent1;
-    if (potExtent0 > 0) t.pot.assign(potential, potential + 2 * (size_t)potExtent0 * potExtent1);
-    t.slot = slot;
-    op->terms.push_back(std::move(t));
-    return PG_OK;
+    if (!op) return PG_ERR_ARG;
+    if (op->rank != 2) return PG_ERR_STATE;  // rank-3 operators take pg_op_add_term_ranks
+    const int ext[2] = {potExtent0, potExtent1};
+    const int np[2] = {npairs0, 0};
+    return add_term(op, storage, potential, ext, pairs0, np, slot);
+}
+
+extern "C" int pg_op_add_term_ranks(pg_op *op, const char *storage, const double *potential, const int *extents,
+                                    const int *pairs, const int *npairs, int slot)
+{
+    return add_term(op, storage, potential, extents, pairs, npairs, slot);
 }
 
 template <typename R>
@@ -407,47 +543,178 @@ static int upload_bands(pg_op *op)
     return PG_OK;
 }
 
+// One angular (row, col) block of a term: the radial data at index i0 of the angular rank,
+// complex conjugated when the reference's loop passes conjugate = true (the mirrored half of
+// Herm and Band angular storage).
+struct BlockRef {
+    int row, col;
+    size_t i0;
+    bool conj;
+};
+
+// Expansion of one non-fibre rank, following the generator's loops for each storage: the
+// (row, col) blocks with the potential index along that rank and the conjugate flag.
+static void expand_rank(const std::string &kind, int e, const std::vector<int> &pairs, int n,
+                        std::vector<BlockRef> &out)
+{
+    if (kind == "Simp" || kind == "Herm") {
+        for (int p = 0; p < e; ++p) out.push_back({pairs[2 * p], pairs[2 * p + 1], (size_t)p, false});
+        if (kind == "Herm")  // :380-386: second pass with row/col swapped and the potential conjugated
+            for (int p = 0; p < e; ++p) out.push_back({pairs[2 * p + 1], pairs[2 * p], (size_t)p, true});
+    } else if (kind == "Diag") {
+        for (int l = 0; l < n; ++l) out.push_back({l, l, (size_t)l, false});
+    } else if (kind == "Ident") {
+        for (int l = 0; l < n; ++l) out.push_back({l, l, 0, false});
+    } else if (kind == "Dense") {  // :1268-1275: index row * n + col
+        for (int r = 0; r < n; ++r)
+            for (int c = 0; c < n; ++c) out.push_back({r, c, (size_t)r * n + c, false});
+    } else if (kind == "Band") {
+        // :507-552: stored (row, col >= row) at row * bc + (col - row); mirrored (col, row) conjugated
+        const int bc = e / n;
+        for (int r = 0; r < n; ++r)
+            for (int c = r; c < std::min(n, r + bc); ++c) out.push_back({r, c, (size_t)r * bc + (c - r), false});
+        for (int r = 0; r < n; ++r)
+            for (int c = r + 1; c < std::min(n, r + bc); ++c) out.push_back({c, r, (size_t)r * bc + (c - r), true});
+    } else {  // BandNH, :662-694: element (row, col) at col * bc + (sub + row - col)
+        const int bc = e / n, sub = (bc - 1) / 2;
+        for (int c = 0; c < n; ++c)
+            for (int r = std::max(0, c - sub); r <= std::min(n - 1, c + sub); ++r)
+                out.push_back({r, c, (size_t)c * bc + (sub + r - c), false});
+    }
+}
+
+// All non-fibre ranks of a term: rank r's loop nests inside rank r-1's (the generator's
+// nesting), rows and columns flatten C-order, potential indices flatten over the extents,
+// and conjugate flags of nested ranks combine (each mirrored pass toggles the flag).
+static void expand_outer(const HostTerm &t, const std::vector<int> &shape, std::vector<BlockRef> &out)
+{
+    out.assign(1, BlockRef{0, 0, 0, false});
+    std::vector<BlockRef> rank_blocks, next;
+    for (size_t r = 0; r + 1 < t.kinds.size(); ++r) {
+        rank_blocks.clear();
+        expand_rank(t.kinds[r], t.ext[r], t.pairs[r], shape[r], rank_blocks);
+        next.clear();
+        next.reserve(out.size() * rank_blocks.size());
+        for (const BlockRef &a : out)
+            for (const BlockRef &q : rank_blocks)
+                next.push_back({a.row * shape[r] + q.row, a.col * shape[r] + q.col, a.i0 * (size_t)t.ext[r] + q.i0,
+                                a.conj != q.conj});
+        out.swap(next);
+    }
+}
+
 extern "C" int pg_op_finalize(pg_op *op)
 {
     if (!op) return PG_ERR_ARG;
     if (op->finalized) return PG_ERR_STATE;
     const int N = op->N, b = op->b, kb = op->kb, nrows = op->nrows;
+    typedef std::complex<double> zc;
     struct Ent { int row, col, band, slot; };
-    std::vector<Ent> ents;
-    std::vector<std::complex<double>> bands;
-    auto add_band = [&](const double *pot) {
-        // reference slot j*b + (kb + i - j) -> device [d][i], d = j - i + kb
-        const int id = (int)(bands.size() / ((size_t)b * N));
-        bands.resize(bands.size() + (size_t)b * N);
-        std::complex<double> *B = bands.data() + (size_t)id * b * N;
-        for (int d = 0; d < b; ++d)
-            for (int i = 0; i < N; ++i) {
-                const int j = i + d - kb;
-                std::complex<double> v(0.0, 0.0);
-                if (j >= 0 && j < N) {
-                    const size_t s = (size_t)j * b + (kb + i - j);
-                    v = std::complex<double>(pot[2 * s], pot[2 * s + 1]);
-                }
-                B[(size_t)d * N + i] = v;
+    std::vector<Ent> ents, dents;
+    std::vector<zc> bands, dense;
+    // fibre block -> general band [d][i] (d = j - i + kb); false when it is all zero
+    auto radial_band = [&](const HostTerm &t, const double *pot, bool conj, std::vector<zc> &B) {
+        const std::string &inner = t.kinds.back();
+        B.assign((size_t)b * N, zc(0.0, 0.0));
+        auto val = [&](size_t s) { return zc(pot[2 * s], pot[2 * s + 1]); };
+        if (inner == "Simp") {  // (i, j) pair list, all within the band (checked by the caller)
+            const std::vector<int> &pr = t.pairs.back();
+            for (int p = 0; p < t.ext.back(); ++p) {
+                const int i = pr[2 * p], j = pr[2 * p + 1];
+                const zc v = conj ? std::conj(val(p)) : val(p);
+                B[(size_t)(j - i + kb) * N + i] += v;
             }
-        return id;
-    };
-    for (const HostTerm &t : op->terms) {
-        const size_t stride = (size_t)t.e1;
-        if (t.storage == "Diag_BandNH") {
-            for (int l = 0; l < nrows; ++l) ents.push_back({l, l, add_band(t.pot.data() + 2 * stride * l), t.slot});
-        } else if (t.storage == "Ident_BandNH") {
-            const int id = add_band(t.pot.data());
-            for (int l = 0; l < nrows; ++l) ents.push_back({l, l, id, t.slot});
         } else {
-            for (int p = 0; p < t.e0; ++p)
-                ents.push_back({t.pairs[2 * p], t.pairs[2 * p + 1], add_band(t.pot.data() + 2 * stride * p), t.slot});
+            for (int d = 0; d < b; ++d)
+                for (int i = 0; i < N; ++i) {
+                    const int j = i + d - kb;
+                    if (j < 0 || j >= N) continue;
+                    zc v(0.0, 0.0);
+                    if (inner == "BandNH") {
+                        v = val((size_t)j * b + (kb + i - j));  // zgbmv band layout, :700-723
+                        if (conj) v = std::conj(v);
+                    } else if (inner == "Band") {
+                        // zhbmv('L') (:585-600): lower triangle column-major with lda = kb + 1,
+                        // upper = conjugate, imaginary part of the diagonal ignored. The reference
+                        // calls zhbmv whatever the conjugate flag, and so does this expansion.
+                        const int kl = kb + 1;
+                        if (i > j) v = val((size_t)j * kl + (i - j));
+                        else if (i < j) v = std::conj(val((size_t)i * kl + (j - i)));
+                        else v = zc(val((size_t)j * kl).real(), 0.0);
+                    } else if (inner == "Diag") {
+                        if (i == j) v = conj ? std::conj(val(i)) : val(i);
+                    } else {  // Ident: one value for the whole diagonal
+                        if (i == j) v = conj ? std::conj(val(0)) : val(0);
+                    }
+                    B[(size_t)d * N + i] = v;
+                }
+        }
+        for (const zc &v : B)
+            if (v != zc(0.0, 0.0)) return true;
+        return false;
+    };
+    // fibre block -> dense [j][i] (transposed); false when it is all zero
+    auto radial_dense = [&](const HostTerm &t, const double *pot, bool conj, std::vector<zc> &D) {
+        const std::string &inner = t.kinds.back();
+        D.assign((size_t)N * N, zc(0.0, 0.0));
+        auto val = [&](size_t s) { return zc(pot[2 * s], pot[2 * s + 1]); };
+        if (inner == "Dense") {  // :1268-1275, index row * N + col
+            for (int i = 0; i < N; ++i)
+                for (int j = 0; j < N; ++j) D[(size_t)j * N + i] = conj ? std::conj(val((size_t)i * N + j)) : val((size_t)i * N + j);
+        } else {  // Simp pairs reaching outside the band
+            const std::vector<int> &pr = t.pairs.back();
+            for (int p = 0; p < t.ext.back(); ++p)
+                D[(size_t)pr[2 * p + 1] * N + pr[2 * p]] += conj ? std::conj(val(p)) : val(p);
+        }
+        for (const zc &v : D)
+            if (v != zc(0.0, 0.0)) return true;
+        return false;
+    };
+    std::vector<BlockRef> blocks;
+    std::vector<zc> B;
+    for (const HostTerm &t : op->terms) {
+        expand_outer(t, op->shape, blocks);
+        const size_t stride = (size_t)t.ext.back();
+        const std::string &inner = t.kinds.back();
+        bool as_dense = inner == "Dense";
+        if (inner == "Simp") {
+            const std::vector<int> &pr = t.pairs.back();
+            for (int p = 0; p < t.ext.back() && !as_dense; ++p) as_dense = std::abs(pr[2 * p] - pr[2 * p + 1]) > kb;
+        }
+        // blocks that read the same potential entry (Ident ranks, both Herm halves of a
+        // real block, ...) share one device copy; -1 marks an all-zero block
+        std::map<std::pair<size_t, bool>, int> made;
+        for (const BlockRef &br : blocks) {
+            const auto key = std::make_pair(br.i0, br.conj);
+            auto it = made.find(key);
+            int id;
+            if (it != made.end()) {
+                id = it->second;
+            } else {
+                const double *pot = t.pot.data() + 2 * stride * br.i0;
+                id = -1;
+                if (as_dense) {
+                    if (radial_dense(t, pot, br.conj, B)) {
+                        id = (int)(dense.size() / ((size_t)N * N));
+                        dense.insert(dense.end(), B.begin(), B.end());
+                    }
+                } else if (radial_band(t, pot, br.conj, B)) {
+                    id = (int)(bands.size() / ((size_t)b * N));
+                    bands.insert(bands.end(), B.begin(), B.end());
+                }
+                made[key] = id;
+            }
+            if (id < 0) continue;  // an all-zero block adds nothing
+            (as_dense ? dents : ents).push_back({br.row, br.col, id, t.slot});
         }
     }
-    std::stable_sort(ents.begin(), ents.end(), [](const Ent &a, const Ent &c) { return a.row < c.row; });
-    op->h_row_ptr.assign(nrows + 1, 0);
-    for (const Ent &e : ents) op->h_row_ptr[e.row + 1]++;
-    for (int r = 0; r < nrows; ++r) op->h_row_ptr[r + 1] += op->h_row_ptr[r];
+    auto build_csr = [&](std::vector<Ent> &e, std::vector<int> &row_ptr) {
+        std::stable_sort(e.begin(), e.end(), [](const Ent &a, const Ent &c) { return a.row < c.row; });
+        row_ptr.assign(nrows + 1, 0);
+        for (const Ent &x : e) row_ptr[x.row + 1]++;
+        for (int r = 0; r < nrows; ++r) row_ptr[r + 1] += row_ptr[r];
+    };
+    build_csr(ents, op->h_row_ptr);
     op->h_ent_col.clear(); op->h_ent_band.clear(); op->h_ent_slot.clear();
     for (const Ent &e : ents) {
         op->h_ent_col.push_back(e.col);
@@ -470,6 +737,34 @@ extern "C" int pg_op_finalize(pg_op *op)
     }
     int st = (op->precision == PG_FP64) ? upload_bands<double>(op) : upload_bands<float>(op);
     if (st != PG_OK) return st;
+    if (!dents.empty()) {
+        std::vector<int> drow;
+        build_csr(dents, drow);
+        std::vector<int> dcol, dmat, dslot;
+        for (const Ent &e : dents) { dcol.push_back(e.col); dmat.push_back(e.band); dslot.push_back(e.slot); }
+        op->ndense = (int)(dense.size() / ((size_t)N * N));
+        op->ndense_entries = (long long)dents.size();
+        PG_CUDA_TRY(cudaMalloc(&op->d_drow_ptr, (nrows + 1) * sizeof(int)));
+        PG_CUDA_TRY(cudaMalloc(&op->d_dent_col, dents.size() * sizeof(int)));
+        PG_CUDA_TRY(cudaMalloc(&op->d_dent_mat, dents.size() * sizeof(int)));
+        PG_CUDA_TRY(cudaMalloc(&op->d_dent_slot, dents.size() * sizeof(int)));
+        PG_CUDA_TRY(cudaMemcpy(op->d_drow_ptr, drow.data(), (nrows + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        PG_CUDA_TRY(cudaMemcpy(op->d_dent_col, dcol.data(), dcol.size() * sizeof(int), cudaMemcpyHostToDevice));
+        PG_CUDA_TRY(cudaMemcpy(op->d_dent_mat, dmat.data(), dmat.size() * sizeof(int), cudaMemcpyHostToDevice));
+        PG_CUDA_TRY(cudaMemcpy(op->d_dent_slot, dslot.data(), dslot.size() * sizeof(int), cudaMemcpyHostToDevice));
+        const size_t cnt = dense.size();
+        if (op->precision == PG_FP64) {
+            std::vector<cxd> tmp(cnt);
+            for (size_t q = 0; q < cnt; ++q) tmp[q] = mk<double>(dense[q].real(), dense[q].imag());
+            PG_CUDA_TRY(cudaMalloc(&op->d_dense, cnt * sizeof(cxd)));
+            PG_CUDA_TRY(cudaMemcpy(op->d_dense, tmp.data(), cnt * sizeof(cxd), cudaMemcpyHostToDevice));
+        } else {
+            std::vector<cxf> tmp(cnt);
+            for (size_t q = 0; q < cnt; ++q) tmp[q] = mk<float>((float)dense[q].real(), (float)dense[q].imag());
+            PG_CUDA_TRY(cudaMalloc(&op->d_dense, cnt * sizeof(cxf)));
+            PG_CUDA_TRY(cudaMemcpy(op->d_dense, tmp.data(), cnt * sizeof(cxf), cudaMemcpyHostToDevice));
+        }
+    }
     op->finalized = true;
     return PG_OK;
 }
@@ -477,7 +772,7 @@ extern "C" int pg_op_finalize(pg_op *op)
 extern "C" long long pg_op_stored_elements(const pg_op *op)
 {
     if (!op) return -1;
-    return (long long)op->nbands * op->b * op->N;
+    return (long long)op->nbands * op->b * op->N + (long long)op->ndense * op->N * op->N;
 }
 
 extern "C" int pg_op_matvec(pg_op *op, const double *scales, int nscales, const void *src, void *dst, int accumulate)

@@ -113,16 +113,18 @@ struct OpDev {
 
 struct HostTerm {
     std::string storage;
-    std::vector<double> pot;  // complex interleaved, reference layout
-    int e0 = 0, e1 = 0;
-    std::vector<int> pairs;   // (row, col) for Simp
+    std::vector<std::string> kinds;        // storage id of each rank ("Simp", "BandNH", ...)
+    std::vector<int> ext;                  // potential extent of each rank
+    std::vector<std::vector<int>> pairs;   // (row, col) lists of the ranks that have one
+    std::vector<double> pot;               // complex interleaved, reference layout
     int slot = 0;
 };
 
 struct pg_op {
     pg_ctx *ctx = nullptr;
     int rank = 2;
-    int nrows = 0, N = 0, kb = 0, b = 0;
+    std::vector<int> shape;  // extents of the wavefunction ranks
+    int nrows = 0, N = 0, kb = 0, b = 0;  // nrows: product of all but the last extent
     int precision = PG_FP64;
     std::vector<HostTerm> terms;
     bool finalized = false;
@@ -143,12 +145,19 @@ struct pg_op {
     // host copy of bands in diagonal-major form (complex128), kept for preconditioner setup
     std::vector<std::complex<double>> h_bands;   // [nbands][b][N]
     std::vector<int> h_row_ptr, h_ent_col, h_ent_band, h_ent_slot;
+    // radial ranks stored dense (N x N per angular pair), a second CSR over the rows
+    int ndense = 0;
+    long long ndense_entries = 0;
+    int *d_drow_ptr = nullptr, *d_dent_col = nullptr, *d_dent_mat = nullptr, *d_dent_slot = nullptr;
+    void *d_dense = nullptr;  // [ndense][j][i] (transposed: thread i reads row j contiguously)
 };
 
 // matvec launcher shared by the drivers: dst = acc*dst + sum scales * V src
 // scales_dev (optional) overrides `scales` when non-null.
 int pg_op_matvec_dev(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src,
                      void *dst, int accumulate, const double *src_inv_scale_dev, void *src_copy_out);
+// kernels one pg_op_matvec_dev call launches (banded part, plus the dense part when present)
+int pg_op_matvec_kernels(const pg_op *op);
 
 // ------------------------------------------------------------------------------------
 // banded fibre operators
@@ -187,10 +196,14 @@ int pg_banded_apply_dev(pg_banded *b, int which, void *x);
 // red_out[2j], red_out[2j+1] = h[j]; red_out[2J] = ||w||^2.
 // With Jdev non-null the column count is *Jdev + 1 (read on the device; J is then the
 // host-side upper bound used for the scratch check).
+// With atomic != 0 the cross-CTA sums are FP64 atomic adds into out_dev, which must hold
+// zeros on entry (the consumer clears it after reading); out_dev[2J+1] (the norm) is then
+// not written. Otherwise the last CTA to finish sums the partials (deterministic order).
 template <typename R>
 int pg_multidot(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const cx<R> *w, long long n, double *out_dev,
-                const int *Jdev = nullptr);
-// w -= sum_j V[j] h[j] with h complex128 on device; then, if J2 > 0, out2 = V[0..J2)^H w and ||w||^2
+                const int *Jdev = nullptr, int atomic = 0);
+// w -= sum_j V[j] h[j] with h complex128 on device; then the dots V[0..J)^H w (want_dots)
+// and ||w||^2 into out_dev as pg_multidot
 template <typename R>
 int pg_gs_update(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const double *h_dev, cx<R> *w, long long n,
-                 int want_dots, double *out_dev, const int *Jdev = nullptr);
+                 int want_dots, double *out_dev, const int *Jdev = nullptr, int atomic = 0);

@@ -11,8 +11,10 @@
 #include <algorithm>
 #include <mutex>
 
-static const int RED_THREADS = 256;
-static const int RED_ELEMS = 4;  // elements per thread per chunk pass
+static const int RED_THREADS = 128;
+static const int RED_WARPS = RED_THREADS / 32;
+static const int RED_ELEMS = 1;  // elements per thread before another CTA is added
+static const int RED_CB = 16;    // columns per register block
 
 static inline int red_blocks(pg_ctx *ctx, long long n)
 {
@@ -29,43 +31,74 @@ template <typename R> __device__ __forceinline__ R warp_sum(R v)
     return v;
 }
 
-// Block-reduce two values; result valid in thread 0.
-template <typename R> __device__ __forceinline__ void block_sum2(R &a, R &b, R *sm)
+// acc += conj(a) * b
+template <typename R> __device__ __forceinline__ void cdot_acc(R &ax, R &ay, cx<R> a, cx<R> b)
 {
-    a = warp_sum(a);
-    b = warp_sum(b);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) { sm[2 * wid] = a; sm[2 * wid + 1] = b; }
-    __syncthreads();
-    if (wid == 0) {
-        const int nw = blockDim.x >> 5;
-        a = lane < nw ? sm[2 * lane] : (R)0;
-        b = lane < nw ? sm[2 * lane + 1] : (R)0;
-        a = warp_sum(a);
-        b = warp_sum(b);
-    }
+    ax = fma(a.x, b.x, ax);
+    ax = fma(a.y, b.y, ax);
+    ay = fma(a.x, b.y, ay);
+    ay = fma(-a.y, b.x, ay);
 }
 
-// Final cross-block reduction by the last CTA. partial: [nblocks][ncols] complex128.
-__device__ void finish_reduction(double *partial, int ncols, unsigned int *counter, double *out, bool last)
+// Column sums over this CTA's element range [lo, hi) for columns [jbeg, J]: column j < J is
+// <V_j, w>, column J is ||w||^2. Each thread walks its elements once per block of RED_CB
+// columns, so RED_CB independent loads are in flight per element. Only the columns in use
+// are reduced across the warp (FP64 arithmetic is scarce on this GPU, so no work is spent
+// on empty columns); the CTA sum of each column is formed in FP64 and either added to
+// atomic_out (FP64 atomics; the consumer clears the buffer after reading it) or stored as
+// partial[col][blockIdx] for the last-CTA pass.
+template <typename R>
+__device__ __forceinline__ void column_sums(const cx<R> *__restrict__ V, long long ldv, int J, int jbeg,
+                                            const cx<R> *w, long long lo, long long hi, double (*red)[2 * PG_RED_COLS],
+                                            double *partial, double *atomic_out)
 {
-    if (!last) return;
-    __threadfence();
-    const volatile double *vp = partial;  // other CTAs' partials: read past L1
-    for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
-        double sx = 0.0, sy = 0.0;
-        for (int blk = 0; blk < (int)gridDim.x; ++blk) {
-            sx += vp[2 * ((size_t)blk * ncols + c)];
-            sy += vp[2 * ((size_t)blk * ncols + c) + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ncols = J + 1;
+    for (int j0 = jbeg; j0 < ncols; j0 += RED_CB) {
+        R ax[RED_CB], ay[RED_CB];
+#pragma unroll
+        for (int c = 0; c < RED_CB; ++c) ax[c] = ay[c] = (R)0;
+        for (long long i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
+            const cx<R> b = w[i];
+#pragma unroll
+            for (int c = 0; c < RED_CB; ++c) {
+                const int j = j0 + c;
+                if (j < J) {
+                    cdot_acc(ax[c], ay[c], V[(size_t)j * ldv + i], b);
+                } else if (j == J) {
+                    ax[c] = fma(b.x, b.x, ax[c]);
+                    ax[c] = fma(b.y, b.y, ax[c]);
+                }
+            }
         }
-        out[2 * c] = sx;
-        out[2 * c + 1] = sy;
+#pragma unroll
+        for (int c = 0; c < RED_CB; ++c) {
+            const int j = j0 + c;
+            if (j < ncols) {  // warp-uniform
+                const R sx = warp_sum(ax[c]);
+                const R sy = (j < J) ? warp_sum(ay[c]) : (R)0;
+                if (lane == 0) {
+                    red[warp][2 * j] = (double)sx;
+                    red[warp][2 * j + 1] = (double)sy;
+                }
+            }
+        }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        // column ncols-1 holds ||w||^2 in its real part: publish sqrt next to it
-        *counter = 0;
+    for (int j = jbeg + (int)threadIdx.x; j < ncols; j += RED_THREADS) {
+        double sx = 0.0, sy = 0.0;
+#pragma unroll
+        for (int q = 0; q < RED_WARPS; ++q) {
+            sx += red[q][2 * j];
+            sy += red[q][2 * j + 1];
+        }
+        if (atomic_out) {
+            atomicAdd(atomic_out + 2 * j, sx);
+            if (j < J) atomicAdd(atomic_out + 2 * j + 1, sy);
+        } else {
+            partial[(size_t)(2 * j) * gridDim.x + blockIdx.x] = sx;
+            partial[(size_t)(2 * j + 1) * gridDim.x + blockIdx.x] = sy;
+        }
     }
 }
 
@@ -82,137 +115,135 @@ __device__ __forceinline__ bool arrive_last(unsigned int *counter)
     return is_last;
 }
 
+// Final cross-CTA reduction by the last CTA to arrive: one warp per column, lanes reading
+// consecutive CTAs' partials (from L2: other CTAs wrote them), FP64 throughout. Columns
+// below jbeg are zero. out[2J+1] = sqrt(out[2J]); the ticket is reset for the next launch.
+__device__ void finish_reduction(const double *partial, int J, int jbeg, unsigned int *counter, double *out)
+{
+    __threadfence();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ncols = J + 1;
+    const int nb = (int)gridDim.x;
+    for (int j = warp; j < ncols; j += RED_WARPS) {
+        double sx = 0.0, sy = 0.0;
+        if (j >= jbeg) {
+            const double *px = partial + (size_t)(2 * j) * nb;
+            const double *py = partial + (size_t)(2 * j + 1) * nb;
+            double ax[4] = {0.0, 0.0, 0.0, 0.0}, ay[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int b0 = 0; b0 < nb; b0 += 128) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int blk = b0 + 32 * u + lane;
+                    if (blk < nb) {
+                        ax[u] += __ldcg(px + blk);
+                        ay[u] += __ldcg(py + blk);
+                    }
+                }
+            }
+            sx = warp_sum((ax[0] + ax[1]) + (ax[2] + ax[3]));
+            sy = warp_sum((ay[0] + ay[1]) + (ay[2] + ay[3]));
+        }
+        if (lane == 0) {
+            out[2 * j] = sx;
+            out[2 * j + 1] = sy;
+            if (j == J) out[2 * J + 1] = sqrt(sx);
+        }
+    }
+    if (threadIdx.x == 0) *counter = 0;
+}
+
 // out[2j..2j+1] = <V_j, w> (j < J); out[2J] = ||w||^2, out[2J+1] = ||w||.
+// With atomic_out the CTA sums are added to atomic_out (zero on entry; no square root).
 template <typename R>
 __global__ void __launch_bounds__(RED_THREADS) multidot_kernel(const cx<R> *__restrict__ V, long long ldv, int J,
                                                                const int *__restrict__ Jdev, const cx<R> *__restrict__ w,
                                                                long long n, double *partial, unsigned int *counter,
-                                                               double *out)
+                                                               double *out, double *atomic_out)
 {
-    __shared__ R sm[64];
+    __shared__ double red[RED_WARPS][2 * PG_RED_COLS];
     if (Jdev) J = min(*Jdev + 1, J);  // device count, bounded by the host-checked maximum
     const long long chunk = (n + gridDim.x - 1) / gridDim.x;
     const long long lo = (long long)blockIdx.x * chunk;
     const long long hi = min(n, lo + chunk);
-    const int ncols = J + 1;
-    for (int j = 0; j <= J; ++j) {
-        R ax = 0, ay = 0;
-        if (j < J) {
-            const cx<R> *v = V + (size_t)j * ldv;
-            for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-                const cx<R> a = v[i], b = w[i];
-                ax = fma(a.x, b.x, ax); ax = fma(a.y, b.y, ax);
-                ay = fma(a.x, b.y, ay); ay = fma(-a.y, b.x, ay);
-            }
-        } else {
-            for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-                const cx<R> b = w[i];
-                ax = fma(b.x, b.x, ax); ax = fma(b.y, b.y, ax);
-            }
-        }
-        block_sum2(ax, ay, sm);
-        if (threadIdx.x == 0) {
-            partial[2 * ((size_t)blockIdx.x * ncols + j)] = (double)ax;
-            partial[2 * ((size_t)blockIdx.x * ncols + j) + 1] = (double)ay;
-        }
-    }
-    const bool last = arrive_last(counter);
-    finish_reduction(partial, ncols, counter, out, last);
-    if (last && threadIdx.x == 0) out[2 * J + 1] = sqrt(out[2 * J]);
+    column_sums<R>(V, ldv, J, 0, w, lo, hi, red, partial, atomic_out);
+    if (atomic_out) return;
+    if (arrive_last(counter)) finish_reduction(partial, J, 0, counter, out);
 }
 
-// w -= sum_j V_j h_j (h complex128 on device); then optional dots <V_j, w> (j < J) and
-// ||w||^2 into out exactly as multidot_kernel.
+// w -= sum_j V_j h_j (h complex128 on device); then the dots <V_j, w> (j < J, when
+// want_dots) and ||w||^2 into out exactly as multidot_kernel.
 template <typename R>
 __global__ void __launch_bounds__(RED_THREADS) gs_update_kernel(const cx<R> *__restrict__ V, long long ldv, int J,
                                                                 const int *__restrict__ Jdev,
                                                                 const double *__restrict__ h, cx<R> *__restrict__ w,
                                                                 long long n, int want_dots, double *partial,
-                                                                unsigned int *counter, double *out)
+                                                                unsigned int *counter, double *out, double *atomic_out)
 {
-    __shared__ R sm[64];
-    if (Jdev) J = min(*Jdev + 1, J);  // device count, bounded by the host-checked maximum
+    __shared__ double red[RED_WARPS][2 * PG_RED_COLS];
     __shared__ cx<R> hs[PG_RED_COLS];
+    if (Jdev) J = min(*Jdev + 1, J);  // device count, bounded by the host-checked maximum
     for (int j = threadIdx.x; j < J; j += blockDim.x) hs[j] = mk<R>((R)h[2 * j], (R)h[2 * j + 1]);
     __syncthreads();
     const long long chunk = (n + gridDim.x - 1) / gridDim.x;
     const long long lo = (long long)blockIdx.x * chunk;
     const long long hi = min(n, lo + chunk);
-    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    for (long long i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
         cx<R> acc = w[i];
-        for (int j = 0; j < J; ++j) {
-            const cx<R> v = V[(size_t)j * ldv + i];
-            const cx<R> c = hs[j];
-            acc.x = fma(-v.x, c.x, acc.x); acc.x = fma(v.y, c.y, acc.x);
-            acc.y = fma(-v.x, c.y, acc.y); acc.y = fma(-v.y, c.x, acc.y);
+        for (int j0 = 0; j0 < J; j0 += RED_CB) {
+            cx<R> v[RED_CB];
+#pragma unroll
+            for (int c = 0; c < RED_CB; ++c)
+                v[c] = (j0 + c < J) ? V[(size_t)(j0 + c) * ldv + i] : mk<R>((R)0, (R)0);
+#pragma unroll
+            for (int c = 0; c < RED_CB; ++c)
+                if (j0 + c < J) {
+                    const cx<R> hc = hs[j0 + c];
+                    acc.x = fma(-v[c].x, hc.x, acc.x);
+                    acc.x = fma(v[c].y, hc.y, acc.x);
+                    acc.y = fma(-v[c].x, hc.y, acc.y);
+                    acc.y = fma(-v[c].y, hc.x, acc.y);
+                }
         }
-        w[i] = acc;
+        w[i] = acc;  // read back below by this same thread only
     }
-    __syncthreads();
-    const int ncols = J + 1;
-    for (int j = want_dots ? 0 : J; j <= J; ++j) {
-        R ax = 0, ay = 0;
-        if (j < J) {
-            const cx<R> *v = V + (size_t)j * ldv;
-            for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-                const cx<R> a = v[i], b = w[i];
-                ax = fma(a.x, b.x, ax); ax = fma(a.y, b.y, ax);
-                ay = fma(a.x, b.y, ay); ay = fma(-a.y, b.x, ay);
-            }
-        } else {
-            for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-                const cx<R> b = w[i];
-                ax = fma(b.x, b.x, ax); ax = fma(b.y, b.y, ax);
-            }
-        }
-        block_sum2(ax, ay, sm);
-        if (threadIdx.x == 0) {
-            partial[2 * ((size_t)blockIdx.x * ncols + j)] = (double)ax;
-            partial[2 * ((size_t)blockIdx.x * ncols + j) + 1] = (double)ay;
-        }
-    }
-    if (!want_dots) {
-        // columns < J untouched: zero them so the final sum is well defined
-        if (threadIdx.x < J) {
-            partial[2 * ((size_t)blockIdx.x * ncols + threadIdx.x)] = 0.0;
-            partial[2 * ((size_t)blockIdx.x * ncols + threadIdx.x) + 1] = 0.0;
-        }
-    }
-    const bool last = arrive_last(counter);
-    finish_reduction(partial, ncols, counter, out, last);
-    if (last && threadIdx.x == 0) out[2 * J + 1] = sqrt(out[2 * J]);
+    const int jbeg = want_dots ? 0 : J;
+    column_sums<R>(V, ldv, J, jbeg, w, lo, hi, red, partial, atomic_out);
+    if (atomic_out) return;
+    if (arrive_last(counter)) finish_reduction(partial, J, jbeg, counter, out);
 }
 
 template <typename R>
 int pg_multidot(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const cx<R> *w, long long n, double *out_dev,
-                const int *Jdev)
+                const int *Jdev, int atomic)
 {
     if (J + 1 > ctx->red_max_cols) return PG_ERR_ARG;
     const int nb = red_blocks(ctx, n);
     multidot_kernel<R><<<nb, RED_THREADS, 0, ctx->stream>>>(V, ldv, J, Jdev, w, n, ctx->red_partial, ctx->red_counter,
-                                                            out_dev);
+                                                            out_dev, atomic ? out_dev : nullptr);
     ctx->launches++;
     return pg_check_launch(ctx);
 }
 
 template <typename R>
 int pg_gs_update(pg_ctx *ctx, const cx<R> *V, long long ldv, int J, const double *h_dev, cx<R> *w, long long n,
-                 int want_dots, double *out_dev, const int *Jdev)
+                 int want_dots, double *out_dev, const int *Jdev, int atomic)
 {
     if (J + 1 > ctx->red_max_cols) return PG_ERR_ARG;
     const int nb = red_blocks(ctx, n);
     gs_update_kernel<R><<<nb, RED_THREADS, 0, ctx->stream>>>(V, ldv, J, Jdev, h_dev, w, n, want_dots, ctx->red_partial,
-                                                            ctx->red_counter, out_dev);
+                                                            ctx->red_counter, out_dev, atomic ? out_dev : nullptr);
     ctx->launches++;
     return pg_check_launch(ctx);
 }
 
-template int pg_multidot<double>(pg_ctx *, const cxd *, long long, int, const cxd *, long long, double *, const int *);
-template int pg_multidot<float>(pg_ctx *, const cxf *, long long, int, const cxf *, long long, double *, const int *);
+template int pg_multidot<double>(pg_ctx *, const cxd *, long long, int, const cxd *, long long, double *, const int *,
+                                 int);
+template int pg_multidot<float>(pg_ctx *, const cxf *, long long, int, const cxf *, long long, double *, const int *,
+                                int);
 template int pg_gs_update<double>(pg_ctx *, const cxd *, long long, int, const double *, cxd *, long long, int, double *,
-                                  const int *);
+                                  const int *, int);
 template int pg_gs_update<float>(pg_ctx *, const cxf *, long long, int, const double *, cxf *, long long, int, double *,
-                                 const int *);
+                                 const int *, int);
 
 // ------------------------------------------------------------------------------------
 // elementwise helpers
@@ -419,10 +450,10 @@ extern "C" int pg_vec_multidot_noalloc(int precision, const void *V, long long l
     const int nb = (int)std::max<long long>(1, std::min<long long>((n + per - 1) / per, d->max_blocks));
     if (precision == PG_FP64)
         multidot_kernel<double><<<nb, RED_THREADS, 0, s>>>((const cxd *)V, ldv, J, nullptr, (const cxd *)w, n,
-                                                           d->partial, d->ticket, out);
+                                                           d->partial, d->ticket, out, nullptr);
     else
         multidot_kernel<float><<<nb, RED_THREADS, 0, s>>>((const cxf *)V, ldv, J, nullptr, (const cxf *)w, n,
-                                                          d->partial, d->ticket, out);
+                                                          d->partial, d->ticket, out, nullptr);
     PG_CUDA_TRY(cudaGetLastError());
     return PG_OK;
 }

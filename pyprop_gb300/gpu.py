@@ -120,7 +120,7 @@ class DeviceOperator:
             self._add("Ident_BandNH", band, None, 0)
         for p, pot in enumerate(self.potentials):
             ids = "_".join(g.GetStorageId() for g in pot.GeometryList)
-            pairs = pot.GeometryList[0].GetBasisPairs() if ids.startswith("Simp") else None
+            pairs = pot.GeometryList[0].GetBasisPairs() if ids.startswith(("Simp", "Herm")) else None
             self._add(ids, pot.PotentialData, pairs, 1 + p)
         check(self.lib.pg_op_finalize(self.h), "pg_op_finalize")
 

@@ -52,3 +52,61 @@ def infidelity(ref, psi, S=None):
         ip = np.vdot(ref, Sp)
         n1, n2 = np.vdot(ref, Sr).real, np.vdot(psi, Sp).real
     return float(1.0 - abs(ip) ** 2 / (n1 * n2))
+
+
+# ---------------------------------------------------------------------------------------
+# random potentials in every storage of the generated multiply kernels
+# ---------------------------------------------------------------------------------------
+OUTER_KINDS = ("Simp", "Herm", "Diag", "Ident", "Band", "BandNH", "Dense")
+INNER_KINDS = ("BandNH", "Band", "Dense", "Diag", "Ident")
+
+
+def radial_extent(inner, N, kb):
+    return {"BandNH": N * (2 * kb + 1), "Band": N * (kb + 1), "Dense": N * N, "Diag": N, "Ident": 1}[inner]
+
+
+def random_storage_term(outer, inner, nang, N, kb, seed, outer_band=3):
+    """(storage id, potential [e0][e1] complex128, pairs or None) with seeded random values."""
+    rng = np.random.default_rng(seed)
+    pairs = None
+    if outer in ("Simp", "Herm"):
+        pairs = np.array([(r, c) for r in range(nang) for c in range(nang) if abs(r - c) <= 1 and (r + c) % 3 != 2],
+                         dtype=np.int32)
+        e0 = len(pairs)
+    elif outer == "Diag":
+        e0 = nang
+    elif outer == "Ident":
+        e0 = 1
+    elif outer == "Dense":
+        e0 = nang * nang
+    elif outer == "Band":
+        e0 = nang * outer_band
+    else:  # BandNH, odd band count
+        e0 = nang * (2 * (outer_band // 2) + 1)
+    e1 = radial_extent(inner, N, kb)
+    pot = rng.standard_normal((e0, e1)) + 1j * rng.standard_normal((e0, e1))
+    return "%s_%s" % (outer, inner), pot, pairs
+
+
+class FakeGeometry:
+    def __init__(self, storage_id, pairs=None):
+        self.sid, self.pairs = storage_id, pairs
+
+    def GetStorageId(self):
+        return self.sid
+
+    def GetBasisPairs(self):
+        return self.pairs
+
+
+class FakePotential:
+    """The parts of a consolidated TensorPotential the device operator reads."""
+
+    def __init__(self, storage, data, pairs, factor=1.0):
+        outer, inner = storage.split("_")
+        self.GeometryList = [FakeGeometry(outer, pairs), FakeGeometry(inner)]
+        self.PotentialData = data
+        self.factor = factor
+
+    def GetTimeScaling(self, t):
+        return self.factor
