@@ -109,56 +109,89 @@ def radial_rows(kind, pot, N, kb, conj):
     return out
 
 
+def fibre_block(kind, pot, pairs, N, kb, conj):
+    """Last-rank block as ("band", rows (N, 2kb+1)) or ("dense", (N, N)).
+
+    Simp on the last rank (the generator's pair loop, :326-333) is a band when every pair
+    lies within kb of the diagonal, else dense; Dense follows :1268-1275 (row*N + col)."""
+    if kind == "Dense":
+        m = pot.reshape(N, N)
+        return "dense", (m.conj() if conj else m)
+    if kind == "Simp":
+        pairs = np.asarray(pairs).reshape(-1, 2)
+        v = pot.conj() if conj else pot
+        if np.all(np.abs(pairs[:, 0] - pairs[:, 1]) <= kb):
+            rows = np.zeros((N, 2 * kb + 1), dtype=np.complex128)
+            np.add.at(rows, (pairs[:, 0], kb + pairs[:, 1] - pairs[:, 0]), v)
+            return "band", rows
+        m = np.zeros((N, N), dtype=np.complex128)
+        np.add.at(m, (pairs[:, 0], pairs[:, 1]), v)
+        return "dense", m
+    return "band", radial_rows(kind, pot, N, kb, conj)
+
+
 class TermOracle:
     """One consolidated tensor potential in the reference layout, ready to multiply.
 
-    ``storage`` is "<angular>_<radial>"; banded radial blocks are kept as band rows
-    (``rows``, ``cols``, ``bands``), dense radial blocks (:1227-1330) as matrices
-    (``drows``, ``dcols``, ``dense``)."""
+    ``storage`` is "<rank0>_<rank1>[_<rank2>]"; the loops of rank r nest inside those of
+    rank r-1 (the generator's nesting), each mirrored Herm/Band pass toggling the conjugate
+    flag. Rows and columns flatten all ranks but the last (C order); banded last-rank blocks
+    are kept as band rows (``rows``, ``cols``, ``bands``), dense ones (:1227-1330) as matrices
+    (``drows``, ``dcols``, ``dense``). For rank 2, ``pairs`` is the angular pair list; for
+    rank 3 pass ``shape`` and a per-rank list of pair arrays."""
 
-    def __init__(self, storage, potential, pairs, nang, N, kb, time_function=None):
+    def __init__(self, storage, potential, pairs, nang, N, kb, time_function=None, shape=None):
         self.storage = storage
-        self.nang, self.N, self.kb = nang, N, kb
+        kinds = storage.split("_")
+        self.shape = tuple(shape) if shape is not None else (nang, N)
+        self.nang, self.N, self.kb = int(np.prod(self.shape[:-1])), self.shape[-1], kb
         self.time_function = time_function
-        outer, inner = storage.split("_")
         pot = np.asarray(potential, dtype=np.complex128)
         if pot.ndim == 1:
             pot = pot.reshape(1, -1)
-        blocks = outer_blocks(outer, pot.shape[0], pairs, nang)
-        b = 2 * kb + 1
-        self.rows = np.zeros(0, dtype=np.int64)
-        self.cols = np.zeros(0, dtype=np.int64)
-        self.bands = np.zeros((0, N, b), dtype=np.complex128)
-        self.drows = np.zeros(0, dtype=np.int64)
-        self.dcols = np.zeros(0, dtype=np.int64)
-        self.dense = np.zeros((0, N, N), dtype=np.complex128)
-        if not blocks:
-            return
-        rows = np.array([r for r, _, _, _ in blocks])
-        cols = np.array([c for _, c, _, _ in blocks])
-        if inner == "Dense":
-            mats = [pot[i].reshape(N, N) for _, _, i, _ in blocks]
-            self.dense = np.stack([m.conj() if cj else m for m, (_, _, _, cj) in zip(mats, blocks)])
-            self.drows, self.dcols = rows, cols
+        if len(kinds) == 2 and shape is None:
+            pairs_list = [pairs, None]
         else:
-            self.bands = np.stack([radial_rows(inner, pot[i], N, kb, cj) for _, _, i, cj in blocks])
-            self.rows, self.cols = rows, cols
+            pairs_list = list(pairs) if pairs is not None else [None] * len(kinds)
+        ext = pot.shape[:len(kinds) - 1] if pot.ndim >= len(kinds) else (pot.shape[0],)
+        blocks = [(0, 0, 0, False)]
+        for r, kind in enumerate(kinds[:-1]):
+            n = self.shape[r]
+            rb = outer_blocks(kind, ext[r], pairs_list[r], n)
+            blocks = [(a[0] * n + q[0], a[1] * n + q[1], a[2] * ext[r] + q[2], a[3] != q[3]) for a in blocks for q in rb]
+        flat = pot.reshape(int(np.prod(ext)), -1) if pot.size else np.zeros((0, 1), dtype=np.complex128)
+        N, b = self.N, 2 * kb + 1
+        bl, db = [], []
+        for r, c, i, cj in blocks:
+            what, m = fibre_block(kinds[-1], flat[i], pairs_list[-1], N, kb, cj)
+            (bl if what == "band" else db).append((r, c, m))
+        self.rows = np.array([x[0] for x in bl], dtype=np.int64)
+        self.cols = np.array([x[1] for x in bl], dtype=np.int64)
+        self.bands = np.stack([x[2] for x in bl]) if bl else np.zeros((0, N, b), dtype=np.complex128)
+        self.drows = np.array([x[0] for x in db], dtype=np.int64)
+        self.dcols = np.array([x[1] for x in db], dtype=np.int64)
+        self.dense = np.stack([x[2] for x in db]) if db else np.zeros((0, N, N), dtype=np.complex128)
 
     def scaling(self, t):
         return 1.0 if self.time_function is None else float(self.time_function(t))
 
     def multiply(self, src, dest, scaling):
-        """dest += scaling * V src (loop over the angular blocks)."""
+        """dest += scaling * V src (src/dest flattened to (fibres, N) internally)."""
         kb = self.kb
+        shape = src.shape
+        src = src.reshape(-1, self.N)
+        d2 = dest.reshape(-1, self.N)
         if len(self.rows):
             pad = np.zeros((src.shape[0], src.shape[1] + 2 * kb), dtype=np.complex128)
             pad[:, kb:kb + src.shape[1]] = src
             win = sliding_window_view(pad, 2 * kb + 1, axis=1)  # win[c, i, d] = src[c, i+d-kb]
             y = np.einsum("pid,pid->pi", self.bands, win[self.cols])
-            np.add.at(dest, self.rows, scaling * y)
+            np.add.at(d2, self.rows, scaling * y)
         if len(self.drows):
             y = np.einsum("pij,pj->pi", self.dense, src[self.dcols])
-            np.add.at(dest, self.drows, scaling * y)
+            np.add.at(d2, self.drows, scaling * y)
+        if d2.base is not dest and d2 is not dest:
+            dest[...] = d2.reshape(shape)
 
 
 def tensor_multiply(terms, scalings, src, dest):

@@ -116,24 +116,31 @@ class DeviceOperator:
         self.h = h
         self.has_overlap = overlap_rows is not None
         if overlap_rows is not None:
+            if len(shape) != 2:
+                raise ValueError("the overlap slot is built for rank-2 operators")
             band = bandnh_from_rows(np.asarray(overlap_rows, dtype=np.float64), kb)[None, :]
-            self._add("Ident_BandNH", band, None, 0)
+            self._add(["Ident", "BandNH"], band, [None, None], 0)
         for p, pot in enumerate(self.potentials):
-            ids = "_".join(g.GetStorageId() for g in pot.GeometryList)
-            pairs = pot.GeometryList[0].GetBasisPairs() if ids.startswith(("Simp", "Herm")) else None
-            self._add(ids, pot.PotentialData, pairs, 1 + p)
+            kinds = [g.GetStorageId() for g in pot.GeometryList]
+            pairs = [g.GetBasisPairs() if k in ("Simp", "Herm") else None for g, k in zip(pot.GeometryList, kinds)]
+            self._add(kinds, pot.PotentialData, pairs, 1 + p)
         check(self.lib.pg_op_finalize(self.h), "pg_op_finalize")
 
-    def _add(self, ids, data, pairs, slot):
+    def _add(self, kinds, data, pairs, slot):
+        ids = "_".join(kinds)
+        rank = len(kinds)
         data = np.ascontiguousarray(data, dtype=np.complex128)
+        if data.ndim != rank:
+            data = data.reshape(data.shape[:rank - 1] + (-1,)) if data.ndim > rank else data.reshape((1,) * (rank - data.ndim) + data.shape)
         _, dp = nat.dptr(data.view(np.float64))
-        if pairs is not None:
-            pa, pp = nat.iptr(pairs)
-            npairs = pa.shape[0]
-        else:
-            pp, npairs = None, 0
-        check(self.lib.pg_op_add_term(self.h, ids.encode(), dp, data.shape[0], data.shape[1], pp, npairs, slot),
-              "pg_op_add_term(%s)" % ids)
+        ext = np.asarray(data.shape, dtype=np.int32)
+        lists = [np.asarray(pr, dtype=np.int32).reshape(-1, 2) for pr in pairs if pr is not None]
+        allp = np.ascontiguousarray(np.concatenate(lists) if lists else np.zeros((0, 2), dtype=np.int32))
+        npairs = np.asarray([0 if pr is None else len(np.asarray(pr).reshape(-1, 2)) for pr in pairs], dtype=np.int32)
+        _, ep = nat.iptr(ext)
+        _, pp = nat.iptr(allp)
+        _, npp = nat.iptr(npairs)
+        check(self.lib.pg_op_add_term_ranks(self.h, ids.encode(), dp, ep, pp, npp, slot), "pg_op_add_term(%s)" % ids)
 
     @property
     def nslots(self):

@@ -103,8 +103,11 @@ class FakePotential:
     """The parts of a consolidated TensorPotential the device operator reads."""
 
     def __init__(self, storage, data, pairs, factor=1.0):
-        outer, inner = storage.split("_")
-        self.GeometryList = [FakeGeometry(outer, pairs), FakeGeometry(inner)]
+        """pairs: the angular pair list (rank 2) or a per-rank list of pair arrays."""
+        kinds = storage.split("_")
+        if not isinstance(pairs, (list, tuple)):
+            pairs = [pairs] + [None] * (len(kinds) - 1)
+        self.GeometryList = [FakeGeometry(k, pr) for k, pr in zip(kinds, pairs)]
         self.PotentialData = data
         self.factor = factor
 

@@ -34,3 +34,26 @@ def test_storage_matvec_fp64_fp32(gpu, outer):
             op.matvec(np.array([0.0, 0.7 - 0.2j, 1.3]), src, dst, accumulate=True)
             got = dst.to(torch.complex128).cpu().numpy()
             assert relerr(got, ref) < tol, (sid, prec, relerr(got, ref))
+
+
+@pytest.mark.parametrize("storage", ["Diag_Simp_BandNH", "Simp_Simp_BandNH", "Herm_Simp_BandNH", "Diag_Simp_Simp",
+                                     "Simp_Diag_Band"])
+def test_rank3_matvec_fp64_fp32(gpu, storage):
+    import torch
+    from oracle.operators import TermOracle
+    from pyprop_gb300.gpu import Context, DeviceOperator
+    from tests.test_storages import rank3_case
+    pot, pairs, shape, kb = rank3_case(storage, nang=4, N=24, kb=3, seed=9)
+    # two-electron shape; the angular pair list must stay inside nang = 4
+    ctx = Context.get()
+    rng = np.random.default_rng(12)
+    x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    ref = np.zeros(shape, dtype=np.complex128)
+    TermOracle(storage, pot, pairs, None, None, kb, shape=shape).multiply(x, ref, 0.9 + 0.1j)
+    for prec, dt, tol in [(nat.PG_FP64, torch.complex128, 1e-13), (nat.PG_FP32, torch.complex64, 2e-5)]:
+        op = DeviceOperator(ctx, [FakePotential(storage, pot, pairs)], shape, kb, prec)
+        src = torch.as_tensor(x, device="cuda").to(dt)
+        dst = torch.zeros(shape, dtype=dt, device="cuda")
+        op.matvec(np.array([0.0, 0.9 + 0.1j]), src, dst)
+        got = dst.to(torch.complex128).cpu().numpy()
+        assert relerr(got, ref) < tol, (storage, prec, relerr(got, ref))

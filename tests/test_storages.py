@@ -119,3 +119,89 @@ def test_multiply_matches_dense_assembly(outer):
         t.multiply(x, y, 0.5)
         M = dense_operator([t], [0.5], NANG, N)
         assert np.abs(y.ravel() - M @ x.ravel()).max() < 1e-12, sid
+
+
+# ---------------------------------------------------------------------------------------
+# rank 3: [Nang][N][N] two-electron layout
+# ---------------------------------------------------------------------------------------
+def packed_pairs(n, k):
+    """banded-packed pairs (basis/BSpline.py:25-44): row-major, |i-j| < k."""
+    return np.array([(i, j) for i in range(n) for j in range(max(0, i - k + 1), min(n, i + k))], dtype=np.int32)
+
+
+def rank3_case(storage, nang=3, N=9, kb=2, seed=0):
+    rng = np.random.default_rng(seed)
+    k0, k1, k2 = storage.split("_")
+    ang_pairs = np.array([(0, 0), (0, 1), (1, 0), (1, 2), (2, 2)], dtype=np.int32)
+    r1_pairs = packed_pairs(N, kb + 1)
+    r2_pairs = packed_pairs(N, kb + 1)
+    e0 = {"Diag": nang, "Simp": len(ang_pairs), "Herm": len(ang_pairs)}[k0]
+    e1 = {"Simp": len(r1_pairs), "Diag": N}[k1]
+    e2 = {"BandNH": N * (2 * kb + 1), "Band": N * (kb + 1), "Simp": len(r2_pairs)}[k2]
+    pot = rng.standard_normal((e0, e1, e2)) + 1j * rng.standard_normal((e0, e1, e2))
+    pairs = [ang_pairs if k0 in ("Simp", "Herm") else None, r1_pairs if k1 == "Simp" else None,
+             r2_pairs if k2 == "Simp" else None]
+    return pot, pairs, (nang, N, N), kb
+
+
+def direct_rank3(storage, pot, pairs, shape, kb):
+    """Dense operator from the generated loops written out as three nested loops."""
+    nang, N, _ = shape
+    k0, k1, k2 = storage.split("_")
+    M = np.zeros((nang * N * N, nang * N * N), dtype=np.complex128)
+
+    def rank_loop(kind, pr, n):
+        if kind == "Diag":
+            return [(a, a, a, False) for a in range(n)]
+        out = [(int(r), int(c), p, False) for p, (r, c) in enumerate(pr)]
+        if kind == "Herm":
+            out += [(int(c), int(r), p, True) for p, (r, c) in enumerate(pr)]
+        return out
+
+    for a_r, a_c, ia, c0 in rank_loop(k0, pairs[0], nang):
+        for i_r, i_c, i1, c1 in rank_loop(k1, pairs[1], N):
+            v = pot[ia, i1]
+            conj = c0 != c1
+            blk = np.zeros((N, N), dtype=np.complex128)
+            if k2 == "BandNH":
+                b = 2 * kb + 1
+                for i in range(N):
+                    for j in range(max(0, i - kb), min(N, i + kb + 1)):
+                        blk[i, j] = v[j * b + kb + i - j]
+                if conj:
+                    blk = blk.conj()
+            elif k2 == "Band":  # zhbmv('L'), conjugate flag ignored, diagonal real
+                for i in range(N):
+                    for j in range(max(0, i - kb), i + 1):
+                        blk[i, j] = v[j * (kb + 1) + i - j]
+                        blk[j, i] = np.conj(blk[i, j])
+                    blk[i, i] = blk[i, i].real
+            else:  # Simp
+                for p, (i, j) in enumerate(pairs[2]):
+                    blk[i, j] += np.conj(v[p]) if conj else v[p]
+            r0 = (a_r * N + i_r) * N
+            c0_ = (a_c * N + i_c) * N
+            M[r0:r0 + N, c0_:c0_ + N] += blk
+    return M
+
+
+@pytest.mark.parametrize("storage", ["Diag_Simp_BandNH", "Simp_Simp_BandNH", "Herm_Simp_BandNH", "Diag_Simp_Simp",
+                                     "Simp_Diag_Band", "Herm_Simp_Simp"])
+def test_rank3_oracle_matches_direct_loops(storage):
+    pot, pairs, shape, kb = rank3_case(storage)
+    t = TermOracle(storage, pot, pairs, None, None, kb, shape=shape)
+    M = dense_operator([t], [1.0], shape[0] * shape[1], shape[2])
+    assert np.abs(M - direct_rank3(storage, pot, pairs, shape, kb)).max() < 1e-13
+    x = np.random.default_rng(3).standard_normal(shape) + 0j
+    y = np.zeros(shape, dtype=np.complex128)
+    t.multiply(x, y, 2.0)
+    assert np.abs(y.ravel() - 2.0 * M @ x.ravel()).max() < 1e-12
+
+
+def test_empty_pair_list_term():
+    # lmax = 0: the dipole term has no angular pairs and adds nothing
+    pot = np.zeros((0, N * (2 * KB + 1)), dtype=np.complex128)
+    t = TermOracle("Simp_BandNH", pot, np.zeros((0, 2), dtype=np.int32), 1, N, KB)
+    y = np.zeros((1, N), dtype=np.complex128)
+    t.multiply(np.ones((1, N), dtype=np.complex128), y, 1.0)
+    assert not y.any() and len(t.rows) == 0
