@@ -245,6 +245,19 @@ int pg_cayley_set_true_residual(pg_cayley *c, int on);
  * from the host (one wait per iteration). For profilers that cannot look inside
  * conditional graph nodes; results are identical to the graph mode. */
 int pg_cayley_set_eager(pg_cayley *c, int on);
+/*
+ * Learned preconditioner (no counterpart in the reference; mixed-precision steppers only).
+ * With a network set, each refinement pass runs flexible GMRES right-preconditioned by
+ *     P(v) = M^-1 v + s(t) * mlp(features(M^-1 v)),  s(t) = i dt/2 h_slot(t + dt/2)
+ * (M the block-diagonal radial LU, features as pg_mlp_block_features, d_out >= 2N). The FP64
+ * true residual judges each pass: a pass that does not halve it is discarded and the rest of
+ * the step uses M^-1 alone (the fallback). mlp == NULL switches the learned part off. The
+ * network must live on the stepper's context and outlive its use.
+ */
+struct pg_mlp;
+int pg_cayley_set_learned(pg_cayley *c, struct pg_mlp *mlp, int coupling_slot);
+/* passes rejected by the residual test so far (waits for the stream) */
+int pg_cayley_learned_rejected(pg_cayley *c, long long *out);
 
 /* Ensembles: many pg_cayley members (each with its own operator, basis size, field) advanced
  * together by one CUDA graph launch whose branches (one per member) run concurrently. The
@@ -285,6 +298,34 @@ int pg_vec_dot(pg_ctx *ctx, int precision, const void *x, const void *y, long lo
 int pg_vec_convert(pg_ctx *ctx, int src_precision, const void *x, int dst_precision, void *y, long long n);
 /* V (complex128 [k][n]) <- V (complex128 [m][n]) * Q (host complex128 [m][k], row major) */
 int pg_vec_combine(pg_ctx *ctx, void *V, long long n, int m, const double *Q, int k);
+
+/* ---------------------------------------------------------------------------------- */
+/* learned preconditioner network                                                     */
+/* ---------------------------------------------------------------------------------- */
+/*
+ * No counterpart in the reference (its Cayley preconditioners are fixed factorizations,
+ * pyprop/propagator/CayleyPropagator.py:56-63, examples/tensor/helium_stabilization/
+ * preconditioner.py:77-244). A bias-free 3-layer ReLU MLP, y = W3^T relu(W2^T relu(W1^T x)),
+ * one row per angular block: BF16 weights and activations into tensor-core products with
+ * FP32 accumulation; FP32 master weights, gradients and Adam moments. d_in, hidden and d_out
+ * must be multiples of 8. Weights on the host: FP32 [W1 d_in x hidden | W2 hidden x hidden |
+ * W3 hidden x d_out], row-major with fan-in rows. X is BF16 [batch][d_in], Y and T FP32
+ * [batch][d_out], all device pointers; the loss is mean over rows of ||y - t||^2.
+ */
+typedef struct pg_mlp pg_mlp;
+int pg_mlp_create(pg_ctx *ctx, int d_in, int hidden, int d_out, unsigned long long seed, pg_mlp **out);
+int pg_mlp_destroy(pg_mlp *m);
+long long pg_mlp_parameter_count(const pg_mlp *m);
+int pg_mlp_get_weights(pg_mlp *m, float *host);
+int pg_mlp_set_weights(pg_mlp *m, const float *host);  /* also resets the optimizer */
+int pg_mlp_forward(pg_mlp *m, const void *X_bf16, int batch, float *Y);
+/* loss and gradients (grads_host optional, FP32, layout of the weights) */
+int pg_mlp_gradients(pg_mlp *m, const void *X_bf16, const float *T, int batch, double *loss, float *grads_host);
+/* one Adam step (beta1 0.9, beta2 0.999, eps 1e-8); loss optional (waits when given) */
+int pg_mlp_train_step(pg_mlp *m, const void *X_bf16, const float *T, int batch, float lr, double *loss);
+/* network input of the block-preconditioned vector y (complex64 [nblk][N], device): row a =
+ * [y_{a-1}, y_a, y_{a+1}] real/imaginary interleaved, zero outside, padded to d_in >= 6N */
+int pg_mlp_block_features(pg_ctx *ctx, const void *y, int nblk, int N, int d_in, void *X_bf16);
 
 /* ---------------------------------------------------------------------------------- */
 /* allocation-free entry point                                                        */

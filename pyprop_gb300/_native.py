@@ -87,6 +87,8 @@ _SIGS = {
     "pg_cayley_last_stats": (_I, [_P, C.POINTER(KrylovStats)]),
     "pg_cayley_set_true_residual": (_I, [_P, _I]),
     "pg_cayley_set_eager": (_I, [_P, _I]),
+    "pg_cayley_set_learned": (_I, [_P, _P, _I]),
+    "pg_cayley_learned_rejected": (_I, [_P, C.POINTER(_LL)]),
     "pg_cayley_batch_create": (_I, [C.POINTER(_P), _I, C.POINTER(_P)]),
     "pg_cayley_batch_destroy": (_I, [_P]),
     "pg_cayley_batch_step": (_I, [_P, C.POINTER(_P), _D, _DP, _I]),
@@ -96,6 +98,15 @@ _SIGS = {
     "pg_vec_dot": (_I, [_P, _I, _P, _P, _LL, _DP]),
     "pg_vec_convert": (_I, [_P, _I, _P, _I, _P, _LL]),
     "pg_vec_combine": (_I, [_P, _P, _LL, _I, _DP, _I]),
+    "pg_mlp_create": (_I, [_P, _I, _I, _I, C.c_ulonglong, C.POINTER(_P)]),
+    "pg_mlp_destroy": (_I, [_P]),
+    "pg_mlp_parameter_count": (_LL, [_P]),
+    "pg_mlp_get_weights": (_I, [_P, _P]),
+    "pg_mlp_set_weights": (_I, [_P, _P]),
+    "pg_mlp_forward": (_I, [_P, _P, _I, _P]),
+    "pg_mlp_gradients": (_I, [_P, _P, _P, _I, _DP, _P]),
+    "pg_mlp_train_step": (_I, [_P, _P, _P, _I, C.c_float, _DP]),
+    "pg_mlp_block_features": (_I, [_P, _P, _I, _I, _I, _P]),
     "pg_vec_multidot_noalloc": (_I, [_I, _P, _LL, _I, _P, _LL, _P, _P]),
 }
 

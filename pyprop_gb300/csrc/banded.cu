@@ -48,18 +48,20 @@ template <typename R> __device__ __forceinline__ void coef_fms(cx<R> &acc, cx<R>
 // (lower sweep: the last w values of block b-1; upper sweep: the first w values of block
 // b+1), the solution of block b is
 //     y_b = z_b - G_b s,   z_b = T_b^-1 f_b,   G_b = T_b^-1 C_b   (G_b: 32 x w, precomputed).
-// So every z_b and every correction G_b s is independent work, spread over the CTA's warps
-// (lane t owns row 32b + t), and only the w-wide boundary recurrence
-//     s_b = z_b[boundary rows] - G_b[boundary rows] s_{b-1 or b+1}
-// is sequential: one step per block, w lanes of one warp, operands in shared memory.
-// The fibre stays in shared memory for both sweeps.
+// The boundary values of all blocks solve the block-bidiagonal system
+//     s_b + G_b[boundary rows] s_{b-/+1} = z_b[boundary rows],
+// whose inverse Rb (nblk*w square, block triangular) depends only on the factor, so it is
+// precomputed on the host: s = Rb z[boundary rows]. Every step is then parallel - z_b for all
+// blocks, the Rb product, the corrections G_b s - with no sequential recurrence left. Lane t
+// of a warp owns row 32b + t of block b; the fibre stays in shared memory for both sweeps.
 // C: coefficient type (R or cx<R>). inv: [nmat][nblk][32 s][32 t] = T^-1[t][s],
-// g: [nmat][nblk][w c][32 t] = G[t][c].
+// g: [nmat][nblk][w c][32 t] = G[t][c], rb: [nmat][nblk*w][nblk*w] row-major.
 template <typename R, typename C, int NW>
 __global__ void __launch_bounds__(32 * NW, 1)
     tri_solve_kernel(int N, int nblk, int w, const C *__restrict__ lo_inv, const C *__restrict__ lo_g,
-                     const C *__restrict__ up_inv, const C *__restrict__ up_g, int do_lower, int do_upper,
-                     int per_fibre_matrix, int g_in_smem, cx<R> *__restrict__ x, int nfib)
+                     const C *__restrict__ lo_rb, const C *__restrict__ up_inv, const C *__restrict__ up_g,
+                     const C *__restrict__ up_rb, int do_lower, int do_upper, int per_fibre_matrix, int g_in_smem,
+                     cx<R> *__restrict__ x, int nfib)
 {
     extern __shared__ __align__(16) unsigned char tri_smem[];
     const int lane = threadIdx.x & 31;
@@ -67,19 +69,18 @@ __global__ void __launch_bounds__(32 * NW, 1)
     const int f = blockIdx.x;
     if (f >= nfib) return;
     cx<R> *xs = (cx<R> *)tri_smem;              // [nblk*32] the fibre: f, then z, then y
-    cx<R> *sb = xs + (size_t)nblk * 32;          // [nblk][w] boundary values s_b
-    C *gt = (C *)(sb + (size_t)nblk * w);        // [nblk][w c][w r] boundary rows of G_b
-    C *sg = gt + (size_t)nblk * w * w;           // [nblk][w][32] G_b (when g_in_smem)
+    cx<R> *sb = xs + (size_t)nblk * 32;          // [nblk*w] boundary values s_b
+    C *sg = (C *)(sb + (size_t)nblk * w);        // [nblk][w][32] G_b (when g_in_smem)
     const size_t m = per_fibre_matrix ? (size_t)f : 0;
     const size_t gstride = (size_t)w * 32;
+    const int nb = nblk * w;
     cx<R> *xf = x + (size_t)f * N;
     for (int i = threadIdx.x; i < nblk * 32; i += 32 * NW) xs[i] = (i < N) ? xf[i] : mk<R>((R)0, (R)0);
     __syncthreads();
 
-    // z_b = T_b^-1 r for lane's row; G_b staged for the boundary recurrence and the correction
-    auto solve_block = [&](int blk, cx<R> r, const C *inv, const C *g, bool lower) {
+    // z_b = T_b^-1 r for lane's row; G_b staged for the correction
+    auto solve_block = [&](int blk, cx<R> r, const C *inv, const C *g) {
         const C *ib = inv + (m * nblk + blk) * 1024;
-        const C *gb = g + (m * nblk + blk) * gstride;
         cx<R> acc[4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) acc[a] = mk<R>((R)0, (R)0);
@@ -89,89 +90,73 @@ __global__ void __launch_bounds__(32 * NW, 1)
             for (int q = 0; q < 16; ++q) coef_fma(acc[q & 3], ib[(q0 + q) * 32 + lane], shfl_cx(r, q0 + q));
         }
         xs[blk * 32 + lane] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
-        const int r0 = lower ? 32 - w : 0;  // boundary rows of this block
-        for (int c = 0; c < w; ++c) {
-            const C v = gb[c * 32 + lane];
-            if (g_in_smem) sg[((size_t)blk * w + c) * 32 + lane] = v;
-            if (lane >= r0 && lane < r0 + w) gt[((size_t)blk * w + c) * w + (lane - r0)] = v;
+        if (g_in_smem) {
+            const C *gb = g + (m * nblk + blk) * gstride;
+            for (int c = 0; c < w; ++c) sg[((size_t)blk * w + c) * 32 + lane] = gb[c * 32 + lane];
         }
     };
-    // w-wide recurrence over the blocks (warp 0; lanes >= w mirror lane w-1 to keep shuffles
-    // whole). For w <= 8 the next block's operands are loaded while the current step's
-    // dependent chain runs, and the chain is split in two partial sums.
-    auto scan = [&](bool lower) {
-        if (warp != 0) return;
-        const int r = min(lane, w - 1);
+    // s = Rb z[boundary rows]: each warp takes BRW consecutive output rows at a time, lanes
+    // over the columns, so all of a lane's Rb loads for those rows are in flight together;
+    // the block-triangular zero part is skipped by a per-element predicate
+    auto boundary = [&](bool lower, const C *rb) {
+        constexpr int BRW = 8;
+        const C *Rm = rb + m * (size_t)nb * nb;
         const int r0 = lower ? 32 - w : 0;
-        int blk = lower ? 0 : nblk - 1;
-        cx<R> s = xs[blk * 32 + r0 + r];
-        if (lane < w) sb[blk * w + lane] = s;
-        if (w <= 8) {
-            C gn[8];
-            cx<R> zn = mk<R>((R)0, (R)0);
-            auto load = [&](int b) {
-                zn = xs[b * 32 + r0 + r];
-                const C *gtb = gt + (size_t)b * w * w;
+        for (int row0 = warp * BRW; row0 < nb; row0 += NW * BRW) {
+            cx<R> acc[BRW];
 #pragma unroll
-                for (int c = 0; c < 8; ++c) gn[c] = (c < w) ? gtb[c * w + r] : C{};
-            };
-            if (nblk > 1) load(lower ? 1 : nblk - 2);
-            for (int step = 1; step < nblk; ++step) {
-                blk = lower ? step : nblk - 1 - step;
-                C g[8];
+            for (int q = 0; q < BRW; ++q) acc[q] = mk<R>((R)0, (R)0);
+            const int bo_first = row0 / w, bo_last = min(row0 + BRW - 1, nb - 1) / w;
+            const int c_lo = lower ? 0 : bo_first * w, c_hi = lower ? (bo_last + 1) * w : nb;
+            for (int col = c_lo + lane; col < c_hi; col += 32) {
+                const int bc = col / w, rc = col - bc * w;
+                const cx<R> zc = xs[bc * 32 + r0 + rc];
 #pragma unroll
-                for (int c = 0; c < 8; ++c) g[c] = gn[c];
-                cx<R> acc0 = zn, acc1 = mk<R>((R)0, (R)0);
-                if (step + 1 < nblk) load(lower ? step + 1 : nblk - 2 - step);
-#pragma unroll
-                for (int c = 0; c < 8; ++c)
-                    if (c < w) {
-                        const cx<R> sc = shfl_cx(s, c);
-                        if (c & 1) coef_fms(acc1, g[c], sc);
-                        else coef_fms(acc0, g[c], sc);
-                    }
-                s = acc0 + acc1;
-                if (lane < w) sb[blk * w + lane] = s;
+                for (int q = 0; q < BRW; ++q) {
+                    const int row = row0 + q, bo = row / w;
+                    const bool nz = row < nb && (lower ? bc <= bo : bc >= bo);
+                    if (nz) coef_fma(acc[q], Rm[(size_t)row * nb + col], zc);
+                }
             }
-        } else {
-            for (int step = 1; step < nblk; ++step) {
-                blk = lower ? step : nblk - 1 - step;
-                cx<R> acc = xs[blk * 32 + r0 + r];
-                const C *gtb = gt + (size_t)blk * w * w;
-                for (int c = 0; c < w; ++c) coef_fms(acc, gtb[c * w + r], shfl_cx(s, c));
-                s = acc;
-                if (lane < w) sb[blk * w + lane] = s;
+#pragma unroll
+            for (int q = 0; q < BRW; ++q) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    acc[q].x += __shfl_xor_sync(0xffffffffu, acc[q].x, o);
+                    acc[q].y += __shfl_xor_sync(0xffffffffu, acc[q].y, o);
+                }
+                if (lane == 0 && row0 + q < nb) sb[row0 + q] = acc[q];
             }
         }
     };
     // y_b = z_b - G_b s (returns the corrected row)
     auto correct = [&](int blk, const C *g, bool lower) -> cx<R> {
         cx<R> y = xs[blk * 32 + lane];
-        const int nb = lower ? blk - 1 : blk + 1;
-        if (nb >= 0 && nb < nblk) {
+        const int nbk = lower ? blk - 1 : blk + 1;
+        if (nbk >= 0 && nbk < nblk) {
             const C *gb = g_in_smem ? sg + (size_t)blk * gstride : g + (m * nblk + blk) * gstride;
-            for (int c = 0; c < w; ++c) coef_fms(y, gb[c * 32 + lane], sb[nb * w + c]);
+            for (int c = 0; c < w; ++c) coef_fms(y, gb[c * 32 + lane], sb[nbk * w + c]);
         }
         return y;
     };
 
     if (do_lower) {
-        for (int blk = warp; blk < nblk; blk += NW) solve_block(blk, xs[blk * 32 + lane], lo_inv, lo_g, true);
+        for (int blk = warp; blk < nblk; blk += NW) solve_block(blk, xs[blk * 32 + lane], lo_inv, lo_g);
         __syncthreads();
-        scan(true);
+        boundary(true, lo_rb);
         __syncthreads();
         for (int blk = warp; blk < nblk; blk += NW) {
             const cx<R> y = correct(blk, lo_g, true);
-            if (do_upper) solve_block(blk, y, up_inv, up_g, false);  // same rows, same warp
+            if (do_upper) solve_block(blk, y, up_inv, up_g);  // same rows, same warp
             else xs[blk * 32 + lane] = y;
         }
         __syncthreads();
     } else if (do_upper) {
-        for (int blk = warp; blk < nblk; blk += NW) solve_block(blk, xs[blk * 32 + lane], up_inv, up_g, false);
+        for (int blk = warp; blk < nblk; blk += NW) solve_block(blk, xs[blk * 32 + lane], up_inv, up_g);
         __syncthreads();
     }
     if (do_upper) {
-        scan(false);
+        boundary(false, up_rb);
         __syncthreads();
         for (int blk = warp; blk < nblk; blk += NW) {
             const cx<R> y = correct(blk, up_g, false);
@@ -250,7 +235,7 @@ void invert_triangular_32(const zd *T, bool lower, zd *Tinv)
 // the coupling C[t][c] = A(32 blk + t, col_c) to the neighbouring block's boundary columns
 // col_c = 32 blk - w + c (lower) or 32 (blk + 1) + c (upper), c < w.
 template <typename Acc>
-void build_blocks(int N, int w, bool lower, Acc A, std::vector<zd> &inv, std::vector<zd> &g)
+void build_blocks(int N, int w, bool lower, Acc A, std::vector<zd> &inv, std::vector<zd> &g, std::vector<zd> &rb)
 {
     const int nblk = (N + 31) / 32;
     inv.assign((size_t)nblk * 1024, zd(0.0, 0.0));
@@ -286,6 +271,25 @@ void build_blocks(int N, int w, bool lower, Acc A, std::vector<zd> &inv, std::ve
                 for (int s = 0; s < 32; ++s) acc += Ti[t * 32 + s] * Cm[(size_t)s * w + c];
                 g[(size_t)blk * w * 32 + (size_t)c * 32 + t] = acc;
             }
+    }
+    // Boundary system s_b + T_b s_{b-/+1} = z_b[boundary rows], T_b = G_b[boundary rows]
+    // (lower: rows 32-w.., coupling to block b-1; upper: rows 0.., coupling to block b+1).
+    // rb = its inverse, [nb][nb] row-major, by substitution on the unit vectors.
+    const int nb = nblk * w, r0 = lower ? 32 - w : 0;
+    rb.assign((size_t)nb * nb, zd(0.0, 0.0));
+    std::vector<zd> sv(nb);
+    for (int j = 0; j < nb; ++j) {
+        std::fill(sv.begin(), sv.end(), zd(0.0, 0.0));
+        sv[j] = zd(1.0, 0.0);
+        for (int step = 1; step < nblk; ++step) {
+            const int bk = lower ? step : nblk - 1 - step, prev = lower ? bk - 1 : bk + 1;
+            for (int r = 0; r < w; ++r) {
+                zd acc = sv[bk * w + r];
+                for (int c = 0; c < w; ++c) acc -= g[(size_t)bk * w * 32 + (size_t)c * 32 + r0 + r] * sv[prev * w + c];
+                sv[bk * w + r] = acc;
+            }
+        }
+        for (int i = 0; i < nb; ++i) rb[(size_t)i * nb + j] = sv[i];
     }
 }
 
@@ -372,9 +376,9 @@ extern "C" int pg_overlap_create(pg_op *op, const double *overlap_rows, pg_bande
     if (!cholesky_band(N, kb, overlap_rows, U)) return PG_ERR_ARG;
     auto Ufun = [&](int i, int j) { return zd(U[(size_t)i * (kb + 1) + (j - i)], 0.0); };
     auto Lfun = [&](int i, int j) { return zd(U[(size_t)j * (kb + 1) + (i - j)], 0.0); };  // L = U^T
-    std::vector<zd> up_inv, up_cpl, lo_inv, lo_cpl;
-    build_blocks(N, kb, false, Ufun, up_inv, up_cpl);
-    build_blocks(N, kb, true, Lfun, lo_inv, lo_cpl);
+    std::vector<zd> up_inv, up_cpl, up_rb, lo_inv, lo_cpl, lo_rb;
+    build_blocks(N, kb, false, Ufun, up_inv, up_cpl, up_rb);
+    build_blocks(N, kb, true, Lfun, lo_inv, lo_cpl, lo_rb);
     pg_banded_ext *b = new pg_banded_ext();
     b->op = op;
     b->kind = 0;
@@ -391,6 +395,8 @@ extern "C" int pg_overlap_create(pg_op *op, const double *overlap_rows, pg_bande
         if ((st = upload_real<double>(up_cpl, &b->d_up_cpl)) != PG_OK) return st;
         if ((st = upload_real<double>(lo_inv, &b->d_lo_inv)) != PG_OK) return st;
         if ((st = upload_real<double>(lo_cpl, &b->d_lo_cpl)) != PG_OK) return st;
+        if ((st = upload_real<double>(up_rb, &b->d_up_rb)) != PG_OK) return st;
+        if ((st = upload_real<double>(lo_rb, &b->d_lo_rb)) != PG_OK) return st;
     } else {
         if ((st = upload_real_d<float>(U, &b->d_U)) != PG_OK) return st;
         if ((st = upload_real_d<float>(Srows, &b->d_S)) != PG_OK) return st;
@@ -398,6 +404,8 @@ extern "C" int pg_overlap_create(pg_op *op, const double *overlap_rows, pg_bande
         if ((st = upload_real<float>(up_cpl, &b->d_up_cpl)) != PG_OK) return st;
         if ((st = upload_real<float>(lo_inv, &b->d_lo_inv)) != PG_OK) return st;
         if ((st = upload_real<float>(lo_cpl, &b->d_lo_cpl)) != PG_OK) return st;
+        if ((st = upload_real<float>(up_rb, &b->d_up_rb)) != PG_OK) return st;
+        if ((st = upload_real<float>(lo_rb, &b->d_lo_rb)) != PG_OK) return st;
     }
     const size_t esz = op->precision == PG_FP64 ? sizeof(cxd) : sizeof(cxf);
     PG_CUDA_TRY(cudaMalloc(&b->d_scratch, esz * (size_t)op->nrows * N));
@@ -414,7 +422,7 @@ extern "C" int pg_prec_blockdiag_create(pg_op *op, const double *overlap_rows, c
     if (op->rank != 2) return PG_ERR_STORAGE;  // blocks are angular channels of a rank-2 operator
     const int N = op->N, kb = op->kb, b = 2 * kb + 1, na = op->nrows;
     const zd zS(cS[0], cS[1]), zH(cH[0], cH[1]);
-    std::vector<zd> all_lo_inv, all_lo_cpl, all_up_inv, all_up_cpl;
+    std::vector<zd> all_lo_inv, all_lo_cpl, all_up_inv, all_up_cpl, all_lo_rb, all_up_rb;
     for (int a = 0; a < na; ++a) {
         std::vector<zd> M((size_t)N * b, zd(0.0, 0.0));
         for (int i = 0; i < N; ++i)
@@ -436,9 +444,11 @@ extern "C" int pg_prec_blockdiag_create(pg_op *op, const double *overlap_rows, c
         if (!lu_band_nopivot(N, kb, M)) return PG_ERR_ARG;
         auto Lf = [&](int i, int j) { return i == j ? zd(1.0, 0.0) : M[(size_t)i * b + kb + (j - i)]; };
         auto Uf = [&](int i, int j) { return M[(size_t)i * b + kb + (j - i)]; };
-        std::vector<zd> li, lc, ui, uc;
-        build_blocks(N, kb, true, Lf, li, lc);
-        build_blocks(N, kb, false, Uf, ui, uc);
+        std::vector<zd> li, lc, lr, ui, uc, ur;
+        build_blocks(N, kb, true, Lf, li, lc, lr);
+        build_blocks(N, kb, false, Uf, ui, uc, ur);
+        all_lo_rb.insert(all_lo_rb.end(), lr.begin(), lr.end());
+        all_up_rb.insert(all_up_rb.end(), ur.begin(), ur.end());
         all_lo_inv.insert(all_lo_inv.end(), li.begin(), li.end());
         all_lo_cpl.insert(all_lo_cpl.end(), lc.begin(), lc.end());
         all_up_inv.insert(all_up_inv.end(), ui.begin(), ui.end());
@@ -457,11 +467,15 @@ extern "C" int pg_prec_blockdiag_create(pg_op *op, const double *overlap_rows, c
         if ((st = upload_cplx<double>(all_lo_cpl, &bd->d_lo_cpl)) != PG_OK) return st;
         if ((st = upload_cplx<double>(all_up_inv, &bd->d_up_inv)) != PG_OK) return st;
         if ((st = upload_cplx<double>(all_up_cpl, &bd->d_up_cpl)) != PG_OK) return st;
+        if ((st = upload_cplx<double>(all_lo_rb, &bd->d_lo_rb)) != PG_OK) return st;
+        if ((st = upload_cplx<double>(all_up_rb, &bd->d_up_rb)) != PG_OK) return st;
     } else {
         if ((st = upload_cplx<float>(all_lo_inv, &bd->d_lo_inv)) != PG_OK) return st;
         if ((st = upload_cplx<float>(all_lo_cpl, &bd->d_lo_cpl)) != PG_OK) return st;
         if ((st = upload_cplx<float>(all_up_inv, &bd->d_up_inv)) != PG_OK) return st;
         if ((st = upload_cplx<float>(all_up_cpl, &bd->d_up_cpl)) != PG_OK) return st;
+        if ((st = upload_cplx<float>(all_lo_rb, &bd->d_lo_rb)) != PG_OK) return st;
+        if ((st = upload_cplx<float>(all_up_rb, &bd->d_up_rb)) != PG_OK) return st;
     }
     *out = bd;
     return PG_OK;
@@ -477,6 +491,8 @@ extern "C" int pg_banded_destroy(pg_banded *b)
     cudaFree(e->d_lo_cpl);
     cudaFree(e->d_up_inv);
     cudaFree(e->d_up_cpl);
+    cudaFree(e->d_lo_rb);
+    cudaFree(e->d_up_rb);
     cudaFree(e->d_scratch);
     delete e;
     return PG_OK;
@@ -490,8 +506,7 @@ static int launch_tri_nw(pg_banded *b, bool do_lower, bool do_upper, void *x)
     pg_ctx *ctx = b->op->ctx;
     const int N = b->N, nblk = (N + 31) / 32, w = b->kb;
     const int nfib = b->op->nrows;
-    const size_t base = (size_t)nblk * 32 * sizeof(cx<R>) + (size_t)nblk * w * sizeof(cx<R>) +
-                        (size_t)nblk * w * w * sizeof(C);
+    const size_t base = (size_t)nblk * 32 * sizeof(cx<R>) + (size_t)nblk * w * sizeof(cx<R>);
     const size_t full = base + (size_t)nblk * w * 32 * sizeof(C);
     const size_t limit = 200 * 1024;
     if (base > limit) return PG_ERR_SHAPE;  // fibre too long for the shared-memory solve
@@ -504,8 +519,8 @@ static int launch_tri_nw(pg_banded *b, bool do_lower, bool do_upper, void *x)
         configured = smem;
     }
     tri_solve_kernel<R, C, NW><<<nfib, 32 * NW, smem, ctx->stream>>>(
-        N, nblk, w, (const C *)b->d_lo_inv, (const C *)b->d_lo_cpl, (const C *)b->d_up_inv, (const C *)b->d_up_cpl,
-        do_lower ? 1 : 0, do_upper ? 1 : 0, b->nmat > 1, g_in_smem ? 1 : 0, (cx<R> *)x, nfib);
+        N, nblk, w, (const C *)b->d_lo_inv, (const C *)b->d_lo_cpl, (const C *)b->d_lo_rb, (const C *)b->d_up_inv,
+        (const C *)b->d_up_cpl, (const C *)b->d_up_rb, do_lower ? 1 : 0, do_upper ? 1 : 0, b->nmat > 1, g_in_smem ? 1 : 0, (cx<R> *)x, nfib);
     ctx->launches++;
     return pg_check_launch(ctx);
 }

@@ -39,6 +39,7 @@ struct GmresStats {
     double true_resid;     // ||(S + i dt/2 H) psi' - b|| in FP64 (mixed; FP64 mode when requested)
     double beta0;          // norm of the preconditioned right-hand side of the last solve
     long long kernels;     // kernels run by all steps so far (never reset; see the K_* counts)
+    long long rejected;    // learned-preconditioner passes rejected by the true residual (cumulative)
 };
 
 // Kernels a step runs, counted on the device as the loops decide (one graph launch hides them):
@@ -50,12 +51,18 @@ struct GmresStats {
 // Each count has one matvec kernel per operator product; an operator with dense radial blocks
 // launches one more (pg_op_matvec_kernels).
 static const int K_FP64_BASE = 7, K_TRUE_RESID = 4, K_MIXED_BASE = 2, K_MIXED_PASS = 9, K_ITER = 7;
+// learned preconditioner (right-preconditioned flexible GMRES): per iteration next vector,
+// block solve, features, 3 network products, correction, matvec, multidot, 2 GS updates,
+// Givens; per pass convert, norm, init, back-substitution, combine, matvec, norm, decide, commit
+static const int K_LEARN_ITER = 12, K_LEARN_PASS = 9;
 
 struct GmresState {
     GmresStats stats;
     int j;            // Krylov vector being expanded in this iteration
     int cont_inner;   // loop decisions, mirrored for the eager (host-driven) mode
     int cont_outer;
+    int learned_on;   // learned preconditioner in use for the rest of this step
+    int accept;       // the last learned pass met the residual test
     int pad;
     double tol_eff;
     double beta_last;
@@ -105,6 +112,8 @@ __global__ void cay_scales_kernel(const StepParams *__restrict__ p, cxd *__restr
         st->stats.passes = 0;
         st->stats.true_resid = -1.0;
         st->stats.kernels += kernels;
+        st->learned_on = 1;  // each step starts with the learned preconditioner (when configured)
+        st->accept = 1;
     }
 }
 
@@ -314,6 +323,70 @@ __global__ void cay_refine_decide_kernel(GmresState *st, double *nrm, double tol
     if (use_cond) cudaGraphSetConditional(outer, again ? 1u : 0u);
 }
 
+// Learned preconditioner application for flexible GMRES: z = y + s * (out_re + i out_im)
+// with y = M^-1 V_j (in vcur), out the network's correction per block ([nblk][d_out]) and s
+// the coupling's scale; the result goes to Z[j] (the flexible basis) and zcur (matvec source).
+// With the learned part switched off for this step (st->learned_on == 0) z = y.
+__global__ void cay_learned_apply_kernel(const GmresState *__restrict__ st, const cxf *__restrict__ y,
+                                         const float *__restrict__ out, int N, int d_out,
+                                         const cxd *__restrict__ s, cxf *__restrict__ Z, cxf *__restrict__ zcur,
+                                         long long n)
+{
+    const int j = st->j;
+    const bool on = st->learned_on != 0;
+    const cxf sc = mk<float>((float)s->x, (float)s->y);
+    cxf *Zj = Z + (size_t)j * n;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        cxf v = y[e];
+        if (on) {
+            const long long a = e / N, i = e - a * N;
+            const float ox = out[a * d_out + 2 * i], oy = out[a * d_out + 2 * i + 1];
+            v.x += sc.x * ox - sc.y * oy;
+            v.y += sc.x * oy + sc.y * ox;
+        }
+        Zj[e] = v;
+        zcur[e] = v;
+    }
+}
+
+// End of a learned pass: the candidate residual rn = r - A e (FP64) is judged against the
+// pass's starting residual (beta0). A pass with the learned part that does not halve the
+// residual (or gives a non-finite one) is discarded and the rest of the step runs with the
+// block preconditioner alone. Decides whether another pass runs.
+__global__ void cay_learned_decide_kernel(GmresState *st, double *nrm, double tol, int maxpass,
+                                          cudaGraphConditionalHandle outer, int use_cond)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double r = sqrt(fmax(nrm[0], 0.0));
+    nrm[0] = 0.0;
+    nrm[1] = 0.0;
+    const double r0 = st->stats.beta0;
+    bool accept = (r == r) && r < 1e300;
+    if (accept && st->learned_on && !(r < 0.5 * r0)) accept = false;
+    if (!accept && st->learned_on) {
+        st->learned_on = 0;
+        st->stats.rejected += 1;
+    }
+    st->accept = accept ? 1 : 0;
+    const double rc = accept ? r : r0;
+    st->stats.true_resid = rc;
+    const bool again = (rc > tol) && (rc == rc) && st->stats.passes < maxpass;
+    st->cont_outer = again ? 1 : 0;
+    if (use_cond) cudaGraphSetConditional(outer, again ? 1u : 0u);
+}
+
+// psi += e and r = rn when the pass was accepted
+__global__ void cay_learned_commit_kernel(const GmresState *__restrict__ st, const cxd *__restrict__ e,
+                                          const cxd *__restrict__ rn, cxd *__restrict__ psi, cxd *__restrict__ r,
+                                          long long n)
+{
+    if (!st->accept) return;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        psi[i] = psi[i] + e[i];
+        r[i] = rn[i];
+    }
+}
+
 // ------------------------------------------------------------------------------------
 // host object
 // ------------------------------------------------------------------------------------
@@ -345,6 +418,12 @@ struct pg_cayley {
     bool eager = false;  // host-driven loops (same kernels; for profilers that cannot see graph loops)
     int h_flag = 0;
     long long kernels_counted = 0;  // device kernel count already added to ctx->launches
+    // learned preconditioner (mixed precision only)
+    pg_mlp *mlp = nullptr;
+    int learned_slot = 0;          // operator slot whose scale i dt/2 h(t) multiplies the correction
+    void *Z = nullptr, *zcur = nullptr, *Xf = nullptr;
+    float *mlp_out = nullptr;
+    cxd *rn64 = nullptr;
 };
 
 static int nblocks_for(pg_ctx *ctx, long long n)
@@ -406,6 +485,42 @@ static int capture_iteration(pg_cayley *c, pg_op *op, pg_banded *pre, cudaGraphC
     PG_TRY(pg_gs_update<R>(rc, V, n, c->m, c->h2, w, n, 0, c->h3, &c->st->j, 1));
     cay_gmres_finalize_kernel<T><<<1, 32, 0, s>>>(c->st, c->h1, c->h2, c->h3, c->m, inner, c->eager ? 0 : 1,
                                                    K_ITER - 1 + pg_op_matvec_kernels(op));
+    return pg_check_launch(ctx);
+}
+
+// kernels of one flexible GMRES iteration with the learned preconditioner (complex64):
+// y = M^-1 V_j, z_j = y + s MLP(features(y)), w = A z_j, then the same orthogonalization and
+// Givens update as capture_iteration
+static int capture_iteration_learned(pg_cayley *c, cudaGraphConditionalHandle inner)
+{
+    pg_ctx *ctx = c->ctx;
+    cudaStream_t s = ctx->stream;
+    const long long n = c->n;
+    const int nb = nblocks_for(ctx, n);
+    cxf *V = (cxf *)c->V, *w = (cxf *)c->w, *vcur = (cxf *)c->vcur;
+    cay_next_vector_kernel<float><<<nb, 256, 0, s>>>(c->st, V, w, vcur, n);
+    PG_TRY(pg_check_launch(ctx));
+    PG_TRY(pg_banded_apply_dev(c->precb, PG_BAND_PREC_SOLVE, vcur));
+    pg_ctx *mctx = nullptr;
+    int d_in = 0, d_out = 0;
+    PG_TRY(pg_mlp_describe(c->mlp, &mctx, &d_in, &d_out));
+    const int nblk = c->opb->nrows, N = c->opb->N;
+    PG_TRY(pg_mlp_block_features_dev(ctx, vcur, nblk, N, d_in, nullptr, c->Xf));
+    PG_TRY(pg_mlp_forward_dev(c->mlp, c->Xf, nblk, c->mlp_out));
+    cay_learned_apply_kernel<<<nb, 256, 0, s>>>(c->st, vcur, c->mlp_out, N, d_out,
+                                                c->d_sc + SC_PLUS * PG_MAX_SLOTS + c->learned_slot, (cxf *)c->Z,
+                                                (cxf *)c->zcur, n);
+    PG_TRY(pg_check_launch(ctx));
+    pg_scales dummy;
+    memset(&dummy, 0, sizeof(dummy));
+    PG_TRY(pg_op_matvec_dev(c->opb, dummy, c->d_sc + SC_PLUS * PG_MAX_SLOTS, c->zcur, w, 0, nullptr, nullptr));
+    pg_ctx *rc = &c->rctx;
+    rc->stream = s;
+    PG_TRY(pg_multidot<float>(rc, V, n, c->m, w, n, c->h1, &c->st->j, 1));
+    PG_TRY(pg_gs_update<float>(rc, V, n, c->m, c->h1, w, n, 1, c->h2, &c->st->j, 1));
+    PG_TRY(pg_gs_update<float>(rc, V, n, c->m, c->h2, w, n, 0, c->h3, &c->st->j, 1));
+    cay_gmres_finalize_kernel<float><<<1, 32, 0, s>>>(c->st, c->h1, c->h2, c->h3, c->m, inner, c->eager ? 0 : 1,
+                                                      K_LEARN_ITER - 1 + pg_op_matvec_kernels(c->opb));
     return pg_check_launch(ctx);
 }
 
@@ -514,22 +629,42 @@ static int record_mixed(pg_cayley *c, cxd *psi)
     } else {
         PG_CUDA_TRY(cudaMemsetAsync(&c->st->cont_outer, 0xff, sizeof(int), s0));  // first pass always runs
     }
+    const bool learned = c->mlp != nullptr;
     PG_TRY(loop_while(c, outer, c->cap[1], &c->st->cont_outer, [&]() -> int {
         cudaStream_t s1 = ctx->stream;
         cxf *dconv = (cxf *)c->dconv;
         PG_TRY((pg_scale_copy<float, double>(ctx, c->r64, dconv, nullptr, n, nullptr, 1.0)));
-        PG_TRY(pg_banded_apply_dev(c->precb, PG_BAND_PREC_SOLVE, dconv));
+        // left preconditioning solves M^-1 A e = M^-1 r; the learned (flexible, right)
+        // variant solves A P e' = r, its residual estimate being the true residual's
+        if (!learned) PG_TRY(pg_banded_apply_dev(c->precb, PG_BAND_PREC_SOLVE, dconv));
         rc->stream = s1;
         PG_TRY(pg_multidot<float>(rc, dconv, n, 0, dconv, n, c->nrm, nullptr, 1));
         cudaGraphConditionalHandle inner = 0;
         if (!c->eager) PG_TRY(capture_handle(s1, &inner, 0, 0));
         cay_gmres_init_kernel<float><<<nb, 256, 0, s1>>>(c->st, c->nrm, dconv, (cxf *)c->V, (cxf *)c->vcur, n, c->tol,
-                                                         2e-6, K_MIXED_PASS + mv, inner, outer, c->eager ? -1 : 1);
+                                                         2e-6, (learned ? K_LEARN_PASS : K_MIXED_PASS) + mv, inner, outer,
+                                                         c->eager ? -1 : 1);
         PG_TRY(pg_check_launch(ctx));
-        PG_TRY(loop_while(c, inner, c->cap[2], &c->st->cont_inner,
-                          [&]() { return capture_iteration<float, float>(c, c->opb, c->precb, inner); }));
+        PG_TRY(loop_while(c, inner, c->cap[2], &c->st->cont_inner, [&]() {
+            return learned ? capture_iteration_learned(c, inner)
+                           : capture_iteration<float, float>(c, c->opb, c->precb, inner);
+        }));
         cay_backsolve_kernel<float><<<1, 32, 0, s1>>>(c->st, c->nrm);
         PG_TRY(pg_check_launch(ctx));
+        if (learned) {
+            // e = Z y; rn = r - A e; judged, then committed or discarded
+            cay_combine_kernel<float><<<nb, 256, 0, s1>>>((const cxf *)c->Z, n, c->st, c->e64, nullptr);
+            PG_TRY(pg_check_launch(ctx));
+            PG_CUDA_TRY(cudaMemcpyAsync(c->rn64, c->r64, sizeof(cxd) * n, cudaMemcpyDeviceToDevice, s1));
+            PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_NEGPLUS * PG_MAX_SLOTS, c->e64, c->rn64, 1, nullptr,
+                                    nullptr));
+            rc->stream = s1;
+            PG_TRY(pg_multidot<double>(rc, c->rn64, n, 0, c->rn64, n, c->nrm2, nullptr, 1));
+            cay_learned_decide_kernel<<<1, 32, 0, s1>>>(c->st, c->nrm2, c->tol, 4, outer, c->eager ? 0 : 1);
+            PG_TRY(pg_check_launch(ctx));
+            cay_learned_commit_kernel<<<nb, 256, 0, s1>>>(c->st, c->e64, c->rn64, psi, c->r64, n);
+            return pg_check_launch(ctx);
+        }
         cay_combine_kernel<float><<<nb, 256, 0, s1>>>((const cxf *)c->V, n, c->st, c->e64, psi);
         PG_TRY(pg_check_launch(ctx));
         // r -= (S + i dt/2 H) e   in FP64, then ||r|| decides whether another pass runs
@@ -635,6 +770,7 @@ extern "C" int pg_cayley_destroy(pg_cayley *c)
     for (int k = 0; k < 3; ++k)
         if (c->cap[k]) cudaStreamDestroy(c->cap[k]);
     for (int k = 0; k < RING; ++k) cudaEventDestroy(c->ring_ev[k]);
+    for (void *p : {c->Z, c->zcur, c->Xf, (void *)c->mlp_out, (void *)c->rn64}) cudaFree(p);
     void *bufs[] = {c->V, c->w, c->vcur, c->dconv, c->b64, c->r64, c->d64, c->e64, c->h1, c->h2, c->h3, c->nrm,
                     c->nrm2, c->st, c->d_params, c->d_sc, c->rctx.red_partial, c->rctx.red_counter,
                     c->rctx.red_out, c->rctx.d_err};
@@ -702,6 +838,49 @@ extern "C" int pg_cayley_step(pg_cayley *c, void *psi, double dt, const double *
         PG_CUDA_TRY(cudaStreamSynchronize(c->ctx->stream));
         fill_stats(c, st);
     }
+    return PG_OK;
+}
+
+// Learned preconditioner for the mixed-precision step (nullptr switches it off). The
+// correction is scaled by the slot's i dt/2 h(t); the network must take d_in >= 6N and give
+// d_out >= 2N per angular block.
+extern "C" int pg_cayley_set_learned(pg_cayley *c, pg_mlp *mlp, int coupling_slot)
+{
+    if (!c || coupling_slot < 0 || coupling_slot >= PG_MAX_SLOTS) return PG_ERR_ARG;
+    if (!mlp) {
+        c->mlp = nullptr;
+        c->built_psi = nullptr;
+        return PG_OK;
+    }
+    if (c->prec != PG_FP32 || c->opb->rank != 2) return PG_ERR_STATE;
+    pg_ctx *mctx = nullptr;
+    int d_in = 0, d_out = 0;
+    PG_TRY(pg_mlp_describe(mlp, &mctx, &d_in, &d_out));
+    const int nblk = c->opb->nrows, N = c->opb->N;
+    if (mctx != c->ctx) return PG_ERR_ARG;
+    if (d_in < 6 * N || d_out < 2 * N) return PG_ERR_SHAPE;
+    PG_TRY(pg_mlp_reserve(mlp, nblk));
+    cudaFree(c->Z); cudaFree(c->zcur); cudaFree(c->Xf); cudaFree(c->mlp_out); cudaFree(c->rn64);
+    c->Z = c->zcur = c->Xf = nullptr;
+    c->mlp_out = nullptr;
+    c->rn64 = nullptr;
+    PG_CUDA_TRY(cudaMalloc(&c->Z, sizeof(cxf) * (size_t)c->m * c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->zcur, sizeof(cxf) * (size_t)c->n));
+    PG_CUDA_TRY(cudaMalloc(&c->Xf, 2 * (size_t)nblk * d_in));
+    PG_CUDA_TRY(cudaMalloc(&c->mlp_out, sizeof(float) * (size_t)nblk * d_out));
+    PG_CUDA_TRY(cudaMalloc(&c->rn64, sizeof(cxd) * (size_t)c->n));
+    c->mlp = mlp;
+    c->learned_slot = coupling_slot;
+    c->built_psi = nullptr;  // rebuild the step graph
+    return PG_OK;
+}
+
+// passes of the learned preconditioner rejected by the residual test so far (waits)
+extern "C" int pg_cayley_learned_rejected(pg_cayley *c, long long *out)
+{
+    if (!c || !out) return PG_ERR_ARG;
+    PG_CUDA_TRY(cudaStreamSynchronize(c->ctx->stream));
+    *out = c->h_stats->rejected;
     return PG_OK;
 }
 

@@ -184,10 +184,23 @@ struct pg_banded {
     // neighbouring block's kb boundary values
     void *d_lo_inv = nullptr, *d_lo_cpl = nullptr;   // lower factor (U^T or L)
     void *d_up_inv = nullptr, *d_up_cpl = nullptr;   // upper factor (U)
+    void *d_lo_rb = nullptr, *d_up_rb = nullptr;     // inverses of the block-boundary systems
     int complex_coef = 0;
 };
 
 int pg_banded_apply_dev(pg_banded *b, int which, void *x);
+
+// ------------------------------------------------------------------------------------
+// learned preconditioner network (mlp.cu)
+// ------------------------------------------------------------------------------------
+struct pg_mlp;
+int pg_mlp_describe(pg_mlp *m, pg_ctx **ctx, int *d_in, int *d_out);
+int pg_mlp_reserve(pg_mlp *m, int batch);
+// Y (FP32 [batch][d_out]) = network(X (BF16 [batch][d_in])) on the network's context stream
+int pg_mlp_forward_dev(pg_mlp *m, const void *X, int batch, float *Y);
+// X (BF16 [nblk][d_in]) = [y_{a-1}, y_a, y_{a+1}] of y (complex64 [nblk][N]), scaled by *inv_scale
+int pg_mlp_block_features_dev(pg_ctx *ctx, const void *y, int nblk, int N, int d_in, const double *inv_scale,
+                              void *X);
 
 // ------------------------------------------------------------------------------------
 // vector kernels (vector.cu)

@@ -266,6 +266,18 @@ class CayleyStepper:
         check(self.lib.pg_cayley_last_stats(self.h, C.byref(self.stats)), "pg_cayley_last_stats")
         return self.stats
 
+    def set_learned(self, net, coupling_slot):
+        """Use the learned preconditioner ``net`` (MlpNet, or None to switch it off); its
+        correction is scaled by i dt/2 times the scale of ``coupling_slot``."""
+        self.learned_net = net  # keeps the network alive while the stepper uses it
+        check(self.lib.pg_cayley_set_learned(self.h, net.h if net is not None else None, int(coupling_slot)),
+              "pg_cayley_set_learned")
+
+    def learned_rejected(self):
+        out = C.c_longlong(0)
+        check(self.lib.pg_cayley_learned_rejected(self.h, C.byref(out)), "pg_cayley_learned_rejected")
+        return int(out.value)
+
     def set_eager(self, on):
         """Host-driven loops instead of the graph's conditional nodes (for profilers)."""
         check(self.lib.pg_cayley_set_eager(self.h, int(bool(on))), "pg_cayley_set_eager")

@@ -1,0 +1,129 @@
+"""Learned preconditioner network on the GPU vs the CPU oracle (gradient check, training)."""
+import numpy as np
+import pytest
+
+from tests.helpers import relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def _net(d_in, hidden, d_out, seed=3):
+    from pyprop_gb300.learned import MlpNet
+    return MlpNet(d_in, hidden, d_out, seed=seed)
+
+
+def test_forward_and_gradients_match_oracle(gpu):
+    import torch
+    from oracle.mlp import bf16, forward, loss_and_gradients
+    rng = np.random.default_rng(4)
+    d_in, h, d_out, B = 96, 64, 48, 37
+    net = _net(d_in, h, d_out)
+    W = [rng.standard_normal((d_in, h)) * np.sqrt(2.0 / d_in), rng.standard_normal((h, h)) * np.sqrt(2.0 / h),
+         rng.standard_normal((h, d_out)) * np.sqrt(1.0 / h)]
+    net.set_weights(W)
+    Wd = net.get_weights()
+    assert max(np.abs(a - b).max() for a, b in zip(Wd, W)) < 1e-6
+    X = bf16(rng.standard_normal((B, d_in)))
+    T = rng.standard_normal((B, d_out))
+    Xd = torch.as_tensor(X, dtype=torch.float32, device="cuda").to(torch.bfloat16)
+    Td = torch.as_tensor(T, dtype=torch.float32, device="cuda")
+    Y = torch.zeros((B, d_out), dtype=torch.float32, device="cuda")
+    net.forward(Xd, Y)
+    y_ref = forward(W, X)[2]
+    assert relerr(Y.cpu().numpy(), y_ref) < 1e-2
+    loss, g = net.gradients(Xd, Td)
+    loss_ref, g_ref = loss_and_gradients(W, X, T)
+    assert abs(loss - loss_ref) < 1e-3 * loss_ref
+    for layer in range(3):
+        assert relerr(g[layer], g_ref[layer]) < 2e-2, (layer, relerr(g[layer], g_ref[layer]))
+
+
+def test_training_reduces_loss_on_a_linear_target(gpu):
+    import torch
+    rng = np.random.default_rng(5)
+    d_in, h, d_out, B = 64, 256, 32, 512
+    A = rng.standard_normal((d_in, d_out)) / np.sqrt(d_in)
+    X = rng.standard_normal((B, d_in))
+    T = X @ A
+    net = _net(d_in, h, d_out, seed=11)
+    Xd = torch.as_tensor(X, dtype=torch.float32, device="cuda").to(torch.bfloat16)
+    Td = torch.as_tensor(T, dtype=torch.float32, device="cuda")
+    first = net.train_step(Xd, Td, 1e-3, want_loss=True)
+    for _ in range(400):
+        net.train_step(Xd, Td, 1e-3)
+    last = net.train_step(Xd, Td, 1e-3, want_loss=True)
+    assert last < 0.05 * first, (first, last)
+
+
+def _strong_field_problem(precision="fp32"):
+    from tests.helpers import hydrogen_problem
+    return hydrogen_problem(lmax=7, nbsplines=40, rmax=40.0, propagator="CayleyPropagatorGPU", precision=precision,
+                            gmres_tolerance=1e-12, amplitude=0.1, pulse_duration=4.0, duration=4.0)
+
+
+def test_learned_cayley_steps_match_the_plain_path(gpu):
+    """Flexible GMRES with the (untrained) learned preconditioner reaches the same states."""
+    from pyprop_gb300.learned import LearnedPreconditioner
+    from tests.helpers import golden
+    plain = _strong_field_problem()
+    plain.SetupStep(skipWavefunctionSetup=True)
+    learned = _strong_field_problem()
+    learned.SetupStep(skipWavefunctionSetup=True)
+    lp = LearnedPreconditioner(learned.Propagator, hidden=64)
+    lp.attach()
+    rng = np.random.default_rng(0)
+    psi = rng.standard_normal(plain.psi.GetData().shape) + 0j
+    import torch
+    for p in (plain, learned):
+        p.psi.GetData().copy_(torch.as_tensor(psi / np.linalg.norm(psi), device="cuda"))
+        p.PropagatedTime = 1.0
+    for _ in range(10):
+        plain.AdvanceStep()
+        learned.AdvanceStep()
+        assert learned.Propagator.LastStats.TrueResidual < 1e-12
+    assert relerr(learned.psi.numpy(), plain.psi.numpy()) < 1e-10
+    assert learned.Propagator.stepper.learned_rejected() == 0
+
+
+def test_trained_network_improves_the_block_preconditioner(gpu):
+    """Trained on the plain solver's residual/correction pairs, the learned correction lowers
+    the one-step residual ||A P(r) - r|| / ||r|| on held-out steps, and the learned Cayley
+    steps need no more GMRES iterations than the plain ones."""
+    import torch
+    from pyprop_gb300.learned import LearnedPreconditioner
+    prob = _strong_field_problem()
+    prob.SetupStep(skipWavefunctionSetup=True)
+    psi = np.zeros(prob.psi.GetData().shape, dtype=np.complex128)
+    rng = np.random.default_rng(1)
+    psi[0] = rng.standard_normal(psi.shape[1])
+    psi[1] = 0.3 * rng.standard_normal(psi.shape[1])
+    prob.psi.GetData().copy_(torch.as_tensor(psi / np.linalg.norm(psi), device="cuda"))
+    prob.PropagatedTime = 0.5
+    lp = LearnedPreconditioner(prob.Propagator, hidden=256, seed=3)
+    lp.harvest(prob, 160)
+    train, held = lp.pairs[:120], lp.pairs[120:]
+    X, T = lp.training_set(train, rng=np.random.default_rng(2), phases=4)
+    losses = lp.train(X, T, steps=600, lr=1e-3, batch=512)
+    assert losses[-1] < 0.5 * losses[0], losses
+    plain_rho = lp.one_step_residual(held, learned=False)
+    learned_rho = lp.one_step_residual(held, learned=True)
+    print("one-step residual: block %.3e, learned %.3e; loss %.3e -> %.3e" % (plain_rho, learned_rho, losses[0],
+                                                                            losses[-1]))
+    assert learned_rho < plain_rho
+    # in the Cayley step: continue the propagation with and without the network
+    state = prob.psi.GetData().clone()
+    t0 = prob.PropagatedTime
+    iters = {}
+    for use in (False, True):
+        lp.attach(use)
+        prob.psi.GetData().copy_(state)
+        prob.PropagatedTime = t0
+        n = 0
+        for _ in range(20):
+            prob.AdvanceStep()
+            st = prob.Propagator.LastStats
+            assert st.TrueResidual < 1e-12
+            n += st.Iterations
+        iters[use] = n
+    print("GMRES iterations over 20 steps: block %d, learned %d" % (iters[False], iters[True]))
+    assert iters[True] <= iters[False]
