@@ -121,9 +121,27 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def _time_launches(torch, fn, flush, reps):
+    """Average device time of fn() (CUDA events on the launching stream, L2 flushed before
+    every launch, 3 untimed launches first)."""
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        fn()
+    total = 0.0
+    for _ in range(reps):
+        flush.fill_(1.0)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        fn()
+        e.record(stream)
+        e.synchronize()
+        total += s.elapsed_time(e) * 1e-3
+    return total / reps
+
+
 def time_matvec(torch, prob, flush, reps=50):
-    """Average duration of the complex64 H matvec kernel (events on the launching stream,
-    L2 flushed before every launch) and its algorithmic bytes per launch."""
+    """Average duration of the complex64 H matvec kernel and its algorithmic bytes per launch
+    s (sum_t P_t + 2 N_psi), s = 8."""
     from pyprop_gb300 import _native as nat
     bp = prob.Propagator.BasePropagator
     op = bp.device_operator(nat.PG_FP32)
@@ -131,22 +149,60 @@ def time_matvec(torch, prob, flush, reps=50):
     src = torch.randn((nang, N), dtype=torch.complex64, device="cuda")
     dst = torch.empty_like(src)
     sc = op.scales(5.0)
-    stream = torch.cuda.current_stream()
-    for _ in range(3):
-        op.matvec(sc, src, dst)
-    total = 0.0
-    for _ in range(reps):
-        flush.fill_(1.0)
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record(stream)
-        op.matvec(sc, src, dst)
-        e.record(stream)
-        e.synchronize()
-        total += s.elapsed_time(e) * 1e-3
-    avg = total / reps
+    avg = _time_launches(torch, lambda: op.matvec(sc, src, dst), flush, reps)
     elems = op.stored_elements()
-    bytes_per = 8 * (elems + 2 * nang * N)
-    return avg, bytes_per, elems
+    return avg, 8 * (elems + 2 * nang * N), elems
+
+
+def time_block_solve(torch, prob, flush, reps=50):
+    """Average duration of the complex64 block-diagonal LU solve (both sweeps, one launch) and
+    its algorithmic bytes: per fibre and sweep the inverse diagonal blocks (nblk 32x32), the
+    couplings (nblk 32 x k) and the nonzero block-triangular half of the boundary inverse
+    (k^2 nblk (nblk+1)/2), complex64; plus the fibre read and written."""
+    from pyprop_gb300 import _native as nat
+    pre = prob.Propagator.Preconditioner.solvers[nat.PG_FP32]
+    nang, N = prob.psi.GetRepresentation().GetFullShape()
+    kb = prob.Propagator.op64.kb
+    x = torch.randn((nang, N), dtype=torch.complex64, device="cuda")
+    avg = _time_launches(torch, lambda: pre.apply(nat.PG_BAND_PREC_SOLVE, x), flush, reps)
+    nblk = (N + 31) // 32
+    per_sweep = nblk * (32 * 32 + 32 * kb) + kb * kb * nblk * (nblk + 1) // 2
+    return avg, 8 * (nang * 2 * per_sweep + 2 * nang * N)
+
+
+LARGE = dict(lmax=300, nbsplines=2000, rmax=2000.0)
+
+
+def time_large_matvec(torch, flush, reps=20):
+    """The fused complex64 matvec on an operator larger than L2 (hydrogen lmax 300, 2000
+    B-splines: 901 band blocks, 187 MB), where it is HBM-bound: (avg s, algorithmic bytes)."""
+    import pyprop_gb300 as pp
+    from pyprop_gb300 import _native as nat
+    from pyprop_gb300.workloads import hydrogen
+    prob = pp.Problem(pp.LoadString(hydrogen(propagator="PamPropagatorGPU", **LARGE)))
+    bp = prob.Propagator.BasePropagator
+    bp.SetupStep(0.01)
+    op = bp.device_operator(nat.PG_FP32)
+    nang, N = prob.psi.GetRepresentation().GetFullShape()
+    src = torch.randn((nang, N), dtype=torch.complex64, device="cuda")
+    dst = torch.empty_like(src)
+    sc = op.scales(5.0)
+    avg = _time_launches(torch, lambda: op.matvec(sc, src, dst), flush, reps)
+    nbytes = 8 * (op.stored_elements() + 2 * nang * N)
+    del op, bp, prob
+    return avg, nbytes
+
+
+def profile_traffic(name):
+    """dram bytes per launch recorded in a committed ncu summary (line 'dram_bytes_per_launch: N')."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        for line in fh:
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return int(line.split(":")[1].strip())
+    return None
 
 
 def run_ours(args):
@@ -236,13 +292,9 @@ def run_ours(args):
     nbytes = psi0.size * 16
 
     avg_mv, bytes_mv, elems = time_matvec(torch, prob, flush)
+    avg_ts, bytes_ts = time_block_solve(torch, prob, flush)
+    avg_lg, bytes_lg = time_large_matvec(torch, flush)
     peak, peak_kind = measured_peaks()
-    achieved = bytes_mv / avg_mv / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "matvec_traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as fh:
-            traffic = json.load(fh).get("bytes_per_launch")
 
     ens = run_ensemble(args, torch, flush) if args.ensemble > 0 else None
     cpu = cpu_baseline_sample(nsteps=args.cpu_steps) if (rank == 0 and world == 1 and args.cpu_steps > 0) else None
@@ -262,11 +314,23 @@ def run_ours(args):
             "gmres_iterations_per_step": it_mixed,
             "e2e": {"value": world * args.steps / e2e_t, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "kernel": "op_matvec_kernel<float,6>", "avg_launch_us": 1e6 * avg_mv,
-                         "algorithmic_bytes": bytes_mv, "peak_kind": peak_kind,
-                         "note": "working set (%.1f MB) is L2 resident between launches only without the flush" %
-                                 (bytes_mv / 1e6)},
+            # dominant kernel of the step: the block-diagonal LU solve (5 launches per step)
+            "roofline": {"bound": "hbm", "achieved": bytes_ts / avg_ts / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": bytes_ts / avg_ts / 1e9 / peak,
+                         "traffic": profile_traffic("tri_solve_kernel_fp32_lmax40_n600.md"),
+                         "kernel": "tri_solve_kernel<float,cx<float>,24>", "avg_launch_us": 1e6 * avg_ts,
+                         "algorithmic_bytes": bytes_ts, "peak_kind": peak_kind,
+                         "timing": "CUDA events around 50 launches on the launching stream, L2 flushed before each"},
+            "roofline_matvec": {"bound": "hbm", "achieved": bytes_mv / avg_mv / 1e9, "peak": peak, "unit": "GB/s",
+                                "frac": bytes_mv / avg_mv / 1e9 / peak,
+                                "traffic": profile_traffic("op_matvec_bulk_kernel_fp32_lmax40_n600.md"),
+                                "kernel": "op_matvec_bulk_kernel<float,6>", "avg_launch_us": 1e6 * avg_mv,
+                                "algorithmic_bytes": bytes_mv,
+                                "note": "7.9 MB operator: launch- and latency-bound at this size"},
+            "roofline_matvec_hbm": {"bound": "hbm", "achieved": bytes_lg / avg_lg / 1e9, "peak": peak, "unit": "GB/s",
+                                    "frac": bytes_lg / avg_lg / 1e9 / peak, "kernel": "op_matvec_bulk_kernel<float,6>",
+                                    "avg_launch_us": 1e6 * avg_lg, "algorithmic_bytes": bytes_lg,
+                                    "workload": "hydrogen lmax 300, 2000 B-splines (operator > L2)"},
             "cpu_baseline": cpu,
             "ensemble": ens,
             "clocks": clk.summary(),
@@ -369,7 +433,6 @@ def _oracle_setup():
 
 
 def _oracle_worker(nsteps, q):
-    os.environ["OPENBLAS_NUM_THREADS"] = "1"
     cay, psi = _oracle_setup()
     dt = WORKLOAD["timestep"]
     t0 = time.perf_counter()
@@ -385,9 +448,20 @@ def cpu_baseline_sample(nsteps=20, procs=1):
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    ps = [ctx.Process(target=_oracle_worker, args=(nsteps, q)) for _ in range(procs)]
-    for p in ps:
-        p.start()
+    # one BLAS thread per process: set before the children start (their numpy reads it at import)
+    saved = {k: os.environ.get(k) for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")}
+    for k in saved:
+        os.environ[k] = "1"
+    try:
+        ps = [ctx.Process(target=_oracle_worker, args=(nsteps, q)) for _ in range(procs)]
+        for p in ps:
+            p.start()
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
     times = [q.get() for _ in ps]
     for p in ps:
         p.join()

@@ -12,9 +12,28 @@ from __future__ import annotations
 import math
 
 import numpy as np
-from scipy.special import lpmv
 
 from .bspline import gauss_legendre
+
+
+def normalized_legendre(lmax, m, x):
+    """sqrt((2l+1)/2 (l-m)!/(l+m)!) P_l^m(x) for l = m..lmax (columns), Condon-Shortley phase
+    included (as scipy's lpmv), by the three-term recurrence in l of the normalised functions,
+    which stays finite where the factorials overflow (l > 170)."""
+    x = np.asarray(x, dtype=np.float64)
+    s = np.sqrt(np.maximum(0.0, 1.0 - x * x))
+    q = np.full_like(x, math.sqrt(0.5))
+    for k in range(1, m + 1):  # Q_k^k = -sqrt((2k+1)/(2k)) sin(theta) Q_{k-1}^{k-1}
+        q = -math.sqrt((2.0 * k + 1.0) / (2.0 * k)) * s * q
+    out = np.empty((len(x), lmax - m + 1))
+    out[:, 0] = q
+    if lmax > m:
+        out[:, 1] = math.sqrt(2.0 * m + 3.0) * x * q
+    for l in range(m + 2, lmax + 1):
+        a = math.sqrt((4.0 * l * l - 1.0) / (l * l - m * m))
+        b = math.sqrt(((l - 1.0) ** 2 - m * m) / (4.0 * (l - 1.0) ** 2 - 1.0))
+        out[:, l - m] = a * (x * out[:, l - m - 1] - b * out[:, l - m - 2])
+    return out
 
 
 class ReducedSphericalTools:
@@ -30,11 +49,7 @@ class ReducedSphericalTools:
         self.l_values = ls
         cos_t = np.cos(self.ThetaGrid)
         sign = (-1.0) ** self.M if self.M > 0 else 1.0
-        P = np.empty((len(x), len(ls)))
-        for idx, l in enumerate(ls):
-            norm = sign * math.sqrt((2.0 * l + 1) / (4 * math.pi) * math.factorial(l - abs(self.M))
-                                    / math.factorial(l + abs(self.M))) * math.sqrt(2 * math.pi)
-            P[:, idx] = lpmv(abs(self.M), l, cos_t) * norm
+        P = sign * normalized_legendre(self.LMax, abs(self.M), cos_t)
         self.AssocLegendrePoly = P
         D = np.zeros_like(P)
         for idx, l in enumerate(ls):
