@@ -151,7 +151,7 @@ def time_matvec(torch, prob, flush, reps=50):
     sc = op.scales(5.0)
     avg = _time_launches(torch, lambda: op.matvec(sc, src, dst), flush, reps)
     elems = op.stored_elements()
-    return avg, 8 * (elems + 2 * nang * N), elems
+    return avg, 8 * (elems + 2 * nang * N), op.variant()[0]
 
 
 def time_block_solve(torch, prob, flush, reps=50):
@@ -173,6 +173,10 @@ def time_block_solve(torch, prob, flush, reps=50):
 LARGE = dict(lmax=300, nbsplines=2000, rmax=2000.0)
 
 
+MATVEC_KERNELS = {1: "op_matvec_bulk_kernel<float,6,64>", 2: "op_matvec_bulk_kernel<float,6,128>",
+                  3: "op_matvec_kernel<float,6>"}
+
+
 def time_large_matvec(torch, flush, reps=20):
     """The fused complex64 matvec on an operator larger than L2 (hydrogen lmax 300, 2000
     B-splines: 901 band blocks, 187 MB), where it is HBM-bound: (avg s, algorithmic bytes)."""
@@ -189,8 +193,9 @@ def time_large_matvec(torch, flush, reps=20):
     sc = op.scales(5.0)
     avg = _time_launches(torch, lambda: op.matvec(sc, src, dst), flush, reps)
     nbytes = 8 * (op.stored_elements() + 2 * nang * N)
+    variant = op.variant()
     del op, bp, prob
-    return avg, nbytes
+    return avg, nbytes, variant
 
 
 def profile_traffic(name):
@@ -291,9 +296,9 @@ def run_ours(args):
     e2e_t = time.perf_counter() - t0
     nbytes = psi0.size * 16
 
-    avg_mv, bytes_mv, elems = time_matvec(torch, prob, flush)
+    avg_mv, bytes_mv, variant_mv = time_matvec(torch, prob, flush)
     avg_ts, bytes_ts = time_block_solve(torch, prob, flush)
-    avg_lg, bytes_lg = time_large_matvec(torch, flush)
+    avg_lg, bytes_lg, variant_lg = time_large_matvec(torch, flush)
     peak, peak_kind = measured_peaks()
 
     ens = run_ensemble(args, torch, flush) if args.ensemble > 0 else None
@@ -324,13 +329,14 @@ def run_ours(args):
             "roofline_matvec": {"bound": "hbm", "achieved": bytes_mv / avg_mv / 1e9, "peak": peak, "unit": "GB/s",
                                 "frac": bytes_mv / avg_mv / 1e9 / peak,
                                 "traffic": profile_traffic("op_matvec_bulk_kernel_fp32_lmax40_n600.md"),
-                                "kernel": "op_matvec_bulk_kernel<float,6>", "avg_launch_us": 1e6 * avg_mv,
+                                "kernel": MATVEC_KERNELS[variant_mv], "avg_launch_us": 1e6 * avg_mv,
                                 "algorithmic_bytes": bytes_mv,
                                 "note": "7.9 MB operator: launch- and latency-bound at this size"},
             "roofline_matvec_hbm": {"bound": "hbm", "achieved": bytes_lg / avg_lg / 1e9, "peak": peak, "unit": "GB/s",
-                                    "frac": bytes_lg / avg_lg / 1e9 / peak, "kernel": "op_matvec_bulk_kernel<float,6>",
+                                    "frac": bytes_lg / avg_lg / 1e9 / peak, "kernel": MATVEC_KERNELS[variant_lg[0]],
                                     "avg_launch_us": 1e6 * avg_lg, "algorithmic_bytes": bytes_lg,
-                                    "workload": "hydrogen lmax 300, 2000 B-splines (operator > L2)"},
+                                    "workload": "hydrogen lmax 300, 2000 B-splines (operator > L2)",
+                                    "variant": variant_lg[0], "tuning_us": variant_lg[1]},
             "cpu_baseline": cpu,
             "ensemble": ens,
             "clocks": clk.summary(),

@@ -134,6 +134,12 @@ int pg_op_add_term_ranks(pg_op *op, const char *storage, const double *potential
                          const int *pairs, const int *npairs, int slot);
 /* Upload. Must be called once after the last add_term. */
 int pg_op_finalize(pg_op *op);
+/* Matvec kernel variant (no reference counterpart): pg_op_finalize times the candidates on
+ * the operator's own shape (1 bulk-copy staging with 64-row tiles, 2 with 128-row tiles,
+ * 3 plain coalesced loads) and keeps the fastest. variant 1..3 forces one, variant < 0 only
+ * reads; current (optional) receives the variant in use, times_us (optional, 4 floats) the
+ * tuning times per variant index. */
+int pg_op_variant(pg_op *op, int variant, int *current, float *times_us);
 /* Number of complex band elements the operator stores (for roofline bookkeeping). */
 long long pg_op_stored_elements(const pg_op *op);
 /*
@@ -298,6 +304,11 @@ int pg_vec_dot(pg_ctx *ctx, int precision, const void *x, const void *y, long lo
 int pg_vec_convert(pg_ctx *ctx, int src_precision, const void *x, int dst_precision, void *y, long long n);
 /* V (complex128 [k][n]) <- V (complex128 [m][n]) * Q (host complex128 [m][k], row major) */
 int pg_vec_combine(pg_ctx *ctx, void *V, long long n, int m, const double *Q, int k);
+/* y[a][j][i] = x[a][i][j] for x [n0][n1][n2] (device, precision PG_FP64/PG_FP32, x != y): the
+ * two-electron wavefunction's radial ranks swapped, so that operations along the first
+ * electron's rank run as fibre operations (CombinedRepresentation over two B-spline ranks,
+ * core/representation/combinedrepresentation.cpp:164-238). */
+int pg_vec_swap_last2(pg_ctx *ctx, int precision, const void *x, void *y, int n0, int n1, int n2);
 
 /* ---------------------------------------------------------------------------------- */
 /* learned preconditioner network                                                     */

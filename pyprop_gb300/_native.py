@@ -71,6 +71,7 @@ _SIGS = {
     "pg_op_add_term": (_I, [_P, C.c_char_p, _DP, _I, _I, _IP, _I, _I]),
     "pg_op_add_term_ranks": (_I, [_P, C.c_char_p, _DP, _IP, _IP, _IP, _I]),
     "pg_op_finalize": (_I, [_P]),
+    "pg_op_variant": (_I, [_P, _I, _IP, C.POINTER(C.c_float)]),
     "pg_op_stored_elements": (_LL, [_P]),
     "pg_op_matvec": (_I, [_P, _DP, _I, _P, _P, _I]),
     "pg_overlap_create": (_I, [_P, _DP, C.POINTER(_P)]),
@@ -98,6 +99,7 @@ _SIGS = {
     "pg_vec_dot": (_I, [_P, _I, _P, _P, _LL, _DP]),
     "pg_vec_convert": (_I, [_P, _I, _P, _I, _P, _LL]),
     "pg_vec_combine": (_I, [_P, _P, _LL, _I, _DP, _I]),
+    "pg_vec_swap_last2": (_I, [_P, _I, _P, _P, _I, _I, _I]),
     "pg_mlp_create": (_I, [_P, _I, _I, _I, C.c_ulonglong, C.POINTER(_P)]),
     "pg_mlp_destroy": (_I, [_P]),
     "pg_mlp_parameter_count": (_LL, [_P]),

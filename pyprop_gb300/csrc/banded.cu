@@ -366,6 +366,7 @@ int upload_cplx(const std::vector<zd> &v, void **dptr)
 
 struct pg_banded_ext : pg_banded {
     void *d_scratch = nullptr;
+    void *d_swap = nullptr;  // two-electron operators: the wavefunction with its radial ranks swapped
 };
 
 extern "C" int pg_overlap_create(pg_op *op, const double *overlap_rows, pg_banded **out)
@@ -409,6 +410,10 @@ extern "C" int pg_overlap_create(pg_op *op, const double *overlap_rows, pg_bande
     }
     const size_t esz = op->precision == PG_FP64 ? sizeof(cxd) : sizeof(cxf);
     PG_CUDA_TRY(cudaMalloc(&b->d_scratch, esz * (size_t)op->nrows * N));
+    if (op->rank == 3) {
+        if (op->shape[1] != N) return PG_ERR_SHAPE;  // both radial ranks share the B-spline basis
+        PG_CUDA_TRY(cudaMalloc(&b->d_swap, esz * (size_t)op->nrows * N));
+    }
     *out = b;
     return PG_OK;
 }
@@ -494,6 +499,7 @@ extern "C" int pg_banded_destroy(pg_banded *b)
     cudaFree(e->d_lo_rb);
     cudaFree(e->d_up_rb);
     cudaFree(e->d_scratch);
+    cudaFree(e->d_swap);
     delete e;
     return PG_OK;
 }
@@ -583,11 +589,25 @@ static int banded_apply_t(pg_banded *bb, int which, void *x)
     }
 }
 
+static int banded_apply_fibres(pg_banded *b, int which, void *x)
+{
+    if (b->op->precision == PG_FP64) return banded_apply_t<double>(b, which, x);
+    return banded_apply_t<float>(b, which, x);
+}
+
+// Overlap operations act on every B-spline rank: for a two-electron operator [Nang][N][N]
+// the last rank as fibres, then the middle rank on the copy with the two radial ranks swapped
+// (S x S = (S x 1)(1 x S); the same for the factors U).
 int pg_banded_apply_dev(pg_banded *b, int which, void *x)
 {
     if (!b || !x) return PG_ERR_ARG;
-    if (b->op->precision == PG_FP64) return banded_apply_t<double>(b, which, x);
-    return banded_apply_t<float>(b, which, x);
+    PG_TRY(banded_apply_fibres(b, which, x));
+    if (b->kind != 0 || b->op->rank != 3) return PG_OK;
+    pg_banded_ext *e = static_cast<pg_banded_ext *>(b);
+    const int n0 = b->op->shape[0], n1 = b->op->shape[1], n2 = b->op->shape[2];
+    PG_TRY(pg_swap_last2_dev(b->op->ctx, b->op->precision, x, e->d_swap, n0, n1, n2));
+    PG_TRY(banded_apply_fibres(b, which, e->d_swap));
+    return pg_swap_last2_dev(b->op->ctx, b->op->precision, e->d_swap, x, n0, n2, n1);
 }
 
 extern "C" int pg_banded_apply(pg_banded *b, int which, void *x) { return pg_banded_apply_dev(b, which, x); }

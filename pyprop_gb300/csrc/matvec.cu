@@ -202,13 +202,12 @@ __global__ void __launch_bounds__(128) op_dense_kernel(int N, const int *__restr
 // ------------------------------------------------------------------------------------
 // fused operator, bulk-copy staged variant
 // ------------------------------------------------------------------------------------
-// One CTA = BT radial rows of one angular row. Thread 0 issues one cp.async.bulk per
+// One CTA = BT radial rows of one angular row. Warp 0 issues one cp.async.bulk per
 // (entry, diagonal) band slab [d][i0 .. i0+BT) into shared memory, all completing on one
 // mbarrier (expected bytes), while all threads load the source slabs x[col][i0-kb .. i0+BT+kb)
 // with ordinary coalesced loads. The whole CTA's operator tile is in flight at once, so the
 // kernel is bound by HBM rather than by load latency. Entries of a row are processed in
 // groups of BMAXE. Requires band leading dimension ld (>= N) with 16-byte aligned slabs.
-static const int BT = 64;
 static const int BMAXE = 4;
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -246,7 +245,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
     return false;
 }
 
-template <typename R, int KB>
+template <typename R, int KB, int BT>
 __global__ void __launch_bounds__(BT) op_matvec_bulk_kernel(OpDev op, pg_scales scales, const cxd *__restrict__ scales_dev,
                                                             const cx<R> *__restrict__ src, cx<R> *__restrict__ dst,
                                                             int accumulate, int *err)
@@ -274,12 +273,14 @@ __global__ void __launch_bounds__(BT) op_matvec_bulk_kernel(OpDev op, pg_scales 
     unsigned phase = 0;
     for (int e0 = e_begin; e0 < e_end; e0 += BMAXE) {
         const int ne = min(BMAXE, e_end - e0);
-        if (t == 0) {
-            mbar_arrive_expect_tx(bar, slab_bytes * (unsigned)(ne * B));
-            for (int q = 0; q < ne; ++q) {
+        if (t < 32) {
+            // lane 0 announces the bytes, then the 32 lanes of warp 0 issue the slab copies
+            if (t == 0) mbar_arrive_expect_tx(bar, slab_bytes * (unsigned)(ne * B));
+            __syncwarp();
+            for (int sl = t; sl < ne * B; sl += 32) {
+                const int q = sl / B, d = sl - q * B;
                 const cx<R> *V = bands + (size_t)op.ent_band[e0 + q] * B * ld + i0;
-                for (int d = 0; d < B; ++d)
-                    bulk_g2s(bs + ((size_t)q * B + d) * BT, V + (size_t)d * ld, slab_bytes, bar);
+                bulk_g2s(bs + ((size_t)q * B + d) * BT, V + (size_t)d * ld, slab_bytes, bar);
             }
         }
         for (int q = 0; q < ne; ++q) {
@@ -319,24 +320,32 @@ __global__ void __launch_bounds__(BT) op_matvec_bulk_kernel(OpDev op, pg_scales 
     }
 }
 
+template <typename R, int KB, int BT>
+static int launch_bulk_bt(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
+                          int accumulate)
+{
+    constexpr int B = 2 * KB + 1;
+    const size_t smem = 128 + sizeof(cx<R>) * ((size_t)BMAXE * B * BT + (size_t)BMAXE * (BT + 2 * KB));
+    static bool configured = false;
+    if (!configured) {
+        PG_CUDA_TRY(cudaFuncSetAttribute(op_matvec_bulk_kernel<R, KB, BT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = true;
+    }
+    dim3 grid((op->N + BT - 1) / BT, op->nrows);
+    op_matvec_bulk_kernel<R, KB, BT><<<grid, BT, smem, op->ctx->stream>>>(
+        op->dev(), scales, scales_dev, (const cx<R> *)src, (cx<R> *)dst, accumulate, op->ctx->d_err);
+    op->ctx->launches++;
+    return pg_check_launch(op->ctx);
+}
+
+// tile width by the operator's tuned variant (64-row tiles: more CTAs; 128-row: fewer, larger copies)
 template <typename R, int KB>
 static int launch_bulk(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
                        int accumulate)
 {
-    constexpr int B = 2 * KB + 1;
-    const size_t smem = 128 + sizeof(cx<R>) * ((size_t)BMAXE * B * BT + (size_t)BMAXE * (BT + 2 * KB));
-    static bool configured[2] = {false, false};
-    const int which = sizeof(R) == 8 ? 1 : 0;
-    if (!configured[which]) {
-        PG_CUDA_TRY(cudaFuncSetAttribute(op_matvec_bulk_kernel<R, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem));
-        configured[which] = true;
-    }
-    dim3 grid((op->N + BT - 1) / BT, op->nrows);
-    op_matvec_bulk_kernel<R, KB><<<grid, BT, smem, op->ctx->stream>>>(op->dev(), scales, scales_dev, (const cx<R> *)src,
-                                                                       (cx<R> *)dst, accumulate, op->ctx->d_err);
-    op->ctx->launches++;
-    return pg_check_launch(op->ctx);
+    if (op->variant == 2) return launch_bulk_bt<R, KB, 128>(op, scales, scales_dev, src, dst, accumulate);
+    return launch_bulk_bt<R, KB, 64>(op, scales, scales_dev, src, dst, accumulate);
 }
 
 template <typename R>
@@ -379,7 +388,7 @@ int pg_op_matvec_dev(pg_op *op, const pg_scales &scales, const cxd *scales_dev, 
 {
     if (!op || !op->finalized) return PG_ERR_STATE;
     const bool fp64 = op->precision == PG_FP64;
-    if (op->kb == 6 && !src_inv_scale_dev && !src_copy_out && op->use_bulk) {
+    if (op->kb == 6 && !src_inv_scale_dev && !src_copy_out && op->use_bulk && op->variant != 3) {
         PG_TRY(fp64 ? launch_bulk<double, 6>(op, scales, scales_dev, src, dst, accumulate)
                     : launch_bulk<float, 6>(op, scales, scales_dev, src, dst, accumulate));
     } else {
@@ -603,6 +612,8 @@ static void expand_outer(const HostTerm &t, const std::vector<int> &shape, std::
     }
 }
 
+static int autotune(pg_op *op);
+
 extern "C" int pg_op_finalize(pg_op *op)
 {
     if (!op) return PG_ERR_ARG;
@@ -766,6 +777,70 @@ extern "C" int pg_op_finalize(pg_op *op)
         }
     }
     op->finalized = true;
+    return autotune(op);
+}
+
+// The matvec kernel variant for this operator, by measurement: each candidate runs 2 untimed
+// and 5 timed launches (CUDA events on the context's stream) on zero vectors of the
+// operator's shape; the fastest is kept. All variants compute the same sums in the same order.
+static int autotune(pg_op *op)
+{
+    op->variant = 1;
+    if (op->kb != 6 || !op->use_bulk) return PG_OK;  // only the bulk kernels have variants
+    cudaStream_t s = op->ctx->stream;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PG_CUDA_TRY(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return PG_OK;  // no timing inside a capture
+    const size_t esz = op->precision == PG_FP64 ? sizeof(cxd) : sizeof(cxf);
+    const size_t n = (size_t)op->nrows * op->N;
+    void *x = nullptr, *y = nullptr;
+    PG_CUDA_TRY(cudaMalloc(&x, esz * n));
+    PG_CUDA_TRY(cudaMalloc(&y, esz * n));
+    PG_CUDA_TRY(cudaMemsetAsync(x, 0, esz * n, s));
+    cudaEvent_t a, b;
+    PG_CUDA_TRY(cudaEventCreate(&a));
+    PG_CUDA_TRY(cudaEventCreate(&b));
+    pg_scales sc;
+    memset(&sc, 0, sizeof(sc));
+    const long long launches = op->ctx->launches;
+    int code = PG_OK;
+    float best = 1e30f;
+    int best_v = 1;
+    for (int v = 1; v <= 3 && code == PG_OK; ++v) {
+        op->variant = v;
+        for (int k = 0; k < 2 && code == PG_OK; ++k) code = pg_op_matvec_dev(op, sc, nullptr, x, y, 0, nullptr, nullptr);
+        if (code != PG_OK) break;
+        cudaEventRecord(a, s);
+        for (int k = 0; k < 5 && code == PG_OK; ++k) code = pg_op_matvec_dev(op, sc, nullptr, x, y, 0, nullptr, nullptr);
+        cudaEventRecord(b, s);
+        if (cudaEventSynchronize(b) != cudaSuccess) code = PG_ERR_CUDA;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        op->variant_us[v] = 1e3f * ms / 5.f;
+        if (op->variant_us[v] < best) {
+            best = op->variant_us[v];
+            best_v = v;
+        }
+    }
+    op->ctx->launches = launches;  // tuning launches are not the caller's work
+    op->variant = best_v;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(x);
+    cudaFree(y);
+    return code;
+}
+
+// Force (1 bulk 64-row tiles, 2 bulk 128-row, 3 plain loads) or read (variant < 0) the matvec
+// kernel variant; times_us (optional, 4 floats) receives the tuning measurements.
+extern "C" int pg_op_variant(pg_op *op, int variant, int *current, float *times_us)
+{
+    if (!op || !op->finalized) return PG_ERR_STATE;
+    if (variant >= 1 && variant <= 3) op->variant = variant;
+    else if (variant >= 0) return PG_ERR_ARG;
+    if (current) *current = op->variant;
+    if (times_us)
+        for (int k = 0; k < 4; ++k) times_us[k] = op->variant_us[k];
     return PG_OK;
 }
 

@@ -135,6 +135,10 @@ struct pg_op {
     long long nentries = 0;
     int ld = 0;
     int use_bulk = 1;
+    // matvec kernel variant, chosen by measurement at finalize (pg_op_set_variant overrides):
+    // 1 bulk-copy 64-row tiles, 2 bulk-copy 128-row tiles, 3 plain loads (128 threads)
+    int variant = 1;
+    float variant_us[4] = {0.f, 0.f, 0.f, 0.f};
     OpDev dev() const {
         OpDev o;
         o.nrows = nrows; o.N = N; o.ld = ld; o.kb = kb; o.b = b;
@@ -189,6 +193,8 @@ struct pg_banded {
 };
 
 int pg_banded_apply_dev(pg_banded *b, int which, void *x);
+// y[a][j][i] = x[a][i][j], x [n0][n1][n2] (vector.cu)
+int pg_swap_last2_dev(pg_ctx *ctx, int precision, const void *x, void *y, int n0, int n1, int n2);
 
 // ------------------------------------------------------------------------------------
 // learned preconditioner network (mlp.cu)

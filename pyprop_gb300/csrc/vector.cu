@@ -457,3 +457,48 @@ extern "C" int pg_vec_multidot_noalloc(int precision, const void *V, long long l
     PG_CUDA_TRY(cudaGetLastError());
     return PG_OK;
 }
+
+// ------------------------------------------------------------------------------------
+// swap of the last two ranks: y[a][j][i] = x[a][i][j] (x: [n0][n1][n2])
+// ------------------------------------------------------------------------------------
+// Two-electron wavefunctions [Nang][N][N] keep their fibres along the last rank; operations
+// along the middle rank (the first electron's overlap) run on the swapped copy. 32x32 tiles
+// through shared memory, both global sides coalesced.
+template <typename R>
+__global__ void swap_last2_kernel(const cx<R> *__restrict__ x, cx<R> *__restrict__ y, int n1, int n2)
+{
+    __shared__ cx<R> tile[32][33];
+    const int a = blockIdx.z;
+    const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+    const cx<R> *xa = x + (size_t)a * n1 * n2;
+    cx<R> *ya = y + (size_t)a * n1 * n2;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int i = i0 + r, j = j0 + threadIdx.x;
+        if (i < n1 && j < n2) tile[r][threadIdx.x] = xa[(size_t)i * n2 + j];
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int j = j0 + r, i = i0 + threadIdx.x;
+        if (i < n1 && j < n2) ya[(size_t)j * n1 + i] = tile[threadIdx.x][r];
+    }
+}
+
+extern "C" int pg_vec_swap_last2(pg_ctx *ctx, int precision, const void *x, void *y, int n0, int n1, int n2)
+{
+    if (!ctx || !x || !y || n0 < 0 || n1 < 0 || n2 < 0 || x == y) return PG_ERR_ARG;
+    if (precision != PG_FP64 && precision != PG_FP32) return PG_ERR_ARG;
+    return pg_swap_last2_dev(ctx, precision, x, y, n0, n1, n2);
+}
+
+int pg_swap_last2_dev(pg_ctx *ctx, int precision, const void *x, void *y, int n0, int n1, int n2)
+{
+    if (n0 == 0 || n1 == 0 || n2 == 0) return PG_OK;
+    if (n0 > 65535) return PG_ERR_SHAPE;
+    dim3 grid((n2 + 31) / 32, (n1 + 31) / 32, n0), block(32, 8);
+    if (precision == PG_FP64)
+        swap_last2_kernel<double><<<grid, block, 0, ctx->stream>>>((const cxd *)x, (cxd *)y, n1, n2);
+    else
+        swap_last2_kernel<float><<<grid, block, 0, ctx->stream>>>((const cxf *)x, (cxf *)y, n1, n2);
+    ctx->launches++;
+    return pg_check_launch(ctx);
+}

@@ -156,6 +156,13 @@ class DeviceOperator:
     def stored_elements(self):
         return int(self.lib.pg_op_stored_elements(self.h))
 
+    def variant(self, force=-1):
+        """(variant in use, tuning times in us per variant 1..3); force 1..3 selects one."""
+        cur = C.c_int(0)
+        times = (C.c_float * 4)()
+        check(self.lib.pg_op_variant(self.h, int(force), C.byref(cur), times), "pg_op_variant")
+        return cur.value, [float(times[k]) for k in range(1, 4)]
+
     def matvec(self, scales, src, dst, accumulate=False):
         sc = np.ascontiguousarray(scales, dtype=np.complex128)
         _, sp = nat.dptr(sc.view(np.float64))
@@ -288,6 +295,15 @@ class CayleyStepper:
                 self.lib.pg_cayley_destroy(self.h)
         except Exception:
             pass
+
+
+def swap_last2(ctx, x, y):
+    """y[a][j][i] = x[a][i][j] for rank-3 device tensors (complex128 or complex64)."""
+    t = torch()
+    prec = nat.PG_FP64 if x.dtype == t.complex128 else nat.PG_FP32
+    n0, n1, n2 = x.shape
+    ctx.bind_stream()
+    check(ctx.lib.pg_vec_swap_last2(ctx.h, prec, ptr(x), ptr(y), n0, n1, n2), "pg_vec_swap_last2")
 
 
 def vec_dot(ctx, x, y, precision=nat.PG_FP64):

@@ -172,3 +172,90 @@ def register_potential(cls):
     """Make a user evaluator class available to ``classname = "..."`` in configs."""
     POTENTIAL_CLASSES[cls.__name__] = cls
     return cls
+
+
+# ---------------------------------------------------------------------------------------
+# two-electron (coupled spherical harmonics) evaluators
+# ---------------------------------------------------------------------------------------
+# The coupled angular rank is never on a grid: its "coordinate" is the index of an angular
+# basis pair, and these evaluators are bound to the angular basis and its pair list before
+# they are evaluated (``bind``), as the reference's custom evaluators receive the basis pairs
+# (examples/tensor/helium_stabilization/coupledspherical.cpp, coupledbase.h).
+
+
+class CoupledPotentialBase(PotentialBase):
+    _keys = ("angular_rank", "radial_rank1", "radial_rank2", "mass", "z")
+    angular_rank = 0
+    radial_rank1 = 1
+    radial_rank2 = 2
+    mass = 1.0
+    needs_basis = True
+
+    def bind(self, bases, geoms):
+        self.basis = bases[self.angular_rank]
+        self.pairs = geoms[self.angular_rank].GetBasisPairs()
+
+    def _left_right(self):
+        idx = self.basis.indices
+        return [(idx[int(a)], idx[int(b)]) for a, b in self.pairs]
+
+
+class CoupledSphericalCoulombPotential(PotentialBase):
+    """Nuclear attraction of both electrons, ``-z/r1 - z/r2`` (potential.cpp:44-78)."""
+    _keys = ("z", "radial_rank1", "radial_rank2")
+    z = 2.0
+    radial_rank1 = 1
+    radial_rank2 = 2
+
+    def GetPotentialValue(self, pos):
+        r1, r2 = pos[self.radial_rank1], pos[self.radial_rank2]
+        return np.broadcast_to(-self.z / r1 - self.z / r2, np.broadcast(*pos).shape)
+
+
+class CoupledSphericalKineticEnergyEvaluator(CoupledPotentialBase):
+    """Angular kinetic energy ``l1(l1+1)/(2 m r1^2) + l2(l2+1)/(2 m r2^2)`` on pairs of equal
+    coupled indices, zero on others (coupledspherical.cpp:132-210)."""
+
+    def GetPotentialValue(self, pos):
+        r1, r2 = pos[self.radial_rank1], pos[self.radial_rank2]
+        lr = self._left_right()
+        shape = np.broadcast(*pos).shape
+        out = np.zeros(shape)
+        for p, (a, b) in enumerate(lr):
+            if (a.L, a.M, a.l1, a.l2) != (b.L, b.M, b.l1, b.l2):
+                continue
+            sl = [slice(None)] * len(shape)
+            sl[self.angular_rank] = p
+            v = a.l1 * (a.l1 + 1.0) / (2.0 * self.mass * r1 * r1) + a.l2 * (a.l2 + 1.0) / (2.0 * self.mass * r2 * r2)
+            out[tuple(sl)] = np.squeeze(np.broadcast_to(v, shape)[tuple(sl)])
+        return out
+
+
+class CustomPotentialEvaluationR12(CoupledPotentialBase):
+    """Electron-electron repulsion ``1/|r1 - r2|`` in the multipole expansion
+    (coupledspherical.cpp:7-127): for each angular pair, sum over l3 of the angular factor
+    times r<^l3 / r>^(l3+1)."""
+
+    def GetPotentialValue(self, pos):
+        from .spherical import r12_angular_sum, r12_multipoles
+        r1, r2 = pos[self.radial_rank1], pos[self.radial_rank2]
+        rmin, rmax = np.minimum(r1, r2), np.maximum(r1, r2)
+        frac = rmin / rmax
+        shape = np.broadcast(*pos).shape
+        out = np.zeros(shape)
+        for p, (left, right) in enumerate(self._left_right()):
+            v = 0.0
+            for l3 in r12_multipoles(left, right):
+                c = r12_angular_sum(left, right, l3)
+                if c != 0.0:
+                    v = v + c * frac ** l3 / rmax
+            if np.isscalar(v) and v == 0.0:
+                continue
+            sl = [slice(None)] * len(shape)
+            sl[self.angular_rank] = p
+            out[tuple(sl)] = np.squeeze(np.broadcast_to(v, shape)[tuple(sl)])
+        return out
+
+
+for _cls in (CoupledSphericalCoulombPotential, CoupledSphericalKineticEnergyEvaluator, CustomPotentialEvaluationR12):
+    POTENTIAL_CLASSES[_cls.__name__] = _cls

@@ -2,9 +2,10 @@
 
 Follows ``pyprop/Problem.py:62-307`` (``SetupStep``, ``AdvanceStep``, ``Advance``,
 ``GetEnergyExpectationValue``) and the representation factory of
-``pyprop/CreateInstance.py:11-93`` for the two ranks this path supports: a
+``pyprop/CreateInstance.py:11-93`` for the ranks this path supports: a
 ``ReducedSphericalHarmonicRepresentation`` angular rank and a ``BSplineRepresentation``
-radial rank.
+radial rank (one electron), or a ``CoupledSphericalHarmonicRepresentation`` angular rank and
+two B-spline radial ranks (two electrons).
 """
 from __future__ import annotations
 
@@ -12,7 +13,7 @@ import numpy as np
 
 from .bspline import bspline_from_config
 from .representation import CombinedRepresentation, Wavefunction
-from .tensorpotential import BSplineRankBasis, ReducedSphericalRankBasis
+from .tensorpotential import BSplineRankBasis, CoupledSphericalRankBasis, ReducedSphericalRankBasis
 
 
 class _CoreNamespace:
@@ -25,6 +26,12 @@ class _CoreNamespace:
         pass
 
     class BSplineRepresentation:
+        pass
+
+    class CombinedRepresentation_3:
+        pass
+
+    class CoupledSphericalHarmonicRepresentation:
         pass
 
 
@@ -54,6 +61,9 @@ def CreateRepresentation(config):
             bases.append(ReducedSphericalRankBasis(int(sub.maxl), int(getattr(sub, "m", 0))))
         elif t is core.BSplineRepresentation or getattr(t, "__name__", "") == "BSplineRepresentation":
             bases.append(BSplineRankBasis(bspline_from_config(sub)))
+        elif t is core.CoupledSphericalHarmonicRepresentation or getattr(t, "__name__", "") == \
+                "CoupledSphericalHarmonicRepresentation":
+            bases.append(CoupledSphericalRankBasis(sub.index_iterator))
         else:
             raise NotImplementedError("representation type %r is outside the GPU path" % (t,))
     return CombinedRepresentation(bases)

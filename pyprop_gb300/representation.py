@@ -44,28 +44,34 @@ class CombinedRepresentation:
         if self._ovl is None:
             ctx = Context.get()
             shape = self.GetFullShape()
+            if len(shape) == 3 and (shape[1] != shape[2] or not isinstance(self.bases[1], BSplineRankBasis)):
+                raise ValueError("two-electron ranks must share one B-spline basis")
             # an empty operator only carries the shape/precision for the banded object
             self._ovl_op = _ShapeOp(ctx, shape, self.kb)
             self._ovl = Banded.overlap(self._ovl_op, self.overlap_rows)
         return self._ovl
 
+    def _radial(self, which, data):
+        """A banded overlap operation along every B-spline rank (for two electrons the library
+        applies it along both radial ranks)."""
+        self._overlap().apply(which, data)
+
     def MultiplyOverlap(self, psi):
-        self._overlap().apply(nat.PG_BAND_MUL_S, psi.GetData())
+        self._radial(nat.PG_BAND_MUL_S, psi.GetData())
 
     def SolveOverlap(self, psi):
-        self._overlap().apply(nat.PG_BAND_SOLVE_S, psi.GetData())
+        self._radial(nat.PG_BAND_SOLVE_S, psi.GetData())
 
     def MultiplySqrtOverlap(self, conj, psi):
-        self._overlap().apply(nat.PG_BAND_MUL_UT if conj else nat.PG_BAND_MUL_U, psi.GetData())
+        self._radial(nat.PG_BAND_MUL_UT if conj else nat.PG_BAND_MUL_U, psi.GetData())
 
     def SolveSqrtOverlap(self, conj, psi):
-        self._overlap().apply(nat.PG_BAND_SOLVE_UT if conj else nat.PG_BAND_SOLVE_U, psi.GetData())
+        self._radial(nat.PG_BAND_SOLVE_UT if conj else nat.PG_BAND_SOLVE_U, psi.GetData())
 
     def InnerProduct(self, psi1, psi2):
-        """<psi1 | S | psi2> over the B-spline rank (Euclidean over the angular rank)."""
-        t = torch()
+        """<psi1 | S | psi2> over the B-spline ranks (Euclidean over the angular rank)."""
         tmp = psi2.GetData().clone()
-        self._overlap().apply(nat.PG_BAND_MUL_S, tmp)
+        self._radial(nat.PG_BAND_MUL_S, tmp)
         return vec_dot(Context.get(), psi1.GetData(), tmp)
 
 

@@ -132,3 +132,86 @@ class DefaultCoupledIndexIterator:
 
     def __repr__(self):
         return "DefaultCoupledIndexIterator(lmax=%d, L=%r, M=%r)" % (self.lmax, self.L, self.M)
+
+
+def clebsch_gordan(j1, j2, m1, m2, J, M):
+    """<j1 m1 j2 m2 | J M> for integer angular momenta (Racah's closed form, evaluated with
+    log-factorials), the coefficient ``CoupledSpherical::ClebschGordan`` returns as
+    ``cg(j1, j2, m1, m2, J, M)``. Zero outside the selection rules."""
+    if m1 + m2 != M or abs(m1) > j1 or abs(m2) > j2 or abs(M) > J:
+        return 0.0
+    if J < abs(j1 - j2) or J > j1 + j2:
+        return 0.0
+    lf = math.lgamma
+
+    def f(n):
+        return lf(n + 1.0)
+
+    pre = 0.5 * (math.log(2.0 * J + 1.0) + f(J + j1 - j2) + f(J - j1 + j2) + f(j1 + j2 - J) - f(j1 + j2 + J + 1)
+                 + f(J + M) + f(J - M) + f(j1 - m1) + f(j1 + m1) + f(j2 - m2) + f(j2 + m2))
+    total = 0.0
+    kmin = max(0, j2 - J - m1, j1 - J + m2)
+    kmax = min(j1 + j2 - J, j1 - m1, j2 + m2)
+    for k in range(kmin, kmax + 1):
+        den = (f(k) + f(j1 + j2 - J - k) + f(j1 - m1 - k) + f(j2 + m2 - k) + f(J - j2 + m1 + k)
+               + f(J - j1 - m2 + k))
+        total += (-1.0) ** k * math.exp(pre - den)
+    return total
+
+
+class CoupledSphericalBasis:
+    """The coupled two-electron angular basis ``CoupledSphericalHarmonicRepresentation``:
+    an ordered list of (l1, l2, L, M) from an index iterator."""
+
+    def __init__(self, index_iterator):
+        self.indices = list(index_iterator)
+        self.size = len(self.indices)
+
+    def pairs(self, rule):
+        """(left, right) pairs accepted by ``rule(left, right)``, left-major
+        (core/tensorpotential/coupledsphericalselectionrule.h:16-52)."""
+        out = [(i, j) for i, a in enumerate(self.indices) for j, b in enumerate(self.indices) if rule(a, b)]
+        return np.asarray(out, dtype=np.int32).reshape(-1, 2)
+
+
+def rule_diagonal(a, b):
+    """``CoupledSphericalSelectionRuleDiagonal`` (coupledsphericalselectionrule.h:357-367)."""
+    return a.L == b.L and a.M == b.M and a.l1 == b.l1 and a.l2 == b.l2
+
+
+def rule_r12_old(a, b):
+    """``CoupledSphericalSelectionRuleR12Old`` (:58-86): equal L, M and both triangles."""
+    return (a.L == b.L and a.M == b.M and a.L <= a.l1 + a.l2 and abs(a.l1 - a.l2) <= a.L
+            and b.L <= b.l1 + b.l2 and abs(b.l1 - b.l2) <= b.L)
+
+
+def r12_angular_sum(left, right, l3):
+    """The angular factor of the multipole l3 of 1/|r1 - r2| between coupled states
+    (examples/tensor/helium_stabilization/coupledspherical.cpp:63-92): the m-sum over four
+    Clebsch-Gordan coefficients times the l3 coefficient, without the radial r<^l3/r>^(l3+1)."""
+    L, M = left.L, left.M
+    l1p, l2p, l1, l2 = left.l1, left.l2, right.l1, right.l2
+    coef = (math.sqrt((2.0 * l1p + 1.0) * (2.0 * l1 + 1.0) / (2.0 * l3 + 1.0))
+            * math.sqrt((2.0 * l2p + 1.0) * (2.0 * l2 + 1.0) / (2.0 * l3 + 1.0)) / (2.0 * l3 + 1.0)
+            * clebsch_gordan(l1p, l1, 0, 0, l3, 0) * clebsch_gordan(l2p, l2, 0, 0, l3, 0))
+    if coef == 0.0:
+        return 0.0
+    stop = max(l1, l1p, l2, l2p)
+    s = 0.0
+    for m1p in range(-stop, stop + 1):
+        m2p = M - m1p
+        for m1 in range(-stop, stop + 1):
+            m2 = M - m1
+            m3 = m1 - m1p
+            cur = (clebsch_gordan(l1p, l2p, m1p, m2p, L, M) * clebsch_gordan(l1, l2, m1, m2, L, M)
+                   * clebsch_gordan(l1p, l1, -m1p, m1, l3, m3) * clebsch_gordan(l2p, l2, -m2p, m2, l3, -m3))
+            if cur != 0.0:
+                s += cur * (-1.0) ** (m1p + m2p + m3)
+    return s * coef
+
+
+def r12_multipoles(left, right):
+    """l3 range of the multipole expansion between two coupled states (:60-61)."""
+    if left.L != right.L or left.M != right.M:
+        return range(0)
+    return range(max(abs(right.l1 - left.l1), abs(right.l2 - left.l2)), min(right.l1 + left.l1, right.l2 + left.l2) + 1)

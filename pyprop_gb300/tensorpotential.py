@@ -162,6 +162,42 @@ class ReducedSphericalRankBasis:
         return self.tools.project_pairs(values, geometry.Pairs, differentiation)
 
 
+class CoupledSphericalRankBasis:
+    """Two-electron angular rank (``CoupledSphericalHarmonicRepresentation``,
+    pyprop/tensorpotential/basis/CoupledSphericalHarmonic.py:94-170): never on a grid; its
+    geometries are pair lists from selection rules (core/tensorpotential/
+    coupledsphericalselectionrule.h) and its matrix elements come from custom evaluators."""
+
+    orthogonal = True
+
+    def __init__(self, index_iterator):
+        from .spherical import CoupledSphericalBasis
+        self.basis = CoupledSphericalBasis(index_iterator)
+        self.indices = self.basis.indices
+        self.size = self.basis.size
+
+    def GetGeometryInfo(self, name):
+        from .spherical import rule_diagonal, rule_r12_old
+        geom = name.lower().strip()
+        n = self.size
+        if geom == "identity":
+            return GeometryInfo("Ident", None, False)
+        if geom == "diagonal":
+            return GeometryInfo("Simp", self.basis.pairs(rule_diagonal), False)
+        if geom == "dense":
+            return GeometryInfo("Dense", [(i, j) for i in range(n) for j in range(n)], False)
+        if geom == "selectionrule_r12":
+            return GeometryInfo("Simp", self.basis.pairs(rule_r12_old), False)
+        raise ValueError("Geometry '%s' not supported by the coupled spherical rank" % name)
+
+    def grid(self, geometry):
+        n = 1 if geometry.Pairs is None else len(geometry.Pairs)
+        return np.arange(n, dtype=np.float64)
+
+    def represent(self, values, geometry, differentiation):
+        raise ValueError("coupled spherical harmonics are already a basis")
+
+
 # ---------------------------------------------------------------------------------------
 # generator + tensor potential
 # ---------------------------------------------------------------------------------------
@@ -186,6 +222,8 @@ def generate_potential(bases, conf):
     rank = len(bases)
     geoms = [bases[r].GetGeometryInfo(conf.Get("geometry%d" % r)) for r in range(rank)]
     evaluator = _evaluator_from_section(conf)
+    if getattr(evaluator, "needs_basis", False):
+        evaluator.bind(bases, geoms)
     grids = [bases[r].grid(geoms[r]) for r in range(rank)]
     pos = tuple(np.asarray(g).reshape([-1 if rr == r else 1 for rr in range(rank)]) for r, g in enumerate(grids))
     data = np.asarray(evaluator(pos), dtype=np.complex128)

@@ -130,3 +130,106 @@ radial_rank = 1
 charge = -1.0
 time_function = LaserFunctionSimpleLength
 """
+
+
+def helium(lmax=2, L=(0,), nbsplines=20, rmax=20.0, order=7, quad_order_additional=10, z=2.0,
+           propagator="PamPropagatorGPU", precision="fp64", timestep=0.01, duration=1.0, krylov_basis_size=20):
+    """Two-electron (helium-like) model in the layout of
+    examples/tensor/helium_stabilization/config.ini:1-124: coupled spherical harmonics
+    (``DefaultCoupledIndexIterator(lmax, L, M=0)``) x B-splines x B-splines, radial kinetic
+    energy of each electron, angular kinetic energy, nuclear attraction -z/r1 - z/r2 and the
+    electron-electron repulsion on ``SelectionRule_R12`` pairs. Field-free."""
+    total = nbsplines - 3 if order == 7 else nbsplines - (order - 4)
+    rpart, xsize = exponential_linear_params_for(0.0, rmax, total, gamma=2.0, rpartition=min(10.0, rmax / 2))
+    Ls = list(L)
+    return f"""
+[Representation]
+rank = 3
+type = core.CombinedRepresentation_3
+representation0 = "AngularRepresentation"
+representation1 = "RadialRepresentation"
+representation2 = "RadialRepresentation"
+
+[AngularRepresentation]
+type = core.CoupledSphericalHarmonicRepresentation
+index_iterator = DefaultCoupledIndexIterator(lmax={lmax}, L={Ls!r}, M=[0])
+
+[RadialRepresentation]
+type = core.BSplineRepresentation
+init_function = InitBSpline
+xmin = 0.0
+xmax = {rmax!r}
+xsize = {xsize}
+gamma = 2.0
+xpartition = {rpart!r}
+bpstype = 'exponentiallinear'
+continuity = 'zero'
+order = {order}
+quad_order_additional = {quad_order_additional}
+projection_algorithm = 0
+
+[InitialCondition]
+type = InitialConditionType.Function
+function = lambda conf, x: 1.0 * (x[0] == 0)
+
+[Propagation]
+grid_potential_list = ["RadialKineticEnergy1", "RadialKineticEnergy2", "AngularKineticEnergy", "CoulombPotential", "ElectronicCouplingPotential"]
+propagator = {propagator}
+base_propagator = BasisPropagatorGPU
+timestep = {timestep!r}
+duration = {duration!r}
+renormalization = False
+krylov_basis_size = {krylov_basis_size}
+krylov_tolerance = 0
+krylov_double_orthogonalization = True
+gpu_precision = "{precision}"
+silent = True
+
+[RadialKineticEnergy1]
+classname = "KineticEnergyPotential"
+geometry0 = "Diagonal"
+geometry1 = "banded-packed"
+geometry2 = "banded-packed"
+differentiation0 = 0
+differentiation1 = 2
+differentiation2 = 0
+mass = 1
+
+[RadialKineticEnergy2]
+classname = "KineticEnergyPotential"
+geometry0 = "Diagonal"
+geometry1 = "banded-packed"
+geometry2 = "banded-packed"
+differentiation0 = 0
+differentiation1 = 0
+differentiation2 = 2
+mass = 1
+
+[AngularKineticEnergy]
+classname = "CoupledSphericalKineticEnergyEvaluator"
+geometry0 = "Diagonal"
+geometry1 = "banded-packed"
+geometry2 = "banded-packed"
+angular_rank = 0
+radial_rank1 = 1
+radial_rank2 = 2
+mass = 1
+
+[CoulombPotential]
+classname = "CoupledSphericalCoulombPotential"
+geometry0 = "Diagonal"
+geometry1 = "banded-packed"
+geometry2 = "banded-packed"
+radial_rank1 = 1
+radial_rank2 = 2
+z = {z!r}
+
+[ElectronicCouplingPotential]
+classname = "CustomPotentialEvaluationR12"
+geometry0 = "SelectionRule_R12"
+geometry1 = "banded-packed"
+geometry2 = "banded-nonhermitian"
+angular_rank = 0
+radial_rank1 = 1
+radial_rank2 = 2
+"""

@@ -113,3 +113,23 @@ class FakePotential:
 
     def GetTimeScaling(self, t):
         return self.factor
+
+
+def helium_problem(lmax=1, nbsplines=16, rmax=15.0, **kw):
+    import pyprop_gb300 as pp
+    from pyprop_gb300.workloads import helium
+    return pp.Problem(pp.LoadString(helium(lmax=lmax, nbsplines=nbsplines, rmax=rmax, **kw)))
+
+
+def helium_dense(prob):
+    """Dense H and S (x) S of a two-electron problem from the oracle's rank-3 storage loops."""
+    from oracle.operators import Overlap, TermOracle, dense_operator
+    bp = prob.Propagator.BasePropagator
+    repr_ = prob.psi.GetRepresentation()
+    shape = repr_.GetFullShape()
+    terms = [TermOracle("_".join(g.GetStorageId() for g in pot.GeometryList), pot.PotentialData,
+                        [g.GetBasisPairs() for g in pot.GeometryList], None, None, repr_.kb, shape=shape)
+             for pot in bp.PotentialList]
+    H = dense_operator(terms, [1.0] * len(terms), shape[0] * shape[1], shape[2])
+    S = Overlap(repr_.overlap_rows).S
+    return H, np.kron(np.eye(shape[0]), np.kron(S, S)), terms

@@ -57,3 +57,33 @@ def test_rank3_matvec_fp64_fp32(gpu, storage):
         op.matvec(np.array([0.0, 0.9 + 0.1j]), src, dst)
         got = dst.to(torch.complex128).cpu().numpy()
         assert relerr(got, ref) < tol, (storage, prec, relerr(got, ref))
+
+
+def test_long_fibre_matvec_uses_wide_tiles(gpu):
+    """N >= 1024 takes the 128-row bulk-copy tiles (and a partial last tile): parity with the oracle."""
+    import torch
+    from oracle.operators import TermOracle
+    from pyprop_gb300.gpu import Context, DeviceOperator
+    nang, N, kb = 5, 1100, 6
+    ctx = Context.get()
+    terms = [random_storage_term("Diag", "BandNH", nang, N, kb, seed=31),
+             random_storage_term("Simp", "BandNH", nang, N, kb, seed=32)]
+    rng = np.random.default_rng(33)
+    x = rng.standard_normal((nang, N)) + 1j * rng.standard_normal((nang, N))
+    ref = np.zeros_like(x)
+    for (sid, pot, pairs), s in zip(terms, (1.0, 0.3 - 0.4j)):
+        TermOracle(sid, pot, pairs, nang, N, kb).multiply(x, ref, s)
+    for prec, dt, tol in [(nat.PG_FP64, torch.complex128, 1e-13), (nat.PG_FP32, torch.complex64, 2e-5)]:
+        op = DeviceOperator(ctx, [FakePotential(*t) for t in terms], (nang, N), kb, prec)
+        tuned, times = op.variant()
+        assert tuned in (1, 2, 3) and all(t > 0 for t in times)
+        src = torch.as_tensor(x, device="cuda").to(dt)
+        outs = []
+        for v in (1, 2, 3):  # every kernel variant, then back to the tuned one
+            op.variant(v)
+            dst = torch.zeros((nang, N), dtype=dt, device="cuda")
+            op.matvec(np.array([0.0, 1.0, 0.3 - 0.4j]), src, dst)
+            outs.append(dst.to(torch.complex128).cpu().numpy())
+            assert relerr(outs[-1], ref) < tol, (prec, v)
+        assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+        op.variant(tuned)
