@@ -123,13 +123,14 @@ def measured_peaks():
 
 def _time_launches(torch, fn, flush, reps):
     """Average device time of fn() (CUDA events on the launching stream, L2 flushed before
-    every launch, 3 untimed launches first)."""
+    every launch unless flush is None, 3 untimed launches first)."""
     stream = torch.cuda.current_stream()
     for _ in range(3):
         fn()
     total = 0.0
     for _ in range(reps):
-        flush.fill_(1.0)
+        if flush is not None:
+            flush.fill_(1.0)
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s.record(stream)
         fn()
@@ -173,8 +174,10 @@ def time_block_solve(torch, prob, flush, reps=50):
 LARGE = dict(lmax=300, nbsplines=2000, rmax=2000.0)
 
 
-MATVEC_KERNELS = {1: "op_matvec_bulk_kernel<float,6,64>", 2: "op_matvec_bulk_kernel<float,6,128>",
-                  3: "op_matvec_kernel<float,6>"}
+MATVEC_KERNELS = {1: "op_matvec_bulk_kernel<float,6,64,false>", 2: "op_matvec_bulk_kernel<float,6,128,false>",
+                  3: "op_matvec_kernel<float,6>", 4: "op_matvec_bulk_kernel<float,6,64,true> (TMA)",
+                  5: "op_matvec_tma_persistent_kernel<float,6>", 6: "op_matvec_bulk_kernel<float,6,64,rowmajor>",
+                  7: "op_matvec_bulk_kernel<float,6,64,true,2> (TMA, 2-block groups)"}
 
 
 def time_large_matvec(torch, flush, reps=20):
@@ -191,7 +194,18 @@ def time_large_matvec(torch, flush, reps=20):
     src = torch.randn((nang, N), dtype=torch.complex64, device="cuda")
     dst = torch.empty_like(src)
     sc = op.scales(5.0)
-    avg = _time_launches(torch, lambda: op.matvec(sc, src, dst), flush, reps)
+    # the operator (197 MB) is larger than L2: no flush; the launches run back to back between
+    # one pair of events (steady-state duration per launch)
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        op.matvec(sc, src, dst)
+    s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s_ev.record(stream)
+    for _ in range(reps):
+        op.matvec(sc, src, dst)
+    e_ev.record(stream)
+    e_ev.synchronize()
+    avg = s_ev.elapsed_time(e_ev) * 1e-3 / reps
     nbytes = 8 * (op.stored_elements() + 2 * nang * N)
     variant = op.variant()
     del op, bp, prob
@@ -335,7 +349,7 @@ def run_ours(args):
             "roofline_matvec_hbm": {"bound": "hbm", "achieved": bytes_lg / avg_lg / 1e9, "peak": peak, "unit": "GB/s",
                                     "frac": bytes_lg / avg_lg / 1e9 / peak, "kernel": MATVEC_KERNELS[variant_lg[0]],
                                     "avg_launch_us": 1e6 * avg_lg, "algorithmic_bytes": bytes_lg,
-                                    "workload": "hydrogen lmax 300, 2000 B-splines (operator > L2)",
+                                    "workload": "hydrogen lmax 300, 2000 B-splines (operator > L2; 20 launches back to back)",
                                     "variant": variant_lg[0], "tuning_us": variant_lg[1]},
             "cpu_baseline": cpu,
             "ensemble": ens,

@@ -236,6 +236,15 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
                  : "memory");
 }
 
+// 3-D tensor copy of one box into shared memory, completing on the mbarrier
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                            unsigned long long *bar)
+{
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n"
+                 ::"r"(smem_u32(dst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+                 : "memory");
+}
+
 // bounded wait: gives up after `limit` polls and reports through *err
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, int *err)
 {
@@ -245,16 +254,18 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
     return false;
 }
 
-template <typename R, int KB, int BT>
+template <typename R, int KB, int BT, int MODE, int GE>
 __global__ void __launch_bounds__(BT) op_matvec_bulk_kernel(OpDev op, pg_scales scales, const cxd *__restrict__ scales_dev,
                                                             const cx<R> *__restrict__ src, cx<R> *__restrict__ dst,
-                                                            int accumulate, int *err)
+                                                            int accumulate, int *err,
+                                                            const __grid_constant__ CUtensorMap tmap,
+                                                            const cx<R> *__restrict__ rowmajor)
 {
     constexpr int B = 2 * KB + 1;
     extern __shared__ __align__(128) unsigned char mv_smem[];
     unsigned long long *bar = (unsigned long long *)mv_smem;
-    cx<R> *bs = (cx<R> *)(mv_smem + 128);            // [BMAXE][B][BT]
-    cx<R> *xs = bs + (size_t)BMAXE * B * BT;          // [BMAXE][BT + 2KB]
+    cx<R> *bs = (cx<R> *)(mv_smem + 128);            // [GE][B][BT]
+    cx<R> *xs = bs + (size_t)GE * B * BT;          // [GE][BT + 2KB]
     const int r = blockIdx.y;
     const int i0 = blockIdx.x * BT;
     const int t = threadIdx.x;
@@ -271,9 +282,31 @@ __global__ void __launch_bounds__(BT) op_matvec_bulk_kernel(OpDev op, pg_scales 
     cx<R> acc = mk<R>((R)0, (R)0);
     const int e_begin = op.row_ptr[r], e_end = op.row_ptr[r + 1];
     unsigned phase = 0;
-    for (int e0 = e_begin; e0 < e_end; e0 += BMAXE) {
-        const int ne = min(BMAXE, e_end - e0);
-        if (t < 32) {
+    for (int e0 = e_begin; e0 < e_end; e0 += GE) {
+        const int ne = min(GE, e_end - e0);
+        if (MODE == 2) {
+            // row-major band copy [band][ld][B]: one contiguous bulk copy per entry (the rows up
+            // to the band's padded end ld, so the last tile stays inside its band)
+            const int rows = min(BT, ld - i0);
+            const unsigned bytes = (unsigned)(rows * B * sizeof(cx<R>));
+            if (t < 32) {
+                if (t == 0) mbar_arrive_expect_tx(bar, bytes * (unsigned)ne);
+                __syncwarp();
+                if (t < ne)
+                    bulk_g2s(bs + (size_t)t * B * BT, rowmajor + ((size_t)op.ent_band[e0 + t] * ld + i0) * B, bytes, bar);
+            }
+        } else if (MODE == 1) {
+            // one tensor copy per entry: the box [B diagonals][BT rows] of band ent_band (the
+            // box is always full: rows past the band's end read as zero)
+            if (t < 32) {
+                if (t == 0) mbar_arrive_expect_tx(bar, (unsigned)(ne * B * BT * sizeof(cx<R>)));
+                __syncwarp();
+                if (t < ne) {
+                    const int x0 = (sizeof(R) == 8 ? 2 : 1) * i0;
+                    tma_load_3d(bs + (size_t)t * B * BT, &tmap, x0, 0, op.ent_band[e0 + t], bar);
+                }
+            }
+        } else if (t < 32) {
             // lane 0 announces the bytes, then the 32 lanes of warp 0 issue the slab copies
             if (t == 0) mbar_arrive_expect_tx(bar, slab_bytes * (unsigned)(ne * B));
             __syncwarp();
@@ -305,7 +338,7 @@ __global__ void __launch_bounds__(BT) op_matvec_bulk_kernel(OpDev op, pg_scales 
                 const cx<R> *xb = xs + q * (BT + 2 * KB) + t;
                 cx<R> tq = mk<R>((R)0, (R)0);
 #pragma unroll
-                for (int d = 0; d < B; ++d) cfma(tq, Vb[d * BT + t], xb[d]);
+                for (int d = 0; d < B; ++d) cfma(tq, MODE == 2 ? Vb[t * B + d] : Vb[d * BT + t], xb[d]);
                 const int slot = op.ent_slot[e0 + q];
                 const cx<R> sc = scales_dev ? cvt<R>(scales_dev[slot]) : cvt<R>(scales.s[slot]);
                 cfma(acc, sc, tq);
@@ -320,21 +353,180 @@ __global__ void __launch_bounds__(BT) op_matvec_bulk_kernel(OpDev op, pg_scales 
     }
 }
 
-template <typename R, int KB, int BT>
+// ------------------------------------------------------------------------------------
+// persistent TMA variant: each CTA walks tiles (64 rows of one angular row) with a stride of
+// the grid, the next unit's band boxes (TMA) and source halo (cp.async, zero-filled outside
+// the fibre) in flight in one shared-memory stage while the current unit is computed from the
+// other. A unit is a tile's group of up to BMAXE entries.
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async_8(void *smem, const void *gmem, bool valid)
+{
+    const unsigned s = smem_u32(smem);
+    const int n = valid ? 8 : 0;  // source size 0: the 8 bytes are zero-filled
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_16z(void *smem, const void *gmem, bool valid)
+{
+    const unsigned s = smem_u32(smem);
+    const int n = valid ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_mv() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_mv(int pending)
+{
+    if (pending) asm volatile("cp.async.wait_group 1;\n" ::);
+    else asm volatile("cp.async.wait_group 0;\n" ::);
+}
+
+template <typename R, int KB>
+__global__ void __launch_bounds__(64) op_matvec_tma_persistent_kernel(OpDev op, pg_scales scales,
+                                                                       const cxd *__restrict__ scales_dev,
+                                                                       const cx<R> *__restrict__ src,
+                                                                       cx<R> *__restrict__ dst, int accumulate,
+                                                                       int *err, const __grid_constant__ CUtensorMap tmap)
+{
+    constexpr int BT = 64, B = 2 * KB + 1, XW = BT + 2 * KB;
+    extern __shared__ __align__(128) unsigned char mv_smem[];
+    unsigned long long *bar = (unsigned long long *)mv_smem;          // [2]
+    cx<R> *bs = (cx<R> *)(mv_smem + 128);                             // [2][BMAXE][B][BT]
+    cx<R> *xs = bs + (size_t)2 * BMAXE * B * BT;                      // [2][BMAXE][XW]
+    const int t = threadIdx.x;
+    const int N = op.N;
+    const int tiles_i = (N + BT - 1) / BT;
+    const long long ntiles = (long long)op.nrows * tiles_i;
+    if (t == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    // unit iterator: (tile u, group g)
+    auto ngroups = [&](long long u) {
+        const int r = (int)(u / tiles_i);
+        const int ne = op.row_ptr[r + 1] - op.row_ptr[r];
+        return max(1, (ne + BMAXE - 1) / BMAXE);
+    };
+    auto issue = [&](long long u, int g, int stage) {
+        const int r = (int)(u / tiles_i), i0 = (int)(u % tiles_i) * BT;
+        const int e0 = op.row_ptr[r] + g * BMAXE;
+        const int ne = max(0, min(BMAXE, op.row_ptr[r + 1] - e0));
+        if (t < 32) {
+            if (t == 0) mbar_arrive_expect_tx(&bar[stage], (unsigned)(ne * B * BT * sizeof(cx<R>)));
+            __syncwarp();
+            if (t < ne) {
+                const int x0 = (sizeof(R) == 8 ? 2 : 1) * i0;
+                tma_load_3d(bs + ((size_t)stage * BMAXE + t) * B * BT, &tmap, x0, 0, op.ent_band[e0 + t], &bar[stage]);
+            }
+        }
+        for (int q = 0; q < ne; ++q) {
+            const cx<R> *x = src + (size_t)op.ent_col[e0 + q] * N;
+            cx<R> *xd = xs + ((size_t)stage * BMAXE + q) * XW;
+            for (int u2 = t; u2 < XW; u2 += BT) {
+                const int j = i0 - KB + u2;
+                const bool ok = j >= 0 && j < N;
+                if (sizeof(cx<R>) == 8) cp_async_8(xd + u2, ok ? (const void *)(x + j) : (const void *)x, ok);
+                else cp_async_16z(xd + u2, ok ? (const void *)(x + j) : (const void *)x, ok);
+            }
+        }
+        cp_async_commit_mv();
+    };
+    long long u = blockIdx.x;
+    int g = 0;
+    if (u >= ntiles) return;
+    unsigned phase[2] = {0u, 0u};
+    issue(u, 0, 0);
+    int stage = 0;
+    cx<R> acc = mk<R>((R)0, (R)0);
+    for (;;) {
+        // the unit after this one
+        long long un = u;
+        int gn = g + 1;
+        if (gn >= ngroups(u)) {
+            un = u + gridDim.x;
+            gn = 0;
+        }
+        const bool more = un < ntiles;
+        if (more) issue(un, gn, stage ^ 1);
+        const bool ok = mbar_wait_bounded(&bar[stage], phase[stage], err);
+        cp_async_wait_mv(more ? 1 : 0);
+        if (__syncthreads_or(ok ? 0 : 1)) {
+            // give up uniformly: wait (bounded) for the copies still in flight, then leave
+            if (!ok) mbar_wait_bounded(&bar[stage], phase[stage], err);
+            if (more) mbar_wait_bounded(&bar[stage ^ 1], phase[stage ^ 1], err);
+            cp_async_wait_mv(0);
+            return;
+        }
+        phase[stage] ^= 1u;
+        const int r = (int)(u / tiles_i), i0 = (int)(u % tiles_i) * BT;
+        const int e0 = op.row_ptr[r] + g * BMAXE;
+        const int ne = max(0, min(BMAXE, op.row_ptr[r + 1] - e0));
+        const int cnt = min(BT, N - i0);
+        if (t < cnt) {
+            for (int q = 0; q < ne; ++q) {
+                const cx<R> *Vb = bs + ((size_t)stage * BMAXE + q) * B * BT;
+                const cx<R> *xb = xs + ((size_t)stage * BMAXE + q) * XW + t;
+                cx<R> tq = mk<R>((R)0, (R)0);
+#pragma unroll
+                for (int d = 0; d < B; ++d) cfma(tq, Vb[d * BT + t], xb[d]);
+                const int slot = op.ent_slot[e0 + q];
+                const cx<R> sc = scales_dev ? cvt<R>(scales_dev[slot]) : cvt<R>(scales.s[slot]);
+                cfma(acc, sc, tq);
+            }
+        }
+        if (gn == 0) {  // last group of this tile: store
+            if (t < cnt) {
+                const size_t o = (size_t)r * N + i0 + t;
+                dst[o] = accumulate ? acc + dst[o] : acc;
+            }
+            acc = mk<R>((R)0, (R)0);
+        }
+        __syncthreads();  // this stage is refilled two units from now
+        if (!more) break;
+        u = un;
+        g = gn;
+        stage ^= 1;
+    }
+}
+
+template <typename R, int KB>
+static int launch_tma_persistent(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
+                                 int accumulate)
+{
+    constexpr int B = 2 * KB + 1, BT = 64;
+    const size_t smem = 128 + sizeof(cx<R>) * ((size_t)2 * BMAXE * B * BT + (size_t)2 * BMAXE * (BT + 2 * KB));
+    static bool configured = false;
+    if (!configured) {
+        PG_CUDA_TRY(cudaFuncSetAttribute(op_matvec_tma_persistent_kernel<R, KB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = true;
+    }
+    const long long ntiles = (long long)op->nrows * ((op->N + BT - 1) / BT);
+    int per_sm = 1;
+    PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, op_matvec_tma_persistent_kernel<R, KB>, BT, smem));
+    const long long grid = std::max<long long>(1, std::min<long long>(ntiles, (long long)std::max(1, per_sm) *
+                                                                                  std::max(1, op->ctx->num_sms)));
+    op_matvec_tma_persistent_kernel<R, KB><<<(unsigned)grid, BT, smem, op->ctx->stream>>>(
+        op->dev(), scales, scales_dev, (const cx<R> *)src, (cx<R> *)dst, accumulate, op->ctx->d_err, op->tmap);
+    op->ctx->launches++;
+    return pg_check_launch(op->ctx);
+}
+
+template <typename R, int KB, int BT, int MODE, int GE = BMAXE>
 static int launch_bulk_bt(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
                           int accumulate)
 {
     constexpr int B = 2 * KB + 1;
-    const size_t smem = 128 + sizeof(cx<R>) * ((size_t)BMAXE * B * BT + (size_t)BMAXE * (BT + 2 * KB));
+    const size_t smem = 128 + sizeof(cx<R>) * ((size_t)GE * B * BT + (size_t)GE * (BT + 2 * KB));
     static bool configured = false;
     if (!configured) {
-        PG_CUDA_TRY(cudaFuncSetAttribute(op_matvec_bulk_kernel<R, KB, BT>,
+        PG_CUDA_TRY(cudaFuncSetAttribute(op_matvec_bulk_kernel<R, KB, BT, MODE, GE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = true;
     }
     dim3 grid((op->N + BT - 1) / BT, op->nrows);
-    op_matvec_bulk_kernel<R, KB, BT><<<grid, BT, smem, op->ctx->stream>>>(
-        op->dev(), scales, scales_dev, (const cx<R> *)src, (cx<R> *)dst, accumulate, op->ctx->d_err);
+    op_matvec_bulk_kernel<R, KB, BT, MODE, GE><<<grid, BT, smem, op->ctx->stream>>>(
+        op->dev(), scales, scales_dev, (const cx<R> *)src, (cx<R> *)dst, accumulate, op->ctx->d_err, op->tmap,
+        (const cx<R> *)op->d_bands_rm);
     op->ctx->launches++;
     return pg_check_launch(op->ctx);
 }
@@ -344,8 +536,12 @@ template <typename R, int KB>
 static int launch_bulk(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
                        int accumulate)
 {
-    if (op->variant == 2) return launch_bulk_bt<R, KB, 128>(op, scales, scales_dev, src, dst, accumulate);
-    return launch_bulk_bt<R, KB, 64>(op, scales, scales_dev, src, dst, accumulate);
+    if (op->variant == 2) return launch_bulk_bt<R, KB, 128, 0>(op, scales, scales_dev, src, dst, accumulate);
+    if (op->variant == 4 && op->has_tmap) return launch_bulk_bt<R, KB, 64, 1>(op, scales, scales_dev, src, dst, accumulate);
+    if (op->variant == 5 && op->has_tmap) return launch_tma_persistent<R, KB>(op, scales, scales_dev, src, dst, accumulate);
+    if (op->variant == 6 && op->d_bands_rm) return launch_bulk_bt<R, KB, 64, 2>(op, scales, scales_dev, src, dst, accumulate);
+    if (op->variant == 7 && op->has_tmap) return launch_bulk_bt<R, KB, 64, 1, 2>(op, scales, scales_dev, src, dst, accumulate);
+    return launch_bulk_bt<R, KB, 64, 0>(op, scales, scales_dev, src, dst, accumulate);
 }
 
 template <typename R>
@@ -437,6 +633,7 @@ extern "C" int pg_op_destroy(pg_op *op)
     cudaFree(op->d_ent_band);
     cudaFree(op->d_ent_slot);
     cudaFree(op->d_bands);
+    cudaFree(op->d_bands_rm);
     cudaFree(op->d_drow_ptr);
     cudaFree(op->d_dent_col);
     cudaFree(op->d_dent_mat);
@@ -614,6 +811,65 @@ static void expand_outer(const HostTerm &t, const std::vector<int> &shape, std::
 
 static int autotune(pg_op *op);
 
+// Row-major copy of the bands, [band][ld][2kb+1] (transposed on the device from [band][2kb+1][ld]),
+// for the variant that loads each tile's band block as one contiguous bulk copy.
+template <typename R>
+__global__ void bands_rowmajor_kernel(const cx<R> *__restrict__ dm, cx<R> *__restrict__ rm, int B, int ld, long long n)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const long long band = e / ((long long)B * ld);
+        const long long rem = e - band * B * ld;
+        const int i = (int)(rem / B), d = (int)(rem - (long long)i * B);
+        rm[e] = dm[(band * B + d) * ld + i];
+    }
+}
+
+static int make_rowmajor_bands(pg_op *op)
+{
+    if (op->d_bands_rm || op->nbands == 0) return PG_OK;
+    const size_t esz = op->precision == PG_FP64 ? sizeof(cxd) : sizeof(cxf);
+    const long long n = (long long)op->nbands * op->b * op->ld;
+    if (cudaMalloc(&op->d_bands_rm, esz * n) != cudaSuccess) {  // no room: the variant is not offered
+        cudaGetLastError();
+        op->d_bands_rm = nullptr;
+        return PG_OK;
+    }
+    const int nb = (int)std::min<long long>((n + 255) / 256, 4096);
+    if (op->precision == PG_FP64)
+        bands_rowmajor_kernel<double><<<nb, 256, 0, op->ctx->stream>>>((const cxd *)op->d_bands, (cxd *)op->d_bands_rm,
+                                                                      op->b, op->ld, n);
+    else
+        bands_rowmajor_kernel<float><<<nb, 256, 0, op->ctx->stream>>>((const cxf *)op->d_bands, (cxf *)op->d_bands_rm,
+                                                                     op->b, op->ld, n);
+    return pg_check_launch(op->ctx);
+}
+
+// Tensor map of the band array [nbands][2kb+1][ld] (complex64 as 8-byte elements, complex128
+// as pairs of doubles) with a box of one band's 2kb+1 diagonals x 64 rows, for the TMA variant
+// of the bulk matvec. Without the driver entry point the variant is simply not offered.
+static void make_band_tensor_map(pg_op *op)
+{
+    typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    op->has_tmap = false;
+    if (op->kb != 6 || op->nbands == 0 || !op->d_bands) return;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+        return;
+    const int per = op->precision == PG_FP64 ? 2 : 1;  // 8-byte elements per complex
+    const cuuint64_t dims[3] = {(cuuint64_t)op->ld * per, (cuuint64_t)op->b, (cuuint64_t)op->nbands};
+    const cuuint64_t strides[2] = {(cuuint64_t)op->ld * per * 8, (cuuint64_t)op->ld * per * 8 * op->b};
+    const cuuint32_t box[3] = {(cuuint32_t)(64 * per), (cuuint32_t)op->b, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = ((EncodeTiled)fn)(&op->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, op->d_bands, dims, strides, box, estr,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    op->has_tmap = (r == CUDA_SUCCESS);
+}
+
 extern "C" int pg_op_finalize(pg_op *op)
 {
     if (!op) return PG_ERR_ARG;
@@ -777,6 +1033,7 @@ extern "C" int pg_op_finalize(pg_op *op)
         }
     }
     op->finalized = true;
+    make_band_tensor_map(op);
     return autotune(op);
 }
 
@@ -806,7 +1063,10 @@ static int autotune(pg_op *op)
     int code = PG_OK;
     float best = 1e30f;
     int best_v = 1;
-    for (int v = 1; v <= 3 && code == PG_OK; ++v) {
+    code = make_rowmajor_bands(op);
+    for (int v = 1; v <= 7 && code == PG_OK; ++v) {
+        if ((v == 4 || v == 5 || v == 7) && !op->has_tmap) continue;
+        if (v == 6 && !op->d_bands_rm) continue;
         op->variant = v;
         for (int k = 0; k < 2 && code == PG_OK; ++k) code = pg_op_matvec_dev(op, sc, nullptr, x, y, 0, nullptr, nullptr);
         if (code != PG_OK) break;
@@ -824,6 +1084,10 @@ static int autotune(pg_op *op)
     }
     op->ctx->launches = launches;  // tuning launches are not the caller's work
     op->variant = best_v;
+    if (best_v != 6 && op->d_bands_rm) {  // the row-major copy is kept only when it is used
+        cudaFree(op->d_bands_rm);
+        op->d_bands_rm = nullptr;
+    }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     cudaFree(x);
@@ -836,11 +1100,17 @@ static int autotune(pg_op *op)
 extern "C" int pg_op_variant(pg_op *op, int variant, int *current, float *times_us)
 {
     if (!op || !op->finalized) return PG_ERR_STATE;
-    if (variant >= 1 && variant <= 3) op->variant = variant;
+    if ((variant >= 1 && variant <= 3) || ((variant == 4 || variant == 5 || variant == 7) && op->has_tmap))
+        op->variant = variant;
+    else if (variant == 6) {
+        PG_TRY(make_rowmajor_bands(op));
+        if (!op->d_bands_rm) return PG_ERR_ARG;
+        op->variant = 6;
+    }
     else if (variant >= 0) return PG_ERR_ARG;
     if (current) *current = op->variant;
     if (times_us)
-        for (int k = 0; k < 4; ++k) times_us[k] = op->variant_us[k];
+        for (int k = 0; k < 8; ++k) times_us[k] = op->variant_us[k];
     return PG_OK;
 }
 

@@ -157,11 +157,11 @@ class DeviceOperator:
         return int(self.lib.pg_op_stored_elements(self.h))
 
     def variant(self, force=-1):
-        """(variant in use, tuning times in us per variant 1..3); force 1..3 selects one."""
+        """(variant in use, tuning times in us per variant 1..7; 0 = not offered); force selects one."""
         cur = C.c_int(0)
-        times = (C.c_float * 4)()
+        times = (C.c_float * 8)()
         check(self.lib.pg_op_variant(self.h, int(force), C.byref(cur), times), "pg_op_variant")
-        return cur.value, [float(times[k]) for k in range(1, 4)]
+        return cur.value, [float(times[k]) for k in range(1, 8)]
 
     def matvec(self, scales, src, dst, accumulate=False):
         sc = np.ascontiguousarray(scales, dtype=np.complex128)

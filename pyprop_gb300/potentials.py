@@ -257,5 +257,26 @@ class CustomPotentialEvaluationR12(CoupledPotentialBase):
         return out
 
 
-for _cls in (CoupledSphericalCoulombPotential, CoupledSphericalKineticEnergyEvaluator, CustomPotentialEvaluationR12):
+class CustomPotential_LaserLength(CoupledPotentialBase):
+    """Length-gauge laser coupling of both electrons on ``SelectionRule_LinearPolarizedField``
+    pairs, I1 r1 + I2 r2 (coupledlength.cpp:9-124); the field strength comes from the
+    section's time function."""
+
+    def GetPotentialValue(self, pos):
+        from .spherical import laser_length_factors
+        r1, r2 = pos[self.radial_rank1], pos[self.radial_rank2]
+        shape = np.broadcast(*pos).shape
+        out = np.zeros(shape)
+        for p, (left, right) in enumerate(self._left_right()):
+            I1, I2 = laser_length_factors(left, right)
+            if I1 == 0.0 and I2 == 0.0:
+                continue
+            sl = [slice(None)] * len(shape)
+            sl[self.angular_rank] = p
+            out[tuple(sl)] = np.squeeze(np.broadcast_to(I1 * r1 + I2 * r2, shape)[tuple(sl)])
+        return out
+
+
+for _cls in (CoupledSphericalCoulombPotential, CoupledSphericalKineticEnergyEvaluator, CustomPotentialEvaluationR12,
+             CustomPotential_LaserLength):
     POTENTIAL_CLASSES[_cls.__name__] = _cls

@@ -215,3 +215,41 @@ def r12_multipoles(left, right):
     if left.L != right.L or left.M != right.M:
         return range(0)
     return range(max(abs(right.l1 - left.l1), abs(right.l2 - left.l2)), min(right.l1 + left.l1, right.l2 + left.l2) + 1)
+
+
+def rule_linear_polarized_field(a, b):
+    """``CoupledSphericalSelectionRuleLinearPolarizedField`` (coupledsphericalselectionrule.h:
+    333-355): L changes by one, M kept, one electron's l changes by one, the other's is kept."""
+    if abs(a.L - b.L) != 1 or a.M != b.M:
+        return False
+    return (abs(a.l1 - b.l1) == 1 and a.l2 == b.l2) or (abs(a.l2 - b.l2) == 1 and a.l1 == b.l1)
+
+
+def laser_length_factors(left, right):
+    """(I1, I2): the angular factors of the length-gauge coupling r1 I1 + r2 I2 between coupled
+    states (examples/tensor/helium_stabilization/coupledlength.cpp:44-124). As in the reference,
+    the single-electron factor is <l m|Y_10|l' m> (cos(theta) = sqrt(4 pi / 3) Y_10) with its
+    sign convention (the m >= 0 Condon-Shortley phase divided out)."""
+    if abs(left.L - right.L) != 1 or left.M != right.M:
+        return 0.0, 0.0
+    L, M, l1, l2 = left.L, left.M, left.l1, left.l2
+    Lp, l1p, l2p = right.L, right.l1, right.l2
+
+    def coef(l, lp):
+        return math.sqrt((2 * l + 1.0) * (2 * lp + 1.0) / (12 * math.pi))
+
+    def cs(m):
+        return 1.0 if m < 0 else (-1.0) ** m
+
+    I1 = I2 = 0.0
+    stop = max(l1, l1p, l2, l2p)
+    for m1 in range(-stop, stop + 1):
+        m2 = M - m1
+        if abs(m1) > l1 or abs(m1) > l1p or abs(m2) > l2 or abs(m2) > l2p:
+            continue
+        base = clebsch_gordan(l1, l2, m1, m2, L, M) * clebsch_gordan(l1p, l2p, m1, m2, Lp, M)
+        if base == 0.0:
+            continue
+        I1 += base * coef(l1, l1p) * clebsch_gordan(l1, l1p, 0, 0, 1, 0) * clebsch_gordan(l1, l1p, -m1, m1, 1, 0) / cs(m1)
+        I2 += base * coef(l2, l2p) * clebsch_gordan(l2, l2p, 0, 0, 1, 0) * clebsch_gordan(l2, l2p, -m2, m2, 1, 0) / cs(m2)
+    return I1, I2

@@ -177,7 +177,7 @@ class CoupledSphericalRankBasis:
         self.size = self.basis.size
 
     def GetGeometryInfo(self, name):
-        from .spherical import rule_diagonal, rule_r12_old
+        from .spherical import rule_diagonal, rule_linear_polarized_field, rule_r12_old
         geom = name.lower().strip()
         n = self.size
         if geom == "identity":
@@ -188,6 +188,8 @@ class CoupledSphericalRankBasis:
             return GeometryInfo("Dense", [(i, j) for i in range(n) for j in range(n)], False)
         if geom == "selectionrule_r12":
             return GeometryInfo("Simp", self.basis.pairs(rule_r12_old), False)
+        if geom == "selectionrule_linearpolarizedfield":
+            return GeometryInfo("Simp", self.basis.pairs(rule_linear_polarized_field), False)
         raise ValueError("Geometry '%s' not supported by the coupled spherical rank" % name)
 
     def grid(self, geometry):

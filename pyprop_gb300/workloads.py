@@ -133,13 +133,34 @@ time_function = LaserFunctionSimpleLength
 
 
 def helium(lmax=2, L=(0,), nbsplines=20, rmax=20.0, order=7, quad_order_additional=10, z=2.0,
-           propagator="PamPropagatorGPU", precision="fp64", timestep=0.01, duration=1.0, krylov_basis_size=20):
+           propagator="PamPropagatorGPU", precision="fp64", timestep=0.01, duration=1.0, krylov_basis_size=20,
+           amplitude=0.0, frequency=1.0, pulse_duration=10.0):
     """Two-electron (helium-like) model in the layout of
-    examples/tensor/helium_stabilization/config.ini:1-124: coupled spherical harmonics
+    examples/tensor/helium_stabilization/config.ini:1-188: coupled spherical harmonics
     (``DefaultCoupledIndexIterator(lmax, L, M=0)``) x B-splines x B-splines, radial kinetic
-    energy of each electron, angular kinetic energy, nuclear attraction -z/r1 - z/r2 and the
-    electron-electron repulsion on ``SelectionRule_R12`` pairs. Field-free."""
+    energy of each electron, angular kinetic energy, nuclear attraction -z/r1 - z/r2, the
+    electron-electron repulsion on ``SelectionRule_R12`` pairs and, with amplitude != 0, the
+    length-gauge laser coupling on ``SelectionRule_LinearPolarizedField`` pairs with a sin^2
+    pulse (L must then hold neighbouring values)."""
     total = nbsplines - 3 if order == 7 else nbsplines - (order - 4)
+    laser_name = ', "LaserPotential"' if amplitude else ""
+    laser = f"""
+[PulseParameters]
+frequency = {frequency!r}
+amplitude = {amplitude!r}
+pulse_duration = {pulse_duration!r}
+
+[LaserPotential]
+base = "PulseParameters"
+classname = "CustomPotential_LaserLength"
+geometry0 = "SelectionRule_LinearPolarizedField"
+geometry1 = "banded-packed"
+geometry2 = "banded-packed"
+angular_rank = 0
+radial_rank1 = 1
+radial_rank2 = 2
+time_function = LaserFunctionLength
+""" if amplitude else ""
     rpart, xsize = exponential_linear_params_for(0.0, rmax, total, gamma=2.0, rpartition=min(10.0, rmax / 2))
     Ls = list(L)
     return f"""
@@ -173,7 +194,7 @@ type = InitialConditionType.Function
 function = lambda conf, x: 1.0 * (x[0] == 0)
 
 [Propagation]
-grid_potential_list = ["RadialKineticEnergy1", "RadialKineticEnergy2", "AngularKineticEnergy", "CoulombPotential", "ElectronicCouplingPotential"]
+grid_potential_list = ["RadialKineticEnergy1", "RadialKineticEnergy2", "AngularKineticEnergy", "CoulombPotential", "ElectronicCouplingPotential"{laser_name}]
 propagator = {propagator}
 base_propagator = BasisPropagatorGPU
 timestep = {timestep!r}
@@ -232,4 +253,4 @@ geometry2 = "banded-nonhermitian"
 angular_rank = 0
 radial_rank1 = 1
 radial_rank2 = 2
-"""
+{laser}"""

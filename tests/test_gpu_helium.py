@@ -67,3 +67,32 @@ def test_helium_ground_state_energy_and_pamp_propagation(gpu):
     ref = np.exp(-1j * e0 * dt * nsteps) * psi0.ravel() / np.sqrt(np.vdot(psi0.ravel(), S3 @ psi0.ravel()).real)
     assert relerr(out, ref) < 1e-9
     assert abs(prob.psi.GetNorm() - 1.0) < 1e-12
+
+
+def test_helium_in_a_laser_field_pamp_matches_dense_exponential(gpu):
+    """Time-dependent two-electron propagation (length-gauge coupling on
+    SelectionRule_LinearPolarizedField pairs): pAMP steps with H frozen at the step start
+    against exp(-i dt S^-1 H(t)) of the dense oracle operator."""
+    import torch
+    from oracle.operators import dense_operator
+    prob = helium_problem(lmax=1, nbsplines=12, rmax=12.0, L=(0, 1), amplitude=0.1, frequency=1.0,
+                          pulse_duration=2.0)
+    H, S3, terms = helium_dense(prob)
+    pots = prob.Propagator.BasePropagator.PotentialList
+    mats = [dense_operator([t], [1.0], terms[0].nang, terms[0].N) for t in terms]
+    prob.SetupStep(skipWavefunctionSetup=True)
+    shape = prob.psi.GetRepresentation().GetFullShape()
+    rng = np.random.default_rng(8)
+    psi = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    psi /= np.sqrt(np.vdot(psi.ravel(), S3 @ psi.ravel()).real)
+    prob.psi.GetData().copy_(torch.as_tensor(psi, device="cuda"))
+    Sinv = np.linalg.inv(S3)
+    ref = psi.ravel().copy()
+    t0, dt = 0.5, 0.01
+    for n in range(5):
+        t = t0 + n * dt
+        Ht = sum(pot.GetTimeScaling(t) * M for pot, M in zip(pots, mats))
+        ref = sl.expm(-1j * dt * Sinv @ Ht) @ ref
+        prob.Propagator.AdvanceStep(t, dt)
+    assert relerr(prob.psi.numpy().ravel(), ref) < 1e-10
+    assert abs(prob.psi.GetNorm() - 1.0) < 1e-11

@@ -48,3 +48,33 @@ def test_helium_partial_waves_converge_from_above():
     # the reference's own table (doc/test_and_benchmark.tex:41) gives -2.903586 at lmax = 5;
     # l <= 2 is within 1e-3 of it
     assert abs(e[2] - (-2.903586)) < 1e-3, e
+
+
+def test_laser_coupling_factors():
+    from pyprop_gb300.spherical import (CoupledIndex, DefaultCoupledIndexIterator, laser_length_factors,
+                                        rule_linear_polarized_field)
+    # s -> p of electron 1 with electron 2 in s: <Y00|Y10|Y10> = 1/sqrt(4 pi)
+    I1, I2 = laser_length_factors(CoupledIndex(0, 0, 0, 0), CoupledIndex(1, 0, 1, 0))
+    assert abs(I1 - 1 / np.sqrt(4 * np.pi)) < 1e-14 and I2 == 0.0
+    # the factors are evaluated on the selection rule's pairs only (the m-sum alone does not
+    # enforce the spectator electron's delta); there they are symmetric, and the spectator's
+    # factor vanishes
+    idx = list(DefaultCoupledIndexIterator(3, L=[0, 1, 2, 3]))
+    for a in idx:
+        for b in idx:
+            if not rule_linear_polarized_field(a, b):
+                continue
+            f, g = laser_length_factors(a, b), laser_length_factors(b, a)
+            assert abs(f[0] - g[0]) < 1e-14 and abs(f[1] - g[1]) < 1e-14
+            if a.l1 == b.l1:
+                assert abs(f[0]) < 1e-14
+            if a.l2 == b.l2:
+                assert abs(f[1]) < 1e-14
+
+
+def test_helium_with_laser_term_is_hermitian():
+    prob = helium_problem(lmax=1, nbsplines=12, rmax=12.0, L=(0, 1), amplitude=0.1, frequency=1.0, pulse_duration=2.0)
+    H, S3, terms = helium_dense(prob)
+    assert np.abs(H - H.conj().T).max() < 1e-12
+    pots = prob.Propagator.BasePropagator.PotentialList
+    assert len(pots) == 3 and [p.IsTimeDependent for p in pots] == [False, False, True]
