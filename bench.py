@@ -177,7 +177,8 @@ LARGE = dict(lmax=300, nbsplines=2000, rmax=2000.0)
 MATVEC_KERNELS = {1: "op_matvec_bulk_kernel<float,6,64,false>", 2: "op_matvec_bulk_kernel<float,6,128,false>",
                   3: "op_matvec_kernel<float,6>", 4: "op_matvec_bulk_kernel<float,6,64,true> (TMA)",
                   5: "op_matvec_tma_persistent_kernel<float,6>", 6: "op_matvec_bulk_kernel<float,6,64,rowmajor>",
-                  7: "op_matvec_bulk_kernel<float,6,64,true,2> (TMA, 2-block groups)"}
+                  7: "op_matvec_bulk_kernel<float,6,64,true,2> (TMA, 2-block groups)",
+                  8: "op_matvec_bulk_kernel<float,6,64,true,1> (TMA, 1-block groups)"}
 
 
 def time_large_matvec(torch, flush, reps=20):

@@ -138,10 +138,11 @@ int pg_op_finalize(pg_op *op);
  * the operator's own shape (1 bulk-copy staging with 64-row tiles, 2 with 128-row tiles,
  * 3 plain coalesced loads, 4 one TMA tensor copy per band block, 5 persistent CTAs with
  * double-buffered TMA stages - 4 and 5 when the driver offers tensor maps - and 6 one bulk
- * copy per block from a row-major copy of the bands, kept only when chosen; 7 variant 4 with
- * groups of two blocks) and keeps the fastest. variant 1..7 forces one (PG_ERR_ARG for 4, 5, 7
- * without a tensor map), variant < 0 only reads; current (optional) receives the variant in
- * use, times_us (optional, 8 floats) the tuning times per variant index (0: not measured). */
+ * copy per block from a row-major copy of the bands, kept only when chosen; 7 and 8 variant 4
+ * with groups of two or one block) and keeps the fastest. variant 1..8 forces one (PG_ERR_ARG
+ * for 4, 5, 7, 8 without a tensor map), variant < 0 only reads; current (optional) receives the
+ * variant in use, times_us (optional, 9 floats) the tuning times per variant index (0: not
+ * measured). */
 int pg_op_variant(pg_op *op, int variant, int *current, float *times_us);
 /* Number of complex band elements the operator stores (for roofline bookkeeping). */
 long long pg_op_stored_elements(const pg_op *op);

@@ -541,6 +541,7 @@ static int launch_bulk(pg_op *op, const pg_scales &scales, const cxd *scales_dev
     if (op->variant == 5 && op->has_tmap) return launch_tma_persistent<R, KB>(op, scales, scales_dev, src, dst, accumulate);
     if (op->variant == 6 && op->d_bands_rm) return launch_bulk_bt<R, KB, 64, 2>(op, scales, scales_dev, src, dst, accumulate);
     if (op->variant == 7 && op->has_tmap) return launch_bulk_bt<R, KB, 64, 1, 2>(op, scales, scales_dev, src, dst, accumulate);
+    if (op->variant == 8 && op->has_tmap) return launch_bulk_bt<R, KB, 64, 1, 1>(op, scales, scales_dev, src, dst, accumulate);
     return launch_bulk_bt<R, KB, 64, 0>(op, scales, scales_dev, src, dst, accumulate);
 }
 
@@ -1064,8 +1065,8 @@ static int autotune(pg_op *op)
     float best = 1e30f;
     int best_v = 1;
     code = make_rowmajor_bands(op);
-    for (int v = 1; v <= 7 && code == PG_OK; ++v) {
-        if ((v == 4 || v == 5 || v == 7) && !op->has_tmap) continue;
+    for (int v = 1; v <= 8 && code == PG_OK; ++v) {
+        if ((v == 4 || v == 5 || v >= 7) && !op->has_tmap) continue;
         if (v == 6 && !op->d_bands_rm) continue;
         op->variant = v;
         for (int k = 0; k < 2 && code == PG_OK; ++k) code = pg_op_matvec_dev(op, sc, nullptr, x, y, 0, nullptr, nullptr);
@@ -1100,7 +1101,7 @@ static int autotune(pg_op *op)
 extern "C" int pg_op_variant(pg_op *op, int variant, int *current, float *times_us)
 {
     if (!op || !op->finalized) return PG_ERR_STATE;
-    if ((variant >= 1 && variant <= 3) || ((variant == 4 || variant == 5 || variant == 7) && op->has_tmap))
+    if ((variant >= 1 && variant <= 3) || ((variant == 4 || variant == 5 || variant == 7 || variant == 8) && op->has_tmap))
         op->variant = variant;
     else if (variant == 6) {
         PG_TRY(make_rowmajor_bands(op));
@@ -1110,7 +1111,7 @@ extern "C" int pg_op_variant(pg_op *op, int variant, int *current, float *times_
     else if (variant >= 0) return PG_ERR_ARG;
     if (current) *current = op->variant;
     if (times_us)
-        for (int k = 0; k < 8; ++k) times_us[k] = op->variant_us[k];
+        for (int k = 0; k < 9; ++k) times_us[k] = op->variant_us[k];
     return PG_OK;
 }
 

@@ -139,8 +139,8 @@ struct pg_op {
     // matvec kernel variant, chosen by measurement at finalize (pg_op_set_variant overrides):
     // 1 bulk-copy 64-row tiles, 2 bulk-copy 128-row tiles, 3 plain loads (128 threads)
     int variant = 1;
-    float variant_us[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    // 7: variant 4 with groups of 2 band blocks (smaller shared memory, more CTAs per SM)
+    float variant_us[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    // 7, 8: variant 4 with groups of 2 or 1 band blocks (smaller shared memory, more CTAs per SM)
     void *d_bands_rm = nullptr;  // 6: row-major band copy [band][ld][2kb+1], one bulk copy per block
     // 4: bulk matvec with one TMA tensor copy per band block (when the tensor map exists);
     // 5: persistent CTAs, double-buffered TMA stages

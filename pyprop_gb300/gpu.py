@@ -157,11 +157,11 @@ class DeviceOperator:
         return int(self.lib.pg_op_stored_elements(self.h))
 
     def variant(self, force=-1):
-        """(variant in use, tuning times in us per variant 1..7; 0 = not offered); force selects one."""
+        """(variant in use, tuning times in us per variant 1..8; 0 = not offered); force selects one."""
         cur = C.c_int(0)
-        times = (C.c_float * 8)()
+        times = (C.c_float * 9)()
         check(self.lib.pg_op_variant(self.h, int(force), C.byref(cur), times), "pg_op_variant")
-        return cur.value, [float(times[k]) for k in range(1, 8)]
+        return cur.value, [float(times[k]) for k in range(1, 9)]
 
     def matvec(self, scales, src, dst, accumulate=False):
         sc = np.ascontiguousarray(scales, dtype=np.complex128)

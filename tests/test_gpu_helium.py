@@ -75,7 +75,8 @@ def test_helium_in_a_laser_field_pamp_matches_dense_exponential(gpu):
     against exp(-i dt S^-1 H(t)) of the dense oracle operator."""
     import torch
     from oracle.operators import dense_operator
-    prob = helium_problem(lmax=1, nbsplines=12, rmax=12.0, L=(0, 1), amplitude=0.1, frequency=1.0,
+    # the radial band (2k-1 = 13 diagonals) needs more than 12 B-splines on the device
+    prob = helium_problem(lmax=1, nbsplines=14, rmax=12.0, L=(0, 1), amplitude=0.1, frequency=1.0,
                           pulse_duration=2.0)
     H, S3, terms = helium_dense(prob)
     pots = prob.Propagator.BasePropagator.PotentialList

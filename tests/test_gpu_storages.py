@@ -76,9 +76,9 @@ def test_long_fibre_matvec_uses_wide_tiles(gpu):
     for prec, dt, tol in [(nat.PG_FP64, torch.complex128, 1e-13), (nat.PG_FP32, torch.complex64, 2e-5)]:
         op = DeviceOperator(ctx, [FakePotential(*t) for t in terms], (nang, N), kb, prec)
         tuned, times = op.variant()
-        assert tuned in (1, 2, 3, 4, 5, 6, 7) and all(t > 0 for t in times[:3])
-        # 4, 5, 7 (TMA) when the tensor map exists; 6 builds its row-major band copy on demand
-        variants = ((1, 2, 3, 4, 5, 7) if times[3] > 0 else (1, 2, 3)) + (6,)
+        assert tuned in range(1, 9) and all(t > 0 for t in times[:3])
+        # 4, 5, 7, 8 (TMA) when the tensor map exists; 6 builds its row-major band copy on demand
+        variants = ((1, 2, 3, 4, 5, 7, 8) if times[3] > 0 else (1, 2, 3)) + (6,)
         src = torch.as_tensor(x, device="cuda").to(dt)
         outs = []
         for v in variants:  # every kernel variant, then back to the tuned one
