@@ -179,6 +179,15 @@ int pg_overlap_create(pg_op *op, const double *overlap_rows, pg_banded **out);
 int pg_prec_blockdiag_create(pg_op *op, const double *overlap_rows, const double *cS,
                              const double *cH, const int *slots, const double *slot_weights,
                              int nslots, pg_banded **out);
+/* Two-electron radial preconditioner for rank-3 operators [Nang][N][N], Kronecker-factorized
+ * per angular channel: M_a = (cS S + cH h1_a) x (cS S + cH h2_a), h1_a, h2_a (host complex128
+ * rows [Nang][N][2k+1], layout of overlap_rows) the one-electron radial Hamiltonians of the
+ * channel's two electrons. Stands in for the reference's sparse direct / ILU block
+ * preconditioners (examples/tensor/helium_stabilization/preconditioner.py:77-244): it omits
+ * the electron-electron repulsion of the block. Applied by PG_BAND_PREC_SOLVE (one banded
+ * block solve along each radial rank). */
+int pg_prec_kron_create(pg_op *op, const double *overlap_rows, const double *cS, const double *cH,
+                        const double *h1, const double *h2, pg_banded **out);
 int pg_banded_destroy(pg_banded *b);
 
 enum {

@@ -17,7 +17,9 @@ from .potentials import (AngularKineticEnergyPotential, ComplexAbsorbingPotentia
                          SingleActiveElectronPotential, register_potential)
 from .problem import InitBSpline, InitialConditionType, Problem, core
 from .propagator import (BasisPropagator, BasisPropagatorGPU, BSplinePreconditioner, CayleyPropagator,
-                         CayleyPropagatorGPU, PamPropagator, PamPropagatorGPU, RadialPreconditioner)
+                         CayleyPropagatorGPU, PamPropagator, PamPropagatorGPU, RadialPreconditioner,
+                         RadialTwoElectronPreconditionerIfpack, RadialTwoElectronPreconditionerSuperLU,
+                         TwoElectronKroneckerPreconditioner)
 from .solver import PiramSolver, PiramSolverGPU
 from .spherical import DefaultCoupledIndexIterator
 

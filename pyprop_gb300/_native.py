@@ -100,6 +100,7 @@ _SIGS = {
     "pg_vec_convert": (_I, [_P, _I, _P, _I, _P, _LL]),
     "pg_vec_combine": (_I, [_P, _P, _LL, _I, _DP, _I]),
     "pg_vec_swap_last2": (_I, [_P, _I, _P, _P, _I, _I, _I]),
+    "pg_prec_kron_create": (_I, [_P, _DP, _DP, _DP, _DP, _DP, C.POINTER(_P)]),
     "pg_mlp_create": (_I, [_P, _I, _I, _I, C.c_ulonglong, C.POINTER(_P)]),
     "pg_mlp_destroy": (_I, [_P]),
     "pg_mlp_parameter_count": (_LL, [_P]),

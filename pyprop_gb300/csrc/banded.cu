@@ -60,7 +60,7 @@ template <typename R, typename C, int NW>
 __global__ void __launch_bounds__(32 * NW, 1)
     tri_solve_kernel(int N, int nblk, int w, const C *__restrict__ lo_inv, const C *__restrict__ lo_g,
                      const C *__restrict__ lo_rb, const C *__restrict__ up_inv, const C *__restrict__ up_g,
-                     const C *__restrict__ up_rb, int do_lower, int do_upper, int per_fibre_matrix, int g_in_smem,
+                     const C *__restrict__ up_rb, int do_lower, int do_upper, int fib_per_mat, int g_in_smem,
                      cx<R> *__restrict__ x, int nfib)
 {
     extern __shared__ __align__(16) unsigned char tri_smem[];
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(32 * NW, 1)
     cx<R> *xs = (cx<R> *)tri_smem;              // [nblk*32] the fibre: f, then z, then y
     cx<R> *sb = xs + (size_t)nblk * 32;          // [nblk*w] boundary values s_b
     C *sg = (C *)(sb + (size_t)nblk * w);        // [nblk][w][32] G_b (when g_in_smem)
-    const size_t m = per_fibre_matrix ? (size_t)f : 0;
+    const size_t m = (size_t)(f / fib_per_mat);
     const size_t gstride = (size_t)w * 32;
     const int nb = nblk * w;
     cx<R> *xf = x + (size_t)f * N;
@@ -386,6 +386,7 @@ extern "C" int pg_overlap_create(pg_op *op, const double *overlap_rows, pg_bande
     b->N = N;
     b->kb = kb;
     b->nmat = 1;
+    b->fib_per_mat = std::max(1, op->nrows);  // one factor for every fibre
     b->complex_coef = 0;
     std::vector<double> Srows(overlap_rows, overlap_rows + (size_t)N * (2 * kb + 1));
     int st;
@@ -486,6 +487,84 @@ extern "C" int pg_prec_blockdiag_create(pg_op *op, const double *overlap_rows, c
     return PG_OK;
 }
 
+// Factor one complex band matrix A = cS S + cH h (rows [N][2kb+1]) and append its block data.
+static int factor_append(int N, int kb, const double *S, const zd &zS, const zd &zH, const double *h,
+                         std::vector<zd> *lo, std::vector<zd> *up)
+{
+    const int b = 2 * kb + 1;
+    std::vector<zd> M((size_t)N * b);
+    for (size_t q = 0; q < (size_t)N * b; ++q) M[q] = zS * S[q] + zH * zd(h[2 * q], h[2 * q + 1]);
+    if (!lu_band_nopivot(N, kb, M)) return PG_ERR_ARG;
+    auto Lf = [&](int i, int j) { return i == j ? zd(1.0, 0.0) : M[(size_t)i * b + kb + (j - i)]; };
+    auto Uf = [&](int i, int j) { return M[(size_t)i * b + kb + (j - i)]; };
+    std::vector<zd> li, lc, lr, ui, uc, ur;
+    build_blocks(N, kb, true, Lf, li, lc, lr);
+    build_blocks(N, kb, false, Uf, ui, uc, ur);
+    lo[0].insert(lo[0].end(), li.begin(), li.end());
+    lo[1].insert(lo[1].end(), lc.begin(), lc.end());
+    lo[2].insert(lo[2].end(), lr.begin(), lr.end());
+    up[0].insert(up[0].end(), ui.begin(), ui.end());
+    up[1].insert(up[1].end(), uc.begin(), uc.end());
+    up[2].insert(up[2].end(), ur.begin(), ur.end());
+    return PG_OK;
+}
+
+template <typename R>
+static int upload_sets(pg_banded_ext *bd, std::vector<zd> *lo, std::vector<zd> *up, std::vector<zd> *lo1,
+                       std::vector<zd> *up1)
+{
+    PG_TRY(upload_cplx<R>(lo[0], &bd->d_lo_inv));
+    PG_TRY(upload_cplx<R>(lo[1], &bd->d_lo_cpl));
+    PG_TRY(upload_cplx<R>(lo[2], &bd->d_lo_rb));
+    PG_TRY(upload_cplx<R>(up[0], &bd->d_up_inv));
+    PG_TRY(upload_cplx<R>(up[1], &bd->d_up_cpl));
+    PG_TRY(upload_cplx<R>(up[2], &bd->d_up_rb));
+    PG_TRY(upload_cplx<R>(lo1[0], &bd->d_lo_inv1));
+    PG_TRY(upload_cplx<R>(lo1[1], &bd->d_lo_cpl1));
+    PG_TRY(upload_cplx<R>(lo1[2], &bd->d_lo_rb1));
+    PG_TRY(upload_cplx<R>(up1[0], &bd->d_up_inv1));
+    PG_TRY(upload_cplx<R>(up1[1], &bd->d_up_cpl1));
+    return upload_cplx<R>(up1[2], &bd->d_up_rb1);
+}
+
+// Two-electron radial preconditioner, Kronecker-factorized per angular channel a:
+//     M_a = (cS S + cH h1_a) x (cS S + cH h2_a)  ~  cS^2 S x S + cS cH (h1_a x S + S x h2_a),
+// h1_a, h2_a the one-electron radial Hamiltonians of the channel's two electrons (host
+// complex128 rows [nchan][N][2kb+1]). It stands in for the reference's sparse direct / ILU
+// block preconditioners (examples/tensor/helium_stabilization/preconditioner.py:77-244):
+// it leaves out the electron-electron repulsion of the block and adds the small
+// cH^2 h1 x h2, and its inverse is two banded block solves, one along each radial rank.
+extern "C" int pg_prec_kron_create(pg_op *op, const double *overlap_rows, const double *cS, const double *cH,
+                                   const double *h1, const double *h2, pg_banded **out)
+{
+    if (!op || !overlap_rows || !cS || !cH || !h1 || !h2 || !out) return PG_ERR_ARG;
+    if (!op->finalized) return PG_ERR_STATE;
+    if (op->rank != 3 || op->shape[1] != op->N) return PG_ERR_STORAGE;
+    const int N = op->N, kb = op->kb, b = 2 * kb + 1, nchan = op->shape[0];
+    const zd zS(cS[0], cS[1]), zH(cH[0], cH[1]);
+    std::vector<zd> lo2[3], up2[3], lo1[3], up1[3];
+    const size_t per = (size_t)N * b * 2;  // doubles per channel
+    for (int a = 0; a < nchan; ++a) {
+        PG_TRY(factor_append(N, kb, overlap_rows, zS, zH, h2 + a * per, lo2, up2));
+        PG_TRY(factor_append(N, kb, overlap_rows, zS, zH, h1 + a * per, lo1, up1));
+    }
+    pg_banded_ext *bd = new pg_banded_ext();
+    bd->op = op;
+    bd->kind = 2;
+    bd->N = N;
+    bd->kb = kb;
+    bd->nmat = nchan;
+    bd->complex_coef = 1;
+    bd->fib_per_mat = op->shape[1];   // fibres (a, i1): channel a = f / N1
+    bd->fib_per_mat1 = op->shape[2];  // swapped fibres (a, i2): channel a = f / N2
+    const size_t esz = op->precision == PG_FP64 ? sizeof(cxd) : sizeof(cxf);
+    PG_CUDA_TRY(cudaMalloc(&bd->d_swap, esz * (size_t)op->nrows * N));
+    if (op->precision == PG_FP64) PG_TRY(upload_sets<double>(bd, lo2, up2, lo1, up1));
+    else PG_TRY(upload_sets<float>(bd, lo2, up2, lo1, up1));
+    *out = bd;
+    return PG_OK;
+}
+
 extern "C" int pg_banded_destroy(pg_banded *b)
 {
     if (!b) return PG_ERR_ARG;
@@ -498,6 +577,7 @@ extern "C" int pg_banded_destroy(pg_banded *b)
     cudaFree(e->d_up_cpl);
     cudaFree(e->d_lo_rb);
     cudaFree(e->d_up_rb);
+    for (void *p : {e->d_lo_inv1, e->d_lo_cpl1, e->d_lo_rb1, e->d_up_inv1, e->d_up_cpl1, e->d_up_rb1}) cudaFree(p);
     cudaFree(e->d_scratch);
     cudaFree(e->d_swap);
     delete e;
@@ -506,8 +586,22 @@ extern "C" int pg_banded_destroy(pg_banded *b)
 
 // One CTA of NW warps per fibre; NW covers the blocks of a fibre (one block per warp where
 // possible), bounded by the registers of the unrolled block product.
+// One factor set of a blocked triangular solve (the device arrays of build_blocks).
+struct TriSet {
+    const void *lo_inv, *lo_cpl, *lo_rb, *up_inv, *up_cpl, *up_rb;
+    int fib_per_mat;
+};
+
+static TriSet tri_set(const pg_banded *b, bool first_rank)
+{
+    if (first_rank) return {b->d_lo_inv1, b->d_lo_cpl1, b->d_lo_rb1, b->d_up_inv1, b->d_up_cpl1, b->d_up_rb1, b->fib_per_mat1};
+    return {b->d_lo_inv, b->d_lo_cpl, b->d_lo_rb, b->d_up_inv, b->d_up_cpl, b->d_up_rb, b->fib_per_mat};
+}
+
+// One CTA of NW warps per fibre; NW covers the blocks of a fibre (one block per warp where
+// possible), bounded by the registers of the unrolled block product.
 template <typename R, typename C, int NW>
-static int launch_tri_nw(pg_banded *b, bool do_lower, bool do_upper, void *x)
+static int launch_tri_nw(pg_banded *b, const TriSet &ts, bool do_lower, bool do_upper, void *x)
 {
     pg_ctx *ctx = b->op->ctx;
     const int N = b->N, nblk = (N + 31) / 32, w = b->kb;
@@ -525,24 +619,26 @@ static int launch_tri_nw(pg_banded *b, bool do_lower, bool do_upper, void *x)
         configured = smem;
     }
     tri_solve_kernel<R, C, NW><<<nfib, 32 * NW, smem, ctx->stream>>>(
-        N, nblk, w, (const C *)b->d_lo_inv, (const C *)b->d_lo_cpl, (const C *)b->d_lo_rb, (const C *)b->d_up_inv,
-        (const C *)b->d_up_cpl, (const C *)b->d_up_rb, do_lower ? 1 : 0, do_upper ? 1 : 0, b->nmat > 1, g_in_smem ? 1 : 0, (cx<R> *)x, nfib);
+        N, nblk, w, (const C *)ts.lo_inv, (const C *)ts.lo_cpl, (const C *)ts.lo_rb, (const C *)ts.up_inv,
+        (const C *)ts.up_cpl, (const C *)ts.up_rb, do_lower ? 1 : 0, do_upper ? 1 : 0, std::max(1, ts.fib_per_mat),
+        g_in_smem ? 1 : 0, (cx<R> *)x, nfib);
     ctx->launches++;
     return pg_check_launch(ctx);
 }
 
 template <typename R, typename C>
-static int launch_tri(pg_banded *b, bool do_lower, bool do_upper, void *x)
+static int launch_tri(pg_banded *b, bool do_lower, bool do_upper, void *x, bool first_rank = false)
 {
     const int nblk = (b->N + 31) / 32;
     if (b->kb < 1 || b->kb > 32) return PG_ERR_ARG;
-    if (nblk <= 8) return launch_tri_nw<R, C, 8>(b, do_lower, do_upper, x);
+    const TriSet ts = tri_set(b, first_rank);
+    if (nblk <= 8) return launch_tri_nw<R, C, 8>(b, ts, do_lower, do_upper, x);
     // FP64 stays at 16 warps (register budget of the complex128 block product)
     if constexpr (sizeof(R) == 8) {
-        return launch_tri_nw<R, C, 16>(b, do_lower, do_upper, x);
+        return launch_tri_nw<R, C, 16>(b, ts, do_lower, do_upper, x);
     } else {
-        if (nblk <= 16) return launch_tri_nw<R, C, 16>(b, do_lower, do_upper, x);
-        return launch_tri_nw<R, C, 24>(b, do_lower, do_upper, x);
+        if (nblk <= 16) return launch_tri_nw<R, C, 16>(b, ts, do_lower, do_upper, x);
+        return launch_tri_nw<R, C, 24>(b, ts, do_lower, do_upper, x);
     }
 }
 
@@ -582,8 +678,17 @@ static int banded_apply_t(pg_banded *bb, int which, void *x)
         if (b->kind != 0) return PG_ERR_STATE;
         return launch_tri<R, R>(b, true, true, x);
     case PG_BAND_PREC_SOLVE:
-        if (b->kind != 1) return PG_ERR_STATE;
-        return launch_tri<R, cx<R>>(b, true, true, x);
+        if (b->kind == 1) return launch_tri<R, cx<R>>(b, true, true, x);
+        if (b->kind == 2) {
+            // (A1 x A2)^-1 = (A1^-1 x 1)(1 x A2^-1): the second electron's rank as fibres, then
+            // the first electron's rank on the swapped copy
+            const int n0 = b->op->shape[0], n1 = b->op->shape[1], n2 = b->op->shape[2];
+            PG_TRY((launch_tri<R, cx<R>>(b, true, true, x)));
+            PG_TRY(pg_swap_last2_dev(ctx, b->op->precision, x, b->d_swap, n0, n1, n2));
+            PG_TRY((launch_tri<R, cx<R>>(b, true, true, b->d_swap, true)));
+            return pg_swap_last2_dev(ctx, b->op->precision, b->d_swap, x, n0, n2, n1);
+        }
+        return PG_ERR_STATE;
     default:
         return PG_ERR_ARG;
     }
@@ -611,3 +716,5 @@ int pg_banded_apply_dev(pg_banded *b, int which, void *x)
 }
 
 extern "C" int pg_banded_apply(pg_banded *b, int which, void *x) { return pg_banded_apply_dev(b, which, x); }
+
+int pg_banded_solve_kernels(const pg_banded *b) { return b->kind == 2 ? 4 : 1; }

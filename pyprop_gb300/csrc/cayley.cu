@@ -484,7 +484,7 @@ static int capture_iteration(pg_cayley *c, pg_op *op, pg_banded *pre, cudaGraphC
     PG_TRY(pg_gs_update<R>(rc, V, n, c->m, c->h1, w, n, 1, c->h2, &c->st->j, 1));
     PG_TRY(pg_gs_update<R>(rc, V, n, c->m, c->h2, w, n, 0, c->h3, &c->st->j, 1));
     cay_gmres_finalize_kernel<T><<<1, 32, 0, s>>>(c->st, c->h1, c->h2, c->h3, c->m, inner, c->eager ? 0 : 1,
-                                                   K_ITER - 1 + pg_op_matvec_kernels(op));
+                                                   K_ITER - 2 + pg_op_matvec_kernels(op) + pg_banded_solve_kernels(pre));
     return pg_check_launch(ctx);
 }
 
@@ -504,7 +504,8 @@ static int capture_iteration_learned(pg_cayley *c, cudaGraphConditionalHandle in
     pg_ctx *mctx = nullptr;
     int d_in = 0, d_out = 0;
     PG_TRY(pg_mlp_describe(c->mlp, &mctx, &d_in, &d_out));
-    const int nblk = c->opb->nrows, N = c->opb->N;
+    // one network row per angular channel; a channel's block is [N] (one electron) or [N][N]
+    const int nblk = c->opb->shape[0], N = (int)(c->n / nblk);
     PG_TRY(pg_mlp_block_features_dev(ctx, vcur, nblk, N, d_in, nullptr, c->Xf));
     PG_TRY(pg_mlp_forward_dev(c->mlp, c->Xf, nblk, c->mlp_out));
     cay_learned_apply_kernel<<<nb, 256, 0, s>>>(c->st, vcur, c->mlp_out, N, d_out,
@@ -520,7 +521,8 @@ static int capture_iteration_learned(pg_cayley *c, cudaGraphConditionalHandle in
     PG_TRY(pg_gs_update<float>(rc, V, n, c->m, c->h1, w, n, 1, c->h2, &c->st->j, 1));
     PG_TRY(pg_gs_update<float>(rc, V, n, c->m, c->h2, w, n, 0, c->h3, &c->st->j, 1));
     cay_gmres_finalize_kernel<float><<<1, 32, 0, s>>>(c->st, c->h1, c->h2, c->h3, c->m, inner, c->eager ? 0 : 1,
-                                                      K_LEARN_ITER - 1 + pg_op_matvec_kernels(c->opb));
+                                                      K_LEARN_ITER - 2 + pg_op_matvec_kernels(c->opb) +
+                                                          pg_banded_solve_kernels(c->precb));
     return pg_check_launch(ctx);
 }
 
@@ -578,7 +580,8 @@ static int record_fp64(pg_cayley *c, cxd *psi)
     rc->stream = s0;
     const int mv = pg_op_matvec_kernels(c->op64) - 1;
     cay_scales_kernel<<<1, 32, 0, s0>>>(c->params_dev, c->d_sc, c->st,
-                                        K_FP64_BASE + mv + (c->true_residual ? K_TRUE_RESID + mv : 0));
+                                        K_FP64_BASE + mv + pg_banded_solve_kernels(c->prec64) - 1 +
+                                            (c->true_residual ? K_TRUE_RESID + mv : 0));
     PG_TRY(pg_check_launch(ctx));
     PG_TRY(pg_op_matvec_dev(c->op64, dummy, c->d_sc + SC_MINUS * PG_MAX_SLOTS, psi, c->b64, 0, nullptr, nullptr));
     PG_CUDA_TRY(cudaMemcpyAsync(c->d64, c->b64, sizeof(cxd) * n, cudaMemcpyDeviceToDevice, s0));
@@ -642,7 +645,8 @@ static int record_mixed(pg_cayley *c, cxd *psi)
         cudaGraphConditionalHandle inner = 0;
         if (!c->eager) PG_TRY(capture_handle(s1, &inner, 0, 0));
         cay_gmres_init_kernel<float><<<nb, 256, 0, s1>>>(c->st, c->nrm, dconv, (cxf *)c->V, (cxf *)c->vcur, n, c->tol,
-                                                         2e-6, (learned ? K_LEARN_PASS : K_MIXED_PASS) + mv, inner, outer,
+                                                         2e-6, (learned ? K_LEARN_PASS : K_MIXED_PASS + pg_banded_solve_kernels(c->precb) - 1) + mv,
+                                                         inner, outer,
                                                          c->eager ? -1 : 1);
         PG_TRY(pg_check_launch(ctx));
         PG_TRY(loop_while(c, inner, c->cap[2], &c->st->cont_inner, [&]() {
@@ -710,7 +714,7 @@ extern "C" int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64,
     if (!op64 || !op_basis || !prec64 || !prec_basis || !out) return PG_ERR_ARG;
     if (basis_size < 2 || basis_size > GM_MAXM || basis_size > PG_RED_COLS - 2) return PG_ERR_ARG;
     if (op64->precision != PG_FP64 || op_basis->precision != basis_precision) return PG_ERR_ARG;
-    if (prec64->kind != 1 || prec_basis->kind != 1) return PG_ERR_ARG;
+    if ((prec64->kind != 1 && prec64->kind != 2) || (prec_basis->kind != 1 && prec_basis->kind != 2)) return PG_ERR_ARG;
     if (prec64->op->precision != PG_FP64 || prec_basis->op->precision != basis_precision) return PG_ERR_ARG;
     if (basis_precision != PG_FP64 && basis_precision != PG_FP32) return PG_ERR_ARG;
     pg_cayley *c = new pg_cayley();
@@ -852,11 +856,11 @@ extern "C" int pg_cayley_set_learned(pg_cayley *c, pg_mlp *mlp, int coupling_slo
         c->built_psi = nullptr;
         return PG_OK;
     }
-    if (c->prec != PG_FP32 || c->opb->rank != 2) return PG_ERR_STATE;
+    if (c->prec != PG_FP32) return PG_ERR_STATE;
     pg_ctx *mctx = nullptr;
     int d_in = 0, d_out = 0;
     PG_TRY(pg_mlp_describe(mlp, &mctx, &d_in, &d_out));
-    const int nblk = c->opb->nrows, N = c->opb->N;
+    const int nblk = c->opb->shape[0], N = (int)(c->n / nblk);
     if (mctx != c->ctx) return PG_ERR_ARG;
     if (d_in < 6 * N || d_out < 2 * N) return PG_ERR_SHAPE;
     PG_TRY(pg_mlp_reserve(mlp, nblk));

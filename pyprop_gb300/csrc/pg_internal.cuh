@@ -186,8 +186,9 @@ struct TriDev {
 
 struct pg_banded {
     pg_op *op = nullptr;
-    int kind = 0;            // 0 overlap, 1 preconditioner
+    int kind = 0;            // 0 overlap, 1 block preconditioner, 2 two-electron Kronecker preconditioner
     int N = 0, kb = 0, nmat = 0;
+    int fib_per_mat = 1;     // consecutive fibres sharing one factor (fibre f uses factor f / fib_per_mat)
     // overlap: U upper Cholesky factor rows (real) for multiplies, lower = U^T
     void *d_U = nullptr;     // [N][kb+1]  U(i, i+j) at [i][j]   (real, precision of op)
     void *d_S = nullptr;     // [N][2kb+1] S rows (real)
@@ -197,9 +198,15 @@ struct pg_banded {
     void *d_up_inv = nullptr, *d_up_cpl = nullptr;   // upper factor (U)
     void *d_lo_rb = nullptr, *d_up_rb = nullptr;     // inverses of the block-boundary systems
     int complex_coef = 0;
+    // kind 2: the factors along the first electron's rank (applied on the swapped copy)
+    void *d_lo_inv1 = nullptr, *d_lo_cpl1 = nullptr, *d_lo_rb1 = nullptr;
+    void *d_up_inv1 = nullptr, *d_up_cpl1 = nullptr, *d_up_rb1 = nullptr;
+    int fib_per_mat1 = 1;
 };
 
 int pg_banded_apply_dev(pg_banded *b, int which, void *x);
+// kernels one PG_BAND_PREC_SOLVE launches (a two-electron Kronecker preconditioner: 2 solves, 2 swaps)
+int pg_banded_solve_kernels(const pg_banded *b);
 // y[a][j][i] = x[a][i][j], x [n0][n1][n2] (vector.cu)
 int pg_swap_last2_dev(pg_ctx *ctx, int precision, const void *x, void *y, int n0, int n1, int n2);
 

@@ -116,10 +116,17 @@ class DeviceOperator:
         self.h = h
         self.has_overlap = overlap_rows is not None
         if overlap_rows is not None:
-            if len(shape) != 2:
-                raise ValueError("the overlap slot is built for rank-2 operators")
-            band = bandnh_from_rows(np.asarray(overlap_rows, dtype=np.float64), kb)[None, :]
-            self._add(["Ident", "BandNH"], band, [None, None], 0)
+            rows = np.asarray(overlap_rows, dtype=np.float64)
+            band = bandnh_from_rows(rows, kb)[None, :]
+            if len(shape) == 2:
+                self._add(["Ident", "BandNH"], band, [None, None], 0)
+            else:
+                # two electrons: S x S on the radial ranks, the first one as a packed pair list
+                N = rows.shape[0]
+                pr = np.array([(i, j) for i in range(N) for j in range(max(0, i - kb), min(N, i + kb + 1))],
+                              dtype=np.int32)
+                s1 = rows[pr[:, 0], kb + pr[:, 1] - pr[:, 0]]
+                self._add(["Ident", "Simp", "BandNH"], (s1[:, None] * band)[None], [None, pr, None], 0)
         for p, pot in enumerate(self.potentials):
             kinds = [g.GetStorageId() for g in pot.GeometryList]
             pairs = [g.GetBasisPairs() if k in ("Simp", "Herm") else None for g, k in zip(pot.GeometryList, kinds)]
@@ -202,6 +209,18 @@ class Banded:
         h = C.c_void_p()
         check(op.lib.pg_prec_blockdiag_create(op.h, rp, csp, chp, slp, wtp, len(sl), C.byref(h)),
               "pg_prec_blockdiag_create")
+        return cls(op, h)
+
+    @classmethod
+    def kron(cls, op, overlap_rows, cS, cH, h1, h2):
+        """Two-electron Kronecker-factorized radial preconditioner (pg_prec_kron_create)."""
+        rows, rp = nat.dptr(np.asarray(overlap_rows, dtype=np.float64))
+        cs, csp = nat.dptr(np.array([cS], dtype=np.complex128).view(np.float64))
+        ch, chp = nat.dptr(np.array([cH], dtype=np.complex128).view(np.float64))
+        a1, a1p = nat.dptr(np.ascontiguousarray(h1, dtype=np.complex128).view(np.float64))
+        a2, a2p = nat.dptr(np.ascontiguousarray(h2, dtype=np.complex128).view(np.float64))
+        h = C.c_void_p()
+        check(op.lib.pg_prec_kron_create(op.h, rp, csp, chp, a1p, a2p, C.byref(h)), "pg_prec_kron_create")
         return cls(op, h)
 
     def apply(self, which, x):

@@ -110,19 +110,27 @@ class LearnedPreconditioner:
     exact correction that the block preconditioner misses, per unit coupling strength.
     """
 
-    def __init__(self, prop, hidden=256, seed=7):
-        nang, N = prop.psi.GetRepresentation().GetFullShape()
+    def __init__(self, prop, hidden=256, seed=7, coupling_potential=None):
+        """coupling_potential: index (in the propagator's potential list) of the term whose
+        scale i dt/2 h(t) multiplies the correction - by default the one time-dependent term
+        (the field coupling the block preconditioner leaves out); a time-independent term gives
+        the constant scale i dt/2 (for a part of H the preconditioner omits at all times, such
+        as the two-electron repulsion)."""
+        shape = prop.psi.GetRepresentation().GetFullShape()
         self.prop = prop
-        self.nblk, self.N = nang, N
-        self.d_in = features_width(N)
-        self.d_out = ((2 * N + 7) // 8) * 8
+        self.shape = shape
+        self.nblk, self.N = shape[0], int(np.prod(shape[1:]))  # one network row per angular channel
+        self.d_in = features_width(self.N)
+        self.d_out = ((2 * self.N + 7) // 8) * 8
         self.net = MlpNet(self.d_in, hidden, self.d_out, seed=seed, ctx=prop.op64.ctx)
         pots = prop.BasePropagator.PotentialList
-        dep = [p for p, pot in enumerate(pots) if pot.IsTimeDependent]
-        if len(dep) != 1:
-            raise ValueError("the learned preconditioner expects exactly one time-dependent coupling term")
-        self.pot_index = dep[0]
-        self.slot = 1 + dep[0]  # slot of that potential in the device operator (slot 0: overlap)
+        if coupling_potential is None:
+            dep = [p for p, pot in enumerate(pots) if pot.IsTimeDependent]
+            if len(dep) != 1:
+                raise ValueError("give coupling_potential: the propagator has %d time-dependent terms" % len(dep))
+            coupling_potential = dep[0]
+        self.pot_index = int(coupling_potential)
+        self.slot = 1 + self.pot_index  # slot of that potential in the device operator (slot 0: overlap)
         self.pairs = []
 
     def coupling_scale(self, t, dt):
@@ -158,7 +166,8 @@ class LearnedPreconditioner:
             s = self.coupling_scale(t, dt)
             if abs(s) < min_field * smax:
                 continue
-            y = self._block_solve(r)
+            y = self._block_solve(r).reshape(self.nblk, self.N)
+            e = e.reshape(self.nblk, self.N)
             ny = float(torch.linalg.vector_norm(y))
             for k in range(phases):
                 ph = 1.0 if (rng is None or k == 0) else complex(np.exp(1j * rng.uniform(0, 2 * np.pi)))
@@ -191,12 +200,13 @@ class LearnedPreconditioner:
         y = self._block_solve(r)
         if not learned:
             return y
+        yb = y.reshape(self.nblk, self.N).contiguous()
         X = torch.empty((self.nblk, self.d_in), dtype=torch.bfloat16, device=y.device)
-        self.net.block_features(y.contiguous(), X)
+        self.net.block_features(yb, X)
         out = torch.empty((self.nblk, self.d_out), dtype=torch.float32, device=y.device)
         self.net.forward(X, out)
         corr = torch.view_as_complex(out[:, :2 * self.N].reshape(self.nblk, self.N, 2).contiguous())
-        return y + self.coupling_scale(t, dt) * corr
+        return (yb + self.coupling_scale(t, dt) * corr).reshape(y.shape)
 
     def one_step_residual(self, pairs, learned=True):
         """Mean over pairs of ||A P(r) - r|| / ||r|| (A = S + i dt/2 H(t + dt/2), complex64)."""

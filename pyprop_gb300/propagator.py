@@ -220,6 +220,57 @@ class BSplinePreconditioner:
 RadialPreconditioner = BSplinePreconditioner
 
 
+class TwoElectronKroneckerPreconditioner(BSplinePreconditioner):
+    """Two-electron radial preconditioner for the Cayley step on [channel][r1][r2]: per coupled
+    channel (l1, l2, L, M) the Kronecker product (cS S + cH h_l1) x (cS S + cH h_l2) of the
+    one-electron radial operators h_l = -1/2 d^2/dr^2 + l(l+1)/(2 r^2) - z/r, factored on the
+    host and solved on the device along each radial rank. It takes the place of the
+    reference's RadialTwoElectronPreconditionerSuperLU / Ifpack
+    (examples/tensor/helium_stabilization/preconditioner.py:77-244), which factor the full
+    channel block including the electron-electron repulsion; this one leaves the repulsion out
+    (the learned preconditioner can add the missing part). Config keys: z (default 2), mass."""
+
+    def ApplyConfigSection(self, conf):
+        self.Z = float(getattr(conf, "z", 2.0))
+        self.Mass = float(getattr(conf, "mass", 1.0))
+
+    def _one_electron(self, l):
+        bs = self.psi.GetRepresentation().radial.BSplineObject
+        r = bs.grid
+        kin = bs.band_elements(np.full(r.shape, -1.0 / (2.0 * self.Mass)), 2)
+        pot = bs.band_elements(l * (l + 1.0) / (2.0 * self.Mass * r * r) - self.Z / r, 0)
+        return np.asarray(kin + pot, dtype=np.complex128)
+
+    def Setup(self, prop, precision=nat.PG_FP64):
+        repr_ = self.psi.GetRepresentation()
+        shape = repr_.GetFullShape()
+        if len(shape) != 3:
+            raise ValueError("TwoElectronKroneckerPreconditioner needs a two-electron representation")
+        indices = repr_.bases[0].indices
+        cache = {}
+
+        def h(l):
+            if l not in cache:
+                cache[l] = self._one_electron(l)
+            return cache[l]
+
+        h1 = np.stack([h(ix.l1) for ix in indices])
+        h2 = np.stack([h(ix.l2) for ix in indices])
+        self.ops, self.solvers = {}, {}
+        for prec in (nat.PG_FP64, precision):
+            if prec in self.solvers:
+                continue
+            op = DeviceOperator(Context.get(), [], shape, repr_.kb, prec)
+            self.ops[prec] = op
+            self.solvers[prec] = Banded.kron(op, repr_.overlap_rows, self.OverlapScaling, self.HamiltonianScaling,
+                                             h1, h2)
+
+
+# the reference's two-electron preconditioner names select the GPU one
+RadialTwoElectronPreconditionerSuperLU = TwoElectronKroneckerPreconditioner
+RadialTwoElectronPreconditionerIfpack = TwoElectronKroneckerPreconditioner
+
+
 class CayleyPropagatorGPU(PropagatorBase):
     def ApplyConfig(self, config):
         PropagatorBase.ApplyConfig(self, config)

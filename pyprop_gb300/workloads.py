@@ -134,7 +134,7 @@ time_function = LaserFunctionSimpleLength
 
 def helium(lmax=2, L=(0,), nbsplines=20, rmax=20.0, order=7, quad_order_additional=10, z=2.0,
            propagator="PamPropagatorGPU", precision="fp64", timestep=0.01, duration=1.0, krylov_basis_size=20,
-           amplitude=0.0, frequency=1.0, pulse_duration=10.0):
+           amplitude=0.0, frequency=1.0, pulse_duration=10.0, gmres_tolerance=1e-12):
     """Two-electron (helium-like) model in the layout of
     examples/tensor/helium_stabilization/config.ini:1-188: coupled spherical harmonics
     (``DefaultCoupledIndexIterator(lmax, L, M=0)``) x B-splines x B-splines, radial kinetic
@@ -144,6 +144,13 @@ def helium(lmax=2, L=(0,), nbsplines=20, rmax=20.0, order=7, quad_order_addition
     pulse (L must then hold neighbouring values)."""
     total = nbsplines - 3 if order == 7 else nbsplines - (order - 4)
     laser_name = ', "LaserPotential"' if amplitude else ""
+    cayley = "Cayley" in str(propagator)
+    prec_key = 'preconditioner = "RadialPreconditioner"' if cayley else ""
+    prec_sec = f"""
+[RadialPreconditioner]
+type = RadialTwoElectronPreconditionerSuperLU
+z = {z!r}
+""" if cayley else ""
     laser = f"""
 [PulseParameters]
 frequency = {frequency!r}
@@ -201,11 +208,12 @@ timestep = {timestep!r}
 duration = {duration!r}
 renormalization = False
 krylov_basis_size = {krylov_basis_size}
-krylov_tolerance = 0
+krylov_tolerance = {gmres_tolerance if cayley else 0!r}
 krylov_double_orthogonalization = True
 gpu_precision = "{precision}"
 silent = True
-
+{prec_key}
+{prec_sec}
 [RadialKineticEnergy1]
 classname = "KineticEnergyPotential"
 geometry0 = "Diagonal"
