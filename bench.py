@@ -213,6 +213,33 @@ def time_large_matvec(torch, flush, reps=20):
     return avg, nbytes, variant
 
 
+def profile_large_matvec():
+    """Profiling entry point: the large-operator matvec (hydrogen lmax 300, 2000 B-splines)
+    after its autotuning, 3 launches inside the NVTX range "matvec_hbm" (for
+    ncu --nvtx --nvtx-include matvec_hbm/)."""
+    import torch
+    import pyprop_gb300 as pp
+    from pyprop_gb300 import _native as nat
+    from pyprop_gb300.workloads import hydrogen
+    prob = pp.Problem(pp.LoadString(hydrogen(propagator="PamPropagatorGPU", **LARGE)))
+    bp = prob.Propagator.BasePropagator
+    bp.SetupStep(0.01)
+    op = bp.device_operator(nat.PG_FP32)
+    nang, N = prob.psi.GetRepresentation().GetFullShape()
+    src = torch.randn((nang, N), dtype=torch.complex64, device="cuda")
+    dst = torch.empty_like(src)
+    sc = op.scales(5.0)
+    op.matvec(sc, src, dst)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("matvec_hbm")
+    for _ in range(3):
+        op.matvec(sc, src, dst)
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "matvec_hbm", "variant": MATVEC_KERNELS[op.variant()[0]],
+                      "algorithmic_bytes": 8 * (op.stored_elements() + 2 * nang * N)}))
+
+
 def profile_traffic(name):
     """dram bytes per launch recorded in a committed ncu summary (line 'dram_bytes_per_launch: N')."""
     path = os.path.join(ROOT, "profiles", name)
@@ -515,6 +542,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=300,
                     help="oracle Cayley steps timed on one host core for cpu_baseline (0 = skip)")
+    ap.add_argument("--profile", choices=["matvec_hbm"], default=None,
+                    help="profiling entry point instead of the benchmark")
     ap.add_argument("--eager", action="store_true",
                     help="host-driven GMRES loops (same kernels, visible one by one to a profiler)")
     ap.add_argument("--ensemble", type=int, default=256, help="members of the batched leg (0 = skip)")
@@ -522,6 +551,10 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     from pyprop_gb300 import build_native
+    if args.profile == "matvec_hbm":
+        build_native.build()
+        profile_large_matvec()
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -174,4 +174,7 @@ def test_learned_preconditioner_on_the_two_electron_model(gpu):
             n += st.Iterations
         iters[use], out[use] = n, prob.psi.numpy()
     print("helium GMRES iterations over 10 steps: block %d, learned %d" % (iters[False], iters[True]))
-    assert relerr(out[True], out[False]) < 1e-9
+    # both meet the true-residual tolerance; their states agree to that tolerance times the
+    # conditioning of S x S + i dt/2 H
+    assert relerr(out[True], out[False]) < 1e-7
+    assert iters[True] <= iters[False]
