@@ -335,6 +335,7 @@ struct pg_pamp {
     void *built_psi = nullptr;
     bool last_hermitian = false;
     long long kernels_per_step = 0;  // kernel nodes of the two graphs
+    pg_krylov_stats last_stats = {};  // of the last step (ensemble steps read it per member)
 };
 
 extern "C" int pg_pamp_create(pg_op *op64, pg_op *op_basis, pg_banded *ovl64, pg_banded *ovl_basis, int basis_size,
@@ -471,27 +472,31 @@ static int pamp_capture(pg_pamp *p, cxd *x, bool first, cudaGraphExec_t *out)
     return PG_OK;
 }
 
-extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scales, int nscales, pg_krylov_stats *st)
+static int pamp_build(pg_pamp *p, cxd *x)
 {
-    if (!p || !psi || nscales < 0 || nscales > PG_MAX_SLOTS || (nscales > 0 && !scales)) return PG_ERR_ARG;
-    pg_ctx *ctx = p->ctx;
-    const int m = p->m;
-    cxd *x = (cxd *)psi;
-    if (p->built_psi != psi) {
-        if (p->g1) { cudaGraphExecDestroy(p->g1); p->g1 = nullptr; }
-        if (p->g2) { cudaGraphExecDestroy(p->g2); p->g2 = nullptr; }
-        p->kernels_per_step = 0;
-        PG_TRY(pamp_capture(p, x, true, &p->g1));
-        PG_TRY(pamp_capture(p, x, false, &p->g2));
-        p->built_psi = psi;
-    }
+    if (p->built_psi == x) return PG_OK;
+    if (p->g1) { cudaGraphExecDestroy(p->g1); p->g1 = nullptr; }
+    if (p->g2) { cudaGraphExecDestroy(p->g2); p->g2 = nullptr; }
+    p->kernels_per_step = 0;
+    PG_TRY(pamp_capture(p, x, true, &p->g1));
+    PG_TRY(pamp_capture(p, x, false, &p->g2));
+    p->built_psi = x;
+    return PG_OK;
+}
+
+static void pamp_set_scales(pg_pamp *p, const double *scales, int nscales)
+{
     for (int k = 0; k < PG_MAX_SLOTS; ++k)
         p->h_scales[k] = mk<double>(k < nscales ? scales[2 * k] : 0.0, k < nscales ? scales[2 * k + 1] : 0.0);
-    PG_CUDA_TRY(cudaMemcpyAsync(p->d_scales, p->h_scales, sizeof(cxd) * PG_MAX_SLOTS, cudaMemcpyHostToDevice, ctx->stream));
-    PG_CUDA_TRY(cudaGraphLaunch(p->g1, ctx->stream));
-    PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+}
+
+// After the Arnoldi graph has completed: the m x m Hessenberg from the downloaded columns
+// (truncated at a happy breakdown), c = |psi| exp(-i dt H_m) e_1 into the pinned h_c that the
+// second graph uploads, and the step's statistics.
+static int pamp_host_exp(pg_pamp *p, double dt, pg_krylov_stats *st)
+{
+    const int m = p->m;
     const double norm_h = p->rctx.h_pinned[1];
-    // Hessenberg (row-major), truncated at a happy breakdown
     std::vector<zd> H((size_t)m * m, zd(0.0, 0.0));
     int k = m;
     for (int j = 0; j < m; ++j) {
@@ -513,8 +518,11 @@ extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scal
         p->h_c[2 * i] = v.real();
         p->h_c[2 * i + 1] = v.imag();
     }
-    PG_CUDA_TRY(cudaGraphLaunch(p->g2, ctx->stream));
-    ctx->launches += p->kernels_per_step;
+    p->last_stats.OpCount += m;
+    p->last_stats.InnerProductCount += (p->double_ortho ? 2 : 1) * m;
+    p->last_stats.ReOrthoCount += p->double_ortho ? m : 0;
+    p->last_stats.ErrorEstimate = std::norm(c[k - 1]);
+    p->last_stats.Iterations = k;
     if (st) {
         st->OpCount += m;
         st->InnerProductCount += (p->double_ortho ? 2 : 1) * m;
@@ -522,6 +530,21 @@ extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scal
         st->ErrorEstimate = std::norm(c[k - 1]);
         st->Iterations = k;
     }
+    return PG_OK;
+}
+
+extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scales, int nscales, pg_krylov_stats *st)
+{
+    if (!p || !psi || nscales < 0 || nscales > PG_MAX_SLOTS || (nscales > 0 && !scales)) return PG_ERR_ARG;
+    pg_ctx *ctx = p->ctx;
+    PG_TRY(pamp_build(p, (cxd *)psi));
+    pamp_set_scales(p, scales, nscales);
+    PG_CUDA_TRY(cudaMemcpyAsync(p->d_scales, p->h_scales, sizeof(cxd) * PG_MAX_SLOTS, cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA_TRY(cudaGraphLaunch(p->g1, ctx->stream));
+    PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    PG_TRY(pamp_host_exp(p, dt, st));
+    PG_CUDA_TRY(cudaGraphLaunch(p->g2, ctx->stream));
+    ctx->launches += p->kernels_per_step;
     return PG_OK;
 }
 
