@@ -132,6 +132,30 @@ int pg_op_add_term(pg_op *op, const char *storage, const double *potential, int 
  */
 int pg_op_add_term_ranks(pg_op *op, const char *storage, const double *potential, const int *extents,
                          const int *pairs, const int *npairs, int slot);
+/*
+ * Factorized rank-3 terms: V = sum_q w_q * scale[slot_q] * A_q (x) R_q, each factor q an
+ * angular matrix A_q (sparse, real) times a radial operator R_q on both radial ranks that is
+ * shared by every angular pair. This is the multipole form of the electron-electron
+ * repulsion, V(pair) = sum_l3 c_l3(pair) r<^l3 / r>^(l3+1)
+ * (examples/tensor/helium_stabilization/coupledspherical.cpp:7-127, potential data per pair
+ * on SelectionRule_R12 x banded-packed x banded-nonhermitian): the reference stores the sum
+ * per angular pair (Simp_Simp_BandNH, tensorpotentialmultiply_generator.py:302-363,622-762),
+ * which at L <= 8, l <= 16, 200 splines is 14 TB; per factor it is one band x band block.
+ * radial: host float64 [nfactors][N1][2k+1][2k+1][N2], element (i1, d1, d2, i2) coupling
+ * output (i1, i2) to input (i1 + d1 - k, i2 + d2 - k) (k = bandCount, N1 = shape[1],
+ * N2 = shape[2]). weights: complex128 [nfactors]; slots [nfactors]. Entries (factor, row,
+ * col, coef): A_factor[row][col] += coef, dst[row] += ... src[col]. Several calls add
+ * factors. Applied by every matvec after the banded terms (two more kernels: the angular
+ * mix of src into per-factor scratch, then the radial stencil summed over factors into dst).
+ */
+int pg_op_add_factored(pg_op *op, int nfactors, const double *radial, const double *weights, const int *slots,
+                       long long nentries, const int *ent_factor, const int *ent_row, const int *ent_col,
+                       const double *ent_coef);
+/* Bookkeeping of the factorized part (no reference counterpart): info[0] factors, [1]
+ * angular entries (row, col), [2] flops of the angular mix and [3] of the radial stencil per
+ * matvec (real multiply-adds x 2, zero blocks skipped as the kernels skip them), [4] bytes
+ * of radial factors, [5] bytes of the per-factor scratch. Zeros when there is none. */
+int pg_op_factored_info(const pg_op *op, double *info);
 /* Upload. Must be called once after the last add_term. */
 int pg_op_finalize(pg_op *op);
 /* Matvec kernel variant (no reference counterpart): pg_op_finalize times the candidates on

@@ -578,7 +578,7 @@ static int launch_dense(pg_op *op, const pg_scales &scales, const cxd *scales_de
     return pg_check_launch(op->ctx);
 }
 
-int pg_op_matvec_kernels(const pg_op *op) { return op->ndense_entries > 0 ? 2 : 1; }
+int pg_op_matvec_kernels(const pg_op *op) { return (op->ndense_entries > 0 ? 2 : 1) + (op->fact.Q > 0 ? 2 : 0); }
 
 int pg_op_matvec_dev(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
                      int accumulate, const double *src_inv_scale_dev, void *src_copy_out)
@@ -594,9 +594,11 @@ int pg_op_matvec_dev(pg_op *op, const pg_scales &scales, const cxd *scales_dev, 
                     : launch_op_matvec<float>(op, scales, scales_dev, src, dst, accumulate, src_inv_scale_dev,
                                               src_copy_out));
     }
-    if (op->ndense_entries == 0) return PG_OK;
-    return fp64 ? launch_dense<double>(op, scales, scales_dev, src, dst, src_inv_scale_dev)
-                : launch_dense<float>(op, scales, scales_dev, src, dst, src_inv_scale_dev);
+    if (op->ndense_entries > 0)
+        PG_TRY(fp64 ? launch_dense<double>(op, scales, scales_dev, src, dst, src_inv_scale_dev)
+                    : launch_dense<float>(op, scales, scales_dev, src, dst, src_inv_scale_dev));
+    if (op->fact.Q > 0 && !op->tuning) PG_TRY(pg_factored_apply(op, scales, scales_dev, src, dst, src_inv_scale_dev));
+    return PG_OK;
 }
 
 extern "C" int pg_op_create(pg_ctx *ctx, int rank, const int *shape, int bandCount, int precision, pg_op **out)
@@ -640,6 +642,7 @@ extern "C" int pg_op_destroy(pg_op *op)
     cudaFree(op->d_dent_mat);
     cudaFree(op->d_dent_slot);
     cudaFree(op->d_dense);
+    pg_factored_free(op);
     delete op;
     return PG_OK;
 }
@@ -1033,9 +1036,13 @@ extern "C" int pg_op_finalize(pg_op *op)
             PG_CUDA_TRY(cudaMemcpy(op->d_dense, tmp.data(), cnt * sizeof(cxf), cudaMemcpyHostToDevice));
         }
     }
+    PG_TRY(pg_factored_finalize(op));
     op->finalized = true;
     make_band_tensor_map(op);
-    return autotune(op);
+    op->tuning = true;
+    st = autotune(op);
+    op->tuning = false;
+    return st;
 }
 
 // The matvec kernel variant for this operator, by measurement: each candidate runs 2 untimed

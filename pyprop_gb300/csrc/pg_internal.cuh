@@ -121,6 +121,28 @@ struct HostTerm {
     int slot = 0;
 };
 
+// one factor of a factorized rank-3 term (pg_op_add_factored)
+struct HostFactor {
+    std::vector<double> radial;  // [N1][b][b][N2]
+    double w[2] = {1.0, 0.0};
+    int slot = 0;
+    std::vector<int> row, col;
+    std::vector<double> coef;
+};
+
+// device form of all factors of an operator (factored.cu)
+struct FactDev {
+    int Q = 0, Qp = 0, A = 0, N1 = 0, N2 = 0, N2p = 0, nct = 0, nE = 0;
+    int *row_ptr = nullptr, *col = nullptr, *qlo = nullptr, *qhi = nullptr, *slot = nullptr;
+    void *coef = nullptr;             // [nE][Qp] real (operator precision)
+    unsigned char *chunk = nullptr;   // [A][Qp / chunk] rows that have entries in the chunk
+    unsigned char *bflag = nullptr;   // [Q][nct] channel tiles with a nonzero row
+    void *radial = nullptr;           // [Q][N1][b][b][N2p] real
+    cxd *w = nullptr;                 // [Q]
+    void *Z = nullptr;                // [Q][A][N1*N2] complex scratch
+    double flops_mix = 0, flops_radial = 0, radial_bytes = 0, z_bytes = 0;
+};
+
 struct pg_op {
     pg_ctx *ctx = nullptr;
     int rank = 2;
@@ -161,7 +183,18 @@ struct pg_op {
     long long ndense_entries = 0;
     int *d_drow_ptr = nullptr, *d_dent_col = nullptr, *d_dent_mat = nullptr, *d_dent_slot = nullptr;
     void *d_dense = nullptr;  // [ndense][j][i] (transposed: thread i reads row j contiguously)
+    // factorized rank-3 terms
+    std::vector<HostFactor> factors;
+    FactDev fact;
+    bool tuning = false;  // the variant autotuner times the banded part alone
 };
+
+// factorized terms (factored.cu): upload at finalize, release, and the two-kernel apply that
+// adds them to dst after the banded part
+int pg_factored_finalize(pg_op *op);
+void pg_factored_free(pg_op *op);
+int pg_factored_apply(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
+                      const double *src_inv_scale_dev);
 
 // matvec launcher shared by the drivers: dst = acc*dst + sum scales * V src
 // scales_dev (optional) overrides `scales` when non-null.
