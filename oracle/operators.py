@@ -11,6 +11,9 @@
   core/transform/bspline/bsplinesolver.h:43-162).
 * ``dense_operator``: dense assembly from the tensor layout, after
   examples/tensor/helium_stabilization/twoelectron_test.py:31-56.
+* ``factored_multiply``: a two-electron term as angular coefficients x shared radial
+  operators (the multipole sum of examples/tensor/helium_stabilization/coupledspherical.cpp:
+  7-127 kept per multipole), applied point by point on the radial grid.
 """
 from __future__ import annotations
 
@@ -281,3 +284,34 @@ class BandLU:
             x, info = sl.lapack.zgbtrs(lu, self.kb, self.kb, psi[a], piv)
             out[a] = x
         return out
+
+
+def stencil_apply(R, x, kb):
+    """y[i1, i2] = sum_{d1, d2} R[i1, d1, d2, i2] x[i1 + d1 - kb, i2 + d2 - kb], zero outside
+    the grid: one radial factor [N1][2kb+1][2kb+1][N2] on one channel's [N1][N2] block."""
+    N1, b, _, N2 = R.shape
+    xp = np.zeros((N1 + 2 * kb, N2 + 2 * kb), dtype=np.complex128)
+    xp[kb:kb + N1, kb:kb + N2] = x
+    y = np.zeros((N1, N2), dtype=np.complex128)
+    for d1 in range(b):
+        for d2 in range(b):
+            y += R[:, d1, d2, :] * xp[d1:d1 + N1, d2:d2 + N2]
+    return y
+
+
+def factored_multiply(factored, scales, src, dest):
+    """dest[row] += scale * weight_q * coef_q(row, col) * R_q applied to src[col], for
+    factored = [(FactoredPotential, slot)] and src/dest [Nang][N1][N2]."""
+    for fac, slot in factored:
+        rows, cols = fac.entries()
+        for q in range(fac.nfactors):
+            c = fac.coefs[q]
+            w = scales[slot] * fac.weights[q]
+            cache = {}
+            for r, col, v in zip(rows, cols, c):
+                if v == 0.0:
+                    continue
+                if col not in cache:
+                    cache[col] = stencil_apply(fac.stencil[q], src[col], fac.kb)
+                dest[r] += w * v * cache[col]
+    return dest

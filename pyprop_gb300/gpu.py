@@ -127,11 +127,62 @@ class DeviceOperator:
                               dtype=np.int32)
                 s1 = rows[pr[:, 0], kb + pr[:, 1] - pr[:, 0]]
                 self._add(["Ident", "Simp", "BandNH"], (s1[:, None] * band)[None], [None, pr, None], 0)
+        factored = []
         for p, pot in enumerate(self.potentials):
+            if getattr(pot, "Factors", None) is not None:
+                factored.append((pot.Factors, 1 + p))
+                continue
             kinds = [g.GetStorageId() for g in pot.GeometryList]
             pairs = [g.GetBasisPairs() if k in ("Simp", "Herm") else None for g, k in zip(pot.GeometryList, kinds)]
             self._add(kinds, pot.PotentialData, pairs, 1 + p)
+        self.nfactors = 0
+        if factored:
+            self._add_factored(factored)
         check(self.lib.pg_op_finalize(self.h), "pg_op_finalize")
+
+    def _add_factored(self, factored):
+        """All factors of the factorized terms in one call; factors with the same slot, weight
+        and angular coefficients (the radial kinetic energies and the nuclear attraction, all
+        1 on the diagonal) are summed into one radial operator."""
+        merged = {}
+        order = []
+        for fac, slot in factored:
+            rows, cols = fac.entries()
+            for q in range(fac.nfactors):
+                c = fac.coefs[q]
+                nz = np.nonzero(c)[0]
+                key = (slot, complex(fac.weights[q]), rows[nz].tobytes(), cols[nz].tobytes(), c[nz].tobytes())
+                if key in merged:
+                    merged[key][0] = merged[key][0] + fac.stencil[q]
+                else:
+                    merged[key] = [fac.stencil[q], rows[nz], cols[nz], c[nz], slot, complex(fac.weights[q])]
+                    order.append(key)
+        Q = len(order)
+        radial = np.ascontiguousarray(np.stack([merged[k][0] for k in order]), dtype=np.float64)
+        weights = np.ascontiguousarray(np.array([merged[k][5] for k in order], dtype=np.complex128))
+        slots = np.asarray([merged[k][4] for k in order], dtype=np.int32)
+        ef = np.concatenate([np.full(len(merged[k][1]), q, dtype=np.int32) for q, k in enumerate(order)])
+        er = np.ascontiguousarray(np.concatenate([merged[k][1] for k in order]), dtype=np.int32)
+        ec = np.ascontiguousarray(np.concatenate([merged[k][2] for k in order]), dtype=np.int32)
+        ev = np.ascontiguousarray(np.concatenate([merged[k][3] for k in order]), dtype=np.float64)
+        _, rp = nat.dptr(radial.reshape(-1))
+        _, wp = nat.dptr(weights.view(np.float64))
+        _, sp = nat.iptr(slots)
+        _, fp = nat.iptr(ef)
+        _, rowp = nat.iptr(er)
+        _, colp = nat.iptr(ec)
+        _, vp = nat.dptr(ev)
+        check(self.lib.pg_op_add_factored(self.h, Q, rp, wp, sp, len(ev), fp, rowp, colp, vp), "pg_op_add_factored")
+        self.nfactors = Q
+
+    def factored_info(self):
+        """dict: factors, angular entries, flops of the angular mix and of the radial stencil
+        per matvec, bytes of the radial factors and of the per-factor scratch."""
+        info = np.zeros(6)
+        _, ip = nat.dptr(info)
+        check(self.lib.pg_op_factored_info(self.h, ip), "pg_op_factored_info")
+        keys = ("factors", "entries", "flops_mix", "flops_radial", "radial_bytes", "scratch_bytes")
+        return dict(zip(keys, info.tolist()))
 
     def _add(self, kinds, data, pairs, slot):
         ids = "_".join(kinds)

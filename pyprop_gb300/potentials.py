@@ -230,6 +230,16 @@ class CoupledSphericalKineticEnergyEvaluator(CoupledPotentialBase):
             out[tuple(sl)] = np.squeeze(np.broadcast_to(v, shape)[tuple(sl)])
         return out
 
+    def factors(self, pos):
+        """Angular coefficient x radial function pairs that sum to the potential:
+        l1(l1+1) x 1/(2 m r1^2) and l2(l2+1) x 1/(2 m r2^2) on pairs of equal indices."""
+        r1, r2 = pos[self.radial_rank1], pos[self.radial_rank2]
+        lr = self._left_right()
+        same = np.array([(a.L, a.M, a.l1, a.l2) == (b.L, b.M, b.l1, b.l2) for a, b in lr], dtype=bool)
+        c1 = np.array([a.l1 * (a.l1 + 1.0) for a, _ in lr]) * same
+        c2 = np.array([a.l2 * (a.l2 + 1.0) for a, _ in lr]) * same
+        return [(1.0 / (2.0 * self.mass * r1 * r1), c1), (1.0 / (2.0 * self.mass * r2 * r2), c2)]
+
 
 class CustomPotentialEvaluationR12(CoupledPotentialBase):
     """Electron-electron repulsion ``1/|r1 - r2|`` in the multipole expansion
@@ -237,7 +247,7 @@ class CustomPotentialEvaluationR12(CoupledPotentialBase):
     times r<^l3 / r>^(l3+1)."""
 
     def GetPotentialValue(self, pos):
-        from .spherical import r12_angular_sum, r12_multipoles
+        from .spherical import r12_angular_factor, r12_multipoles
         r1, r2 = pos[self.radial_rank1], pos[self.radial_rank2]
         rmin, rmax = np.minimum(r1, r2), np.maximum(r1, r2)
         frac = rmin / rmax
@@ -246,7 +256,7 @@ class CustomPotentialEvaluationR12(CoupledPotentialBase):
         for p, (left, right) in enumerate(self._left_right()):
             v = 0.0
             for l3 in r12_multipoles(left, right):
-                c = r12_angular_sum(left, right, l3)
+                c = r12_angular_factor(left, right, l3)
                 if c != 0.0:
                     v = v + c * frac ** l3 / rmax
             if np.isscalar(v) and v == 0.0:
@@ -255,6 +265,22 @@ class CustomPotentialEvaluationR12(CoupledPotentialBase):
             sl[self.angular_rank] = p
             out[tuple(sl)] = np.squeeze(np.broadcast_to(v, shape)[tuple(sl)])
         return out
+
+    def factors(self, pos):
+        """One (radial function, angular coefficients) pair per multipole l3:
+        r<^l3 / r>^(l3+1) and the coefficient of each angular pair (zero outside its l3 range)."""
+        from .spherical import r12_angular_factor, r12_multipoles
+        r1, r2 = pos[self.radial_rank1], pos[self.radial_rank2]
+        rmin, rmax = np.minimum(r1, r2), np.maximum(r1, r2)
+        frac = rmin / rmax
+        lr = self._left_right()
+        table = {}
+        for p, (left, right) in enumerate(lr):
+            for l3 in r12_multipoles(left, right):
+                c = r12_angular_factor(left, right, l3)
+                if c != 0.0:
+                    table.setdefault(l3, np.zeros(len(lr)))[p] = c
+        return [(frac ** l3 / rmax, table[l3]) for l3 in sorted(table)]
 
 
 class CustomPotential_LaserLength(CoupledPotentialBase):
@@ -275,6 +301,13 @@ class CustomPotential_LaserLength(CoupledPotentialBase):
             sl[self.angular_rank] = p
             out[tuple(sl)] = np.squeeze(np.broadcast_to(I1 * r1 + I2 * r2, shape)[tuple(sl)])
         return out
+
+    def factors(self, pos):
+        """(r1, I1) and (r2, I2) over the angular pairs."""
+        from .spherical import laser_length_factors
+        r1, r2 = pos[self.radial_rank1], pos[self.radial_rank2]
+        II = np.array([laser_length_factors(left, right) for left, right in self._left_right()]).reshape(-1, 2)
+        return [(r1 + 0.0 * r2, II[:, 0].copy()), (r2 + 0.0 * r1, II[:, 1].copy())]
 
 
 for _cls in (CoupledSphericalCoulombPotential, CoupledSphericalKineticEnergyEvaluator, CustomPotentialEvaluationR12,

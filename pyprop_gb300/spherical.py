@@ -9,6 +9,7 @@ The l grid of the basis representation is ``|m|, |m|+1, ..., lmax``
 """
 from __future__ import annotations
 
+import functools
 import math
 
 import numpy as np
@@ -208,6 +209,61 @@ def r12_angular_sum(left, right, l3):
             if cur != 0.0:
                 s += cur * (-1.0) ** (m1p + m2p + m3)
     return s * coef
+
+
+@functools.lru_cache(maxsize=None)
+def wigner_6j(j1, j2, j3, j4, j5, j6):
+    """{j1 j2 j3; j4 j5 j6} for integer arguments (Racah's single sum, log-factorials)."""
+    def ok(a, b, c):
+        return abs(a - b) <= c <= a + b
+
+    if not (ok(j1, j2, j3) and ok(j1, j5, j6) and ok(j4, j2, j6) and ok(j4, j5, j3)):
+        return 0.0
+    f = _log_factorial
+
+    def tri(a, b, c):
+        return 0.5 * (f(a + b - c) + f(a - b + c) + f(-a + b + c) - f(a + b + c + 1))
+
+    pre = tri(j1, j2, j3) + tri(j1, j5, j6) + tri(j4, j2, j6) + tri(j4, j5, j3)
+    tmin = max(j1 + j2 + j3, j1 + j5 + j6, j4 + j2 + j6, j4 + j5 + j3)
+    tmax = min(j1 + j2 + j4 + j5, j2 + j3 + j5 + j6, j3 + j1 + j6 + j4)
+    total = 0.0
+    for t in range(tmin, tmax + 1):
+        den = (f(t - j1 - j2 - j3) + f(t - j1 - j5 - j6) + f(t - j4 - j2 - j6) + f(t - j4 - j5 - j3)
+               + f(j1 + j2 + j4 + j5 - t) + f(j2 + j3 + j5 + j6 - t) + f(j3 + j1 + j6 + j4 - t))
+        total += (-1.0) ** t * math.exp(pre + f(t + 1) - den)
+    return total
+
+
+def _log_factorial(n):
+    return math.lgamma(n + 1.0)
+
+
+@functools.lru_cache(maxsize=None)
+def reduced_c(lp, k, l):
+    """<lp || C^k || l> = (-1)^lp sqrt((2lp+1)(2l+1)) (lp k l; 0 0 0), the reduced matrix
+    element of the renormalised spherical harmonic C^k = sqrt(4 pi / (2k+1)) Y_k."""
+    three_j = (-1.0) ** (lp - k) / math.sqrt(2.0 * l + 1.0) * clebsch_gordan(lp, k, 0, 0, l, 0)
+    return (-1.0) ** lp * math.sqrt((2.0 * lp + 1.0) * (2.0 * l + 1.0)) * three_j
+
+
+def r12_angular_factor(left, right, l3):
+    """The same factor as :func:`r12_angular_sum`, in closed form: the matrix element of
+    P_l3(cos theta_12) = C^l3(1) . C^l3(2) between coupled states,
+    (-1)^(l1 + l2' + L) {l1' l2' L; l2 l1 l3} <l1'||C^l3||l1> <l2'||C^l3||l2>
+    (left = (l1', l2', L), right = (l1, l2, L)). One 6j symbol instead of the double m-sum
+    over four Clebsch-Gordan coefficients; the two agree to rounding."""
+    if left.L != right.L or left.M != right.M:
+        return 0.0
+    L = left.L
+    l1p, l2p, l1, l2 = left.l1, left.l2, right.l1, right.l2
+    c = reduced_c(l1p, l3, l1)
+    if c == 0.0:
+        return 0.0
+    c *= reduced_c(l2p, l3, l2)
+    if c == 0.0:
+        return 0.0
+    return (-1.0) ** (l1 + l2p + L) * wigner_6j(l1p, l2p, L, l2, l1, l3) * c
 
 
 def r12_multipoles(left, right):

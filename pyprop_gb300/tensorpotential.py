@@ -215,11 +215,26 @@ def _evaluator_from_section(conf):
     return pot
 
 
+def _project(bases, geoms, conf, data, ranks):
+    """Represent the grid axes ``ranks`` of ``data`` in their bases, last rank first
+    (``TensorPotentialGenerator.py:80-274``)."""
+    for r in reversed(ranks):
+        geom = geoms[r]
+        if not geom.UseGrid:
+            continue
+        diff = conf.Get("differentiation%d" % r) if conf.Exists("differentiation%d" % r) else 0
+        moved = np.moveaxis(data, r, -1 if isinstance(bases[r], BSplineRankBasis) else 0)
+        projected = bases[r].represent(moved, geom, diff)
+        data = np.moveaxis(projected, -1 if isinstance(bases[r], BSplineRankBasis) else 0, r)
+    return data
+
+
 def generate_potential(bases, conf):
     """Evaluate ``conf``'s potential on the tensor grid and represent it in the bases.
 
     Returns ``(geometry_list, PotentialData)`` with ``PotentialData`` of shape
-    ``(pairs_rank0, pairs_rank1, ...)``.
+    ``(pairs_rank0, pairs_rank1, ...)``, or ``(geometry_list, FactoredPotential)`` for a
+    two-electron term that factorizes (see :func:`factorize_potential`).
     """
     rank = len(bases)
     geoms = [bases[r].GetGeometryInfo(conf.Get("geometry%d" % r)) for r in range(rank)]
@@ -228,17 +243,132 @@ def generate_potential(bases, conf):
         evaluator.bind(bases, geoms)
     grids = [bases[r].grid(geoms[r]) for r in range(rank)]
     pos = tuple(np.asarray(g).reshape([-1 if rr == r else 1 for rr in range(rank)]) for r, g in enumerate(grids))
+    fac = factorize_potential(bases, geoms, conf, evaluator, pos)
+    if fac is not None:
+        return geoms, fac
     data = np.asarray(evaluator(pos), dtype=np.complex128)
     data = np.broadcast_to(data, tuple(len(g) for g in grids)).copy()
-    for r in reversed(range(rank)):
-        geom = geoms[r]
-        if not geom.UseGrid:
+    return geoms, np.ascontiguousarray(_project(bases, geoms, conf, data, list(range(rank))))
+
+
+class FactoredPotential:
+    """A two-electron term as a sum of factors, angular coefficients x one radial operator:
+    V(pair) = sum_q weights[q] * coefs[q][pair] * R_q.
+
+    The reference evaluates such terms per angular pair (the electron-electron repulsion's
+    multipoles in examples/tensor/helium_stabilization/coupledspherical.cpp:7-127, the laser
+    coupling's two radial functions in coupledlength.cpp:9-124, and every term that does not
+    depend on the angular pair) and stores one radial block per pair. Here each radial
+    operator is kept once, as ``stencil[q][i1][d1][d2][i2]`` (the coupling of output
+    (i1, i2) to input (i1 + d1 - k, i2 + d2 - k), real), with the coefficients per pair of
+    the angular geometry. ``reference_data()`` expands it to the reference layout
+    ``[pairs0][pairs1][pairs2]`` (small cases only: tests and the oracle)."""
+
+    def __init__(self, pairs, coefs, weights, stencil, radial_pairs, kb, nangular):
+        self.pairs = pairs            # [npairs][2] of the angular rank, or None (identity)
+        self.coefs = coefs            # [Q][npairs] float64
+        self.weights = weights        # [Q] complex128
+        self.stencil = stencil        # [Q][N1][2k+1][2k+1][N2] float64
+        self.radial_pairs = radial_pairs  # pair lists of ranks 1 and 2 (reference layout)
+        self.kb = kb
+        self.nangular = nangular
+
+    @property
+    def nfactors(self):
+        return len(self.weights)
+
+    def entries(self):
+        """(rows, cols) of the angular pairs."""
+        if self.pairs is None:
+            a = np.arange(self.nangular, dtype=np.int32)
+            return a, a
+        return self.pairs[:, 0].astype(np.int32), self.pairs[:, 1].astype(np.int32)
+
+    def reference_data(self):
+        kb = self.kb
+        p1, p2 = self.radial_pairs
+        i1, j1 = p1[:, 0], p1[:, 1]
+        i2, j2 = p2[:, 0], p2[:, 1]
+        m1 = np.abs(j1 - i1) <= kb
+        m2 = np.abs(j2 - i2) <= kb
+        out = np.zeros((self.coefs.shape[1], len(p1), len(p2)), dtype=np.complex128)
+        for q in range(self.nfactors):
+            blk = np.zeros((len(p1), len(p2)))
+            R = self.stencil[q]
+            blk[np.ix_(m1, m2)] = R[i1[m1][:, None], (j1 - i1 + kb)[m1][:, None], (j2 - i2 + kb)[m2][None, :],
+                                    i2[m2][None, :]]
+            out += (self.weights[q] * self.coefs[q])[:, None, None] * blk[None]
+        return out
+
+
+def _radial_stencil(data2, pairs1, pairs2, N1, N2, kb):
+    """Reference-layout radial block [pairs1][pairs2] -> stencil [N1][2k+1][2k+1][N2]."""
+    b = 2 * kb + 1
+    R = np.zeros((N1, b, b, N2), dtype=data2.dtype)
+    i1, j1 = pairs1[:, 0], pairs1[:, 1]
+    i2, j2 = pairs2[:, 0], pairs2[:, 1]
+    m1 = np.abs(j1 - i1) <= kb
+    m2 = np.abs(j2 - i2) <= kb
+    sub = data2[np.ix_(m1, m2)]
+    np.add.at(R, (i1[m1][:, None], (j1 - i1 + kb)[m1][:, None], (j2 - i2 + kb)[m2][None, :], i2[m2][None, :]), sub)
+    return R
+
+
+def factorize_potential(bases, geoms, conf, evaluator, pos):
+    """FactoredPotential for a rank-3 term on a coupled angular rank and two banded B-spline
+    ranks, or None (then the term is stored per pair as in the reference).
+
+    Factors come from the evaluator's ``factors(pos)`` (a list of (radial function on the
+    grid, coefficient per angular pair)); an evaluator that ignores the angular pair (no
+    ``needs_basis``) is one factor with coefficient 1. Each radial function is projected with
+    the section's geometries and differentiation exactly as the full potential would be, so
+    the expansion equals the per-pair data up to rounding. ``factorize = False`` in the
+    section keeps the per-pair form."""
+    if len(bases) != 3 or not isinstance(bases[0], CoupledSphericalRankBasis):
+        return None
+    if conf.Exists("factorize") and not conf.Get("factorize"):
+        return None
+    if not all(isinstance(bases[r], BSplineRankBasis) for r in (1, 2)):
+        return None
+    if any(geoms[r].StorageId not in ("Simp", "BandNH") or not geoms[r].UseGrid for r in (1, 2)):
+        return None
+    kbs = [bases[r].BSplineObject.MaxSplineOrder - 1 for r in (1, 2)]
+    if kbs[0] != kbs[1]:
+        return None
+    kb = kbs[0]
+    for r in (1, 2):
+        p = geoms[r].Pairs
+        if geoms[r].StorageId == "Simp" and np.any(np.abs(p[:, 1] - p[:, 0]) > kb):
+            return None
+    g0 = geoms[0]
+    npairs = 1 if g0.Pairs is None else len(g0.Pairs)
+    if hasattr(evaluator, "factors"):
+        facs = evaluator.factors(pos)
+    elif not getattr(evaluator, "needs_basis", False):
+        single = tuple(np.asarray(x)[:1] if i == 0 else x for i, x in enumerate(pos))
+        facs = [(np.asarray(evaluator(single)), np.ones(npairs))]
+    else:
+        return None
+    shape = (1, len(bases[1].grid(geoms[1])), len(bases[2].grid(geoms[2])))
+    N1, N2 = bases[1].size, bases[2].size
+    stencils, coefs, weights = [], [], []
+    for values, c in facs:
+        c = np.asarray(c, dtype=np.float64).reshape(-1)
+        if c.size != npairs or not np.any(c):
             continue
-        diff = conf.Get("differentiation%d" % r) if conf.Exists("differentiation%d" % r) else 0
-        moved = np.moveaxis(data, r, -1 if isinstance(bases[r], BSplineRankBasis) else 0)
-        projected = bases[r].represent(moved, geom, diff)
-        data = np.moveaxis(projected, -1 if isinstance(bases[r], BSplineRankBasis) else 0, r)
-    return geoms, np.ascontiguousarray(data)
+        v = np.broadcast_to(np.asarray(values, dtype=np.complex128), shape).copy()
+        data2 = _project(bases, geoms, conf, v, [1, 2])[0]
+        for part, w in ((data2.real, 1.0), (data2.imag, 1j)):
+            if not np.any(part):
+                continue
+            stencils.append(_radial_stencil(part, geoms[1].Pairs, geoms[2].Pairs, N1, N2, kb))
+            coefs.append(c)
+            weights.append(w)
+    if not stencils:
+        return None
+    return FactoredPotential(None if g0.Pairs is None else np.asarray(g0.Pairs, dtype=np.int32), np.asarray(coefs),
+                             np.asarray(weights, dtype=np.complex128), np.asarray(stencils),
+                             (geoms[1].Pairs, geoms[2].Pairs), kb, bases[0].size)
 
 
 class TensorPotential:
@@ -251,7 +381,8 @@ class TensorPotential:
     def __init__(self, psi):
         self.psi = psi
         self.GeometryList = None
-        self.PotentialData = None
+        self._data = None
+        self.Factors = None
         self.Name = None
         self.IsTimeDependent = False
         self.TimeFunction = None
@@ -267,7 +398,22 @@ class TensorPotential:
             self.TimeFunction = lambda t, _c=conf, _f=tf: _f(_c, t)
         self.Name = conf.name
         bases = self.psi.GetRepresentation().bases
-        self.GeometryList, self.PotentialData = generate_potential(bases, conf)
+        self.GeometryList, data = generate_potential(bases, conf)
+        if isinstance(data, FactoredPotential):
+            self.Factors = data
+        else:
+            self.PotentialData = data
+
+    @property
+    def PotentialData(self):
+        """Reference-layout data; a factorized term expands on first use (small cases)."""
+        if self._data is None and self.Factors is not None:
+            self._data = self.Factors.reference_data()
+        return self._data
+
+    @PotentialData.setter
+    def PotentialData(self, value):
+        self._data = value
 
     def SetupStep(self, timestep):
         self.BasisPairs = [g.GetBasisPairs() for g in self.GeometryList]
@@ -278,6 +424,8 @@ class TensorPotential:
 
     def CanConsolidate(self, other):
         """Same time dependence, same storage and basis pairs in every rank (``:128-163``)."""
+        if self.Factors is not None or other.Factors is not None:
+            return False  # factorized terms stay separate (their factors are merged on the device)
         if self.IsTimeDependent != other.IsTimeDependent:
             return False
         if self.IsTimeDependent and self.OriginalTimeFunction is not other.OriginalTimeFunction:

@@ -134,14 +134,16 @@ time_function = LaserFunctionSimpleLength
 
 def helium(lmax=2, L=(0,), nbsplines=20, rmax=20.0, order=7, quad_order_additional=10, z=2.0,
            propagator="PamPropagatorGPU", precision="fp64", timestep=0.01, duration=1.0, krylov_basis_size=20,
-           amplitude=0.0, frequency=1.0, pulse_duration=10.0, gmres_tolerance=1e-12):
+           amplitude=0.0, frequency=1.0, pulse_duration=10.0, gmres_tolerance=1e-12, factorize=True):
     """Two-electron (helium-like) model in the layout of
     examples/tensor/helium_stabilization/config.ini:1-188: coupled spherical harmonics
     (``DefaultCoupledIndexIterator(lmax, L, M=0)``) x B-splines x B-splines, radial kinetic
     energy of each electron, angular kinetic energy, nuclear attraction -z/r1 - z/r2, the
     electron-electron repulsion on ``SelectionRule_R12`` pairs and, with amplitude != 0, the
     length-gauge laser coupling on ``SelectionRule_LinearPolarizedField`` pairs with a sin^2
-    pulse (L must then hold neighbouring values)."""
+    pulse (L must then hold neighbouring values). factorize=False stores every term per
+    angular pair as the reference does (by default the two-electron terms are kept as angular
+    coefficients x shared radial operators)."""
     total = nbsplines - 3 if order == 7 else nbsplines - (order - 4)
     laser_name = ', "LaserPotential"' if amplitude else ""
     cayley = "Cayley" in str(propagator)
@@ -170,7 +172,7 @@ time_function = LaserFunctionLength
 """ if amplitude else ""
     rpart, xsize = exponential_linear_params_for(0.0, rmax, total, gamma=2.0, rpartition=min(10.0, rmax / 2))
     Ls = list(L)
-    return f"""
+    text = f"""
 [Representation]
 rank = 3
 type = core.CombinedRepresentation_3
@@ -262,3 +264,6 @@ angular_rank = 0
 radial_rank1 = 1
 radial_rank2 = 2
 {laser}"""
+    if not factorize:
+        text = text.replace('\nclassname = ', '\nfactorize = False\nclassname = ')
+    return text

@@ -77,4 +77,69 @@ def test_helium_with_laser_term_is_hermitian():
     H, S3, terms = helium_dense(prob)
     assert np.abs(H - H.conj().T).max() < 1e-12
     pots = prob.Propagator.BasePropagator.PotentialList
-    assert len(pots) == 3 and [p.IsTimeDependent for p in pots] == [False, False, True]
+    # factorized terms are not consolidated: 5 field-free terms, then the laser coupling
+    assert [p.IsTimeDependent for p in pots] == [False] * 5 + [True]
+    assert all(p.Factors is not None for p in pots)
+    plain = helium_problem(lmax=1, nbsplines=12, rmax=12.0, L=(0, 1), amplitude=0.1, frequency=1.0,
+                           pulse_duration=2.0, factorize=False).Propagator.BasePropagator.PotentialList
+    assert len(plain) == 3 and [p.IsTimeDependent for p in plain] == [False, False, True]
+
+
+def test_r12_closed_form_matches_m_sum():
+    """The 6j closed form of the multipole coefficient equals the reference's m-sum over four
+    Clebsch-Gordan coefficients (coupledspherical.cpp:63-92) on random coupled states."""
+    from pyprop_gb300.spherical import CoupledIndex, r12_angular_factor, r12_angular_sum, r12_multipoles
+    rng = np.random.default_rng(11)
+    n = 0
+    for _ in range(200):
+        L = int(rng.integers(0, 5))
+        while True:
+            l = [int(v) for v in rng.integers(0, 6, size=4)]
+            if abs(l[0] - l[1]) <= L <= l[0] + l[1] and abs(l[2] - l[3]) <= L <= l[2] + l[3]:
+                break
+        a, b = CoupledIndex(l[0], l[1], L, 0), CoupledIndex(l[2], l[3], L, 0)
+        for l3 in r12_multipoles(a, b):
+            assert abs(r12_angular_factor(a, b, l3) - r12_angular_sum(a, b, l3)) < 1e-13
+            n += 1
+    assert n > 300
+
+
+def test_factored_terms_expand_to_the_per_pair_data():
+    """Every two-electron term kept as angular coefficients x radial factors expands to the
+    reference-layout data that the per-pair generation produces (same geometries,
+    quadrature and differentiation), and the oracle's point-wise factored multiply equals the
+    per-pair tensor multiply."""
+    from collections import defaultdict
+    from oracle.operators import TermOracle, factored_multiply
+    pa = helium_problem(lmax=2, L=[0, 1], nbsplines=16, rmax=15.0, amplitude=0.05)
+    pb = helium_problem(lmax=2, L=[0, 1], nbsplines=16, rmax=15.0, amplitude=0.05, factorize=False)
+    la = pa.Propagator.BasePropagator.PotentialList
+    lb = pb.Propagator.BasePropagator.PotentialList
+    assert all(p.Factors is not None for p in la)
+    assert all(p.Factors is None for p in lb)
+    assert any(p.Factors.nfactors >= 4 for p in la)  # the multipoles l3 = 0..4
+
+    def key(p):
+        g0 = p.GeometryList[0].GetBasisPairs()
+        return tuple(g.GetStorageId() for g in p.GeometryList), g0.tobytes(), p.IsTimeDependent
+
+    sa, sb = defaultdict(lambda: 0), defaultdict(lambda: 0)
+    for p in la:
+        sa[key(p)] = sa[key(p)] + p.PotentialData
+    for p in lb:
+        sb[key(p)] = sb[key(p)] + p.PotentialData
+    assert set(sa) == set(sb)
+    for k in sb:
+        assert np.abs(sa[k] - sb[k]).max() <= 1e-13 * np.abs(sb[k]).max()
+    repr_ = pa.psi.GetRepresentation()
+    shape = repr_.GetFullShape()
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    scales = [1.0] + [0.7 if p.IsTimeDependent else 1.0 for p in la]
+    y1 = factored_multiply([(p.Factors, 1 + i) for i, p in enumerate(la)], scales, x, np.zeros(shape, complex))
+    y2 = np.zeros(shape, complex)
+    for p in lb:
+        t = TermOracle("_".join(g.GetStorageId() for g in p.GeometryList), p.PotentialData,
+                       [g.GetBasisPairs() for g in p.GeometryList], None, None, repr_.kb, shape=shape)
+        t.multiply(x, y2, 0.7 if p.IsTimeDependent else 1.0)
+    assert np.linalg.norm(y1 - y2) < 1e-12 * np.linalg.norm(y2)
