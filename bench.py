@@ -240,6 +240,76 @@ def profile_large_matvec():
                       "algorithmic_bytes": 8 * (op.stored_elements() + 2 * nang * N)}))
 
 
+TWO_ELECTRON = dict(lmax=10, L=tuple(range(6)), nbsplines=80, rmax=40.0)
+
+
+def _two_electron_operator(precision):
+    import pyprop_gb300 as pp
+    from pyprop_gb300.workloads import helium
+    prob = pp.Problem(pp.LoadString(helium(**TWO_ELECTRON)))
+    bp = prob.Propagator.BasePropagator
+    bp.SetupStep(0.01)
+    return prob, bp.device_operator(precision)
+
+
+def time_two_electron(torch, reps=5):
+    """The factorized two-electron Hamiltonian (coupled channels L <= 5, l1, l2 <= 10, 80
+    B-splines per electron: 291 channels, 1.86e6 coefficients; repulsion multipoles l3 <= 20
+    and the field-free terms as angular coefficients x radial band x band operators) applied
+    in complex64: (avg s per matvec, flops per matvec, info). The per-factor scratch (> L2)
+    makes a flush unnecessary; launches run back to back between one pair of events."""
+    from pyprop_gb300 import _native as nat
+    t0 = time.perf_counter()
+    prob, op = _two_electron_operator(nat.PG_FP32)
+    setup = time.perf_counter() - t0
+    shape = prob.psi.GetRepresentation().GetFullShape()
+    src = torch.randn(shape, dtype=torch.complex64, device="cuda")
+    dst = torch.zeros_like(src)
+    sc = op.scales(0.0)
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        op.matvec(sc, src, dst)
+    s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s_ev.record(stream)
+    for _ in range(reps):
+        op.matvec(sc, src, dst)
+    e_ev.record(stream)
+    e_ev.synchronize()
+    avg = s_ev.elapsed_time(e_ev) * 1e-3 / reps
+    info = op.factored_info()
+    info["setup_s"] = setup
+    info["shape"] = list(shape)
+    del op, prob
+    return avg, info["flops_mix"] + info["flops_radial"], info
+
+
+def profile_two_electron():
+    """Profiling entry point: three factorized two-electron matvecs (the sizes of
+    time_two_electron) after two warm-up launches."""
+    import torch
+    from pyprop_gb300 import _native as nat
+    prob, op = _two_electron_operator(nat.PG_FP32)
+    shape = prob.psi.GetRepresentation().GetFullShape()
+    src = torch.randn(shape, dtype=torch.complex64, device="cuda")
+    dst = torch.zeros_like(src)
+    sc = op.scales(0.0)
+    for _ in range(5):
+        op.matvec(sc, src, dst)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "two_electron", "info": op.factored_info()}))
+
+
+def fp32_fma_peak_tflops():
+    """Nominal FP32 FMA peak of the GB300 at the maximum SM clock: 152 SMs x 128 lanes x 2 flops
+    (no measured FP32 peak exists for this machine)."""
+    mhz = 2070.0
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            mhz = float(json.load(fh).get("sm_max_mhz", mhz))
+    return 152 * 128 * 2 * mhz * 1e6 / 1e12
+
+
 def profile_traffic(name):
     """dram bytes per launch recorded in a committed ncu summary (line 'dram_bytes_per_launch: N')."""
     path = os.path.join(ROOT, "profiles", name)
@@ -341,6 +411,7 @@ def run_ours(args):
     avg_mv, bytes_mv, variant_mv = time_matvec(torch, prob, flush)
     avg_ts, bytes_ts = time_block_solve(torch, prob, flush)
     avg_lg, bytes_lg, variant_lg = time_large_matvec(torch, flush)
+    two_e = time_two_electron(torch) if args.two_electron else None
     peak, peak_kind = measured_peaks()
 
     ens = run_ensemble(args, torch, flush) if args.ensemble > 0 else None
@@ -379,6 +450,15 @@ def run_ours(args):
                                     "avg_launch_us": 1e6 * avg_lg, "algorithmic_bytes": bytes_lg,
                                     "workload": "hydrogen lmax 300, 2000 B-splines (operator > L2; 20 launches back to back)",
                                     "variant": variant_lg[0], "tuning_us": variant_lg[1]},
+            "roofline_two_electron": None if two_e is None else {
+                "bound": "fma", "achieved": two_e[1] / two_e[0] / 1e12, "peak": fp32_fma_peak_tflops(),
+                "unit": "TFLOP/s", "frac": two_e[1] / two_e[0] / 1e12 / fp32_fma_peak_tflops(),
+                "peak_kind": "nominal FP32 FMA peak at the maximum SM clock (no measured FP32 peak)",
+                "kernels": "fact_mix_kernel<float> + fact_radial_kernel<float,6,128,32,8,4>",
+                "ms_per_matvec": 1e3 * two_e[0], "flops_per_matvec": two_e[1],
+                "workload": "helium-like, coupled L<=5, l1,l2<=10, 80 B-splines per electron (rank 3, factorized "
+                            "repulsion multipoles + field-free terms), complex64, 5 launches back to back",
+                "info": two_e[2]},
             "cpu_baseline": cpu,
             "ensemble": ens,
             "clocks": clk.summary(),
@@ -542,7 +622,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=300,
                     help="oracle Cayley steps timed on one host core for cpu_baseline (0 = skip)")
-    ap.add_argument("--profile", choices=["matvec_hbm"], default=None,
+    ap.add_argument("--two-electron", type=int, default=1, help="factorized two-electron matvec leg (0 = skip)")
+    ap.add_argument("--profile", choices=["matvec_hbm", "two_electron"], default=None,
                     help="profiling entry point instead of the benchmark")
     ap.add_argument("--eager", action="store_true",
                     help="host-driven GMRES loops (same kernels, visible one by one to a profiler)")
@@ -554,6 +635,10 @@ def main():
     if args.profile == "matvec_hbm":
         build_native.build()
         profile_large_matvec()
+        return
+    if args.profile == "two_electron":
+        build_native.build()
+        profile_two_electron()
         return
     if args.impl == "reference":
         run_reference(args)
