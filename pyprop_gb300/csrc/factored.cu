@@ -9,16 +9,21 @@
 // matrix, so the term costs one radial block per multipole instead of one per angular pair.
 //
 // One application, after the banded part of the operator has written dst:
-//   mix:    Z[q][a'] = w_q s_slot(q) sum_a A_q[a'][a] src[a]       (per point of the N1 x N2 grid)
-//   radial: dst[a'][i1][i2] += sum_q sum_{d1,d2} R_q[i1][d1][d2][i2] Z[q][a'][i1+d1-k][i2+d2-k]
-// The mix handles the factors in chunks of QC (accumulators in registers, src re-read per
-// chunk from L1/L2); rows without entries in a chunk skip it, and their scratch rows stay at
-// the zeros written at upload. The radial kernel is a 169-point stencil (k = 6) with
-// coefficients varying per point and shared by all channels: a CTA stages one radial row of
-// Z for CA channels (transposed, channels innermost) and the matching row of R in shared
-// memory, and each thread keeps PI consecutive points x PC channels of accumulators and a
-// sliding window of PI rows of Z in registers, so each shared-memory load feeds 4 PC (or PI x
-// PC / 2 for the window) fused multiply-adds. It is bound by FP32 (or FP64) FMA throughput.
+//   mix:    Z[q][p][a'] = w_q s_slot(q) sum_a A_q[a'][a] src[a][p]   (p: point of the N1 x N2 grid)
+//   radial: dst[a'][i1][i2] += sum_q sum_{d1,d2} R_q[i1][d1][d2][i2] Z[q][i1+d1-k][i2+d2-k][a']
+// The scratch Z keeps the channels innermost, so one radial row of Z for a tile of channels
+// is a plain 2-D box for the tensor-memory-access unit.
+//
+// mix: one warp per output channel a' and 32 points; the factors in chunks of QC accumulated
+// in registers (rows without entries in a chunk skip it; their scratch stays at the zeros
+// written at upload); the 4 warps of a CTA (4 consecutive channels) transpose through shared
+// memory so that each point's 4 channels leave as one 32-byte write.
+// radial: a 169-point stencil (k = 6) with coefficients varying per point and shared by all
+// channels. A CTA = one radial row i1, a tile of tw points of the last rank and CA channels;
+// per stage (factor q, row offset d1) one TMA box brings the Z rows [tw + 2k][CA] and one the
+// coefficient rows [2k+1][tw] into shared memory (double-buffered on two mbarriers, bounded
+// waits); each thread keeps PI consecutive points x PC channels of accumulators and a sliding
+// window of PI rows of Z in registers. Bound by FP32 (or FP64) FMA throughput.
 #include "pg_internal.cuh"
 
 #include <algorithm>
@@ -28,210 +33,287 @@
 namespace {
 
 const int QC = 16;  // factors per register chunk of the mix kernel
+const int CB = 4;   // channels per mix CTA (one warp each)
 
 struct FactArgs {
-    int Q, Qp, A, N1, N2, N2p, nct;
+    int Q, Qp, A, Ap, N1, N2, N2p, nct, tw;
     const int *row_ptr, *col, *qlo, *qhi, *slot;
     const void *coef;
     const unsigned char *chunk, *bflag;
-    const void *radial;
     const cxd *w;
     void *Z;
+    int *err;
 };
 
-FactArgs args_of(const FactDev &f)
+FactArgs args_of(const FactDev &f, int *err)
 {
     FactArgs a;
-    a.Q = f.Q; a.Qp = f.Qp; a.A = f.A; a.N1 = f.N1; a.N2 = f.N2; a.N2p = f.N2p; a.nct = f.nct;
+    a.Q = f.Q; a.Qp = f.Qp; a.A = f.A; a.Ap = f.Ap; a.N1 = f.N1; a.N2 = f.N2; a.N2p = f.N2p; a.nct = f.nct;
+    a.tw = f.tw;
     a.row_ptr = f.row_ptr; a.col = f.col; a.qlo = f.qlo; a.qhi = f.qhi; a.slot = f.slot;
-    a.coef = f.coef; a.chunk = f.chunk; a.bflag = f.bflag; a.radial = f.radial; a.w = f.w; a.Z = f.Z;
+    a.coef = f.coef; a.chunk = f.chunk; a.bflag = f.bflag; a.w = f.w; a.Z = f.Z; a.err = err;
     return a;
 }
 
-// Z[q][a][p] = w_q s_slot(q) / inv_scale * sum_e coef[e][q] x[col_e][p]; one CTA = 128 points
-// of one output row a.
-template <typename R>
-__global__ void __launch_bounds__(128) fact_mix_kernel(FactArgs f, pg_scales scales, const cxd *__restrict__ scales_dev,
-                                                       const cx<R> *__restrict__ x, const double *__restrict__ inv_scale)
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void fbar_init(unsigned long long *bar, unsigned count)
 {
-    const int a = blockIdx.y;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fbar_expect(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool fbar_try(unsigned long long *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok)
+                 : "r"(smem_addr(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+// bounded wait: gives up after 2^26 polls and reports through *err
+__device__ __forceinline__ bool fbar_wait(unsigned long long *bar, unsigned parity, int *err)
+{
+    for (long long it = 0; it < (1LL << 26); ++it)
+        if (fbar_try(bar, parity)) return true;
+    if (err) atomicExch(err, 1);
+    return false;
+}
+__device__ __forceinline__ void tma_2d(void *dst, const CUtensorMap *map, int c0, int c1, unsigned long long *bar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n"
+                 ::"r"(smem_addr(dst)), "l"(map), "r"(c0), "r"(c1), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tma_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                       unsigned long long *bar)
+{
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n"
+                 ::"r"(smem_addr(dst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// Z[q][p][a] = w_q s_slot(q) / inv_scale * sum_e coef[e][q] x[col_e][p]. CTA = CB warps (channels
+// a0 .. a0+CB) x 32 points.
+template <typename R>
+__global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales scales,
+                                                          const cxd *__restrict__ scales_dev,
+                                                          const cx<R> *__restrict__ x,
+                                                          const double *__restrict__ inv_scale)
+{
+    __shared__ cx<R> zt[QC][32][CB + 1];
+    const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
+    const int a0 = blockIdx.y * CB;
+    const int a = a0 + wrp;
     const long long NP = (long long)f.N1 * f.N2;
-    const long long p = (long long)blockIdx.x * 128 + threadIdx.x;
+    const long long p = (long long)blockIdx.x * 32 + lane;
     const bool live = p < NP;
     const double sc = inv_scale ? 1.0 / *inv_scale : 1.0;
-    const int e0 = f.row_ptr[a], e1 = f.row_ptr[a + 1];
     const int nch = f.Qp / QC;
     const R *__restrict__ coef = (const R *)f.coef;
     cx<R> *__restrict__ Z = (cx<R> *)f.Z;
     for (int k = 0; k < nch; ++k) {
-        if (!f.chunk[(size_t)a * nch + k]) continue;
+        bool any = false;
+        for (int r = 0; r < CB; ++r)
+            if (a0 + r < f.A && f.chunk[(size_t)(a0 + r) * nch + k]) any = true;
+        if (!any) continue;  // CTA-uniform: the scratch of these rows stays zero
         const int q0 = k * QC;
         cx<R> acc[QC];
 #pragma unroll
         for (int j = 0; j < QC; ++j) acc[j] = mk<R>((R)0, (R)0);
-        for (int e = e0; e < e1; ++e) {
-            if (f.qhi[e] < q0 || f.qlo[e] >= q0 + QC) continue;
-            const cx<R> xv = live ? x[(size_t)f.col[e] * NP + p] : mk<R>((R)0, (R)0);
-            const R *__restrict__ c = coef + (size_t)e * f.Qp + q0;
+        if (a < f.A && f.chunk[(size_t)a * nch + k]) {
+            for (int e = f.row_ptr[a]; e < f.row_ptr[a + 1]; ++e) {
+                if (f.qhi[e] < q0 || f.qlo[e] >= q0 + QC) continue;
+                const cx<R> xv = live ? x[(size_t)f.col[e] * NP + p] : mk<R>((R)0, (R)0);
+                const R *__restrict__ c = coef + (size_t)e * f.Qp + q0;
 #pragma unroll
-            for (int j = 0; j < QC; ++j) {
-                const R cj = c[j];
-                acc[j].x = fma(cj, xv.x, acc[j].x);
-                acc[j].y = fma(cj, xv.y, acc[j].y);
+                for (int j = 0; j < QC; ++j) {
+                    const R cj = c[j];
+                    acc[j].x = fma(cj, xv.x, acc[j].x);
+                    acc[j].y = fma(cj, xv.y, acc[j].y);
+                }
             }
         }
-        if (!live) continue;
 #pragma unroll
         for (int j = 0; j < QC; ++j) {
             const int q = q0 + j;
-            if (q >= f.Q) break;
-            const cxd s = scales_dev ? scales_dev[f.slot[q]] : scales.s[f.slot[q]];
-            const cxd ws = sc * (f.w[q] * s);
-            Z[((size_t)q * f.A + a) * NP + p] = cvt<R>(ws) * acc[j];
+            cx<R> v = mk<R>((R)0, (R)0);
+            if (q < f.Q) {
+                const cxd s = scales_dev ? scales_dev[f.slot[q]] : scales.s[f.slot[q]];
+                v = cvt<R>(sc * (f.w[q] * s)) * acc[j];
+            }
+            zt[j][lane][wrp] = v;
         }
+        __syncthreads();
+        // thread -> (point, factor) pairs; each writes the CB channels of one point
+        for (int u = threadIdx.x; u < 32 * QC; u += 32 * CB) {
+            const int j = u >> 5, pl = u & 31;
+            const int q = q0 + j;
+            const long long pp = (long long)blockIdx.x * 32 + pl;
+            if (q < f.Q && pp < NP) {
+                cx<R> *dst = Z + ((size_t)q * NP + pp) * f.Ap + a0;
+#pragma unroll
+                for (int r = 0; r < CB; ++r) dst[r] = zt[j][pl][r];
+            }
+        }
+        __syncthreads();
     }
 }
 
-// PC consecutive complex values from 16-byte aligned shared memory
-template <typename R, int PC>
-__device__ __forceinline__ void load_row(const cx<R> *p, cx<R> (&out)[PC])
+// tile shapes per precision: PI points x NV 16-byte vectors of channels per thread, 8 channel
+// lanes, CA = 8 x NV x (complex per vector) channels per CTA
+template <typename R> struct RadialTile;
+template <> struct RadialTile<float> { static const int PI = 8, NV = 2, PCV = 2, TCN = 8, CA = 32; };
+template <> struct RadialTile<double> { static const int PI = 4, NV = 2, PCV = 1, TCN = 8, CA = 16; };
+
+template <typename R>
+__host__ __device__ inline size_t rad_round128(size_t b) { return (b + 127) & ~(size_t)127; }
+
+// bytes of one stage's Z box and coefficient box
+template <typename R>
+__host__ __device__ inline size_t rad_zbytes(int tw, int kb)
 {
-    if constexpr (sizeof(R) == 4) {
-        static_assert(PC % 2 == 0, "float rows load in pairs");
-#pragma unroll
-        for (int h = 0; h < PC / 2; ++h) {
-            const float4 v = reinterpret_cast<const float4 *>(p)[h];
-            out[2 * h] = mk<R>(v.x, v.y);
-            out[2 * h + 1] = mk<R>(v.z, v.w);
-        }
-    } else {
-#pragma unroll
-        for (int h = 0; h < PC; ++h) out[h] = p[h];
-    }
+    return (size_t)(tw + 2 * kb) * RadialTile<R>::CA * sizeof(cx<R>);
+}
+template <typename R>
+__host__ __device__ inline size_t rad_rbytes(int tw, int kb)
+{
+    return (size_t)(2 * kb + 1) * tw * sizeof(R);
 }
 
-template <typename R, int PI>
-__device__ __forceinline__ void load_coefs(const R *p, R (&out)[PI])
+// One CTA = radial row i1 (blockIdx.x), tw points of the last rank (blockIdx.y), CA channels
+// (blockIdx.z); thread = PI consecutive points x NV vectors of channels. blockDim = tw / PI x 8.
+template <typename R, int KB>
+__global__ void __launch_bounds__(128, 2) fact_radial_kernel(FactArgs f, cx<R> *__restrict__ y,
+                                                             const __grid_constant__ CUtensorMap zmap,
+                                                             const __grid_constant__ CUtensorMap rmap)
 {
-    if constexpr (sizeof(R) == 4) {
-        static_assert(PI % 4 == 0, "float coefficients load in fours");
-#pragma unroll
-        for (int h = 0; h < PI / 4; ++h) {
-            const float4 v = reinterpret_cast<const float4 *>(p)[h];
-            out[4 * h] = v.x; out[4 * h + 1] = v.y; out[4 * h + 2] = v.z; out[4 * h + 3] = v.w;
-        }
-    } else {
-        static_assert(PI % 2 == 0, "double coefficients load in pairs");
-#pragma unroll
-        for (int h = 0; h < PI / 2; ++h) {
-            const double2 v = reinterpret_cast<const double2 *>(p)[h];
-            out[2 * h] = v.x; out[2 * h + 1] = v.y;
-        }
-    }
-}
-
-// Shared-memory position (in complex elements) of window row j, channel c. Rows are CA + 2
-// complex long (a multiple of 16 bytes); every other block of PI rows is shifted by 16 bytes so
-// that the four point groups of a warp, which read rows PI apart, fall on different banks.
-template <typename R, int CA, int PI>
-__device__ __forceinline__ int zpos(int j, int c)
-{
-    constexpr int OFF = 16 / (int)sizeof(cx<R>);
-    return j * (CA + 2) + ((j / PI) & 1) * OFF + c;
-}
-
-// One CTA = radial row i1 (blockIdx.x), T2 points of the last rank (blockIdx.y), CA channels
-// (blockIdx.z); thread = PI consecutive points x PC channels.
-template <typename R, int KB, int T2, int CA, int PI, int PC>
-__global__ void __launch_bounds__((T2 / PI) * (CA / PC), 2)
-    fact_radial_kernel(FactArgs f, cx<R> *__restrict__ y)
-{
+    typedef RadialTile<R> T;
     constexpr int B = 2 * KB + 1;
-    constexpr int TW = T2 + 2 * KB;
-    constexpr int NT = (T2 / PI) * (CA / PC);
-    constexpr int TCN = CA / PC;
-    constexpr int ZELEMS = TW * (CA + 2) + 16 / (int)sizeof(cx<R>);
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    cx<R> *zs = reinterpret_cast<cx<R> *>(smem_raw);
-    R *rs = reinterpret_cast<R *>(smem_raw + (size_t)ZELEMS * sizeof(cx<R>));
-
-    const int i1 = blockIdx.x, t0 = blockIdx.y * T2, c0 = blockIdx.z * CA;
-    const int tid = threadIdx.x;
-    const int tc = tid % TCN, ti = tid / TCN;
-    const int N1 = f.N1, N2 = f.N2, A = f.A;
-    const long long NP = (long long)N1 * N2;
-    const cx<R> *__restrict__ Z = (const cx<R> *)f.Z;
-    const R *__restrict__ radial = (const R *)f.radial;
-
+    constexpr int PI = T::PI, NV = T::NV, PCV = T::PCV, TCN = T::TCN, CA = T::CA, PC = NV * PCV;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned long long *bar = (unsigned long long *)smem_raw;
+    const int tw = f.tw;
+    const unsigned zbytes = (unsigned)rad_zbytes<R>(tw, KB), rbytes = (unsigned)rad_rbytes<R>(tw, KB);
+    const size_t zb = rad_round128<R>(zbytes), stage = zb + rad_round128<R>(rbytes);
+    unsigned char *buf = smem_raw + 128;
+    const int tid = threadIdx.x, tc = tid % TCN, ti = tid / TCN;
+    const int i1 = blockIdx.x, t0 = blockIdx.y * tw, ct = blockIdx.z, c0 = ct * CA;
+    const int N1 = f.N1, N2 = f.N2;
+    if (tid == 0) {
+        fbar_init(&bar[0], 1);
+        fbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    // stages (q, d1): factors with a nonzero row in this channel tile, rows inside the grid
+    auto advance = [&](int &q, int &d1) {
+        for (;;) {
+            if (++d1 == B) {
+                d1 = 0;
+                ++q;
+            }
+            if (q >= f.Q) return;
+            if (!f.bflag[(size_t)q * f.nct + ct]) {
+                d1 = B - 1;
+                continue;
+            }
+            const int j1 = i1 + d1 - KB;
+            if (j1 >= 0 && j1 < N1) return;
+        }
+    };
+    auto issue = [&](int s, int q, int d1) {
+        unsigned char *dst = buf + (size_t)s * stage;
+        fbar_expect(&bar[s], zbytes + rbytes);
+        tma_3d(dst, &zmap, 2 * c0, t0 - KB, q * N1 + i1 + d1 - KB, &bar[s]);
+        tma_2d(dst + zb, &rmap, t0, ((q * N1 + i1) * B + d1) * B, &bar[s]);
+    };
     cx<R> acc[PI][PC];
 #pragma unroll
     for (int p = 0; p < PI; ++p)
 #pragma unroll
         for (int c = 0; c < PC; ++c) acc[p][c] = mk<R>((R)0, (R)0);
-
-    for (int q = 0; q < f.Q; ++q) {
-        if (!f.bflag[(size_t)q * f.nct + blockIdx.z]) continue;
-        for (int d1 = 0; d1 < B; ++d1) {
-            const int j1 = i1 + d1 - KB;
-            if (j1 < 0 || j1 >= N1) continue;
-            const R *__restrict__ Rrow = radial + (((size_t)q * N1 + i1) * B + d1) * B * (size_t)f.N2p;
-            __syncthreads();  // the previous stage's reads are done
-            for (int idx = tid; idx < CA * TW; idx += NT) {
-                const int c = idx / TW, j = idx - c * TW;
-                const int ch = c0 + c, j2 = t0 - KB + j;
-                cx<R> v = mk<R>((R)0, (R)0);
-                if (ch < A && j2 >= 0 && j2 < N2) v = Z[((size_t)q * A + ch) * NP + (size_t)j1 * N2 + j2];
-                zs[zpos<R, CA, PI>(j, c)] = v;
+    int q = 0, d1 = -1;
+    advance(q, d1);
+    if (tid == 0 && q < f.Q) issue(0, q, d1);
+    for (int k = 0; q < f.Q; ++k) {
+        const int s = k & 1;
+        int qn = q, dn = d1;
+        advance(qn, dn);
+        // the other buffer was released by the barrier at the end of the previous stage
+        if (tid == 0 && qn < f.Q) issue(s ^ 1, qn, dn);
+        const unsigned parity = (unsigned)(k >> 1) & 1u;
+        const bool ok = fbar_wait(&bar[s], parity, f.err);
+        if (__syncthreads_or(ok ? 0 : 1)) {
+            // a wait ran out: let the copies in flight land (bounded), then leave
+            if (!ok) fbar_wait(&bar[s], parity, f.err);
+            if (tid == 0 && qn < f.Q) fbar_wait(&bar[s ^ 1], (unsigned)((k + 1) >> 1) & 1u, f.err);
+            return;
+        }
+        const cx<R> *zs = (const cx<R> *)(buf + (size_t)s * stage);
+        const R *rs = (const R *)(buf + (size_t)s * stage + zb);
+        cx<R> win[PI + B - 1][PC];
+        auto load_row = [&](int j, cx<R> (&out)[PC]) {
+#pragma unroll
+            for (int h = 0; h < NV; ++h) {
+                const cx<R> *src = zs + (size_t)j * CA + (h * TCN + tc) * PCV;
+                if constexpr (sizeof(R) == 4) {
+                    const float4 v = *reinterpret_cast<const float4 *>(src);
+                    out[h * PCV] = mk<R>(v.x, v.y);
+                    out[h * PCV + 1] = mk<R>(v.z, v.w);
+                } else {
+                    out[h * PCV] = src[0];
+                }
             }
-            for (int idx = tid; idx < B * T2; idx += NT) {
-                const int d2 = idx / T2, i = idx - d2 * T2;
-                const int i2 = t0 + i;
-                rs[idx] = i2 < N2 ? Rrow[(size_t)d2 * f.N2p + i2] : (R)0;
+        };
+#pragma unroll
+        for (int r = 0; r < PI - 1; ++r) load_row(ti * PI + r, win[r]);
+#pragma unroll
+        for (int d2 = 0; d2 < B; ++d2) {
+            load_row(ti * PI + d2 + PI - 1, win[d2 + PI - 1]);
+            R rv[PI];
+            const R *rp = rs + d2 * tw + ti * PI;
+            if constexpr (sizeof(R) == 4) {
+#pragma unroll
+                for (int h = 0; h < PI / 4; ++h) {
+                    const float4 v = reinterpret_cast<const float4 *>(rp)[h];
+                    rv[4 * h] = v.x; rv[4 * h + 1] = v.y; rv[4 * h + 2] = v.z; rv[4 * h + 3] = v.w;
+                }
+            } else {
+#pragma unroll
+                for (int h = 0; h < PI / 2; ++h) {
+                    const double2 v = reinterpret_cast<const double2 *>(rp)[h];
+                    rv[2 * h] = v.x; rv[2 * h + 1] = v.y;
+                }
             }
-            __syncthreads();
-            cx<R> win[PI + B - 1][PC];
 #pragma unroll
-            for (int r = 0; r < PI - 1; ++r) load_row<R, PC>(zs + zpos<R, CA, PI>(ti * PI + r, tc * PC), win[r]);
+            for (int p = 0; p < PI; ++p)
 #pragma unroll
-            for (int d2 = 0; d2 < B; ++d2) {
-                load_row<R, PC>(zs + zpos<R, CA, PI>(ti * PI + d2 + PI - 1, tc * PC), win[d2 + PI - 1]);
-                R rv[PI];
-                load_coefs<R, PI>(rs + d2 * T2 + ti * PI, rv);
+                for (int c = 0; c < PC; ++c) {
+                    acc[p][c].x = fma(rv[p], win[p + d2][c].x, acc[p][c].x);
+                    acc[p][c].y = fma(rv[p], win[p + d2][c].y, acc[p][c].y);
+                }
+        }
+        __syncthreads();  // buffer s is free for the stage after next
+        q = qn;
+        d1 = dn;
+    }
+    const long long NP = (long long)N1 * N2;
 #pragma unroll
-                for (int p = 0; p < PI; ++p)
+    for (int h = 0; h < NV; ++h)
 #pragma unroll
-                    for (int c = 0; c < PC; ++c) {
-                        acc[p][c].x = fma(rv[p], win[p + d2][c].x, acc[p][c].x);
-                        acc[p][c].y = fma(rv[p], win[p + d2][c].y, acc[p][c].y);
-                    }
+        for (int v = 0; v < PCV; ++v) {
+            const int ch = c0 + (h * TCN + tc) * PCV + v;
+            if (ch >= f.A) continue;
+            cx<R> *__restrict__ yr = y + (size_t)ch * NP + (size_t)i1 * N2;
+#pragma unroll
+            for (int p = 0; p < PI; ++p) {
+                const int i2 = t0 + ti * PI + p;
+                if (i2 < N2) yr[i2] = yr[i2] + acc[p][h * PCV + v];
             }
         }
-    }
-#pragma unroll
-    for (int c = 0; c < PC; ++c) {
-        const int ch = c0 + tc * PC + c;
-        if (ch >= A) continue;
-        cx<R> *__restrict__ yr = y + (size_t)ch * NP + (size_t)i1 * N2;
-#pragma unroll
-        for (int p = 0; p < PI; ++p) {
-            const int i2 = t0 + ti * PI + p;
-            if (i2 < N2) yr[i2] = yr[i2] + acc[p][c];
-        }
-    }
-}
-
-// tile shapes per precision
-template <typename R> struct RadialTile;
-template <> struct RadialTile<float> { static const int T2 = 128, CA = 32, PI = 8, PC = 4; };
-template <> struct RadialTile<double> { static const int T2 = 64, CA = 16, PI = 4, PC = 2; };
-
-template <typename R>
-size_t radial_smem(int kb)
-{
-    typedef RadialTile<R> T;
-    const int TW = T::T2 + 2 * kb;
-    const size_t z = ((size_t)TW * (T::CA + 2) + 16 / sizeof(cx<R>)) * sizeof(cx<R>);
-    return z + (size_t)(2 * kb + 1) * T::T2 * sizeof(R);
 }
 
 template <typename R>
@@ -240,22 +322,17 @@ int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, c
 {
     typedef RadialTile<R> T;
     const FactDev &fd = op->fact;
-    const FactArgs fa = args_of(fd);
+    const FactArgs fa = args_of(fd, op->ctx->d_err);
     cudaStream_t s = op->ctx->stream;
     const long long NP = (long long)fd.N1 * fd.N2;
-    dim3 g1((unsigned)((NP + 127) / 128), (unsigned)fd.A);
-    fact_mix_kernel<R><<<g1, 128, 0, s>>>(fa, scales, scales_dev, (const cx<R> *)src, inv_scale);
+    dim3 g1((unsigned)((NP + 31) / 32), (unsigned)((fd.A + CB - 1) / CB));
+    fact_mix_kernel<R><<<g1, 32 * CB, 0, s>>>(fa, scales, scales_dev, (const cx<R> *)src, inv_scale);
     op->ctx->launches++;
     PG_TRY(pg_check_launch(op->ctx));
-    dim3 g2((unsigned)fd.N1, (unsigned)((fd.N2 + T::T2 - 1) / T::T2), (unsigned)fd.nct);
-    const int nt = (T::T2 / T::PI) * (T::CA / T::PC);
-    const size_t sm = radial_smem<R>(op->kb);
-    switch (op->kb) {
-    case 6:
-        fact_radial_kernel<R, 6, T::T2, T::CA, T::PI, T::PC><<<g2, nt, sm, s>>>(fa, (cx<R> *)dst);
-        break;
-    default: return PG_ERR_STORAGE;
-    }
+    dim3 g2((unsigned)fd.N1, (unsigned)fd.ntiles, (unsigned)fd.nct);
+    const int nt = fd.tw / T::PI * T::TCN;
+    if (op->kb != 6) return PG_ERR_STORAGE;
+    fact_radial_kernel<R, 6><<<g2, nt, fd.radial_smem, s>>>(fa, (cx<R> *)dst, fd.zmap, fd.rmap);
     op->ctx->launches++;
     return pg_check_launch(op->ctx);
 }
@@ -345,8 +422,15 @@ int pg_factored_finalize(pg_op *op)
     f.A = A; f.N1 = N1; f.N2 = N2; f.Q = Q;
     f.Qp = (Q + QC - 1) / QC * QC;
     f.N2p = (N2 + 3) & ~3;
+    f.Ap = (A + CB - 1) / CB * CB;
     const int CA = fp64 ? RadialTile<double>::CA : RadialTile<float>::CA;
+    const int PI = fp64 ? RadialTile<double>::PI : RadialTile<float>::PI;
     f.nct = (A + CA - 1) / CA;
+    // point tiles of the last rank: at most 16 point groups (128 threads) per CTA, as even as
+    // the multiple of PI allows
+    const int tmax = 16 * PI;
+    f.ntiles = (N2 + tmax - 1) / tmax;
+    f.tw = ((N2 + f.ntiles - 1) / f.ntiles + PI - 1) / PI * PI;
     // angular rows: coefficient vector over the factors per (row, col)
     std::vector<std::map<int, std::vector<double>>> rows(A);
     for (int q = 0; q < Q; ++q) {
@@ -423,7 +507,6 @@ int pg_factored_finalize(pg_op *op)
     f.flops_radial = 4.0 * radial_terms;     // per in-grid stencil point and nonzero row
     const size_t esz = fp64 ? sizeof(double) : sizeof(float);
     f.radial_bytes = (double)rad.size() * esz;
-    f.z_bytes = (double)Q * A * NP * 2 * esz;
     std::vector<double> w(2 * (size_t)Q);
     std::vector<int> slot(Q);
     for (int q = 0; q < Q; ++q) {
@@ -442,16 +525,64 @@ int pg_factored_finalize(pg_op *op)
     PG_CUDA_TRY(cudaMemcpy(f.w, w.data(), sizeof(cxd) * Q, cudaMemcpyHostToDevice));
     PG_TRY(fp64 ? upload_real<double>(&f.coef, coef) : upload_real<float>(&f.coef, coef));
     PG_TRY(fp64 ? upload_real<double>(&f.radial, rad) : upload_real<float>(&f.radial, rad));
-    const size_t zbytes = (size_t)Q * A * (size_t)N1 * N2 * 2 * esz;
+    const size_t zbytes = (size_t)Q * f.Ap * (size_t)N1 * N2 * 2 * esz;
     PG_CUDA_TRY(cudaMalloc(&f.Z, zbytes));
     PG_CUDA_TRY(cudaMemset(f.Z, 0, zbytes));  // rows without entries are read as zeros
-    const size_t sm = fp64 ? radial_smem<double>(kb) : radial_smem<float>(kb);
+    f.z_bytes = (double)zbytes;
+    // shared memory: two barriers, then two stages of (Z box, coefficient box)
     if (fp64)
-        PG_CUDA_TRY(cudaFuncSetAttribute(fact_radial_kernel<double, 6, 64, 16, 4, 2>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        f.radial_smem = 128 + 2 * (rad_round128<double>(rad_zbytes<double>(f.tw, kb)) +
+                                   rad_round128<double>(rad_rbytes<double>(f.tw, kb)));
     else
-        PG_CUDA_TRY(cudaFuncSetAttribute(fact_radial_kernel<float, 6, 128, 32, 8, 4>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        f.radial_smem = 128 + 2 * (rad_round128<float>(rad_zbytes<float>(f.tw, kb)) +
+                                   rad_round128<float>(rad_rbytes<float>(f.tw, kb)));
+    int dev = 0, optin = 0;
+    PG_CUDA_TRY(cudaGetDevice(&dev));
+    PG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (f.radial_smem > (size_t)optin) return PG_ERR_SHAPE;
+    if (fp64)
+        PG_CUDA_TRY(cudaFuncSetAttribute(fact_radial_kernel<double, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    else
+        PG_CUDA_TRY(cudaFuncSetAttribute(fact_radial_kernel<float, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    // TMA maps. Z as [Q * N1][N2][2 Ap] reals: box = 2 CA reals x (tw + 2k) points x 1 row,
+    // the innermost coordinate 2 c0 (c0 a multiple of CA: 256-byte aligned); rows before 0 and
+    // past N2 read as zeros. Coefficients as [Q * N1 * b * b][N2p] reals: box = tw x b.
+    typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult qr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr) != cudaSuccess ||
+        qr != cudaDriverEntryPointSuccess || !fn) {
+        pg_set_last_error(cudaErrorNotSupported, "cuTensorMapEncodeTiled", __FILE__, __LINE__);
+        return PG_ERR_CUDA;
+    }
+    const CUtensorMapDataType dt = fp64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const cuuint32_t estr[3] = {1, 1, 1};
+    {
+        const cuuint64_t dims[3] = {(cuuint64_t)2 * f.Ap, (cuuint64_t)N2, (cuuint64_t)Q * N1};
+        const cuuint64_t strides[2] = {(cuuint64_t)2 * f.Ap * esz, (cuuint64_t)2 * f.Ap * esz * N2};
+        const cuuint32_t box[3] = {(cuuint32_t)(2 * CA), (cuuint32_t)(f.tw + 2 * kb), 1};
+        CUresult r = ((EncodeTiled)fn)(&f.zmap, dt, 3, f.Z, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) {
+            pg_set_last_error(cudaErrorInvalidValue, "cuTensorMapEncodeTiled(scratch)", __FILE__, __LINE__);
+            return PG_ERR_CUDA;
+        }
+    }
+    {
+        const cuuint64_t dims[2] = {(cuuint64_t)f.N2p, (cuuint64_t)Q * N1 * b * b};
+        const cuuint64_t strides[1] = {(cuuint64_t)f.N2p * esz};
+        const cuuint32_t box[2] = {(cuuint32_t)f.tw, (cuuint32_t)b};
+        CUresult r = ((EncodeTiled)fn)(&f.rmap, dt, 2, f.radial, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) {
+            pg_set_last_error(cudaErrorInvalidValue, "cuTensorMapEncodeTiled(radial)", __FILE__, __LINE__);
+            return PG_ERR_CUDA;
+        }
+    }
     return PG_OK;
 }
 

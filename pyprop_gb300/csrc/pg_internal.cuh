@@ -132,14 +132,17 @@ struct HostFactor {
 
 // device form of all factors of an operator (factored.cu)
 struct FactDev {
-    int Q = 0, Qp = 0, A = 0, N1 = 0, N2 = 0, N2p = 0, nct = 0, nE = 0;
+    int Q = 0, Qp = 0, A = 0, Ap = 0, N1 = 0, N2 = 0, N2p = 0, nct = 0, nE = 0;
+    int tw = 0, ntiles = 0;        // radial kernel: points of the last rank per CTA, tiles per row
+    size_t radial_smem = 0;        // its dynamic shared memory
+    CUtensorMap zmap, rmap;        // TMA maps of the scratch and of the radial factors
     int *row_ptr = nullptr, *col = nullptr, *qlo = nullptr, *qhi = nullptr, *slot = nullptr;
     void *coef = nullptr;             // [nE][Qp] real (operator precision)
     unsigned char *chunk = nullptr;   // [A][Qp / chunk] rows that have entries in the chunk
     unsigned char *bflag = nullptr;   // [Q][nct] channel tiles with a nonzero row
     void *radial = nullptr;           // [Q][N1][b][b][N2p] real
     cxd *w = nullptr;                 // [Q]
-    void *Z = nullptr;                // [Q][A][N1*N2] complex scratch
+    void *Z = nullptr;                // [Q][N1*N2][Ap] complex scratch (channels innermost)
     double flops_mix = 0, flops_radial = 0, radial_bytes = 0, z_bytes = 0;
 };
 
