@@ -95,24 +95,34 @@ __device__ __forceinline__ void tma_3d(void *dst, const CUtensorMap *map, int c0
                  : "memory");
 }
 
+// points per lane of the mix kernel (a 16-byte load of x per lane for FP32)
+template <typename R> struct MixTile;
+template <> struct MixTile<float> { static const int PPL = 2; };
+template <> struct MixTile<double> { static const int PPL = 1; };
+
 // Z[q][p][a] = w_q s_slot(q) / inv_scale * sum_e coef[e][q] x[col_e][p]. CTA = CB warps (channels
-// a0 .. a0+CB) x 32 points.
+// a0 .. a0+CB) x 32 PPL points; entry e = (col, qlo, qhi) packed as one int4, its coefficients
+// loaded as 16-byte vectors (uniform across the warp).
 template <typename R>
 __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales scales,
                                                           const cxd *__restrict__ scales_dev,
                                                           const cx<R> *__restrict__ x,
                                                           const double *__restrict__ inv_scale)
 {
-    __shared__ cx<R> zt[QC][32][CB + 1];
+    constexpr int PPL = MixTile<R>::PPL;
+    constexpr int TP = 32 * PPL;
+    __shared__ cx<R> zt[QC][TP][CB + 1];
     const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
     const int a0 = blockIdx.y * CB;
     const int a = a0 + wrp;
     const long long NP = (long long)f.N1 * f.N2;
-    const long long p = (long long)blockIdx.x * 32 + lane;
-    const bool live = p < NP;
+    const long long p0 = (long long)blockIdx.x * TP + (long long)lane * PPL;  // this lane's first point
+    const bool live = p0 < NP;
+    const bool vec = (NP % PPL) == 0;  // 16-byte aligned pairs of points in every row
     const double sc = inv_scale ? 1.0 / *inv_scale : 1.0;
     const int nch = f.Qp / QC;
     const R *__restrict__ coef = (const R *)f.coef;
+    const int4 *__restrict__ meta = (const int4 *)f.col;
     cx<R> *__restrict__ Z = (cx<R> *)f.Z;
     for (int k = 0; k < nch; ++k) {
         bool any = false;
@@ -120,38 +130,70 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
             if (a0 + r < f.A && f.chunk[(size_t)(a0 + r) * nch + k]) any = true;
         if (!any) continue;  // CTA-uniform: the scratch of these rows stays zero
         const int q0 = k * QC;
-        cx<R> acc[QC];
+        cx<R> acc[QC][PPL];
 #pragma unroll
-        for (int j = 0; j < QC; ++j) acc[j] = mk<R>((R)0, (R)0);
+        for (int j = 0; j < QC; ++j)
+#pragma unroll
+            for (int u = 0; u < PPL; ++u) acc[j][u] = mk<R>((R)0, (R)0);
         if (a < f.A && f.chunk[(size_t)a * nch + k]) {
             for (int e = f.row_ptr[a]; e < f.row_ptr[a + 1]; ++e) {
-                if (f.qhi[e] < q0 || f.qlo[e] >= q0 + QC) continue;
-                const cx<R> xv = live ? x[(size_t)f.col[e] * NP + p] : mk<R>((R)0, (R)0);
-                const R *__restrict__ c = coef + (size_t)e * f.Qp + q0;
-#pragma unroll
-                for (int j = 0; j < QC; ++j) {
-                    const R cj = c[j];
-                    acc[j].x = fma(cj, xv.x, acc[j].x);
-                    acc[j].y = fma(cj, xv.y, acc[j].y);
+                const int4 m = meta[e];  // col, qlo, qhi
+                if (m.z < q0 || m.y >= q0 + QC) continue;
+                cx<R> xv[PPL];
+                if constexpr (PPL == 2) {
+                    const cx<R> *xr = x + (size_t)m.x * NP + p0;
+                    if (vec && live) {
+                        const float4 v = *reinterpret_cast<const float4 *>(xr);
+                        xv[0] = mk<R>(v.x, v.y);
+                        xv[1] = mk<R>(v.z, v.w);
+                    } else {
+                        xv[0] = live ? xr[0] : mk<R>((R)0, (R)0);
+                        xv[1] = (p0 + 1 < NP) ? xr[1] : mk<R>((R)0, (R)0);
+                    }
+                } else {
+                    xv[0] = live ? x[(size_t)m.x * NP + p0] : mk<R>((R)0, (R)0);
                 }
+                R c[QC];
+                const R *__restrict__ cp = coef + (size_t)e * f.Qp + q0;
+                if constexpr (sizeof(R) == 4) {
+#pragma unroll
+                    for (int h = 0; h < QC / 4; ++h) {
+                        const float4 v = reinterpret_cast<const float4 *>(cp)[h];
+                        c[4 * h] = v.x; c[4 * h + 1] = v.y; c[4 * h + 2] = v.z; c[4 * h + 3] = v.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int h = 0; h < QC / 2; ++h) {
+                        const double2 v = reinterpret_cast<const double2 *>(cp)[h];
+                        c[2 * h] = v.x; c[2 * h + 1] = v.y;
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < QC; ++j)
+#pragma unroll
+                    for (int u = 0; u < PPL; ++u) {
+                        acc[j][u].x = fma(c[j], xv[u].x, acc[j][u].x);
+                        acc[j][u].y = fma(c[j], xv[u].y, acc[j][u].y);
+                    }
             }
         }
 #pragma unroll
         for (int j = 0; j < QC; ++j) {
             const int q = q0 + j;
-            cx<R> v = mk<R>((R)0, (R)0);
+            cx<R> ws = mk<R>((R)0, (R)0);
             if (q < f.Q) {
                 const cxd s = scales_dev ? scales_dev[f.slot[q]] : scales.s[f.slot[q]];
-                v = cvt<R>(sc * (f.w[q] * s)) * acc[j];
+                ws = cvt<R>(sc * (f.w[q] * s));
             }
-            zt[j][lane][wrp] = v;
+#pragma unroll
+            for (int u = 0; u < PPL; ++u) zt[j][lane * PPL + u][wrp] = ws * acc[j][u];
         }
         __syncthreads();
         // thread -> (point, factor) pairs; each writes the CB channels of one point
-        for (int u = threadIdx.x; u < 32 * QC; u += 32 * CB) {
-            const int j = u >> 5, pl = u & 31;
+        for (int u = threadIdx.x; u < TP * QC; u += 32 * CB) {
+            const int j = u / TP, pl = u - j * TP;
             const int q = q0 + j;
-            const long long pp = (long long)blockIdx.x * 32 + pl;
+            const long long pp = (long long)blockIdx.x * TP + pl;
             if (q < f.Q && pp < NP) {
                 cx<R> *dst = Z + ((size_t)q * NP + pp) * f.Ap + a0;
 #pragma unroll
@@ -325,7 +367,8 @@ int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, c
     const FactArgs fa = args_of(fd, op->ctx->d_err);
     cudaStream_t s = op->ctx->stream;
     const long long NP = (long long)fd.N1 * fd.N2;
-    dim3 g1((unsigned)((NP + 31) / 32), (unsigned)((fd.A + CB - 1) / CB));
+    const int TP = 32 * MixTile<R>::PPL;
+    dim3 g1((unsigned)((NP + TP - 1) / TP), (unsigned)((fd.A + CB - 1) / CB));
     fact_mix_kernel<R><<<g1, 32 * CB, 0, s>>>(fa, scales, scales_dev, (const cx<R> *)src, inv_scale);
     op->ctx->launches++;
     PG_TRY(pg_check_launch(op->ctx));
@@ -442,7 +485,7 @@ int pg_factored_finalize(pg_op *op)
         }
     }
     const int nch = f.Qp / QC;
-    std::vector<int> row_ptr(A + 1, 0), col, qlo, qhi;
+    std::vector<int> row_ptr(A + 1, 0), col;
     std::vector<double> coef;
     std::vector<unsigned char> chunk((size_t)A * nch, 0), bflag((size_t)Q * f.nct, 0);
     std::vector<long long> rows_of_q(Q, 0);
@@ -458,23 +501,24 @@ int pg_factored_finalize(pg_op *op)
                     row_has[q] = 1;
                 }
             if (hi < 0) continue;  // all coefficients zero
-            col.push_back(kv.first);
-            qlo.push_back(lo);
-            qhi.push_back(hi);
+            col.push_back(kv.first);  // entry metadata: col, qlo, qhi, 0
+            col.push_back(lo);
+            col.push_back(hi);
+            col.push_back(0);
             coef.insert(coef.end(), kv.second.begin(), kv.second.end());
             for (int k = lo / QC; k <= hi / QC; ++k) {
                 chunk[(size_t)a * nch + k] = 1;
                 mix_terms += QC;
             }
         }
-        row_ptr[a + 1] = (int)col.size();
+        row_ptr[a + 1] = (int)(col.size() / 4);
         for (int q = 0; q < Q; ++q)
             if (row_has[q]) {
                 bflag[(size_t)q * f.nct + a / CA] = 1;
                 rows_of_q[q]++;
             }
     }
-    f.nE = (int)col.size();
+    f.nE = (int)(col.size() / 4);
     // radial factors, last rank padded to N2p; points outside the grid are dropped
     std::vector<double> rad((size_t)Q * N1 * b * b * f.N2p, 0.0);
     double pts = 0;  // in-grid stencil points of one factor
@@ -516,8 +560,6 @@ int pg_factored_finalize(pg_op *op)
     }
     PG_TRY(upload_vec(&f.row_ptr, row_ptr));
     PG_TRY(upload_vec(&f.col, col));
-    PG_TRY(upload_vec(&f.qlo, qlo));
-    PG_TRY(upload_vec(&f.qhi, qhi));
     PG_TRY(upload_vec(&f.slot, slot));
     PG_TRY(upload_vec(&f.chunk, chunk));
     PG_TRY(upload_vec(&f.bflag, bflag));
