@@ -14,10 +14,11 @@
 // The scratch Z keeps the channels innermost, so one radial row of Z for a tile of channels
 // is a plain 2-D box for the tensor-memory-access unit.
 //
-// mix: one warp per output channel a' and 32 points; the factors in chunks of QC accumulated
-// in registers (rows without entries in a chunk skip it; their scratch stays at the zeros
-// written at upload); the 4 warps of a CTA (4 consecutive channels) transpose through shared
-// memory so that each point's 4 channels leave as one 32-byte write.
+// mix: one warp per output channel a' and 32 (FP32: 64) points; only the nonzero (entry,
+// factor) pairs are applied, into per-factor accumulators in shared memory; the 4 warps of a
+// CTA (4 consecutive channels) then write each point's 4 channels as one 32-byte segment,
+// skipping factors none of the 4 channels has (their scratch stays at the zeros written at
+// upload).
 // radial: a 169-point stencil (k = 6) with coefficients varying per point and shared by all
 // channels. A CTA = one radial row i1, a tile of tw points of the last rank and CA channels;
 // per stage (factor q, row offset d1) one TMA box brings the Z rows [tw + 2k][CA] and one the
@@ -32,12 +33,11 @@
 
 namespace {
 
-const int QC = 16;  // factors per register chunk of the mix kernel
 const int CB = 4;   // channels per mix CTA (one warp each)
 
 struct FactArgs {
     int Q, Qp, A, Ap, N1, N2, N2p, nct, tw;
-    const int *row_ptr, *col, *qlo, *qhi, *slot;
+    const int *row_ptr, *col, *slot, *nzq;
     const void *coef;
     const unsigned char *chunk, *bflag;
     const cxd *w;
@@ -50,7 +50,7 @@ FactArgs args_of(const FactDev &f, int *err)
     FactArgs a;
     a.Q = f.Q; a.Qp = f.Qp; a.A = f.A; a.Ap = f.Ap; a.N1 = f.N1; a.N2 = f.N2; a.N2p = f.N2p; a.nct = f.nct;
     a.tw = f.tw;
-    a.row_ptr = f.row_ptr; a.col = f.col; a.qlo = f.qlo; a.qhi = f.qhi; a.slot = f.slot;
+    a.row_ptr = f.row_ptr; a.col = f.col; a.slot = f.slot; a.nzq = f.nzq;
     a.coef = f.coef; a.chunk = f.chunk; a.bflag = f.bflag; a.w = f.w; a.Z = f.Z; a.err = err;
     return a;
 }
@@ -95,14 +95,17 @@ __device__ __forceinline__ void tma_3d(void *dst, const CUtensorMap *map, int c0
                  : "memory");
 }
 
-// points per lane of the mix kernel (a 16-byte load of x per lane for FP32)
+// points per lane of the mix kernel
 template <typename R> struct MixTile;
 template <> struct MixTile<float> { static const int PPL = 2; };
 template <> struct MixTile<double> { static const int PPL = 1; };
 
-// Z[q][p][a] = w_q s_slot(q) / inv_scale * sum_e coef[e][q] x[col_e][p]. CTA = CB warps (channels
-// a0 .. a0+CB) x 32 PPL points; entry e = (col, qlo, qhi) packed as one int4, its coefficients
-// loaded as 16-byte vectors (uniform across the warp).
+// Z[q][p][a] = w_q s_slot(q) / inv_scale * sum_e coef_e(q) x[col_e][p] over the nonzero
+// (entry, factor) pairs only. CTA = CB warps (channels a0 .. a0+CB) x 32 PPL points (lane +
+// 32 u); the accumulators of every factor live in shared memory [CB][Q][32 PPL] (each
+// thread updates its own column: no conflicts, no synchronisation), then the CTA writes each
+// point's CB channels as one contiguous segment, skipping factors that no row of the group
+// touches (their scratch stays at the zeros written at upload).
 template <typename R>
 __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales scales,
                                                           const cxd *__restrict__ scales_dev,
@@ -111,97 +114,64 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
 {
     constexpr int PPL = MixTile<R>::PPL;
     constexpr int TP = 32 * PPL;
-    __shared__ cx<R> zt[QC][TP][CB + 1];
+    extern __shared__ __align__(16) unsigned char mix_smem[];
+    cx<R> *acc = reinterpret_cast<cx<R> *>(mix_smem);  // [CB][Q][TP]
     const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
+    const int Q = f.Q;
     const int a0 = blockIdx.y * CB;
     const int a = a0 + wrp;
     const long long NP = (long long)f.N1 * f.N2;
-    const long long p0 = (long long)blockIdx.x * TP + (long long)lane * PPL;  // this lane's first point
-    const bool live = p0 < NP;
-    const bool vec = (NP % PPL) == 0;  // 16-byte aligned pairs of points in every row
+    const long long base = (long long)blockIdx.x * TP;
     const double sc = inv_scale ? 1.0 / *inv_scale : 1.0;
-    const int nch = f.Qp / QC;
-    const R *__restrict__ coef = (const R *)f.coef;
     const int4 *__restrict__ meta = (const int4 *)f.col;
-    cx<R> *__restrict__ Z = (cx<R> *)f.Z;
-    for (int k = 0; k < nch; ++k) {
-        bool any = false;
-        for (int r = 0; r < CB; ++r)
-            if (a0 + r < f.A && f.chunk[(size_t)(a0 + r) * nch + k]) any = true;
-        if (!any) continue;  // CTA-uniform: the scratch of these rows stays zero
-        const int q0 = k * QC;
-        cx<R> acc[QC][PPL];
+    const int *__restrict__ nzq = f.nzq;  // factor indices of the nonzero pairs
+    const R *__restrict__ nzc = (const R *)f.coef;
+    cx<R> *__restrict__ mine = acc + (size_t)wrp * Q * TP + lane;
+    for (int q = 0; q < Q; ++q)
 #pragma unroll
-        for (int j = 0; j < QC; ++j)
+        for (int u = 0; u < PPL; ++u) mine[(size_t)q * TP + u * 32] = mk<R>((R)0, (R)0);
+    if (a < f.A) {
+        for (int e = f.row_ptr[a]; e < f.row_ptr[a + 1]; ++e) {
+            const int4 m = meta[e];  // col, first and last+1 nonzero pair
+            cx<R> xv[PPL];
 #pragma unroll
-            for (int u = 0; u < PPL; ++u) acc[j][u] = mk<R>((R)0, (R)0);
-        if (a < f.A && f.chunk[(size_t)a * nch + k]) {
-            for (int e = f.row_ptr[a]; e < f.row_ptr[a + 1]; ++e) {
-                const int4 m = meta[e];  // col, qlo, qhi
-                if (m.z < q0 || m.y >= q0 + QC) continue;
-                cx<R> xv[PPL];
-                if constexpr (PPL == 2) {
-                    const cx<R> *xr = x + (size_t)m.x * NP + p0;
-                    if (vec && live) {
-                        const float4 v = *reinterpret_cast<const float4 *>(xr);
-                        xv[0] = mk<R>(v.x, v.y);
-                        xv[1] = mk<R>(v.z, v.w);
-                    } else {
-                        xv[0] = live ? xr[0] : mk<R>((R)0, (R)0);
-                        xv[1] = (p0 + 1 < NP) ? xr[1] : mk<R>((R)0, (R)0);
-                    }
-                } else {
-                    xv[0] = live ? x[(size_t)m.x * NP + p0] : mk<R>((R)0, (R)0);
+            for (int u = 0; u < PPL; ++u) {
+                const long long pp = base + u * 32 + lane;
+                xv[u] = pp < NP ? x[(size_t)m.x * NP + pp] : mk<R>((R)0, (R)0);
+            }
+            for (int z = m.y; z < m.z; ++z) {
+                const int q = nzq[z];
+                const R c = nzc[z];
+                cx<R> *ap = mine + (size_t)q * TP;
+#pragma unroll
+                for (int u = 0; u < PPL; ++u) {
+                    cx<R> v = ap[u * 32];
+                    v.x = fma(c, xv[u].x, v.x);
+                    v.y = fma(c, xv[u].y, v.y);
+                    ap[u * 32] = v;
                 }
-                R c[QC];
-                const R *__restrict__ cp = coef + (size_t)e * f.Qp + q0;
-                if constexpr (sizeof(R) == 4) {
-#pragma unroll
-                    for (int h = 0; h < QC / 4; ++h) {
-                        const float4 v = reinterpret_cast<const float4 *>(cp)[h];
-                        c[4 * h] = v.x; c[4 * h + 1] = v.y; c[4 * h + 2] = v.z; c[4 * h + 3] = v.w;
-                    }
-                } else {
-#pragma unroll
-                    for (int h = 0; h < QC / 2; ++h) {
-                        const double2 v = reinterpret_cast<const double2 *>(cp)[h];
-                        c[2 * h] = v.x; c[2 * h + 1] = v.y;
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < QC; ++j)
-#pragma unroll
-                    for (int u = 0; u < PPL; ++u) {
-                        acc[j][u].x = fma(c[j], xv[u].x, acc[j][u].x);
-                        acc[j][u].y = fma(c[j], xv[u].y, acc[j][u].y);
-                    }
             }
         }
-#pragma unroll
-        for (int j = 0; j < QC; ++j) {
-            const int q = q0 + j;
-            cx<R> ws = mk<R>((R)0, (R)0);
-            if (q < f.Q) {
-                const cxd s = scales_dev ? scales_dev[f.slot[q]] : scales.s[f.slot[q]];
-                ws = cvt<R>(sc * (f.w[q] * s));
-            }
-#pragma unroll
-            for (int u = 0; u < PPL; ++u) zt[j][lane * PPL + u][wrp] = ws * acc[j][u];
-        }
-        __syncthreads();
-        // thread -> (point, factor) pairs; each writes the CB channels of one point
-        for (int u = threadIdx.x; u < TP * QC; u += 32 * CB) {
-            const int j = u / TP, pl = u - j * TP;
-            const int q = q0 + j;
-            const long long pp = (long long)blockIdx.x * TP + pl;
-            if (q < f.Q && pp < NP) {
-                cx<R> *dst = Z + ((size_t)q * NP + pp) * f.Ap + a0;
-#pragma unroll
-                for (int r = 0; r < CB; ++r) dst[r] = zt[j][pl][r];
-            }
-        }
-        __syncthreads();
     }
+    __syncthreads();
+    const unsigned char *gf = f.chunk + (size_t)blockIdx.y * Q;  // factors touched by this group
+    cx<R> *__restrict__ Z = (cx<R> *)f.Z;
+    for (int t = threadIdx.x; t < Q * TP; t += 32 * CB) {
+        const int q = t / TP, pl = t - q * TP;
+        const long long pp = base + pl;
+        if (!gf[q] || pp >= NP) continue;
+        const cxd s = scales_dev ? scales_dev[f.slot[q]] : scales.s[f.slot[q]];
+        const cx<R> ws = cvt<R>(sc * (f.w[q] * s));
+        cx<R> *dst = Z + ((size_t)q * NP + pp) * f.Ap + a0;
+#pragma unroll
+        for (int r = 0; r < CB; ++r) dst[r] = ws * acc[((size_t)r * Q + q) * TP + pl];
+    }
+}
+
+template <typename R>
+size_t mix_smem_bytes(int Q)
+{
+    return (size_t)CB * Q * 32 * MixTile<R>::PPL * sizeof(cx<R>);
 }
 
 // tile shapes per precision: PI points x NV 16-byte vectors of channels per thread, 8 channel
@@ -369,7 +339,8 @@ int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, c
     const long long NP = (long long)fd.N1 * fd.N2;
     const int TP = 32 * MixTile<R>::PPL;
     dim3 g1((unsigned)((NP + TP - 1) / TP), (unsigned)((fd.A + CB - 1) / CB));
-    fact_mix_kernel<R><<<g1, 32 * CB, 0, s>>>(fa, scales, scales_dev, (const cx<R> *)src, inv_scale);
+    fact_mix_kernel<R><<<g1, 32 * CB, mix_smem_bytes<R>(fd.Q), s>>>(fa, scales, scales_dev, (const cx<R> *)src,
+                                                                     inv_scale);
     op->ctx->launches++;
     PG_TRY(pg_check_launch(op->ctx));
     dim3 g2((unsigned)fd.N1, (unsigned)fd.ntiles, (unsigned)fd.nct);
@@ -393,7 +364,7 @@ int pg_factored_apply(pg_op *op, const pg_scales &scales, const cxd *scales_dev,
 void pg_factored_free(pg_op *op)
 {
     FactDev &f = op->fact;
-    cudaFree(f.row_ptr); cudaFree(f.col); cudaFree(f.qlo); cudaFree(f.qhi); cudaFree(f.slot);
+    cudaFree(f.row_ptr); cudaFree(f.col); cudaFree(f.nzq); cudaFree(f.slot);
     cudaFree(f.coef); cudaFree(f.chunk); cudaFree(f.bflag); cudaFree(f.radial); cudaFree(f.w); cudaFree(f.Z);
     f = FactDev();
 }
@@ -463,7 +434,7 @@ int pg_factored_finalize(pg_op *op)
     const bool fp64 = op->precision == PG_FP64;
     const int Q = (int)op->factors.size();
     f.A = A; f.N1 = N1; f.N2 = N2; f.Q = Q;
-    f.Qp = (Q + QC - 1) / QC * QC;
+    f.Qp = Q;
     f.N2p = (N2 + 3) & ~3;
     f.Ap = (A + CB - 1) / CB * CB;
     const int CA = fp64 ? RadialTile<double>::CA : RadialTile<float>::CA;
@@ -474,50 +445,47 @@ int pg_factored_finalize(pg_op *op)
     const int tmax = 16 * PI;
     f.ntiles = (N2 + tmax - 1) / tmax;
     f.tw = ((N2 + f.ntiles - 1) / f.ntiles + PI - 1) / PI * PI;
-    // angular rows: coefficient vector over the factors per (row, col)
+    // angular rows: coefficient vector over the factors per (row, col); each entry keeps the
+    // list of its nonzero (factor, coefficient) pairs
     std::vector<std::map<int, std::vector<double>>> rows(A);
     for (int q = 0; q < Q; ++q) {
         const HostFactor &h = op->factors[q];
         for (size_t e = 0; e < h.row.size(); ++e) {
             std::vector<double> &v = rows[h.row[e]][h.col[e]];
-            if (v.empty()) v.assign(f.Qp, 0.0);
+            if (v.empty()) v.assign(Q, 0.0);
             v[q] += h.coef[e];
         }
     }
-    const int nch = f.Qp / QC;
-    std::vector<int> row_ptr(A + 1, 0), col;
+    std::vector<int> row_ptr(A + 1, 0), col, nzq;
     std::vector<double> coef;
-    std::vector<unsigned char> chunk((size_t)A * nch, 0), bflag((size_t)Q * f.nct, 0);
+    const int ngroups = f.Ap / CB;
+    std::vector<unsigned char> chunk((size_t)ngroups * Q, 0), bflag((size_t)Q * f.nct, 0);
     std::vector<long long> rows_of_q(Q, 0);
-    double mix_terms = 0;
     for (int a = 0; a < A; ++a) {
         std::vector<unsigned char> row_has(Q, 0);
         for (const auto &kv : rows[a]) {
-            int lo = f.Qp, hi = -1;
+            const int first = (int)nzq.size();
             for (int q = 0; q < Q; ++q)
                 if (kv.second[q] != 0.0) {
-                    lo = std::min(lo, q);
-                    hi = std::max(hi, q);
+                    nzq.push_back(q);
+                    coef.push_back(kv.second[q]);
                     row_has[q] = 1;
                 }
-            if (hi < 0) continue;  // all coefficients zero
-            col.push_back(kv.first);  // entry metadata: col, qlo, qhi, 0
-            col.push_back(lo);
-            col.push_back(hi);
+            if ((int)nzq.size() == first) continue;  // all coefficients zero
+            col.push_back(kv.first);  // entry metadata: col, first and last+1 nonzero pair, 0
+            col.push_back(first);
+            col.push_back((int)nzq.size());
             col.push_back(0);
-            coef.insert(coef.end(), kv.second.begin(), kv.second.end());
-            for (int k = lo / QC; k <= hi / QC; ++k) {
-                chunk[(size_t)a * nch + k] = 1;
-                mix_terms += QC;
-            }
         }
         row_ptr[a + 1] = (int)(col.size() / 4);
         for (int q = 0; q < Q; ++q)
             if (row_has[q]) {
                 bflag[(size_t)q * f.nct + a / CA] = 1;
+                chunk[(size_t)(a / CB) * Q + q] = 1;
                 rows_of_q[q]++;
             }
     }
+    const double mix_terms = (double)nzq.size();
     f.nE = (int)(col.size() / 4);
     // radial factors, last rank padded to N2p; points outside the grid are dropped
     std::vector<double> rad((size_t)Q * N1 * b * b * f.N2p, 0.0);
@@ -547,7 +515,7 @@ int pg_factored_finalize(pg_op *op)
         radial_terms += pts * (double)rows_of_q[q];
     }
     const double NP = (double)N1 * N2;
-    f.flops_mix = 4.0 * mix_terms * NP;      // complex x real = 2 FMA per factor, entry and point
+    f.flops_mix = 4.0 * mix_terms * NP;      // complex x real = 2 FMA per nonzero pair and point
     f.flops_radial = 4.0 * radial_terms;     // per in-grid stencil point and nonzero row
     const size_t esz = fp64 ? sizeof(double) : sizeof(float);
     f.radial_bytes = (double)rad.size() * esz;
@@ -561,6 +529,7 @@ int pg_factored_finalize(pg_op *op)
     PG_TRY(upload_vec(&f.row_ptr, row_ptr));
     PG_TRY(upload_vec(&f.col, col));
     PG_TRY(upload_vec(&f.slot, slot));
+    PG_TRY(upload_vec(&f.nzq, nzq));
     PG_TRY(upload_vec(&f.chunk, chunk));
     PG_TRY(upload_vec(&f.bflag, bflag));
     PG_CUDA_TRY(cudaMalloc(&f.w, sizeof(cxd) * Q));
@@ -582,6 +551,11 @@ int pg_factored_finalize(pg_op *op)
     PG_CUDA_TRY(cudaGetDevice(&dev));
     PG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     if (f.radial_smem > (size_t)optin) return PG_ERR_SHAPE;
+    if ((fp64 ? mix_smem_bytes<double>(Q) : mix_smem_bytes<float>(Q)) > (size_t)optin) return PG_ERR_SHAPE;
+    if (fp64)
+        PG_CUDA_TRY(cudaFuncSetAttribute(fact_mix_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    else
+        PG_CUDA_TRY(cudaFuncSetAttribute(fact_mix_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     if (fp64)
         PG_CUDA_TRY(cudaFuncSetAttribute(fact_radial_kernel<double, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     else
