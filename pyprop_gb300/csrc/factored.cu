@@ -95,83 +95,76 @@ __device__ __forceinline__ void tma_3d(void *dst, const CUtensorMap *map, int c0
                  : "memory");
 }
 
-// points per lane of the mix kernel
-template <typename R> struct MixTile;
-template <> struct MixTile<float> { static const int PPL = 2; };
-template <> struct MixTile<double> { static const int PPL = 1; };
-
 // Z[q][p][a] = w_q s_slot(q) / inv_scale * sum_e coef_e(q) x[col_e][p] over the nonzero
-// (entry, factor) pairs only. CTA = CB warps (channels a0 .. a0+CB) x 32 PPL points (lane +
-// 32 u); the accumulators of every factor live in shared memory [CB][Q][32 PPL] (each
-// thread updates its own column: no conflicts, no synchronisation), then the CTA writes each
-// point's CB channels as one contiguous segment, skipping factors that no row of the group
-// touches (their scratch stays at the zeros written at upload).
+// (entry, factor) pairs only. CTA = CB warps (channels a0 .. a0+CB) x 32 points; the
+// accumulators of every factor live in shared memory [Q][32][CB + 1] (a thread updates only
+// its own point and channel); the x loads of MIXU entries are issued together. The CTA then
+// writes the CB channels of each point as one contiguous segment (lanes = 8 points x 4
+// channels), skipping factors that no channel of the group has (their scratch stays at the
+// zeros written at upload).
+const int MIXU = 4;
+
 template <typename R>
 __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales scales,
                                                           const cxd *__restrict__ scales_dev,
                                                           const cx<R> *__restrict__ x,
                                                           const double *__restrict__ inv_scale)
 {
-    constexpr int PPL = MixTile<R>::PPL;
-    constexpr int TP = 32 * PPL;
     extern __shared__ __align__(16) unsigned char mix_smem[];
-    cx<R> *acc = reinterpret_cast<cx<R> *>(mix_smem);  // [CB][Q][TP]
+    cx<R> *acc = reinterpret_cast<cx<R> *>(mix_smem);  // [Q][32][CB + 1]
     const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
     const int Q = f.Q;
     const int a0 = blockIdx.y * CB;
     const int a = a0 + wrp;
     const long long NP = (long long)f.N1 * f.N2;
-    const long long base = (long long)blockIdx.x * TP;
+    const long long p = (long long)blockIdx.x * 32 + lane;
+    const bool live = p < NP;
     const double sc = inv_scale ? 1.0 / *inv_scale : 1.0;
     const int4 *__restrict__ meta = (const int4 *)f.col;
-    const int *__restrict__ nzq = f.nzq;  // factor indices of the nonzero pairs
+    const int *__restrict__ nzq = f.nzq;
     const R *__restrict__ nzc = (const R *)f.coef;
-    cx<R> *__restrict__ mine = acc + (size_t)wrp * Q * TP + lane;
-    for (int q = 0; q < Q; ++q)
-#pragma unroll
-        for (int u = 0; u < PPL; ++u) mine[(size_t)q * TP + u * 32] = mk<R>((R)0, (R)0);
+    cx<R> *mine = acc + (size_t)lane * (CB + 1) + wrp;
+    constexpr int QS = 32 * (CB + 1);  // stride of one factor
+    for (int q = 0; q < Q; ++q) mine[(size_t)q * QS] = mk<R>((R)0, (R)0);
     if (a < f.A) {
-        for (int e = f.row_ptr[a]; e < f.row_ptr[a + 1]; ++e) {
-            const int4 m = meta[e];  // col, first and last+1 nonzero pair
-            cx<R> xv[PPL];
+        const int e_end = f.row_ptr[a + 1];
+        for (int e0 = f.row_ptr[a]; e0 < e_end; e0 += MIXU) {
+            int4 m[MIXU];
+            cx<R> xv[MIXU];
 #pragma unroll
-            for (int u = 0; u < PPL; ++u) {
-                const long long pp = base + u * 32 + lane;
-                xv[u] = pp < NP ? x[(size_t)m.x * NP + pp] : mk<R>((R)0, (R)0);
+            for (int u = 0; u < MIXU; ++u) {
+                m[u] = e0 + u < e_end ? meta[e0 + u] : make_int4(0, 0, 0, 0);
+                xv[u] = (live && e0 + u < e_end) ? x[(size_t)m[u].x * NP + p] : mk<R>((R)0, (R)0);
             }
-            for (int z = m.y; z < m.z; ++z) {
-                const int q = nzq[z];
-                const R c = nzc[z];
-                cx<R> *ap = mine + (size_t)q * TP;
 #pragma unroll
-                for (int u = 0; u < PPL; ++u) {
-                    cx<R> v = ap[u * 32];
+            for (int u = 0; u < MIXU; ++u)
+                for (int z = m[u].y; z < m[u].z; ++z) {
+                    cx<R> *ap = mine + (size_t)nzq[z] * QS;
+                    const R c = nzc[z];
+                    cx<R> v = *ap;
                     v.x = fma(c, xv[u].x, v.x);
                     v.y = fma(c, xv[u].y, v.y);
-                    ap[u * 32] = v;
+                    *ap = v;
                 }
-            }
         }
     }
     __syncthreads();
     const unsigned char *gf = f.chunk + (size_t)blockIdx.y * Q;  // factors touched by this group
     cx<R> *__restrict__ Z = (cx<R> *)f.Z;
-    for (int t = threadIdx.x; t < Q * TP; t += 32 * CB) {
-        const int q = t / TP, pl = t - q * TP;
-        const long long pp = base + pl;
+    for (int t = threadIdx.x; t < Q * 32 * CB; t += 32 * CB) {
+        const int r = t % CB, rest = t / CB;
+        const int pl = rest % 32, q = rest / 32;
+        const long long pp = (long long)blockIdx.x * 32 + pl;
         if (!gf[q] || pp >= NP) continue;
         const cxd s = scales_dev ? scales_dev[f.slot[q]] : scales.s[f.slot[q]];
-        const cx<R> ws = cvt<R>(sc * (f.w[q] * s));
-        cx<R> *dst = Z + ((size_t)q * NP + pp) * f.Ap + a0;
-#pragma unroll
-        for (int r = 0; r < CB; ++r) dst[r] = ws * acc[((size_t)r * Q + q) * TP + pl];
+        Z[((size_t)q * NP + pp) * f.Ap + a0 + r] = cvt<R>(sc * (f.w[q] * s)) * acc[(size_t)q * QS + pl * (CB + 1) + r];
     }
 }
 
 template <typename R>
 size_t mix_smem_bytes(int Q)
 {
-    return (size_t)CB * Q * 32 * MixTile<R>::PPL * sizeof(cx<R>);
+    return (size_t)Q * 32 * (CB + 1) * sizeof(cx<R>);
 }
 
 // tile shapes per precision: PI points x NV 16-byte vectors of channels per thread, 8 channel
@@ -337,8 +330,7 @@ int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, c
     const FactArgs fa = args_of(fd, op->ctx->d_err);
     cudaStream_t s = op->ctx->stream;
     const long long NP = (long long)fd.N1 * fd.N2;
-    const int TP = 32 * MixTile<R>::PPL;
-    dim3 g1((unsigned)((NP + TP - 1) / TP), (unsigned)((fd.A + CB - 1) / CB));
+    dim3 g1((unsigned)((NP + 31) / 32), (unsigned)((fd.A + CB - 1) / CB));
     fact_mix_kernel<R><<<g1, 32 * CB, mix_smem_bytes<R>(fd.Q), s>>>(fa, scales, scales_dev, (const cx<R> *)src,
                                                                      inv_scale);
     op->ctx->launches++;
