@@ -37,7 +37,7 @@ const int CB = 4;   // channels per mix CTA (one warp each)
 
 struct FactArgs {
     int Q, Qp, A, Ap, N1, N2, N2p, nct, tw;
-    const int *row_ptr, *col, *slot, *nzq;
+    const int *row_ptr, *col, *slot, *nzq, *perm;
     const void *coef;
     const unsigned char *chunk, *bflag;
     const cxd *w;
@@ -50,7 +50,7 @@ FactArgs args_of(const FactDev &f, int *err)
     FactArgs a;
     a.Q = f.Q; a.Qp = f.Qp; a.A = f.A; a.Ap = f.Ap; a.N1 = f.N1; a.N2 = f.N2; a.N2p = f.N2p; a.nct = f.nct;
     a.tw = f.tw;
-    a.row_ptr = f.row_ptr; a.col = f.col; a.slot = f.slot; a.nzq = f.nzq;
+    a.row_ptr = f.row_ptr; a.col = f.col; a.slot = f.slot; a.nzq = f.nzq; a.perm = f.perm;
     a.coef = f.coef; a.chunk = f.chunk; a.bflag = f.bflag; a.w = f.w; a.Z = f.Z; a.err = err;
     return a;
 }
@@ -114,8 +114,8 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
     cx<R> *acc = reinterpret_cast<cx<R> *>(mix_smem);  // [Q][32][CB + 1]
     const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
     const int Q = f.Q;
-    const int a0 = blockIdx.y * CB;
-    const int a = a0 + wrp;
+    const int a0 = blockIdx.y * CB;                      // first scratch slot of the group
+    const int a = a0 + wrp < f.A ? f.perm[a0 + wrp] : -1;  // channel of this warp's slot
     const long long NP = (long long)f.N1 * f.N2;
     const long long p = (long long)blockIdx.x * 32 + lane;
     const bool live = p < NP;
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
     cx<R> *mine = acc + (size_t)lane * (CB + 1) + wrp;
     constexpr int QS = 32 * (CB + 1);  // stride of one factor
     for (int q = 0; q < Q; ++q) mine[(size_t)q * QS] = mk<R>((R)0, (R)0);
-    if (a < f.A) {
+    if (a >= 0) {
         const int e_end = f.row_ptr[a + 1];
         for (int e0 = f.row_ptr[a]; e0 < e_end; e0 += MIXU) {
             int4 m[MIXU];
@@ -310,9 +310,9 @@ __global__ void __launch_bounds__(128, 2) fact_radial_kernel(FactArgs f, cx<R> *
     for (int h = 0; h < NV; ++h)
 #pragma unroll
         for (int v = 0; v < PCV; ++v) {
-            const int ch = c0 + (h * TCN + tc) * PCV + v;
-            if (ch >= f.A) continue;
-            cx<R> *__restrict__ yr = y + (size_t)ch * NP + (size_t)i1 * N2;
+            const int sl = c0 + (h * TCN + tc) * PCV + v;  // scratch slot -> channel
+            if (sl >= f.A) continue;
+            cx<R> *__restrict__ yr = y + (size_t)f.perm[sl] * NP + (size_t)i1 * N2;
 #pragma unroll
             for (int p = 0; p < PI; ++p) {
                 const int i2 = t0 + ti * PI + p;
@@ -356,7 +356,7 @@ int pg_factored_apply(pg_op *op, const pg_scales &scales, const cxd *scales_dev,
 void pg_factored_free(pg_op *op)
 {
     FactDev &f = op->fact;
-    cudaFree(f.row_ptr); cudaFree(f.col); cudaFree(f.nzq); cudaFree(f.slot);
+    cudaFree(f.row_ptr); cudaFree(f.col); cudaFree(f.nzq); cudaFree(f.slot); cudaFree(f.perm);
     cudaFree(f.coef); cudaFree(f.chunk); cudaFree(f.bflag); cudaFree(f.radial); cudaFree(f.w); cudaFree(f.Z);
     f = FactDev();
 }
@@ -453,8 +453,9 @@ int pg_factored_finalize(pg_op *op)
     const int ngroups = f.Ap / CB;
     std::vector<unsigned char> chunk((size_t)ngroups * Q, 0), bflag((size_t)Q * f.nct, 0);
     std::vector<long long> rows_of_q(Q, 0);
+    std::vector<std::vector<unsigned char>> has(A, std::vector<unsigned char>(Q, 0));
     for (int a = 0; a < A; ++a) {
-        std::vector<unsigned char> row_has(Q, 0);
+        std::vector<unsigned char> &row_has = has[a];
         for (const auto &kv : rows[a]) {
             const int first = (int)nzq.size();
             for (int q = 0; q < Q; ++q)
@@ -470,13 +471,25 @@ int pg_factored_finalize(pg_op *op)
             col.push_back(0);
         }
         row_ptr[a + 1] = (int)(col.size() / 4);
-        for (int q = 0; q < Q; ++q)
-            if (row_has[q]) {
-                bflag[(size_t)q * f.nct + a / CA] = 1;
-                chunk[(size_t)(a / CB) * Q + q] = 1;
-                rows_of_q[q]++;
-            }
+        for (int q = 0; q < Q; ++q) rows_of_q[q] += row_has[q];
     }
+    // scratch slots: channels sorted by the set of factors they have, so that the radial
+    // kernel's channel tiles skip more (factor, tile) stages; slot s holds channel perm[s]
+    std::vector<int> perm(A);
+    for (int a = 0; a < A; ++a) perm[a] = a;
+    std::vector<int> cnt(A, 0);
+    for (int a = 0; a < A; ++a)
+        for (int q = 0; q < Q; ++q) cnt[a] += has[a][q];
+    std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) {
+        if (cnt[x] != cnt[y]) return cnt[x] < cnt[y];
+        return has[x] < has[y];
+    });
+    for (int sl = 0; sl < A; ++sl)
+        for (int q = 0; q < Q; ++q)
+            if (has[perm[sl]][q]) {
+                bflag[(size_t)q * f.nct + sl / CA] = 1;
+                chunk[(size_t)(sl / CB) * Q + q] = 1;
+            }
     const double mix_terms = (double)nzq.size();
     f.nE = (int)(col.size() / 4);
     // radial factors, last rank padded to N2p; points outside the grid are dropped
@@ -522,6 +535,7 @@ int pg_factored_finalize(pg_op *op)
     PG_TRY(upload_vec(&f.col, col));
     PG_TRY(upload_vec(&f.slot, slot));
     PG_TRY(upload_vec(&f.nzq, nzq));
+    PG_TRY(upload_vec(&f.perm, perm));
     PG_TRY(upload_vec(&f.chunk, chunk));
     PG_TRY(upload_vec(&f.bflag, bflag));
     PG_CUDA_TRY(cudaMalloc(&f.w, sizeof(cxd) * Q));

@@ -140,12 +140,13 @@ struct FactDev {
     int *col = nullptr;               // [nE][4]: column, first and last+1 nonzero pair, 0
     int *nzq = nullptr;               // [nnz] factor of each nonzero (entry, factor) pair
     int *slot = nullptr;              // [Q]
+    int *perm = nullptr;              // [A] channel held by each scratch slot
     void *coef = nullptr;             // [nnz] its coefficient (operator precision)
     unsigned char *chunk = nullptr;   // [Ap / 4][Q] factors touched by each group of 4 channels
     unsigned char *bflag = nullptr;   // [Q][nct] channel tiles with a nonzero row
     void *radial = nullptr;           // [Q][N1][b][b][N2p] real
     cxd *w = nullptr;                 // [Q]
-    void *Z = nullptr;                // [Q][N1*N2][Ap] complex scratch (channels innermost)
+    void *Z = nullptr;                // [Q][N1*N2][Ap] complex scratch (slots innermost)
     double flops_mix = 0, flops_radial = 0, radial_bytes = 0, z_bytes = 0;
 };
 
