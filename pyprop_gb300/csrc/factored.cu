@@ -95,15 +95,13 @@ __device__ __forceinline__ void tma_3d(void *dst, const CUtensorMap *map, int c0
                  : "memory");
 }
 
-// Z[q][p][a] = w_q s_slot(q) / inv_scale * sum_e coef_e(q) x[col_e][p] over the nonzero
-// (entry, factor) pairs only. CTA = CB warps (channels a0 .. a0+CB) x 32 points; the
-// accumulators of every factor live in shared memory [Q][32][CB + 1] (a thread updates only
-// its own point and channel); the x loads of MIXU entries are issued together. The CTA then
-// writes the CB channels of each point as one contiguous segment (lanes = 8 points x 4
-// channels), skipping factors that no channel of the group has (their scratch stays at the
-// zeros written at upload).
-const int MIXU = 4;
-
+// Z[q][p][a] = w_q s_slot(q) / inv_scale * sum_(col, c) c x[col][p] over the nonzero pairs of
+// (channel a, factor q). CTA = CB warps (scratch slots a0 .. a0+CB) x 32 points (one per lane).
+// Each channel's pairs are grouped by factor (segments), so a factor's sum stays in a register
+// and reaches shared memory [Q][32][CB + 1] once; x is read through the read-only cache (the
+// same columns recur across factors). The CTA then writes the CB slots of each point as one
+// contiguous segment (lanes = 8 points x 4 slots), skipping factors that no slot of the group
+// has (their scratch stays at the zeros written at upload).
 template <typename R>
 __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales scales,
                                                           const cxd *__restrict__ scales_dev,
@@ -120,32 +118,30 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
     const long long p = (long long)blockIdx.x * 32 + lane;
     const bool live = p < NP;
     const double sc = inv_scale ? 1.0 / *inv_scale : 1.0;
-    const int4 *__restrict__ meta = (const int4 *)f.col;
-    const int *__restrict__ nzq = f.nzq;
-    const R *__restrict__ nzc = (const R *)f.coef;
-    cx<R> *mine = acc + (size_t)lane * (CB + 1) + wrp;
+    const int4 *__restrict__ seg = (const int4 *)f.col;  // factor, first pair, last+1 pair
+    const int *__restrict__ pcol = f.nzq;
+    const R *__restrict__ pc = (const R *)f.coef;
     constexpr int QS = 32 * (CB + 1);  // stride of one factor
+    cx<R> *mine = acc + (size_t)lane * (CB + 1) + wrp;
     for (int q = 0; q < Q; ++q) mine[(size_t)q * QS] = mk<R>((R)0, (R)0);
-    if (a >= 0) {
-        const int e_end = f.row_ptr[a + 1];
-        for (int e0 = f.row_ptr[a]; e0 < e_end; e0 += MIXU) {
-            int4 m[MIXU];
-            cx<R> xv[MIXU];
-#pragma unroll
-            for (int u = 0; u < MIXU; ++u) {
-                m[u] = e0 + u < e_end ? meta[e0 + u] : make_int4(0, 0, 0, 0);
-                xv[u] = (live && e0 + u < e_end) ? x[(size_t)m[u].x * NP + p] : mk<R>((R)0, (R)0);
+    if (a >= 0 && live) {
+        const cx<R> *__restrict__ xp = x + p;
+        for (int g = f.row_ptr[a]; g < f.row_ptr[a + 1]; ++g) {
+            const int4 sg = seg[g];
+            cx<R> s0 = mk<R>((R)0, (R)0), s1 = mk<R>((R)0, (R)0);
+            int z = sg.y;
+            for (; z + 1 < sg.z; z += 2) {  // two independent chains
+                const cx<R> x0 = __ldg(xp + (size_t)pcol[z] * NP), x1 = __ldg(xp + (size_t)pcol[z + 1] * NP);
+                const R c0 = pc[z], c1 = pc[z + 1];
+                s0.x = fma(c0, x0.x, s0.x); s0.y = fma(c0, x0.y, s0.y);
+                s1.x = fma(c1, x1.x, s1.x); s1.y = fma(c1, x1.y, s1.y);
             }
-#pragma unroll
-            for (int u = 0; u < MIXU; ++u)
-                for (int z = m[u].y; z < m[u].z; ++z) {
-                    cx<R> *ap = mine + (size_t)nzq[z] * QS;
-                    const R c = nzc[z];
-                    cx<R> v = *ap;
-                    v.x = fma(c, xv[u].x, v.x);
-                    v.y = fma(c, xv[u].y, v.y);
-                    *ap = v;
-                }
+            if (z < sg.z) {
+                const cx<R> x0 = __ldg(xp + (size_t)pcol[z] * NP);
+                const R c0 = pc[z];
+                s0.x = fma(c0, x0.x, s0.x); s0.y = fma(c0, x0.y, s0.y);
+            }
+            mine[(size_t)sg.x * QS] = s0 + s1;
         }
     }
     __syncthreads();
@@ -456,16 +452,17 @@ int pg_factored_finalize(pg_op *op)
     std::vector<std::vector<unsigned char>> has(A, std::vector<unsigned char>(Q, 0));
     for (int a = 0; a < A; ++a) {
         std::vector<unsigned char> &row_has = has[a];
-        for (const auto &kv : rows[a]) {
+        // pairs of this channel grouped by factor: one segment (q, first, last+1) per factor
+        for (int q = 0; q < Q; ++q) {
             const int first = (int)nzq.size();
-            for (int q = 0; q < Q; ++q)
+            for (const auto &kv : rows[a])
                 if (kv.second[q] != 0.0) {
-                    nzq.push_back(q);
+                    nzq.push_back(kv.first);  // column
                     coef.push_back(kv.second[q]);
-                    row_has[q] = 1;
                 }
-            if ((int)nzq.size() == first) continue;  // all coefficients zero
-            col.push_back(kv.first);  // entry metadata: col, first and last+1 nonzero pair, 0
+            if ((int)nzq.size() == first) continue;
+            row_has[q] = 1;
+            col.push_back(q);
             col.push_back(first);
             col.push_back((int)nzq.size());
             col.push_back(0);
@@ -491,7 +488,8 @@ int pg_factored_finalize(pg_op *op)
                 chunk[(size_t)(sl / CB) * Q + q] = 1;
             }
     const double mix_terms = (double)nzq.size();
-    f.nE = (int)(col.size() / 4);
+    f.nE = 0;
+    for (int a = 0; a < A; ++a) f.nE += (int)rows[a].size();
     // radial factors, last rank padded to N2p; points outside the grid are dropped
     std::vector<double> rad((size_t)Q * N1 * b * b * f.N2p, 0.0);
     double pts = 0;  // in-grid stencil points of one factor

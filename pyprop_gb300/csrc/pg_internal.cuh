@@ -136,12 +136,12 @@ struct FactDev {
     int tw = 0, ntiles = 0;        // radial kernel: points of the last rank per CTA, tiles per row
     size_t radial_smem = 0;        // its dynamic shared memory
     CUtensorMap zmap, rmap;        // TMA maps of the scratch and of the radial factors
-    int *row_ptr = nullptr;           // [A + 1] angular entries per output channel
-    int *col = nullptr;               // [nE][4]: column, first and last+1 nonzero pair, 0
-    int *nzq = nullptr;               // [nnz] factor of each nonzero (entry, factor) pair
+    int *row_ptr = nullptr;           // [A + 1] segments per output channel
+    int *col = nullptr;               // [segments][4]: factor, first and last+1 pair, 0
+    int *nzq = nullptr;               // [pairs] input channel of each nonzero (channel, factor) pair
     int *slot = nullptr;              // [Q]
     int *perm = nullptr;              // [A] channel held by each scratch slot
-    void *coef = nullptr;             // [nnz] its coefficient (operator precision)
+    void *coef = nullptr;             // [pairs] its coefficient (operator precision)
     unsigned char *chunk = nullptr;   // [Ap / 4][Q] factors touched by each group of 4 channels
     unsigned char *bflag = nullptr;   // [Q][nct] channel tiles with a nonzero row
     void *radial = nullptr;           // [Q][N1][b][b][N2p] real
