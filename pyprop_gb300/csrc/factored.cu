@@ -95,6 +95,18 @@ __device__ __forceinline__ void tma_3d(void *dst, const CUtensorMap *map, int c0
                  : "memory");
 }
 
+template <typename R>
+__device__ __forceinline__ cx<R> ldg_cx(const cx<R> *p)
+{
+    if constexpr (sizeof(R) == 4) {
+        const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+        return mk<R>(v.x, v.y);
+    } else {
+        const double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+        return mk<R>(v.x, v.y);
+    }
+}
+
 // Z[q][p][a] = w_q s_slot(q) / inv_scale * sum_(col, c) c x[col][p] over the nonzero pairs of
 // (channel a, factor q). CTA = CB warps (scratch slots a0 .. a0+CB) x 32 points (one per lane).
 // Each channel's pairs are grouped by factor (segments), so a factor's sum stays in a register
@@ -131,13 +143,13 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
             cx<R> s0 = mk<R>((R)0, (R)0), s1 = mk<R>((R)0, (R)0);
             int z = sg.y;
             for (; z + 1 < sg.z; z += 2) {  // two independent chains
-                const cx<R> x0 = __ldg(xp + (size_t)pcol[z] * NP), x1 = __ldg(xp + (size_t)pcol[z + 1] * NP);
+                const cx<R> x0 = ldg_cx(xp + (size_t)pcol[z] * NP), x1 = ldg_cx(xp + (size_t)pcol[z + 1] * NP);
                 const R c0 = pc[z], c1 = pc[z + 1];
                 s0.x = fma(c0, x0.x, s0.x); s0.y = fma(c0, x0.y, s0.y);
                 s1.x = fma(c1, x1.x, s1.x); s1.y = fma(c1, x1.y, s1.y);
             }
             if (z < sg.z) {
-                const cx<R> x0 = __ldg(xp + (size_t)pcol[z] * NP);
+                const cx<R> x0 = ldg_cx(xp + (size_t)pcol[z] * NP);
                 const R c0 = pc[z];
                 s0.x = fma(c0, x0.x, s0.x); s0.y = fma(c0, x0.y, s0.y);
             }
