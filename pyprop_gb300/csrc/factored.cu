@@ -134,6 +134,11 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
     const int *__restrict__ pcol = f.nzq;
     const R *__restrict__ pc = (const R *)f.coef;
     constexpr int QS = 32 * (CB + 1);  // stride of one factor
+    cx<R> *ws = acc + (size_t)Q * QS;  // [Q] factor scales in the compute precision
+    for (int q = threadIdx.x; q < Q; q += 32 * CB) {
+        const cxd s = scales_dev ? scales_dev[f.slot[q]] : scales.s[f.slot[q]];
+        ws[q] = cvt<R>(sc * (f.w[q] * s));
+    }
     cx<R> *mine = acc + (size_t)lane * (CB + 1) + wrp;
     for (int q = 0; q < Q; ++q) mine[(size_t)q * QS] = mk<R>((R)0, (R)0);
     if (a >= 0 && live) {
@@ -164,15 +169,14 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
         const int pl = rest % 32, q = rest / 32;
         const long long pp = (long long)blockIdx.x * 32 + pl;
         if (!gf[q] || pp >= NP) continue;
-        const cxd s = scales_dev ? scales_dev[f.slot[q]] : scales.s[f.slot[q]];
-        Z[((size_t)q * NP + pp) * f.Ap + a0 + r] = cvt<R>(sc * (f.w[q] * s)) * acc[(size_t)q * QS + pl * (CB + 1) + r];
+        Z[((size_t)q * NP + pp) * f.Ap + a0 + r] = ws[q] * acc[(size_t)q * QS + pl * (CB + 1) + r];
     }
 }
 
 template <typename R>
 size_t mix_smem_bytes(int Q)
 {
-    return (size_t)Q * 32 * (CB + 1) * sizeof(cx<R>);
+    return ((size_t)Q * 32 * (CB + 1) + Q) * sizeof(cx<R>);
 }
 
 // tile shapes per precision: PI points x NV 16-byte vectors of channels per thread, 8 channel
