@@ -108,75 +108,126 @@ __device__ __forceinline__ cx<R> ldg_cx(const cx<R> *p)
 }
 
 // Z[q][p][a] = w_q s_slot(q) / inv_scale * sum_(col, c) c x[col][p] over the nonzero pairs of
-// (channel a, factor q). CTA = CB warps (scratch slots a0 .. a0+CB) x 32 points (one per lane).
-// Each channel's pairs are grouped by factor (segments), so a factor's sum stays in a register
-// and reaches shared memory [Q][32][CB + 1] once; x is read through the read-only cache (the
-// same columns recur across factors). The CTA then writes the CB slots of each point as one
-// contiguous segment (lanes = 8 points x 4 slots), skipping factors that no slot of the group
-// has (their scratch stays at the zeros written at upload).
+// (channel a, factor q). CTA = CB warps (scratch slots a0 .. a0+CB) x 32 MPT points (MPT
+// consecutive points per lane, 16-byte source loads). Each channel's pairs are grouped by
+// factor (segments, in factor order), so a factor's sum stays in registers; the factors are
+// taken MQC at a time through shared memory [MQC][MPT][32][CB + 1], and the CTA then writes
+// the CB slots of each point as one contiguous segment (lanes = 8 points x 4 slots),
+// skipping factors that no slot of the group has (their scratch stays at the zeros written
+// at upload).
+template <typename R> struct MixTile;
+template <> struct MixTile<float> { static const int MPT = 4, MQC = 8; };
+template <> struct MixTile<double> { static const int MPT = 2, MQC = 8; };
+
 template <typename R>
 __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales scales,
                                                           const cxd *__restrict__ scales_dev,
                                                           const cx<R> *__restrict__ x,
                                                           const double *__restrict__ inv_scale)
 {
+    constexpr int MPT = MixTile<R>::MPT, MQC = MixTile<R>::MQC, TP = 32 * MPT;
     extern __shared__ __align__(16) unsigned char mix_smem[];
-    cx<R> *acc = reinterpret_cast<cx<R> *>(mix_smem);  // [Q][32][CB + 1]
+    cx<R> *acc = reinterpret_cast<cx<R> *>(mix_smem);  // [MQC][MPT][32][CB + 1]
+    cx<R> *ws = acc + (size_t)MQC * TP * (CB + 1);      // [Q] factor scales
     const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
     const int Q = f.Q;
     const int a0 = blockIdx.y * CB;                      // first scratch slot of the group
     const int a = a0 + wrp < f.A ? f.perm[a0 + wrp] : -1;  // channel of this warp's slot
     const long long NP = (long long)f.N1 * f.N2;
-    const long long p = (long long)blockIdx.x * 32 + lane;
-    const bool live = p < NP;
+    const long long pbase = (long long)blockIdx.x * TP;
+    const long long p0 = pbase + (long long)lane * MPT;  // this lane's first point
+    const bool vec = (NP % 2) == 0;                      // rows start 16-byte aligned
     const double sc = inv_scale ? 1.0 / *inv_scale : 1.0;
-    const int4 *__restrict__ seg = (const int4 *)f.col;  // factor, first pair, last+1 pair
-    const int *__restrict__ pcol = f.nzq;
-    const R *__restrict__ pc = (const R *)f.coef;
-    constexpr int QS = 32 * (CB + 1);  // stride of one factor
-    cx<R> *ws = acc + (size_t)Q * QS;  // [Q] factor scales in the compute precision
     for (int q = threadIdx.x; q < Q; q += 32 * CB) {
         const cxd s = scales_dev ? scales_dev[f.slot[q]] : scales.s[f.slot[q]];
         ws[q] = cvt<R>(sc * (f.w[q] * s));
     }
-    cx<R> *mine = acc + (size_t)lane * (CB + 1) + wrp;
-    for (int q = 0; q < Q; ++q) mine[(size_t)q * QS] = mk<R>((R)0, (R)0);
-    if (a >= 0 && live) {
-        const cx<R> *__restrict__ xp = x + p;
-        for (int g = f.row_ptr[a]; g < f.row_ptr[a + 1]; ++g) {
-            const int4 sg = seg[g];
-            cx<R> s0 = mk<R>((R)0, (R)0), s1 = mk<R>((R)0, (R)0);
-            int z = sg.y;
-            for (; z + 1 < sg.z; z += 2) {  // two independent chains
-                const cx<R> x0 = ldg_cx(xp + (size_t)pcol[z] * NP), x1 = ldg_cx(xp + (size_t)pcol[z + 1] * NP);
-                const R c0 = pc[z], c1 = pc[z + 1];
-                s0.x = fma(c0, x0.x, s0.x); s0.y = fma(c0, x0.y, s0.y);
-                s1.x = fma(c1, x1.x, s1.x); s1.y = fma(c1, x1.y, s1.y);
-            }
-            if (z < sg.z) {
-                const cx<R> x0 = ldg_cx(xp + (size_t)pcol[z] * NP);
-                const R c0 = pc[z];
-                s0.x = fma(c0, x0.x, s0.x); s0.y = fma(c0, x0.y, s0.y);
-            }
-            mine[(size_t)sg.x * QS] = s0 + s1;
-        }
-    }
-    __syncthreads();
+    const int4 *__restrict__ seg = (const int4 *)f.col;  // factor, first pair, last+1 pair
+    const int *__restrict__ pcol = f.nzq;
+    const R *__restrict__ pc = (const R *)f.coef;
     const unsigned char *gf = f.chunk + (size_t)blockIdx.y * Q;  // factors touched by this group
     cx<R> *__restrict__ Z = (cx<R> *)f.Z;
-    for (int t = threadIdx.x; t < Q * 32 * CB; t += 32 * CB) {
-        const int r = t % CB, rest = t / CB;
-        const int pl = rest % 32, q = rest / 32;
-        const long long pp = (long long)blockIdx.x * 32 + pl;
-        if (!gf[q] || pp >= NP) continue;
-        Z[((size_t)q * NP + pp) * f.Ap + a0 + r] = ws[q] * acc[(size_t)q * QS + pl * (CB + 1) + r];
+    int g = a >= 0 ? f.row_ptr[a] : 0;
+    const int g_end = a >= 0 ? f.row_ptr[a + 1] : 0;
+    auto load_x = [&](int col, cx<R> (&v)[MPT]) {
+        const cx<R> *xr = x + (size_t)col * NP + p0;
+        if (vec && p0 + MPT <= NP) {
+            if constexpr (sizeof(R) == 4) {
+#pragma unroll
+                for (int h = 0; h < MPT / 2; ++h) {
+                    const float4 t = __ldg(reinterpret_cast<const float4 *>(xr) + h);
+                    v[2 * h] = mk<R>(t.x, t.y);
+                    v[2 * h + 1] = mk<R>(t.z, t.w);
+                }
+            } else {
+#pragma unroll
+                for (int h = 0; h < MPT; ++h) {
+                    const double2 t = __ldg(reinterpret_cast<const double2 *>(xr) + h);
+                    v[h] = mk<R>(t.x, t.y);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < MPT; ++u) v[u] = p0 + u < NP ? xr[u] : mk<R>((R)0, (R)0);
+        }
+    };
+    for (int qc = 0; qc < Q; qc += MQC) {
+        bool any = false;
+        for (int j = 0; j < MQC && qc + j < Q; ++j) any |= gf[qc + j] != 0;
+        if (!any) continue;  // CTA-uniform
+        for (int j = 0; j < MQC; ++j)
+#pragma unroll
+            for (int u = 0; u < MPT; ++u)
+                acc[(((size_t)j * MPT + u) * 32 + lane) * (CB + 1) + wrp] = mk<R>((R)0, (R)0);
+        for (; g < g_end; ++g) {
+            const int4 sg = seg[g];
+            if (sg.x >= qc + MQC) break;  // segments are in factor order
+            cx<R> s0[MPT], s1[MPT];
+#pragma unroll
+            for (int u = 0; u < MPT; ++u) s0[u] = s1[u] = mk<R>((R)0, (R)0);
+            int z = sg.y;
+            for (; z + 1 < sg.z; z += 2) {  // two independent chains
+                cx<R> x0[MPT], x1[MPT];
+                load_x(pcol[z], x0);
+                load_x(pcol[z + 1], x1);
+                const R c0 = pc[z], c1 = pc[z + 1];
+#pragma unroll
+                for (int u = 0; u < MPT; ++u) {
+                    s0[u].x = fma(c0, x0[u].x, s0[u].x); s0[u].y = fma(c0, x0[u].y, s0[u].y);
+                    s1[u].x = fma(c1, x1[u].x, s1[u].x); s1[u].y = fma(c1, x1[u].y, s1[u].y);
+                }
+            }
+            if (z < sg.z) {
+                cx<R> x0[MPT];
+                load_x(pcol[z], x0);
+                const R c0 = pc[z];
+#pragma unroll
+                for (int u = 0; u < MPT; ++u) {
+                    s0[u].x = fma(c0, x0[u].x, s0[u].x); s0[u].y = fma(c0, x0[u].y, s0[u].y);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < MPT; ++u)
+                acc[(((size_t)(sg.x - qc) * MPT + u) * 32 + lane) * (CB + 1) + wrp] = s0[u] + s1[u];
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < MQC * TP * CB; t += 32 * CB) {
+            const int r = t % CB, rest = t / CB;
+            const int pl = rest % TP, j = rest / TP;
+            const int q = qc + j;
+            const long long pp = pbase + pl;
+            if (q >= Q || !gf[q] || pp >= NP) continue;
+            const int u = pl % MPT, ln = pl / MPT;
+            Z[((size_t)q * NP + pp) * f.Ap + a0 + r] = ws[q] * acc[(((size_t)j * MPT + u) * 32 + ln) * (CB + 1) + r];
+        }
+        __syncthreads();
     }
 }
 
 template <typename R>
 size_t mix_smem_bytes(int Q)
 {
-    return ((size_t)Q * 32 * (CB + 1) + Q) * sizeof(cx<R>);
+    return ((size_t)MixTile<R>::MQC * 32 * MixTile<R>::MPT * (CB + 1) + Q) * sizeof(cx<R>);
 }
 
 // tile shapes per precision: PI points x NV 16-byte vectors of channels per thread, 8 channel
@@ -342,7 +393,8 @@ int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, c
     const FactArgs fa = args_of(fd, op->ctx->d_err);
     cudaStream_t s = op->ctx->stream;
     const long long NP = (long long)fd.N1 * fd.N2;
-    dim3 g1((unsigned)((NP + 31) / 32), (unsigned)((fd.A + CB - 1) / CB));
+    const int TP = 32 * MixTile<R>::MPT;
+    dim3 g1((unsigned)((NP + TP - 1) / TP), (unsigned)((fd.A + CB - 1) / CB));
     fact_mix_kernel<R><<<g1, 32 * CB, mix_smem_bytes<R>(fd.Q), s>>>(fa, scales, scales_dev, (const cx<R> *)src,
                                                                      inv_scale);
     op->ctx->launches++;
