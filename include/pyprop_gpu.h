@@ -212,6 +212,19 @@ int pg_prec_blockdiag_create(pg_op *op, const double *overlap_rows, const double
  * block solve along each radial rank). */
 int pg_prec_kron_create(pg_op *op, const double *overlap_rows, const double *cS, const double *cH,
                         const double *h1, const double *h2, pg_banded **out);
+/* Two-electron radial preconditioner by fast diagonalization: per angular channel a the exact
+ * inverse of cS S x S + cH (h_l1 x S + S x h_l2), applied as (V1 x V2) D_a (V1 x V2)^T with the
+ * generalized eigenvectors of the one-electron Hamiltonians (h_l V_l = S V_l Lambda_l,
+ * V_l^T S V_l = 1). V: host float64 [nl][N][N] (V[l][k][i] = component k of eigenvector i),
+ * lam [nl][N], lidx [Nang][2] the eigenvector set of each channel's two electrons. In place of
+ * the reference's per-channel sparse LU / ILU block preconditioners
+ * (examples/tensor/helium_stabilization/preconditioner.py:77-244): exact for every term but
+ * the electron-electron repulsion. Requires N1 = N2 <= pg_prec_fd_max_n(precision) (the
+ * channel block lives in shared memory); PG_ERR_SHAPE otherwise. Applied by
+ * PG_BAND_PREC_SOLVE (one kernel). */
+int pg_prec_fd_create(pg_op *op, int nl, const double *V, const double *lam, const int *lidx, const double *cS,
+                      const double *cH, pg_banded **out);
+int pg_prec_fd_max_n(int precision);
 int pg_banded_destroy(pg_banded *b);
 
 enum {

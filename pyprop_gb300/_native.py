@@ -73,6 +73,8 @@ _SIGS = {
     "pg_op_finalize": (_I, [_P]),
     "pg_op_variant": (_I, [_P, _I, _IP, C.POINTER(C.c_float)]),
     "pg_op_stored_elements": (_LL, [_P]),
+    "pg_prec_fd_create": (_I, [_P, _I, _DP, _DP, _IP, _DP, _DP, C.POINTER(_P)]),
+    "pg_prec_fd_max_n": (_I, [_I]),
     "pg_op_add_factored": (_I, [_P, _I, _DP, _DP, _IP, _LL, _IP, _IP, _IP, _DP]),
     "pg_op_factored_info": (_I, [_P, _DP]),
     "pg_op_matvec": (_I, [_P, _DP, _I, _P, _P, _I]),

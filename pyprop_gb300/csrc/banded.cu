@@ -580,6 +580,9 @@ extern "C" int pg_banded_destroy(pg_banded *b)
     for (void *p : {e->d_lo_inv1, e->d_lo_cpl1, e->d_lo_rb1, e->d_up_inv1, e->d_up_cpl1, e->d_up_rb1}) cudaFree(p);
     cudaFree(e->d_scratch);
     cudaFree(e->d_swap);
+    cudaFree(e->d_fdV);
+    cudaFree(e->d_fdD);
+    cudaFree(e->d_fdl);
     delete e;
     return PG_OK;
 }
@@ -679,6 +682,7 @@ static int banded_apply_t(pg_banded *bb, int which, void *x)
         return launch_tri<R, R>(b, true, true, x);
     case PG_BAND_PREC_SOLVE:
         if (b->kind == 1) return launch_tri<R, cx<R>>(b, true, true, x);
+        if (b->kind == 3) return pg_fd_apply_dev(b, x);
         if (b->kind == 2) {
             // (A1 x A2)^-1 = (A1^-1 x 1)(1 x A2^-1): the second electron's rank as fibres, then
             // the first electron's rank on the swapped copy
@@ -718,3 +722,61 @@ int pg_banded_apply_dev(pg_banded *b, int which, void *x)
 extern "C" int pg_banded_apply(pg_banded *b, int which, void *x) { return pg_banded_apply_dev(b, which, x); }
 
 int pg_banded_solve_kernels(const pg_banded *b) { return b->kind == 2 ? 4 : 1; }
+
+// Two-electron preconditioner by fast diagonalization (fdprec.cu): per channel a the exact
+// inverse of cS S x S + cH (h_l1 x S + S x h_l2) from the generalized eigenvectors
+// V_l (h_l V = S V Lambda, V^T S V = 1) of the one-electron Hamiltonians.
+extern "C" int pg_prec_fd_create(pg_op *op, int nl, const double *V, const double *lam, const int *lidx,
+                                 const double *cS, const double *cH, pg_banded **out)
+{
+    if (!op || nl < 1 || !V || !lam || !lidx || !cS || !cH || !out) return PG_ERR_ARG;
+    if (!op->finalized) return PG_ERR_STATE;
+    if (op->rank != 3 || op->shape[1] != op->shape[2]) return PG_ERR_STORAGE;
+    const int A = op->shape[0], N = op->shape[1];
+    const int NP = (N + 3) & ~3;
+    for (int a = 0; a < 2 * A; ++a)
+        if (lidx[a] < 0 || lidx[a] >= nl) return PG_ERR_ARG;
+    PG_TRY(pg_fd_prepare(op->precision, NP));
+    const zd zS(cS[0], cS[1]), zH(cH[0], cH[1]);
+    std::vector<double> Vp((size_t)nl * NP * NP, 0.0);
+    for (int l = 0; l < nl; ++l)
+        for (int k = 0; k < N; ++k)
+            for (int i = 0; i < N; ++i) Vp[((size_t)l * NP + k) * NP + i] = V[((size_t)l * N + k) * N + i];
+    std::vector<zd> D((size_t)A * N * N);
+    for (int a = 0; a < A; ++a) {
+        const double *L1 = lam + (size_t)lidx[2 * a] * N, *L2 = lam + (size_t)lidx[2 * a + 1] * N;
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) D[((size_t)a * N + i) * N + j] = 1.0 / (zS + zH * (L1[i] + L2[j]));
+    }
+    pg_banded_ext *bd = new pg_banded_ext();
+    bd->op = op;
+    bd->kind = 3;
+    bd->N = N;
+    bd->kb = op->kb;
+    bd->nmat = A;
+    bd->complex_coef = 1;
+    bd->fdN = N;
+    bd->fdNP = NP;
+    PG_CUDA_TRY(cudaMalloc(&bd->d_fdl, sizeof(int) * 2 * A));
+    PG_CUDA_TRY(cudaMemcpy(bd->d_fdl, lidx, sizeof(int) * 2 * A, cudaMemcpyHostToDevice));
+    if (op->precision == PG_FP64) {
+        PG_CUDA_TRY(cudaMalloc(&bd->d_fdV, sizeof(double) * Vp.size()));
+        PG_CUDA_TRY(cudaMemcpy(bd->d_fdV, Vp.data(), sizeof(double) * Vp.size(), cudaMemcpyHostToDevice));
+        std::vector<cxd> Dd(D.size());
+        for (size_t t = 0; t < D.size(); ++t) Dd[t] = mk<double>(D[t].real(), D[t].imag());
+        PG_CUDA_TRY(cudaMalloc(&bd->d_fdD, sizeof(cxd) * Dd.size()));
+        PG_CUDA_TRY(cudaMemcpy(bd->d_fdD, Dd.data(), sizeof(cxd) * Dd.size(), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> Vf(Vp.begin(), Vp.end());
+        PG_CUDA_TRY(cudaMalloc(&bd->d_fdV, sizeof(float) * Vf.size()));
+        PG_CUDA_TRY(cudaMemcpy(bd->d_fdV, Vf.data(), sizeof(float) * Vf.size(), cudaMemcpyHostToDevice));
+        std::vector<cxf> Df(D.size());
+        for (size_t t = 0; t < D.size(); ++t) Df[t] = mk<float>((float)D[t].real(), (float)D[t].imag());
+        PG_CUDA_TRY(cudaMalloc(&bd->d_fdD, sizeof(cxf) * Df.size()));
+        PG_CUDA_TRY(cudaMemcpy(bd->d_fdD, Df.data(), sizeof(cxf) * Df.size(), cudaMemcpyHostToDevice));
+    }
+    *out = bd;
+    return PG_OK;
+}
+
+extern "C" int pg_prec_fd_max_n(int precision) { return pg_fd_max_n(precision); }

@@ -714,7 +714,7 @@ extern "C" int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64,
     if (!op64 || !op_basis || !prec64 || !prec_basis || !out) return PG_ERR_ARG;
     if (basis_size < 2 || basis_size > GM_MAXM || basis_size > PG_RED_COLS - 2) return PG_ERR_ARG;
     if (op64->precision != PG_FP64 || op_basis->precision != basis_precision) return PG_ERR_ARG;
-    if ((prec64->kind != 1 && prec64->kind != 2) || (prec_basis->kind != 1 && prec_basis->kind != 2)) return PG_ERR_ARG;
+    if (prec64->kind < 1 || prec64->kind > 3 || prec_basis->kind < 1 || prec_basis->kind > 3) return PG_ERR_ARG;
     if (prec64->op->precision != PG_FP64 || prec_basis->op->precision != basis_precision) return PG_ERR_ARG;
     if (basis_precision != PG_FP64 && basis_precision != PG_FP32) return PG_ERR_ARG;
     pg_cayley *c = new pg_cayley();

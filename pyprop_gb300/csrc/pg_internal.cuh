@@ -242,7 +242,19 @@ struct pg_banded {
     void *d_lo_inv1 = nullptr, *d_lo_cpl1 = nullptr, *d_lo_rb1 = nullptr;
     void *d_up_inv1 = nullptr, *d_up_cpl1 = nullptr, *d_up_rb1 = nullptr;
     int fib_per_mat1 = 1;
+    // kind 3: fast diagonalization per channel (fdprec.cu): eigenvectors V_l [nl][NP][NP]
+    // (row k, column = eigenvector), the inverse spectra D [A][N][N] (complex), the eigenvector
+    // set of each channel's two electrons [A][2]
+    void *d_fdV = nullptr, *d_fdD = nullptr;
+    int *d_fdl = nullptr;
+    int fdN = 0, fdNP = 0;
 };
+
+// kind-3 solve x <- M^-1 x on every channel (fdprec.cu); largest supported radial size
+int pg_fd_apply_dev(pg_banded *b, void *x);
+int pg_fd_max_n(int precision);
+// checks the shared memory the solve needs for padded size NP and raises the kernel's limit
+int pg_fd_prepare(int precision, int NP);
 
 int pg_banded_apply_dev(pg_banded *b, int which, void *x);
 // kernels one PG_BAND_PREC_SOLVE launches (a two-electron Kronecker preconditioner: 2 solves, 2 swaps)

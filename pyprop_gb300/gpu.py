@@ -274,6 +274,23 @@ class Banded:
         check(op.lib.pg_prec_kron_create(op.h, rp, csp, chp, a1p, a2p, C.byref(h)), "pg_prec_kron_create")
         return cls(op, h)
 
+    @classmethod
+    def fast_diagonalization(cls, op, V, lam, lidx, cS, cH):
+        """Two-electron radial preconditioner by fast diagonalization (pg_prec_fd_create):
+        V [nl][N][N] generalized eigenvectors (columns), lam [nl][N], lidx [Nang][2]."""
+        v, vp = nat.dptr(np.ascontiguousarray(V, dtype=np.float64))
+        l, lp = nat.dptr(np.ascontiguousarray(lam, dtype=np.float64))
+        li, lip = nat.iptr(np.ascontiguousarray(lidx, dtype=np.int32))
+        cs, csp = nat.dptr(np.array([cS], dtype=np.complex128).view(np.float64))
+        ch, chp = nat.dptr(np.array([cH], dtype=np.complex128).view(np.float64))
+        h = C.c_void_p()
+        check(op.lib.pg_prec_fd_create(op.h, len(V), vp, lp, lip, csp, chp, C.byref(h)), "pg_prec_fd_create")
+        return cls(op, h)
+
+    @staticmethod
+    def fast_diagonalization_max_n(ctx, precision):
+        return int(ctx.lib.pg_prec_fd_max_n(precision))
+
     def apply(self, which, x):
         self.op.ctx.bind_stream()
         check(self.lib.pg_banded_apply(self.h, which, ptr(x)), "pg_banded_apply")

@@ -266,9 +266,64 @@ class TwoElectronKroneckerPreconditioner(BSplinePreconditioner):
                                              h1, h2)
 
 
+class TwoElectronFastDiagonalizationPreconditioner(TwoElectronKroneckerPreconditioner):
+    """Two-electron radial preconditioner for the Cayley step: per coupled channel the exact
+    inverse of the part of the channel block that is separable in r1 and r2,
+        M_a = cS S x S + cH (h_l1 x S + S x h_l2),
+    by fast diagonalization: with the generalized eigenvectors h_l V_l = S V_l Lambda_l
+    (V^T S V = 1, from scipy on the host once per l), M_a^-1 = (V1 x V2) D_a (V1 x V2)^T with
+    D_a = 1 / (cS + cH (lambda_l1 + lambda_l2)), four dense N x N products per channel on the
+    device. Unlike the Kronecker product (cS S + cH h1) x (cS S + cH h2), it has no cH^2 h1 x h2
+    error, so GMRES is left only with the electron-electron repulsion that the reference's
+    RadialTwoElectronPreconditionerSuperLU / Ifpack also put in the block
+    (examples/tensor/helium_stabilization/preconditioner.py:77-244). For radial sizes beyond
+    the shared-memory limit of the device kernel it falls back to the Kronecker product."""
+
+    def _dense(self, l):
+        band = self._one_electron(l).real  # rows [N][2k+1], [i, k + j - i] = h(i, j)
+        N, b = band.shape
+        kb = (b - 1) // 2
+        D = np.zeros((N, N))
+        for d in range(-kb, kb + 1):
+            i = np.arange(max(0, -d), min(N, N - d))
+            D[i, i + d] = band[i, kb + d]
+        return 0.5 * (D + D.T)
+
+    def Setup(self, prop, precision=nat.PG_FP64):
+        import scipy.linalg as sl
+        repr_ = self.psi.GetRepresentation()
+        shape = repr_.GetFullShape()
+        if len(shape) != 3:
+            raise ValueError("TwoElectronFastDiagonalizationPreconditioner needs a two-electron representation")
+        ctx = Context.get()
+        N = shape[1]
+        if any(N > Banded.fast_diagonalization_max_n(ctx, p) for p in (nat.PG_FP64, precision)):
+            self.Method = "kronecker-product"
+            return TwoElectronKroneckerPreconditioner.Setup(self, prop, precision)
+        self.Method = "fast-diagonalization"
+        indices = repr_.bases[0].indices
+        S = repr_.radial.BSplineObject.dense(repr_.overlap_rows)
+        ls = sorted(set(ix.l1 for ix in indices) | set(ix.l2 for ix in indices))
+        pos = {l: k for k, l in enumerate(ls)}
+        V, lam = [], []
+        for l in ls:
+            w, v = sl.eigh(self._dense(l), S)
+            V.append(v)
+            lam.append(w)
+        lidx = np.array([(pos[ix.l1], pos[ix.l2]) for ix in indices], dtype=np.int32)
+        self.ops, self.solvers = {}, {}
+        for prec in (nat.PG_FP64, precision):
+            if prec in self.solvers:
+                continue
+            op = DeviceOperator(ctx, [], shape, repr_.kb, prec)
+            self.ops[prec] = op
+            self.solvers[prec] = Banded.fast_diagonalization(op, np.stack(V), np.stack(lam), lidx,
+                                                             self.OverlapScaling, self.HamiltonianScaling)
+
+
 # the reference's two-electron preconditioner names select the GPU one
-RadialTwoElectronPreconditionerSuperLU = TwoElectronKroneckerPreconditioner
-RadialTwoElectronPreconditionerIfpack = TwoElectronKroneckerPreconditioner
+RadialTwoElectronPreconditionerSuperLU = TwoElectronFastDiagonalizationPreconditioner
+RadialTwoElectronPreconditionerIfpack = TwoElectronFastDiagonalizationPreconditioner
 
 
 class CayleyPropagatorGPU(PropagatorBase):

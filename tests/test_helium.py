@@ -143,3 +143,24 @@ def test_factored_terms_expand_to_the_per_pair_data():
                        [g.GetBasisPairs() for g in p.GeometryList], None, None, repr_.kb, shape=shape)
         t.multiply(x, y2, 0.7 if p.IsTimeDependent else 1.0)
     assert np.linalg.norm(y1 - y2) < 1e-12 * np.linalg.norm(y2)
+
+
+def test_fast_diagonalization_inverts_the_separable_channel_block():
+    """(V1 x V2) D (V1 x V2)^T, from the generalized eigenvectors of the one-electron radial
+    Hamiltonians, is the inverse of cS S x S + cH (h_l1 x S + S x h_l2) (the separable part of
+    a channel block of the Cayley matrix)."""
+    import scipy.linalg as sl
+    from pyprop_gb300.propagator import TwoElectronFastDiagonalizationPreconditioner
+    prob = helium_problem(lmax=1, nbsplines=14, rmax=12.0)
+    repr_ = prob.psi.GetRepresentation()
+    pre = TwoElectronFastDiagonalizationPreconditioner(prob.psi)
+    pre.Z, pre.Mass = 2.0, 1.0
+    S = repr_.radial.BSplineObject.dense(repr_.overlap_rows)
+    cS, cH = 1.0, 0.5j * 0.01
+    h0, h1 = pre._dense(0), pre._dense(1)
+    w0, v0 = sl.eigh(h0, S)
+    w1, v1 = sl.eigh(h1, S)
+    M = cS * np.kron(S, S) + cH * (np.kron(h0, S) + np.kron(S, h1))
+    D = 1.0 / (cS + cH * (w0[:, None] + w1[None, :]))
+    Minv = np.kron(v0, v1) @ np.diag(D.ravel()) @ np.kron(v0, v1).T
+    assert np.abs(Minv @ M - np.eye(M.shape[0])).max() < 1e-10
