@@ -283,6 +283,51 @@ def time_two_electron(torch, reps=5):
     return avg, info["flops_mix"] + info["flops_radial"], info
 
 
+def time_two_electron_steps(torch, steps=3, warmup=1):
+    """Cayley steps of the two-electron model of time_two_electron (complex64 matvec with FP64
+    refinement, against the plain FP64 path), fast-diagonalization radial preconditioner, a
+    length-gauge field on: (dict of steps/s, GMRES iterations, infidelity between the paths)."""
+    import pyprop_gb300 as pp
+    from pyprop_gb300.workloads import helium
+    out, states = {}, {}
+    psi0 = None
+    for prec in ("fp32", "fp64"):
+        prob = pp.Problem(pp.LoadString(helium(propagator="CayleyPropagatorGPU", precision=prec, amplitude=0.05,
+                                               frequency=0.5, pulse_duration=20.0, duration=20.0, timestep=0.01,
+                                               **TWO_ELECTRON)))
+        prob.SetupStep(skipWavefunctionSetup=True)
+        shape = prob.psi.GetRepresentation().GetFullShape()
+        if psi0 is None:
+            rng = np.random.default_rng(1)
+            decay = np.exp(-0.1 * np.arange(shape[1]))
+            psi0 = np.zeros(shape, complex)
+            psi0[0] = rng.standard_normal(shape[1:]) * decay[:, None] * decay[None, :]
+            psi0 /= np.linalg.norm(psi0)
+        prob.psi.GetData().copy_(torch.as_tensor(psi0, device="cuda"))
+        prob.PropagatedTime = 1.0
+        for _ in range(warmup):
+            prob.AdvanceStep()
+        torch.cuda.synchronize()
+        stream = torch.cuda.current_stream()
+        s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        iters = 0
+        s_ev.record(stream)
+        for _ in range(steps):
+            prob.AdvanceStep()
+            iters += prob.Propagator.LastStats.Iterations
+        e_ev.record(stream)
+        e_ev.synchronize()
+        out[prec] = {"steps_per_s": steps / (s_ev.elapsed_time(e_ev) * 1e-3), "gmres_iterations_per_step": iters / steps,
+                     "preconditioner": prob.Propagator.Preconditioner.Method}
+        states[prec] = prob.psi.numpy()
+        del prob
+    a, b = states["fp32"], states["fp64"]
+    out["infidelity_mixed_vs_fp64"] = float(1.0 - abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real))
+    out["speedup_mixed_vs_fp64"] = out["fp32"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    out["steps"] = steps
+    return out
+
+
 def profile_two_electron():
     """Profiling entry point: three factorized two-electron matvecs (the sizes of
     time_two_electron) after two warm-up launches."""
@@ -412,6 +457,7 @@ def run_ours(args):
     avg_ts, bytes_ts = time_block_solve(torch, prob, flush)
     avg_lg, bytes_lg, variant_lg = time_large_matvec(torch, flush)
     two_e = time_two_electron(torch) if args.two_electron else None
+    two_e_steps = time_two_electron_steps(torch) if args.two_electron else None
     peak, peak_kind = measured_peaks()
 
     ens = run_ensemble(args, torch, flush) if args.ensemble > 0 else None
@@ -459,6 +505,7 @@ def run_ours(args):
                 "workload": "helium-like, coupled L<=5, l1,l2<=10, 80 B-splines per electron (rank 3, factorized "
                             "repulsion multipoles + field-free terms), complex64, 5 launches back to back",
                 "info": two_e[2]},
+            "two_electron_cayley": two_e_steps,
             "cpu_baseline": cpu,
             "ensemble": ens,
             "clocks": clk.summary(),
