@@ -19,7 +19,7 @@ from .problem import InitBSpline, InitialConditionType, Problem, core
 from .propagator import (BasisPropagator, BasisPropagatorGPU, BSplinePreconditioner, CayleyPropagator,
                          CayleyPropagatorGPU, PamPropagator, PamPropagatorGPU, RadialPreconditioner,
                          RadialTwoElectronPreconditionerIfpack, RadialTwoElectronPreconditionerSuperLU,
-                         TwoElectronKroneckerPreconditioner)
+                         TwoElectronFastDiagonalizationPreconditioner, TwoElectronKroneckerPreconditioner)
 from .solver import PiramSolver, PiramSolverGPU
 from .spherical import DefaultCoupledIndexIterator
 

@@ -246,6 +246,7 @@ class TwoElectronKroneckerPreconditioner(BSplinePreconditioner):
         shape = repr_.GetFullShape()
         if len(shape) != 3:
             raise ValueError("TwoElectronKroneckerPreconditioner needs a two-electron representation")
+        self.Method = "kronecker-product"
         indices = repr_.bases[0].indices
         cache = {}
 
@@ -298,7 +299,6 @@ class TwoElectronFastDiagonalizationPreconditioner(TwoElectronKroneckerPrecondit
         ctx = Context.get()
         N = shape[1]
         if any(N > Banded.fast_diagonalization_max_n(ctx, p) for p in (nat.PG_FP64, precision)):
-            self.Method = "kronecker-product"
             return TwoElectronKroneckerPreconditioner.Setup(self, prop, precision)
         self.Method = "fast-diagonalization"
         indices = repr_.bases[0].indices

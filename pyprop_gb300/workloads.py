@@ -134,7 +134,8 @@ time_function = LaserFunctionSimpleLength
 
 def helium(lmax=2, L=(0,), nbsplines=20, rmax=20.0, order=7, quad_order_additional=10, z=2.0,
            propagator="PamPropagatorGPU", precision="fp64", timestep=0.01, duration=1.0, krylov_basis_size=20,
-           amplitude=0.0, frequency=1.0, pulse_duration=10.0, gmres_tolerance=1e-12, factorize=True):
+           amplitude=0.0, frequency=1.0, pulse_duration=10.0, gmres_tolerance=1e-12, factorize=True,
+           preconditioner_type="RadialTwoElectronPreconditionerSuperLU"):
     """Two-electron (helium-like) model in the layout of
     examples/tensor/helium_stabilization/config.ini:1-188: coupled spherical harmonics
     (``DefaultCoupledIndexIterator(lmax, L, M=0)``) x B-splines x B-splines, radial kinetic
@@ -150,7 +151,7 @@ def helium(lmax=2, L=(0,), nbsplines=20, rmax=20.0, order=7, quad_order_addition
     prec_key = 'preconditioner = "RadialPreconditioner"' if cayley else ""
     prec_sec = f"""
 [RadialPreconditioner]
-type = RadialTwoElectronPreconditionerSuperLU
+type = {preconditioner_type}
 z = {z!r}
 """ if cayley else ""
     laser = f"""

@@ -139,8 +139,10 @@ def test_learned_preconditioner_on_the_two_electron_model(gpu):
     from pyprop_gb300.learned import LearnedPreconditioner
     from tests.helpers import helium_problem
     prob = helium_problem(lmax=1, nbsplines=14, rmax=12.0, L=(0, 1), amplitude=0.1, frequency=1.0,
-                          pulse_duration=4.0, duration=4.0, propagator="CayleyPropagatorGPU", precision="fp32")
+                          pulse_duration=4.0, duration=4.0, propagator="CayleyPropagatorGPU", precision="fp32",
+                          preconditioner_type="TwoElectronKroneckerPreconditioner")
     prob.SetupStep(skipWavefunctionSetup=True)
+    assert prob.Propagator.Preconditioner.__class__.__name__ == "TwoElectronKroneckerPreconditioner"
     pots = prob.Propagator.BasePropagator.PotentialList
     r12 = [i for i, p in enumerate(pots) if "ElectronicCoupling" in p.Name][0]
     shape = prob.psi.GetRepresentation().GetFullShape()
