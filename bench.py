@@ -329,19 +329,29 @@ def time_two_electron_steps(torch, steps=3, warmup=1):
 
 
 def profile_two_electron():
-    """Profiling entry point: three factorized two-electron matvecs (the sizes of
-    time_two_electron) after two warm-up launches."""
+    """Profiling entry point: the two-electron model of time_two_electron set up for mixed
+    Cayley steps; five complex64 matvecs of its operator (overlap slot + factorized terms),
+    then three solves of its fast-diagonalization preconditioner."""
     import torch
+    import pyprop_gb300 as pp
     from pyprop_gb300 import _native as nat
-    prob, op = _two_electron_operator(nat.PG_FP32)
+    from pyprop_gb300.workloads import helium
+    prob = pp.Problem(pp.LoadString(helium(propagator="CayleyPropagatorGPU", precision="fp32", **TWO_ELECTRON)))
+    prob.SetupStep(skipWavefunctionSetup=True)
+    prop = prob.Propagator
+    op = prop.opb
     shape = prob.psi.GetRepresentation().GetFullShape()
     src = torch.randn(shape, dtype=torch.complex64, device="cuda")
     dst = torch.zeros_like(src)
-    sc = op.scales(0.0)
+    sc = op.scales(0.0, 0.005j, 1.0)
     for _ in range(5):
         op.matvec(sc, src, dst)
+    solver = prop.Preconditioner.solvers[nat.PG_FP32]
+    for _ in range(3):
+        solver.apply(nat.PG_BAND_PREC_SOLVE, dst)
     torch.cuda.synchronize()
-    print(json.dumps({"profile": "two_electron", "info": op.factored_info()}))
+    print(json.dumps({"profile": "two_electron", "info": op.factored_info(),
+                      "preconditioner": prop.Preconditioner.Method}))
 
 
 def fp32_fma_peak_tflops():
