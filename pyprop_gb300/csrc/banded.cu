@@ -169,12 +169,12 @@ __global__ void __launch_bounds__(32 * NW, 1)
 
 // U x (up=1) or U^T x (up=0), U real upper with kb super diagonals, rows [N][kb+1]
 template <typename R>
-__global__ void tri_mul_kernel(int N, int kb, const R *__restrict__ U, const cx<R> *__restrict__ x,
+__global__ void tri_mul_kernel(int nfib, int N, int kb, const R *__restrict__ U, const cx<R> *__restrict__ x,
                                cx<R> *__restrict__ y, int up)
 {
-    const int f = blockIdx.y;
+    const int f = pg_grid_row();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
+    if (i >= N || f >= nfib) return;
     const cx<R> *xf = x + (size_t)f * N;
     cx<R> acc = mk<R>((R)0, (R)0);
     if (up) {
@@ -187,12 +187,12 @@ __global__ void tri_mul_kernel(int N, int kb, const R *__restrict__ U, const cx<
 
 // S x with S rows [N][2kb+1]
 template <typename R>
-__global__ void band_mul_kernel(int N, int kb, const R *__restrict__ S, const cx<R> *__restrict__ x,
+__global__ void band_mul_kernel(int nfib, int N, int kb, const R *__restrict__ S, const cx<R> *__restrict__ x,
                                 cx<R> *__restrict__ y)
 {
-    const int f = blockIdx.y;
+    const int f = pg_grid_row();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
+    if (i >= N || f >= nfib) return;
     const cx<R> *xf = x + (size_t)f * N;
     cx<R> acc = mk<R>((R)0, (R)0);
     for (int d = 0; d <= 2 * kb; ++d) {
@@ -652,12 +652,12 @@ static int banded_apply_t(pg_banded *bb, int which, void *x)
     pg_ctx *ctx = b->op->ctx;
     const int N = b->N, kb = b->kb, nfib = b->op->nrows;
     const size_t bytes = sizeof(cx<R>) * (size_t)nfib * N;
-    dim3 grid((N + 127) / 128, nfib);
+    const dim3 grid = pg_row_grid((N + 127) / 128, nfib);
     switch (which) {
     case PG_BAND_MUL_U:
     case PG_BAND_MUL_UT:
         if (b->kind != 0) return PG_ERR_STATE;
-        tri_mul_kernel<R><<<grid, 128, 0, ctx->stream>>>(N, kb, (const R *)b->d_U, (const cx<R> *)x,
+        tri_mul_kernel<R><<<grid, 128, 0, ctx->stream>>>(nfib, N, kb, (const R *)b->d_U, (const cx<R> *)x,
                                                         (cx<R> *)b->d_scratch, which == PG_BAND_MUL_U);
         ctx->launches++;
         PG_TRY(pg_check_launch(ctx));
@@ -665,7 +665,7 @@ static int banded_apply_t(pg_banded *bb, int which, void *x)
         return PG_OK;
     case PG_BAND_MUL_S:
         if (b->kind != 0) return PG_ERR_STATE;
-        band_mul_kernel<R><<<grid, 128, 0, ctx->stream>>>(N, kb, (const R *)b->d_S, (const cx<R> *)x,
+        band_mul_kernel<R><<<grid, 128, 0, ctx->stream>>>(nfib, N, kb, (const R *)b->d_S, (const cx<R> *)x,
                                                          (cx<R> *)b->d_scratch);
         ctx->launches++;
         PG_TRY(pg_check_launch(ctx));

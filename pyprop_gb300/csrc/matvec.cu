@@ -117,10 +117,10 @@ __global__ void __launch_bounds__(128) op_matvec_kernel(OpDev op, pg_scales scal
                                                         int accumulate, const double *__restrict__ src_inv_scale,
                                                         cx<R> *__restrict__ src_copy_out)
 {
-    const int r = blockIdx.y;
+    const int r = pg_grid_row();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = op.N;
-    if (i >= N) return;
+    if (i >= N || r >= op.nrows) return;
     const int kb = (KB >= 0) ? KB : op.kb;
     const int b = 2 * kb + 1;
     const cx<R> *bands = (const cx<R> *)op.bands;
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(128) op_matvec_kernel(OpDev op, pg_scales scal
 // angular row; the source row is staged through shared memory in tiles of 128, and D is
 // stored transposed ([j][i]) so the threads of a warp read consecutive i.
 template <typename R>
-__global__ void __launch_bounds__(128) op_dense_kernel(int N, const int *__restrict__ row_ptr,
+__global__ void __launch_bounds__(128) op_dense_kernel(int N, int nrows, const int *__restrict__ row_ptr,
                                                        const int *__restrict__ ent_col, const int *__restrict__ ent_mat,
                                                        const int *__restrict__ ent_slot, const cx<R> *__restrict__ dense,
                                                        pg_scales scales, const cxd *__restrict__ scales_dev,
@@ -172,7 +172,8 @@ __global__ void __launch_bounds__(128) op_dense_kernel(int N, const int *__restr
                                                        const double *__restrict__ src_inv_scale)
 {
     __shared__ cx<R> xs[128];
-    const int r = blockIdx.y;
+    const int r = pg_grid_row();
+    if (r >= nrows) return;
     const int i = blockIdx.x * 128 + threadIdx.x;
     const R sc = src_inv_scale ? (R)(1.0 / *src_inv_scale) : (R)1;
     cx<R> acc = mk<R>((R)0, (R)0);
@@ -266,7 +267,8 @@ __global__ void __launch_bounds__(BT) op_matvec_bulk_kernel(OpDev op, pg_scales 
     unsigned long long *bar = (unsigned long long *)mv_smem;
     cx<R> *bs = (cx<R> *)(mv_smem + 128);            // [GE][B][BT]
     cx<R> *xs = bs + (size_t)GE * B * BT;          // [GE][BT + 2KB]
-    const int r = blockIdx.y;
+    const int r = pg_grid_row();
+    if (r >= op.nrows) return;  // CTA-uniform, before any barrier
     const int i0 = blockIdx.x * BT;
     const int t = threadIdx.x;
     const int N = op.N;
@@ -523,7 +525,7 @@ static int launch_bulk_bt(pg_op *op, const pg_scales &scales, const cxd *scales_
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = true;
     }
-    dim3 grid((op->N + BT - 1) / BT, op->nrows);
+    const dim3 grid = pg_row_grid((op->N + BT - 1) / BT, op->nrows);
     op_matvec_bulk_kernel<R, KB, BT, MODE, GE><<<grid, BT, smem, op->ctx->stream>>>(
         op->dev(), scales, scales_dev, (const cx<R> *)src, (cx<R> *)dst, accumulate, op->ctx->d_err, op->tmap,
         (const cx<R> *)op->d_bands_rm);
@@ -550,7 +552,7 @@ static int launch_op_matvec(pg_op *op, const pg_scales &scales, const cxd *scale
                             int accumulate, const double *inv_scale, void *copy_out)
 {
     dim3 block(128);
-    dim3 grid((op->N + 127) / 128, op->nrows);
+    const dim3 grid = pg_row_grid((op->N + 127) / 128, op->nrows);
     cudaStream_t s = op->ctx->stream;
     const OpDev d = op->dev();
     const cx<R> *x = (const cx<R> *)src;
@@ -570,8 +572,8 @@ template <typename R>
 static int launch_dense(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
                         const double *inv_scale)
 {
-    dim3 grid((op->N + 127) / 128, op->nrows);
-    op_dense_kernel<R><<<grid, 128, 0, op->ctx->stream>>>(op->N, op->d_drow_ptr, op->d_dent_col, op->d_dent_mat,
+    const dim3 grid = pg_row_grid((op->N + 127) / 128, op->nrows);
+    op_dense_kernel<R><<<grid, 128, 0, op->ctx->stream>>>(op->N, op->nrows, op->d_drow_ptr, op->d_dent_col, op->d_dent_mat,
                                                           op->d_dent_slot, (const cx<R> *)op->d_dense, scales,
                                                           scales_dev, (const cx<R> *)src, (cx<R> *)dst, inv_scale);
     op->ctx->launches++;

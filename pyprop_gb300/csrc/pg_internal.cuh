@@ -95,6 +95,16 @@ int pg_ctx_ensure_reduction(pg_ctx *ctx);
 // ------------------------------------------------------------------------------------
 static const int PG_MAX_SLOTS = 16;
 
+// Row-indexed launches: rows spread over grid y and z (gridDim.y is limited to 65535, a
+// two-electron operator has Nang * N rows).
+static const int PG_GRID_Y = 65535;
+__host__ inline dim3 pg_row_grid(unsigned tiles, long long rows)
+{
+    const long long y = rows < PG_GRID_Y ? rows : PG_GRID_Y;
+    return dim3(tiles, (unsigned)(y > 0 ? y : 1), (unsigned)((rows + PG_GRID_Y - 1) / PG_GRID_Y > 0 ? (rows + PG_GRID_Y - 1) / PG_GRID_Y : 1));
+}
+__device__ __forceinline__ int pg_grid_row() { return (int)(blockIdx.y + (unsigned)PG_GRID_Y * blockIdx.z); }
+
 struct pg_scales {
     cxd s[PG_MAX_SLOTS];
 };
