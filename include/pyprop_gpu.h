@@ -267,6 +267,22 @@ int pg_pamp_destroy(pg_pamp *p);
 /* One step. scales: host complex128 [nscales], H(t) slot values. psi: device complex128. */
 int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scales, int nscales,
                  pg_krylov_stats *stats);
+/*
+ * pAMP ensembles (no reference counterpart: the reference runs one wavefunction per process):
+ * many pg_pamp members (each with its own operator, overlap and basis size) advanced by one
+ * graph launch per ensemble step. The m x m exponential runs on the device (one CTA per
+ * member, scaling and squaring of the order-6 Pade approximant, pamp.h:430-565) instead of
+ * on the host. While a batch exists its members read their slot values from the batch;
+ * pg_pamp_batch_destroy gives them back their own. scales: [nmembers][nscales] complex.
+ */
+typedef struct pg_pamp_batch pg_pamp_batch;
+int pg_pamp_batch_create(pg_pamp **members, int nmembers, pg_pamp_batch **out);
+int pg_pamp_batch_destroy(pg_pamp_batch *b);
+int pg_pamp_batch_step(pg_pamp_batch *b, void **psis, double dt, const double *scales, int nscales);
+/* Per-member statistics of the last completed ensemble step (waits); Iterations = Krylov
+ * basis size used (smaller after a happy breakdown). PG_ERR_BREAKDOWN if a Pade denominator
+ * was singular. */
+int pg_pamp_batch_stats(pg_pamp_batch *b, pg_krylov_stats *stats);
 
 typedef struct pg_cayley pg_cayley;
 /*

@@ -75,6 +75,10 @@ _SIGS = {
     "pg_op_stored_elements": (_LL, [_P]),
     "pg_prec_fd_create": (_I, [_P, _I, _DP, _DP, _IP, _DP, _DP, C.POINTER(_P)]),
     "pg_prec_fd_max_n": (_I, [_I]),
+    "pg_pamp_batch_create": (_I, [C.POINTER(_P), _I, C.POINTER(_P)]),
+    "pg_pamp_batch_destroy": (_I, [_P]),
+    "pg_pamp_batch_step": (_I, [_P, C.POINTER(_P), _D, _DP, _I]),
+    "pg_pamp_batch_stats": (_I, [_P, C.POINTER(KrylovStats)]),
     "pg_op_add_factored": (_I, [_P, _I, _DP, _DP, _IP, _LL, _IP, _IP, _IP, _DP]),
     "pg_op_factored_info": (_I, [_P, _DP]),
     "pg_op_matvec": (_I, [_P, _DP, _I, _P, _P, _I]),

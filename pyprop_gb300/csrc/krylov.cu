@@ -401,7 +401,7 @@ extern "C" int pg_pamp_destroy(pg_pamp *p)
 }
 
 template <typename R>
-static int pamp_record_arnoldi(pg_pamp *p, cxd *x)
+static int pamp_record_arnoldi(pg_pamp *p, cxd *x, bool download = true)
 {
     pg_ctx *ctx = p->ctx;
     pg_ctx *rc = &p->rctx;
@@ -423,6 +423,7 @@ static int pamp_record_arnoldi(pg_pamp *p, cxd *x)
         PG_TRY(pg_banded_apply_dev(p->ovlb, PG_BAND_SOLVE_UT, w));
         PG_TRY(cgs2<R>(rc, V, n, j + 1, w, p->ab, j, p->double_ortho, nullptr));
     }
+    if (!download) return PG_OK;
     const size_t cnt = (size_t)p->m * 3 * p->ab.col_doubles();
     PG_CUDA_TRY(cudaMemcpyAsync(p->ab.h_cols, p->ab.d_cols, cnt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     PG_CUDA_TRY(cudaMemcpyAsync(rc->h_pinned, p->d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -430,10 +431,11 @@ static int pamp_record_arnoldi(pg_pamp *p, cxd *x)
 }
 
 template <typename R>
-static int pamp_record_finish(pg_pamp *p, cxd *x)
+static int pamp_record_finish(pg_pamp *p, cxd *x, bool upload = true)
 {
     pg_ctx *ctx = p->ctx;
-    PG_CUDA_TRY(cudaMemcpyAsync(p->d_c, p->h_c, sizeof(double) * 2 * p->m, cudaMemcpyHostToDevice, ctx->stream));
+    if (upload)
+        PG_CUDA_TRY(cudaMemcpyAsync(p->d_c, p->h_c, sizeof(double) * 2 * p->m, cudaMemcpyHostToDevice, ctx->stream));
     PG_TRY(pg_combine<R>(ctx, (const cx<R> *)p->V, p->n, p->m, p->d_c, 1.0, x, p->n, 0));
     return pg_banded_apply_dev(p->ovl64, PG_BAND_SOLVE_U, x);
 }
@@ -551,6 +553,408 @@ extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scal
 // ------------------------------------------------------------------------------------
 // Arnoldi expansion for pIRAM: operator S^-1 H, Euclidean inner product, CGS2
 // ------------------------------------------------------------------------------------
+// ------------------------------------------------------------------------------------
+// pAMP ensembles: one graph launch per ensemble step
+// ------------------------------------------------------------------------------------
+// The single-wavefunction step computes exp(-i dt H_m) e1 on the host between its two graphs;
+// an ensemble cannot stop for the host once per member. Here the m x m exponential runs on the
+// device, one CTA per member, with the reference's method (pamp.h:430-565: scaling and squaring
+// of the diagonal Pade approximant of order 6, the formulation of dense::expm_pade above), so the
+// graph is: fork -> each member's Arnoldi steps -> join -> all exponentials in one kernel ->
+// fork -> each member's psi = ||psi|| V c and overlap solve -> join.
+namespace {
+
+struct PampExpArgs {
+    const double *cols;  // the member's Hessenberg columns (ArnoldiBuf::d_cols)
+    const double *norm;  // [1] = ||psi||
+    double *c;           // out: [2m] coefficients of psi = V c
+    double *stats;       // out: [0] basis size used, [1] error estimate |c_(k-1)|^2 (before ||psi||), [2] 0 or -1 (singular)
+    int m, double_ortho;
+    double tol;
+};
+
+__device__ __forceinline__ cxd cdiv(cxd a, cxd b)
+{
+    const double d = b.x * b.x + b.y * b.y;
+    return mk<double>((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+// C = A B for k x k row-major matrices in shared memory (C distinct from A and B)
+__device__ void smem_matmul(int k, const cxd *A, const cxd *B, cxd *C)
+{
+    for (int t = threadIdx.x; t < k * k; t += blockDim.x) {
+        const int i = t / k, j = t - i * k;
+        cxd s = mk<double>(0.0, 0.0);
+        for (int q = 0; q < k; ++q) cfma(s, A[i * k + q], B[q * k + j]);
+        C[t] = s;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) pamp_expm_kernel(const PampExpArgs *__restrict__ args,
+                                                        const double *__restrict__ dt_dev)
+{
+    const PampExpArgs a = args[blockIdx.x];
+    const int m = a.m, tid = threadIdx.x, nt = blockDim.x;
+    extern __shared__ __align__(16) unsigned char pe_smem[];
+    cxd *A = reinterpret_cast<cxd *>(pe_smem);
+    cxd *A2 = A + m * m, *P = A2 + m * m, *Q = P + m * m, *T = Q + m * m, *D = T + m * m;
+    __shared__ int k_sh, s_sh, piv_sh, bad_sh;
+    __shared__ double red[256];
+    const size_t cd = 2 * (size_t)(m + 2);
+    if (tid == 0) {  // happy breakdown (pamp.h:306-313): truncate at the first small subdiagonal
+        int k = m;
+        for (int j = 0; j + 1 < m; ++j)
+            if (a.cols[((size_t)j * 3 + 2) * cd + 2 * (j + 1) + 1] < a.tol) {
+                k = j + 1;
+                break;
+            }
+        k_sh = k;
+        bad_sh = 0;
+    }
+    __syncthreads();
+    const int k = k_sh;
+    const double dt = *dt_dev;
+    // A = -i dt H_k
+    double mx = 0.0;
+    for (int t = tid; t < k * k; t += nt) {
+        const int i = t / k, j = t - i * k;
+        cxd h = mk<double>(0.0, 0.0);
+        if (i <= j) {
+            const double *p0 = a.cols + ((size_t)j * 3 + 0) * cd;
+            h = mk<double>(p0[2 * i], p0[2 * i + 1]);
+            if (a.double_ortho) {
+                const double *p1 = a.cols + ((size_t)j * 3 + 1) * cd;
+                h = h + mk<double>(p1[2 * i], p1[2 * i + 1]);
+            }
+        } else if (i == j + 1) {
+            h = mk<double>(a.cols[((size_t)j * 3 + 2) * cd + 2 * (j + 1) + 1], 0.0);
+        }
+        A[t] = mk<double>(dt * h.y, -dt * h.x);
+        mx = fmax(mx, sqrt(A[t].x * A[t].x + A[t].y * A[t].y));
+    }
+    red[tid] = mx;
+    __syncthreads();
+    for (int w = nt / 2; w > 0; w >>= 1) {
+        if (tid < w) red[tid] = fmax(red[tid], red[tid + w]);
+        __syncthreads();
+    }
+    if (tid == 0) s_sh = red[0] > 0.0 ? max(0, (int)ceil(log2(red[0]))) : 0;
+    __syncthreads();
+    const int sq = s_sh;
+    const double scale = ldexp(1.0, -sq);
+    for (int t = tid; t < k * k; t += nt) A[t] = scale * A[t];
+    __syncthreads();
+    smem_matmul(k, A, A, A2);
+    // diagonal Pade approximant of order 6: c_0 = 1, c_(i+1) = c_i (p - i) / ((i + 1)(2p - i))
+    const int order = 6;
+    double c[order + 1];
+    c[0] = 1.0;
+    for (int i = 0; i < order; ++i) c[i + 1] = c[i] * (double)(order - i) / (double)((i + 1) * (2 * order - i));
+    for (int t = tid; t < k * k; t += nt) {
+        const bool dg = (t / k) == (t % k);
+        Q[t] = mk<double>(dg ? c[order] : 0.0, 0.0);
+        P[t] = mk<double>(dg ? c[order - 1] : 0.0, 0.0);
+    }
+    __syncthreads();
+    bool odd = true;
+    for (int i = order - 2; i >= 0; --i) {
+        cxd *M = odd ? Q : P;
+        smem_matmul(k, M, A2, T);
+        for (int t = tid; t < k * k; t += nt) M[t] = T[t] + mk<double>((t / k) == (t % k) ? c[i] : 0.0, 0.0);
+        __syncthreads();
+        odd = !odd;
+    }
+    {
+        cxd *M = odd ? Q : P;
+        smem_matmul(k, M, A, T);
+        for (int t = tid; t < k * k; t += nt) M[t] = T[t];
+        __syncthreads();
+    }
+    // solve (Q - P) X = P by LU with partial pivoting; X overwrites P
+    for (int t = tid; t < k * k; t += nt) D[t] = Q[t] - P[t];
+    __syncthreads();
+    for (int pc = 0; pc < k; ++pc) {
+        if (tid == 0) {
+            int r = pc;
+            double best = -1.0;
+            for (int i = pc; i < k; ++i) {
+                const double v = D[i * k + pc].x * D[i * k + pc].x + D[i * k + pc].y * D[i * k + pc].y;
+                if (v > best) { best = v; r = i; }
+            }
+            piv_sh = r;
+            if (best == 0.0) bad_sh = 1;
+        }
+        __syncthreads();
+        if (bad_sh) break;
+        const int r = piv_sh;
+        if (r != pc)
+            for (int j = tid; j < k; j += nt) {
+                cxd t0 = D[pc * k + j]; D[pc * k + j] = D[r * k + j]; D[r * k + j] = t0;
+                t0 = P[pc * k + j]; P[pc * k + j] = P[r * k + j]; P[r * k + j] = t0;
+            }
+        __syncthreads();
+        for (int i = pc + 1 + tid; i < k; i += nt) D[i * k + pc] = cdiv(D[i * k + pc], D[pc * k + pc]);
+        __syncthreads();
+        for (int t = tid; t < (k - pc - 1) * k; t += nt) {
+            const int i = pc + 1 + t / k, j = t % k;
+            const cxd l = D[i * k + pc];
+            if (j > pc) D[i * k + j] = D[i * k + j] - l * D[pc * k + j];
+            P[i * k + j] = P[i * k + j] - l * P[pc * k + j];
+        }
+        __syncthreads();
+    }
+    if (bad_sh) {
+        for (int t = tid; t < 2 * m; t += nt) a.c[t] = 0.0;
+        if (tid == 0) { a.stats[0] = k; a.stats[1] = 0.0; a.stats[2] = -1.0; }
+        return;
+    }
+    for (int j = tid; j < k; j += nt)
+        for (int i = k - 1; i >= 0; --i) {
+            cxd sum = P[i * k + j];
+            for (int q = i + 1; q < k; ++q) sum = sum - D[i * k + q] * P[q * k + j];
+            P[i * k + j] = cdiv(sum, D[i * k + i]);
+        }
+    __syncthreads();
+    // E = +-(I + 2 X), then squared sq times
+    cxd *E = P;
+    for (int t = tid; t < k * k; t += nt) {
+        cxd e = 2.0 * E[t];
+        if ((t / k) == (t % k)) e.x += 1.0;
+        E[t] = odd ? mk<double>(-e.x, -e.y) : e;
+    }
+    __syncthreads();
+    for (int q = 0; q < sq; ++q) {
+        smem_matmul(k, E, E, T);
+        for (int t = tid; t < k * k; t += nt) E[t] = T[t];
+        __syncthreads();
+    }
+    const double nrm = a.norm[1];
+    for (int i = tid; i < m; i += nt) {
+        const cxd v = i < k ? E[i * k] : mk<double>(0.0, 0.0);
+        a.c[2 * i] = v.x * nrm;
+        a.c[2 * i + 1] = v.y * nrm;
+    }
+    if (tid == 0) {
+        const cxd last = E[(k - 1) * k];
+        a.stats[0] = k;
+        a.stats[1] = last.x * last.x + last.y * last.y;
+        a.stats[2] = 0.0;
+    }
+}
+
+}  // namespace
+
+struct pg_pamp_batch {
+    std::vector<pg_pamp *> members;
+    std::vector<void *> psis;
+    std::vector<cxd *> own_scales;  // the members' own scale slots, restored at destroy
+    pg_ctx *ctx = nullptr;
+    cxd *d_scales = nullptr, *h_scales = nullptr;  // [n][PG_MAX_SLOTS], then dt
+    PampExpArgs *d_args = nullptr;
+    double *d_stats = nullptr, *h_stats = nullptr;  // [n][4]
+    cudaEvent_t params_done = nullptr;
+    bool params_pending = false;
+    cudaStream_t origin = nullptr;
+    cudaEvent_t fork = nullptr, mid = nullptr;
+    std::vector<cudaEvent_t> join, join2;
+    cudaGraphExec_t exec = nullptr;
+    int mmax = 0;
+    long long kernels_per_step = 0;
+};
+
+extern "C" int pg_pamp_batch_create(pg_pamp **members, int nmembers, pg_pamp_batch **out)
+{
+    if (!members || nmembers < 1 || !out) return PG_ERR_ARG;
+    pg_pamp_batch *b = new pg_pamp_batch();
+    b->ctx = members[0]->ctx;
+    for (int k = 0; k < nmembers; ++k) {
+        if (!members[k] || members[k]->ctx != b->ctx) { delete b; return PG_ERR_ARG; }
+        for (int q = 0; q < k; ++q)
+            if (members[q] == members[k]) { delete b; return PG_ERR_ARG; }
+        b->members.push_back(members[k]);
+        b->own_scales.push_back(members[k]->d_scales);
+        b->mmax = std::max(b->mmax, members[k]->m);
+    }
+    const size_t nsc = (size_t)nmembers * PG_MAX_SLOTS + 1;
+    PG_CUDA_TRY(cudaMalloc(&b->d_scales, sizeof(cxd) * nsc));
+    PG_CUDA_TRY(cudaMallocHost(&b->h_scales, sizeof(cxd) * nsc));
+    memset(b->h_scales, 0, sizeof(cxd) * nsc);
+    PG_CUDA_TRY(cudaMalloc(&b->d_stats, sizeof(double) * 4 * nmembers));
+    PG_CUDA_TRY(cudaMemset(b->d_stats, 0, sizeof(double) * 4 * nmembers));
+    PG_CUDA_TRY(cudaMallocHost(&b->h_stats, sizeof(double) * 4 * nmembers));
+    std::vector<PampExpArgs> args(nmembers);
+    for (int k = 0; k < nmembers; ++k) {
+        pg_pamp *p = members[k];
+        args[k].cols = p->ab.d_cols;
+        args[k].norm = p->d_norm;
+        args[k].c = p->d_c;
+        args[k].stats = b->d_stats + 4 * k;
+        args[k].m = p->m;
+        args[k].double_ortho = p->double_ortho;
+        args[k].tol = p->tolerance;
+    }
+    PG_CUDA_TRY(cudaMalloc(&b->d_args, sizeof(PampExpArgs) * nmembers));
+    PG_CUDA_TRY(cudaMemcpy(b->d_args, args.data(), sizeof(PampExpArgs) * nmembers, cudaMemcpyHostToDevice));
+    const size_t smem = 6 * sizeof(cxd) * (size_t)b->mmax * b->mmax;
+    PG_CUDA_TRY(cudaFuncSetAttribute(pamp_expm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PG_CUDA_TRY(cudaEventCreateWithFlags(&b->params_done, cudaEventDisableTiming));
+    PG_CUDA_TRY(cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking));
+    PG_CUDA_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    PG_CUDA_TRY(cudaEventCreateWithFlags(&b->mid, cudaEventDisableTiming));
+    b->join.resize(nmembers);
+    b->join2.resize(nmembers);
+    for (int k = 0; k < nmembers; ++k) {
+        PG_CUDA_TRY(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
+        PG_CUDA_TRY(cudaEventCreateWithFlags(&b->join2[k], cudaEventDisableTiming));
+    }
+    // the members read their slot values from the batch's array from now on
+    for (int k = 0; k < nmembers; ++k) {
+        members[k]->d_scales = b->d_scales + (size_t)k * PG_MAX_SLOTS;
+        members[k]->built_psi = nullptr;
+    }
+    *out = b;
+    return PG_OK;
+}
+
+extern "C" int pg_pamp_batch_destroy(pg_pamp_batch *b)
+{
+    if (!b) return PG_ERR_ARG;
+    cudaStreamSynchronize(b->ctx->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    for (auto e : b->join) cudaEventDestroy(e);
+    for (auto e : b->join2) cudaEventDestroy(e);
+    cudaEventDestroy(b->fork);
+    cudaEventDestroy(b->mid);
+    cudaEventDestroy(b->params_done);
+    cudaStreamDestroy(b->origin);
+    for (size_t k = 0; k < b->members.size(); ++k) {
+        b->members[k]->d_scales = b->own_scales[k];
+        b->members[k]->built_psi = nullptr;  // its own graphs captured the batch's slot pointer
+        if (b->members[k]->g1) { cudaGraphExecDestroy(b->members[k]->g1); b->members[k]->g1 = nullptr; }
+        if (b->members[k]->g2) { cudaGraphExecDestroy(b->members[k]->g2); b->members[k]->g2 = nullptr; }
+    }
+    cudaFree(b->d_scales);
+    cudaFreeHost(b->h_scales);
+    cudaFree(b->d_stats);
+    cudaFreeHost(b->h_stats);
+    cudaFree(b->d_args);
+    delete b;
+    return PG_OK;
+}
+
+static int pamp_batch_build(pg_pamp_batch *b, void **psis)
+{
+    pg_ctx *ctx = b->ctx;
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    const int n = (int)b->members.size();
+    cudaStream_t saved = ctx->stream;
+    long long kernels = 0;
+    const long long l0 = ctx->launches;
+    PG_CUDA_TRY(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
+    int code = PG_OK;
+    if (cudaEventRecord(b->fork, b->origin) != cudaSuccess) code = PG_ERR_CUDA;
+    for (int k = 0; k < n && code == PG_OK; ++k) {
+        pg_pamp *p = b->members[k];
+        const long long r0 = p->rctx.launches;
+        if (cudaStreamWaitEvent(p->cap, b->fork, 0) != cudaSuccess) { code = PG_ERR_CUDA; break; }
+        ctx->stream = p->cap;
+        code = (p->prec == PG_FP64) ? pamp_record_arnoldi<double>(p, (cxd *)psis[k], false)
+                                    : pamp_record_arnoldi<float>(p, (cxd *)psis[k], false);
+        ctx->stream = saved;
+        kernels += p->rctx.launches - r0;
+        p->rctx.launches = r0;
+        if (code != PG_OK) break;
+        if (cudaEventRecord(b->join[k], p->cap) != cudaSuccess || cudaStreamWaitEvent(b->origin, b->join[k], 0) != cudaSuccess)
+            code = PG_ERR_CUDA;
+    }
+    if (code == PG_OK) {
+        const size_t smem = 6 * sizeof(cxd) * (size_t)b->mmax * b->mmax;
+        pamp_expm_kernel<<<n, 256, smem, b->origin>>>(b->d_args, (const double *)(b->d_scales + (size_t)n * PG_MAX_SLOTS));
+        kernels += 1;
+        if (cudaGetLastError() != cudaSuccess || cudaEventRecord(b->mid, b->origin) != cudaSuccess) code = PG_ERR_CUDA;
+    }
+    for (int k = 0; k < n && code == PG_OK; ++k) {
+        pg_pamp *p = b->members[k];
+        if (cudaStreamWaitEvent(p->cap, b->mid, 0) != cudaSuccess) { code = PG_ERR_CUDA; break; }
+        ctx->stream = p->cap;
+        code = (p->prec == PG_FP64) ? pamp_record_finish<double>(p, (cxd *)psis[k], false)
+                                    : pamp_record_finish<float>(p, (cxd *)psis[k], false);
+        ctx->stream = saved;
+        if (code != PG_OK) break;
+        if (cudaEventRecord(b->join2[k], p->cap) != cudaSuccess || cudaStreamWaitEvent(b->origin, b->join2[k], 0) != cudaSuccess)
+            code = PG_ERR_CUDA;
+    }
+    ctx->stream = saved;
+    kernels += ctx->launches - l0;
+    ctx->launches = l0;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->origin, &g);
+    if (code != PG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return code;
+    }
+    if (e != cudaSuccess) {
+        pg_set_last_error(e, "cudaStreamEndCapture(pamp batch)", __FILE__, __LINE__);
+        return PG_ERR_CUDA;
+    }
+    cudaError_t ie = cudaGraphInstantiate(&b->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        pg_set_last_error(ie, "cudaGraphInstantiate(pamp batch)", __FILE__, __LINE__);
+        return PG_ERR_CUDA;
+    }
+    b->kernels_per_step = kernels;
+    b->psis.assign(psis, psis + n);
+    return PG_OK;
+}
+
+// One ensemble step: member k's wavefunction psis[k] (complex128, device), slot values
+// scales[k][0..nscales) (complex, interleaved), one time step dt for all.
+extern "C" int pg_pamp_batch_step(pg_pamp_batch *b, void **psis, double dt, const double *scales, int nscales)
+{
+    if (!b || !psis || nscales < 0 || nscales > PG_MAX_SLOTS || (nscales > 0 && !scales)) return PG_ERR_ARG;
+    const int n = (int)b->members.size();
+    bool same = b->exec && (int)b->psis.size() == n;
+    for (int k = 0; same && k < n; ++k) same = (b->psis[k] == psis[k]);
+    if (!same) PG_TRY(pamp_batch_build(b, psis));
+    if (b->params_pending) PG_CUDA_TRY(cudaEventSynchronize(b->params_done));
+    for (int k = 0; k < n; ++k)
+        for (int q = 0; q < PG_MAX_SLOTS; ++q)
+            b->h_scales[(size_t)k * PG_MAX_SLOTS + q] =
+                mk<double>(q < nscales ? scales[2 * ((size_t)k * nscales + q)] : 0.0,
+                           q < nscales ? scales[2 * ((size_t)k * nscales + q) + 1] : 0.0);
+    b->h_scales[(size_t)n * PG_MAX_SLOTS] = mk<double>(dt, 0.0);
+    cudaStream_t s = b->ctx->stream;
+    PG_CUDA_TRY(cudaMemcpyAsync(b->d_scales, b->h_scales, sizeof(cxd) * ((size_t)n * PG_MAX_SLOTS + 1),
+                                cudaMemcpyHostToDevice, s));
+    PG_CUDA_TRY(cudaEventRecord(b->params_done, s));
+    b->params_pending = true;
+    PG_CUDA_TRY(cudaGraphLaunch(b->exec, s));
+    b->ctx->launches += b->kernels_per_step;
+    return PG_OK;
+}
+
+// Per-member statistics of the last completed ensemble step (waits for the stream).
+extern "C" int pg_pamp_batch_stats(pg_pamp_batch *b, pg_krylov_stats *stats)
+{
+    if (!b || !stats) return PG_ERR_ARG;
+    const int n = (int)b->members.size();
+    PG_CUDA_TRY(cudaMemcpyAsync(b->h_stats, b->d_stats, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, b->ctx->stream));
+    PG_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+    for (int k = 0; k < n; ++k) {
+        const pg_pamp *p = b->members[k];
+        memset(&stats[k], 0, sizeof(pg_krylov_stats));
+        stats[k].Iterations = (int)b->h_stats[4 * k];
+        stats[k].ErrorEstimate = b->h_stats[4 * k + 1];
+        stats[k].OpCount = p->m;
+        stats[k].InnerProductCount = (p->double_ortho ? 2 : 1) * p->m;
+        stats[k].ReOrthoCount = p->double_ortho ? p->m : 0;
+        if (b->h_stats[4 * k + 2] != 0.0) return PG_ERR_BREAKDOWN;
+    }
+    return PG_OK;
+}
+
 extern "C" int pg_arnoldi_expand(pg_op *op64, pg_banded *ovl64, pg_banded *shift_invert, const double *scales,
                                  int nscales, void *Vv, int m, int j0, void *fv, double *Hio, double breakdown_tol,
                                  int inject, int *steps_done, double *residual_norm_out, pg_krylov_stats *st)

@@ -1,9 +1,10 @@
 """Ensembles of independent hydrogen-like propagations advanced together on one GPU.
 
-Each member is an ordinary ``Problem`` with ``CayleyPropagatorGPU`` (its own basis size,
-angular size and laser parameters). ``CayleyEnsembleGPU`` binds their device steppers into a
-``pg_cayley_batch``: one CUDA graph launch per ensemble step, one branch per member, the
-branches running concurrently. This is the ensemble mode the reference runs as separate
+Each member is an ordinary ``Problem`` with ``CayleyPropagatorGPU`` or ``PamPropagatorGPU``
+(its own basis size, angular size and laser parameters). ``CayleyEnsembleGPU`` binds their
+device steppers into a ``pg_cayley_batch``, ``PamEnsembleGPU`` into a ``pg_pamp_batch``: one
+CUDA graph launch per ensemble step, one branch per member, the branches running
+concurrently (the pAMP exponentials of all members in one kernel between the branches). This is the ensemble mode the reference runs as separate
 processes (one job per field parameter set, ``pyprop/utilities/submitpbs*.py``).
 
 ``partition_members`` splits an ensemble over ranks for multi-GPU runs (members are
@@ -98,5 +99,57 @@ class CayleyEnsembleGPU:
         try:
             if getattr(self, "h", None):
                 self.lib.pg_cayley_batch_destroy(self.h)
+        except Exception:
+            pass
+
+
+class PamEnsembleGPU(CayleyEnsembleGPU):
+    """Advance many ``Problem`` objects (PamPropagatorGPU, same dt) with one launch per step;
+    each member's H is frozen at the step start, as in PamPropagatorGPU.AdvanceStep."""
+
+    def __init__(self, problems):
+        self.problems = list(problems)
+        if not self.problems:
+            raise ValueError("empty ensemble")
+        props = [p.Propagator for p in self.problems]
+        for pr in props:
+            if not hasattr(pr, "stepper"):
+                raise ValueError("call SetupStep() on every member first")
+        self.lib = props[0].stepper.lib
+        self.ctx = props[0].stepper.ctx
+        n = len(props)
+        arr = (C.c_void_p * n)(*[pr.stepper.h.value for pr in props])
+        h = C.c_void_p()
+        check(self.lib.pg_pamp_batch_create(arr, n, C.byref(h)), "pg_pamp_batch_create")
+        self.h = h
+        self._keep = props
+        self.nslots = props[0].op64.nslots
+        if any(pr.op64.nslots != self.nslots for pr in props):
+            raise ValueError("ensemble members must have the same number of potential slots")
+        self.dt = self.problems[0].TimeStep
+        self._psis = (C.c_void_p * n)(*[p.psi.GetData().data_ptr() for p in self.problems])
+        self.stats = (nat.KrylovStats * n)()
+
+    def scales(self):
+        """(n, nslots) slot values of each member's H at its current time."""
+        return np.stack([p.Propagator.op64.scales(p.PropagatedTime) for p in self.problems])
+
+    def AdvanceStep(self, scales=None):
+        sc = np.ascontiguousarray(self.scales() if scales is None else scales, dtype=np.complex128)
+        self.ctx.bind_stream()
+        check(self.lib.pg_pamp_batch_step(self.h, self._psis, float(self.dt), sc.view(np.float64).ctypes.data_as(
+            nat._DP), self.nslots), "pg_pamp_batch_step")
+        for p in self.problems:
+            p.PropagatedTime += self.dt
+
+    def Stats(self):
+        self.ctx.bind_stream()
+        check(self.lib.pg_pamp_batch_stats(self.h, self.stats), "pg_pamp_batch_stats")
+        return [s.as_dict() for s in self.stats]
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.lib.pg_pamp_batch_destroy(self.h)
         except Exception:
             pass

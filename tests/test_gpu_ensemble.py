@@ -55,3 +55,50 @@ def test_ensemble_member_against_oracle(gpu):
         cay = OracleCayley(ham, 0.01, [0], 20, 1e-13)
         ref = cay.step(cay.step(start, 1.0, 0.01), 1.01, 0.01)
         assert relerr(p.psi.numpy(), ref) < 1e-10
+
+
+def _pamp_members(precision, with_field=True):
+    specs = [dict(lmax=3, nbsplines=40, rmax=40.0, amplitude=0.05 if with_field else 0.0),
+             dict(lmax=5, nbsplines=33, rmax=30.0, amplitude=0.08 if with_field else 0.0, wavelength_nm=400.0),
+             dict(lmax=2, nbsplines=55, rmax=50.0, amplitude=0.02 if with_field else 0.0, wavelength_nm=1600.0)]
+    probs = []
+    for k, sp in enumerate(specs):
+        p = hydrogen_problem(propagator="PamPropagatorGPU", precision=precision, **sp)
+        p.SetupStep(skipWavefunctionSetup=True)
+        rng = np.random.default_rng(200 + k)
+        shape = p.psi.GetRepresentation().GetFullShape()
+        psi = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+        p.psi.SetData(psi / np.linalg.norm(psi))
+        p.PropagatedTime = 1.0
+        probs.append(p)
+    return probs
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_pamp_ensemble_matches_single_members(gpu, precision):
+    """pAMP members of different sizes and fields advanced by one graph launch per step (the
+    m x m exponentials on the device, Pade of order 6) against the same members stepped alone
+    (host exponential), and a second batch built on the same members after the first is
+    destroyed."""
+    from pyprop_gb300.ensemble import PamEnsembleGPU
+    alone = _pamp_members(precision)
+    together = _pamp_members(precision)
+    for _ in range(4):
+        for p in alone:
+            p.AdvanceStep()
+    ens = PamEnsembleGPU(together)
+    for _ in range(4):
+        ens.AdvanceStep()
+    stats = ens.Stats()
+    tol = 1e-11 if precision == "fp64" else 1e-6
+    for a, b, st in zip(alone, together, stats):
+        assert relerr(b.psi.numpy(), a.psi.numpy()) < tol, (precision, relerr(b.psi.numpy(), a.psi.numpy()))
+        assert st["Iterations"] == 20
+        assert 0.0 <= st["ErrorEstimate"] < 1e-6
+        assert abs(a.PropagatedTime - b.PropagatedTime) < 1e-12
+    del ens
+    # members step alone again (their own slots back) and agree with the lone copies
+    for p, q in zip(alone, together):
+        p.AdvanceStep()
+        q.AdvanceStep()
+        assert relerr(q.psi.numpy(), p.psi.numpy()) < tol
