@@ -471,6 +471,7 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
 
     ens = run_ensemble(args, torch, flush) if args.ensemble > 0 else None
+    ens_pamp = run_pamp_ensemble(args, torch, flush) if args.ensemble > 0 else None
     cpu = cpu_baseline_sample(nsteps=args.cpu_steps) if (rank == 0 and world == 1 and args.cpu_steps > 0) else None
     if rank == 0:
         steps_per_s = world * args.steps / t_mixed
@@ -518,6 +519,7 @@ def run_ours(args):
             "two_electron_cayley": two_e_steps,
             "cpu_baseline": cpu,
             "ensemble": ens,
+            "ensemble_pamp": ens_pamp,
             "clocks": clk.summary(),
             "gpu_launches": launches,
             "ground_energy": e0,
@@ -595,6 +597,77 @@ def run_ensemble(args, torch, flush):
             "workload": "%d hydrogen members, lmax U{8..32}, N U{100..400} on r in [0,100], E0 U[0.01,0.1], "
                         "lambda U[400,1600] nm (rng seed 20261203), Cayley mixed precision, one graph launch per "
                         "ensemble step, L2 flushed between steps" % len(probs),
+            "setup_s": setup_s}
+
+
+def run_pamp_ensemble(args, torch, flush):
+    """The ensemble of run_ensemble with pAMP steps (Krylov basis 20, complex64 basis with FP64
+    Gram-Schmidt sums, the m x m exponentials of all members on the device), one graph launch
+    per ensemble step, against the same members stepped one at a time on the plain FP64 pAMP
+    path (host exponential)."""
+    import pyprop_gb300 as pp
+    from pyprop_gb300.ensemble import PamEnsembleGPU, hydrogen_ensemble_params
+    from pyprop_gb300.workloads import hydrogen
+    t_setup = time.perf_counter()
+    params = hydrogen_ensemble_params(args.ensemble)
+
+    def member(prm, precision):
+        p = pp.Problem(pp.LoadString(hydrogen(propagator="PamPropagatorGPU", precision=precision, rmax=100.0,
+                                              timestep=0.01, pulse_duration=10.0, duration=10.0,
+                                              krylov_basis_size=20, **prm)))
+        p.SetupStep(skipWavefunctionSetup=True)
+        psi, _ = initial_state(p)
+        p.psi.SetData(psi)
+        return p
+
+    probs = [member(prm, "fp32") for prm in params]
+    ens = PamEnsembleGPU(probs)
+    setup_s = time.perf_counter() - t_setup
+    for _ in range(args.warmup):
+        ens.AdvanceStep()
+    torch.cuda.synchronize()
+    K = max(1, min(args.steps, 20))
+    tables = []
+    for k in range(K):
+        tables.append(np.stack([p.Propagator.op64.scales(p.PropagatedTime + k * ens.dt) for p in probs]))
+    stream = torch.cuda.current_stream()
+    total = 0.0
+    for k in range(K):
+        flush.fill_(1.0)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        ens.AdvanceStep(tables[k])
+        e.record(stream)
+        e.synchronize()
+        total += s.elapsed_time(e) * 1e-3
+    err = max(st["ErrorEstimate"] for st in ens.Stats())
+    member_steps = K * len(probs)
+    sample = list(range(0, len(params), max(1, len(params) // 16)))[:16]
+    t64 = 0.0
+    n64 = 0
+    for i in sample:
+        p64 = member(params[i], "fp64")
+        for _ in range(3):
+            p64.AdvanceStep()
+        torch.cuda.synchronize()
+        for _ in range(5):
+            flush.fill_(1.0)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            p64.AdvanceStep()
+            e.record(stream)
+            e.synchronize()
+            t64 += s.elapsed_time(e) * 1e-3
+            n64 += 1
+        del p64
+    fp64_rate = n64 / t64
+    rate = member_steps / total
+    del ens
+    return {"members": len(probs), "member_steps_per_s": rate, "ms_per_ensemble_step": 1e3 * total / K,
+            "max_error_estimate": err, "plain_fp64_single_member_steps_per_s": fp64_rate,
+            "speedup_vs_plain_fp64": rate / fp64_rate,
+            "workload": "the members of `ensemble` with pAMP (m=20, complex64 basis, FP64 sums), one graph launch "
+                        "per ensemble step including the device Pade exponentials, L2 flushed between steps",
             "setup_s": setup_s}
 
 
