@@ -20,6 +20,8 @@ from .propagator import (BasisPropagator, BasisPropagatorGPU, BSplinePreconditio
                          CayleyPropagatorGPU, PamPropagator, PamPropagatorGPU, RadialPreconditioner,
                          RadialTwoElectronPreconditionerIfpack, RadialTwoElectronPreconditionerSuperLU,
                          TwoElectronFastDiagonalizationPreconditioner, TwoElectronKroneckerPreconditioner)
+from .serialization import (CheckBasisPairs, GetConfigText, LoadTensorPotential, LoadWavefunction,
+                            SaveTensorPotential, SaveWavefunction)
 from .solver import PiramSolver, PiramSolverGPU
 from .spherical import DefaultCoupledIndexIterator
 

@@ -120,6 +120,26 @@ class Problem:
         self.StartTime = startTime
         self.Duration = propagationTime
 
+    def SaveCheckpoint(self, filename, datasetPath="/checkpoint"):
+        """Wavefunction, propagated time and time step in one ``.npz`` file (see
+        :mod:`pyprop_gb300.serialization`), with the config as an attribute."""
+        from .serialization import SaveWavefunction, _norm, _read, _write
+        SaveWavefunction(filename, datasetPath + "/psi", self.psi, self.Config)
+        entries = _read(filename)
+        path = _norm(datasetPath)
+        entries[path + "/time"] = np.array([self.PropagatedTime, np.real(self.TimeStep), np.imag(self.TimeStep)])
+        _write(filename, entries)
+
+    def LoadCheckpoint(self, filename, datasetPath="/checkpoint"):
+        """Restore the wavefunction and the propagated time written by SaveCheckpoint (the
+        problem must have the same representation)."""
+        from .serialization import LoadWavefunction, _norm
+        LoadWavefunction(filename, datasetPath + "/psi", self.psi)
+        with np.load(filename, allow_pickle=False) as z:
+            t = z[_norm(datasetPath) + "/time"]
+        self.PropagatedTime = float(t[0])
+        return self.PropagatedTime
+
     def AdvanceStep(self):
         self.Propagator.AdvanceStep(self.PropagatedTime, self.TimeStep)
         if self.Propagator.RenormalizeActive:
