@@ -151,6 +151,12 @@ int pg_op_add_term_ranks(pg_op *op, const char *storage, const double *potential
 int pg_op_add_factored(pg_op *op, int nfactors, const double *radial, const double *weights, const int *slots,
                        long long nentries, const int *ent_factor, const int *ent_row, const int *ent_col,
                        const double *ent_coef);
+/* FP64 operators only, before pg_op_finalize (no reference counterpart): compute the radial
+ * stencil of the factorized terms in double-float arithmetic (each value an FP32 pair hi + lo,
+ * error-free products and sums: relative accuracy about 2^-48 instead of 2^-53) instead of FP64
+ * FMAs, which run at a small fraction of the FP32 rate on this GPU. Meant for the FP64
+ * residuals of mixed-precision solves. */
+int pg_op_set_fp64_emulation(pg_op *op, int on);
 /* Bookkeeping of the factorized part (no reference counterpart): info[0] factors, [1]
  * angular entries (row, col), [2] flops of the angular mix and [3] of the radial stencil per
  * matvec (real multiply-adds x 2, zero blocks skipped as the kernels skip them), [4] bytes

@@ -81,6 +81,7 @@ _SIGS = {
     "pg_pamp_batch_stats": (_I, [_P, C.POINTER(KrylovStats)]),
     "pg_op_add_factored": (_I, [_P, _I, _DP, _DP, _IP, _LL, _IP, _IP, _IP, _DP]),
     "pg_op_factored_info": (_I, [_P, _DP]),
+    "pg_op_set_fp64_emulation": (_I, [_P, _I]),
     "pg_op_matvec": (_I, [_P, _DP, _I, _P, _P, _I]),
     "pg_overlap_create": (_I, [_P, _DP, C.POINTER(_P)]),
     "pg_prec_blockdiag_create": (_I, [_P, _DP, _DP, _DP, _IP, _DP, _I, C.POINTER(_P)]),

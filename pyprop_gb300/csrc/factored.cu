@@ -37,6 +37,7 @@ const int CB = 4;   // channels per mix CTA (one warp each)
 
 struct FactArgs {
     int Q, Qp, A, Ap, N1, N2, N2p, nct, tw;
+    int df;  // FP64 operator with FP32-pair (double-float) scratch and radial factors
     const int *row_ptr, *col, *slot, *nzq, *perm;
     const void *coef;
     const unsigned char *chunk, *bflag;
@@ -50,6 +51,7 @@ FactArgs args_of(const FactDev &f, int *err)
     FactArgs a;
     a.Q = f.Q; a.Qp = f.Qp; a.A = f.A; a.Ap = f.Ap; a.N1 = f.N1; a.N2 = f.N2; a.N2p = f.N2p; a.nct = f.nct;
     a.tw = f.tw;
+    a.df = f.df;
     a.row_ptr = f.row_ptr; a.col = f.col; a.slot = f.slot; a.nzq = f.nzq; a.perm = f.perm;
     a.coef = f.coef; a.chunk = f.chunk; a.bflag = f.bflag; a.w = f.w; a.Z = f.Z; a.err = err;
     return a;
@@ -218,7 +220,16 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
             const long long pp = pbase + pl;
             if (q >= Q || !gf[q] || pp >= NP) continue;
             const int u = pl % MPT, ln = pl / MPT;
-            Z[((size_t)q * NP + pp) * f.Ap + a0 + r] = ws[q] * acc[(((size_t)j * MPT + u) * 32 + ln) * (CB + 1) + r];
+            const cx<R> v = ws[q] * acc[(((size_t)j * MPT + u) * 32 + ln) * (CB + 1) + r];
+            const size_t zi = ((size_t)q * NP + pp) * f.Ap + a0 + r;
+            if constexpr (sizeof(R) == 8) {
+                if (f.df) {  // the 16 bytes hold (re_hi, re_lo, im_hi, im_lo)
+                    const float rh = (float)v.x, ih = (float)v.y;
+                    reinterpret_cast<float4 *>(Z)[zi] = make_float4(rh, (float)(v.x - (double)rh), ih, (float)(v.y - (double)ih));
+                    continue;
+                }
+            }
+            Z[zi] = v;
         }
         __syncthreads();
     }
@@ -384,6 +395,137 @@ __global__ void __launch_bounds__(128, 2) fact_radial_kernel(FactArgs f, cx<R> *
         }
 }
 
+// Double-float accumulation for the FP64 operator (FP64 arithmetic runs at a small fraction of
+// the FP32 rate on this GPU): a value v is held as hi + lo, hi = fp32(v), lo = fp32(v - hi).
+// Each product r * z is formed exactly in its leading part (p = rh zh, the rounding error of p
+// by one FMA) plus the cross terms rh zl + rl zh; p is added to the running hi with an
+// error-free two-sum (Knuth), the errors gather in lo. Relative accuracy about 2^-48 per sum
+// instead of 2^-53.
+// (the _rn intrinsics keep the compiler from contracting these steps into FMAs, which would
+// break the error-free transformations)
+__device__ __forceinline__ void df_fma(float &hi, float &lo, float rh, float rl, float zh, float zl)
+{
+    const float p = __fmul_rn(rh, zh);
+    float e = fmaf(rh, zh, -p);
+    e = fmaf(rh, zl, e);
+    e = fmaf(rl, zh, e);
+    const float s = __fadd_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(err, e));
+}
+
+// The radial stencil of the FP64 operator in double-float arithmetic: the tiles of the FP64
+// kernel (scratch elements and coefficients of 16 and 8 bytes: (re_hi, re_lo, im_hi, im_lo) and
+// (hi, lo)), the same TMA boxes and stages.
+template <int KB>
+__global__ void __launch_bounds__(128, 2) fact_radial_df_kernel(FactArgs f, cxd *__restrict__ y,
+                                                                const __grid_constant__ CUtensorMap zmap,
+                                                                const __grid_constant__ CUtensorMap rmap)
+{
+    typedef RadialTile<double> T;
+    constexpr int B = 2 * KB + 1;
+    constexpr int PI = T::PI, NV = T::NV, TCN = T::TCN, CA = T::CA, PC = NV;  // one complex per 16 bytes
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned long long *bar = (unsigned long long *)smem_raw;
+    const int tw = f.tw;
+    const unsigned zbytes = (unsigned)rad_zbytes<double>(tw, KB), rbytes = (unsigned)rad_rbytes<double>(tw, KB);
+    const size_t zb = rad_round128<double>(zbytes), stage = zb + rad_round128<double>(rbytes);
+    unsigned char *buf = smem_raw + 128;
+    const int tid = threadIdx.x, tc = tid % TCN, ti = tid / TCN;
+    const int i1 = blockIdx.x, t0 = blockIdx.y * tw, ct = blockIdx.z, c0 = ct * CA;
+    const int N1 = f.N1, N2 = f.N2;
+    if (tid == 0) {
+        fbar_init(&bar[0], 1);
+        fbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    auto advance = [&](int &q, int &d1) {
+        for (;;) {
+            if (++d1 == B) {
+                d1 = 0;
+                ++q;
+            }
+            if (q >= f.Q) return;
+            if (!f.bflag[(size_t)q * f.nct + ct]) {
+                d1 = B - 1;
+                continue;
+            }
+            const int j1 = i1 + d1 - KB;
+            if (j1 >= 0 && j1 < N1) return;
+        }
+    };
+    auto issue = [&](int s, int q, int d1) {
+        unsigned char *dst = buf + (size_t)s * stage;
+        fbar_expect(&bar[s], zbytes + rbytes);
+        tma_3d(dst, &zmap, 2 * c0, t0 - KB, q * N1 + i1 + d1 - KB, &bar[s]);
+        tma_2d(dst + zb, &rmap, t0, ((q * N1 + i1) * B + d1) * B, &bar[s]);
+    };
+    float ah[PI][PC][2], al[PI][PC][2];  // [point][channel][re, im]
+#pragma unroll
+    for (int p = 0; p < PI; ++p)
+#pragma unroll
+        for (int c = 0; c < PC; ++c) ah[p][c][0] = ah[p][c][1] = al[p][c][0] = al[p][c][1] = 0.f;
+    int q = 0, d1 = -1;
+    advance(q, d1);
+    if (tid == 0 && q < f.Q) issue(0, q, d1);
+    for (int k = 0; q < f.Q; ++k) {
+        const int s = k & 1;
+        int qn = q, dn = d1;
+        advance(qn, dn);
+        if (tid == 0 && qn < f.Q) issue(s ^ 1, qn, dn);
+        const unsigned parity = (unsigned)(k >> 1) & 1u;
+        const bool ok = fbar_wait(&bar[s], parity, f.err);
+        if (__syncthreads_or(ok ? 0 : 1)) {
+            if (!ok) fbar_wait(&bar[s], parity, f.err);
+            if (tid == 0 && qn < f.Q) fbar_wait(&bar[s ^ 1], (unsigned)((k + 1) >> 1) & 1u, f.err);
+            return;
+        }
+        const float4 *zs = (const float4 *)(buf + (size_t)s * stage);
+        const float2 *rs = (const float2 *)(buf + (size_t)s * stage + zb);
+        float4 win[PI + B - 1][PC];
+#pragma unroll
+        for (int r = 0; r < PI - 1; ++r)
+#pragma unroll
+            for (int h = 0; h < NV; ++h) win[r][h] = zs[(size_t)(ti * PI + r) * CA + h * TCN + tc];
+#pragma unroll
+        for (int d2 = 0; d2 < B; ++d2) {
+#pragma unroll
+            for (int h = 0; h < NV; ++h) win[d2 + PI - 1][h] = zs[(size_t)(ti * PI + d2 + PI - 1) * CA + h * TCN + tc];
+            float2 rv[PI];
+#pragma unroll
+            for (int p = 0; p < PI; ++p) rv[p] = rs[d2 * tw + ti * PI + p];
+#pragma unroll
+            for (int p = 0; p < PI; ++p)
+#pragma unroll
+                for (int c = 0; c < PC; ++c) {
+                    const float4 z = win[p + d2][c];
+                    df_fma(ah[p][c][0], al[p][c][0], rv[p].x, rv[p].y, z.x, z.y);
+                    df_fma(ah[p][c][1], al[p][c][1], rv[p].x, rv[p].y, z.z, z.w);
+                }
+        }
+        __syncthreads();
+        q = qn;
+        d1 = dn;
+    }
+    const long long NP = (long long)N1 * N2;
+#pragma unroll
+    for (int h = 0; h < NV; ++h) {
+        const int sl = c0 + h * TCN + tc;
+        if (sl >= f.A) continue;
+        cxd *__restrict__ yr = y + (size_t)f.perm[sl] * NP + (size_t)i1 * N2;
+#pragma unroll
+        for (int p = 0; p < PI; ++p) {
+            const int i2 = t0 + ti * PI + p;
+            if (i2 < N2)
+                yr[i2] = yr[i2] + mk<double>((double)ah[p][h][0] + (double)al[p][h][0],
+                                             (double)ah[p][h][1] + (double)al[p][h][1]);
+        }
+    }
+}
+
 template <typename R>
 int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
                     const double *inv_scale)
@@ -402,6 +544,13 @@ int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, c
     dim3 g2((unsigned)fd.N1, (unsigned)fd.ntiles, (unsigned)fd.nct);
     const int nt = fd.tw / T::PI * T::TCN;
     if (op->kb != 6) return PG_ERR_STORAGE;
+    if constexpr (sizeof(R) == 8) {
+        if (fd.df) {
+            fact_radial_df_kernel<6><<<g2, nt, fd.radial_smem, s>>>(fa, (cxd *)dst, fd.zmap, fd.rmap);
+            op->ctx->launches++;
+            return pg_check_launch(op->ctx);
+        }
+    }
     fact_radial_kernel<R, 6><<<g2, nt, fd.radial_smem, s>>>(fa, (cx<R> *)dst, fd.zmap, fd.rmap);
     op->ctx->launches++;
     return pg_check_launch(op->ctx);
@@ -607,7 +756,19 @@ int pg_factored_finalize(pg_op *op)
     PG_CUDA_TRY(cudaMalloc(&f.w, sizeof(cxd) * Q));
     PG_CUDA_TRY(cudaMemcpy(f.w, w.data(), sizeof(cxd) * Q, cudaMemcpyHostToDevice));
     PG_TRY(fp64 ? upload_real<double>(&f.coef, coef) : upload_real<float>(&f.coef, coef));
-    PG_TRY(fp64 ? upload_real<double>(&f.radial, rad) : upload_real<float>(&f.radial, rad));
+    f.df = fp64 && op->fp64_emulation;
+    if (f.df) {  // (hi, lo) float pairs in the 8 bytes of each coefficient
+        std::vector<float> pairs(2 * rad.size());
+        for (size_t t = 0; t < rad.size(); ++t) {
+            const float hi = (float)rad[t];
+            pairs[2 * t] = hi;
+            pairs[2 * t + 1] = (float)(rad[t] - (double)hi);
+        }
+        PG_CUDA_TRY(cudaMalloc(&f.radial, sizeof(float) * pairs.size()));
+        PG_CUDA_TRY(cudaMemcpy(f.radial, pairs.data(), sizeof(float) * pairs.size(), cudaMemcpyHostToDevice));
+    } else {
+        PG_TRY(fp64 ? upload_real<double>(&f.radial, rad) : upload_real<float>(&f.radial, rad));
+    }
     const size_t zbytes = (size_t)Q * f.Ap * (size_t)N1 * N2 * 2 * esz;
     PG_CUDA_TRY(cudaMalloc(&f.Z, zbytes));
     PG_CUDA_TRY(cudaMemset(f.Z, 0, zbytes));  // rows without entries are read as zeros
@@ -628,8 +789,10 @@ int pg_factored_finalize(pg_op *op)
         PG_CUDA_TRY(cudaFuncSetAttribute(fact_mix_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     else
         PG_CUDA_TRY(cudaFuncSetAttribute(fact_mix_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    if (fp64)
+    if (fp64) {
         PG_CUDA_TRY(cudaFuncSetAttribute(fact_radial_kernel<double, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+        PG_CUDA_TRY(cudaFuncSetAttribute(fact_radial_df_kernel<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    }
     else
         PG_CUDA_TRY(cudaFuncSetAttribute(fact_radial_kernel<float, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     // TMA maps. Z as [Q * N1][N2][2 Ap] reals: box = 2 CA reals x (tw + 2k) points x 1 row,
@@ -684,5 +847,14 @@ extern "C" int pg_op_factored_info(const pg_op *op, double *info)
     info[3] = f.flops_radial;
     info[4] = f.radial_bytes;
     info[5] = f.z_bytes;
+    return PG_OK;
+}
+
+extern "C" int pg_op_set_fp64_emulation(pg_op *op, int on)
+{
+    if (!op) return PG_ERR_ARG;
+    if (op->finalized) return PG_ERR_STATE;
+    if (op->precision != PG_FP64) return PG_ERR_ARG;
+    op->fp64_emulation = on != 0;
     return PG_OK;
 }

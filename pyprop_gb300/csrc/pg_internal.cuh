@@ -144,6 +144,7 @@ struct HostFactor {
 struct FactDev {
     int Q = 0, Qp = 0, A = 0, Ap = 0, N1 = 0, N2 = 0, N2p = 0, nct = 0, nE = 0;
     int tw = 0, ntiles = 0;        // radial kernel: points of the last rank per CTA, tiles per row
+    int df = 0;                    // FP64 operator computing its radial stencil in double-float
     size_t radial_smem = 0;        // its dynamic shared memory
     CUtensorMap zmap, rmap;        // TMA maps of the scratch and of the radial factors
     int *row_ptr = nullptr;           // [A + 1] segments per output channel
@@ -204,6 +205,7 @@ struct pg_op {
     std::vector<HostFactor> factors;
     FactDev fact;
     bool tuning = false;  // the variant autotuner times the banded part alone
+    bool fp64_emulation = false;  // FP64 operator: factorized radial stencil in double-float
 };
 
 // factorized terms (factored.cu): upload at finalize, release, and the two-kernel apply that

@@ -101,7 +101,7 @@ class DeviceOperator:
     the host, as the reference does per matvec).
     """
 
-    def __init__(self, ctx, potentials, shape, kb, precision, overlap_rows=None):
+    def __init__(self, ctx, potentials, shape, kb, precision, overlap_rows=None, fp64_emulation=False):
         self.ctx = ctx
         self.lib = ctx.lib
         self.shape = tuple(shape)
@@ -114,11 +114,20 @@ class DeviceOperator:
         shp, shp_p = nat.iptr(np.asarray(shape, dtype=np.int32))
         check(self.lib.pg_op_create(ctx.h, len(shape), shp_p, kb, precision, C.byref(h)), "pg_op_create")
         self.h = h
+        self.fp64_emulation = bool(fp64_emulation) and precision == nat.PG_FP64
+        if self.fp64_emulation:
+            check(self.lib.pg_op_set_fp64_emulation(self.h, 1), "pg_op_set_fp64_emulation")
         self.has_overlap = overlap_rows is not None
+        any_factored = any(getattr(pot, "Factors", None) is not None for pot in self.potentials)
+        overlap_factor = None
         if overlap_rows is not None:
             rows = np.asarray(overlap_rows, dtype=np.float64)
             band = bandnh_from_rows(rows, kb)[None, :]
-            if len(shape) == 2:
+            if len(shape) == 3 and any_factored:
+                # two electrons with factorized terms: S x S as one more factor (identity on the
+                # channels, S[i1][d1] S[i2][d2] on the radial grid)
+                overlap_factor = np.einsum("ad,ce->adec", rows, rows)
+            elif len(shape) == 2:
                 self._add(["Ident", "BandNH"], band, [None, None], 0)
             else:
                 # two electrons: S x S on the radial ranks, the first one as a packed pair list
@@ -136,6 +145,10 @@ class DeviceOperator:
             pairs = [g.GetBasisPairs() if k in ("Simp", "Herm") else None for g, k in zip(pot.GeometryList, kinds)]
             self._add(kinds, pot.PotentialData, pairs, 1 + p)
         self.nfactors = 0
+        if overlap_factor is not None:
+            from .tensorpotential import FactoredPotential
+            factored.insert(0, (FactoredPotential(None, np.ones((1, shape[0])), np.ones(1, dtype=np.complex128),
+                                                  overlap_factor[None], None, kb, shape[0]), 0))
         if factored:
             self._add_factored(factored)
         check(self.lib.pg_op_finalize(self.h), "pg_op_finalize")

@@ -96,14 +96,15 @@ class BasisPropagatorGPU(PropagatorBase):
         self._ops = {}
 
     # device operators, built on first use
-    def device_operator(self, precision, with_overlap=False):
-        key = (precision, with_overlap)
+    def device_operator(self, precision, with_overlap=False, fp64_emulation=False):
+        key = (precision, with_overlap, bool(fp64_emulation))
         if key not in getattr(self, "_ops", {}):
             if not hasattr(self, "_ops"):
                 self._ops = {}
             repr_ = self.psi.GetRepresentation()
             self._ops[key] = DeviceOperator(Context.get(), self.PotentialList, repr_.GetFullShape(), repr_.kb,
-                                            precision, repr_.overlap_rows if with_overlap else None)
+                                            precision, repr_.overlap_rows if with_overlap else None,
+                                            fp64_emulation=fp64_emulation)
         return self._ops[key]
 
     def MultiplyPotential(self, srcPsi, destPsi, t, dt):
@@ -338,6 +339,9 @@ class CayleyPropagatorGPU(PropagatorBase):
         self.StepStats = bool(getattr(conf, "gpu_step_stats", True))
         self.TrueResidual = bool(getattr(conf, "gpu_true_residual", False))
         self.Eager = bool(getattr(conf, "gpu_eager", False))
+        # mixed precision: the FP64 residual operator computes its factorized (two-electron)
+        # terms in double-float arithmetic unless gpu_fp64_emulation = False
+        self.Fp64Emulation = bool(getattr(conf, "gpu_fp64_emulation", True))
         name = getattr(conf, "preconditioner", None)
         self.Preconditioner = None
         if name:
@@ -357,7 +361,8 @@ class CayleyPropagatorGPU(PropagatorBase):
         self.Preconditioner.SetOverlapScaling(1.0)
         self.Preconditioner.Setup(self, self.Precision)
         bp = self.BasePropagator
-        self.op64 = bp.device_operator(nat.PG_FP64, with_overlap=True)
+        emulate = self.Precision != nat.PG_FP64 and self.Fp64Emulation
+        self.op64 = bp.device_operator(nat.PG_FP64, with_overlap=True, fp64_emulation=emulate)
         self.opb = bp.device_operator(self.Precision, with_overlap=True)
         self.stepper = CayleyStepper(self.op64, self.opb, self.Preconditioner.solvers[nat.PG_FP64],
                                      self.Preconditioner.solvers[self.Precision], self.BasisSize, self.Precision,

@@ -244,3 +244,32 @@ def test_fast_diagonalization_preconditioner_solves_the_separable_block(gpu):
         iters[name] = prob.Propagator.LastStats.Iterations
     print("GMRES iterations per Cayley step:", iters)
     assert iters["fd"] < iters["kron"]
+
+
+def test_factored_fp64_emulation_matches_oracle(gpu):
+    """The FP64 operator with its factorized terms in double-float arithmetic (FP32 pairs,
+    error-free products and sums) meets the FP64 tolerance against the oracle, with and without
+    the S x S overlap factor (the overlap slot of the Cayley residual operator)."""
+    import torch
+    from oracle.operators import factored_multiply
+    prob = helium_problem(lmax=4, L=(0, 1, 2), nbsplines=14, rmax=12.0, amplitude=0.07, frequency=1.0,
+                          pulse_duration=2.0)
+    bp = prob.Propagator.BasePropagator
+    bp.SetupStep(0.01)
+    pots = bp.PotentialList
+    repr_ = prob.psi.GetRepresentation()
+    shape = repr_.GetFullShape()
+    rng = np.random.default_rng(31)
+    x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    S = repr_.radial.BSplineObject.dense(repr_.overlap_rows)
+    for with_overlap in (False, True):
+        op = bp.device_operator(nat.PG_FP64, with_overlap=with_overlap, fp64_emulation=True)
+        assert op.fp64_emulation
+        sc = op.scales(0.37, 0.5j * 0.01, 1.0 if with_overlap else 0.0)
+        src = torch.as_tensor(x, device="cuda")
+        dst = torch.zeros_like(src)
+        op.matvec(sc, src, dst)
+        ref = factored_multiply([(p.Factors, 1 + i) for i, p in enumerate(pots)], sc, x, np.zeros(shape, complex))
+        if with_overlap:
+            ref += np.einsum("ij,ajk,lk->ail", S, x, S)
+        assert relerr(dst.cpu().numpy(), ref) < 1e-12, with_overlap
