@@ -225,9 +225,10 @@ int pg_prec_kron_create(pg_op *op, const double *overlap_rows, const double *cS,
  * lam [nl][N], lidx [Nang][2] the eigenvector set of each channel's two electrons. In place of
  * the reference's per-channel sparse LU / ILU block preconditioners
  * (examples/tensor/helium_stabilization/preconditioner.py:77-244): exact for every term but
- * the electron-electron repulsion. Requires N1 = N2 <= pg_prec_fd_max_n(precision) (the
- * channel block lives in shared memory); PG_ERR_SHAPE otherwise. Applied by
- * PG_BAND_PREC_SOLVE (one kernel). */
+ * the electron-electron repulsion. Requires N1 = N2. Up to pg_prec_fd_max_n(precision) the
+ * channel block lives in shared memory (one kernel per solve); beyond, the four products run
+ * as batched GEMMs on planar copies in global memory (seven kernels, two scratch copies of the
+ * wavefunction). Applied by PG_BAND_PREC_SOLVE. */
 int pg_prec_fd_create(pg_op *op, int nl, const double *V, const double *lam, const int *lidx, const double *cS,
                       const double *cH, pg_banded **out);
 int pg_prec_fd_max_n(int precision);

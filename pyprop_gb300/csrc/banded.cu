@@ -583,6 +583,8 @@ extern "C" int pg_banded_destroy(pg_banded *b)
     cudaFree(e->d_fdV);
     cudaFree(e->d_fdD);
     cudaFree(e->d_fdl);
+    cudaFree(e->d_fdP0);
+    cudaFree(e->d_fdP1);
     delete e;
     return PG_OK;
 }
@@ -721,7 +723,7 @@ int pg_banded_apply_dev(pg_banded *b, int which, void *x)
 
 extern "C" int pg_banded_apply(pg_banded *b, int which, void *x) { return pg_banded_apply_dev(b, which, x); }
 
-int pg_banded_solve_kernels(const pg_banded *b) { return b->kind == 2 ? 4 : 1; }
+int pg_banded_solve_kernels(const pg_banded *b) { return b->kind == 2 ? 4 : b->kind == 3 ? pg_fd_kernels(b) : 1; }
 
 // Two-electron preconditioner by fast diagonalization (fdprec.cu): per channel a the exact
 // inverse of cS S x S + cH (h_l1 x S + S x h_l2) from the generalized eigenvectors
@@ -733,10 +735,12 @@ extern "C" int pg_prec_fd_create(pg_op *op, int nl, const double *V, const doubl
     if (!op->finalized) return PG_ERR_STATE;
     if (op->rank != 3 || op->shape[1] != op->shape[2]) return PG_ERR_STORAGE;
     const int A = op->shape[0], N = op->shape[1];
-    const int NP = (N + 3) & ~3;
+    const int NP0 = (N + 3) & ~3;
     for (int a = 0; a < 2 * A; ++a)
         if (lidx[a] < 0 || lidx[a] >= nl) return PG_ERR_ARG;
-    PG_TRY(pg_fd_prepare(op->precision, NP));
+    // the shared-memory kernel when the channel block fits, batched GEMMs otherwise
+    const bool global = pg_fd_prepare(op->precision, NP0) != PG_OK;
+    const int NP = global ? N : NP0;
     const zd zS(cS[0], cS[1]), zH(cH[0], cH[1]);
     std::vector<double> Vp((size_t)nl * NP * NP, 0.0);
     for (int l = 0; l < nl; ++l)
@@ -757,6 +761,12 @@ extern "C" int pg_prec_fd_create(pg_op *op, int nl, const double *V, const doubl
     bd->complex_coef = 1;
     bd->fdN = N;
     bd->fdNP = NP;
+    bd->fdGlobal = global ? 1 : 0;
+    if (global) {
+        const size_t bytes = (op->precision == PG_FP64 ? sizeof(double) : sizeof(float)) * 2 * (size_t)A * N * N;
+        PG_CUDA_TRY(cudaMalloc(&bd->d_fdP0, bytes));
+        PG_CUDA_TRY(cudaMalloc(&bd->d_fdP1, bytes));
+    }
     PG_CUDA_TRY(cudaMalloc(&bd->d_fdl, sizeof(int) * 2 * A));
     PG_CUDA_TRY(cudaMemcpy(bd->d_fdl, lidx, sizeof(int) * 2 * A, cudaMemcpyHostToDevice));
     if (op->precision == PG_FP64) {

@@ -16,6 +16,8 @@
 // reads done before the barrier that precedes the write-back).
 #include "pg_internal.cuh"
 
+#include <algorithm>
+
 namespace {
 
 template <typename R>
@@ -154,6 +156,130 @@ size_t fd_smem(int NP)
     return 2 * (size_t)NP * NP * sizeof(R) + (size_t)NP * NP * sizeof(cx<R>);
 }
 
+// ---- radial sizes beyond the shared-memory kernel: the four products as batched GEMMs on
+// planar (real, imaginary) copies in global memory. Batch z = 2 a + c (channel a, part c).
+// x [A][N][N] complex <-> P [A][2][N][N] real
+template <typename R>
+__global__ void fd_split_kernel(const cx<R> *__restrict__ x, R *__restrict__ P, long long NN, long long total)
+{
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        const long long a = t / NN, e = t - a * NN;
+        const cx<R> v = x[t];
+        P[(2 * a) * NN + e] = v.x;
+        P[(2 * a + 1) * NN + e] = v.y;
+    }
+}
+template <typename R>
+__global__ void fd_merge_kernel(const R *__restrict__ P, cx<R> *__restrict__ x, long long NN, long long total)
+{
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        const long long a = t / NN, e = t - a * NN;
+        x[t] = mk<R>(P[(2 * a) * NN + e], P[(2 * a + 1) * NN + e]);
+    }
+}
+// Q = D o P (complex, planar)
+template <typename R>
+__global__ void fd_dmul_kernel(const R *__restrict__ P, const cx<R> *__restrict__ D, R *__restrict__ Q, long long NN,
+                               long long total)
+{
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        const long long a = t / NN, e = t - a * NN;
+        const R re = P[(2 * a) * NN + e], im = P[(2 * a + 1) * NN + e];
+        const cx<R> d = D[t];
+        Q[(2 * a) * NN + e] = d.x * re - d.y * im;
+        Q[(2 * a + 1) * NN + e] = d.x * im + d.y * re;
+    }
+}
+
+// Batched N x N products C_z = op(A_z) op(B_z), row-major. MODE picks the operands of batch
+// z = 2a + c: 1: V_l1^T S_z, 2: S_z V_l2, 3: V_l1 S_z, 4: S_z V_l2^T (V the eigenvector set of
+// the channel's electron). 64 x 64 outputs per CTA, 256 threads with 4 x 4 each, K in steps of 16.
+template <typename R, int MODE>
+__global__ void __launch_bounds__(256) fd_gemm_kernel(int N, const R *__restrict__ V, const int *__restrict__ lidx,
+                                                      const R *__restrict__ S, R *__restrict__ C)
+{
+    constexpr int TM = 64, TK = 16;
+    __shared__ R As[TK][TM + 4];
+    __shared__ R Bs[TK][TM + 4];
+    const int z = blockIdx.z, a = z >> 1;
+    const size_t NN = (size_t)N * N;
+    const R *Vm = V + (size_t)lidx[2 * a + ((MODE == 1 || MODE == 3) ? 0 : 1)] * NN;
+    const R *Sm = S + (size_t)z * NN;
+    R *Cm = C + (size_t)z * NN;
+    const int i0 = blockIdx.y * TM, j0 = blockIdx.x * TM;
+    const int tid = threadIdx.x, tr = tid / 16, tcol = tid % 16;
+    R acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = (R)0;
+    for (int k0 = 0; k0 < N; k0 += TK) {
+        // As[kk][ii] = opA[i0 + ii][k0 + kk], Bs[kk][jj] = opB[k0 + kk][j0 + jj]
+        for (int t = tid; t < TK * TM; t += 256) {
+            const int kk = t / TM, ii = t - kk * TM;
+            const int i = i0 + ii, k = k0 + kk;
+            R av = (R)0;
+            if (i < N && k < N) {
+                if (MODE == 1) av = Vm[(size_t)k * N + i];       // V^T
+                else if (MODE == 3) av = Vm[(size_t)i * N + k];  // V
+                else av = Sm[(size_t)i * N + k];                 // S
+            }
+            As[kk][ii] = av;
+            const int j = j0 + ii;
+            R bv = (R)0;
+            if (j < N && k < N) {
+                if (MODE == 2) bv = Vm[(size_t)k * N + j];       // V
+                else if (MODE == 4) bv = Vm[(size_t)j * N + k];  // V^T
+                else bv = Sm[(size_t)k * N + j];                 // S
+            }
+            Bs[kk][ii] = bv;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < TK; ++kk) {
+            R ar[4], br[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) ar[u] = As[kk][tr * 4 + u];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) br[v] = Bs[kk][tcol * 4 + v];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] = fma(ar[u], br[v], acc[u][v]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int i = i0 + tr * 4 + u, j = j0 + tcol * 4 + v;
+            if (i < N && j < N) Cm[(size_t)i * N + j] = acc[u][v];
+        }
+}
+
+template <typename R>
+int fd_apply_global(pg_banded *b, void *x)
+{
+    pg_ctx *ctx = b->op->ctx;
+    const int A = b->op->shape[0], N = b->fdN;
+    const long long NN = (long long)N * N, total = (long long)A * NN;
+    cudaStream_t s = ctx->stream;
+    const int eb = (int)std::min<long long>((total + 255) / 256, 152LL * 16);
+    R *P0 = (R *)b->d_fdP0, *P1 = (R *)b->d_fdP1;
+    const R *V = (const R *)b->d_fdV;
+    dim3 g((N + 63) / 64, (N + 63) / 64, 2 * A);
+    fd_split_kernel<R><<<eb, 256, 0, s>>>((const cx<R> *)x, P0, NN, total);
+    fd_gemm_kernel<R, 1><<<g, 256, 0, s>>>(N, V, b->d_fdl, P0, P1);
+    fd_gemm_kernel<R, 2><<<g, 256, 0, s>>>(N, V, b->d_fdl, P1, P0);
+    fd_dmul_kernel<R><<<eb, 256, 0, s>>>(P0, (const cx<R> *)b->d_fdD, P1, NN, total);
+    fd_gemm_kernel<R, 3><<<g, 256, 0, s>>>(N, V, b->d_fdl, P1, P0);
+    fd_gemm_kernel<R, 4><<<g, 256, 0, s>>>(N, V, b->d_fdl, P0, P1);
+    fd_merge_kernel<R><<<eb, 256, 0, s>>>(P1, (cx<R> *)x, NN, total);
+    ctx->launches += 7;
+    return pg_check_launch(ctx);
+}
+
 }  // namespace
 
 int pg_fd_max_n(int precision)
@@ -169,6 +295,8 @@ int pg_fd_max_n(int precision)
 
 int pg_fd_apply_dev(pg_banded *b, void *x)
 {
+    if (b->fdGlobal)
+        return b->op->precision == PG_FP64 ? fd_apply_global<double>(b, x) : fd_apply_global<float>(b, x);
     pg_ctx *ctx = b->op->ctx;
     const int A = b->op->shape[0], NP = b->fdNP;
     const int TN = NP / 4;
@@ -196,3 +324,5 @@ int pg_fd_prepare(int precision, int NP)
         PG_CUDA_TRY(cudaFuncSetAttribute(fd_solve_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     return PG_OK;
 }
+
+int pg_fd_kernels(const pg_banded *b) { return b->fdGlobal ? 7 : 1; }

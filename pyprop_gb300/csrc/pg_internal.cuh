@@ -260,11 +260,15 @@ struct pg_banded {
     void *d_fdV = nullptr, *d_fdD = nullptr;
     int *d_fdl = nullptr;
     int fdN = 0, fdNP = 0;
+    int fdGlobal = 0;                        // products as batched GEMMs through global memory
+    void *d_fdP0 = nullptr, *d_fdP1 = nullptr;  // their planar scratch [A][2][N][N]
 };
 
-// kind-3 solve x <- M^-1 x on every channel (fdprec.cu); largest supported radial size
+// kind-3 solve x <- M^-1 x on every channel (fdprec.cu); largest radial size of the
+// shared-memory kernel (larger sizes use batched GEMMs through global memory); kernels per solve
 int pg_fd_apply_dev(pg_banded *b, void *x);
 int pg_fd_max_n(int precision);
+int pg_fd_kernels(const pg_banded *b);
 // checks the shared memory the solve needs for padded size NP and raises the kernel's limit
 int pg_fd_prepare(int precision, int NP);
 

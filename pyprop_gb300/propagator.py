@@ -278,8 +278,8 @@ class TwoElectronFastDiagonalizationPreconditioner(TwoElectronKroneckerPrecondit
     device. Unlike the Kronecker product (cS S + cH h1) x (cS S + cH h2), it has no cH^2 h1 x h2
     error, so GMRES is left only with the electron-electron repulsion that the reference's
     RadialTwoElectronPreconditionerSuperLU / Ifpack also put in the block
-    (examples/tensor/helium_stabilization/preconditioner.py:77-244). For radial sizes beyond
-    the shared-memory limit of the device kernel it falls back to the Kronecker product."""
+    (examples/tensor/helium_stabilization/preconditioner.py:77-244). Radial sizes beyond the
+    shared-memory limit of the one-kernel solve run as batched GEMMs through global memory."""
 
     def _dense(self, l):
         band = self._one_electron(l).real  # rows [N][2k+1], [i, k + j - i] = h(i, j)
@@ -298,9 +298,6 @@ class TwoElectronFastDiagonalizationPreconditioner(TwoElectronKroneckerPrecondit
         if len(shape) != 3:
             raise ValueError("TwoElectronFastDiagonalizationPreconditioner needs a two-electron representation")
         ctx = Context.get()
-        N = shape[1]
-        if any(N > Banded.fast_diagonalization_max_n(ctx, p) for p in (nat.PG_FP64, precision)):
-            return TwoElectronKroneckerPreconditioner.Setup(self, prop, precision)
         self.Method = "fast-diagonalization"
         indices = repr_.bases[0].indices
         S = repr_.radial.BSplineObject.dense(repr_.overlap_rows)

@@ -273,3 +273,31 @@ def test_factored_fp64_emulation_matches_oracle(gpu):
         if with_overlap:
             ref += np.einsum("ij,ajk,lk->ail", S, x, S)
         assert relerr(dst.cpu().numpy(), ref) < 1e-12, with_overlap
+
+
+def test_fast_diagonalization_large_radial_rank(gpu):
+    """130 splines per electron: beyond the shared-memory solve (FP64 at least), the four
+    products as batched GEMMs; both precisions against the host evaluation of
+    V1 (D o (V1^T X V2)) V2^T."""
+    import scipy.linalg as sl
+    import torch
+    prob = helium_problem(lmax=1, nbsplines=130, rmax=40.0, L=(0,), propagator="CayleyPropagatorGPU",
+                          precision="fp32")
+    prob.SetupStep(skipWavefunctionSetup=True)
+    pre = prob.Propagator.Preconditioner
+    repr_ = prob.psi.GetRepresentation()
+    shape = repr_.GetFullShape()
+    S = repr_.radial.BSplineObject.dense(repr_.overlap_rows)
+    cS, cH = pre.OverlapScaling, pre.HamiltonianScaling
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    ref = np.empty_like(x)
+    for a, ix in enumerate(repr_.bases[0].indices):
+        w1, v1 = sl.eigh(pre._dense(ix.l1), S)
+        w2, v2 = sl.eigh(pre._dense(ix.l2), S)
+        D = 1.0 / (cS + cH * (w1[:, None] + w2[None, :]))
+        ref[a] = v1 @ (D * (v1.T @ x[a] @ v2)) @ v2.T
+    for prec, dt, tol in ((nat.PG_FP64, torch.complex128, 1e-10), (nat.PG_FP32, torch.complex64, 1e-4)):
+        y = torch.as_tensor(x, device="cuda").to(dt)
+        pre.solvers[prec].apply(nat.PG_BAND_PREC_SOLVE, y)
+        assert relerr(y.to(torch.complex128).cpu().numpy(), ref) < tol, prec
