@@ -184,33 +184,41 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
         for (; g < g_end; ++g) {
             const int4 sg = seg[g];
             if (sg.x >= qc + MQC) break;  // segments are in factor order
-            cx<R> s0[MPT], s1[MPT];
+            constexpr int CH = 4;  // independent chains: four source loads in flight per lane
+            cx<R> sum[CH][MPT];
 #pragma unroll
-            for (int u = 0; u < MPT; ++u) s0[u] = s1[u] = mk<R>((R)0, (R)0);
+            for (int h = 0; h < CH; ++h)
+#pragma unroll
+                for (int u = 0; u < MPT; ++u) sum[h][u] = mk<R>((R)0, (R)0);
             int z = sg.y;
-            for (; z + 1 < sg.z; z += 2) {  // two independent chains
-                cx<R> x0[MPT], x1[MPT];
-                load_x(pcol[z], x0);
-                load_x(pcol[z + 1], x1);
-                const R c0 = pc[z], c1 = pc[z + 1];
+            for (; z + CH - 1 < sg.z; z += CH) {
+                cx<R> xv[CH][MPT];
 #pragma unroll
-                for (int u = 0; u < MPT; ++u) {
-                    s0[u].x = fma(c0, x0[u].x, s0[u].x); s0[u].y = fma(c0, x0[u].y, s0[u].y);
-                    s1[u].x = fma(c1, x1[u].x, s1[u].x); s1[u].y = fma(c1, x1[u].y, s1[u].y);
+                for (int h = 0; h < CH; ++h) load_x(pcol[z + h], xv[h]);
+#pragma unroll
+                for (int h = 0; h < CH; ++h) {
+                    const R c = pc[z + h];
+#pragma unroll
+                    for (int u = 0; u < MPT; ++u) {
+                        sum[h][u].x = fma(c, xv[h][u].x, sum[h][u].x);
+                        sum[h][u].y = fma(c, xv[h][u].y, sum[h][u].y);
+                    }
                 }
             }
-            if (z < sg.z) {
+            for (; z < sg.z; ++z) {
                 cx<R> x0[MPT];
                 load_x(pcol[z], x0);
-                const R c0 = pc[z];
+                const R c = pc[z];
 #pragma unroll
                 for (int u = 0; u < MPT; ++u) {
-                    s0[u].x = fma(c0, x0[u].x, s0[u].x); s0[u].y = fma(c0, x0[u].y, s0[u].y);
+                    sum[0][u].x = fma(c, x0[u].x, sum[0][u].x);
+                    sum[0][u].y = fma(c, x0[u].y, sum[0][u].y);
                 }
             }
 #pragma unroll
             for (int u = 0; u < MPT; ++u)
-                acc[(((size_t)(sg.x - qc) * MPT + u) * 32 + lane) * (CB + 1) + wrp] = s0[u] + s1[u];
+                acc[(((size_t)(sg.x - qc) * MPT + u) * 32 + lane) * (CB + 1) + wrp] =
+                    (sum[0][u] + sum[1][u]) + (sum[2][u] + sum[3][u]);
         }
         __syncthreads();
         for (int t = threadIdx.x; t < MQC * TP * CB; t += 32 * CB) {
