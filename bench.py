@@ -354,6 +354,40 @@ def profile_two_electron():
                       "preconditioner": prop.Preconditioner.Method}))
 
 
+TWO_ELECTRON_LARGE = dict(lmax=16, L=tuple(range(9)), nbsplines=200, rmax=200.0)
+
+
+def profile_two_electron_large():
+    """Profiling entry point: the largest two-electron model (coupled L <= 8, l1, l2 <= 16, 200
+    splines per electron: 1017 channels, 4.07e7 coefficients), three complex64 matvecs of its
+    factorized operator after one untimed launch (setup takes about a minute on the host)."""
+    import torch
+    from pyprop_gb300 import _native as nat
+    import pyprop_gb300 as pp
+    from pyprop_gb300.workloads import helium
+    prob = pp.Problem(pp.LoadString(helium(**TWO_ELECTRON_LARGE)))
+    bp = prob.Propagator.BasePropagator
+    bp.SetupStep(0.01)
+    op = bp.device_operator(nat.PG_FP32)
+    shape = prob.psi.GetRepresentation().GetFullShape()
+    src = torch.randn(shape, dtype=torch.complex64, device="cuda")
+    dst = torch.zeros_like(src)
+    sc = op.scales(0.0)
+    op.matvec(sc, src, dst)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s_ev.record(stream)
+    for _ in range(3):
+        op.matvec(sc, src, dst)
+    e_ev.record(stream)
+    e_ev.synchronize()
+    info = op.factored_info()
+    ms = s_ev.elapsed_time(e_ev) / 3
+    print(json.dumps({"profile": "two_electron_large", "ms_per_matvec": ms,
+                      "tflops": (info["flops_mix"] + info["flops_radial"]) / ms / 1e9, "info": info}))
+
+
 def fp32_fma_peak_tflops():
     """Nominal FP32 FMA peak of the GB300 at the maximum SM clock: 152 SMs x 128 lanes x 2 flops
     (no measured FP32 peak exists for this machine)."""
@@ -753,7 +787,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=300,
                     help="oracle Cayley steps timed on one host core for cpu_baseline (0 = skip)")
     ap.add_argument("--two-electron", type=int, default=1, help="factorized two-electron matvec leg (0 = skip)")
-    ap.add_argument("--profile", choices=["matvec_hbm", "two_electron"], default=None,
+    ap.add_argument("--profile", choices=["matvec_hbm", "two_electron", "two_electron_large"], default=None,
                     help="profiling entry point instead of the benchmark")
     ap.add_argument("--eager", action="store_true",
                     help="host-driven GMRES loops (same kernels, visible one by one to a profiler)")
@@ -769,6 +803,10 @@ def main():
     if args.profile == "two_electron":
         build_native.build()
         profile_two_electron()
+        return
+    if args.profile == "two_electron_large":
+        build_native.build()
+        profile_two_electron_large()
         return
     if args.impl == "reference":
         run_reference(args)
