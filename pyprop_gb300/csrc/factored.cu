@@ -20,11 +20,12 @@
 // skipping factors none of the 4 channels has (their scratch stays at the zeros written at
 // upload).
 // radial: a 169-point stencil (k = 6) with coefficients varying per point and shared by all
-// channels. A CTA = one radial row i1, a tile of tw points of the last rank and CA channels;
-// per stage (factor q, row offset d1) one TMA box brings the Z rows [tw + 2k][CA] and one the
-// coefficient rows [2k+1][tw] into shared memory (double-buffered on two mbarriers, bounded
-// waits); each thread keeps PI consecutive points x PC channels of accumulators and a sliding
-// window of PI rows of Z in registers. Bound by FP32 (or FP64) FMA throughput.
+// channels. A CTA = two radial rows, a tile of tw points of the last rank and CA channels;
+// per stage (factor q, input row j1) one TMA box brings the Z rows [tw + 2k][CA] (used by both
+// output rows) and one box per output row its coefficient rows [2k+1][tw] into shared memory
+// (double-buffered on two mbarriers, bounded waits); each thread keeps PI consecutive points x
+// PC channels of accumulators and a sliding window of PI rows of Z in registers. Bound by FP32
+// (or FP64) FMA throughput.
 #include "pg_internal.cuh"
 
 #include <algorithm>
@@ -270,10 +271,15 @@ __host__ __device__ inline size_t rad_rbytes(int tw, int kb)
     return (size_t)(2 * kb + 1) * tw * sizeof(R);
 }
 
-// One CTA = radial row i1 (blockIdx.x), tw points of the last rank (blockIdx.y), CA channels
-// (blockIdx.z); thread = PI consecutive points x NV vectors of channels. blockDim = tw / PI x 8.
+// rows of the first radial rank per radial-stencil CTA (they share each staged row of Z)
+const int RB = 2;
+
+// One CTA = radial rows i1_0 .. i1_0 + RB (blockIdx.x), tw points of the last rank
+// (blockIdx.y), CA channels (blockIdx.z); thread = (row rr, PI consecutive points, NV vectors of
+// channels). blockDim = RB x tw / PI x 8. A stage is (factor q, input row j1): one TMA box of Z
+// row j1 serves both output rows, each with its own box of coefficients R_q[i1][j1 - i1 + k].
 template <typename R, int KB>
-__global__ void __launch_bounds__(128, 2) fact_radial_kernel(FactArgs f, cx<R> *__restrict__ y,
+__global__ void __launch_bounds__(256, 1) fact_radial_kernel(FactArgs f, cx<R> *__restrict__ y,
                                                              const __grid_constant__ CUtensorMap zmap,
                                                              const __grid_constant__ CUtensorMap rmap)
 {
@@ -284,10 +290,13 @@ __global__ void __launch_bounds__(128, 2) fact_radial_kernel(FactArgs f, cx<R> *
     unsigned long long *bar = (unsigned long long *)smem_raw;
     const int tw = f.tw;
     const unsigned zbytes = (unsigned)rad_zbytes<R>(tw, KB), rbytes = (unsigned)rad_rbytes<R>(tw, KB);
-    const size_t zb = rad_round128<R>(zbytes), stage = zb + rad_round128<R>(rbytes);
+    const size_t zb = rad_round128<R>(zbytes), rb = rad_round128<R>(rbytes), stage = zb + RB * rb;
     unsigned char *buf = smem_raw + 128;
-    const int tid = threadIdx.x, tc = tid % TCN, ti = tid / TCN;
-    const int i1 = blockIdx.x, t0 = blockIdx.y * tw, ct = blockIdx.z, c0 = ct * CA;
+    const int per_row = (tw / PI) * TCN;
+    const int tid = threadIdx.x, rr = tid / per_row, lt = tid - rr * per_row;
+    const int tc = lt % TCN, ti = lt / TCN;
+    const int i1b = blockIdx.x * RB, t0 = blockIdx.y * tw, ct = blockIdx.z, c0 = ct * CA;
+    const int i1 = i1b + rr;
     const int N1 = f.N1, N2 = f.N2;
     if (tid == 0) {
         fbar_init(&bar[0], 1);
@@ -295,42 +304,52 @@ __global__ void __launch_bounds__(128, 2) fact_radial_kernel(FactArgs f, cx<R> *
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
-    // stages (q, d1): factors with a nonzero row in this channel tile, rows inside the grid
-    auto advance = [&](int &q, int &d1) {
+    // stages (q, j1): factors with a nonzero row in this channel tile, input rows of the grid
+    // within k of one of the CTA's output rows
+    const int jlo = max(0, i1b - KB), jhi = min(N1 - 1, min(N1 - 1, i1b + RB - 1) + KB);
+    auto advance = [&](int &q, int &j1) {
         for (;;) {
-            if (++d1 == B) {
-                d1 = 0;
+            if (++j1 > jhi) {
+                j1 = jlo;
                 ++q;
             }
             if (q >= f.Q) return;
             if (!f.bflag[(size_t)q * f.nct + ct]) {
-                d1 = B - 1;
+                j1 = jhi;
                 continue;
             }
-            const int j1 = i1 + d1 - KB;
-            if (j1 >= 0 && j1 < N1) return;
+            return;
         }
     };
-    auto issue = [&](int s, int q, int d1) {
+    auto issue = [&](int s, int q, int j1) {
         unsigned char *dst = buf + (size_t)s * stage;
-        fbar_expect(&bar[s], zbytes + rbytes);
-        tma_3d(dst, &zmap, 2 * c0, t0 - KB, q * N1 + i1 + d1 - KB, &bar[s]);
-        tma_2d(dst + zb, &rmap, t0, ((q * N1 + i1) * B + d1) * B, &bar[s]);
+        unsigned bytes = zbytes;
+        for (int r = 0; r < RB; ++r) {
+            const int d1 = j1 - (i1b + r) + KB;
+            if (i1b + r < N1 && d1 >= 0 && d1 < B) bytes += rbytes;
+        }
+        fbar_expect(&bar[s], bytes);
+        tma_3d(dst, &zmap, 2 * c0, t0 - KB, q * N1 + j1, &bar[s]);
+        for (int r = 0; r < RB; ++r) {
+            const int d1 = j1 - (i1b + r) + KB;
+            if (i1b + r < N1 && d1 >= 0 && d1 < B)
+                tma_2d(dst + zb + r * rb, &rmap, t0, ((q * N1 + i1b + r) * B + d1) * B, &bar[s]);
+        }
     };
     cx<R> acc[PI][PC];
 #pragma unroll
     for (int p = 0; p < PI; ++p)
 #pragma unroll
         for (int c = 0; c < PC; ++c) acc[p][c] = mk<R>((R)0, (R)0);
-    int q = 0, d1 = -1;
-    advance(q, d1);
-    if (tid == 0 && q < f.Q) issue(0, q, d1);
+    int q = 0, j1 = jlo - 1;
+    advance(q, j1);
+    if (tid == 0 && q < f.Q) issue(0, q, j1);
     for (int k = 0; q < f.Q; ++k) {
         const int s = k & 1;
-        int qn = q, dn = d1;
-        advance(qn, dn);
+        int qn = q, jn = j1;
+        advance(qn, jn);
         // the other buffer was released by the barrier at the end of the previous stage
-        if (tid == 0 && qn < f.Q) issue(s ^ 1, qn, dn);
+        if (tid == 0 && qn < f.Q) issue(s ^ 1, qn, jn);
         const unsigned parity = (unsigned)(k >> 1) & 1u;
         const bool ok = fbar_wait(&bar[s], parity, f.err);
         if (__syncthreads_or(ok ? 0 : 1)) {
@@ -339,54 +358,58 @@ __global__ void __launch_bounds__(128, 2) fact_radial_kernel(FactArgs f, cx<R> *
             if (tid == 0 && qn < f.Q) fbar_wait(&bar[s ^ 1], (unsigned)((k + 1) >> 1) & 1u, f.err);
             return;
         }
-        const cx<R> *zs = (const cx<R> *)(buf + (size_t)s * stage);
-        const R *rs = (const R *)(buf + (size_t)s * stage + zb);
-        cx<R> win[PI + B - 1][PC];
-        auto load_row = [&](int j, cx<R> (&out)[PC]) {
+        const int d1 = j1 - i1 + KB;
+        if (i1 < N1 && d1 >= 0 && d1 < B) {
+            const cx<R> *zs = (const cx<R> *)(buf + (size_t)s * stage);
+            const R *rs = (const R *)(buf + (size_t)s * stage + zb + rr * rb);
+            cx<R> win[PI + B - 1][PC];
+            auto load_row = [&](int j, cx<R> (&out)[PC]) {
 #pragma unroll
-            for (int h = 0; h < NV; ++h) {
-                const cx<R> *src = zs + (size_t)j * CA + (h * TCN + tc) * PCV;
+                for (int h = 0; h < NV; ++h) {
+                    const cx<R> *src = zs + (size_t)j * CA + (h * TCN + tc) * PCV;
+                    if constexpr (sizeof(R) == 4) {
+                        const float4 v = *reinterpret_cast<const float4 *>(src);
+                        out[h * PCV] = mk<R>(v.x, v.y);
+                        out[h * PCV + 1] = mk<R>(v.z, v.w);
+                    } else {
+                        out[h * PCV] = src[0];
+                    }
+                }
+            };
+#pragma unroll
+            for (int r = 0; r < PI - 1; ++r) load_row(ti * PI + r, win[r]);
+#pragma unroll
+            for (int d2 = 0; d2 < B; ++d2) {
+                load_row(ti * PI + d2 + PI - 1, win[d2 + PI - 1]);
+                R rv[PI];
+                const R *rp = rs + d2 * tw + ti * PI;
                 if constexpr (sizeof(R) == 4) {
-                    const float4 v = *reinterpret_cast<const float4 *>(src);
-                    out[h * PCV] = mk<R>(v.x, v.y);
-                    out[h * PCV + 1] = mk<R>(v.z, v.w);
+#pragma unroll
+                    for (int h = 0; h < PI / 4; ++h) {
+                        const float4 v = reinterpret_cast<const float4 *>(rp)[h];
+                        rv[4 * h] = v.x; rv[4 * h + 1] = v.y; rv[4 * h + 2] = v.z; rv[4 * h + 3] = v.w;
+                    }
                 } else {
-                    out[h * PCV] = src[0];
+#pragma unroll
+                    for (int h = 0; h < PI / 2; ++h) {
+                        const double2 v = reinterpret_cast<const double2 *>(rp)[h];
+                        rv[2 * h] = v.x; rv[2 * h + 1] = v.y;
+                    }
                 }
+#pragma unroll
+                for (int p = 0; p < PI; ++p)
+#pragma unroll
+                    for (int c = 0; c < PC; ++c) {
+                        acc[p][c].x = fma(rv[p], win[p + d2][c].x, acc[p][c].x);
+                        acc[p][c].y = fma(rv[p], win[p + d2][c].y, acc[p][c].y);
+                    }
             }
-        };
-#pragma unroll
-        for (int r = 0; r < PI - 1; ++r) load_row(ti * PI + r, win[r]);
-#pragma unroll
-        for (int d2 = 0; d2 < B; ++d2) {
-            load_row(ti * PI + d2 + PI - 1, win[d2 + PI - 1]);
-            R rv[PI];
-            const R *rp = rs + d2 * tw + ti * PI;
-            if constexpr (sizeof(R) == 4) {
-#pragma unroll
-                for (int h = 0; h < PI / 4; ++h) {
-                    const float4 v = reinterpret_cast<const float4 *>(rp)[h];
-                    rv[4 * h] = v.x; rv[4 * h + 1] = v.y; rv[4 * h + 2] = v.z; rv[4 * h + 3] = v.w;
-                }
-            } else {
-#pragma unroll
-                for (int h = 0; h < PI / 2; ++h) {
-                    const double2 v = reinterpret_cast<const double2 *>(rp)[h];
-                    rv[2 * h] = v.x; rv[2 * h + 1] = v.y;
-                }
-            }
-#pragma unroll
-            for (int p = 0; p < PI; ++p)
-#pragma unroll
-                for (int c = 0; c < PC; ++c) {
-                    acc[p][c].x = fma(rv[p], win[p + d2][c].x, acc[p][c].x);
-                    acc[p][c].y = fma(rv[p], win[p + d2][c].y, acc[p][c].y);
-                }
         }
         __syncthreads();  // buffer s is free for the stage after next
         q = qn;
-        d1 = dn;
+        j1 = jn;
     }
+    if (i1 >= N1) return;
     const long long NP = (long long)N1 * N2;
 #pragma unroll
     for (int h = 0; h < NV; ++h)
@@ -551,6 +574,7 @@ int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, c
     PG_TRY(pg_check_launch(op->ctx));
     dim3 g2((unsigned)fd.N1, (unsigned)fd.ntiles, (unsigned)fd.nct);
     const int nt = fd.tw / T::PI * T::TCN;
+    dim3 g2r((unsigned)((fd.N1 + RB - 1) / RB), (unsigned)fd.ntiles, (unsigned)fd.nct);
     if (op->kb != 6) return PG_ERR_STORAGE;
     if constexpr (sizeof(R) == 8) {
         if (fd.df) {
@@ -559,7 +583,7 @@ int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, c
             return pg_check_launch(op->ctx);
         }
     }
-    fact_radial_kernel<R, 6><<<g2, nt, fd.radial_smem, s>>>(fa, (cx<R> *)dst, fd.zmap, fd.rmap);
+    fact_radial_kernel<R, 6><<<g2r, RB * nt, fd.radial_smem, s>>>(fa, (cx<R> *)dst, fd.zmap, fd.rmap);
     op->ctx->launches++;
     return pg_check_launch(op->ctx);
 }
@@ -784,10 +808,10 @@ int pg_factored_finalize(pg_op *op)
     // shared memory: two barriers, then two stages of (Z box, coefficient box)
     if (fp64)
         f.radial_smem = 128 + 2 * (rad_round128<double>(rad_zbytes<double>(f.tw, kb)) +
-                                   rad_round128<double>(rad_rbytes<double>(f.tw, kb)));
+                                   RB * rad_round128<double>(rad_rbytes<double>(f.tw, kb)));
     else
         f.radial_smem = 128 + 2 * (rad_round128<float>(rad_zbytes<float>(f.tw, kb)) +
-                                   rad_round128<float>(rad_rbytes<float>(f.tw, kb)));
+                                   RB * rad_round128<float>(rad_rbytes<float>(f.tw, kb)));
     int dev = 0, optin = 0;
     PG_CUDA_TRY(cudaGetDevice(&dev));
     PG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
