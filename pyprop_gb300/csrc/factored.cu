@@ -110,17 +110,36 @@ __device__ __forceinline__ cx<R> ldg_cx(const cx<R> *p)
     }
 }
 
-// Z[q][p][a] = w_q s_slot(q) / inv_scale * sum_(col, c) c x[col][p] over the nonzero pairs of
-// (channel a, factor q). CTA = CB warps (scratch slots a0 .. a0+CB) x 32 MPT points (MPT
-// consecutive points per lane, 16-byte source loads). Each channel's pairs are grouped by
-// factor (segments, in factor order), so a factor's sum stays in registers; the factors are
-// taken MQC at a time through shared memory [MQC][MPT][32][CB + 1], and the CTA then writes
-// the CB slots of each point as one contiguous segment (lanes = 8 points x 4 slots),
-// skipping factors that no slot of the group has (their scratch stays at the zeros written
-// at upload).
+// Z[q][p][a] = w_q s_slot(q) / inv_scale * sum_e coef_e[q] x[col_e][p]. CTA = CB warps (scratch
+// slots a0 .. a0+CB) x 32 MPT points (MPT consecutive points per lane, 16-byte source loads).
+// The factors are taken MQC at a time with their sums in registers: each angular entry (a, col)
+// whose factor range meets the chunk loads its source points once and applies its MQC
+// coefficients (16-byte loads, the same for the whole warp). Factors are ordered so that an
+// entry's nonzero factors are contiguous (the repulsion's multipoles by parity), which keeps the
+// zero coefficients inside a chunk few. The chunk's sums go through shared memory
+// [MQC][MPT][32][CB + 1] so that the CTA writes the CB slots of each point as one contiguous
+// segment (lanes = 8 points x 4 slots); chunks that no slot of the group has are skipped (their
+// scratch stays at the zeros written at upload).
 template <typename R> struct MixTile;
 template <> struct MixTile<float> { static const int MPT = 4, MQC = 8; };
 template <> struct MixTile<double> { static const int MPT = 2, MQC = 8; };
+const int MIX_QC = 8;  // == MixTile<R>::MQC: the padding of the coefficient rows
+
+template <typename R>
+__device__ __forceinline__ void load_coef8(const R *p, R (&c)[8])
+{
+    if constexpr (sizeof(R) == 4) {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(p)), b = __ldg(reinterpret_cast<const float4 *>(p) + 1);
+        c[0] = a.x; c[1] = a.y; c[2] = a.z; c[3] = a.w; c[4] = b.x; c[5] = b.y; c[6] = b.z; c[7] = b.w;
+    } else {
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const double2 v = __ldg(reinterpret_cast<const double2 *>(p) + h);
+            c[2 * h] = v.x;
+            c[2 * h + 1] = v.y;
+        }
+    }
+}
 
 template <typename R>
 __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales scales,
@@ -129,11 +148,12 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
                                                           const double *__restrict__ inv_scale)
 {
     constexpr int MPT = MixTile<R>::MPT, MQC = MixTile<R>::MQC, TP = 32 * MPT;
+    static_assert(MQC == 8, "coefficient rows are padded to chunks of 8");
     extern __shared__ __align__(16) unsigned char mix_smem[];
-    cx<R> *acc = reinterpret_cast<cx<R> *>(mix_smem);  // [MQC][MPT][32][CB + 1]
-    cx<R> *ws = acc + (size_t)MQC * TP * (CB + 1);      // [Q] factor scales
+    cx<R> *acc_s = reinterpret_cast<cx<R> *>(mix_smem);  // [MQC][MPT][32][CB + 1]
+    cx<R> *ws = acc_s + (size_t)MQC * TP * (CB + 1);      // [Q] factor scales
     const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
-    const int Q = f.Q;
+    const int Q = f.Q, nch = f.Qp / MQC;
     const int a0 = blockIdx.y * CB;                      // first scratch slot of the group
     const int a = a0 + wrp < f.A ? f.perm[a0 + wrp] : -1;  // channel of this warp's slot
     const long long NP = (long long)f.N1 * f.N2;
@@ -145,13 +165,11 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
         const cxd s = scales_dev ? scales_dev[f.slot[q]] : scales.s[f.slot[q]];
         ws[q] = cvt<R>(sc * (f.w[q] * s));
     }
-    const int4 *__restrict__ seg = (const int4 *)f.col;  // factor, first pair, last+1 pair
-    const int *__restrict__ pcol = f.nzq;
-    const R *__restrict__ pc = (const R *)f.coef;
-    const unsigned char *gf = f.chunk + (size_t)blockIdx.y * Q;  // factors touched by this group
+    const int4 *__restrict__ meta = (const int4 *)f.col;  // col, first and last nonzero factor
+    const R *__restrict__ coef = (const R *)f.coef;        // [entry][Qp]
+    const unsigned char *gf = f.chunk + (size_t)blockIdx.y * nch;  // chunks touched by the group
     cx<R> *__restrict__ Z = (cx<R> *)f.Z;
-    int g = a >= 0 ? f.row_ptr[a] : 0;
-    const int g_end = a >= 0 ? f.row_ptr[a + 1] : 0;
+    const int e_begin = a >= 0 ? f.row_ptr[a] : 0, e_end = a >= 0 ? f.row_ptr[a + 1] : 0;
     auto load_x = [&](int col, cx<R> (&v)[MPT]) {
         const cx<R> *xr = x + (size_t)col * NP + p0;
         if (vec && p0 + MPT <= NP) {
@@ -174,62 +192,43 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
             for (int u = 0; u < MPT; ++u) v[u] = p0 + u < NP ? xr[u] : mk<R>((R)0, (R)0);
         }
     };
-    for (int qc = 0; qc < Q; qc += MQC) {
-        bool any = false;
-        for (int j = 0; j < MQC && qc + j < Q; ++j) any |= gf[qc + j] != 0;
-        if (!any) continue;  // CTA-uniform
+    __syncthreads();  // factor scales ready
+    for (int k = 0; k < nch; ++k) {
+        if (!gf[k]) continue;  // CTA-uniform
+        const int q0 = k * MQC;
+        cx<R> acc[MQC][MPT];
+#pragma unroll
         for (int j = 0; j < MQC; ++j)
 #pragma unroll
-            for (int u = 0; u < MPT; ++u)
-                acc[(((size_t)j * MPT + u) * 32 + lane) * (CB + 1) + wrp] = mk<R>((R)0, (R)0);
-        for (; g < g_end; ++g) {
-            const int4 sg = seg[g];
-            if (sg.x >= qc + MQC) break;  // segments are in factor order
-            constexpr int CH = 4;  // independent chains: four source loads in flight per lane
-            cx<R> sum[CH][MPT];
+            for (int u = 0; u < MPT; ++u) acc[j][u] = mk<R>((R)0, (R)0);
+        for (int e = e_begin; e < e_end; ++e) {
+            const int4 m = meta[e];
+            if (m.z < q0 || m.y >= q0 + MQC) continue;
+            cx<R> xv[MPT];
+            load_x(m.x, xv);
+            R c[MQC];
+            load_coef8<R>(coef + (size_t)e * f.Qp + q0, c);
 #pragma unroll
-            for (int h = 0; h < CH; ++h)
-#pragma unroll
-                for (int u = 0; u < MPT; ++u) sum[h][u] = mk<R>((R)0, (R)0);
-            int z = sg.y;
-            for (; z + CH - 1 < sg.z; z += CH) {
-                cx<R> xv[CH][MPT];
-#pragma unroll
-                for (int h = 0; h < CH; ++h) load_x(pcol[z + h], xv[h]);
-#pragma unroll
-                for (int h = 0; h < CH; ++h) {
-                    const R c = pc[z + h];
-#pragma unroll
-                    for (int u = 0; u < MPT; ++u) {
-                        sum[h][u].x = fma(c, xv[h][u].x, sum[h][u].x);
-                        sum[h][u].y = fma(c, xv[h][u].y, sum[h][u].y);
-                    }
-                }
-            }
-            for (; z < sg.z; ++z) {
-                cx<R> x0[MPT];
-                load_x(pcol[z], x0);
-                const R c = pc[z];
+            for (int j = 0; j < MQC; ++j)
 #pragma unroll
                 for (int u = 0; u < MPT; ++u) {
-                    sum[0][u].x = fma(c, x0[u].x, sum[0][u].x);
-                    sum[0][u].y = fma(c, x0[u].y, sum[0][u].y);
+                    acc[j][u].x = fma(c[j], xv[u].x, acc[j][u].x);
+                    acc[j][u].y = fma(c[j], xv[u].y, acc[j][u].y);
                 }
-            }
-#pragma unroll
-            for (int u = 0; u < MPT; ++u)
-                acc[(((size_t)(sg.x - qc) * MPT + u) * 32 + lane) * (CB + 1) + wrp] =
-                    (sum[0][u] + sum[1][u]) + (sum[2][u] + sum[3][u]);
         }
+#pragma unroll
+        for (int j = 0; j < MQC; ++j)
+#pragma unroll
+            for (int u = 0; u < MPT; ++u) acc_s[(((size_t)j * MPT + u) * 32 + lane) * (CB + 1) + wrp] = acc[j][u];
         __syncthreads();
         for (int t = threadIdx.x; t < MQC * TP * CB; t += 32 * CB) {
             const int r = t % CB, rest = t / CB;
             const int pl = rest % TP, j = rest / TP;
-            const int q = qc + j;
+            const int q = q0 + j;
             const long long pp = pbase + pl;
-            if (q >= Q || !gf[q] || pp >= NP) continue;
+            if (q >= Q || pp >= NP) continue;
             const int u = pl % MPT, ln = pl / MPT;
-            const cx<R> v = ws[q] * acc[(((size_t)j * MPT + u) * 32 + ln) * (CB + 1) + r];
+            const cx<R> v = ws[q] * acc_s[(((size_t)j * MPT + u) * 32 + ln) * (CB + 1) + r];
             const size_t zi = ((size_t)q * NP + pp) * f.Ap + a0 + r;
             if constexpr (sizeof(R) == 8) {
                 if (f.df) {  // the 16 bytes hold (re_hi, re_lo, im_hi, im_lo)
@@ -682,43 +681,52 @@ int pg_factored_finalize(pg_op *op)
     const int tmax = 16 * PI;
     f.ntiles = (N2 + tmax - 1) / tmax;
     f.tw = ((N2 + f.ntiles - 1) / f.ntiles + PI - 1) / PI * PI;
-    // angular rows: coefficient vector over the factors per (row, col); each entry keeps the
-    // list of its nonzero (factor, coefficient) pairs
+    // angular rows: coefficient vector over the factors per (row, col), padded to chunks of
+    // MIX_QC factors; each entry records its first and last nonzero factor
+    f.Qp = (Q + MIX_QC - 1) / MIX_QC * MIX_QC;
+    const int nch = f.Qp / MIX_QC;
     std::vector<std::map<int, std::vector<double>>> rows(A);
     for (int q = 0; q < Q; ++q) {
         const HostFactor &h = op->factors[q];
         for (size_t e = 0; e < h.row.size(); ++e) {
             std::vector<double> &v = rows[h.row[e]][h.col[e]];
-            if (v.empty()) v.assign(Q, 0.0);
+            if (v.empty()) v.assign(f.Qp, 0.0);
             v[q] += h.coef[e];
         }
     }
-    std::vector<int> row_ptr(A + 1, 0), col, nzq;
+    std::vector<int> row_ptr(A + 1, 0), col;
     std::vector<double> coef;
     const int ngroups = f.Ap / CB;
-    std::vector<unsigned char> chunk((size_t)ngroups * Q, 0), bflag((size_t)Q * f.nct, 0);
+    std::vector<unsigned char> bflag((size_t)Q * f.nct, 0);
     std::vector<long long> rows_of_q(Q, 0);
     std::vector<std::vector<unsigned char>> has(A, std::vector<unsigned char>(Q, 0));
+    std::vector<std::vector<unsigned char>> row_chunks(A, std::vector<unsigned char>(nch, 0));
+    double mix_terms = 0;
     for (int a = 0; a < A; ++a) {
         std::vector<unsigned char> &row_has = has[a];
-        // pairs of this channel grouped by factor: one segment (q, first, last+1) per factor
-        for (int q = 0; q < Q; ++q) {
-            const int first = (int)nzq.size();
-            for (const auto &kv : rows[a])
+        for (const auto &kv : rows[a]) {
+            int lo = f.Qp, hi = -1;
+            for (int q = 0; q < Q; ++q)
                 if (kv.second[q] != 0.0) {
-                    nzq.push_back(kv.first);  // column
-                    coef.push_back(kv.second[q]);
+                    lo = std::min(lo, q);
+                    hi = std::max(hi, q);
+                    row_has[q] = 1;
+                    mix_terms += 1;
                 }
-            if ((int)nzq.size() == first) continue;
-            row_has[q] = 1;
-            col.push_back(q);
-            col.push_back(first);
-            col.push_back((int)nzq.size());
+            if (hi < 0) continue;  // all coefficients zero
+            col.push_back(kv.first);  // entry metadata: col, first and last nonzero factor, 0
+            col.push_back(lo);
+            col.push_back(hi);
             col.push_back(0);
+            coef.insert(coef.end(), kv.second.begin(), kv.second.end());
+            for (int k = lo / MIX_QC; k <= hi / MIX_QC; ++k) row_chunks[a][k] = 1;
         }
         row_ptr[a + 1] = (int)(col.size() / 4);
         for (int q = 0; q < Q; ++q) rows_of_q[q] += row_has[q];
     }
+    f.nE = (int)(col.size() / 4);
+    std::vector<int> nzq;  // unused by the chunked mix
+    std::vector<unsigned char> chunk((size_t)ngroups * nch, 0);
     // scratch slots: channels sorted by the set of factors they have, so that the radial
     // kernel's channel tiles skip more (factor, tile) stages; slot s holds channel perm[s]
     std::vector<int> perm(A);
@@ -730,15 +738,13 @@ int pg_factored_finalize(pg_op *op)
         if (cnt[x] != cnt[y]) return cnt[x] < cnt[y];
         return has[x] < has[y];
     });
-    for (int sl = 0; sl < A; ++sl)
+    for (int sl = 0; sl < A; ++sl) {
         for (int q = 0; q < Q; ++q)
-            if (has[perm[sl]][q]) {
-                bflag[(size_t)q * f.nct + sl / CA] = 1;
-                chunk[(size_t)(sl / CB) * Q + q] = 1;
-            }
-    const double mix_terms = (double)nzq.size();
-    f.nE = 0;
-    for (int a = 0; a < A; ++a) f.nE += (int)rows[a].size();
+            if (has[perm[sl]][q]) bflag[(size_t)q * f.nct + sl / CA] = 1;
+        for (int k = 0; k < nch; ++k)
+            if (row_chunks[perm[sl]][k]) chunk[(size_t)(sl / CB) * nch + k] = 1;
+    }
+
     // radial factors, last rank padded to N2p; points outside the grid are dropped
     std::vector<double> rad((size_t)Q * N1 * b * b * f.N2p, 0.0);
     double pts = 0;  // in-grid stencil points of one factor

@@ -280,7 +280,9 @@ class CustomPotentialEvaluationR12(CoupledPotentialBase):
                 c = r12_angular_factor(left, right, l3)
                 if c != 0.0:
                     table.setdefault(l3, np.zeros(len(lr)))[p] = c
-        return [(frac ** l3 / rmax, table[l3]) for l3 in sorted(table)]
+        # even multipoles first, then odd: an angular pair's nonzero multipoles share a parity,
+        # so each pair's factors are contiguous in this order
+        return [(frac ** l3 / rmax, table[l3]) for l3 in sorted(table, key=lambda l: (l % 2, l))]
 
 
 class CustomPotential_LaserLength(CoupledPotentialBase):
