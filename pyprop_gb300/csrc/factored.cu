@@ -111,7 +111,8 @@ __device__ __forceinline__ cx<R> ldg_cx(const cx<R> *p)
 }
 
 // Z[q][p][a] = w_q s_slot(q) / inv_scale * sum_e coef_e[q] x[col_e][p]. CTA = CB warps (scratch
-// slots a0 .. a0+CB) x 32 MPT points (MPT consecutive points per lane, 16-byte source loads).
+// slots a0 .. a0+CB, blockIdx.x) x 32 MPT points (blockIdx.y; MPT consecutive points per lane,
+// 16-byte source loads).
 // The factors are taken MQC at a time with their sums in registers: each angular entry (a, col)
 // whose factor range meets the chunk loads its source points once and applies its MQC
 // coefficients (16-byte loads, the same for the whole warp). Factors are ordered so that an
@@ -154,10 +155,10 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
     cx<R> *ws = acc_s + (size_t)MQC * TP * (CB + 1);      // [Q] factor scales
     const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
     const int Q = f.Q, nch = f.Qp / MQC;
-    const int a0 = blockIdx.y * CB;                      // first scratch slot of the group
+    const int a0 = blockIdx.x * CB;                      // first scratch slot of the group
     const int a = a0 + wrp < f.A ? f.perm[a0 + wrp] : -1;  // channel of this warp's slot
     const long long NP = (long long)f.N1 * f.N2;
-    const long long pbase = (long long)blockIdx.x * TP;
+    const long long pbase = (long long)blockIdx.y * TP;
     const long long p0 = pbase + (long long)lane * MPT;  // this lane's first point
     const bool vec = (NP % 2) == 0;                      // rows start 16-byte aligned
     const double sc = inv_scale ? 1.0 / *inv_scale : 1.0;
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
     }
     const int4 *__restrict__ meta = (const int4 *)f.col;  // col, first and last nonzero factor
     const R *__restrict__ coef = (const R *)f.coef;        // [entry][Qp]
-    const unsigned char *gf = f.chunk + (size_t)blockIdx.y * nch;  // chunks touched by the group
+    const unsigned char *gf = f.chunk + (size_t)blockIdx.x * nch;  // chunks touched by the group
     cx<R> *__restrict__ Z = (cx<R> *)f.Z;
     const int e_begin = a >= 0 ? f.row_ptr[a] : 0, e_end = a >= 0 ? f.row_ptr[a + 1] : 0;
     auto load_x = [&](int col, cx<R> (&v)[MPT]) {
@@ -566,7 +567,8 @@ int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, c
     cudaStream_t s = op->ctx->stream;
     const long long NP = (long long)fd.N1 * fd.N2;
     const int TP = 32 * MixTile<R>::MPT;
-    dim3 g1((unsigned)((NP + TP - 1) / TP), (unsigned)((fd.A + CB - 1) / CB));
+    // channel groups fastest: the CTAs running together share a point tile of the source (L2)
+    dim3 g1((unsigned)((fd.A + CB - 1) / CB), (unsigned)((NP + TP - 1) / TP));
     fact_mix_kernel<R><<<g1, 32 * CB, mix_smem_bytes<R>(fd.Q), s>>>(fa, scales, scales_dev, (const cx<R> *)src,
                                                                      inv_scale);
     op->ctx->launches++;
@@ -618,6 +620,7 @@ extern "C" int pg_op_add_factored(pg_op *op, int nfactors, const double *radial,
     if (op->kb != 6) return PG_ERR_STORAGE;  // the radial stencil is compiled for 13 diagonals
     const int A = op->shape[0], N1 = op->shape[1], N2 = op->shape[2], b = op->b;
     if (N1 <= 2 * op->kb) return PG_ERR_SHAPE;
+    if ((long long)N1 * N2 > 65535LL * 64) return PG_ERR_SHAPE;  // point tiles of the mix kernel in grid y
     if (op->factors.size() + nfactors > (size_t)4096) return PG_ERR_ARG;
     for (int q = 0; q < nfactors; ++q)
         if (slots[q] < 0 || slots[q] >= PG_MAX_SLOTS) return PG_ERR_ARG;
