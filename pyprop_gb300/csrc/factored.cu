@@ -41,7 +41,6 @@ struct FactArgs {
     int df;  // FP64 operator with FP32-pair (double-float) scratch and radial factors
     const int *row_ptr, *col, *slot, *nzq, *perm;
     const void *coef;
-    const float2 *coef_df;  // df: the coefficients as (hi, lo) pairs
     const unsigned char *chunk, *bflag;
     const cxd *w;
     void *Z;
@@ -55,7 +54,7 @@ FactArgs args_of(const FactDev &f, int *err)
     a.tw = f.tw;
     a.df = f.df;
     a.row_ptr = f.row_ptr; a.col = f.col; a.slot = f.slot; a.nzq = f.nzq; a.perm = f.perm;
-    a.coef = f.coef; a.coef_df = (const float2 *)f.coef_df; a.chunk = f.chunk; a.bflag = f.bflag; a.w = f.w; a.Z = f.Z; a.err = err;
+    a.coef = f.coef; a.chunk = f.chunk; a.bflag = f.bflag; a.w = f.w; a.Z = f.Z; a.err = err;
     return a;
 }
 
@@ -558,88 +557,6 @@ __global__ void __launch_bounds__(128, 2) fact_radial_df_kernel(FactArgs f, cxd 
     }
 }
 
-// The mix of an FP64 operator in double-float arithmetic (df): the structure of
-// fact_mix_kernel<double>, the source split into (hi, lo) floats as it is loaded, coefficients
-// stored as (hi, lo) pairs, sums by df_fma; the scratch written as (re_hi, re_lo, im_hi, im_lo).
-__global__ void __launch_bounds__(32 * CB) fact_mix_df_kernel(FactArgs f, pg_scales scales,
-                                                             const cxd *__restrict__ scales_dev,
-                                                             const cxd *__restrict__ x,
-                                                             const double *__restrict__ inv_scale)
-{
-    constexpr int MPT = MixTile<double>::MPT, MQC = MixTile<double>::MQC, TP = 32 * MPT;
-    extern __shared__ __align__(16) unsigned char mix_smem[];
-    cxd *acc_s = reinterpret_cast<cxd *>(mix_smem);  // [MQC][MPT][32][CB + 1]
-    cxd *ws = acc_s + (size_t)MQC * TP * (CB + 1);   // [Q]
-    const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
-    const int Q = f.Q, nch = f.Qp / MQC;
-    const int a0 = blockIdx.x * CB;
-    const int a = a0 + wrp < f.A ? f.perm[a0 + wrp] : -1;
-    const long long NP = (long long)f.N1 * f.N2;
-    const long long pbase = (long long)blockIdx.y * TP;
-    const long long p0 = pbase + (long long)lane * MPT;
-    const double sc = inv_scale ? 1.0 / *inv_scale : 1.0;
-    for (int q = threadIdx.x; q < Q; q += 32 * CB) {
-        const cxd s = scales_dev ? scales_dev[f.slot[q]] : scales.s[f.slot[q]];
-        ws[q] = sc * (f.w[q] * s);
-    }
-    const int4 *__restrict__ meta = (const int4 *)f.col;
-    const unsigned char *gf = f.chunk + (size_t)blockIdx.x * nch;
-    const int e_begin = a >= 0 ? f.row_ptr[a] : 0, e_end = a >= 0 ? f.row_ptr[a + 1] : 0;
-    __syncthreads();
-    for (int k = 0; k < nch; ++k) {
-        if (!gf[k]) continue;  // CTA-uniform
-        const int q0 = k * MQC;
-        float ah[MQC][MPT][2], al[MQC][MPT][2];
-#pragma unroll
-        for (int j = 0; j < MQC; ++j)
-#pragma unroll
-            for (int u = 0; u < MPT; ++u) ah[j][u][0] = ah[j][u][1] = al[j][u][0] = al[j][u][1] = 0.f;
-        for (int e = e_begin; e < e_end; ++e) {
-            const int4 m = meta[e];
-            if (m.z < q0 || m.y >= q0 + MQC) continue;
-            float xh[MPT][2], xl[MPT][2];
-#pragma unroll
-            for (int u = 0; u < MPT; ++u) {
-                const cxd v = p0 + u < NP ? x[(size_t)m.x * NP + p0 + u] : mk<double>(0.0, 0.0);
-                xh[u][0] = (float)v.x;
-                xl[u][0] = (float)(v.x - (double)xh[u][0]);
-                xh[u][1] = (float)v.y;
-                xl[u][1] = (float)(v.y - (double)xh[u][1]);
-            }
-            const float2 *cp = f.coef_df + (size_t)e * f.Qp + q0;
-#pragma unroll
-            for (int j = 0; j < MQC; ++j) {
-                const float2 c = cp[j];
-#pragma unroll
-                for (int u = 0; u < MPT; ++u) {
-                    df_fma(ah[j][u][0], al[j][u][0], c.x, c.y, xh[u][0], xl[u][0]);
-                    df_fma(ah[j][u][1], al[j][u][1], c.x, c.y, xh[u][1], xl[u][1]);
-                }
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < MQC; ++j)
-#pragma unroll
-            for (int u = 0; u < MPT; ++u)
-                acc_s[(((size_t)j * MPT + u) * 32 + lane) * (CB + 1) + wrp] =
-                    mk<double>((double)ah[j][u][0] + (double)al[j][u][0], (double)ah[j][u][1] + (double)al[j][u][1]);
-        __syncthreads();
-        for (int t = threadIdx.x; t < MQC * TP * CB; t += 32 * CB) {
-            const int r = t % CB, rest = t / CB;
-            const int pl = rest % TP, j = rest / TP;
-            const int q = q0 + j;
-            const long long pp = pbase + pl;
-            if (q >= Q || pp >= NP) continue;
-            const int u = pl % MPT, ln = pl / MPT;
-            const cxd v = ws[q] * acc_s[(((size_t)j * MPT + u) * 32 + ln) * (CB + 1) + r];
-            const float rh = (float)v.x, ih = (float)v.y;
-            reinterpret_cast<float4 *>(f.Z)[((size_t)q * NP + pp) * f.Ap + a0 + r] =
-                make_float4(rh, (float)(v.x - (double)rh), ih, (float)(v.y - (double)ih));
-        }
-        __syncthreads();
-    }
-}
-
 template <typename R>
 int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, const void *src, void *dst,
                     const double *inv_scale)
@@ -652,12 +569,8 @@ int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, c
     const int TP = 32 * MixTile<R>::MPT;
     // channel groups fastest: the CTAs running together share a point tile of the source (L2)
     dim3 g1((unsigned)((fd.A + CB - 1) / CB), (unsigned)((NP + TP - 1) / TP));
-    if (sizeof(R) == 8 && fd.df)
-        fact_mix_df_kernel<<<g1, 32 * CB, mix_smem_bytes<double>(fd.Q), s>>>(fa, scales, scales_dev, (const cxd *)src,
-                                                                             inv_scale);
-    else
-        fact_mix_kernel<R><<<g1, 32 * CB, mix_smem_bytes<R>(fd.Q), s>>>(fa, scales, scales_dev, (const cx<R> *)src,
-                                                                         inv_scale);
+    fact_mix_kernel<R><<<g1, 32 * CB, mix_smem_bytes<R>(fd.Q), s>>>(fa, scales, scales_dev, (const cx<R> *)src,
+                                                                     inv_scale);
     op->ctx->launches++;
     PG_TRY(pg_check_launch(op->ctx));
     dim3 g2((unsigned)fd.N1, (unsigned)fd.ntiles, (unsigned)fd.nct);
@@ -690,7 +603,7 @@ void pg_factored_free(pg_op *op)
 {
     FactDev &f = op->fact;
     cudaFree(f.row_ptr); cudaFree(f.col); cudaFree(f.nzq); cudaFree(f.slot); cudaFree(f.perm);
-    cudaFree(f.coef); cudaFree(f.coef_df); cudaFree(f.chunk); cudaFree(f.bflag); cudaFree(f.radial); cudaFree(f.w); cudaFree(f.Z);
+    cudaFree(f.coef); cudaFree(f.chunk); cudaFree(f.bflag); cudaFree(f.radial); cudaFree(f.w); cudaFree(f.Z);
     f = FactDev();
 }
 
@@ -885,17 +798,6 @@ int pg_factored_finalize(pg_op *op)
     PG_CUDA_TRY(cudaMemcpy(f.w, w.data(), sizeof(cxd) * Q, cudaMemcpyHostToDevice));
     PG_TRY(fp64 ? upload_real<double>(&f.coef, coef) : upload_real<float>(&f.coef, coef));
     f.df = fp64 && op->fp64_emulation;
-    if (f.df) {  // the mix's coefficients as (hi, lo) float pairs
-        std::vector<float> cpairs(2 * coef.size());
-        for (size_t t = 0; t < coef.size(); ++t) {
-            const float hi = (float)coef[t];
-            cpairs[2 * t] = hi;
-            cpairs[2 * t + 1] = (float)(coef[t] - (double)hi);
-        }
-        PG_CUDA_TRY(cudaMalloc(&f.coef_df, sizeof(float) * std::max<size_t>(2, cpairs.size())));
-        if (!cpairs.empty())
-            PG_CUDA_TRY(cudaMemcpy(f.coef_df, cpairs.data(), sizeof(float) * cpairs.size(), cudaMemcpyHostToDevice));
-    }
     if (f.df) {  // (hi, lo) float pairs in the 8 bytes of each coefficient
         std::vector<float> pairs(2 * rad.size());
         for (size_t t = 0; t < rad.size(); ++t) {
@@ -924,10 +826,8 @@ int pg_factored_finalize(pg_op *op)
     PG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     if (f.radial_smem > (size_t)optin) return PG_ERR_SHAPE;
     if ((fp64 ? mix_smem_bytes<double>(Q) : mix_smem_bytes<float>(Q)) > (size_t)optin) return PG_ERR_SHAPE;
-    if (fp64) {
+    if (fp64)
         PG_CUDA_TRY(cudaFuncSetAttribute(fact_mix_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-        PG_CUDA_TRY(cudaFuncSetAttribute(fact_mix_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    }
     else
         PG_CUDA_TRY(cudaFuncSetAttribute(fact_mix_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     if (fp64) {

@@ -152,8 +152,7 @@ struct FactDev {
     int *nzq = nullptr;               // [pairs] input channel of each nonzero (channel, factor) pair
     int *slot = nullptr;              // [Q]
     int *perm = nullptr;              // [A] channel held by each scratch slot
-    void *coef = nullptr;             // [entries][Qp] coefficients (operator precision)
-    void *coef_df = nullptr;          // df: the same as (hi, lo) float pairs
+    void *coef = nullptr;             // [pairs] its coefficient (operator precision)
     unsigned char *chunk = nullptr;   // [Ap / 4][Q] factors touched by each group of 4 channels
     unsigned char *bflag = nullptr;   // [Q][nct] channel tiles with a nonzero row
     void *radial = nullptr;           // [Q][N1][b][b][N2p] real
