@@ -123,18 +123,22 @@ __device__ __forceinline__ cx<R> ldg_cx(const cx<R> *p)
 // scratch stays at the zeros written at upload).
 template <typename R> struct MixTile;
 template <> struct MixTile<float> { static const int MPT = 4, MQC = 8; };
-template <> struct MixTile<double> { static const int MPT = 2, MQC = 8; };
+template <> struct MixTile<double> { static const int MPT = 2, MQC = 4; };  // FP64 FMAs: fewer zero factors
 const int MIX_QC = 8;  // == MixTile<R>::MQC: the padding of the coefficient rows
 
-template <typename R>
-__device__ __forceinline__ void load_coef8(const R *p, R (&c)[8])
+// M consecutive coefficients from a 16-byte aligned row (M a multiple of 16 bytes / sizeof(R))
+template <typename R, int M>
+__device__ __forceinline__ void load_coefs_row(const R *p, R (&c)[M])
 {
     if constexpr (sizeof(R) == 4) {
-        const float4 a = __ldg(reinterpret_cast<const float4 *>(p)), b = __ldg(reinterpret_cast<const float4 *>(p) + 1);
-        c[0] = a.x; c[1] = a.y; c[2] = a.z; c[3] = a.w; c[4] = b.x; c[5] = b.y; c[6] = b.z; c[7] = b.w;
+#pragma unroll
+        for (int h = 0; h < M / 4; ++h) {
+            const float4 v = __ldg(reinterpret_cast<const float4 *>(p) + h);
+            c[4 * h] = v.x; c[4 * h + 1] = v.y; c[4 * h + 2] = v.z; c[4 * h + 3] = v.w;
+        }
     } else {
 #pragma unroll
-        for (int h = 0; h < 4; ++h) {
+        for (int h = 0; h < M / 2; ++h) {
             const double2 v = __ldg(reinterpret_cast<const double2 *>(p) + h);
             c[2 * h] = v.x;
             c[2 * h + 1] = v.y;
@@ -149,12 +153,12 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
                                                           const double *__restrict__ inv_scale)
 {
     constexpr int MPT = MixTile<R>::MPT, MQC = MixTile<R>::MQC, TP = 32 * MPT;
-    static_assert(MQC == 8, "coefficient rows are padded to chunks of 8");
+    static_assert(MIX_QC % MQC == 0, "chunks divide the coefficient padding");
     extern __shared__ __align__(16) unsigned char mix_smem[];
     cx<R> *acc_s = reinterpret_cast<cx<R> *>(mix_smem);  // [MQC][MPT][32][CB + 1]
     cx<R> *ws = acc_s + (size_t)MQC * TP * (CB + 1);      // [Q] factor scales
     const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
-    const int Q = f.Q, nch = f.Qp / MQC;
+    const int Q = f.Q, nch = f.Qp / MQC, nflag = f.Qp / MIX_QC;
     const int a0 = blockIdx.x * CB;                      // first scratch slot of the group
     const int a = a0 + wrp < f.A ? f.perm[a0 + wrp] : -1;  // channel of this warp's slot
     const long long NP = (long long)f.N1 * f.N2;
@@ -168,7 +172,7 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
     }
     const int4 *__restrict__ meta = (const int4 *)f.col;  // col, first and last nonzero factor
     const R *__restrict__ coef = (const R *)f.coef;        // [entry][Qp]
-    const unsigned char *gf = f.chunk + (size_t)blockIdx.x * nch;  // chunks touched by the group
+    const unsigned char *gf = f.chunk + (size_t)blockIdx.x * nflag;  // chunks of 8 touched by the group
     cx<R> *__restrict__ Z = (cx<R> *)f.Z;
     const int e_begin = a >= 0 ? f.row_ptr[a] : 0, e_end = a >= 0 ? f.row_ptr[a + 1] : 0;
     auto load_x = [&](int col, cx<R> (&v)[MPT]) {
@@ -195,8 +199,8 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
     };
     __syncthreads();  // factor scales ready
     for (int k = 0; k < nch; ++k) {
-        if (!gf[k]) continue;  // CTA-uniform
         const int q0 = k * MQC;
+        if (!gf[q0 / MIX_QC]) continue;  // CTA-uniform
         cx<R> acc[MQC][MPT];
 #pragma unroll
         for (int j = 0; j < MQC; ++j)
@@ -208,7 +212,7 @@ __global__ void __launch_bounds__(32 * CB) fact_mix_kernel(FactArgs f, pg_scales
             cx<R> xv[MPT];
             load_x(m.x, xv);
             R c[MQC];
-            load_coef8<R>(coef + (size_t)e * f.Qp + q0, c);
+            load_coefs_row<R, MQC>(coef + (size_t)e * f.Qp + q0, c);
 #pragma unroll
             for (int j = 0; j < MQC; ++j)
 #pragma unroll
