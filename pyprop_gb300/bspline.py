@@ -323,10 +323,13 @@ class BSplineBasis:
         if out2.ndim == 1:
             np.add.at(out2, flat, vals)
         else:
+            # one scatter for all leading rows: sum the contributions per target slot with a
+            # sparse (contributions x slots) matrix (the same sums as np.add.at row by row)
+            import scipy.sparse as sp
             lead = out2.reshape(-1, out2.shape[-1])
             v2 = vals.reshape(-1, vals.shape[-1])
-            for r in range(lead.shape[0]):
-                np.add.at(lead[r], flat, v2[r])
+            P = sp.csr_matrix((np.ones(len(flat)), (np.arange(len(flat)), flat)), shape=(len(flat), lead.shape[1]))
+            lead += np.asarray((P.T @ v2.T).T)
         return out
 
     def overlap_band(self):

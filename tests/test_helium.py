@@ -164,3 +164,16 @@ def test_fast_diagonalization_inverts_the_separable_channel_block():
     D = 1.0 / (cS + cH * (w0[:, None] + w1[None, :]))
     Minv = np.kron(v0, v1) @ np.diag(D.ravel()) @ np.kron(v0, v1).T
     assert np.abs(Minv @ M - np.eye(M.shape[0])).max() < 1e-10
+
+
+def test_batched_band_elements_match_row_by_row():
+    """The projection of many grid functions at once (the radial factors of two-electron terms)
+    equals the projection of each row alone."""
+    from tests.helpers import hydrogen_problem
+    bs = hydrogen_problem(lmax=1, nbsplines=30, rmax=20.0).psi.GetRepresentation().radial.BSplineObject
+    rng = np.random.default_rng(0)
+    f = rng.standard_normal((5, 3, len(bs.grid)))
+    for d in (0, 2):
+        a = bs.band_elements(f, d)
+        b = np.stack([np.stack([bs.band_elements(f[i, j], d) for j in range(3)]) for i in range(5)])
+        assert np.array_equal(a, b)
