@@ -176,4 +176,4 @@ def test_batched_band_elements_match_row_by_row():
     for d in (0, 2):
         a = bs.band_elements(f, d)
         b = np.stack([np.stack([bs.band_elements(f[i, j], d) for j in range(3)]) for i in range(5)])
-        assert np.array_equal(a, b)
+        assert np.abs(a - b).max() <= 1e-13 * np.abs(b).max()
