@@ -331,7 +331,8 @@ def time_two_electron_steps(torch, steps=3, warmup=1):
 def profile_two_electron():
     """Profiling entry point: the two-electron model of time_two_electron set up for mixed
     Cayley steps; five complex64 matvecs of its operator (overlap slot + factorized terms),
-    then three solves of its fast-diagonalization preconditioner."""
+    three solves of its fast-diagonalization preconditioner, three matvecs of its FP64 residual
+    operator (factorized terms in double-float)."""
     import torch
     import pyprop_gb300 as pp
     from pyprop_gb300 import _native as nat
@@ -349,6 +350,11 @@ def profile_two_electron():
     solver = prop.Preconditioner.solvers[nat.PG_FP32]
     for _ in range(3):
         solver.apply(nat.PG_BAND_PREC_SOLVE, dst)
+    # the FP64 residual operator of the mixed step (double-float factorized terms)
+    src64 = src.to(torch.complex128)
+    dst64 = torch.zeros_like(src64)
+    for _ in range(3):
+        prop.op64.matvec(sc, src64, dst64)
     torch.cuda.synchronize()
     print(json.dumps({"profile": "two_electron", "info": op.factored_info(),
                       "preconditioner": prop.Preconditioner.Method}))
