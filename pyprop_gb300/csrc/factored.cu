@@ -42,6 +42,9 @@ struct FactArgs {
     const int *row_ptr, *col, *slot, *nzq, *perm;
     const void *coef;
     const unsigned char *chunk, *bflag;
+    const int *seg_ptr, *seg, *pcol;  // segments of the exact-pair mix (FP64 operators)
+    const void *pcoef;
+    const unsigned char *seg_gq;
     const cxd *w;
     void *Z;
     int *err;
@@ -54,7 +57,8 @@ FactArgs args_of(const FactDev &f, int *err)
     a.tw = f.tw;
     a.df = f.df;
     a.row_ptr = f.row_ptr; a.col = f.col; a.slot = f.slot; a.nzq = f.nzq; a.perm = f.perm;
-    a.coef = f.coef; a.chunk = f.chunk; a.bflag = f.bflag; a.w = f.w; a.Z = f.Z; a.err = err;
+    a.coef = f.coef; a.chunk = f.chunk;
+    a.seg_ptr = f.seg_ptr; a.seg = f.seg; a.pcol = f.pcol; a.pcoef = f.pcoef; a.seg_gq = f.seg_gq; a.bflag = f.bflag; a.w = f.w; a.Z = f.Z; a.err = err;
     return a;
 }
 
@@ -123,7 +127,7 @@ __device__ __forceinline__ cx<R> ldg_cx(const cx<R> *p)
 // scratch stays at the zeros written at upload).
 template <typename R> struct MixTile;
 template <> struct MixTile<float> { static const int MPT = 4, MQC = 8; };
-template <> struct MixTile<double> { static const int MPT = 2, MQC = 4; };  // FP64 FMAs: fewer zero factors
+template <> struct MixTile<double> { static const int MPT = 2, MQC = 8; };
 const int MIX_QC = 8;  // == MixTile<R>::MQC: the padding of the coefficient rows
 
 // M consecutive coefficients from a 16-byte aligned row (M a multiple of 16 bytes / sizeof(R))
@@ -253,6 +257,145 @@ size_t mix_smem_bytes(int Q)
 {
     return ((size_t)MixTile<R>::MQC * 32 * MixTile<R>::MPT * (CB + 1) + Q) * sizeof(cx<R>);
 }
+
+// The mix over the exact nonzero (channel, factor) pairs, for the FP64 operator (whose FMAs are
+// the bottleneck there, so the zero coefficients inside the chunks of fact_mix_kernel cost more
+// than the repeated source loads): each channel's pairs grouped by factor (segments, in factor
+// order), a factor's sum in registers (four independent load chains), the factors through
+// shared memory [MQC][MPT][32][CB + 1] MQC at a time, the CB slots of each point written as one
+// segment (lanes = 8 points x 4 slots); factors no slot of the group has are skipped.
+template <typename R> struct SegTile;
+template <> struct SegTile<float> { static const int MPT = 4, MQC = 8; };
+template <> struct SegTile<double> { static const int MPT = 2, MQC = 8; };
+
+template <typename R>
+__global__ void __launch_bounds__(32 * CB) fact_mix_seg_kernel(FactArgs f, pg_scales scales,
+                                                          const cxd *__restrict__ scales_dev,
+                                                          const cx<R> *__restrict__ x,
+                                                          const double *__restrict__ inv_scale)
+{
+    constexpr int MPT = SegTile<R>::MPT, MQC = SegTile<R>::MQC, TP = 32 * MPT;
+    extern __shared__ __align__(16) unsigned char mix_smem[];
+    cx<R> *acc = reinterpret_cast<cx<R> *>(mix_smem);  // [MQC][MPT][32][CB + 1]
+    cx<R> *ws = acc + (size_t)MQC * TP * (CB + 1);      // [Q] factor scales
+    const int lane = threadIdx.x & 31, wrp = threadIdx.x >> 5;
+    const int Q = f.Q;
+    const int a0 = blockIdx.x * CB;                      // first scratch slot of the group
+    const int a = a0 + wrp < f.A ? f.perm[a0 + wrp] : -1;  // channel of this warp's slot
+    const long long NP = (long long)f.N1 * f.N2;
+    const long long pbase = (long long)blockIdx.y * TP;
+    const long long p0 = pbase + (long long)lane * MPT;  // this lane's first point
+    const bool vec = (NP % 2) == 0;                      // rows start 16-byte aligned
+    const double sc = inv_scale ? 1.0 / *inv_scale : 1.0;
+    for (int q = threadIdx.x; q < Q; q += 32 * CB) {
+        const cxd s = scales_dev ? scales_dev[f.slot[q]] : scales.s[f.slot[q]];
+        ws[q] = cvt<R>(sc * (f.w[q] * s));
+    }
+    const int4 *__restrict__ seg = (const int4 *)f.seg;  // factor, first pair, last+1 pair
+    const int *__restrict__ pcol = f.pcol;
+    const R *__restrict__ pc = (const R *)f.pcoef;
+    const unsigned char *gf = f.seg_gq + (size_t)blockIdx.x * Q;  // factors touched by this group
+    cx<R> *__restrict__ Z = (cx<R> *)f.Z;
+    int g = a >= 0 ? f.seg_ptr[a] : 0;
+    const int g_end = a >= 0 ? f.seg_ptr[a + 1] : 0;
+    auto load_x = [&](int col, cx<R> (&v)[MPT]) {
+        const cx<R> *xr = x + (size_t)col * NP + p0;
+        if (vec && p0 + MPT <= NP) {
+            if constexpr (sizeof(R) == 4) {
+#pragma unroll
+                for (int h = 0; h < MPT / 2; ++h) {
+                    const float4 t = __ldg(reinterpret_cast<const float4 *>(xr) + h);
+                    v[2 * h] = mk<R>(t.x, t.y);
+                    v[2 * h + 1] = mk<R>(t.z, t.w);
+                }
+            } else {
+#pragma unroll
+                for (int h = 0; h < MPT; ++h) {
+                    const double2 t = __ldg(reinterpret_cast<const double2 *>(xr) + h);
+                    v[h] = mk<R>(t.x, t.y);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < MPT; ++u) v[u] = p0 + u < NP ? xr[u] : mk<R>((R)0, (R)0);
+        }
+    };
+    for (int qc = 0; qc < Q; qc += MQC) {
+        bool any = false;
+        for (int j = 0; j < MQC && qc + j < Q; ++j) any |= gf[qc + j] != 0;
+        if (!any) continue;  // CTA-uniform
+        for (int j = 0; j < MQC; ++j)
+#pragma unroll
+            for (int u = 0; u < MPT; ++u)
+                acc[(((size_t)j * MPT + u) * 32 + lane) * (CB + 1) + wrp] = mk<R>((R)0, (R)0);
+        for (; g < g_end; ++g) {
+            const int4 sg = seg[g];
+            if (sg.x >= qc + MQC) break;  // segments are in factor order
+            constexpr int CH = 4;  // independent chains: four source loads in flight per lane
+            cx<R> sum[CH][MPT];
+#pragma unroll
+            for (int h = 0; h < CH; ++h)
+#pragma unroll
+                for (int u = 0; u < MPT; ++u) sum[h][u] = mk<R>((R)0, (R)0);
+            int z = sg.y;
+            for (; z + CH - 1 < sg.z; z += CH) {
+                cx<R> xv[CH][MPT];
+#pragma unroll
+                for (int h = 0; h < CH; ++h) load_x(pcol[z + h], xv[h]);
+#pragma unroll
+                for (int h = 0; h < CH; ++h) {
+                    const R c = pc[z + h];
+#pragma unroll
+                    for (int u = 0; u < MPT; ++u) {
+                        sum[h][u].x = fma(c, xv[h][u].x, sum[h][u].x);
+                        sum[h][u].y = fma(c, xv[h][u].y, sum[h][u].y);
+                    }
+                }
+            }
+            for (; z < sg.z; ++z) {
+                cx<R> x0[MPT];
+                load_x(pcol[z], x0);
+                const R c = pc[z];
+#pragma unroll
+                for (int u = 0; u < MPT; ++u) {
+                    sum[0][u].x = fma(c, x0[u].x, sum[0][u].x);
+                    sum[0][u].y = fma(c, x0[u].y, sum[0][u].y);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < MPT; ++u)
+                acc[(((size_t)(sg.x - qc) * MPT + u) * 32 + lane) * (CB + 1) + wrp] =
+                    (sum[0][u] + sum[1][u]) + (sum[2][u] + sum[3][u]);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < MQC * TP * CB; t += 32 * CB) {
+            const int r = t % CB, rest = t / CB;
+            const int pl = rest % TP, j = rest / TP;
+            const int q = qc + j;
+            const long long pp = pbase + pl;
+            if (q >= Q || !gf[q] || pp >= NP) continue;
+            const int u = pl % MPT, ln = pl / MPT;
+            const cx<R> v = ws[q] * acc[(((size_t)j * MPT + u) * 32 + ln) * (CB + 1) + r];
+            const size_t zi = ((size_t)q * NP + pp) * f.Ap + a0 + r;
+            if constexpr (sizeof(R) == 8) {
+                if (f.df) {  // the 16 bytes hold (re_hi, re_lo, im_hi, im_lo)
+                    const float rh = (float)v.x, ih = (float)v.y;
+                    reinterpret_cast<float4 *>(Z)[zi] = make_float4(rh, (float)(v.x - (double)rh), ih, (float)(v.y - (double)ih));
+                    continue;
+                }
+            }
+            Z[zi] = v;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename R>
+size_t seg_smem_bytes(int Q)
+{
+    return ((size_t)SegTile<R>::MQC * 32 * SegTile<R>::MPT * (CB + 1) + Q) * sizeof(cx<R>);
+}
+
 
 // tile shapes per precision: PI points x NV 16-byte vectors of channels per thread, 8 channel
 // lanes, CA = 8 x NV x (complex per vector) channels per CTA
@@ -573,8 +716,15 @@ int launch_factored(pg_op *op, const pg_scales &scales, const cxd *scales_dev, c
     const int TP = 32 * MixTile<R>::MPT;
     // channel groups fastest: the CTAs running together share a point tile of the source (L2)
     dim3 g1((unsigned)((fd.A + CB - 1) / CB), (unsigned)((NP + TP - 1) / TP));
-    fact_mix_kernel<R><<<g1, 32 * CB, mix_smem_bytes<R>(fd.Q), s>>>(fa, scales, scales_dev, (const cx<R> *)src,
-                                                                     inv_scale);
+    if constexpr (sizeof(R) == 8) {
+        const int TPs = 32 * SegTile<R>::MPT;
+        dim3 gs((unsigned)((fd.A + CB - 1) / CB), (unsigned)((NP + TPs - 1) / TPs));
+        fact_mix_seg_kernel<R><<<gs, 32 * CB, seg_smem_bytes<R>(fd.Q), s>>>(fa, scales, scales_dev,
+                                                                            (const cx<R> *)src, inv_scale);
+    } else {
+        fact_mix_kernel<R><<<g1, 32 * CB, mix_smem_bytes<R>(fd.Q), s>>>(fa, scales, scales_dev, (const cx<R> *)src,
+                                                                         inv_scale);
+    }
     op->ctx->launches++;
     PG_TRY(pg_check_launch(op->ctx));
     dim3 g2((unsigned)fd.N1, (unsigned)fd.ntiles, (unsigned)fd.nct);
@@ -607,7 +757,8 @@ void pg_factored_free(pg_op *op)
 {
     FactDev &f = op->fact;
     cudaFree(f.row_ptr); cudaFree(f.col); cudaFree(f.nzq); cudaFree(f.slot); cudaFree(f.perm);
-    cudaFree(f.coef); cudaFree(f.chunk); cudaFree(f.bflag); cudaFree(f.radial); cudaFree(f.w); cudaFree(f.Z);
+    cudaFree(f.coef); cudaFree(f.seg_ptr); cudaFree(f.seg); cudaFree(f.pcol); cudaFree(f.pcoef); cudaFree(f.seg_gq);
+    cudaFree(f.chunk); cudaFree(f.bflag); cudaFree(f.radial); cudaFree(f.w); cudaFree(f.Z);
     f = FactDev();
 }
 
@@ -751,6 +902,33 @@ int pg_factored_finalize(pg_op *op)
         for (int k = 0; k < nch; ++k)
             if (row_chunks[perm[sl]][k]) chunk[(size_t)(sl / CB) * nch + k] = 1;
     }
+    // FP64 operators: the exact nonzero pairs per (channel, factor) segment
+    std::vector<int> seg_ptr, seg, pcol;
+    std::vector<double> pcoef;
+    std::vector<unsigned char> seg_gq;
+    if (fp64) {
+        seg_ptr.assign(A + 1, 0);
+        for (int a = 0; a < A; ++a) {
+            for (int q = 0; q < Q; ++q) {
+                const int first = (int)pcol.size();
+                for (const auto &kv : rows[a])
+                    if (kv.second[q] != 0.0) {
+                        pcol.push_back(kv.first);
+                        pcoef.push_back(kv.second[q]);
+                    }
+                if ((int)pcol.size() == first) continue;
+                seg.push_back(q);
+                seg.push_back(first);
+                seg.push_back((int)pcol.size());
+                seg.push_back(0);
+            }
+            seg_ptr[a + 1] = (int)(seg.size() / 4);
+        }
+        seg_gq.assign((size_t)ngroups * Q, 0);
+        for (int sl = 0; sl < A; ++sl)
+            for (int q = 0; q < Q; ++q)
+                if (has[perm[sl]][q]) seg_gq[(size_t)(sl / CB) * Q + q] = 1;
+    }
 
     // radial factors, last rank padded to N2p; points outside the grid are dropped
     std::vector<double> rad((size_t)Q * N1 * b * b * f.N2p, 0.0);
@@ -796,6 +974,13 @@ int pg_factored_finalize(pg_op *op)
     PG_TRY(upload_vec(&f.slot, slot));
     PG_TRY(upload_vec(&f.nzq, nzq));
     PG_TRY(upload_vec(&f.perm, perm));
+    if (fp64) {
+        PG_TRY(upload_vec(&f.seg_ptr, seg_ptr));
+        PG_TRY(upload_vec(&f.seg, seg));
+        PG_TRY(upload_vec(&f.pcol, pcol));
+        PG_TRY(upload_vec(&f.seg_gq, seg_gq));
+        PG_TRY(upload_real<double>(&f.pcoef, pcoef));
+    }
     PG_TRY(upload_vec(&f.chunk, chunk));
     PG_TRY(upload_vec(&f.bflag, bflag));
     PG_CUDA_TRY(cudaMalloc(&f.w, sizeof(cxd) * Q));
@@ -829,11 +1014,13 @@ int pg_factored_finalize(pg_op *op)
     PG_CUDA_TRY(cudaGetDevice(&dev));
     PG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     if (f.radial_smem > (size_t)optin) return PG_ERR_SHAPE;
-    if ((fp64 ? mix_smem_bytes<double>(Q) : mix_smem_bytes<float>(Q)) > (size_t)optin) return PG_ERR_SHAPE;
-    if (fp64)
-        PG_CUDA_TRY(cudaFuncSetAttribute(fact_mix_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    else
+    if (fp64) {
+        if (seg_smem_bytes<double>(Q) > (size_t)optin) return PG_ERR_SHAPE;
+        PG_CUDA_TRY(cudaFuncSetAttribute(fact_mix_seg_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    } else {
+        if (mix_smem_bytes<float>(Q) > (size_t)optin) return PG_ERR_SHAPE;
         PG_CUDA_TRY(cudaFuncSetAttribute(fact_mix_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    }
     if (fp64) {
         PG_CUDA_TRY(cudaFuncSetAttribute(fact_radial_kernel<double, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
         PG_CUDA_TRY(cudaFuncSetAttribute(fact_radial_df_kernel<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));

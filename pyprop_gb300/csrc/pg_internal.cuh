@@ -155,6 +155,10 @@ struct FactDev {
     void *coef = nullptr;             // [pairs] its coefficient (operator precision)
     unsigned char *chunk = nullptr;   // [Ap / 4][Q] factors touched by each group of 4 channels
     unsigned char *bflag = nullptr;   // [Q][nct] channel tiles with a nonzero row
+    // FP64 operators: the exact nonzero pairs, per (channel, factor) segment
+    int *seg_ptr = nullptr, *seg = nullptr, *pcol = nullptr;  // [A + 1], [segments][4], [pairs]
+    void *pcoef = nullptr;            // [pairs]
+    unsigned char *seg_gq = nullptr;  // [Ap / 4][Q] factors touched by each group of 4 slots
     void *radial = nullptr;           // [Q][N1][b][b][N2p] real
     cxd *w = nullptr;                 // [Q]
     void *Z = nullptr;                // [Q][N1*N2][Ap] complex scratch (slots innermost)
