@@ -322,8 +322,19 @@ int pg_cayley_last_stats(pg_cayley *c, pg_krylov_stats *stats);
 int pg_cayley_set_true_residual(pg_cayley *c, int on);
 /* Eager mode: the same kernels launched one by one with the GMRES/refinement loops driven
  * from the host (one wait per iteration). For profilers that cannot look inside
- * conditional graph nodes; results are identical to the graph mode. */
+ * conditional graph nodes; results are identical to the graph mode. Eager steppers always
+ * take the multi-kernel step. */
 int pg_cayley_set_eager(pg_cayley *c, int on);
+/* Single-kernel mixed step (the same scheme as the PG_FP32 step above, as one cooperative
+ * launch: CTA a solves angular channel a, the FP64 residual rows are spread over all SMs,
+ * grid barriers between the phases, each a bounded wait that sets the context's device error
+ * flag to 2 when it runs out). The default for PG_FP32 steppers of a rank-2 banded operator
+ * (no dense or factorized terms) with the block-diagonal LU preconditioner, basis_size <= 32
+ * and no more channels than resident CTAs; the learned preconditioner and the eager mode
+ * use the multi-kernel step. on = 0 selects the multi-kernel step; on = 1 on a stepper that
+ * does not qualify returns PG_ERR_STATE. Replaces the same reference step as
+ * pg_cayley_step (CayleyPropagator.py:71-150). */
+int pg_cayley_set_fused(pg_cayley *c, int on);
 /*
  * Learned preconditioner (no counterpart in the reference; mixed-precision steppers only).
  * With a network set, each refinement pass runs flexible GMRES right-preconditioned by

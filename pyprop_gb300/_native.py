@@ -23,6 +23,7 @@ PG_BAND_SOLVE_UT = 3
 PG_BAND_MUL_S = 4
 PG_BAND_SOLVE_S = 5
 PG_BAND_PREC_SOLVE = 6
+PG_ERR_STATE = -9
 
 ERRORS = {
     -1: "PG_ERR_ARG", -2: "PG_ERR_CUDA", -3: "PG_ERR_STORAGE", -4: "PG_ERR_SHAPE", -5: "PG_ERR_NONFINITE",
@@ -97,6 +98,7 @@ _SIGS = {
     "pg_cayley_last_stats": (_I, [_P, C.POINTER(KrylovStats)]),
     "pg_cayley_set_true_residual": (_I, [_P, _I]),
     "pg_cayley_set_eager": (_I, [_P, _I]),
+    "pg_cayley_set_fused": (_I, [_P, _I]),
     "pg_cayley_set_learned": (_I, [_P, _P, _I]),
     "pg_cayley_learned_rejected": (_I, [_P, C.POINTER(_LL)]),
     "pg_cayley_batch_create": (_I, [C.POINTER(_P), _I, C.POINTER(_P)]),

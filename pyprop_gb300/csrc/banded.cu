@@ -13,6 +13,7 @@
 // blocks run in parallel; the only sequential part is a recurrence on the kb boundary values
 // of consecutive blocks (tri_solve_kernel).
 #include "pg_internal.cuh"
+#include "tri_solve.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -22,40 +23,8 @@ typedef std::complex<double> zd;
 // ------------------------------------------------------------------------------------
 // kernels
 // ------------------------------------------------------------------------------------
-template <typename R> __device__ __forceinline__ cx<R> shfl_cx(cx<R> v, int lane)
-{
-    v.x = __shfl_sync(0xffffffffu, v.x, lane);
-    v.y = __shfl_sync(0xffffffffu, v.y, lane);
-    return v;
-}
-
-// coefficient multiply-add: acc += c * v (c real or complex)
-template <typename R> __device__ __forceinline__ void coef_fma(cx<R> &acc, R c, cx<R> v)
-{
-    acc.x = fma(c, v.x, acc.x);
-    acc.y = fma(c, v.y, acc.y);
-}
-template <typename R> __device__ __forceinline__ void coef_fma(cx<R> &acc, cx<R> c, cx<R> v) { cfma(acc, c, v); }
-template <typename R> __device__ __forceinline__ void coef_fms(cx<R> &acc, R c, cx<R> v)
-{
-    acc.x = fma(-c, v.x, acc.x);
-    acc.y = fma(-c, v.y, acc.y);
-}
-template <typename R> __device__ __forceinline__ void coef_fms(cx<R> &acc, cx<R> c, cx<R> v) { cfma(acc, mk<R>(-c.x, -c.y), v); }
-
-// Blocked triangular solves, parallel over the blocks of a fibre. With T_b the 32x32 diagonal
-// block of block b and C_b its coupling to the w boundary values s of the neighbouring block
-// (lower sweep: the last w values of block b-1; upper sweep: the first w values of block
-// b+1), the solution of block b is
-//     y_b = z_b - G_b s,   z_b = T_b^-1 f_b,   G_b = T_b^-1 C_b   (G_b: 32 x w, precomputed).
-// The boundary values of all blocks solve the block-bidiagonal system
-//     s_b + G_b[boundary rows] s_{b-/+1} = z_b[boundary rows],
-// whose inverse Rb (nblk*w square, block triangular) depends only on the factor, so it is
-// precomputed on the host: s = Rb z[boundary rows]. Every step is then parallel - z_b for all
-// blocks, the Rb product, the corrections G_b s - with no sequential recurrence left. Lane t
-// of a warp owns row 32b + t of block b; the fibre stays in shared memory for both sweeps.
-// C: coefficient type (R or cx<R>). inv: [nmat][nblk][32 s][32 t] = T^-1[t][s],
-// g: [nmat][nblk][w c][32 t] = G[t][c], rb: [nmat][nblk*w][nblk*w] row-major.
+// One CTA of NW warps per fibre (tri_solve_smem in tri_solve.cuh holds the method): load the
+// fibre into shared memory, run both sweeps, store it back.
 template <typename R, typename C, int NW>
 __global__ void __launch_bounds__(32 * NW, 1)
     tri_solve_kernel(int N, int nblk, int w, const C *__restrict__ lo_inv, const C *__restrict__ lo_g,
@@ -64,106 +33,17 @@ __global__ void __launch_bounds__(32 * NW, 1)
                      cx<R> *__restrict__ x, int nfib)
 {
     extern __shared__ __align__(16) unsigned char tri_smem[];
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
     const int f = blockIdx.x;
     if (f >= nfib) return;
     cx<R> *xs = (cx<R> *)tri_smem;              // [nblk*32] the fibre: f, then z, then y
     cx<R> *sb = xs + (size_t)nblk * 32;          // [nblk*w] boundary values s_b
     C *sg = (C *)(sb + (size_t)nblk * w);        // [nblk][w][32] G_b (when g_in_smem)
     const size_t m = (size_t)(f / fib_per_mat);
-    const size_t gstride = (size_t)w * 32;
-    const int nb = nblk * w;
     cx<R> *xf = x + (size_t)f * N;
     for (int i = threadIdx.x; i < nblk * 32; i += 32 * NW) xs[i] = (i < N) ? xf[i] : mk<R>((R)0, (R)0);
     __syncthreads();
-
-    // z_b = T_b^-1 r for lane's row; G_b staged for the correction
-    auto solve_block = [&](int blk, cx<R> r, const C *inv, const C *g) {
-        const C *ib = inv + (m * nblk + blk) * 1024;
-        cx<R> acc[4];
-#pragma unroll
-        for (int a = 0; a < 4; ++a) acc[a] = mk<R>((R)0, (R)0);
-#pragma unroll 1
-        for (int q0 = 0; q0 < 32; q0 += 16) {
-#pragma unroll
-            for (int q = 0; q < 16; ++q) coef_fma(acc[q & 3], ib[(q0 + q) * 32 + lane], shfl_cx(r, q0 + q));
-        }
-        xs[blk * 32 + lane] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
-        if (g_in_smem) {
-            const C *gb = g + (m * nblk + blk) * gstride;
-            for (int c = 0; c < w; ++c) sg[((size_t)blk * w + c) * 32 + lane] = gb[c * 32 + lane];
-        }
-    };
-    // s = Rb z[boundary rows]: each warp takes BRW consecutive output rows at a time, lanes
-    // over the columns, so all of a lane's Rb loads for those rows are in flight together;
-    // the block-triangular zero part is skipped by a per-element predicate
-    auto boundary = [&](bool lower, const C *rb) {
-        constexpr int BRW = 8;
-        const C *Rm = rb + m * (size_t)nb * nb;
-        const int r0 = lower ? 32 - w : 0;
-        for (int row0 = warp * BRW; row0 < nb; row0 += NW * BRW) {
-            cx<R> acc[BRW];
-#pragma unroll
-            for (int q = 0; q < BRW; ++q) acc[q] = mk<R>((R)0, (R)0);
-            const int bo_first = row0 / w, bo_last = min(row0 + BRW - 1, nb - 1) / w;
-            const int c_lo = lower ? 0 : bo_first * w, c_hi = lower ? (bo_last + 1) * w : nb;
-            for (int col = c_lo + lane; col < c_hi; col += 32) {
-                const int bc = col / w, rc = col - bc * w;
-                const cx<R> zc = xs[bc * 32 + r0 + rc];
-#pragma unroll
-                for (int q = 0; q < BRW; ++q) {
-                    const int row = row0 + q, bo = row / w;
-                    const bool nz = row < nb && (lower ? bc <= bo : bc >= bo);
-                    if (nz) coef_fma(acc[q], Rm[(size_t)row * nb + col], zc);
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < BRW; ++q) {
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    acc[q].x += __shfl_xor_sync(0xffffffffu, acc[q].x, o);
-                    acc[q].y += __shfl_xor_sync(0xffffffffu, acc[q].y, o);
-                }
-                if (lane == 0 && row0 + q < nb) sb[row0 + q] = acc[q];
-            }
-        }
-    };
-    // y_b = z_b - G_b s (returns the corrected row)
-    auto correct = [&](int blk, const C *g, bool lower) -> cx<R> {
-        cx<R> y = xs[blk * 32 + lane];
-        const int nbk = lower ? blk - 1 : blk + 1;
-        if (nbk >= 0 && nbk < nblk) {
-            const C *gb = g_in_smem ? sg + (size_t)blk * gstride : g + (m * nblk + blk) * gstride;
-            for (int c = 0; c < w; ++c) coef_fms(y, gb[c * 32 + lane], sb[nbk * w + c]);
-        }
-        return y;
-    };
-
-    if (do_lower) {
-        for (int blk = warp; blk < nblk; blk += NW) solve_block(blk, xs[blk * 32 + lane], lo_inv, lo_g);
-        __syncthreads();
-        boundary(true, lo_rb);
-        __syncthreads();
-        for (int blk = warp; blk < nblk; blk += NW) {
-            const cx<R> y = correct(blk, lo_g, true);
-            if (do_upper) solve_block(blk, y, up_inv, up_g);  // same rows, same warp
-            else xs[blk * 32 + lane] = y;
-        }
-        __syncthreads();
-    } else if (do_upper) {
-        for (int blk = warp; blk < nblk; blk += NW) solve_block(blk, xs[blk * 32 + lane], up_inv, up_g);
-        __syncthreads();
-    }
-    if (do_upper) {
-        boundary(false, up_rb);
-        __syncthreads();
-        for (int blk = warp; blk < nblk; blk += NW) {
-            const cx<R> y = correct(blk, up_g, false);
-            xs[blk * 32 + lane] = y;
-        }
-        __syncthreads();
-    }
+    tri_solve_smem<R, C, NW>(nblk, w, m, lo_inv, lo_g, lo_rb, up_inv, up_g, up_rb, do_lower, do_upper, g_in_smem, xs,
+                             sb, sg);
     for (int i = threadIdx.x; i < N; i += 32 * NW) xf[i] = xs[i];
 }
 

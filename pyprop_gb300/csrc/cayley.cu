@@ -17,7 +17,7 @@
 //           M^-1 A d = M^-1 r to 2e-6 relative; psi += d and r -= A d in FP64; the outer
 //           WHILE node repeats while the true residual ||r|| (FP64) is above tol (at most
 //           4 passes).
-#include "pg_internal.cuh"
+#include "cayley_state.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -28,19 +28,7 @@ int pg_scale_copy(pg_ctx *ctx, const cx<Rs> *src, cx<Rd> *dst, cx<Rd> *dst2, lon
                   double mul);
 int pg_axpy(pg_ctx *ctx, cxd a, const cxd *x, cxd *y, long long n);
 
-static const int GM_MAXM = 64;
 static const int RING = 64;
-
-struct GmresStats {
-    long long iterations;  // GMRES iterations of the step (all refinement passes)
-    int k;                 // basis vectors used by the last solve
-    int passes;            // refinement passes (mixed) / 1
-    double resid;          // least-squares residual estimate of the last solve
-    double true_resid;     // ||(S + i dt/2 H) psi' - b|| in FP64 (mixed; FP64 mode when requested)
-    double beta0;          // norm of the preconditioned right-hand side of the last solve
-    long long kernels;     // kernels run by all steps so far (never reset; see the K_* counts)
-    long long rejected;    // learned-preconditioner passes rejected by the true residual (cumulative)
-};
 
 // Kernels a step runs, counted on the device as the loops decide (one graph launch hides them):
 // FP64 step: scales, matvec, preconditioner solve, norm, init, back-substitution, combine;
@@ -55,32 +43,6 @@ static const int K_FP64_BASE = 7, K_TRUE_RESID = 4, K_MIXED_BASE = 2, K_MIXED_PA
 // block solve, features, 3 network products, correction, matvec, multidot, 2 GS updates,
 // Givens; per pass convert, norm, init, back-substitution, combine, matvec, norm, decide, commit
 static const int K_LEARN_ITER = 12, K_LEARN_PASS = 9;
-
-struct GmresState {
-    GmresStats stats;
-    int j;            // Krylov vector being expanded in this iteration
-    int cont_inner;   // loop decisions, mirrored for the eager (host-driven) mode
-    int cont_outer;
-    int learned_on;   // learned preconditioner in use for the rest of this step
-    int accept;       // the last learned pass met the residual test
-    int pad;
-    double tol_eff;
-    double beta_last;
-    double cs[GM_MAXM];
-    double sn[2 * GM_MAXM];
-    double g[2 * (GM_MAXM + 1)];
-    double R[2 * GM_MAXM * GM_MAXM];  // column-major R[col * GM_MAXM + row]
-    double y[2 * GM_MAXM];
-};
-
-struct StepParams {
-    double dt;
-    double pad;
-    cxd h[PG_MAX_SLOTS];  // slot values of H(t + dt/2); slot 0 is the overlap slot
-};
-
-// scale sets derived on the device from StepParams
-enum { SC_PLUS = 0, SC_MINUS = 1, SC_DIFF = 2, SC_NEGPLUS = 3, SC_COUNT = 4 };
 
 // ------------------------------------------------------------------------------------
 // kernels
@@ -424,6 +386,9 @@ struct pg_cayley {
     void *Z = nullptr, *zcur = nullptr, *Xf = nullptr;
     float *mlp_out = nullptr;
     cxd *rn64 = nullptr;
+    // single-kernel mixed step (cayley_fused.cu), when the operators qualify
+    FusedCayley *fused = nullptr;
+    bool use_fused = true;
 };
 
 static int nblocks_for(pg_ctx *ctx, long long n)
@@ -761,6 +726,12 @@ extern "C" int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64,
         c->ring_used[k] = false;
     }
     for (int k = 0; k < 3; ++k) PG_CUDA_TRY(cudaStreamCreateWithFlags(&c->cap[k], cudaStreamNonBlocking));
+    // rank-2 banded operators with the block LU preconditioner run the mixed step as one
+    // kernel; anything else (or a failed check) keeps the captured multi-kernel step
+    if (basis_precision == PG_FP32 && pg_cayley_fused_prepare(op64, op_basis, prec_basis, c->m, &c->fused) != PG_OK) {
+        c->fused = nullptr;
+        cudaGetLastError();
+    }
     *out = c;
     return PG_OK;
 }
@@ -774,6 +745,7 @@ extern "C" int pg_cayley_destroy(pg_cayley *c)
     for (int k = 0; k < 3; ++k)
         if (c->cap[k]) cudaStreamDestroy(c->cap[k]);
     for (int k = 0; k < RING; ++k) cudaEventDestroy(c->ring_ev[k]);
+    pg_cayley_fused_free(c->fused);
     for (void *p : {c->Z, c->zcur, c->Xf, (void *)c->mlp_out, (void *)c->rn64}) cudaFree(p);
     void *bufs[] = {c->V, c->w, c->vcur, c->dconv, c->b64, c->r64, c->d64, c->e64, c->h1, c->h2, c->h3, c->nrm,
                     c->nrm2, c->st, c->d_params, c->d_sc, c->rctx.red_partial, c->rctx.red_counter,
@@ -793,7 +765,8 @@ static int cayley_launch(pg_cayley *c, cxd *psi, double dt, const double *scales
     pg_ctx *ctx = c->ctx;
     // kernels are counted on the device (GmresStats::kernels), not while recording
     const long long launches = ctx->launches;
-    if (!c->eager && (!c->exec || c->built_psi != psi)) {
+    const bool fused = c->fused && c->use_fused && !c->mlp && !c->eager;
+    if (!fused && !c->eager && (!c->exec || c->built_psi != psi)) {
         const int code = build_graph(c, psi);
         ctx->launches = launches;
         PG_TRY(code);
@@ -808,6 +781,11 @@ static int cayley_launch(pg_cayley *c, cxd *psi, double dt, const double *scales
     PG_CUDA_TRY(cudaMemcpyAsync(c->d_params, &p, sizeof(StepParams), cudaMemcpyHostToDevice, ctx->stream));
     PG_CUDA_TRY(cudaEventRecord(c->ring_ev[slot], ctx->stream));
     c->ring_used[slot] = true;
+    if (fused) {
+        PG_TRY(pg_cayley_fused_launch(c->fused, ctx->stream, c->d_params, psi, c->st, c->tol, ctx->d_err));
+        PG_CUDA_TRY(cudaMemcpyAsync(c->h_stats, &c->st->stats, sizeof(GmresStats), cudaMemcpyDeviceToHost, ctx->stream));
+        return PG_OK;
+    }
     if (c->eager) {
         c->rctx.stream = ctx->stream;
         const int code = (c->prec == PG_FP64) ? record_fp64(c, psi) : record_mixed(c, psi);
@@ -892,6 +870,16 @@ extern "C" int pg_cayley_set_eager(pg_cayley *c, int on)
 {
     if (!c) return PG_ERR_ARG;
     c->eager = on != 0;
+    return PG_OK;
+}
+
+// Single-kernel mixed step on (the default where the operators qualify) or off (the
+// captured multi-kernel step). PG_ERR_STATE when switching on a stepper that does not qualify.
+extern "C" int pg_cayley_set_fused(pg_cayley *c, int on)
+{
+    if (!c) return PG_ERR_ARG;
+    if (on && !c->fused) return PG_ERR_STATE;
+    c->use_fused = on != 0;
     return PG_OK;
 }
 

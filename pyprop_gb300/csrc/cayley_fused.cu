@@ -1,0 +1,664 @@
+// Single-kernel mixed-precision Cayley / Crank-Nicolson step.
+//
+// The same scheme as the captured multi-kernel mixed step of cayley.cu (the reference's step:
+// pyprop/propagator/CayleyPropagator.py:71-150, GMRES core/krylov/gmres/gmres.h:433-505),
+// run as ONE cooperative launch that keeps every SM busy: CTA a < Nang owns angular channel a.
+//   r = b - A psi = -i dt H psi                      (FP64, rows spread over all CTAs)
+//   per refinement pass (at most 4, while ||r|| > tol):
+//     d = M_a^-1 r_a                                 (complex64 block LU solve, in shared memory)
+//     GMRES on M^-1 A e = d in complex64, Gram-Schmidt sums in FP64 across channels,
+//     Givens rotations and back-substitution in FP32 (the multi-kernel step's arithmetic)
+//     psi += e, r -= A e                             (FP64, rows spread over all CTAs)
+// Everything a GMRES iteration needs is local to the channel except the matvec (the dipole
+// couples neighbouring channels) and three scalar reductions (<V, w> twice, ||w||), so an
+// iteration costs three grid barriers instead of seven kernel launches, and a pass three more.
+// The Krylov vectors of channel a live in V[.][a] and are written only by CTA a; the vector
+// the next matvec reads is published unnormalised in a ping-pong buffer (wbuf) before the
+// barrier that completes its norm, and every reader scales it by 1/beta. Every CTA sums the
+// partials in the same order and runs the (tiny) Givens and back-substitution recurrences
+// itself, so all CTAs take identical decisions without another barrier. The FP64 parts
+// (residual rows, the correction e = V y) are spread over all CTAs: FP64 arithmetic is scarce
+// on this GPU. Grid barriers are bounded waits: one that runs out sets the context's error
+// flag (2) and the CTAs return.
+#include "cayley_state.cuh"
+#include "tri_solve.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+static const int FZ_NW = 24;                 // warps per CTA (the block solve's width for long fibres)
+static const int FZ_THREADS = 32 * FZ_NW;
+static const int FZ_MAXM = 32;               // Krylov basis bound of the single-kernel step
+static const int FZ_CB = 8;                  // columns per register block of the channel sums
+static const int FZ_MAXPASS = 4;             // refinement passes (as the multi-kernel step)
+static const int FZ_PSTRIDE = 2 * (FZ_MAXM + 1);
+static const unsigned int FZ_POLLS = 1u << 24;  // barrier polls (>= 64 ns each) before giving up
+enum { P_NRM = 0, P_H1 = 1, P_H2 = 2, P_H3 = 3, P_RES = 4, P_COUNT = 5 };
+
+struct FzBarrier {
+    unsigned int count;
+    unsigned int gen;
+};
+
+struct FzArgs {
+    OpDev op64, opb;
+    const cxf *lo_inv, *lo_g, *lo_rb, *up_inv, *up_g, *up_rb;
+    int nblk, w, fib_per_mat, g_in_smem;
+    int nch, N, m;
+    double tol;
+    const StepParams *params;
+    cxd *psi;
+    cxd *r64;        // [nch*N] FP64 residual (rows spread over the CTAs)
+    cxd *e64;        // [nch*N] correction of the pass (read across channels by the FP64 rows)
+    cxf *wbuf;       // [2][nch*N] unnormalised next Krylov vector (read across channels)
+    cxf *V;          // [m][nch*N] Krylov vectors (channel a written by CTA a only)
+    double *part;    // [P_COUNT][CTAs][FZ_PSTRIDE] per-CTA partial sums
+    FzBarrier *bar;
+    GmresState *st;
+    int *err;
+};
+
+__device__ __forceinline__ unsigned int fz_ld_acquire(const unsigned int *p)
+{
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// All CTAs meet (the launch is cooperative, so all are resident). Returns false, CTA-uniform,
+// when the wait ran out; the error flag is then set.
+__device__ __forceinline__ bool fz_grid_sync(FzBarrier *bar, unsigned int &gen, int *err, int *s_ok)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(&bar->count, 1u) + 1u;
+        if (arrived == gridDim.x) {
+            atomicExch(&bar->count, 0u);
+            __threadfence();
+            atomicAdd(&bar->gen, 1u);
+        } else {
+            unsigned int polls = 0;
+            while (fz_ld_acquire(&bar->gen) == gen) {
+                if (++polls > FZ_POLLS) { ok = 0; break; }
+                __nanosleep(64);
+            }
+        }
+        if (!ok) atomicExch(err, 2);
+        gen += 1u;
+        __threadfence();
+        *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+template <typename R> __device__ __forceinline__ R fz_warp_sum(R v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ cxf fz_ldcg(const cxf *p)
+{
+    const float2 v = __ldcg((const float2 *)p);
+    return mk<float>(v.x, v.y);
+}
+__device__ __forceinline__ cxd fz_ldcg(const cxd *p)
+{
+    const double2 v = __ldcg((const double2 *)p);
+    return mk<double>(v.x, v.y);
+}
+// read-only data (operator bands)
+__device__ __forceinline__ cxf fz_ldg(const cxf *p)
+{
+    const float2 v = __ldg((const float2 *)p);
+    return mk<float>(v.x, v.y);
+}
+__device__ __forceinline__ cxd fz_ldg(const cxd *p)
+{
+    const double2 v = __ldg((const double2 *)p);
+    return mk<double>(v.x, v.y);
+}
+
+// Sum over the channels of the partials of one phase: hs[t] = sum_a part[a][t], t < nval,
+// one warp per value, the channels over the lanes, a fixed order (identical in every CTA).
+__device__ __forceinline__ void fz_reduce(const double *part, int nch, int nval, double *hs)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int t = warp; t < nval; t += FZ_NW) {
+        double s = 0.0;
+        for (int a = lane; a < nch; a += 32) s += __ldcg(part + (size_t)a * FZ_PSTRIDE + t);
+        s = fz_warp_sum(s);
+        if (lane == 0) hs[t] = s;
+    }
+    __syncthreads();
+}
+
+// Channel sums of the complex64 fibre xs: out[2q], out[2q+1] = <V_q, xs> for q < J (dots),
+// out[0] = ||xs||^2 (norm_only). Element sums in FP32 per thread and warp, CTA sums in FP64.
+__device__ __forceinline__ void fz_channel_sums(const cxf *Vc, long long ldv, int J, bool norm_only, const cxf *xs,
+                                                int N, double (*red)[2 * FZ_CB], double *out)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ncol = norm_only ? 1 : J;
+    for (int j0 = 0; j0 < ncol; j0 += FZ_CB) {
+        float ax[FZ_CB], ay[FZ_CB];
+#pragma unroll
+        for (int q = 0; q < FZ_CB; ++q) ax[q] = ay[q] = 0.f;
+        for (int i = threadIdx.x; i < N; i += FZ_THREADS) {
+            const cxf b = xs[i];
+            if (norm_only) {
+                ax[0] = fmaf(b.x, b.x, ax[0]);
+                ax[0] = fmaf(b.y, b.y, ax[0]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < FZ_CB; ++q)
+                    if (j0 + q < J) {
+                        const cxf v = Vc[(size_t)(j0 + q) * ldv + i];
+                        ax[q] = fmaf(v.x, b.x, ax[q]);
+                        ax[q] = fmaf(v.y, b.y, ax[q]);
+                        ay[q] = fmaf(v.x, b.y, ay[q]);
+                        ay[q] = fmaf(-v.y, b.x, ay[q]);
+                    }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < FZ_CB; ++q) {
+            if (j0 + q < ncol) {  // CTA-uniform
+                const float sx = fz_warp_sum(ax[q]);
+                const float sy = fz_warp_sum(ay[q]);
+                if (lane == 0) {
+                    red[warp][2 * q] = (double)sx;
+                    red[warp][2 * q + 1] = (double)sy;
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 2 * FZ_CB && j0 + (int)threadIdx.x / 2 < ncol) {
+            double s = 0.0;
+            for (int q = 0; q < FZ_NW; ++q) s += red[q][threadIdx.x];
+            out[2 * j0 + threadIdx.x] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// FP64 rows [lo, hi) of the flattened [Nang][N] operator applied to src (read through L2:
+// other CTAs write it): r[o] (+)= sum_e sc[slot_e] sum_d band_e[d][i] src[col_e][i + d - kb],
+// o = a N + i. Returns this thread's share of ||r||^2 over its rows.
+__device__ __forceinline__ double fz_rows64(const OpDev &op, long long lo, long long hi, const cxd *sc,
+                                            const cxd *src, cxd *r, bool accumulate)
+{
+    const int N = op.N, kb = op.kb, b = op.b, ld = op.ld;
+    const cxd *bands = (const cxd *)op.bands;
+    double nrm = 0.0;
+    for (long long o = lo + threadIdx.x; o < hi; o += FZ_THREADS) {
+        const int a = (int)(o / N), i = (int)(o - (long long)a * N);
+        const int e0 = __ldg(op.row_ptr + a), e1 = __ldg(op.row_ptr + a + 1);
+        cxd acc = mk<double>(0.0, 0.0);
+        for (int e = e0; e < e1; ++e) {
+            const cxd *B = bands + (size_t)__ldg(op.ent_band + e) * b * ld;
+            const cxd *x = src + (size_t)__ldg(op.ent_col + e) * N;
+            cxd t = mk<double>(0.0, 0.0);
+            for (int d = 0; d < b; ++d) {
+                const int j = i + d - kb;
+                if (j >= 0 && j < N) cfma(t, fz_ldg(B + (size_t)d * ld + i), fz_ldcg(x + j));
+            }
+            cfma(acc, sc[__ldg(op.ent_slot + e)], t);
+        }
+        if (accumulate) acc = acc + fz_ldcg(r + o);
+        r[o] = acc;
+        nrm = fma(acc.x, acc.x, nrm);
+        nrm = fma(acc.y, acc.y, nrm);
+    }
+    return nrm;
+}
+
+// CTA sum of one FP64 value per thread into out[0] (FP64 throughout)
+__device__ __forceinline__ void fz_cta_sum64(double v, double (*red)[2 * FZ_CB], double *out)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = fz_warp_sum(v);
+    if (lane == 0) red[warp][0] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < FZ_NW; ++q) s += red[q][0];
+        out[0] = s;
+    }
+    __syncthreads();
+}
+
+// complex64 operator row a applied to the normalised vector wsrc * s (wsrc read through
+// L2); xs[i] = result for i < N, zero on the padding up to npad
+__device__ __forceinline__ void fz_matvec32(const OpDev &op, int a, const cxf *sc, const cxf *wsrc, float s, cxf *xs,
+                                            int npad)
+{
+    const int N = op.N, kb = op.kb, b = op.b, ld = op.ld;
+    const cxf *bands = (const cxf *)op.bands;
+    const int e0 = __ldg(op.row_ptr + a), e1 = __ldg(op.row_ptr + a + 1);
+    for (int i = threadIdx.x; i < npad; i += FZ_THREADS) {
+        cxf acc = mk<float>(0.f, 0.f);
+        if (i < N) {
+            for (int e = e0; e < e1; ++e) {
+                const cxf *B = bands + (size_t)__ldg(op.ent_band + e) * b * ld;
+                const cxf *x = wsrc + (size_t)__ldg(op.ent_col + e) * N;
+                cxf t = mk<float>(0.f, 0.f);
+                for (int d = 0; d < b; ++d) {
+                    const int j = i + d - kb;
+                    if (j >= 0 && j < N) {
+                        const cxf v = fz_ldcg(x + j);
+                        cfma(t, fz_ldg(B + (size_t)d * ld + i), mk<float>(v.x * s, v.y * s));
+                    }
+                }
+                cfma(acc, sc[__ldg(op.ent_slot + e)], t);
+            }
+        }
+        xs[i] = acc;
+    }
+}
+
+struct FzGivens {
+    float cs[FZ_MAXM];
+    float sn[2 * FZ_MAXM];
+    float g[2 * (FZ_MAXM + 1)];
+    float R[2 * FZ_MAXM * FZ_MAXM];  // column-major R[col * FZ_MAXM + row]
+};
+
+// New Hessenberg column j (h1 + h2 above the diagonal, beta below) through the previous
+// rotations, the new rotation, the updated g; returns the residual estimate |g_{j+1}|. FP32
+// as the multi-kernel step's Givens kernel.
+__device__ float fz_givens(FzGivens &G, int j, const double *h1, const double *h2, double beta)
+{
+    const int J = j + 1;
+    float hx[FZ_MAXM + 1], hy[FZ_MAXM + 1];
+    for (int i = 0; i < J; ++i) {
+        hx[i] = (float)(h1[2 * i] + h2[2 * i]);
+        hy[i] = (float)(h1[2 * i + 1] + h2[2 * i + 1]);
+    }
+    hx[J] = (float)beta;
+    hy[J] = 0.f;
+    for (int i = 0; i < j; ++i) {
+        const float c = G.cs[i], sx = G.sn[2 * i], sy = G.sn[2 * i + 1];
+        const float tx = c * hx[i] + (sx * hx[i + 1] - sy * hy[i + 1]);
+        const float ty = c * hy[i] + (sx * hy[i + 1] + sy * hx[i + 1]);
+        const float ux = -(sx * hx[i] + sy * hy[i]) + c * hx[i + 1];
+        const float uy = -(sx * hy[i] - sy * hx[i]) + c * hy[i + 1];
+        hx[i] = tx; hy[i] = ty;
+        hx[i + 1] = ux; hy[i + 1] = uy;
+    }
+    const float a = hypotf(hx[j], hy[j]);
+    const float bb = hypotf(hx[j + 1], hy[j + 1]);
+    const float r = hypotf(a, bb);
+    float c, sx, sy;
+    if (r == 0.f) { c = 1.f; sx = 0.f; sy = 0.f; }
+    else if (a == 0.f) { c = 0.f; sx = hx[j + 1] / bb; sy = -hy[j + 1] / bb; }
+    else {
+        c = a / r;
+        const float px = hx[j] / a, py = hy[j] / a;
+        sx = (px * hx[j + 1] + py * hy[j + 1]) / r;
+        sy = (py * hx[j + 1] - px * hy[j + 1]) / r;
+    }
+    const float rjx = c * hx[j] + (sx * hx[j + 1] - sy * hy[j + 1]);
+    const float rjy = c * hy[j] + (sx * hy[j + 1] + sy * hx[j + 1]);
+    hx[j] = rjx; hy[j] = rjy;
+    G.cs[j] = c;
+    G.sn[2 * j] = sx;
+    G.sn[2 * j + 1] = sy;
+    const float gx = G.g[2 * j], gy = G.g[2 * j + 1];
+    const float g1x = -(sx * gx + sy * gy), g1y = -(sx * gy - sy * gx);
+    G.g[2 * j] = c * gx;
+    G.g[2 * j + 1] = c * gy;
+    G.g[2 * (j + 1)] = g1x;
+    G.g[2 * (j + 1) + 1] = g1y;
+    for (int i = 0; i <= j; ++i) {
+        G.R[2 * (j * FZ_MAXM + i)] = hx[i];
+        G.R[2 * (j * FZ_MAXM + i) + 1] = hy[i];
+    }
+    return hypotf(g1x, g1y);
+}
+
+// y = R^-1 g over k columns (FP32), stored as complex128
+__device__ void fz_backsolve(const FzGivens &G, int k, cxd *ys)
+{
+    float yx[FZ_MAXM], yy[FZ_MAXM];
+    for (int i = k - 1; i >= 0; --i) {
+        float sx = G.g[2 * i], sy = G.g[2 * i + 1];
+        for (int q = i + 1; q < k; ++q) {
+            const float rx = G.R[2 * (q * FZ_MAXM + i)], ry = G.R[2 * (q * FZ_MAXM + i) + 1];
+            sx -= rx * yx[q] - ry * yy[q];
+            sy -= rx * yy[q] + ry * yx[q];
+        }
+        const float dx = G.R[2 * (i * FZ_MAXM + i)], dy = G.R[2 * (i * FZ_MAXM + i) + 1];
+        const float den = dx * dx + dy * dy;
+        if (den > 0.f) {
+            yx[i] = (sx * dx + sy * dy) / den;
+            yy[i] = (sy * dx - sx * dy) / den;
+        } else {
+            yx[i] = 0.f;
+            yy[i] = 0.f;
+        }
+    }
+    for (int i = 0; i < k; ++i) ys[i] = mk<double>((double)yx[i], (double)yy[i]);
+}
+
+struct FzCtl {
+    int j, cont, k, again, passes, ok;
+    double beta, tol_eff;
+};
+
+__global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
+{
+    extern __shared__ __align__(16) unsigned char fz_smem[];
+    __shared__ cxd sc_diff[PG_MAX_SLOTS], sc_negplus[PG_MAX_SLOTS];
+    __shared__ cxf sc_plus[PG_MAX_SLOTS];
+    __shared__ double red[FZ_NW][2 * FZ_CB];
+    __shared__ double hsum[3][FZ_PSTRIDE];
+    __shared__ cxf hs[FZ_MAXM];
+    __shared__ cxd ys[FZ_MAXM];
+    __shared__ FzGivens G;
+    __shared__ FzCtl ctl;
+
+    const int ch = blockIdx.x;                 // angular channel of this CTA (when < nch)
+    const bool owner = ch < a.nch;
+    const int tid = threadIdx.x;
+    const int N = a.N, nblk = a.nblk, w = a.w, npad = nblk * 32;
+    const long long n = (long long)a.nch * N;
+    const long long lo = (long long)ch * n / gridDim.x, hi = (long long)(ch + 1) * n / gridDim.x;  // FP64 rows
+    cxf *xs = (cxf *)fz_smem;                  // [nblk*32] the channel's fibre
+    cxf *sb = xs + (size_t)npad;               // [nblk*w]
+    cxf *sg = sb + (size_t)nblk * w;           // [nblk][w][32] (g_in_smem)
+    const size_t mat = (size_t)(owner ? ch / a.fib_per_mat : 0);
+    cxf *Vc = a.V + (size_t)(owner ? ch : 0) * N;  // V[q][ch] at Vc + q * n
+    const size_t pstride = (size_t)gridDim.x * FZ_PSTRIDE;
+    double *part_me = a.part + (size_t)ch * FZ_PSTRIDE;  // + phase * pstride
+    unsigned int gen = 0;
+    const bool lead = (ch == 0 && tid == 0);  // keeps the step statistics
+
+    if (tid == 0) gen = fz_ld_acquire(&a.bar->gen);
+    if (tid < PG_MAX_SLOTS) {
+        const double hdt = 0.5 * a.params->dt;
+        const cxd h = a.params->h[tid];
+        cxd plus, diff;
+        if (tid == 0) {
+            plus = mk<double>(1.0, 0.0);
+            diff = mk<double>(0.0, 0.0);
+        } else {
+            plus = mk<double>(-hdt * h.y, hdt * h.x);
+            diff = mk<double>(2.0 * hdt * h.y, -2.0 * hdt * h.x);
+        }
+        sc_plus[tid] = cvt<float>(plus);
+        sc_diff[tid] = diff;
+        sc_negplus[tid] = mk<double>(-plus.x, -plus.y);
+    }
+    if (lead) {
+        a.st->stats.iterations = 0;
+        a.st->stats.passes = 0;
+        a.st->stats.true_resid = -1.0;
+        a.st->stats.kernels += 1;
+    }
+    if (tid == 0) ctl.passes = 0;
+    __syncthreads();
+
+    // r = -i dt H psi (FP64); psi is read by all CTAs before the first barrier and only
+    // changed after the second
+    fz_rows64(a.op64, lo, hi, sc_diff, a.psi, a.r64, false);
+    if (!fz_grid_sync(a.bar, gen, a.err, &ctl.ok)) return;
+
+    for (;;) {
+        // d = M^-1 r (complex64), published for the first matvec; ||d||^2
+        if (owner) {
+            for (int i = tid; i < npad; i += FZ_THREADS) {
+                cxf v = mk<float>(0.f, 0.f);
+                if (i < N) {
+                    const cxd r = fz_ldcg(a.r64 + (size_t)ch * N + i);
+                    v = mk<float>((float)r.x, (float)r.y);
+                }
+                xs[i] = v;
+            }
+            __syncthreads();
+            tri_solve_smem<float, cxf, FZ_NW>(nblk, w, mat, a.lo_inv, a.lo_g, a.lo_rb, a.up_inv, a.up_g, a.up_rb, 1,
+                                              1, a.g_in_smem, xs, sb, sg);
+            for (int i = tid; i < N; i += FZ_THREADS) a.wbuf[(size_t)ch * N + i] = xs[i];
+            fz_channel_sums(Vc, n, 0, true, xs, N, red, part_me + P_NRM * pstride);
+        }
+        if (!fz_grid_sync(a.bar, gen, a.err, &ctl.ok)) return;
+        fz_reduce(a.part + P_NRM * pstride, a.nch, 1, hsum[2]);
+        if (tid == 0) {
+            const double b = sqrt(fmax(hsum[2][0], 0.0));
+            ctl.beta = b;
+            ctl.tol_eff = fmax(a.tol, 2e-6 * b);
+            ctl.j = 0;
+            ctl.k = 0;
+            ctl.cont = b > 0.0 ? 1 : 0;
+            ctl.passes += 1;
+            G.g[0] = (float)b;
+            G.g[1] = 0.f;
+            if (lead) {
+                a.st->stats.k = 0;
+                a.st->stats.beta0 = b;
+                a.st->stats.resid = b;
+                a.st->stats.passes = ctl.passes;
+            }
+        }
+        __syncthreads();
+
+        while (ctl.cont) {
+            const int j = ctl.j, J = j + 1;
+            const float s = (float)(ctl.beta > 0.0 ? 1.0 / ctl.beta : 0.0);
+            if (owner) {
+                // V_j = w / beta (this channel), then xs = M^-1 A V_j (row ch)
+                for (int i = tid; i < N; i += FZ_THREADS) {
+                    const cxf v = xs[i];
+                    Vc[(size_t)j * n + i] = mk<float>(v.x * s, v.y * s);
+                }
+                fz_matvec32(a.opb, ch, sc_plus, a.wbuf + (size_t)(j & 1) * n, s, xs, npad);
+                __syncthreads();
+                tri_solve_smem<float, cxf, FZ_NW>(nblk, w, mat, a.lo_inv, a.lo_g, a.lo_rb, a.up_inv, a.up_g, a.up_rb,
+                                                  1, 1, a.g_in_smem, xs, sb, sg);
+                // classical Gram-Schmidt, twice: h1 = <V, w>, w -= V h1, h2 = <V, w>, w -= V h2
+                fz_channel_sums(Vc, n, J, false, xs, N, red, part_me + P_H1 * pstride);
+            }
+            if (!fz_grid_sync(a.bar, gen, a.err, &ctl.ok)) return;
+            fz_reduce(a.part + P_H1 * pstride, a.nch, 2 * J, hsum[0]);
+            for (int rep = 0; rep < 2; ++rep) {
+                if (owner) {
+                    const double *h = hsum[rep];
+                    if (tid < J) hs[tid] = mk<float>((float)h[2 * tid], (float)h[2 * tid + 1]);
+                    __syncthreads();
+                    for (int i = tid; i < N; i += FZ_THREADS) {
+                        cxf acc = xs[i];
+                        for (int q = 0; q < J; ++q) {
+                            const cxf v = Vc[(size_t)q * n + i];
+                            const cxf hc = hs[q];
+                            acc.x = fmaf(-v.x, hc.x, acc.x);
+                            acc.x = fmaf(v.y, hc.y, acc.x);
+                            acc.y = fmaf(-v.x, hc.y, acc.y);
+                            acc.y = fmaf(-v.y, hc.x, acc.y);
+                        }
+                        xs[i] = acc;
+                        if (rep == 1) a.wbuf[(size_t)((j + 1) & 1) * n + (size_t)ch * N + i] = acc;
+                    }
+                    __syncthreads();
+                    fz_channel_sums(Vc, n, J, rep == 1, xs, N, red, part_me + (rep == 0 ? P_H2 : P_H3) * pstride);
+                }
+                if (!fz_grid_sync(a.bar, gen, a.err, &ctl.ok)) return;
+                if (rep == 0) fz_reduce(a.part + P_H2 * pstride, a.nch, 2 * J, hsum[1]);
+                else fz_reduce(a.part + P_H3 * pstride, a.nch, 1, hsum[2]);
+            }
+            if (tid == 0) {
+                const double beta = sqrt(fmax(hsum[2][0], 0.0));
+                const double resid = (double)fz_givens(G, j, hsum[0], hsum[1], beta);
+                const bool bad = !(resid == resid);
+                const bool conv = bad || resid <= ctl.tol_eff || J >= a.m || !(beta > 1e-300);
+                ctl.k = J;
+                ctl.beta = beta;
+                ctl.cont = conv ? 0 : 1;
+                if (!conv) ctl.j = j + 1;
+                if (lead) {
+                    a.st->stats.k = J;
+                    a.st->stats.resid = resid;
+                    a.st->stats.iterations += 1;
+                }
+            }
+            __syncthreads();
+        }
+
+        // e = V y (FP64, this CTA's rows; V read through L2), psi += e, e published
+        if (tid == 0) fz_backsolve(G, ctl.k, ys);
+        __syncthreads();
+        const int k = ctl.k;
+        for (long long o = lo + tid; o < hi; o += FZ_THREADS) {
+            double ax = 0.0, ay = 0.0;
+            for (int q = 0; q < k; ++q) {
+                const cxf v = fz_ldcg(a.V + (size_t)q * n + o);
+                const cxd yq = ys[q];
+                ax = fma((double)v.x, yq.x, ax); ax = fma(-(double)v.y, yq.y, ax);
+                ay = fma((double)v.x, yq.y, ay); ay = fma((double)v.y, yq.x, ay);
+            }
+            a.e64[o] = mk<double>(ax, ay);
+            a.psi[o] = a.psi[o] + mk<double>(ax, ay);
+        }
+        if (!fz_grid_sync(a.bar, gen, a.err, &ctl.ok)) return;
+        // r -= (S + i dt/2 H) e in FP64; ||r|| decides whether another pass runs
+        const double rn = fz_rows64(a.op64, lo, hi, sc_negplus, a.e64, a.r64, true);
+        fz_cta_sum64(rn, red, part_me + P_RES * pstride);
+        if (!fz_grid_sync(a.bar, gen, a.err, &ctl.ok)) return;
+        fz_reduce(a.part + P_RES * pstride, gridDim.x, 1, hsum[2]);
+        if (tid == 0) {
+            const double r = sqrt(fmax(hsum[2][0], 0.0));
+            ctl.again = (r > a.tol) && (r == r) && ctl.passes < FZ_MAXPASS;
+            if (lead) a.st->stats.true_resid = r;
+        }
+        __syncthreads();
+        if (!ctl.again) break;
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// host
+// ------------------------------------------------------------------------------------
+struct FusedCayley {
+    FzArgs args;
+    size_t smem = 0;
+    int nctas = 0;
+};
+
+static size_t fz_smem_bytes(int nblk, int w, int g_in_smem)
+{
+    return ((size_t)nblk * 32 + (size_t)nblk * w * (g_in_smem ? 33 : 1)) * sizeof(cxf);
+}
+
+int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, FusedCayley **out)
+{
+    if (!out) return PG_ERR_ARG;
+    *out = nullptr;
+    if (!op64 || !opb || !precb) return PG_ERR_ARG;
+    if (m < 2 || m > FZ_MAXM) return PG_ERR_SHAPE;
+    if (op64->rank != 2 || opb->rank != 2 || opb->precision != PG_FP32 || op64->precision != PG_FP64)
+        return PG_ERR_STORAGE;
+    if (!op64->finalized || !opb->finalized) return PG_ERR_STATE;
+    if (op64->ndense_entries > 0 || opb->ndense_entries > 0 || op64->fact.Q > 0 || opb->fact.Q > 0)
+        return PG_ERR_STORAGE;
+    if (!op64->d_bands || !opb->d_bands || op64->nrows != opb->nrows || op64->N != opb->N || op64->kb != opb->kb)
+        return PG_ERR_STORAGE;
+    if (precb->kind != 1 || precb->op != opb || precb->N != opb->N || precb->kb < 1 || precb->kb > 32)
+        return PG_ERR_STORAGE;
+    pg_ctx *ctx = opb->ctx;
+    const int N = opb->N, nch = opb->nrows, nblk = (N + 31) / 32, w = precb->kb;
+    if (nch < 1 || N < 1) return PG_ERR_SHAPE;
+    const size_t limit = 200 * 1024;
+    int g_in_smem = 1;
+    size_t smem = fz_smem_bytes(nblk, w, 1);
+    if (smem > limit) {
+        g_in_smem = 0;
+        smem = fz_smem_bytes(nblk, w, 0);
+        if (smem > limit) return PG_ERR_SHAPE;
+    }
+    PG_CUDA_TRY(cudaFuncSetAttribute(cay_fused_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cay_fused_step_kernel, FZ_THREADS, smem));
+    const int resident = per_sm * std::max(1, ctx->num_sms);
+    if (per_sm < 1 || nch > resident) return PG_ERR_SHAPE;  // every CTA must be resident at once
+    // one CTA per SM: the channels, and the FP64 rows spread over all of them
+    const int nctas = std::max(nch, std::min(resident, std::max(1, ctx->num_sms)));
+
+    FusedCayley *f = new FusedCayley();
+    FzArgs &a = f->args;
+    memset(&a, 0, sizeof(a));
+    a.op64 = op64->dev();
+    a.opb = opb->dev();
+    a.lo_inv = (const cxf *)precb->d_lo_inv;
+    a.lo_g = (const cxf *)precb->d_lo_cpl;
+    a.lo_rb = (const cxf *)precb->d_lo_rb;
+    a.up_inv = (const cxf *)precb->d_up_inv;
+    a.up_g = (const cxf *)precb->d_up_cpl;
+    a.up_rb = (const cxf *)precb->d_up_rb;
+    a.nblk = nblk;
+    a.w = w;
+    a.fib_per_mat = std::max(1, precb->fib_per_mat);
+    a.g_in_smem = g_in_smem;
+    a.nch = nch;
+    a.N = N;
+    a.m = m;
+    const size_t n = (size_t)nch * N;
+    int code = PG_OK;
+    auto alloc = [&](void **p, size_t bytes) {
+        if (code == PG_OK && cudaMalloc(p, bytes) != cudaSuccess) code = PG_ERR_CUDA;
+    };
+    alloc((void **)&a.r64, sizeof(cxd) * n);
+    alloc((void **)&a.e64, sizeof(cxd) * n);
+    alloc((void **)&a.wbuf, sizeof(cxf) * 2 * n);
+    alloc((void **)&a.V, sizeof(cxf) * (size_t)m * n);
+    alloc((void **)&a.part, sizeof(double) * P_COUNT * (size_t)nctas * FZ_PSTRIDE);
+    alloc((void **)&a.bar, sizeof(FzBarrier));
+    if (code != PG_OK) {
+        pg_cayley_fused_free(f);
+        return code;
+    }
+    f->smem = smem;
+    f->nctas = nctas;
+    *out = f;
+    return PG_OK;
+}
+
+int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams *params, cxd *psi, GmresState *st,
+                           double tol, int *err)
+{
+    FzArgs a = f->args;
+    a.params = params;
+    a.psi = psi;
+    a.st = st;
+    a.tol = tol;
+    a.err = err;
+    // a barrier left half-way by an earlier launch whose wait ran out starts from zero again
+    PG_CUDA_TRY(cudaMemsetAsync(a.bar, 0, sizeof(FzBarrier), s));
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(f->nctas);
+    cfg.blockDim = dim3(FZ_THREADS);
+    cfg.dynamicSmemBytes = f->smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, cay_fused_step_kernel, a));
+    return PG_OK;
+}
+
+void pg_cayley_fused_free(FusedCayley *f)
+{
+    if (!f) return;
+    cudaFree(f->args.r64);
+    cudaFree(f->args.e64);
+    cudaFree(f->args.wbuf);
+    cudaFree(f->args.V);
+    cudaFree(f->args.part);
+    cudaFree(f->args.bar);
+    delete f;
+}

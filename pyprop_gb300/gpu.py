@@ -66,6 +66,13 @@ class Context:
     def synchronize(self):
         check(self.lib.pg_ctx_synchronize(self.h), "pg_ctx_synchronize")
 
+    def device_error(self):
+        """The device error flag (0: clear; set by a bounded wait that ran out). Waits."""
+        flag = C.c_int(0)
+        self.bind_stream()
+        check(self.lib.pg_ctx_device_error(self.h, C.byref(flag)), "pg_ctx_device_error")
+        return int(flag.value)
+
 
 def complex_dtype(precision):
     t = torch()
@@ -388,6 +395,15 @@ class CayleyStepper:
     def set_eager(self, on):
         """Host-driven loops instead of the graph's conditional nodes (for profilers)."""
         check(self.lib.pg_cayley_set_eager(self.h, int(bool(on))), "pg_cayley_set_eager")
+
+    def set_fused(self, on):
+        """Single-kernel mixed step (the default where the operators qualify) or the captured
+        multi-kernel step. Returns whether the single-kernel step is now selected."""
+        code = self.lib.pg_cayley_set_fused(self.h, int(bool(on)))
+        if on and code == nat.PG_ERR_STATE:
+            return False
+        check(code, "pg_cayley_set_fused")
+        return bool(on)
 
     def __del__(self):
         try:

@@ -11,7 +11,9 @@
 A config switches to these by naming them: ``propagator = PamPropagatorGPU`` or
 ``CayleyPropagatorGPU``, ``base_propagator = BasisPropagatorGPU`` (``BasisPropagator`` is
 accepted as the same class). GPU-only keys in [Propagation]: ``gpu_precision``
-("fp64" or "fp32": precision of the Krylov basis and of the operator it multiplies).
+("fp64" or "fp32": precision of the Krylov basis and of the operator it multiplies);
+``gpu_fused_step`` (default True: a mixed-precision Cayley step of a one-electron banded
+operator runs as one cooperative kernel; False keeps the captured multi-kernel step).
 """
 from __future__ import annotations
 
@@ -336,6 +338,9 @@ class CayleyPropagatorGPU(PropagatorBase):
         self.StepStats = bool(getattr(conf, "gpu_step_stats", True))
         self.TrueResidual = bool(getattr(conf, "gpu_true_residual", False))
         self.Eager = bool(getattr(conf, "gpu_eager", False))
+        # mixed precision, rank-2 banded operator: the whole step as one kernel unless
+        # gpu_fused_step = False
+        self.FusedStep = bool(getattr(conf, "gpu_fused_step", True))
         # mixed precision: the FP64 residual operator computes its factorized (two-electron)
         # terms in double-float arithmetic unless gpu_fp64_emulation = False
         self.Fp64Emulation = bool(getattr(conf, "gpu_fp64_emulation", True))
@@ -366,6 +371,7 @@ class CayleyPropagatorGPU(PropagatorBase):
                                      self.Tolerance, self.TrueResidual)
         if self.Eager:
             self.stepper.set_eager(True)
+        self.Fused = self.stepper.set_fused(self.FusedStep and not self.Eager)
 
     def AdvanceStep(self, t, dt):
         """One step at H(t + |dt|/2). With ``gpu_step_stats`` (default) the call waits for the

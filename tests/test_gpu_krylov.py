@@ -92,6 +92,63 @@ def test_cayley_mixed_precision_against_oracle(gpu):
     assert infidelity(psi_ref, out, ham.overlap.S) < 1e-14
 
 
+def test_cayley_single_kernel_step_matches_multi_kernel_step(gpu):
+    """The mixed step of a one-electron banded operator runs as one cooperative kernel by
+    default; the captured multi-kernel step runs the same scheme. Both reach the FP64 true
+    residual bound every step and agree to the GMRES tolerance; the single-kernel stepper
+    counts one kernel per step and leaves the device error flag clear."""
+    g = golden("hydrogen_small.npz")
+    t0, dt, nsteps = 1.0, 0.01, 10
+    states = {}
+    for fused in (True, False):
+        prob = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp32", gmres_tolerance=1e-12)
+        prob.Propagator.FusedStep = fused
+        prob.SetupStep(skipWavefunctionSetup=True)
+        assert prob.Propagator.Fused == fused
+        _set_psi(prob, g["psi"])
+        ctx = prob.Propagator.op64.ctx
+        k0 = ctx.launches()
+        for n in range(nsteps):
+            prob.Propagator.AdvanceStep(t0 + n * dt, dt)
+            st = prob.Propagator.LastStats
+            assert st.TrueResidual < 1e-12 and 1 <= st.Iterations <= 40
+        if fused:
+            assert ctx.launches() - k0 == nsteps
+            assert ctx.device_error() == 0
+        states[fused] = prob.psi.numpy()
+    assert relerr(states[True], states[False]) < 1e-10
+
+
+def test_cayley_single_kernel_step_long_fibres_and_basis_bound(gpu):
+    """Fibres longer than one CTA's threads (N = 1000: several rows per thread) step on the
+    single-kernel path to the same bound; a Krylov basis above its bound (32) keeps the
+    multi-kernel step."""
+    nang, N = 6, 1000
+    i = np.arange(N)
+    psi = np.zeros((nang, N), complex)
+    psi[0] = np.exp(-((i - 150.0) / 60.0) ** 2)
+    psi[1] = 0.3j * np.exp(-((i - 200.0) / 80.0) ** 2)
+    psi /= np.linalg.norm(psi)
+    prob = hydrogen_problem(lmax=nang - 1, nbsplines=N, rmax=200.0, propagator="CayleyPropagatorGPU",
+                            precision="fp32", gmres_tolerance=1e-12)
+    prob.SetupStep(skipWavefunctionSetup=True)
+    assert prob.Propagator.Fused
+    ref = hydrogen_problem(lmax=nang - 1, nbsplines=N, rmax=200.0, propagator="CayleyPropagatorGPU",
+                           precision="fp32", gmres_tolerance=1e-12)
+    ref.Propagator.FusedStep = False
+    ref.SetupStep(skipWavefunctionSetup=True)
+    _set_psi(prob, psi)
+    _set_psi(ref, psi)
+    for n in range(4):
+        for p in (prob, ref):
+            p.Propagator.AdvanceStep(1.0 + 0.01 * n, 0.01)
+            assert p.Propagator.LastStats.TrueResidual < 1e-12
+    assert relerr(prob.psi.numpy(), ref.psi.numpy()) < 1e-10
+    big = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp32", krylov_basis_size=40)
+    big.SetupStep(skipWavefunctionSetup=True)
+    assert not big.Propagator.Fused
+
+
 def test_piram_ground_state_shift_invert(gpu):
     """Config-1 model (lmax 10, N 150): shift-invert pIRAM ground state E = -1/2."""
     import pyprop_gb300 as pp
