@@ -332,7 +332,9 @@ int pg_cayley_set_eager(pg_cayley *c, int on);
  * (no dense or factorized terms) with the block-diagonal LU preconditioner, basis_size <= 32
  * and no more channels than resident CTAs; the learned preconditioner and the eager mode
  * use the multi-kernel step. on = 0 selects the multi-kernel step; on = 1 on a stepper that
- * does not qualify returns PG_ERR_STATE. Replaces the same reference step as
+ * does not qualify returns why: PG_ERR_STATE (not PG_FP32), PG_ERR_STORAGE (operator or
+ * preconditioner kind), PG_ERR_SHAPE (basis size, fibre length, channel count). Replaces the
+ * same reference step as
  * pg_cayley_step (CayleyPropagator.py:71-150). */
 int pg_cayley_set_fused(pg_cayley *c, int on);
 /*

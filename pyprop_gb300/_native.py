@@ -23,6 +23,8 @@ PG_BAND_SOLVE_UT = 3
 PG_BAND_MUL_S = 4
 PG_BAND_SOLVE_S = 5
 PG_BAND_PREC_SOLVE = 6
+PG_ERR_STORAGE = -3
+PG_ERR_SHAPE = -4
 PG_ERR_STATE = -9
 
 ERRORS = {

@@ -388,6 +388,7 @@ struct pg_cayley {
     cxd *rn64 = nullptr;
     // single-kernel mixed step (cayley_fused.cu), when the operators qualify
     FusedCayley *fused = nullptr;
+    int fused_status = PG_ERR_STATE;  // why the single-kernel step is unavailable (PG_OK: it is)
     bool use_fused = true;
 };
 
@@ -728,9 +729,12 @@ extern "C" int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64,
     for (int k = 0; k < 3; ++k) PG_CUDA_TRY(cudaStreamCreateWithFlags(&c->cap[k], cudaStreamNonBlocking));
     // rank-2 banded operators with the block LU preconditioner run the mixed step as one
     // kernel; anything else (or a failed check) keeps the captured multi-kernel step
-    if (basis_precision == PG_FP32 && pg_cayley_fused_prepare(op64, op_basis, prec_basis, c->m, &c->fused) != PG_OK) {
-        c->fused = nullptr;
-        cudaGetLastError();
+    if (basis_precision == PG_FP32) {
+        c->fused_status = pg_cayley_fused_prepare(op64, op_basis, prec_basis, c->m, &c->fused);
+        if (c->fused_status != PG_OK) {
+            c->fused = nullptr;
+            cudaGetLastError();
+        }
     }
     *out = c;
     return PG_OK;
@@ -874,11 +878,13 @@ extern "C" int pg_cayley_set_eager(pg_cayley *c, int on)
 }
 
 // Single-kernel mixed step on (the default where the operators qualify) or off (the
-// captured multi-kernel step). PG_ERR_STATE when switching on a stepper that does not qualify.
+// captured multi-kernel step). Switching it on for a stepper that does not qualify returns
+// the reason (PG_ERR_STATE: not a mixed-precision stepper; PG_ERR_STORAGE: operator or
+// preconditioner kind; PG_ERR_SHAPE: basis size, fibre length or channel count).
 extern "C" int pg_cayley_set_fused(pg_cayley *c, int on)
 {
     if (!c) return PG_ERR_ARG;
-    if (on && !c->fused) return PG_ERR_STATE;
+    if (on && !c->fused) return c->fused_status != PG_OK ? c->fused_status : PG_ERR_STATE;
     c->use_fused = on != 0;
     return PG_OK;
 }

@@ -565,7 +565,8 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
         return PG_ERR_STORAGE;
     if (!op64->d_bands || !opb->d_bands || op64->nrows != opb->nrows || op64->N != opb->N || op64->kb != opb->kb)
         return PG_ERR_STORAGE;
-    if (precb->kind != 1 || precb->op != opb || precb->N != opb->N || precb->kb < 1 || precb->kb > 32)
+    if (precb->kind != 1 || !precb->op || precb->op->precision != PG_FP32 || precb->op->nrows != opb->nrows ||
+        precb->N != opb->N || precb->kb < 1 || precb->kb > 32)
         return PG_ERR_STORAGE;
     pg_ctx *ctx = opb->ctx;
     const int N = opb->N, nch = opb->nrows, nblk = (N + 31) / 32, w = precb->kb;

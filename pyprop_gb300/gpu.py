@@ -400,7 +400,8 @@ class CayleyStepper:
         """Single-kernel mixed step (the default where the operators qualify) or the captured
         multi-kernel step. Returns whether the single-kernel step is now selected."""
         code = self.lib.pg_cayley_set_fused(self.h, int(bool(on)))
-        if on and code == nat.PG_ERR_STATE:
+        self.fused_status = code
+        if on and code in (nat.PG_ERR_STATE, nat.PG_ERR_STORAGE, nat.PG_ERR_SHAPE):
             return False
         check(code, "pg_cayley_set_fused")
         return bool(on)

@@ -104,7 +104,7 @@ def test_cayley_single_kernel_step_matches_multi_kernel_step(gpu):
         prob = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp32", gmres_tolerance=1e-12)
         prob.Propagator.FusedStep = fused
         prob.SetupStep(skipWavefunctionSetup=True)
-        assert prob.Propagator.Fused == fused
+        assert prob.Propagator.Fused == fused, prob.Propagator.stepper.fused_status
         _set_psi(prob, g["psi"])
         ctx = prob.Propagator.op64.ctx
         k0 = ctx.launches()
