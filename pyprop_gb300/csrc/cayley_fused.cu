@@ -32,16 +32,23 @@ static const int FZ_MAXM = 32;               // Krylov basis bound of the single
 static const int FZ_CB = 8;                  // columns per register block of the channel sums
 static const int FZ_MAXPASS = 4;             // refinement passes (as the multi-kernel step)
 static const int FZ_PSTRIDE = 2 * (FZ_MAXM + 1);
-static const unsigned int FZ_POLLS = 1u << 24;  // barrier polls (>= 64 ns each) before giving up
+static const int FZ_MAXU = 4;                // distinct source channels per operator row (staged)
+static const unsigned int FZ_POLLS = 1u << 22;  // barrier polls (each an L2 round trip) before giving up
 enum { P_NRM = 0, P_H1 = 1, P_H2 = 2, P_H3 = 3, P_RES = 4, P_COUNT = 5 };
 
 struct FzBarrier {
-    unsigned int count;
-    unsigned int gen;
+    unsigned int count;  // arrivals during the current launch
+    unsigned int pad;
 };
 
 struct FzArgs {
-    OpDev op64, opb;
+    OpDev op64, opb;             // structure (rows, entries, slots); the bands are the real copies below
+    const double *rb64;          // [bands][2kb+1][ld] real FP64 bands of op64
+    const float *rb32;           // [bands][2kb+1][ld] real FP32 bands of opb
+    const int *ucol;             // [Nang][FZ_MAXU] distinct source channels of each row of opb
+    const int *nucol;            // [Nang] how many
+    const unsigned char *ent_u;  // [entries of opb] which staged source an entry reads
+    const int *row_lo;           // [CTAs + 1] FP64 rows of each CTA (equal numbers of band entries)
     const cxf *lo_inv, *lo_g, *lo_rb, *up_inv, *up_g, *up_rb;
     int nblk, w, fib_per_mat, g_in_smem;
     int nch, N, m;
@@ -65,29 +72,24 @@ __device__ __forceinline__ unsigned int fz_ld_acquire(const unsigned int *p)
     return v;
 }
 
-// All CTAs meet (the launch is cooperative, so all are resident). Returns false, CTA-uniform,
-// when the wait ran out; the error flag is then set.
-__device__ __forceinline__ bool fz_grid_sync(FzBarrier *bar, unsigned int &gen, int *err, int *s_ok)
+// All CTAs meet (the launch is cooperative, so all are resident): the arrival count only
+// grows during a launch (it is zeroed before each), the k-th barrier completes when it
+// reaches k * gridDim.x. Returns false, CTA-uniform, when the wait ran out; the error flag is
+// then set.
+__device__ __forceinline__ bool fz_grid_sync(FzBarrier *bar, unsigned int &target, int *err, int *s_ok)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
+        target += gridDim.x;
         __threadfence();
-        const unsigned int arrived = atomicAdd(&bar->count, 1u) + 1u;
-        if (arrived == gridDim.x) {
-            atomicExch(&bar->count, 0u);
-            __threadfence();
-            atomicAdd(&bar->gen, 1u);
-        } else {
-            unsigned int polls = 0;
-            while (fz_ld_acquire(&bar->gen) == gen) {
-                if (++polls > FZ_POLLS) { ok = 0; break; }
-                __nanosleep(64);
-            }
+        atomicAdd(&bar->count, 1u);
+        unsigned int polls = 0;
+        while (fz_ld_acquire(&bar->count) < target) {
+            if (++polls > FZ_POLLS) { ok = 0; break; }
+            __nanosleep(32);
         }
         if (!ok) atomicExch(err, 2);
-        gen += 1u;
-        __threadfence();
         *s_ok = ok;
     }
     __syncthreads();
@@ -177,10 +179,11 @@ __device__ __forceinline__ void fz_channel_sums(const cxf *Vc, long long ldv, in
             }
         }
         __syncthreads();
-        if (threadIdx.x < 2 * FZ_CB && j0 + (int)threadIdx.x / 2 < ncol) {
-            double s = 0.0;
-            for (int q = 0; q < FZ_NW; ++q) s += red[q][threadIdx.x];
-            out[2 * j0 + threadIdx.x] = s;
+        // warp v sums value v over the warps (lanes), a shuffle tree in FP64
+        if (warp < 2 * FZ_CB && j0 + warp / 2 < ncol) {
+            double s = lane < FZ_NW ? red[lane][warp] : 0.0;
+            s = fz_warp_sum(s);
+            if (lane == 0) out[2 * j0 + warp] = s;
         }
         __syncthreads();
     }
@@ -188,26 +191,42 @@ __device__ __forceinline__ void fz_channel_sums(const cxf *Vc, long long ldv, in
 
 // FP64 rows [lo, hi) of the flattened [Nang][N] operator applied to src (read through L2:
 // other CTAs write it): r[o] (+)= sum_e sc[slot_e] sum_d band_e[d][i] src[col_e][i + d - kb],
-// o = a N + i. Returns this thread's share of ||r||^2 over its rows.
-__device__ __forceinline__ double fz_rows64(const OpDev &op, long long lo, long long hi, const cxd *sc,
-                                            const cxd *src, cxd *r, bool accumulate)
+// o = a N + i, real bands. Returns this thread's share of ||r||^2 over its rows.
+template <int KB>
+__device__ __forceinline__ double fz_rows64(const OpDev &op, const double *__restrict__ rb, long long lo, long long hi,
+                                            const cxd *sc, const cxd *src, cxd *r, bool accumulate)
 {
-    const int N = op.N, kb = op.kb, b = op.b, ld = op.ld;
-    const cxd *bands = (const cxd *)op.bands;
+    const int N = op.N, kb = KB >= 0 ? KB : op.kb, b = 2 * kb + 1, ld = op.ld;
     double nrm = 0.0;
     for (long long o = lo + threadIdx.x; o < hi; o += FZ_THREADS) {
         const int a = (int)(o / N), i = (int)(o - (long long)a * N);
         const int e0 = __ldg(op.row_ptr + a), e1 = __ldg(op.row_ptr + a + 1);
         cxd acc = mk<double>(0.0, 0.0);
         for (int e = e0; e < e1; ++e) {
-            const cxd *B = bands + (size_t)__ldg(op.ent_band + e) * b * ld;
-            const cxd *x = src + (size_t)__ldg(op.ent_col + e) * N;
-            cxd t = mk<double>(0.0, 0.0);
-            for (int d = 0; d < b; ++d) {
-                const int j = i + d - kb;
-                if (j >= 0 && j < N) cfma(t, fz_ldg(B + (size_t)d * ld + i), fz_ldcg(x + j));
+            const cxd se = sc[__ldg(op.ent_slot + e)];
+            if (se.x == 0.0 && se.y == 0.0) continue;  // e.g. the overlap in -i dt H psi
+            const double *B = rb + (size_t)__ldg(op.ent_band + e) * b * ld + i;
+            const cxd *x = src + (size_t)__ldg(op.ent_col + e) * N + i - kb;
+            double tx = 0.0, ty = 0.0;
+            if (KB >= 0) {
+#pragma unroll
+                for (int d = 0; d < 2 * KB + 1; ++d)
+                    if (i + d - kb >= 0 && i + d - kb < N) {
+                        const double c = __ldg(B + (size_t)d * ld);
+                        const cxd v = fz_ldcg(x + d);
+                        tx = fma(c, v.x, tx);
+                        ty = fma(c, v.y, ty);
+                    }
+            } else {
+                for (int d = 0; d < b; ++d)
+                    if (i + d - kb >= 0 && i + d - kb < N) {
+                        const double c = __ldg(B + (size_t)d * ld);
+                        const cxd v = fz_ldcg(x + d);
+                        tx = fma(c, v.x, tx);
+                        ty = fma(c, v.y, ty);
+                    }
             }
-            cfma(acc, sc[__ldg(op.ent_slot + e)], t);
+            cfma(acc, se, mk<double>(tx, ty));
         }
         if (accumulate) acc = acc + fz_ldcg(r + o);
         r[o] = acc;
@@ -224,37 +243,75 @@ __device__ __forceinline__ void fz_cta_sum64(double v, double (*red)[2 * FZ_CB],
     v = fz_warp_sum(v);
     if (lane == 0) red[warp][0] = v;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int q = 0; q < FZ_NW; ++q) s += red[q][0];
-        out[0] = s;
+    if (warp == 0) {
+        double s = lane < FZ_NW ? red[lane][0] : 0.0;
+        s = fz_warp_sum(s);
+        if (lane == 0) out[0] = s;
     }
     __syncthreads();
 }
 
-// complex64 operator row a applied to the normalised vector wsrc * s (wsrc read through
-// L2); xs[i] = result for i < N, zero on the padding up to npad
-__device__ __forceinline__ void fz_matvec32(const OpDev &op, int a, const cxf *sc, const cxf *wsrc, float s, cxf *xs,
-                                            int npad)
+// complex64 operator row a applied to the normalised vector wsrc * s: the row's distinct
+// source fibres are staged (scaled, with a zero halo of kb) in xsrc, then thread i forms
+// xs[i] = sum_e sc[slot_e] sum_d band_e[d][i] x_e[i + d - kb] from real bands (L1-cached:
+// the same rows are read every iteration); zero on the padding up to npad.
+template <int KB>
+__device__ __forceinline__ void fz_matvec32(const FzArgs &A, int a, const cxf *sc, const cxf *wsrc, float s, cxf *xs,
+                                            int npad, cxf *xsrc)
 {
-    const int N = op.N, kb = op.kb, b = op.b, ld = op.ld;
-    const cxf *bands = (const cxf *)op.bands;
+    const OpDev &op = A.opb;
+    const int N = op.N, kb = KB >= 0 ? KB : op.kb, b = 2 * kb + 1, ld = op.ld, W = N + 2 * kb;
+    const int nu = __ldg(A.nucol + a);
+    for (int u = 0; u < nu; ++u) {
+        const cxf *x = wsrc + (size_t)__ldg(A.ucol + (size_t)a * FZ_MAXU + u) * N;
+        for (int q = threadIdx.x; q < W; q += FZ_THREADS) {
+            const int j = q - kb;
+            cxf v = mk<float>(0.f, 0.f);
+            if (j >= 0 && j < N) {
+                v = fz_ldcg(x + j);
+                v = mk<float>(v.x * s, v.y * s);
+            }
+            xsrc[(size_t)u * W + q] = v;
+        }
+    }
+    __syncthreads();
     const int e0 = __ldg(op.row_ptr + a), e1 = __ldg(op.row_ptr + a + 1);
     for (int i = threadIdx.x; i < npad; i += FZ_THREADS) {
         cxf acc = mk<float>(0.f, 0.f);
         if (i < N) {
-            for (int e = e0; e < e1; ++e) {
-                const cxf *B = bands + (size_t)__ldg(op.ent_band + e) * b * ld;
-                const cxf *x = wsrc + (size_t)__ldg(op.ent_col + e) * N;
-                cxf t = mk<float>(0.f, 0.f);
-                for (int d = 0; d < b; ++d) {
-                    const int j = i + d - kb;
-                    if (j >= 0 && j < N) {
-                        const cxf v = fz_ldcg(x + j);
-                        cfma(t, fz_ldg(B + (size_t)d * ld + i), mk<float>(v.x * s, v.y * s));
+            for (int e = e0; e < e1; e += 2) {
+                // two entries at a time: 2(2kb+1) band loads in flight
+                const bool two = e + 1 < e1;
+                const float *B0 = A.rb32 + (size_t)__ldg(op.ent_band + e) * b * ld + i;
+                const float *B1 = A.rb32 + (size_t)__ldg(op.ent_band + (two ? e + 1 : e)) * b * ld + i;
+                const cxf *x0 = xsrc + (size_t)__ldg(A.ent_u + e) * W + i;  // x[d] = x_e[i + d - kb]
+                const cxf *x1 = xsrc + (size_t)__ldg(A.ent_u + (two ? e + 1 : e)) * W + i;
+                float t0x = 0.f, t0y = 0.f, t1x = 0.f, t1y = 0.f;
+                if (KB >= 0) {
+                    float c0[2 * (KB > 0 ? KB : 0) + 1], c1[2 * (KB > 0 ? KB : 0) + 1];
+#pragma unroll
+                    for (int d = 0; d < 2 * KB + 1; ++d) {
+                        c0[d] = __ldg(B0 + (size_t)d * ld);
+                        c1[d] = __ldg(B1 + (size_t)d * ld);
+                    }
+#pragma unroll
+                    for (int d = 0; d < 2 * KB + 1; ++d) {
+                        t0x = fmaf(c0[d], x0[d].x, t0x);
+                        t0y = fmaf(c0[d], x0[d].y, t0y);
+                        t1x = fmaf(c1[d], x1[d].x, t1x);
+                        t1y = fmaf(c1[d], x1[d].y, t1y);
+                    }
+                } else {
+                    for (int d = 0; d < b; ++d) {
+                        const float c = __ldg(B0 + (size_t)d * ld), c2 = __ldg(B1 + (size_t)d * ld);
+                        t0x = fmaf(c, x0[d].x, t0x);
+                        t0y = fmaf(c, x0[d].y, t0y);
+                        t1x = fmaf(c2, x1[d].x, t1x);
+                        t1y = fmaf(c2, x1[d].y, t1y);
                     }
                 }
-                cfma(acc, sc[__ldg(op.ent_slot + e)], t);
+                cfma(acc, sc[__ldg(op.ent_slot + e)], mk<float>(t0x, t0y));
+                if (two) cfma(acc, sc[__ldg(op.ent_slot + e + 1)], mk<float>(t1x, t1y));
             }
         }
         xs[i] = acc;
@@ -348,8 +405,10 @@ __device__ void fz_backsolve(const FzGivens &G, int k, cxd *ys)
 struct FzCtl {
     int j, cont, k, again, passes, ok;
     double beta, tol_eff;
+    float s;  // 1/beta for the next Krylov vector (formed once: FP64 division is slow here)
 };
 
+template <int KB>
 __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
 {
     extern __shared__ __align__(16) unsigned char fz_smem[];
@@ -367,18 +426,18 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
     const int tid = threadIdx.x;
     const int N = a.N, nblk = a.nblk, w = a.w, npad = nblk * 32;
     const long long n = (long long)a.nch * N;
-    const long long lo = (long long)ch * n / gridDim.x, hi = (long long)(ch + 1) * n / gridDim.x;  // FP64 rows
+    const long long lo = __ldg(a.row_lo + ch), hi = __ldg(a.row_lo + ch + 1);  // FP64 rows of this CTA
     cxf *xs = (cxf *)fz_smem;                  // [nblk*32] the channel's fibre
     cxf *sb = xs + (size_t)npad;               // [nblk*w]
     cxf *sg = sb + (size_t)nblk * w;           // [nblk][w][32] (g_in_smem)
+    cxf *xsrc = sg + (a.g_in_smem ? (size_t)nblk * w * 32 : 0);  // [FZ_MAXU][N + 2kb] staged sources
     const size_t mat = (size_t)(owner ? ch / a.fib_per_mat : 0);
     cxf *Vc = a.V + (size_t)(owner ? ch : 0) * N;  // V[q][ch] at Vc + q * n
     const size_t pstride = (size_t)gridDim.x * FZ_PSTRIDE;
     double *part_me = a.part + (size_t)ch * FZ_PSTRIDE;  // + phase * pstride
-    unsigned int gen = 0;
+    unsigned int expect = 0;  // barrier arrivals expected so far (thread 0)
     const bool lead = (ch == 0 && tid == 0);  // keeps the step statistics
 
-    if (tid == 0) gen = fz_ld_acquire(&a.bar->gen);
     if (tid < PG_MAX_SLOTS) {
         const double hdt = 0.5 * a.params->dt;
         const cxd h = a.params->h[tid];
@@ -405,8 +464,8 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
 
     // r = -i dt H psi (FP64); psi is read by all CTAs before the first barrier and only
     // changed after the second
-    fz_rows64(a.op64, lo, hi, sc_diff, a.psi, a.r64, false);
-    if (!fz_grid_sync(a.bar, gen, a.err, &ctl.ok)) return;
+    fz_rows64<KB>(a.op64, a.rb64, lo, hi, sc_diff, a.psi, a.r64, false);
+    if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
 
     for (;;) {
         // d = M^-1 r (complex64), published for the first matvec; ||d||^2
@@ -425,11 +484,12 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
             for (int i = tid; i < N; i += FZ_THREADS) a.wbuf[(size_t)ch * N + i] = xs[i];
             fz_channel_sums(Vc, n, 0, true, xs, N, red, part_me + P_NRM * pstride);
         }
-        if (!fz_grid_sync(a.bar, gen, a.err, &ctl.ok)) return;
+        if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
         fz_reduce(a.part + P_NRM * pstride, a.nch, 1, hsum[2]);
         if (tid == 0) {
             const double b = sqrt(fmax(hsum[2][0], 0.0));
             ctl.beta = b;
+            ctl.s = (float)(b > 0.0 ? 1.0 / b : 0.0);
             ctl.tol_eff = fmax(a.tol, 2e-6 * b);
             ctl.j = 0;
             ctl.k = 0;
@@ -448,21 +508,21 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
 
         while (ctl.cont) {
             const int j = ctl.j, J = j + 1;
-            const float s = (float)(ctl.beta > 0.0 ? 1.0 / ctl.beta : 0.0);
+            const float s = ctl.s;
             if (owner) {
                 // V_j = w / beta (this channel), then xs = M^-1 A V_j (row ch)
                 for (int i = tid; i < N; i += FZ_THREADS) {
                     const cxf v = xs[i];
                     Vc[(size_t)j * n + i] = mk<float>(v.x * s, v.y * s);
                 }
-                fz_matvec32(a.opb, ch, sc_plus, a.wbuf + (size_t)(j & 1) * n, s, xs, npad);
+                fz_matvec32<KB>(a, ch, sc_plus, a.wbuf + (size_t)(j & 1) * n, s, xs, npad, xsrc);
                 __syncthreads();
                 tri_solve_smem<float, cxf, FZ_NW>(nblk, w, mat, a.lo_inv, a.lo_g, a.lo_rb, a.up_inv, a.up_g, a.up_rb,
                                                   1, 1, a.g_in_smem, xs, sb, sg);
                 // classical Gram-Schmidt, twice: h1 = <V, w>, w -= V h1, h2 = <V, w>, w -= V h2
                 fz_channel_sums(Vc, n, J, false, xs, N, red, part_me + P_H1 * pstride);
             }
-            if (!fz_grid_sync(a.bar, gen, a.err, &ctl.ok)) return;
+            if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
             fz_reduce(a.part + P_H1 * pstride, a.nch, 2 * J, hsum[0]);
             for (int rep = 0; rep < 2; ++rep) {
                 if (owner) {
@@ -485,17 +545,20 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                     __syncthreads();
                     fz_channel_sums(Vc, n, J, rep == 1, xs, N, red, part_me + (rep == 0 ? P_H2 : P_H3) * pstride);
                 }
-                if (!fz_grid_sync(a.bar, gen, a.err, &ctl.ok)) return;
+                if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
                 if (rep == 0) fz_reduce(a.part + P_H2 * pstride, a.nch, 2 * J, hsum[1]);
                 else fz_reduce(a.part + P_H3 * pstride, a.nch, 1, hsum[2]);
             }
             if (tid == 0) {
-                const double beta = sqrt(fmax(hsum[2][0], 0.0));
+                // |w| in FP32 (it enters the Hessenberg matrix and the next vector as FP32)
+                const float fb = sqrtf(fmaxf((float)hsum[2][0], 0.f));
+                const double beta = (double)fb;
                 const double resid = (double)fz_givens(G, j, hsum[0], hsum[1], beta);
                 const bool bad = !(resid == resid);
                 const bool conv = bad || resid <= ctl.tol_eff || J >= a.m || !(beta > 1e-300);
                 ctl.k = J;
                 ctl.beta = beta;
+                ctl.s = fb > 0.f ? 1.f / fb : 0.f;
                 ctl.cont = conv ? 0 : 1;
                 if (!conv) ctl.j = j + 1;
                 if (lead) {
@@ -522,11 +585,11 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
             a.e64[o] = mk<double>(ax, ay);
             a.psi[o] = a.psi[o] + mk<double>(ax, ay);
         }
-        if (!fz_grid_sync(a.bar, gen, a.err, &ctl.ok)) return;
+        if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
         // r -= (S + i dt/2 H) e in FP64; ||r|| decides whether another pass runs
-        const double rn = fz_rows64(a.op64, lo, hi, sc_negplus, a.e64, a.r64, true);
+        const double rn = fz_rows64<KB>(a.op64, a.rb64, lo, hi, sc_negplus, a.e64, a.r64, true);
         fz_cta_sum64(rn, red, part_me + P_RES * pstride);
-        if (!fz_grid_sync(a.bar, gen, a.err, &ctl.ok)) return;
+        if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
         fz_reduce(a.part + P_RES * pstride, gridDim.x, 1, hsum[2]);
         if (tid == 0) {
             const double r = sqrt(fmax(hsum[2][0], 0.0));
@@ -545,11 +608,37 @@ struct FusedCayley {
     FzArgs args;
     size_t smem = 0;
     int nctas = 0;
+    bool kb6 = false;  // the instance unrolled for 13-diagonal bands (k = 7 B-splines)
+    void *bufs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // real bands, tables
 };
 
-static size_t fz_smem_bytes(int nblk, int w, int g_in_smem)
+static size_t fz_smem_bytes(int N, int nblk, int w, int kb, int g_in_smem)
 {
-    return ((size_t)nblk * 32 + (size_t)nblk * w * (g_in_smem ? 33 : 1)) * sizeof(cxf);
+    return ((size_t)nblk * 32 + (size_t)nblk * w * (g_in_smem ? 33 : 1) + (size_t)FZ_MAXU * (N + 2 * kb)) * sizeof(cxf);
+}
+
+// real copy of an operator's bands in the device layout [band][2kb+1][ld]; false when a band
+// has a non-zero imaginary part
+template <typename R>
+static bool real_bands(const pg_op *op, std::vector<R> &out)
+{
+    const size_t rows = op->h_bands.size() / (size_t)op->N;
+    out.assign(rows * (size_t)op->ld, (R)0);
+    for (size_t q = 0; q < rows; ++q)
+        for (int i = 0; i < op->N; ++i) {
+            const std::complex<double> v = op->h_bands[q * op->N + i];
+            if (v.imag() != 0.0) return false;
+            out[q * op->ld + i] = (R)v.real();
+        }
+    return true;
+}
+
+template <typename T>
+static int upload_vec(const std::vector<T> &v, void **dst)
+{
+    PG_CUDA_TRY(cudaMalloc(dst, std::max<size_t>(1, v.size()) * sizeof(T)));
+    if (!v.empty()) PG_CUDA_TRY(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return PG_OK;
 }
 
 int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, FusedCayley **out)
@@ -563,25 +652,45 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
     if (!op64->finalized || !opb->finalized) return PG_ERR_STATE;
     if (op64->ndense_entries > 0 || opb->ndense_entries > 0 || op64->fact.Q > 0 || opb->fact.Q > 0)
         return PG_ERR_STORAGE;
-    if (!op64->d_bands || !opb->d_bands || op64->nrows != opb->nrows || op64->N != opb->N || op64->kb != opb->kb)
-        return PG_ERR_STORAGE;
+    if (op64->nrows != opb->nrows || op64->N != opb->N || op64->kb != opb->kb) return PG_ERR_STORAGE;
     if (precb->kind != 1 || !precb->op || precb->op->precision != PG_FP32 || precb->op->nrows != opb->nrows ||
         precb->N != opb->N || precb->kb < 1 || precb->kb > 32)
         return PG_ERR_STORAGE;
     pg_ctx *ctx = opb->ctx;
-    const int N = opb->N, nch = opb->nrows, nblk = (N + 31) / 32, w = precb->kb;
+    const int N = opb->N, nch = opb->nrows, nblk = (N + 31) / 32, w = precb->kb, kb = opb->kb;
     if (nch < 1 || N < 1) return PG_ERR_SHAPE;
+    // real radial bands (the complex factors of a Cayley step are the slot scales)
+    std::vector<double> rb64;
+    std::vector<float> rb32;
+    if (!real_bands<double>(op64, rb64) || !real_bands<float>(opb, rb32)) return PG_ERR_STORAGE;
+    // distinct source channels of each row of opb, staged once per matvec
+    std::vector<int> ucol((size_t)nch * FZ_MAXU, 0), nucol(nch, 0);
+    std::vector<unsigned char> ent_u(opb->h_ent_col.size(), 0);
+    for (int r = 0; r < nch; ++r)
+        for (int e = opb->h_row_ptr[r]; e < opb->h_row_ptr[r + 1]; ++e) {
+            const int col = opb->h_ent_col[e];
+            int u = 0;
+            while (u < nucol[r] && ucol[(size_t)r * FZ_MAXU + u] != col) ++u;
+            if (u == nucol[r]) {
+                if (u == FZ_MAXU) return PG_ERR_STORAGE;  // wider angular coupling: multi-kernel step
+                ucol[(size_t)r * FZ_MAXU + u] = col;
+                nucol[r] = u + 1;
+            }
+            ent_u[e] = (unsigned char)u;
+        }
+    const bool kb6 = (kb == 6);
+    const void *kern = kb6 ? (const void *)cay_fused_step_kernel<6> : (const void *)cay_fused_step_kernel<-1>;
     const size_t limit = 200 * 1024;
     int g_in_smem = 1;
-    size_t smem = fz_smem_bytes(nblk, w, 1);
+    size_t smem = fz_smem_bytes(N, nblk, w, kb, 1);
     if (smem > limit) {
         g_in_smem = 0;
-        smem = fz_smem_bytes(nblk, w, 0);
+        smem = fz_smem_bytes(N, nblk, w, kb, 0);
         if (smem > limit) return PG_ERR_SHAPE;
     }
-    PG_CUDA_TRY(cudaFuncSetAttribute(cay_fused_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cay_fused_step_kernel, FZ_THREADS, smem));
+    PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FZ_THREADS, smem));
     const int resident = per_sm * std::max(1, ctx->num_sms);
     if (per_sm < 1 || nch > resident) return PG_ERR_SHAPE;  // every CTA must be resident at once
     // one CTA per SM: the channels, and the FP64 rows spread over all of them
@@ -616,12 +725,39 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
     alloc((void **)&a.V, sizeof(cxf) * (size_t)m * n);
     alloc((void **)&a.part, sizeof(double) * P_COUNT * (size_t)nctas * FZ_PSTRIDE);
     alloc((void **)&a.bar, sizeof(FzBarrier));
+    if (code == PG_OK) code = upload_vec(rb64, &f->bufs[0]);
+    if (code == PG_OK) code = upload_vec(rb32, &f->bufs[1]);
+    if (code == PG_OK) code = upload_vec(ucol, &f->bufs[2]);
+    if (code == PG_OK) code = upload_vec(nucol, &f->bufs[3]);
+    if (code == PG_OK) code = upload_vec(ent_u, &f->bufs[4]);
+    // FP64 rows split so that every CTA applies about the same number of band entries
+    std::vector<int> row_lo(nctas + 1, 0);
+    {
+        long long total = 0;
+        for (int r = 0; r < nch; ++r) total += (long long)(op64->h_row_ptr[r + 1] - op64->h_row_ptr[r] + 1) * N;
+        long long acc = 0;
+        int g = 1;
+        for (long long o = 0; o < (long long)n && g < nctas; ++o) {
+            const int r = (int)(o / N);
+            acc += op64->h_row_ptr[r + 1] - op64->h_row_ptr[r] + 1;
+            while (g < nctas && acc * nctas >= total * g) row_lo[g++] = (int)(o + 1);
+        }
+        while (g <= nctas) row_lo[g++] = (int)n;
+    }
+    if (code == PG_OK) code = upload_vec(row_lo, &f->bufs[5]);
     if (code != PG_OK) {
         pg_cayley_fused_free(f);
         return code;
     }
+    a.rb64 = (const double *)f->bufs[0];
+    a.rb32 = (const float *)f->bufs[1];
+    a.ucol = (const int *)f->bufs[2];
+    a.nucol = (const int *)f->bufs[3];
+    a.ent_u = (const unsigned char *)f->bufs[4];
+    a.row_lo = (const int *)f->bufs[5];
     f->smem = smem;
     f->nctas = nctas;
+    f->kb6 = kb6;
     *out = f;
     return PG_OK;
 }
@@ -648,7 +784,8 @@ int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams *par
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, cay_fused_step_kernel, a));
+    if (f->kb6) PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, cay_fused_step_kernel<6>, a));
+    else PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, cay_fused_step_kernel<-1>, a));
     return PG_OK;
 }
 
@@ -661,5 +798,6 @@ void pg_cayley_fused_free(FusedCayley *f)
     cudaFree(f->args.V);
     cudaFree(f->args.part);
     cudaFree(f->args.bar);
+    for (void *b : f->bufs) cudaFree(b);
     delete f;
 }

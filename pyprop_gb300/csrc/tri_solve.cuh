@@ -24,6 +24,21 @@ template <typename R> __device__ __forceinline__ void coef_fms(cx<R> &acc, R c, 
 }
 template <typename R> __device__ __forceinline__ void coef_fms(cx<R> &acc, cx<R> c, cx<R> v) { cfma(acc, mk<R>(-c.x, -c.y), v); }
 
+// factor loads through L2 only: every factor element is read once per solve, so caching it in
+// L1 would only evict data that callers reuse
+__device__ __forceinline__ float tri_ld(const float *p) { return __ldcg(p); }
+__device__ __forceinline__ double tri_ld(const double *p) { return __ldcg(p); }
+__device__ __forceinline__ cx<float> tri_ld(const cx<float> *p)
+{
+    const float2 v = __ldcg((const float2 *)p);
+    return mk<float>(v.x, v.y);
+}
+__device__ __forceinline__ cx<double> tri_ld(const cx<double> *p)
+{
+    const double2 v = __ldcg((const double2 *)p);
+    return mk<double>(v.x, v.y);
+}
+
 // Blocked triangular solves, parallel over the blocks of a fibre. With T_b the 32x32 diagonal
 // block of block b and C_b its coupling to the w boundary values s of the neighbouring block
 // (lower sweep: the last w values of block b-1; upper sweep: the first w values of block
@@ -62,17 +77,17 @@ __device__ __forceinline__ void tri_solve_smem(int nblk, int w, size_t m, const 
 #pragma unroll 1
         for (int q0 = 0; q0 < 32; q0 += 16) {
 #pragma unroll
-            for (int q = 0; q < 16; ++q) coef_fma(acc[q & 3], ib[(q0 + q) * 32 + lane], shfl_cx(r, q0 + q));
+            for (int q = 0; q < 16; ++q) coef_fma(acc[q & 3], tri_ld(ib + (q0 + q) * 32 + lane), shfl_cx(r, q0 + q));
         }
         xs[blk * 32 + lane] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
         if (g_in_smem) {
             const C *gb = g + (m * nblk + blk) * gstride;
-            for (int c = 0; c < w; ++c) sg[((size_t)blk * w + c) * 32 + lane] = gb[c * 32 + lane];
+            for (int c = 0; c < w; ++c) sg[((size_t)blk * w + c) * 32 + lane] = tri_ld(gb + c * 32 + lane);
         }
     };
     // s = Rb z[boundary rows]: each warp takes BRW consecutive output rows at a time, lanes
-    // over the columns, so all of a lane's Rb loads for those rows are in flight together;
-    // the block-triangular zero part is skipped by a per-element predicate
+    // over the columns, two 32-column chunks per round so that 2 BRW Rb loads of a lane are in
+    // flight together; the block-triangular zero part is skipped by a per-element predicate
     auto boundary = [&](bool lower, const C *rb) {
         constexpr int BRW = 8;
         const C *Rm = rb + m * (size_t)nb * nb;
@@ -83,14 +98,24 @@ __device__ __forceinline__ void tri_solve_smem(int nblk, int w, size_t m, const 
             for (int q = 0; q < BRW; ++q) acc[q] = mk<R>((R)0, (R)0);
             const int bo_first = row0 / w, bo_last = min(row0 + BRW - 1, nb - 1) / w;
             const int c_lo = lower ? 0 : bo_first * w, c_hi = lower ? (bo_last + 1) * w : nb;
-            for (int col = c_lo + lane; col < c_hi; col += 32) {
-                const int bc = col / w, rc = col - bc * w;
-                const cx<R> zc = xs[bc * 32 + r0 + rc];
+            for (int col0 = c_lo; col0 < c_hi; col0 += 64) {
+                const int ca = col0 + lane, cb = col0 + 32 + lane;
+                const int bca = ca / w, bcb = cb / w;
+                C va[BRW], vb[BRW];
 #pragma unroll
                 for (int q = 0; q < BRW; ++q) {
                     const int row = row0 + q, bo = row / w;
-                    const bool nz = row < nb && (lower ? bc <= bo : bc >= bo);
-                    if (nz) coef_fma(acc[q], Rm[(size_t)row * nb + col], zc);
+                    const bool nza = ca < c_hi && row < nb && (lower ? bca <= bo : bca >= bo);
+                    const bool nzb = cb < c_hi && row < nb && (lower ? bcb <= bo : bcb >= bo);
+                    va[q] = nza ? tri_ld(Rm + (size_t)row * nb + ca) : C();
+                    vb[q] = nzb ? tri_ld(Rm + (size_t)row * nb + cb) : C();
+                }
+                const cx<R> za = ca < c_hi ? xs[bca * 32 + r0 + (ca - bca * w)] : mk<R>((R)0, (R)0);
+                const cx<R> zb = cb < c_hi ? xs[bcb * 32 + r0 + (cb - bcb * w)] : mk<R>((R)0, (R)0);
+#pragma unroll
+                for (int q = 0; q < BRW; ++q) {
+                    coef_fma(acc[q], va[q], za);
+                    coef_fma(acc[q], vb[q], zb);
                 }
             }
 #pragma unroll
@@ -109,8 +134,13 @@ __device__ __forceinline__ void tri_solve_smem(int nblk, int w, size_t m, const 
         cx<R> y = xs[blk * 32 + lane];
         const int nbk = lower ? blk - 1 : blk + 1;
         if (nbk >= 0 && nbk < nblk) {
-            const C *gb = g_in_smem ? sg + (size_t)blk * gstride : g + (m * nblk + blk) * gstride;
-            for (int c = 0; c < w; ++c) coef_fms(y, gb[c * 32 + lane], sb[nbk * w + c]);
+            if (g_in_smem) {
+                const C *gb = sg + (size_t)blk * gstride;
+                for (int c = 0; c < w; ++c) coef_fms(y, gb[c * 32 + lane], sb[nbk * w + c]);
+            } else {
+                const C *gb = g + (m * nblk + blk) * gstride;
+                for (int c = 0; c < w; ++c) coef_fms(y, tri_ld(gb + c * 32 + lane), sb[nbk * w + c]);
+            }
         }
         return y;
     };
