@@ -7,13 +7,14 @@ from tests.helpers import hydrogen_problem, oracle_hamiltonian, relerr
 pytestmark = pytest.mark.gpu
 
 
-def _members(precision):
+def _members(precision, fused=True):
     specs = [dict(lmax=3, nbsplines=40, rmax=40.0, amplitude=0.05),
              dict(lmax=5, nbsplines=33, rmax=30.0, amplitude=0.08, wavelength_nm=400.0),
              dict(lmax=2, nbsplines=55, rmax=50.0, amplitude=0.02, wavelength_nm=1600.0)]
     probs = []
     for k, sp in enumerate(specs):
         p = hydrogen_problem(propagator="CayleyPropagatorGPU", precision=precision, gmres_tolerance=1e-12, **sp)
+        p.Propagator.FusedStep = fused
         p.SetupStep(skipWavefunctionSetup=True)
         rng = np.random.default_rng(100 + k)
         shape = p.psi.GetRepresentation().GetFullShape()
@@ -27,10 +28,14 @@ def _members(precision):
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_ensemble_matches_single_members(gpu, precision):
     from pyprop_gb300.ensemble import CayleyEnsembleGPU
-    alone = _members(precision)
+    # the ensemble graph runs the multi-kernel step of every member: members stepped alone on
+    # that step agree to rounding; mixed-precision members on the single-kernel step agree
+    # to the GMRES tolerance
+    alone = _members(precision, fused=False)
+    alone_fused = _members(precision) if precision == "fp32" else []
     together = _members(precision)
     for _ in range(3):
-        for p in alone:
+        for p in alone + alone_fused:
             p.AdvanceStep()
     ens = CayleyEnsembleGPU(together)
     for _ in range(3):
@@ -40,6 +45,9 @@ def test_ensemble_matches_single_members(gpu, precision):
         assert relerr(b.psi.numpy(), a.psi.numpy()) < 1e-13
         assert st["Iterations"] >= 1
         assert abs(a.PropagatedTime - b.PropagatedTime) < 1e-12
+    for a, b in zip(alone_fused, together):
+        assert a.Propagator.Fused
+        assert relerr(b.psi.numpy(), a.psi.numpy()) < 1e-10
 
 
 def test_ensemble_member_against_oracle(gpu):
