@@ -126,15 +126,17 @@ __device__ __forceinline__ cxd fz_ldg(const cxd *p)
 }
 
 // Sum over the channels of the partials of one phase: hs[t] = sum_a part[a][t], t < nval,
-// one warp per value, the channels over the lanes, a fixed order (identical in every CTA).
-__device__ __forceinline__ void fz_reduce(const double *part, int nch, int nval, double *hs)
+// one warp per value, the channels over the lanes, a fixed order (identical in every CTA);
+// FP64 sums, stored as T (float for what enters the FP32 Givens recurrence).
+template <typename T>
+__device__ __forceinline__ void fz_reduce(const double *part, int nch, int nval, T *hs)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int t = warp; t < nval; t += FZ_NW) {
         double s = 0.0;
         for (int a = lane; a < nch; a += 32) s += __ldcg(part + (size_t)a * FZ_PSTRIDE + t);
         s = fz_warp_sum(s);
-        if (lane == 0) hs[t] = s;
+        if (lane == 0) hs[t] = (T)s;
     }
     __syncthreads();
 }
@@ -328,15 +330,15 @@ struct FzGivens {
 // New Hessenberg column j (h1 + h2 above the diagonal, beta below) through the previous
 // rotations, the new rotation, the updated g; returns the residual estimate |g_{j+1}|. FP32
 // as the multi-kernel step's Givens kernel.
-__device__ float fz_givens(FzGivens &G, int j, const double *h1, const double *h2, double beta)
+__device__ float fz_givens(FzGivens &G, int j, const float *h1, const float *h2, float beta)
 {
     const int J = j + 1;
     float hx[FZ_MAXM + 1], hy[FZ_MAXM + 1];
     for (int i = 0; i < J; ++i) {
-        hx[i] = (float)(h1[2 * i] + h2[2 * i]);
-        hy[i] = (float)(h1[2 * i + 1] + h2[2 * i + 1]);
+        hx[i] = h1[2 * i] + h2[2 * i];
+        hy[i] = h1[2 * i + 1] + h2[2 * i + 1];
     }
-    hx[J] = (float)beta;
+    hx[J] = beta;
     hy[J] = 0.f;
     for (int i = 0; i < j; ++i) {
         const float c = G.cs[i], sx = G.sn[2 * i], sy = G.sn[2 * i + 1];
@@ -404,8 +406,9 @@ __device__ void fz_backsolve(const FzGivens &G, int k, cxd *ys)
 
 struct FzCtl {
     int j, cont, k, again, passes, ok;
-    double beta, tol_eff;
-    float s;  // 1/beta for the next Krylov vector (formed once: FP64 division is slow here)
+    double tol_eff;
+    float tol_f;  // tol_eff in FP32, for the per-iteration test
+    float s;      // 1/beta for the next Krylov vector (formed once: FP64 division is slow here)
 };
 
 template <int KB>
@@ -415,7 +418,8 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
     __shared__ cxd sc_diff[PG_MAX_SLOTS], sc_negplus[PG_MAX_SLOTS];
     __shared__ cxf sc_plus[PG_MAX_SLOTS];
     __shared__ double red[FZ_NW][2 * FZ_CB];
-    __shared__ double hsum[3][FZ_PSTRIDE];
+    __shared__ double hd[1];  // FP64 sums of the pass: ||d||^2, then ||r||^2
+    __shared__ float hf[3][FZ_PSTRIDE];  // the Gram-Schmidt sums h1, h2 and |w|^2 of this iteration
     __shared__ cxf hs[FZ_MAXM];
     __shared__ cxd ys[FZ_MAXM];
     __shared__ FzGivens G;
@@ -485,12 +489,12 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
             fz_channel_sums(Vc, n, 0, true, xs, N, red, part_me + P_NRM * pstride);
         }
         if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
-        fz_reduce(a.part + P_NRM * pstride, a.nch, 1, hsum[2]);
+        fz_reduce(a.part + P_NRM * pstride, a.nch, 1, hd);
         if (tid == 0) {
-            const double b = sqrt(fmax(hsum[2][0], 0.0));
-            ctl.beta = b;
+            const double b = sqrt(fmax(hd[0], 0.0));
             ctl.s = (float)(b > 0.0 ? 1.0 / b : 0.0);
             ctl.tol_eff = fmax(a.tol, 2e-6 * b);
+            ctl.tol_f = (float)ctl.tol_eff;
             ctl.j = 0;
             ctl.k = 0;
             ctl.cont = b > 0.0 ? 1 : 0;
@@ -523,11 +527,11 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                 fz_channel_sums(Vc, n, J, false, xs, N, red, part_me + P_H1 * pstride);
             }
             if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
-            fz_reduce(a.part + P_H1 * pstride, a.nch, 2 * J, hsum[0]);
+            fz_reduce(a.part + P_H1 * pstride, a.nch, 2 * J, hf[0]);
             for (int rep = 0; rep < 2; ++rep) {
                 if (owner) {
-                    const double *h = hsum[rep];
-                    if (tid < J) hs[tid] = mk<float>((float)h[2 * tid], (float)h[2 * tid + 1]);
+                    const float *h = hf[rep];
+                    if (tid < J) hs[tid] = mk<float>(h[2 * tid], h[2 * tid + 1]);
                     __syncthreads();
                     for (int i = tid; i < N; i += FZ_THREADS) {
                         cxf acc = xs[i];
@@ -546,18 +550,16 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                     fz_channel_sums(Vc, n, J, rep == 1, xs, N, red, part_me + (rep == 0 ? P_H2 : P_H3) * pstride);
                 }
                 if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
-                if (rep == 0) fz_reduce(a.part + P_H2 * pstride, a.nch, 2 * J, hsum[1]);
-                else fz_reduce(a.part + P_H3 * pstride, a.nch, 1, hsum[2]);
+                if (rep == 0) fz_reduce(a.part + P_H2 * pstride, a.nch, 2 * J, hf[1]);
+                else fz_reduce(a.part + P_H3 * pstride, a.nch, 1, hf[2]);
             }
             if (tid == 0) {
                 // |w| in FP32 (it enters the Hessenberg matrix and the next vector as FP32)
-                const float fb = sqrtf(fmaxf((float)hsum[2][0], 0.f));
-                const double beta = (double)fb;
-                const double resid = (double)fz_givens(G, j, hsum[0], hsum[1], beta);
+                const float fb = sqrtf(fmaxf(hf[2][0], 0.f));
+                const float resid = fz_givens(G, j, hf[0], hf[1], fb);
                 const bool bad = !(resid == resid);
-                const bool conv = bad || resid <= ctl.tol_eff || J >= a.m || !(beta > 1e-300);
+                const bool conv = bad || resid <= ctl.tol_f || J >= a.m || !(fb > 0.f);
                 ctl.k = J;
-                ctl.beta = beta;
                 ctl.s = fb > 0.f ? 1.f / fb : 0.f;
                 ctl.cont = conv ? 0 : 1;
                 if (!conv) ctl.j = j + 1;
@@ -590,9 +592,9 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
         const double rn = fz_rows64<KB>(a.op64, a.rb64, lo, hi, sc_negplus, a.e64, a.r64, true);
         fz_cta_sum64(rn, red, part_me + P_RES * pstride);
         if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
-        fz_reduce(a.part + P_RES * pstride, gridDim.x, 1, hsum[2]);
+        fz_reduce(a.part + P_RES * pstride, gridDim.x, 1, hd);
         if (tid == 0) {
-            const double r = sqrt(fmax(hsum[2][0], 0.0));
+            const double r = sqrt(fmax(hd[0], 0.0));
             ctl.again = (r > a.tol) && (r == r) && ctl.passes < FZ_MAXPASS;
             if (lead) a.st->stats.true_resid = r;
         }
