@@ -68,9 +68,8 @@ __device__ __forceinline__ void tri_solve_smem(int nblk, int w, size_t m, const 
     const size_t gstride = (size_t)w * 32;
     const int nb = nblk * w;
 
-    // z_b = T_b^-1 r for lane's row; G_b staged for the correction. T_b^-1 is triangular like
-    // T_b (lower sweep: entries s <= t, upper: s >= t), so the zero half is never loaded.
-    auto solve_block = [&](int blk, cx<R> r, const C *inv, const C *g, bool lower) {
+    // z_b = T_b^-1 r for lane's row; G_b staged for the correction
+    auto solve_block = [&](int blk, cx<R> r, const C *inv, const C *g) {
         const C *ib = inv + (m * nblk + blk) * 1024;
         cx<R> acc[4];
 #pragma unroll
@@ -78,12 +77,7 @@ __device__ __forceinline__ void tri_solve_smem(int nblk, int w, size_t m, const 
 #pragma unroll 1
         for (int q0 = 0; q0 < 32; q0 += 16) {
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int sidx = q0 + q;
-                const bool nz = lower ? sidx <= lane : sidx >= lane;
-                const C c = nz ? tri_ld(ib + sidx * 32 + lane) : C();
-                coef_fma(acc[q & 3], c, shfl_cx(r, sidx));
-            }
+            for (int q = 0; q < 16; ++q) coef_fma(acc[q & 3], tri_ld(ib + (q0 + q) * 32 + lane), shfl_cx(r, q0 + q));
         }
         xs[blk * 32 + lane] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
         if (g_in_smem) {
@@ -152,18 +146,18 @@ __device__ __forceinline__ void tri_solve_smem(int nblk, int w, size_t m, const 
     };
 
     if (do_lower) {
-        for (int blk = warp; blk < nblk; blk += NW) solve_block(blk, xs[blk * 32 + lane], lo_inv, lo_g, true);
+        for (int blk = warp; blk < nblk; blk += NW) solve_block(blk, xs[blk * 32 + lane], lo_inv, lo_g);
         __syncthreads();
         boundary(true, lo_rb);
         __syncthreads();
         for (int blk = warp; blk < nblk; blk += NW) {
             const cx<R> y = correct(blk, lo_g, true);
-            if (do_upper) solve_block(blk, y, up_inv, up_g, false);  // same rows, same warp
+            if (do_upper) solve_block(blk, y, up_inv, up_g);  // same rows, same warp
             else xs[blk * 32 + lane] = y;
         }
         __syncthreads();
     } else if (do_upper) {
-        for (int blk = warp; blk < nblk; blk += NW) solve_block(blk, xs[blk * 32 + lane], up_inv, up_g, false);
+        for (int blk = warp; blk < nblk; blk += NW) solve_block(blk, xs[blk * 32 + lane], up_inv, up_g);
         __syncthreads();
     }
     if (do_upper) {
