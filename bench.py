@@ -155,6 +155,25 @@ def time_matvec(torch, prob, flush, reps=50):
     return avg, 8 * (elems + 2 * nang * N), op.variant()[0]
 
 
+def step_bytes(prob, iters, passes):
+    """Algorithmic bytes of one mixed step: every block solve reads the factors (complex64), every
+    complex64 matvec the real FP32 bands and its vectors, every FP64 residual product the real
+    FP64 bands and its vectors; the solves are one per GMRES iteration and refinement pass, the
+    complex64 products one per iteration, the FP64 products one per pass plus the first."""
+    from pyprop_gb300 import _native as nat
+    nang, N = prob.psi.GetRepresentation().GetFullShape()
+    kb = prob.Propagator.op64.kb
+    n = nang * N
+    nblk = (N + 31) // 32
+    per_sweep = nblk * (32 * 32 + 32 * kb) + kb * kb * nblk * (nblk + 1) // 2
+    solve = 8 * (nang * 2 * per_sweep + 2 * n)
+    e32 = prob.Propagator.opb.stored_elements()
+    e64 = prob.Propagator.op64.stored_elements()
+    mv32 = 4 * e32 + 8 * 2 * n
+    mv64 = 8 * e64 + 16 * 2 * n
+    return int((iters + passes) * solve + iters * mv32 + (passes + 1) * mv64)
+
+
 def time_block_solve(torch, prob, flush, reps=50):
     """Average duration of the complex64 block-diagonal LU solve (both sweeps, one launch) and
     its algorithmic bytes: per fibre and sweep the inverse diagonal blocks (nblk 32x32), the
@@ -431,12 +450,13 @@ def run_ours(args):
         dist.init_process_group("nccl")
 
     probs = {}
-    for prec in ("fp32", "fp64"):
+    for name, prec, fused in (("fp32", "fp32", True), ("fp64", "fp64", True), ("multi", "fp32", False)):
         p = pp.Problem(pp.LoadString(_config(prec)))
         p.Propagator.StepStats = False  # steps only enqueue; stats are read after the end event
         p.Propagator.Eager = args.eager
+        p.Propagator.FusedStep = fused
         p.SetupStep(skipWavefunctionSetup=True)
-        probs[prec] = p
+        probs[name] = p
     psi0, e0 = initial_state(probs["fp32"])
     flush = l2_flush_buffer(torch)
     stream = torch.cuda.current_stream()
@@ -451,6 +471,7 @@ def run_ours(args):
             dist.barrier()
         total = 0.0
         iters = 0
+        passes = 0
         ctx = prob.Propagator.op64.ctx
         prob.Propagator.LastStats  # settles the device kernel count of the warm-up steps
         l0 = ctx.launches()
@@ -462,15 +483,20 @@ def run_ours(args):
             e.record(stream)
             e.synchronize()
             total += s.elapsed_time(e) * 1e-3
-            iters += prob.Propagator.LastStats.Iterations
+            st = prob.Propagator.LastStats
+            iters += st.Iterations
+            passes += st.RestartCount
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-        return total, iters / max(K, 1), ctx.launches() - l0
+        return total, iters / max(K, 1), passes / max(K, 1), ctx.launches() - l0
 
     with ClockSampler(local) as clk:
-        t_mixed, it_mixed, launches = run(probs["fp32"], args.steps, args.warmup)
-    t_fp64, it_fp64, _ = run(probs["fp64"], args.steps, args.warmup)
+        t_mixed, it_mixed, pass_mixed, launches = run(probs["fp32"], args.steps, args.warmup)
+    t_fp64, it_fp64, _, _ = run(probs["fp64"], args.steps, args.warmup)
+    # the same mixed step on the captured multi-kernel path (comparison only)
+    t_multi, it_multi, _, launches_multi = run(probs["multi"], args.steps, args.warmup)
+    fused = bool(getattr(probs["fp32"].Propagator, "Fused", False))
     if dist:
         tt = torch.tensor([t_mixed, t_fp64], device="cuda", dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -504,6 +530,7 @@ def run_ours(args):
     nbytes = psi0.size * 16
 
     avg_mv, bytes_mv, variant_mv = time_matvec(torch, prob, flush)
+    bytes_step = step_bytes(prob, it_mixed, pass_mixed)
     avg_ts, bytes_ts = time_block_solve(torch, prob, flush)
     avg_lg, bytes_lg, variant_lg = time_large_matvec(torch, flush)
     two_e = time_two_electron(torch) if args.two_electron else None
@@ -529,13 +556,24 @@ def run_ours(args):
             "gmres_iterations_per_step": it_mixed,
             "e2e": {"value": world * args.steps / e2e_t, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
-            # dominant kernel of the step: the block-diagonal LU solve (5 launches per step)
-            "roofline": {"bound": "hbm", "achieved": bytes_ts / avg_ts / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": bytes_ts / avg_ts / 1e9 / peak,
-                         "traffic": profile_traffic("tri_solve_kernel_fp32_lmax40_n600.md"),
-                         "kernel": "tri_solve_kernel<float,cx<float>,24>", "avg_launch_us": 1e6 * avg_ts,
-                         "algorithmic_bytes": bytes_ts, "peak_kind": peak_kind,
-                         "timing": "CUDA events around 50 launches on the launching stream, L2 flushed before each"},
+            # dominant kernel: the single-kernel step itself (one launch per step)
+            "roofline": {"bound": "hbm", "achieved": bytes_step / (t_mixed / args.steps) / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": bytes_step / (t_mixed / args.steps) / 1e9 / peak,
+                         "traffic": profile_traffic("cay_fused_step_kernel_lmax40_n600.md"),
+                         "kernel": "cay_fused_step_kernel<6>" if fused else "multi-kernel step",
+                         "avg_launch_us": 1e6 * t_mixed / args.steps, "algorithmic_bytes": bytes_step,
+                         "peak_kind": peak_kind,
+                         "timing": "CUDA events around each timed step on the launching stream, L2 flushed before each",
+                         "note": "block-solve factors and bands are re-read from L2 within a step: latency-bound "
+                                 "(grid barriers, dependent block-solve phases), not HBM-bound"},
+            "roofline_block_solve": {"bound": "hbm", "achieved": bytes_ts / avg_ts / 1e9, "peak": peak, "unit": "GB/s",
+                                     "frac": bytes_ts / avg_ts / 1e9 / peak,
+                                     "traffic": profile_traffic("tri_solve_kernel_fp32_lmax40_n600.md"),
+                                     "kernel": "tri_solve_kernel<float,cx<float>,24>", "avg_launch_us": 1e6 * avg_ts,
+                                     "algorithmic_bytes": bytes_ts, "peak_kind": peak_kind,
+                                     "timing": "CUDA events around 50 launches, L2 flushed before each"},
+            "multi_kernel_step": {"steps_per_s": world * args.steps / t_multi, "gmres_iterations_per_step": it_multi,
+                                  "kernels_per_step": launches_multi / max(args.steps, 1)},
             "roofline_matvec": {"bound": "hbm", "achieved": bytes_mv / avg_mv / 1e9, "peak": peak, "unit": "GB/s",
                                 "frac": bytes_mv / avg_mv / 1e9 / peak,
                                 "traffic": profile_traffic("op_matvec_bulk_kernel_fp32_lmax40_n600.md"),
