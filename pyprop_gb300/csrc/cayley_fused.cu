@@ -49,6 +49,7 @@ struct FzArgs {
     const int *nucol;            // [Nang] how many
     const unsigned char *ent_u;  // [entries of opb] which staged source an entry reads
     const int *row_lo;           // [CTAs + 1] FP64 rows of each CTA (equal numbers of band entries)
+    int bands_smem;              // 1: each channel's FP32 bands are copied to shared memory per step
     const cxf *lo_inv, *lo_g, *lo_rb, *up_inv, *up_g, *up_rb;
     int nblk, w, fib_per_mat, g_in_smem;
     int nch, N, m;
@@ -253,13 +254,35 @@ __device__ __forceinline__ void fz_cta_sum64(double v, double (*red)[2 * FZ_CB],
     __syncthreads();
 }
 
+// Copy the real FP32 bands of operator row a ([entry][2kb+1][ld] in entry order) to shared
+// memory with asynchronous 16-byte copies (cp.async; waited for by fz_bands_wait).
+__device__ __forceinline__ void fz_bands_load(const FzArgs &A, int a, float *sband)
+{
+    const OpDev &op = A.opb;
+    const int b = 2 * op.kb + 1, ld = op.ld;  // ld: a multiple of 4, so every row is 16-byte aligned
+    const int e0 = __ldg(op.row_ptr + a), e1 = __ldg(op.row_ptr + a + 1);
+    const int per = b * ld / 4;  // 16-byte pieces per entry
+    for (int q = threadIdx.x; q < (e1 - e0) * per; q += FZ_THREADS) {
+        const int e = q / per, r = q - e * per;
+        const float *src = A.rb32 + (size_t)__ldg(op.ent_band + e0 + e) * b * ld + 4 * (size_t)r;
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(sband + (size_t)e * b * ld + 4 * (size_t)r);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void fz_bands_wait()
+{
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+}
+
 // complex64 operator row a applied to the normalised vector wsrc * s: the row's distinct
 // source fibres are staged (scaled, with a zero halo of kb) in xsrc, then thread i forms
-// xs[i] = sum_e sc[slot_e] sum_d band_e[d][i] x_e[i + d - kb] from real bands (L1-cached:
-// the same rows are read every iteration); zero on the padding up to npad.
+// xs[i] = sum_e sc[slot_e] sum_d band_e[d][i] x_e[i + d - kb] from real bands (in shared
+// memory when sband is set, else read through L1); zero on the padding up to npad.
 template <int KB>
 __device__ __forceinline__ void fz_matvec32(const FzArgs &A, int a, const cxf *sc, const cxf *wsrc, float s, cxf *xs,
-                                            int npad, cxf *xsrc)
+                                            int npad, cxf *xsrc, const float *sband)
 {
     const OpDev &op = A.opb;
     const int N = op.N, kb = KB >= 0 ? KB : op.kb, b = 2 * kb + 1, ld = op.ld, W = N + 2 * kb;
@@ -284,8 +307,11 @@ __device__ __forceinline__ void fz_matvec32(const FzArgs &A, int a, const cxf *s
             for (int e = e0; e < e1; e += 2) {
                 // two entries at a time: 2(2kb+1) band loads in flight
                 const bool two = e + 1 < e1;
-                const float *B0 = A.rb32 + (size_t)__ldg(op.ent_band + e) * b * ld + i;
-                const float *B1 = A.rb32 + (size_t)__ldg(op.ent_band + (two ? e + 1 : e)) * b * ld + i;
+                const int e1s = two ? e + 1 : e;
+                const float *B0 = sband ? sband + (size_t)(e - e0) * b * ld + i
+                                        : A.rb32 + (size_t)__ldg(op.ent_band + e) * b * ld + i;
+                const float *B1 = sband ? sband + (size_t)(e1s - e0) * b * ld + i
+                                        : A.rb32 + (size_t)__ldg(op.ent_band + e1s) * b * ld + i;
                 const cxf *x0 = xsrc + (size_t)__ldg(A.ent_u + e) * W + i;  // x[d] = x_e[i + d - kb]
                 const cxf *x1 = xsrc + (size_t)__ldg(A.ent_u + (two ? e + 1 : e)) * W + i;
                 float t0x = 0.f, t0y = 0.f, t1x = 0.f, t1y = 0.f;
@@ -293,8 +319,8 @@ __device__ __forceinline__ void fz_matvec32(const FzArgs &A, int a, const cxf *s
                     float c0[2 * (KB > 0 ? KB : 0) + 1], c1[2 * (KB > 0 ? KB : 0) + 1];
 #pragma unroll
                     for (int d = 0; d < 2 * KB + 1; ++d) {
-                        c0[d] = __ldg(B0 + (size_t)d * ld);
-                        c1[d] = __ldg(B1 + (size_t)d * ld);
+                        c0[d] = sband ? B0[(size_t)d * ld] : __ldg(B0 + (size_t)d * ld);
+                        c1[d] = sband ? B1[(size_t)d * ld] : __ldg(B1 + (size_t)d * ld);
                     }
 #pragma unroll
                     for (int d = 0; d < 2 * KB + 1; ++d) {
@@ -305,7 +331,8 @@ __device__ __forceinline__ void fz_matvec32(const FzArgs &A, int a, const cxf *s
                     }
                 } else {
                     for (int d = 0; d < b; ++d) {
-                        const float c = __ldg(B0 + (size_t)d * ld), c2 = __ldg(B1 + (size_t)d * ld);
+                        const float c = sband ? B0[(size_t)d * ld] : __ldg(B0 + (size_t)d * ld);
+                        const float c2 = sband ? B1[(size_t)d * ld] : __ldg(B1 + (size_t)d * ld);
                         t0x = fmaf(c, x0[d].x, t0x);
                         t0y = fmaf(c, x0[d].y, t0y);
                         t1x = fmaf(c2, x1[d].x, t1x);
@@ -435,6 +462,11 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
     cxf *sb = xs + (size_t)npad;               // [nblk*w]
     cxf *sg = sb + (size_t)nblk * w;           // [nblk][w][32] (g_in_smem)
     cxf *xsrc = sg + (a.g_in_smem ? (size_t)nblk * w * 32 : 0);  // [FZ_MAXU][N + 2kb] staged sources
+    // [entries][2kb+1][ld] this channel's FP32 bands (16-byte aligned), when they fit
+    float *sband = (owner && a.bands_smem)
+                       ? (float *)(fz_smem + ((((size_t)npad + (size_t)nblk * w * (a.g_in_smem ? 33 : 1) +
+                                                (size_t)FZ_MAXU * (N + 2 * a.opb.kb)) * sizeof(cxf) + 15) / 16) * 16)
+                       : nullptr;
     const size_t mat = (size_t)(owner ? ch / a.fib_per_mat : 0);
     cxf *Vc = a.V + (size_t)(owner ? ch : 0) * N;  // V[q][ch] at Vc + q * n
     const size_t pstride = (size_t)gridDim.x * FZ_PSTRIDE;
@@ -466,9 +498,12 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
     if (tid == 0) ctl.passes = 0;
     __syncthreads();
 
+    // this channel's FP32 bands to shared memory, in flight during the first FP64 rows
+    if (sband) fz_bands_load(a, ch, sband);
     // r = -i dt H psi (FP64); psi is read by all CTAs before the first barrier and only
     // changed after the second
     fz_rows64<KB>(a.op64, a.rb64, lo, hi, sc_diff, a.psi, a.r64, false);
+    if (sband) fz_bands_wait();  // before any exit: no copy outlives the CTA
     if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
 
     for (;;) {
@@ -519,7 +554,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                     const cxf v = xs[i];
                     Vc[(size_t)j * n + i] = mk<float>(v.x * s, v.y * s);
                 }
-                fz_matvec32<KB>(a, ch, sc_plus, a.wbuf + (size_t)(j & 1) * n, s, xs, npad, xsrc);
+                fz_matvec32<KB>(a, ch, sc_plus, a.wbuf + (size_t)(j & 1) * n, s, xs, npad, xsrc, sband);
                 __syncthreads();
                 tri_solve_smem<float, cxf, FZ_NW>(nblk, w, mat, a.lo_inv, a.lo_g, a.lo_rb, a.up_inv, a.up_g, a.up_rb,
                                                   1, 1, a.g_in_smem, xs, sb, sg);
@@ -614,9 +649,11 @@ struct FusedCayley {
     void *bufs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // real bands, tables
 };
 
-static size_t fz_smem_bytes(int N, int nblk, int w, int kb, int g_in_smem)
+static size_t fz_smem_bytes(int N, int nblk, int w, int kb, int g_in_smem, size_t band_bytes)
 {
-    return ((size_t)nblk * 32 + (size_t)nblk * w * (g_in_smem ? 33 : 1) + (size_t)FZ_MAXU * (N + 2 * kb)) * sizeof(cxf);
+    const size_t base = ((size_t)nblk * 32 + (size_t)nblk * w * (g_in_smem ? 33 : 1) + (size_t)FZ_MAXU * (N + 2 * kb)) *
+                        sizeof(cxf);
+    return band_bytes ? (base + 15) / 16 * 16 + band_bytes : base;
 }
 
 // real copy of an operator's bands in the device layout [band][2kb+1][ld]; false when a band
@@ -683,11 +720,19 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
     const bool kb6 = (kb == 6);
     const void *kern = kb6 ? (const void *)cay_fused_step_kernel<6> : (const void *)cay_fused_step_kernel<-1>;
     const size_t limit = 200 * 1024;
-    int g_in_smem = 1;
-    size_t smem = fz_smem_bytes(N, nblk, w, kb, 1);
+    // a channel's FP32 bands in shared memory when the largest row's fit with the rest
+    int max_e = 0;
+    for (int r = 0; r < nch; ++r) max_e = std::max(max_e, opb->h_row_ptr[r + 1] - opb->h_row_ptr[r]);
+    const size_t band_bytes = (size_t)max_e * (2 * kb + 1) * opb->ld * sizeof(float);
+    int g_in_smem = 1, bands_smem = 1;
+    size_t smem = fz_smem_bytes(N, nblk, w, kb, 1, band_bytes);
+    if (smem > limit) {
+        bands_smem = 0;
+        smem = fz_smem_bytes(N, nblk, w, kb, 1, 0);
+    }
     if (smem > limit) {
         g_in_smem = 0;
-        smem = fz_smem_bytes(N, nblk, w, kb, 0);
+        smem = fz_smem_bytes(N, nblk, w, kb, 0, 0);
         if (smem > limit) return PG_ERR_SHAPE;
     }
     PG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -713,6 +758,7 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
     a.w = w;
     a.fib_per_mat = std::max(1, precb->fib_per_mat);
     a.g_in_smem = g_in_smem;
+    a.bands_smem = bands_smem;
     a.nch = nch;
     a.N = N;
     a.m = m;
