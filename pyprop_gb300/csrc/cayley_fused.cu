@@ -287,16 +287,23 @@ __device__ __forceinline__ void fz_matvec32(const FzArgs &A, int a, const cxf *s
     const OpDev &op = A.opb;
     const int N = op.N, kb = KB >= 0 ? KB : op.kb, b = 2 * kb + 1, ld = op.ld, W = N + 2 * kb;
     const int nu = __ldg(A.nucol + a);
-    for (int u = 0; u < nu; ++u) {
-        const cxf *x = wsrc + (size_t)__ldg(A.ucol + (size_t)a * FZ_MAXU + u) * N;
-        for (int q = threadIdx.x; q < W; q += FZ_THREADS) {
-            const int j = q - kb;
-            cxf v = mk<float>(0.f, 0.f);
-            if (j >= 0 && j < N) {
-                v = fz_ldcg(x + j);
-                v = mk<float>(v.x * s, v.y * s);
-            }
-            xsrc[(size_t)u * W + q] = v;
+    int cols[FZ_MAXU];
+#pragma unroll
+    for (int u = 0; u < FZ_MAXU; ++u) cols[u] = u < nu ? __ldg(A.ucol + (size_t)a * FZ_MAXU + u) : 0;
+    // all staged elements of a thread loaded together (nu W elements over the CTA)
+    for (int base = 0; base < nu * W; base += FZ_THREADS * FZ_MAXU) {
+        cxf v[FZ_MAXU];
+#pragma unroll
+        for (int k = 0; k < FZ_MAXU; ++k) {
+            const int idx = base + threadIdx.x + k * FZ_THREADS;
+            const int u = idx / W, q = idx - u * W, j = q - kb;
+            v[k] = (idx < nu * W && j >= 0 && j < N) ? fz_ldcg(wsrc + (size_t)cols[u < FZ_MAXU ? u : 0] * N + j)
+                                                     : mk<float>(0.f, 0.f);
+        }
+#pragma unroll
+        for (int k = 0; k < FZ_MAXU; ++k) {
+            const int idx = base + threadIdx.x + k * FZ_THREADS;
+            if (idx < nu * W) xsrc[idx] = mk<float>(v[k].x * s, v[k].y * s);
         }
     }
     __syncthreads();
@@ -570,13 +577,21 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                     __syncthreads();
                     for (int i = tid; i < N; i += FZ_THREADS) {
                         cxf acc = xs[i];
-                        for (int q = 0; q < J; ++q) {
-                            const cxf v = Vc[(size_t)q * n + i];
-                            const cxf hc = hs[q];
-                            acc.x = fmaf(-v.x, hc.x, acc.x);
-                            acc.x = fmaf(v.y, hc.y, acc.x);
-                            acc.y = fmaf(-v.x, hc.y, acc.y);
-                            acc.y = fmaf(-v.y, hc.x, acc.y);
+                        for (int q0 = 0; q0 < J; q0 += FZ_CB) {
+                            // FZ_CB vectors' loads in flight together
+                            cxf v[FZ_CB];
+#pragma unroll
+                            for (int q = 0; q < FZ_CB; ++q)
+                                v[q] = q0 + q < J ? Vc[(size_t)(q0 + q) * n + i] : mk<float>(0.f, 0.f);
+#pragma unroll
+                            for (int q = 0; q < FZ_CB; ++q) {
+                                if (q0 + q >= J) break;
+                                const cxf hc = hs[q0 + q];
+                                acc.x = fmaf(-v[q].x, hc.x, acc.x);
+                                acc.x = fmaf(v[q].y, hc.y, acc.x);
+                                acc.y = fmaf(-v[q].x, hc.y, acc.y);
+                                acc.y = fmaf(-v[q].y, hc.x, acc.y);
+                            }
                         }
                         xs[i] = acc;
                         if (rep == 1) a.wbuf[(size_t)((j + 1) & 1) * n + (size_t)ch * N + i] = acc;
@@ -613,11 +628,18 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
         const int k = ctl.k;
         for (long long o = lo + tid; o < hi; o += FZ_THREADS) {
             double ax = 0.0, ay = 0.0;
-            for (int q = 0; q < k; ++q) {
-                const cxf v = fz_ldcg(a.V + (size_t)q * n + o);
-                const cxd yq = ys[q];
-                ax = fma((double)v.x, yq.x, ax); ax = fma(-(double)v.y, yq.y, ax);
-                ay = fma((double)v.x, yq.y, ay); ay = fma((double)v.y, yq.x, ay);
+            for (int q0 = 0; q0 < k; q0 += FZ_CB) {
+                cxf v[FZ_CB];
+#pragma unroll
+                for (int q = 0; q < FZ_CB; ++q)
+                    v[q] = q0 + q < k ? fz_ldcg(a.V + (size_t)(q0 + q) * n + o) : mk<float>(0.f, 0.f);
+#pragma unroll
+                for (int q = 0; q < FZ_CB; ++q) {
+                    if (q0 + q >= k) break;
+                    const cxd yq = ys[q0 + q];
+                    ax = fma((double)v[q].x, yq.x, ax); ax = fma(-(double)v[q].y, yq.y, ax);
+                    ay = fma((double)v[q].x, yq.y, ay); ay = fma((double)v[q].y, yq.x, ay);
+                }
             }
             a.e64[o] = mk<double>(ax, ay);
             a.psi[o] = a.psi[o] + mk<double>(ax, ay);
