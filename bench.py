@@ -6,9 +6,11 @@ lmax 40 (41 channels), 600 B-splines of order 7 on an exponential-linear grid r 
 50 a.u. long), dt = 0.01, GMRES (basis 20) left-preconditioned by the block-diagonal
 banded LU. The measured path is the mixed-precision one: FP64 residual, complex64
 operator and Krylov basis, FP64 Gram-Schmidt sums, Hessenberg least squares, norms and
-true residual (refined until the preconditioned residual is below 1e-12). The same steps
-are also run on the plain FP64 GPU path, and the final-state infidelity between the two
-is reported.
+true residual (refined until the true residual is below 1e-12), one cooperative kernel per
+step. The same steps are also run on the plain FP64 GPU path and on the captured
+multi-kernel mixed path, and the final-state infidelity between mixed and FP64 is
+reported. The default 5000 steps are the workload's own length (about a second of timed
+steps, so that the clock sampler sees the timed region).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -825,7 +827,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=300,
