@@ -18,11 +18,8 @@
 // partials in the same order and runs the (tiny) Givens and back-substitution recurrences
 // itself, so all CTAs take identical decisions without another barrier. The FP64 parts
 // (residual rows, the correction e = V y) are spread over all CTAs: FP64 arithmetic is scarce
-// on this GPU. The barriers are exchanges of tagged words: every CTA publishes its partial
-// sums (FP32) packed with a 32-bit tag (launch number, exchange number) by a release store,
-// and every CTA polls the words it needs with acquire loads until their tags are current, so
-// the data travels with the arrival. The polls are bounded: one that runs out sets the
-// context's error flag (2) and the CTAs return.
+// on this GPU. Grid barriers are bounded waits: one that runs out sets the context's error
+// flag (2) and the CTAs return.
 #include "cayley_state.cuh"
 #include "tri_solve.cuh"
 
@@ -36,7 +33,13 @@ static const int FZ_CB = 8;                  // columns per register block of th
 static const int FZ_MAXPASS = 4;             // refinement passes (as the multi-kernel step)
 static const int FZ_PSTRIDE = 2 * (FZ_MAXM + 1);
 static const int FZ_MAXU = 4;                // distinct source channels per operator row (staged)
-static const unsigned int FZ_POLLS = 1u << 22;  // polls of an exchange word (each an L2 round trip) before giving up
+static const unsigned int FZ_POLLS = 1u << 22;  // barrier polls (each an L2 round trip) before giving up
+enum { P_NRM = 0, P_H1 = 1, P_H2 = 2, P_H3 = 3, P_RES = 4, P_COUNT = 5 };
+
+struct FzBarrier {
+    unsigned int count;  // arrivals during the current launch
+    unsigned int pad;
+};
 
 struct FzArgs {
     OpDev op64, opb;             // structure (rows, entries, slots); the bands are the real copies below
@@ -57,11 +60,42 @@ struct FzArgs {
     cxd *e64;        // [nch*N] correction of the pass (read across channels by the FP64 rows)
     cxf *wbuf;       // [2][nch*N] unnormalised next Krylov vector (read across channels)
     cxf *V;          // [m][nch*N] Krylov vectors (channel a written by CTA a only)
-    unsigned long long *xw;  // [2][CTAs][FZ_PSTRIDE] tagged exchange words (by exchange parity)
-    unsigned int seq;        // launch number (1 .. 2^22 - 1): the high bits of the tags
+    double *part;    // [P_COUNT][CTAs][FZ_PSTRIDE] per-CTA partial sums
+    FzBarrier *bar;
     GmresState *st;
     int *err;
 };
+
+__device__ __forceinline__ unsigned int fz_ld_acquire(const unsigned int *p)
+{
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// All CTAs meet (the launch is cooperative, so all are resident): the arrival count only
+// grows during a launch (it is zeroed before each), the k-th barrier completes when it
+// reaches k * gridDim.x. Returns false, CTA-uniform, when the wait ran out; the error flag is
+// then set.
+__device__ __forceinline__ bool fz_grid_sync(FzBarrier *bar, unsigned int &target, int *err, int *s_ok)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        target += gridDim.x;
+        __threadfence();
+        atomicAdd(&bar->count, 1u);
+        unsigned int polls = 0;
+        while (fz_ld_acquire(&bar->count) < target) {
+            if (++polls > FZ_POLLS) { ok = 0; break; }
+            __nanosleep(32);
+        }
+        if (!ok) atomicExch(err, 2);
+        *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
 
 template <typename R> __device__ __forceinline__ R fz_warp_sum(R v)
 {
@@ -92,58 +126,20 @@ __device__ __forceinline__ cxd fz_ldg(const cxd *p)
     return mk<double>(v.x, v.y);
 }
 
-__device__ __forceinline__ unsigned long long fz_ld_acquire64(const unsigned long long *p)
-{
-    unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void fz_st_release64(unsigned long long *p, unsigned long long v)
-{
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
-// Exchange k of this launch (every CTA runs every exchange, in the same order). This CTA
-// publishes vals[0..nval) (FP64 in shared memory, sent as FP32; nullptr: zeros) in the words
-// of slot k % 2, word 0 always (it marks the arrival); then hs[t] = sum over the writers of
-// value t, FP64 sums in a fixed order (identical in every CTA), over all CTAs for t = 0 and the
-// first nwr for t > 0. Two slots suffice: a CTA can publish exchange k + 2 only after every
-// CTA's word 0 of exchange k + 1, which each CTA writes after reading exchange k. Returns
-// false, CTA-uniform, when a poll ran out (error flag set).
+// Sum over the channels of the partials of one phase: hs[t] = sum_a part[a][t], t < nval,
+// one warp per value, the channels over the lanes, a fixed order (identical in every CTA);
+// FP64 sums, stored as T (float for what enters the FP32 Givens recurrence).
 template <typename T>
-__device__ bool fz_exchange(const FzArgs &a, int &k, const double *vals, int nval, int nwr, T *hs)
+__device__ __forceinline__ void fz_reduce(const double *part, int nch, int nval, T *hs)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();  // vals, and the data this CTA publishes with the exchange, are written
-    const unsigned int tag = (a.seq << 10) | (unsigned int)(k & 1023);
-    unsigned long long *slot = a.xw + (size_t)(k & 1) * gridDim.x * FZ_PSTRIDE;
-    const int nw = max(nval, 1);
-    if (threadIdx.x < nw) {
-        const float v = (vals && threadIdx.x < nval) ? (float)vals[threadIdx.x] : 0.f;
-        fz_st_release64(slot + (size_t)blockIdx.x * FZ_PSTRIDE + threadIdx.x,
-                        ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(v));
+    for (int t = warp; t < nval; t += FZ_NW) {
+        double s = 0.0;
+        for (int a = lane; a < nch; a += 32) s += __ldcg(part + (size_t)a * FZ_PSTRIDE + t);
+        s = fz_warp_sum(s);
+        if (lane == 0) hs[t] = (T)s;
     }
-    int ok = 1;
-    for (int t = warp; t < nw; t += FZ_NW) {
-        const int nread = t == 0 ? (int)gridDim.x : nwr;
-        double sum = 0.0;
-        for (int w = lane; w < nread; w += 32) {
-            const unsigned long long *p = slot + (size_t)w * FZ_PSTRIDE + t;
-            unsigned long long x = fz_ld_acquire64(p);
-            unsigned int polls = 0;
-            while ((unsigned int)(x >> 32) != tag) {
-                if (++polls > FZ_POLLS) { ok = 0; break; }
-                __nanosleep(32);
-                x = fz_ld_acquire64(p);
-            }
-            sum += (double)__uint_as_float((unsigned int)(x & 0xffffffffu));
-        }
-        sum = fz_warp_sum(sum);
-        if (lane == 0) hs[t] = (T)sum;
-    }
-    if (!ok) atomicExch(a.err, 2);
-    k += 1;
-    return __syncthreads_and(ok) != 0;
+    __syncthreads();
 }
 
 // Channel sums of the complex64 fibre xs: out[2q], out[2q+1] = <V_q, xs> for q < J (dots),
@@ -443,7 +439,7 @@ __device__ void fz_backsolve(const FzGivens &G, int k, cxd *ys)
 }
 
 struct FzCtl {
-    int j, cont, k, again, passes;
+    int j, cont, k, again, passes, ok;
     double tol_eff;
     float tol_f;  // tol_eff in FP32, for the per-iteration test
     float s;      // 1/beta for the next Krylov vector (formed once: FP64 division is slow here)
@@ -480,8 +476,9 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                        : nullptr;
     const size_t mat = (size_t)(owner ? ch / a.fib_per_mat : 0);
     cxf *Vc = a.V + (size_t)(owner ? ch : 0) * N;  // V[q][ch] at Vc + q * n
-    __shared__ double cv[FZ_PSTRIDE];  // this CTA's partial sums of the current exchange
-    int kx = 0;                        // exchanges so far in this launch
+    const size_t pstride = (size_t)gridDim.x * FZ_PSTRIDE;
+    double *part_me = a.part + (size_t)ch * FZ_PSTRIDE;  // + phase * pstride
+    unsigned int expect = 0;  // barrier arrivals expected so far (thread 0)
     const bool lead = (ch == 0 && tid == 0);  // keeps the step statistics
 
     if (tid < PG_MAX_SLOTS) {
@@ -514,7 +511,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
     // changed after the second
     fz_rows64<KB>(a.op64, a.rb64, lo, hi, sc_diff, a.psi, a.r64, false);
     if (sband) fz_bands_wait();  // before any exit: no copy outlives the CTA
-    if (!fz_exchange(a, kx, (const double *)nullptr, 0, 0, hd)) return;
+    if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
 
     for (;;) {
         // d = M^-1 r (complex64), published for the first matvec; ||d||^2
@@ -531,9 +528,10 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
             tri_solve_smem<float, cxf, FZ_NW>(nblk, w, mat, a.lo_inv, a.lo_g, a.lo_rb, a.up_inv, a.up_g, a.up_rb, 1,
                                               1, a.g_in_smem, xs, sb, sg);
             for (int i = tid; i < N; i += FZ_THREADS) a.wbuf[(size_t)ch * N + i] = xs[i];
-            fz_channel_sums(Vc, n, 0, true, xs, N, red, cv);
+            fz_channel_sums(Vc, n, 0, true, xs, N, red, part_me + P_NRM * pstride);
         }
-        if (!fz_exchange(a, kx, owner ? cv : nullptr, 1, a.nch, hd)) return;
+        if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
+        fz_reduce(a.part + P_NRM * pstride, a.nch, 1, hd);
         if (tid == 0) {
             const double b = sqrt(fmax(hd[0], 0.0));
             ctl.s = (float)(b > 0.0 ? 1.0 / b : 0.0);
@@ -568,9 +566,10 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                 tri_solve_smem<float, cxf, FZ_NW>(nblk, w, mat, a.lo_inv, a.lo_g, a.lo_rb, a.up_inv, a.up_g, a.up_rb,
                                                   1, 1, a.g_in_smem, xs, sb, sg);
                 // classical Gram-Schmidt, twice: h1 = <V, w>, w -= V h1, h2 = <V, w>, w -= V h2
-                fz_channel_sums(Vc, n, J, false, xs, N, red, cv);
+                fz_channel_sums(Vc, n, J, false, xs, N, red, part_me + P_H1 * pstride);
             }
-            if (!fz_exchange(a, kx, owner ? cv : nullptr, 2 * J, a.nch, hf[0])) return;
+            if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
+            fz_reduce(a.part + P_H1 * pstride, a.nch, 2 * J, hf[0]);
             for (int rep = 0; rep < 2; ++rep) {
                 if (owner) {
                     const float *h = hf[rep];
@@ -598,9 +597,11 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                         if (rep == 1) a.wbuf[(size_t)((j + 1) & 1) * n + (size_t)ch * N + i] = acc;
                     }
                     __syncthreads();
-                    fz_channel_sums(Vc, n, J, rep == 1, xs, N, red, cv);
+                    fz_channel_sums(Vc, n, J, rep == 1, xs, N, red, part_me + (rep == 0 ? P_H2 : P_H3) * pstride);
                 }
-                if (!fz_exchange(a, kx, owner ? cv : nullptr, rep == 0 ? 2 * J : 1, a.nch, hf[rep + 1])) return;
+                if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
+                if (rep == 0) fz_reduce(a.part + P_H2 * pstride, a.nch, 2 * J, hf[1]);
+                else fz_reduce(a.part + P_H3 * pstride, a.nch, 1, hf[2]);
             }
             if (tid == 0) {
                 // |w| in FP32 (it enters the Hessenberg matrix and the next vector as FP32)
@@ -643,11 +644,12 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
             a.e64[o] = mk<double>(ax, ay);
             a.psi[o] = a.psi[o] + mk<double>(ax, ay);
         }
-        if (!fz_exchange(a, kx, (const double *)nullptr, 0, 0, hd)) return;
+        if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
         // r -= (S + i dt/2 H) e in FP64; ||r|| decides whether another pass runs
         const double rn = fz_rows64<KB>(a.op64, a.rb64, lo, hi, sc_negplus, a.e64, a.r64, true);
-        fz_cta_sum64(rn, red, cv);
-        if (!fz_exchange(a, kx, cv, 1, (int)gridDim.x, hd)) return;
+        fz_cta_sum64(rn, red, part_me + P_RES * pstride);
+        if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
+        fz_reduce(a.part + P_RES * pstride, gridDim.x, 1, hd);
         if (tid == 0) {
             const double r = sqrt(fmax(hd[0], 0.0));
             ctl.again = (r > a.tol) && (r == r) && ctl.passes < FZ_MAXPASS;
@@ -665,7 +667,6 @@ struct FusedCayley {
     FzArgs args;
     size_t smem = 0;
     int nctas = 0;
-    unsigned int seq = 0;  // launches so far (mod 2^22)
     bool kb6 = false;  // the instance unrolled for 13-diagonal bands (k = 7 B-splines)
     void *bufs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // real bands, tables
 };
@@ -792,9 +793,8 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
     alloc((void **)&a.e64, sizeof(cxd) * n);
     alloc((void **)&a.wbuf, sizeof(cxf) * 2 * n);
     alloc((void **)&a.V, sizeof(cxf) * (size_t)m * n);
-    alloc((void **)&a.xw, sizeof(unsigned long long) * 2 * (size_t)nctas * FZ_PSTRIDE);
-    if (code == PG_OK && cudaMemset(a.xw, 0, sizeof(unsigned long long) * 2 * (size_t)nctas * FZ_PSTRIDE) != cudaSuccess)
-        code = PG_ERR_CUDA;  // tag 0 is never current: launch numbers start at 1
+    alloc((void **)&a.part, sizeof(double) * P_COUNT * (size_t)nctas * FZ_PSTRIDE);
+    alloc((void **)&a.bar, sizeof(FzBarrier));
     if (code == PG_OK) code = upload_vec(rb64, &f->bufs[0]);
     if (code == PG_OK) code = upload_vec(rb32, &f->bufs[1]);
     if (code == PG_OK) code = upload_vec(ucol, &f->bufs[2]);
@@ -841,14 +841,8 @@ int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams *par
     a.st = st;
     a.tol = tol;
     a.err = err;
-    // launch number for the exchange tags (22 bits); when it wraps, the words are cleared so that
-    // no word left from 2^22 launches earlier can carry a current tag
-    f->seq = (f->seq + 1) & 0x3FFFFFu;
-    if (f->seq == 0) {
-        f->seq = 1;
-        PG_CUDA_TRY(cudaMemsetAsync(a.xw, 0, sizeof(unsigned long long) * 2 * (size_t)f->nctas * FZ_PSTRIDE, s));
-    }
-    a.seq = f->seq;
+    // a barrier left half-way by an earlier launch whose wait ran out starts from zero again
+    PG_CUDA_TRY(cudaMemsetAsync(a.bar, 0, sizeof(FzBarrier), s));
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof(cfg));
     cfg.gridDim = dim3(f->nctas);
@@ -872,7 +866,8 @@ void pg_cayley_fused_free(FusedCayley *f)
     cudaFree(f->args.e64);
     cudaFree(f->args.wbuf);
     cudaFree(f->args.V);
-    cudaFree(f->args.xw);
+    cudaFree(f->args.part);
+    cudaFree(f->args.bar);
     for (void *b : f->bufs) cudaFree(b);
     delete f;
 }
