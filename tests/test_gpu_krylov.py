@@ -149,6 +149,27 @@ def test_cayley_single_kernel_step_long_fibres_and_basis_bound(gpu):
     assert not big.Propagator.Fused
 
 
+def test_cayley_single_kernel_step_other_spline_order(gpu):
+    """B-splines of order 5 (9 diagonals) take the generic-width instance of the single-kernel
+    step: the same states as the multi-kernel step to the GMRES tolerance."""
+    out = {}
+    for fused in (True, False):
+        prob = hydrogen_problem(lmax=4, nbsplines=50, rmax=40.0, propagator="CayleyPropagatorGPU", precision="fp32",
+                                gmres_tolerance=1e-12, order=5)
+        prob.Propagator.FusedStep = fused
+        prob.SetupStep(skipWavefunctionSetup=True)
+        assert prob.Propagator.Fused == fused
+        shape = prob.psi.GetRepresentation().GetFullShape()
+        rng = np.random.default_rng(5)
+        psi = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+        _set_psi(prob, psi / np.linalg.norm(psi))
+        for n in range(5):
+            prob.Propagator.AdvanceStep(1.0 + 0.01 * n, 0.01)
+            assert prob.Propagator.LastStats.TrueResidual < 1e-12
+        out[fused] = prob.psi.numpy()
+    assert relerr(out[True], out[False]) < 1e-10
+
+
 def test_piram_ground_state_shift_invert(gpu):
     """Config-1 model (lmax 10, N 150): shift-invert pIRAM ground state E = -1/2."""
     import pyprop_gb300 as pp
