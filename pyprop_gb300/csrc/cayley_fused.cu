@@ -20,6 +20,14 @@
 // (residual rows, the correction e = V y) are spread over all CTAs: FP64 arithmetic is scarce
 // on this GPU. Grid barriers are bounded waits: one that runs out sets the context's error
 // flag (2) and the CTAs return.
+//
+// Qualifying steppers (pg_cayley_fused_prepare): rank-2 operators whose bands are all real
+// (the complex factors of a Cayley step are the slot scales), at most FZ_MAXU distinct source
+// channels per row, the block-diagonal LU preconditioner, basis size <= FZ_MAXM and no more
+// channels than resident CTAs. Launch: one CTA of 768 threads per SM (cooperative). Shared
+// memory of a channel CTA: the fibre and the block solve's scratch (tri_solve_smem), the
+// staged source fibres of the row product, and, when they fit, the channel's FP32 bands
+// (copied once per step while the first FP64 rows run).
 #include "cayley_state.cuh"
 #include "tri_solve.cuh"
 
