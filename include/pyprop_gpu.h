@@ -60,9 +60,12 @@ int pg_ctx_use_own_stream(pg_ctx *ctx);
 /* Count of kernels this context launched since creation (own kernels only). */
 long long pg_ctx_kernel_launches(pg_ctx *ctx);
 int pg_ctx_synchronize(pg_ctx *ctx);
-/* Device error word: non-zero when a kernel's bounded wait on an asynchronous copy ran out
- * (the kernel then skipped its work). Waits for the context's stream. */
+/* Device error word: non-zero when a kernel's bounded wait ran out (1: an asynchronous copy,
+ * 2: a grid barrier of the single-kernel Cayley step); the kernel then skipped the rest of its
+ * work. Waits for the context's stream. */
 int pg_ctx_device_error(pg_ctx *ctx, int *flag);
+/* Clear the device error word (stream-ordered). */
+int pg_ctx_clear_device_error(pg_ctx *ctx);
 
 /* ---------------------------------------------------------------------------------- */
 /* reference-layout tensor multiply                                                   */
@@ -337,6 +340,11 @@ int pg_cayley_set_eager(pg_cayley *c, int on);
  * same reference step as
  * pg_cayley_step (CayleyPropagator.py:71-150). */
 int pg_cayley_set_fused(pg_cayley *c, int on);
+/* Test hook for the bounded grid barriers of the single-kernel step (no counterpart in the
+ * reference): with extra_arrivals > 0 the first barrier of every later step waits for that
+ * many arrivals more than there are CTAs, so its polls run out (a few seconds); the step then
+ * leaves psi unchanged and sets the device error word to 2. 0 restores normal steps. */
+int pg_cayley_set_barrier_probe(pg_cayley *c, int extra_arrivals);
 /*
  * Learned preconditioner (no counterpart in the reference; mixed-precision steppers only).
  * With a network set, each refinement pass runs flexible GMRES right-preconditioned by

@@ -66,6 +66,7 @@ _SIGS = {
     "pg_ctx_kernel_launches": (_LL, [_P]),
     "pg_ctx_synchronize": (_I, [_P]),
     "pg_ctx_device_error": (_I, [_P, _IP]),
+    "pg_ctx_clear_device_error": (_I, [_P]),
     "pg_tensor_multiply_diag_bandnh": (_I, [_P, _I, _I, _D, _P, _I, _I, _P, _I, _I, _I, _P]),
     "pg_tensor_multiply_simp_bandnh": (_I, [_P, _I, _I, _D, _P, _I, _I, _P, _I, _I, _P, _I, _I, _I, _P]),
     "pg_tensor_multiply_ident_bandnh": (_I, [_P, _I, _I, _D, _P, _I, _I, _P, _I, _I, _I, _P]),
@@ -101,6 +102,7 @@ _SIGS = {
     "pg_cayley_set_true_residual": (_I, [_P, _I]),
     "pg_cayley_set_eager": (_I, [_P, _I]),
     "pg_cayley_set_fused": (_I, [_P, _I]),
+    "pg_cayley_set_barrier_probe": (_I, [_P, _I]),
     "pg_cayley_set_learned": (_I, [_P, _P, _I]),
     "pg_cayley_learned_rejected": (_I, [_P, C.POINTER(_LL)]),
     "pg_cayley_batch_create": (_I, [C.POINTER(_P), _I, C.POINTER(_P)]),

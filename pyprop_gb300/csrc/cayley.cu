@@ -889,6 +889,14 @@ extern "C" int pg_cayley_set_fused(pg_cayley *c, int on)
     return PG_OK;
 }
 
+extern "C" int pg_cayley_set_barrier_probe(pg_cayley *c, int extra_arrivals)
+{
+    if (!c || extra_arrivals < 0) return PG_ERR_ARG;
+    if (!c->fused) return PG_ERR_STATE;
+    pg_cayley_fused_set_probe(c->fused, (unsigned int)extra_arrivals);
+    return PG_OK;
+}
+
 extern "C" int pg_cayley_set_true_residual(pg_cayley *c, int on)
 {
     if (!c) return PG_ERR_ARG;

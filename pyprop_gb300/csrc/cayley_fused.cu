@@ -58,6 +58,7 @@ struct FzArgs {
     const unsigned char *ent_u;  // [entries of opb] which staged source an entry reads
     const int *row_lo;           // [CTAs + 1] FP64 rows of each CTA (equal numbers of band entries)
     int bands_smem;              // 1: each channel's FP32 bands are copied to shared memory per step
+    unsigned int probe_extra;    // test hook: arrivals the first barrier waits for in addition (0)
     const cxf *lo_inv, *lo_g, *lo_rb, *up_inv, *up_g, *up_rb;
     int nblk, w, fib_per_mat, g_in_smem;
     int nch, N, m;
@@ -486,7 +487,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
     cxf *Vc = a.V + (size_t)(owner ? ch : 0) * N;  // V[q][ch] at Vc + q * n
     const size_t pstride = (size_t)gridDim.x * FZ_PSTRIDE;
     double *part_me = a.part + (size_t)ch * FZ_PSTRIDE;  // + phase * pstride
-    unsigned int expect = 0;  // barrier arrivals expected so far (thread 0)
+    unsigned int expect = a.probe_extra;  // barrier arrivals expected so far (thread 0)
     const bool lead = (ch == 0 && tid == 0);  // keeps the step statistics
 
     if (tid < PG_MAX_SLOTS) {
@@ -865,6 +866,11 @@ int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams *par
     if (f->kb6) PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, cay_fused_step_kernel<6>, a));
     else PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, cay_fused_step_kernel<-1>, a));
     return PG_OK;
+}
+
+void pg_cayley_fused_set_probe(FusedCayley *f, unsigned int extra_arrivals)
+{
+    if (f) f->args.probe_extra = extra_arrivals;
 }
 
 void pg_cayley_fused_free(FusedCayley *f)

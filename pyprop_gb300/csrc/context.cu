@@ -130,6 +130,13 @@ extern "C" int pg_ctx_device_error(pg_ctx *ctx, int *flag)
     return PG_OK;
 }
 
+extern "C" int pg_ctx_clear_device_error(pg_ctx *ctx)
+{
+    if (!ctx) return PG_ERR_ARG;
+    PG_CUDA_TRY(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    return PG_OK;
+}
+
 extern "C" int pg_ctx_synchronize(pg_ctx *ctx)
 {
     if (!ctx) return PG_ERR_ARG;

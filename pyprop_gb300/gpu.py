@@ -73,6 +73,10 @@ class Context:
         check(self.lib.pg_ctx_device_error(self.h, C.byref(flag)), "pg_ctx_device_error")
         return int(flag.value)
 
+    def clear_device_error(self):
+        self.bind_stream()
+        check(self.lib.pg_ctx_clear_device_error(self.h), "pg_ctx_clear_device_error")
+
 
 def complex_dtype(precision):
     t = torch()
@@ -405,6 +409,11 @@ class CayleyStepper:
             return False
         check(code, "pg_cayley_set_fused")
         return bool(on)
+
+    def set_barrier_probe(self, extra_arrivals):
+        """Test hook: the first grid barrier of later single-kernel steps waits for arrivals that
+        never come (its bounded polls run out; error word 2); 0 restores normal steps."""
+        check(self.lib.pg_cayley_set_barrier_probe(self.h, int(extra_arrivals)), "pg_cayley_set_barrier_probe")
 
     def __del__(self):
         try:

@@ -149,6 +149,35 @@ def test_cayley_single_kernel_step_long_fibres_and_basis_bound(gpu):
     assert not big.Propagator.Fused
 
 
+def test_cayley_single_kernel_step_bounded_barrier_wait(gpu):
+    """A grid barrier of the single-kernel step whose arrivals never all come (the test hook
+    adds one arrival that no CTA makes) gives up after its bounded polls: the step returns, the
+    device error word reads 2, psi is unchanged, and the next normal step is correct."""
+    g = golden("hydrogen_small.npz")
+    prob = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp32", gmres_tolerance=1e-12)
+    prob.SetupStep(skipWavefunctionSetup=True)
+    assert prob.Propagator.Fused
+    stepper = prob.Propagator.stepper
+    ctx = prob.Propagator.op64.ctx
+    _set_psi(prob, g["psi"])
+    scales = prob.Propagator.op64.scales(1.005)
+    ctx.clear_device_error()
+    stepper.set_barrier_probe(1)
+    stepper.step(prob.psi.GetData(), 0.01, scales)
+    assert ctx.device_error() == 2
+    assert relerr(prob.psi.numpy(), g["psi"]) == 0.0
+    stepper.set_barrier_probe(0)
+    ctx.clear_device_error()
+    st = stepper.step(prob.psi.GetData(), 0.01, scales)
+    assert ctx.device_error() == 0
+    assert st.TrueResidual < 1e-12
+    ref = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp32", gmres_tolerance=1e-12)
+    ref.SetupStep(skipWavefunctionSetup=True)
+    _set_psi(ref, g["psi"])
+    ref.Propagator.stepper.step(ref.psi.GetData(), 0.01, scales)
+    assert relerr(prob.psi.numpy(), ref.psi.numpy()) < 1e-13
+
+
 def test_cayley_single_kernel_step_other_spline_order(gpu):
     """B-splines of order 5 (9 diagonals) take the generic-width instance of the single-kernel
     step: the same states as the multi-kernel step to the GMRES tolerance."""
