@@ -149,6 +149,40 @@ def test_cayley_single_kernel_step_long_fibres_and_basis_bound(gpu):
     assert not big.Propagator.Fused
 
 
+def test_cayley_single_kernel_step_full_size_properties(gpu):
+    """At the benchmark's full size (lmax 40, 600 B-splines, 41 x 600 coefficients, dt 0.01 in
+    the 800 nm pulse) size-independent properties of 40 mixed single-kernel steps: every step
+    meets the FP64 true-residual bound, the S-norm is conserved (Crank-Nicolson is unitary in
+    the S metric) to 1e-10, and the state equals the plain FP64 path's to 1e-12 infidelity."""
+    import pyprop_gb300 as pp
+    from pyprop_gb300.workloads import hydrogen
+    kw = dict(lmax=40, nbsplines=600, rmax=400.0, timestep=0.01, pulse_duration=50.0, amplitude=0.05,
+              wavelength_nm=800.0, krylov_basis_size=20, gmres_tolerance=1e-12, duration=50.0)
+    out = {}
+    for prec in ("fp32", "fp64"):
+        prob = pp.Problem(pp.LoadString(hydrogen(propagator="CayleyPropagatorGPU", precision=prec, **kw)))
+        prob.SetupStep(skipWavefunctionSetup=True)
+        assert prob.Propagator.Fused == (prec == "fp32")
+        shape = prob.psi.GetRepresentation().GetFullShape()
+        rng = np.random.default_rng(40)
+        psi = np.zeros(shape, complex)
+        i = np.arange(shape[1])
+        psi[0] = np.exp(-((i - 60.0) / 25.0) ** 2)
+        psi[1] = 0.2 * np.exp(-((i - 80.0) / 30.0) ** 2) * (1 + 0.1j * rng.normal(size=shape[1]))
+        prob.psi.SetData(psi / np.linalg.norm(psi))
+        prob.PropagatedTime = 20.0  # near the pulse maximum
+        S = prob.psi.GetRepresentation().radial.BSplineObject.dense(prob.psi.GetRepresentation().overlap_rows)
+        n0 = np.vdot(prob.psi.numpy(), prob.psi.numpy() @ S.T).real
+        for _ in range(40):
+            prob.AdvanceStep()
+            if prec == "fp32":
+                assert prob.Propagator.LastStats.TrueResidual < 1e-12
+        final = prob.psi.numpy()
+        assert abs(np.vdot(final, final @ S.T).real / n0 - 1.0) < 1e-10, prec
+        out[prec] = final
+    assert infidelity(out["fp64"], out["fp32"], S) < 1e-12
+
+
 def test_cayley_single_kernel_step_bounded_barrier_wait(gpu):
     """A grid barrier of the single-kernel step whose arrivals never all come (the test hook
     adds one arrival that no CTA makes) gives up after its bounded polls: the step returns, the
