@@ -313,7 +313,8 @@ int pg_cayley_destroy(pg_cayley *c);
 /* One step. scales: host complex128 [nscales] slot values of H(t + dt/2) (slot 0 is
  * ignored: the overlap weight is fixed). With stats non-NULL the call waits for the step and
  * fills them (Iterations, ErrorEstimate = last least-squares residual, TrueResidual); with
- * NULL it returns after enqueueing. */
+ * NULL it returns after enqueueing. PG_ERR_NOT_CONVERGED (with stats) when the step was
+ * abandoned because a bounded wait ran out (psi unchanged; device error word set). */
 int pg_cayley_step(pg_cayley *c, void *psi, double dt, const double *scales, int nscales,
                    pg_krylov_stats *stats);
 /* nsteps steps; scales_table: host complex128 [nsteps][nscales]. */

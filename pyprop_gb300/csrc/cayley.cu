@@ -801,8 +801,10 @@ static int cayley_launch(pg_cayley *c, cxd *psi, double dt, const double *scales
 }
 
 // statistics of the last completed step; adds the kernels run since the last call to the
-// context's launch count
-static void fill_stats(pg_cayley *c, pg_krylov_stats *st)
+// context's launch count. PG_ERR_NOT_CONVERGED when that step was abandoned: every step runs
+// at least one pass, so no pass means a bounded wait ran out before the first (the
+// single-kernel step then leaves psi unchanged; the device error word says which wait).
+static int fill_stats(pg_cayley *c, pg_krylov_stats *st)
 {
     const GmresStats &g = *c->h_stats;
     c->ctx->launches += g.kernels - c->kernels_counted;
@@ -814,6 +816,7 @@ static void fill_stats(pg_cayley *c, pg_krylov_stats *st)
     st->RestartCount = g.passes;
     st->ErrorEstimate = g.resid;
     st->TrueResidual = g.true_resid;
+    return g.passes > 0 ? PG_OK : PG_ERR_NOT_CONVERGED;
 }
 
 extern "C" int pg_cayley_step(pg_cayley *c, void *psi, double dt, const double *scales, int nscales, pg_krylov_stats *st)
@@ -822,7 +825,7 @@ extern "C" int pg_cayley_step(pg_cayley *c, void *psi, double dt, const double *
     PG_TRY(cayley_launch(c, (cxd *)psi, dt, scales, nscales));
     if (st) {
         PG_CUDA_TRY(cudaStreamSynchronize(c->ctx->stream));
-        fill_stats(c, st);
+        return fill_stats(c, st);
     }
     return PG_OK;
 }
@@ -916,8 +919,8 @@ extern "C" int pg_cayley_advance(pg_cayley *c, void *psi, double dt, int nsteps,
         PG_TRY(cayley_launch(c, (cxd *)psi, dt, scales_table + 2 * (size_t)k * nscales, nscales));
     if (st) {
         PG_CUDA_TRY(cudaStreamSynchronize(c->ctx->stream));
-        fill_stats(c, st);
         (void)iters;
+        return fill_stats(c, st);
     }
     return PG_OK;
 }
@@ -926,8 +929,7 @@ extern "C" int pg_cayley_last_stats(pg_cayley *c, pg_krylov_stats *st)
 {
     if (!c || !st) return PG_ERR_ARG;
     PG_CUDA_TRY(cudaStreamSynchronize(c->ctx->stream));
-    fill_stats(c, st);
-    return PG_OK;
+    return fill_stats(c, st);
 }
 
 // ------------------------------------------------------------------------------------

@@ -186,7 +186,8 @@ def test_cayley_single_kernel_step_full_size_properties(gpu):
 def test_cayley_single_kernel_step_bounded_barrier_wait(gpu):
     """A grid barrier of the single-kernel step whose arrivals never all come (the test hook
     adds one arrival that no CTA makes) gives up after its bounded polls: the step returns, the
-    device error word reads 2, psi is unchanged, and the next normal step is correct."""
+    device error word reads 2, the step call reports it, psi is unchanged, and the next normal
+    step is correct."""
     g = golden("hydrogen_small.npz")
     prob = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp32", gmres_tolerance=1e-12)
     prob.SetupStep(skipWavefunctionSetup=True)
@@ -197,7 +198,9 @@ def test_cayley_single_kernel_step_bounded_barrier_wait(gpu):
     scales = prob.Propagator.op64.scales(1.005)
     ctx.clear_device_error()
     stepper.set_barrier_probe(1)
-    stepper.step(prob.psi.GetData(), 0.01, scales)
+    with pytest.raises(nat.PygpuError) as exc:
+        stepper.step(prob.psi.GetData(), 0.01, scales)
+    assert exc.value.code == -7  # PG_ERR_NOT_CONVERGED: the step was abandoned
     assert ctx.device_error() == 2
     assert relerr(prob.psi.numpy(), g["psi"]) == 0.0
     stepper.set_barrier_probe(0)
