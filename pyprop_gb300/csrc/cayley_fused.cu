@@ -26,8 +26,9 @@
 // channels per row, the block-diagonal LU preconditioner, basis size <= FZ_MAXM and no more
 // channels than resident CTAs. Launch: one CTA of 768 threads per SM (cooperative). Shared
 // memory of a channel CTA: the fibre and the block solve's scratch (tri_solve_smem), the
-// staged source fibres of the row product, and, when they fit, the channel's FP32 bands
-// (copied once per step while the first FP64 rows run).
+// staged source fibres of the row product, and, when they fit, the channel's Krylov vectors
+// (Gram-Schmidt reads them from there), else the channel's FP32 bands (copied once per step
+// while the first FP64 rows run).
 #include "cayley_state.cuh"
 #include "tri_solve.cuh"
 
@@ -58,6 +59,7 @@ struct FzArgs {
     const unsigned char *ent_u;  // [entries of opb] which staged source an entry reads
     const int *row_lo;           // [CTAs + 1] FP64 rows of each CTA (equal numbers of band entries)
     int bands_smem;              // 1: each channel's FP32 bands are copied to shared memory per step
+    int v_smem;                  // 1: a channel's Krylov vectors are also kept in shared memory
     unsigned int probe_extra;    // test hook: arrivals the first barrier waits for in addition (0)
     const cxf *lo_inv, *lo_g, *lo_rb, *up_inv, *up_g, *up_rb;
     int nblk, w, fib_per_mat, g_in_smem;
@@ -479,12 +481,16 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
     cxf *sg = sb + (size_t)nblk * w;           // [nblk][w][32] (g_in_smem)
     cxf *xsrc = sg + (a.g_in_smem ? (size_t)nblk * w * 32 : 0);  // [FZ_MAXU][N + 2kb] staged sources
     // [entries][2kb+1][ld] this channel's FP32 bands (16-byte aligned), when they fit
-    float *sband = (owner && a.bands_smem)
-                       ? (float *)(fz_smem + ((((size_t)npad + (size_t)nblk * w * (a.g_in_smem ? 33 : 1) +
-                                                (size_t)FZ_MAXU * (N + 2 * a.opb.kb)) * sizeof(cxf) + 15) / 16) * 16)
-                       : nullptr;
     const size_t mat = (size_t)(owner ? ch / a.fib_per_mat : 0);
     cxf *Vc = a.V + (size_t)(owner ? ch : 0) * N;  // V[q][ch] at Vc + q * n
+    unsigned char *extra = fz_smem + ((((size_t)npad + (size_t)nblk * w * (a.g_in_smem ? 33 : 1) +
+                                       (size_t)FZ_MAXU * (N + 2 * a.opb.kb)) * sizeof(cxf) + 15) / 16) * 16;
+    float *sband = (owner && a.bands_smem) ? (float *)extra : nullptr;
+    // [m][N] this channel's Krylov vectors, when they fit (read by the same thread that wrote
+    // each row; the global copy serves the correction e = V y of the other CTAs)
+    cxf *sV = (owner && a.v_smem) ? (cxf *)extra : nullptr;
+    const cxf *Vr = sV ? sV : Vc;
+    const long long vld = sV ? (long long)N : n;
     const size_t pstride = (size_t)gridDim.x * FZ_PSTRIDE;
     double *part_me = a.part + (size_t)ch * FZ_PSTRIDE;  // + phase * pstride
     unsigned int expect = a.probe_extra;  // barrier arrivals expected so far (thread 0)
@@ -537,7 +543,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
             tri_solve_smem<float, cxf, FZ_NW>(nblk, w, mat, a.lo_inv, a.lo_g, a.lo_rb, a.up_inv, a.up_g, a.up_rb, 1,
                                               1, a.g_in_smem, xs, sb, sg);
             for (int i = tid; i < N; i += FZ_THREADS) a.wbuf[(size_t)ch * N + i] = xs[i];
-            fz_channel_sums(Vc, n, 0, true, xs, N, red, part_me + P_NRM * pstride);
+            fz_channel_sums(Vr, vld, 0, true, xs, N, red, part_me + P_NRM * pstride);
         }
         if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
         fz_reduce(a.part + P_NRM * pstride, a.nch, 1, hd);
@@ -568,14 +574,16 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                 // V_j = w / beta (this channel), then xs = M^-1 A V_j (row ch)
                 for (int i = tid; i < N; i += FZ_THREADS) {
                     const cxf v = xs[i];
-                    Vc[(size_t)j * n + i] = mk<float>(v.x * s, v.y * s);
+                    const cxf vs = mk<float>(v.x * s, v.y * s);
+                    Vc[(size_t)j * n + i] = vs;
+                    if (sV) sV[(size_t)j * N + i] = vs;
                 }
                 fz_matvec32<KB>(a, ch, sc_plus, a.wbuf + (size_t)(j & 1) * n, s, xs, npad, xsrc, sband);
                 __syncthreads();
                 tri_solve_smem<float, cxf, FZ_NW>(nblk, w, mat, a.lo_inv, a.lo_g, a.lo_rb, a.up_inv, a.up_g, a.up_rb,
                                                   1, 1, a.g_in_smem, xs, sb, sg);
                 // classical Gram-Schmidt, twice: h1 = <V, w>, w -= V h1, h2 = <V, w>, w -= V h2
-                fz_channel_sums(Vc, n, J, false, xs, N, red, part_me + P_H1 * pstride);
+                fz_channel_sums(Vr, vld, J, false, xs, N, red, part_me + P_H1 * pstride);
             }
             if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
             fz_reduce(a.part + P_H1 * pstride, a.nch, 2 * J, hf[0]);
@@ -591,7 +599,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                             cxf v[FZ_CB];
 #pragma unroll
                             for (int q = 0; q < FZ_CB; ++q)
-                                v[q] = q0 + q < J ? Vc[(size_t)(q0 + q) * n + i] : mk<float>(0.f, 0.f);
+                                v[q] = q0 + q < J ? Vr[(size_t)(q0 + q) * vld + i] : mk<float>(0.f, 0.f);
 #pragma unroll
                             for (int q = 0; q < FZ_CB; ++q) {
                                 if (q0 + q >= J) break;
@@ -606,7 +614,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                         if (rep == 1) a.wbuf[(size_t)((j + 1) & 1) * n + (size_t)ch * N + i] = acc;
                     }
                     __syncthreads();
-                    fz_channel_sums(Vc, n, J, rep == 1, xs, N, red, part_me + (rep == 0 ? P_H2 : P_H3) * pstride);
+                    fz_channel_sums(Vr, vld, J, rep == 1, xs, N, red, part_me + (rep == 0 ? P_H2 : P_H3) * pstride);
                 }
                 if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
                 if (rep == 0) fz_reduce(a.part + P_H2 * pstride, a.nch, 2 * J, hf[1]);
@@ -755,8 +763,14 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
     int max_e = 0;
     for (int r = 0; r < nch; ++r) max_e = std::max(max_e, opb->h_row_ptr[r + 1] - opb->h_row_ptr[r]);
     const size_t band_bytes = (size_t)max_e * (2 * kb + 1) * opb->ld * sizeof(float);
-    int g_in_smem = 1, bands_smem = 1;
-    size_t smem = fz_smem_bytes(N, nblk, w, kb, 1, band_bytes);
+    const size_t v_bytes = (size_t)m * N * sizeof(cxf);
+    int g_in_smem = 1, bands_smem = 0, v_smem = 1;
+    size_t smem = fz_smem_bytes(N, nblk, w, kb, 1, v_bytes);
+    if (smem > limit) {
+        v_smem = 0;
+        bands_smem = 1;
+        smem = fz_smem_bytes(N, nblk, w, kb, 1, band_bytes);
+    }
     if (smem > limit) {
         bands_smem = 0;
         smem = fz_smem_bytes(N, nblk, w, kb, 1, 0);
@@ -790,6 +804,7 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
     a.fib_per_mat = std::max(1, precb->fib_per_mat);
     a.g_in_smem = g_in_smem;
     a.bands_smem = bands_smem;
+    a.v_smem = v_smem;
     a.nch = nch;
     a.N = N;
     a.m = m;
