@@ -125,17 +125,6 @@ __device__ __forceinline__ cxd fz_ldcg(const cxd *p)
     const double2 v = __ldcg((const double2 *)p);
     return mk<double>(v.x, v.y);
 }
-// read-only data (operator bands)
-__device__ __forceinline__ cxf fz_ldg(const cxf *p)
-{
-    const float2 v = __ldg((const float2 *)p);
-    return mk<float>(v.x, v.y);
-}
-__device__ __forceinline__ cxd fz_ldg(const cxd *p)
-{
-    const double2 v = __ldg((const double2 *)p);
-    return mk<double>(v.x, v.y);
-}
 
 // Sum over the channels of the partials of one phase: hs[t] = sum_a part[a][t], t < nval,
 // one warp per value, the channels over the lanes, a fixed order (identical in every CTA);
