@@ -609,14 +609,29 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def _rank_world():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+
+
+def _my_members(n):
+    """This rank's share of the ensemble's member parameters (replicas only: each rank steps
+    its own contiguous range, no collective on the data path)."""
+    from pyprop_gb300.ensemble import hydrogen_ensemble_params, partition_members
+    rank, world = _rank_world()
+    a, b = partition_members(n, world, rank)
+    return hydrogen_ensemble_params(n)[a:b]
+
+
 def run_ensemble(args, torch, flush):
     """Batched ensemble: member-steps/s of one graph launch per ensemble step (mixed
-    precision), against the same members stepped one at a time on the plain FP64 path."""
+    precision), against the same members stepped one at a time on the plain FP64 path. With
+    several ranks each steps its share of the members; the job rate is the member steps of
+    all ranks over the slowest rank's time."""
     import pyprop_gb300 as pp
-    from pyprop_gb300.ensemble import CayleyEnsembleGPU, hydrogen_ensemble_params
+    from pyprop_gb300.ensemble import CayleyEnsembleGPU, job_throughput
     from pyprop_gb300.workloads import hydrogen
     t_setup = time.perf_counter()
-    params = hydrogen_ensemble_params(args.ensemble)
+    params = _my_members(args.ensemble)
 
     def member(prm, precision):
         p = pp.Problem(pp.LoadString(hydrogen(propagator="CayleyPropagatorGPU", precision=precision, rmax=100.0,
@@ -670,8 +685,8 @@ def run_ensemble(args, torch, flush):
             n64 += 1
         del p64
     fp64_rate = n64 / t64
-    rate = member_steps / total
-    return {"members": len(probs), "member_steps_per_s": rate, "ms_per_ensemble_step": 1e3 * total / K,
+    rate, _, t_job = job_throughput(member_steps, total, _rank_world()[1])
+    return {"members": args.ensemble, "member_steps_per_s": rate, "ms_per_ensemble_step": 1e3 * t_job / K,
             "gmres_iterations_per_member_step": iters / member_steps,
             "plain_fp64_single_member_steps_per_s": fp64_rate, "speedup_vs_plain_fp64": rate / fp64_rate,
             "workload": "%d hydrogen members, lmax U{8..32}, N U{100..400} on r in [0,100], E0 U[0.01,0.1], "
@@ -686,10 +701,10 @@ def run_pamp_ensemble(args, torch, flush):
     per ensemble step, against the same members stepped one at a time on the plain FP64 pAMP
     path (host exponential)."""
     import pyprop_gb300 as pp
-    from pyprop_gb300.ensemble import PamEnsembleGPU, hydrogen_ensemble_params
+    from pyprop_gb300.ensemble import PamEnsembleGPU, job_throughput
     from pyprop_gb300.workloads import hydrogen
     t_setup = time.perf_counter()
-    params = hydrogen_ensemble_params(args.ensemble)
+    params = _my_members(args.ensemble)
 
     def member(prm, precision):
         p = pp.Problem(pp.LoadString(hydrogen(propagator="PamPropagatorGPU", precision=precision, rmax=100.0,
@@ -741,9 +756,9 @@ def run_pamp_ensemble(args, torch, flush):
             n64 += 1
         del p64
     fp64_rate = n64 / t64
-    rate = member_steps / total
+    rate, _, t_job = job_throughput(member_steps, total, _rank_world()[1])
     del ens
-    return {"members": len(probs), "member_steps_per_s": rate, "ms_per_ensemble_step": 1e3 * total / K,
+    return {"members": args.ensemble, "member_steps_per_s": rate, "ms_per_ensemble_step": 1e3 * t_job / K,
             "max_error_estimate": err, "plain_fp64_single_member_steps_per_s": fp64_rate,
             "speedup_vs_plain_fp64": rate / fp64_rate,
             "workload": "the members of `ensemble` with pAMP (m=20, complex64 basis, FP64 sums), one graph launch "

@@ -314,10 +314,15 @@ int pg_cayley_destroy(pg_cayley *c);
  * ignored: the overlap weight is fixed). With stats non-NULL the call waits for the step and
  * fills them (Iterations, ErrorEstimate = last least-squares residual, TrueResidual); with
  * NULL it returns after enqueueing. PG_ERR_NOT_CONVERGED (with stats) when the step was
- * abandoned because a bounded wait ran out (psi unchanged; device error word set). */
+ * abandoned because a bounded wait ran out: the context's device error word is set (it stays
+ * set, and later steps report the same, until pg_ctx_clear_device_error). A step abandoned
+ * before its first refinement pass leaves psi unchanged; one abandoned later may leave psi
+ * partly corrected. */
 int pg_cayley_step(pg_cayley *c, void *psi, double dt, const double *scales, int nscales,
                    pg_krylov_stats *stats);
-/* nsteps steps; scales_table: host complex128 [nsteps][nscales]. */
+/* nsteps steps; scales_table: host complex128 [nsteps][nscales]. With stats non-NULL the
+ * call waits and fills the last step's statistics; PG_ERR_NOT_CONVERGED when any of the steps
+ * was abandoned (the device error word, as for pg_cayley_step). */
 int pg_cayley_advance(pg_cayley *c, void *psi, double dt, int nsteps, const double *scales_table,
                       int nscales, pg_krylov_stats *stats);
 /* Statistics of the last completed step (waits for the stream). */
@@ -342,10 +347,12 @@ int pg_cayley_set_eager(pg_cayley *c, int on);
  * pg_cayley_step (CayleyPropagator.py:71-150). */
 int pg_cayley_set_fused(pg_cayley *c, int on);
 /* Test hook for the bounded grid barriers of the single-kernel step (no counterpart in the
- * reference): with extra_arrivals > 0 the first barrier of every later step waits for that
- * many arrivals more than there are CTAs, so its polls run out (a few seconds); the step then
- * leaves psi unchanged and sets the device error word to 2. 0 restores normal steps. */
-int pg_cayley_set_barrier_probe(pg_cayley *c, int extra_arrivals);
+ * reference): with extra_arrivals > 0, grid barrier number at_barrier (0 = the first of a
+ * step) of every later step waits for that many arrivals more than there are CTAs, so its
+ * polls run out (a few seconds); the step returns early and sets the device error word to 2,
+ * and the step call reports PG_ERR_NOT_CONVERGED. A step abandoned at barrier 0 leaves psi
+ * unchanged. extra_arrivals = 0 restores normal steps. */
+int pg_cayley_set_barrier_probe(pg_cayley *c, int extra_arrivals, int at_barrier);
 /*
  * Learned preconditioner (no counterpart in the reference; mixed-precision steppers only).
  * With a network set, each refinement pass runs flexible GMRES right-preconditioned by
@@ -442,16 +449,20 @@ int pg_mlp_block_features(pg_ctx *ctx, const void *y, int nblk, int N, int d_in,
  *     out[2J] = ||w||^2, out[2J+1] = ||w||
  * for complex128 (PG_FP64) or complex64 (PG_FP32) device vectors, written to the caller's
  * device buffer `out` (2J+2 doubles), on `stream` (NULL = legacy default stream). No
- * counterpart in the reference: it serves callers that must not allocate device memory -
- * code recorded into a CUDA graph under global stream capture (where cudaMalloc is not
- * permitted), and hosts that give the library a fixed memory budget at start-up. It needs no
- * pg_ctx and calls no cudaMalloc, cudaFree or allocating library routine: its scratch
- * (per-CTA partial sums and the arrival ticket) is a static device array of about 320 KB that
- * every GPU loading the library keeps until the process exits, so J is limited to 64 vectors
- * (PG_ERR_ARG above that). The first call on a device looks up the array's address on that
- * device (cudaGetSymbolAddress); make that first call before any stream capture. All calls
- * share the one array: calls that overlap on the GPU (two streams, two threads) race and give
- * wrong sums - serialize them.
+ * counterpart in the reference. It is for callers that cannot allocate device memory: a host
+ * application whose own pool allocator has reserved the GPU's memory at start-up (a
+ * cudaMalloc from the library would fail, or take memory the application budgets itself),
+ * and steady-state stepping loops that must not pay cudaMalloc/cudaFree's implicit
+ * device-wide synchronization, which stalls the other streams. It needs no pg_ctx and calls
+ * no cudaMalloc, cudaFree or allocating library routine: its scratch (per-CTA partial sums
+ * and the arrival ticket) is a static device array of about 320 KB that every GPU loading the
+ * library keeps until the process exits, so J is limited to 64 vectors (PG_ERR_ARG above
+ * that). The first call on a device looks up the array's address on that device
+ * (cudaGetSymbolAddress) and keeps it for the life of the process: do not use this entry
+ * point across cudaDeviceReset. Make that first call before any stream capture. All calls
+ * share the one array and it keeps the last call's contents (the arrival ticket is cleared
+ * at the start of every call): calls that overlap on the GPU (two streams, two threads)
+ * race and give wrong sums - serialize them.
  */
 int pg_vec_multidot_noalloc(int precision, const void *V, long long ldv, int J, const void *w,
                             long long n, double *out, void *stream);

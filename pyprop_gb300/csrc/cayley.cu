@@ -367,6 +367,7 @@ struct pg_cayley {
     double *h1 = nullptr, *h2 = nullptr, *h3 = nullptr, *nrm = nullptr, *nrm2 = nullptr;
     GmresState *st = nullptr;
     GmresStats *h_stats = nullptr;
+    int *h_err = nullptr;             // the context's device error word after the last step (pinned)
     StepParams *d_params = nullptr;
     StepParams *h_ring = nullptr;
     cudaEvent_t ring_ev[RING];
@@ -714,6 +715,8 @@ extern "C" int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64,
     PG_CUDA_TRY(cudaMemset(c->st, 0, sizeof(GmresState)));
     PG_CUDA_TRY(cudaMallocHost(&c->h_stats, sizeof(GmresStats)));
     memset(c->h_stats, 0, sizeof(GmresStats));
+    PG_CUDA_TRY(cudaMallocHost(&c->h_err, sizeof(int)));
+    *c->h_err = 0;
     PG_CUDA_TRY(cudaMalloc(&c->d_params, sizeof(StepParams)));
     c->params_dev = c->d_params;
     c->rctx.device = c->ctx->device;
@@ -757,6 +760,7 @@ extern "C" int pg_cayley_destroy(pg_cayley *c)
     for (void *b : bufs) cudaFree(b);
     if (c->rctx.h_pinned) cudaFreeHost(c->rctx.h_pinned);
     if (c->h_stats) cudaFreeHost(c->h_stats);
+    if (c->h_err) cudaFreeHost(c->h_err);
     if (c->h_ring) cudaFreeHost(c->h_ring);
     delete c;
     return PG_OK;
@@ -788,22 +792,26 @@ static int cayley_launch(pg_cayley *c, cxd *psi, double dt, const double *scales
     if (fused) {
         PG_TRY(pg_cayley_fused_launch(c->fused, ctx->stream, c->d_params, psi, c->st, c->tol, ctx->d_err));
         PG_CUDA_TRY(cudaMemcpyAsync(c->h_stats, &c->st->stats, sizeof(GmresStats), cudaMemcpyDeviceToHost, ctx->stream));
-        return PG_OK;
-    }
-    if (c->eager) {
+    } else if (c->eager) {
         c->rctx.stream = ctx->stream;
         const int code = (c->prec == PG_FP64) ? record_fp64(c, psi) : record_mixed(c, psi);
         ctx->launches = launches;
-        return code;
+        PG_TRY(code);
+    } else {
+        PG_CUDA_TRY(cudaGraphLaunch(c->exec, ctx->stream));
     }
-    PG_CUDA_TRY(cudaGraphLaunch(c->exec, ctx->stream));
+    // the error word is sticky (until pg_ctx_clear_device_error): read after the step, it says
+    // whether a bounded wait of this step, or of an earlier one, ran out
+    PG_CUDA_TRY(cudaMemcpyAsync(c->h_err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     return PG_OK;
 }
 
 // statistics of the last completed step; adds the kernels run since the last call to the
-// context's launch count. PG_ERR_NOT_CONVERGED when that step was abandoned: every step runs
-// at least one pass, so no pass means a bounded wait ran out before the first (the
-// single-kernel step then leaves psi unchanged; the device error word says which wait).
+// context's launch count. PG_ERR_NOT_CONVERGED when a step was abandoned: the context's device
+// error word was set when the last step ended (a bounded wait of that step or of an earlier one
+// since the word was last cleared ran out; the word says which kind), or no refinement pass
+// started. A single-kernel step abandoned at its first grid barrier leaves psi unchanged; one
+// abandoned later may have left psi partly corrected.
 static int fill_stats(pg_cayley *c, pg_krylov_stats *st)
 {
     const GmresStats &g = *c->h_stats;
@@ -816,7 +824,7 @@ static int fill_stats(pg_cayley *c, pg_krylov_stats *st)
     st->RestartCount = g.passes;
     st->ErrorEstimate = g.resid;
     st->TrueResidual = g.true_resid;
-    return g.passes > 0 ? PG_OK : PG_ERR_NOT_CONVERGED;
+    return (g.passes > 0 && *c->h_err == 0) ? PG_OK : PG_ERR_NOT_CONVERGED;
 }
 
 extern "C" int pg_cayley_step(pg_cayley *c, void *psi, double dt, const double *scales, int nscales, pg_krylov_stats *st)
@@ -892,11 +900,11 @@ extern "C" int pg_cayley_set_fused(pg_cayley *c, int on)
     return PG_OK;
 }
 
-extern "C" int pg_cayley_set_barrier_probe(pg_cayley *c, int extra_arrivals)
+extern "C" int pg_cayley_set_barrier_probe(pg_cayley *c, int extra_arrivals, int at_barrier)
 {
-    if (!c || extra_arrivals < 0) return PG_ERR_ARG;
+    if (!c || extra_arrivals < 0 || at_barrier < 0) return PG_ERR_ARG;
     if (!c->fused) return PG_ERR_STATE;
-    pg_cayley_fused_set_probe(c->fused, (unsigned int)extra_arrivals);
+    pg_cayley_fused_set_probe(c->fused, (unsigned int)extra_arrivals, (unsigned int)at_barrier);
     return PG_OK;
 }
 

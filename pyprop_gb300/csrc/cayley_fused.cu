@@ -60,7 +60,8 @@ struct FzArgs {
     const int *row_lo;           // [CTAs + 1] FP64 rows of each CTA (equal numbers of band entries)
     int bands_smem;              // 1: each channel's FP32 bands are copied to shared memory per step
     int v_smem;                  // 1: a channel's Krylov vectors are also kept in shared memory
-    unsigned int probe_extra;    // test hook: arrivals the first barrier waits for in addition (0)
+    unsigned int probe_extra;    // test hook: arrivals barrier number probe_at waits for in addition (0)
+    unsigned int probe_at;
     const cxf *lo_inv, *lo_g, *lo_rb, *up_inv, *up_g, *up_rb;
     int nblk, w, fib_per_mat, g_in_smem;
     int nch, N, m;
@@ -87,13 +88,17 @@ __device__ __forceinline__ unsigned int fz_ld_acquire(const unsigned int *p)
 // All CTAs meet (the launch is cooperative, so all are resident): the arrival count only
 // grows during a launch (it is zeroed before each), the k-th barrier completes when it
 // reaches k * gridDim.x. Returns false, CTA-uniform, when the wait ran out; the error flag is
-// then set.
-__device__ __forceinline__ bool fz_grid_sync(FzBarrier *bar, unsigned int &target, int *err, int *s_ok)
+// then set. `ordinal` counts the barriers of the launch (thread 0); the test hook makes
+// barrier number probe_at wait for probe_extra arrivals that no CTA makes.
+__device__ __forceinline__ bool fz_grid_sync(FzBarrier *bar, unsigned int &target, unsigned int &ordinal,
+                                             const FzArgs &a, int *s_ok)
 {
+    int *err = a.err;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        target += gridDim.x;
+        target += gridDim.x + (ordinal == a.probe_at ? a.probe_extra : 0u);
+        ++ordinal;
         __threadfence();
         atomicAdd(&bar->count, 1u);
         unsigned int polls = 0;
@@ -482,7 +487,8 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
     const long long vld = sV ? (long long)N : n;
     const size_t pstride = (size_t)gridDim.x * FZ_PSTRIDE;
     double *part_me = a.part + (size_t)ch * FZ_PSTRIDE;  // + phase * pstride
-    unsigned int expect = a.probe_extra;  // barrier arrivals expected so far (thread 0)
+    unsigned int expect = 0;   // barrier arrivals expected so far (thread 0)
+    unsigned int ordinal = 0;  // barriers met so far (thread 0)
     const bool lead = (ch == 0 && tid == 0);  // keeps the step statistics
 
     if (tid < PG_MAX_SLOTS) {
@@ -515,7 +521,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
     // changed after the second
     fz_rows64<KB>(a.op64, a.rb64, lo, hi, sc_diff, a.psi, a.r64, false);
     if (sband) fz_bands_wait();  // before any exit: no copy outlives the CTA
-    if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
+    if (!fz_grid_sync(a.bar, expect, ordinal, a, &ctl.ok)) return;
 
     for (;;) {
         // d = M^-1 r (complex64), published for the first matvec; ||d||^2
@@ -534,7 +540,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
             for (int i = tid; i < N; i += FZ_THREADS) a.wbuf[(size_t)ch * N + i] = xs[i];
             fz_channel_sums(Vr, vld, 0, true, xs, N, red, part_me + P_NRM * pstride);
         }
-        if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
+        if (!fz_grid_sync(a.bar, expect, ordinal, a, &ctl.ok)) return;
         fz_reduce(a.part + P_NRM * pstride, a.nch, 1, hd);
         if (tid == 0) {
             const double b = sqrt(fmax(hd[0], 0.0));
@@ -574,7 +580,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                 // classical Gram-Schmidt, twice: h1 = <V, w>, w -= V h1, h2 = <V, w>, w -= V h2
                 fz_channel_sums(Vr, vld, J, false, xs, N, red, part_me + P_H1 * pstride);
             }
-            if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
+            if (!fz_grid_sync(a.bar, expect, ordinal, a, &ctl.ok)) return;
             fz_reduce(a.part + P_H1 * pstride, a.nch, 2 * J, hf[0]);
             for (int rep = 0; rep < 2; ++rep) {
                 if (owner) {
@@ -605,7 +611,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                     __syncthreads();
                     fz_channel_sums(Vr, vld, J, rep == 1, xs, N, red, part_me + (rep == 0 ? P_H2 : P_H3) * pstride);
                 }
-                if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
+                if (!fz_grid_sync(a.bar, expect, ordinal, a, &ctl.ok)) return;
                 if (rep == 0) fz_reduce(a.part + P_H2 * pstride, a.nch, 2 * J, hf[1]);
                 else fz_reduce(a.part + P_H3 * pstride, a.nch, 1, hf[2]);
             }
@@ -650,11 +656,11 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
             a.e64[o] = mk<double>(ax, ay);
             a.psi[o] = a.psi[o] + mk<double>(ax, ay);
         }
-        if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
+        if (!fz_grid_sync(a.bar, expect, ordinal, a, &ctl.ok)) return;
         // r -= (S + i dt/2 H) e in FP64; ||r|| decides whether another pass runs
         const double rn = fz_rows64<KB>(a.op64, a.rb64, lo, hi, sc_negplus, a.e64, a.r64, true);
         fz_cta_sum64(rn, red, part_me + P_RES * pstride);
-        if (!fz_grid_sync(a.bar, expect, a.err, &ctl.ok)) return;
+        if (!fz_grid_sync(a.bar, expect, ordinal, a, &ctl.ok)) return;
         fz_reduce(a.part + P_RES * pstride, gridDim.x, 1, hd);
         if (tid == 0) {
             const double r = sqrt(fmax(hd[0], 0.0));
@@ -872,9 +878,11 @@ int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams *par
     return PG_OK;
 }
 
-void pg_cayley_fused_set_probe(FusedCayley *f, unsigned int extra_arrivals)
+void pg_cayley_fused_set_probe(FusedCayley *f, unsigned int extra_arrivals, unsigned int at_barrier)
 {
-    if (f) f->args.probe_extra = extra_arrivals;
+    if (!f) return;
+    f->args.probe_extra = extra_arrivals;
+    f->args.probe_at = at_barrier;
 }
 
 void pg_cayley_fused_free(FusedCayley *f)

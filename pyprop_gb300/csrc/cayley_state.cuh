@@ -51,5 +51,6 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
 int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams *params, cxd *psi, GmresState *st,
                            double tol, int *err);
 void pg_cayley_fused_free(FusedCayley *f);
-// test hook: arrivals added to the first grid barrier of each later step (0: none)
-void pg_cayley_fused_set_probe(FusedCayley *f, unsigned int extra_arrivals);
+// test hook: arrivals that grid barrier number at_barrier (0 = the first of a step) of each
+// later step waits for in addition, which no CTA makes (0: none)
+void pg_cayley_fused_set_probe(FusedCayley *f, unsigned int extra_arrivals, unsigned int at_barrier);

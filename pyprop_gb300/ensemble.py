@@ -28,6 +28,39 @@ def partition_members(nmembers, world_size, rank):
     return start, stop
 
 
+def gather_member_values(values, nmembers, world_size, rank):
+    """Per-member values of this rank's range (partition_members order) gathered into the
+    whole ensemble's member order on every rank (torch.distributed; no data-path exchange:
+    called once after the timed steps). One rank returns ``values`` unchanged."""
+    a, b = partition_members(nmembers, world_size, rank)
+    if len(values) != b - a:
+        raise ValueError("rank %d holds members [%d, %d) but gave %d values" % (rank, a, b, len(values)))
+    if world_size == 1:
+        return list(values)
+    import torch.distributed as dist
+    parts = [None] * world_size
+    dist.all_gather_object(parts, list(values))
+    out = [v for part in parts for v in part]
+    if len(out) != nmembers:
+        raise RuntimeError("gathered %d member values, expected %d" % (len(out), nmembers))
+    return out
+
+
+def job_throughput(local_units, local_seconds, world_size):
+    """Whole-job units per second of ranks that ran independently: the units summed over the
+    ranks divided by the slowest rank's time (torch.distributed SUM and MAX reductions)."""
+    if world_size == 1:
+        return local_units / local_seconds, local_units, local_seconds
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    units = torch.tensor([float(local_units)], dtype=torch.float64, device=dev)
+    secs = torch.tensor([float(local_seconds)], dtype=torch.float64, device=dev)
+    dist.all_reduce(units, op=dist.ReduceOp.SUM)
+    dist.all_reduce(secs, op=dist.ReduceOp.MAX)
+    return units.item() / secs.item(), units.item(), secs.item()
+
+
 def hydrogen_ensemble_params(nmembers=256, seed=20261203, lmax_range=(8, 32), n_range=(100, 400),
                              e0_range=(0.01, 0.1), wavelength_range=(400.0, 1600.0)):
     """Member parameters drawn from numpy's default_rng(seed): lmax ~ U{8..32}, B-splines

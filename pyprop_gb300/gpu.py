@@ -410,10 +410,12 @@ class CayleyStepper:
         check(code, "pg_cayley_set_fused")
         return bool(on)
 
-    def set_barrier_probe(self, extra_arrivals):
-        """Test hook: the first grid barrier of later single-kernel steps waits for arrivals that
-        never come (its bounded polls run out; error word 2); 0 restores normal steps."""
-        check(self.lib.pg_cayley_set_barrier_probe(self.h, int(extra_arrivals)), "pg_cayley_set_barrier_probe")
+    def set_barrier_probe(self, extra_arrivals, at_barrier=0):
+        """Test hook: grid barrier number ``at_barrier`` (0 = the first) of later single-kernel
+        steps waits for arrivals that never come (its bounded polls run out; error word 2);
+        extra_arrivals = 0 restores normal steps."""
+        check(self.lib.pg_cayley_set_barrier_probe(self.h, int(extra_arrivals), int(at_barrier)),
+              "pg_cayley_set_barrier_probe")
 
     def __del__(self):
         try:

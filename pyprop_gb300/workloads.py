@@ -23,6 +23,52 @@ C_AU = 137.035999084
 BOHR_NM = 0.0529177210903
 
 
+# Full-length runs of the hydrogen model whose final states are checked against the
+# complex128 oracle (tests/golden/run_*.npz). Each is a keyword set of ``hydrogen`` plus the
+# propagator and the number of steps (duration / timestep).
+#   * Crank-Nicolson: lmax 40, 600 B-splines on [0, 400], GMRES(20) with the block-diagonal
+#     LU, dt 0.01 through a 50 a.u. sin^2 pulse of 800 nm and 0.05 a.u. (5000 steps) - the
+#     benchmark's workload;
+#   * pAMP: lmax 10, 150 B-splines on [0, 100], Krylov basis 20, dt 0.01 through a 10 a.u.
+#     pulse of 800 nm and 0.05 a.u. (1000 steps), started from the field-free ground state;
+#   * ensemble members: lmax, B-splines, peak field and wavelength drawn by
+#     ``ensemble.hydrogen_ensemble_params``, r in [0, 100], dt 0.01, 10 a.u. pulse (1000 steps).
+HYDROGEN_L40_CAYLEY = dict(lmax=40, nbsplines=600, rmax=400.0, timestep=0.01, pulse_duration=50.0, duration=50.0,
+                           amplitude=0.05, wavelength_nm=800.0, krylov_basis_size=20, gmres_tolerance=1e-12)
+HYDROGEN_L10_PAMP = dict(lmax=10, nbsplines=150, rmax=100.0, timestep=0.01, pulse_duration=10.0, duration=10.0,
+                         amplitude=0.05, wavelength_nm=800.0, krylov_basis_size=20)
+ENSEMBLE_MEMBER = dict(rmax=100.0, timestep=0.01, pulse_duration=10.0, duration=10.0, krylov_basis_size=20,
+                       gmres_tolerance=1e-12)
+
+
+def run_steps(kw):
+    """Number of steps of a run: duration / timestep, rounded."""
+    return int(round(kw["duration"] / kw["timestep"]))
+
+
+def field_free_ground_state(prob):
+    """Field-free ground state of the l = 0 channel of a hydrogen ``Problem`` (host
+    generalized eigenproblem of the time-independent radial band against the overlap, setup
+    only): (psi [Nang][N] complex128 with unit S-norm, energy)."""
+    import numpy as np
+    import scipy.linalg as sl
+    repr_ = prob.psi.GetRepresentation()
+    nang, N = repr_.GetFullShape()
+    h0 = prob.Propagator.BasePropagator.PotentialList[0].PotentialData[0]
+    kb = repr_.kb
+    b = 2 * kb + 1
+    H = np.zeros((N, N), dtype=complex)
+    S = np.zeros((N, N))
+    for i in range(N):
+        for j in range(max(0, i - kb), min(N, i + kb + 1)):
+            H[i, j] = h0[j * b + (kb + i - j)]
+            S[i, j] = repr_.overlap_rows[i, kb + j - i]
+    w, v = sl.eigh(H.real, S)
+    psi = np.zeros((nang, N), dtype=complex)
+    psi[0] = v[:, 0] / np.sqrt(v[:, 0] @ S @ v[:, 0])
+    return psi, float(w[0])
+
+
 def omega_for_wavelength(nm):
     """Photon angular frequency (a.u.) for a wavelength in nm: 2 pi c / lambda."""
     return 2.0 * math.pi * C_AU / (nm / BOHR_NM)

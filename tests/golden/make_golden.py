@@ -1,6 +1,6 @@
 """Regenerate the golden fixtures under tests/golden/.
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/reference
 
 * qdot_piram.npz - the reference's own pIRAM test input (core/krylov/piram/piram/
   qdotmatrix.dat: "row col re im" lines, only the real part is used, piramtest.cpp:34-68;
@@ -78,7 +78,9 @@ def make_hydrogen():
 
 
 if __name__ == "__main__":
-    reference = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py /path/to/reference  (the PyProp source tree)")
+    reference = sys.argv[1]
     n, ev = make_qdot(reference)
     print("qdot", n, ev)
     make_hydrogen()

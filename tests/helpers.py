@@ -40,18 +40,18 @@ def relerr(a, b):
 
 
 def infidelity(ref, psi, S=None):
-    """1 - |<ref|psi>|^2 / (<ref|ref><psi|psi>), Euclidean or S-weighted (S per radial fibre)."""
+    """1 - |<ref|psi>|^2 / (<ref|ref><psi|psi>), Euclidean or S-weighted (S per radial fibre),
+    evaluated as ||psi - P_ref psi||^2 / ||psi||^2 (P_ref the projector on ref in the same
+    metric), which keeps its accuracy far below the 1e-16 that 1 - |<ref|psi>|^2/(...) can
+    resolve."""
     ref = np.asarray(ref)
     psi = np.asarray(psi)
     if S is None:
-        ip = np.vdot(ref, psi)
-        n1, n2 = np.vdot(ref, ref).real, np.vdot(psi, psi).real
+        ip = lambda x, y: np.vdot(x, y)
     else:
-        Sp = psi @ S.T
-        Sr = ref @ S.T
-        ip = np.vdot(ref, Sp)
-        n1, n2 = np.vdot(ref, Sr).real, np.vdot(psi, Sp).real
-    return float(1.0 - abs(ip) ** 2 / (n1 * n2))
+        ip = lambda x, y: np.vdot(x, y @ S.T)
+    r = psi - ref * (ip(ref, psi) / ip(ref, ref).real)
+    return float(ip(r, r).real / ip(psi, psi).real)
 
 
 # ---------------------------------------------------------------------------------------

@@ -215,6 +215,43 @@ def test_cayley_single_kernel_step_bounded_barrier_wait(gpu):
     assert relerr(prob.psi.numpy(), ref.psi.numpy()) < 1e-13
 
 
+def test_cayley_single_kernel_step_abandoned_after_first_pass_started(gpu):
+    """A bounded wait that runs out at a later grid barrier (barrier 4: the second Gram-Schmidt
+    sum of the first GMRES iteration, after the first refinement pass has started) is reported
+    too: the step call fails with PG_ERR_NOT_CONVERGED, the error word reads 2 and stays set,
+    so a step enqueued without statistics and read afterwards reports it as well; once the
+    word is cleared, steps from the original state are correct again."""
+    g = golden("hydrogen_small.npz")
+    prob = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp32", gmres_tolerance=1e-12)
+    prob.SetupStep(skipWavefunctionSetup=True)
+    assert prob.Propagator.Fused
+    stepper = prob.Propagator.stepper
+    ctx = prob.Propagator.op64.ctx
+    _set_psi(prob, g["psi"])
+    scales = prob.Propagator.op64.scales(1.005)
+    ctx.clear_device_error()
+    stepper.set_barrier_probe(1, 4)
+    with pytest.raises(nat.PygpuError) as exc:
+        stepper.step(prob.psi.GetData(), 0.01, scales)
+    assert exc.value.code == -7
+    assert ctx.device_error() == 2
+    # the word is sticky: a normal step enqueued now still reads as abandoned
+    stepper.set_barrier_probe(0)
+    stepper.step(prob.psi.GetData(), 0.01, scales, want_stats=False)
+    with pytest.raises(nat.PygpuError) as exc:
+        stepper.last_stats()
+    assert exc.value.code == -7
+    ctx.clear_device_error()
+    _set_psi(prob, g["psi"])
+    st = stepper.step(prob.psi.GetData(), 0.01, scales)
+    assert ctx.device_error() == 0 and st.TrueResidual < 1e-12
+    ref = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp32", gmres_tolerance=1e-12)
+    ref.SetupStep(skipWavefunctionSetup=True)
+    _set_psi(ref, g["psi"])
+    ref.Propagator.stepper.step(ref.psi.GetData(), 0.01, scales)
+    assert relerr(prob.psi.numpy(), ref.psi.numpy()) < 1e-13
+
+
 def test_cayley_single_kernel_step_other_spline_order(gpu):
     """B-splines of order 5 (9 diagonals) take the generic-width instance of the single-kernel
     step: the same states as the multi-kernel step to the GMRES tolerance."""
