@@ -4,13 +4,16 @@ Workload (one step = one Crank-Nicolson step of the whole wavefunction): hydroge
 lmax 40 (41 channels), 600 B-splines of order 7 on an exponential-linear grid r in
 [0, 400], Coulomb + length-gauge dipole of an 800 nm sin^2 pulse (peak 0.05 a.u.,
 50 a.u. long), dt = 0.01, GMRES (basis 20) left-preconditioned by the block-diagonal
-banded LU. The measured path is the mixed-precision one: FP64 residual, complex64
-operator and Krylov basis, FP64 Gram-Schmidt sums, Hessenberg least squares, norms and
-true residual (refined until the true residual is below 1e-12), one cooperative kernel per
-step. The same steps are also run on the plain FP64 GPU path and on the captured
-multi-kernel mixed path, and the final-state infidelity between mixed and FP64 is
-reported. The default 5000 steps are the workload's own length (about a second of timed
-steps, so that the clock sampler sees the timed region).
+banded LU. The measured path is the mixed-precision one: the residual in FP64, the operator,
+Krylov basis, Givens rotations and back-substitution in complex64/FP32, the Gram-Schmidt
+and norm sums in FP64, the correction added and the true residual checked in FP64 - one
+cooperative kernel per step. Both paths run at equal final-state error: the GMRES tolerance
+of each is the loosest that keeps the state after the whole pulse within an infidelity of
+1e-8 of the complex128 reference run (mixed 1e-7, plain FP64 1e-6; tests/golden/
+run_cayley_l40.npz holds the reference run's final state). Beside the timed steps the whole
+5000-step pulse is run on both paths and its infidelity against the reference reported. The
+default 5000 steps are the workload's own length (about a second of timed steps, so that the
+clock sampler sees the timed region).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -32,14 +35,18 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "Cayley propagation steps/s (hydrogen lmax40 N600, mixed FP32/FP64, vs plain FP64 GPU path)"
+METRIC = "Cayley propagation steps/s (hydrogen lmax40 N600, mixed FP32/FP64, vs plain FP64 GPU path at equal error)"
 WORKLOAD = dict(lmax=40, nbsplines=600, rmax=400.0, timestep=0.01, pulse_duration=50.0, amplitude=0.05,
                 wavelength_nm=800.0, krylov_basis_size=20, gmres_tolerance=1e-12)
+REFERENCE_RUN = os.path.join(ROOT, "tests", "golden", "run_cayley_l40.npz")
 
 
-def _config(precision):
-    from pyprop_gb300.workloads import hydrogen
-    return hydrogen(propagator="CayleyPropagatorGPU", precision=precision, duration=50.0, **WORKLOAD)
+def _config(precision, tolerance=None):
+    """The workload's config text; tolerance None = the equal-error GMRES tolerance of the path."""
+    from pyprop_gb300.workloads import EQUAL_ERROR_TOLERANCE, hydrogen
+    kw = dict(WORKLOAD)
+    kw["gmres_tolerance"] = EQUAL_ERROR_TOLERANCE[precision] if tolerance is None else tolerance
+    return hydrogen(propagator="CayleyPropagatorGPU", precision=precision, duration=50.0, **kw)
 
 
 def initial_state(prob):
@@ -157,11 +164,33 @@ def time_matvec(torch, prob, flush, reps=50):
     return avg, 8 * (elems + 2 * nang * N), op.variant()[0]
 
 
+def algorithmic_step_bytes(prob, iters, passes):
+    """Algorithmic bytes of one mixed step by the per-unit figures of the reference's algorithm:
+    per complex64 product of H s (sum_t P_t + 2 N_psi) with s = 8 (P_t = angular pairs x N (2k-1)
+    stored band elements of the reference layout), per FP64 product the same with s = 16, per
+    block-diagonal solve the LAPACK band LU factors (zgbtrs reads N (3 kb + 1) complex64 values per
+    channel) plus the vector in and out, per GMRES iteration j the two classical Gram-Schmidt
+    passes 2 (2 j + 2) s N_psi. Solves: one per iteration and per pass; complex64 products one
+    per iteration; FP64 products one per pass and one more (the first residual)."""
+    nang, N = prob.psi.GetRepresentation().GetFullShape()
+    kb = prob.Propagator.op64.kb
+    n = nang * N
+    P = sum(len(p.PotentialData) * N * (2 * kb + 1) for p in prob.Propagator.BasePropagator.PotentialList)
+    mv32 = 8 * (P + 2 * n)
+    mv64 = 16 * (P + 2 * n)
+    solve = 8 * (nang * N * (3 * kb + 1) + 2 * n)
+    full = int(iters)
+    cgs = sum(2 * (2 * j + 2) * 8 * n for j in range(full)) + (iters - full) * 2 * (2 * full + 2) * 8 * n
+    return int((iters + passes) * solve + iters * mv32 + (passes + 1) * mv64 + cgs)
+
+
 def step_bytes(prob, iters, passes):
-    """Algorithmic bytes of one mixed step: every block solve reads the factors (complex64), every
-    complex64 matvec the real FP32 bands and its vectors, every FP64 residual product the real
-    FP64 bands and its vectors; the solves are one per GMRES iteration and refinement pass, the
-    complex64 products one per iteration, the FP64 products one per pass plus the first."""
+    """Bytes that this implementation's data layout moves in one mixed step (for comparison with
+    the algorithmic figure): every block solve reads the dense inverse diagonal blocks, the
+    couplings and the boundary inverse (complex64), every complex64 matvec the real FP32 bands
+    and its vectors, every FP64 residual product the real FP64 bands and its vectors; the
+    solves are one per GMRES iteration and refinement pass, the complex64 products one per
+    iteration, the FP64 products one per pass plus the first."""
     from pyprop_gb300 import _native as nat
     nang, N = prob.psi.GetRepresentation().GetFullShape()
     kb = prob.Propagator.op64.kb
@@ -452,8 +481,10 @@ def run_ours(args):
         dist.init_process_group("nccl")
 
     probs = {}
-    for name, prec, fused in (("fp32", "fp32", True), ("fp64", "fp64", True), ("multi", "fp32", False)):
-        p = pp.Problem(pp.LoadString(_config(prec)))
+    legs = (("fp32", "fp32", True, None), ("fp64", "fp64", True, None), ("multi", "fp32", False, None),
+            ("fp32_tight", "fp32", True, 1e-12), ("fp64_tight", "fp64", True, 1e-12))
+    for name, prec, fused, tol in legs:
+        p = pp.Problem(pp.LoadString(_config(prec, tol)))
         p.Propagator.StepStats = False  # steps only enqueue; stats are read after the end event
         p.Propagator.Eager = args.eager
         p.Propagator.FusedStep = fused
@@ -464,6 +495,11 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
 
     def run(prob, K, W, timed=True):
+        """W untimed steps, then K steps each bracketed by its own pair of CUDA events on the
+        launching stream with the L2 flushed (256 MB write) before it, outside the bracket.
+        The steps are enqueued without waiting for each other, so the device timing holds no
+        host enqueue latency; returns (device seconds of the K steps, GMRES iterations and
+        refinement passes per step, kernels launched)."""
         prob.psi.GetData().copy_(torch.as_tensor(psi0, device="cuda"))
         prob.PropagatedTime = 0.0
         for _ in range(W):
@@ -471,45 +507,41 @@ def run_ours(args):
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-        total = 0.0
-        iters = 0
-        passes = 0
+        stepper = prob.Propagator.stepper
         ctx = prob.Propagator.op64.ctx
         prob.Propagator.LastStats  # settles the device kernel count of the warm-up steps
         l0 = ctx.launches()
+        it0, ps0 = stepper.totals()
+        events = []
         for _ in range(K):
             flush.fill_(1.0)
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record(stream)
             prob.AdvanceStep()
             e.record(stream)
-            e.synchronize()
-            total += s.elapsed_time(e) * 1e-3
-            st = prob.Propagator.LastStats
-            iters += st.Iterations
-            passes += st.RestartCount
+            events.append((s, e))
         torch.cuda.synchronize()
+        total = sum(s.elapsed_time(e) for s, e in events) * 1e-3
+        it1, ps1 = stepper.totals()
+        prob.Propagator.LastStats  # adds this run's device kernel count to the context's
         if dist:
             dist.barrier()
-        return total, iters / max(K, 1), passes / max(K, 1), ctx.launches() - l0
+        return total, (it1 - it0) / max(K, 1), (ps1 - ps0) / max(K, 1), ctx.launches() - l0
 
     with ClockSampler(local) as clk:
         t_mixed, it_mixed, pass_mixed, launches = run(probs["fp32"], args.steps, args.warmup)
     t_fp64, it_fp64, _, _ = run(probs["fp64"], args.steps, args.warmup)
     # the same mixed step on the captured multi-kernel path (comparison only)
     t_multi, it_multi, _, launches_multi = run(probs["multi"], args.steps, args.warmup)
+    # both paths at the tight tolerance 1e-12 (comparison only)
+    t_mt, it_mt, pass_mt, _ = run(probs["fp32_tight"], args.steps, args.warmup)
+    t_dt, it_dt, _, _ = run(probs["fp64_tight"], args.steps, args.warmup)
     fused = bool(getattr(probs["fp32"].Propagator, "Fused", False))
     if dist:
         tt = torch.tensor([t_mixed, t_fp64], device="cuda", dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_mixed, t_fp64 = tt.tolist()
-    psi_m = probs["fp32"].psi.numpy()
-    psi_d = probs["fp64"].psi.numpy()
-    repr_ = probs["fp32"].psi.GetRepresentation()
-    S = repr_.radial.BSplineObject.dense(repr_.overlap_rows)
-    Sm, Sd = psi_m @ S.T, psi_d @ S.T
-    fid = abs(np.vdot(psi_d, Sm)) ** 2 / (np.vdot(psi_m, Sm).real * np.vdot(psi_d, Sd).real)
-    infid = float(1.0 - fid)
+    pulse = pulse_against_reference(run, probs, psi0) if args.pulse else None
 
     # end to end through the public API with host buffers: H2D + step + D2H per step
     prob = probs["fp32"]
@@ -532,7 +564,8 @@ def run_ours(args):
     nbytes = psi0.size * 16
 
     avg_mv, bytes_mv, variant_mv = time_matvec(torch, prob, flush)
-    bytes_step = step_bytes(prob, it_mixed, pass_mixed)
+    bytes_step = algorithmic_step_bytes(prob, it_mixed, pass_mixed)
+    layout_bytes_step = step_bytes(prob, it_mixed, pass_mixed)
     avg_ts, bytes_ts = time_block_solve(torch, prob, flush)
     avg_lg, bytes_lg, variant_lg = time_large_matvec(torch, flush)
     two_e = time_two_electron(torch) if args.two_electron else None
@@ -552,10 +585,18 @@ def run_ours(args):
             "config": {"workload": "hydrogen lmax=40 N=600 rmax=400 Cayley-GMRES(20) block-diag LU, dt=0.01, "
                                    "800nm sin2 pulse 0.05au", "global_batch": world, "seq_len": None,
                        "parallelism": "replicas" if world > 1 else "single", "l2": "flushed before every step"},
-            "plain_fp64": {"steps_per_s": world * args.steps / t_fp64, "gmres_iterations_per_step": it_fp64},
+            "gmres_tolerance": probs["fp32"].Propagator.Tolerance,
+            "plain_fp64": {"steps_per_s": world * args.steps / t_fp64, "gmres_iterations_per_step": it_fp64,
+                           "gmres_tolerance": probs["fp64"].Propagator.Tolerance},
             "speedup_vs_plain_fp64": t_fp64 / t_mixed,
-            "infidelity_vs_fp64_gpu": infid,
+            "infidelity_vs_reference": None if pulse is None else pulse["mixed"]["infidelity_vs_reference"],
+            "equal_error": pulse,
             "gmres_iterations_per_step": it_mixed,
+            "refinement_passes_per_step": pass_mixed,
+            "tight_tolerance": {"gmres_tolerance": 1e-12, "mixed_steps_per_s": world * args.steps / t_mt,
+                                "mixed_gmres_iterations_per_step": it_mt, "mixed_passes_per_step": pass_mt,
+                                "fp64_steps_per_s": world * args.steps / t_dt, "fp64_gmres_iterations_per_step": it_dt,
+                                "speedup": t_dt / t_mt},
             "e2e": {"value": world * args.steps / e2e_t, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
             # dominant kernel: the single-kernel step itself (one launch per step)
@@ -564,7 +605,11 @@ def run_ours(args):
                          "traffic": profile_traffic("cay_fused_step_kernel_lmax40_n600.md"),
                          "kernel": "cay_fused_step_kernel<6>" if fused else "multi-kernel step",
                          "avg_launch_us": 1e6 * t_mixed / args.steps, "algorithmic_bytes": bytes_step,
-                         "peak_kind": peak_kind,
+                         "layout_bytes": layout_bytes_step, "peak_kind": peak_kind,
+                         "bytes_rule": "per complex64/FP64 product s(sum P_t + 2 N_psi), per block solve the LAPACK "
+                                       "band LU factors N(3kb+1) per channel + 2 s N_psi, per iteration CGS2 "
+                                       "2(2j+2) s N_psi; layout_bytes = what this implementation's dense block "
+                                       "inverses and real bands move",
                          "timing": "CUDA events around each timed step on the launching stream, L2 flushed before each",
                          "note": "block-solve factors and bands are re-read from L2 within a step: latency-bound "
                                  "(grid barriers, dependent block-solve phases), not HBM-bound"},
@@ -620,6 +665,38 @@ def _my_members(n):
     rank, world = _rank_world()
     a, b = partition_members(n, world, rank)
     return hydrogen_ensemble_params(n)[a:b]
+
+
+def pulse_against_reference(run, probs, psi0):
+    """The whole 5000-step pulse on the mixed and the plain FP64 path at their equal-error
+    tolerances (steps timed as in the headline: CUDA events per step, L2 flushed before each),
+    each final state against the complex128 reference run: S-weighted infidelity, S-norm and
+    energy differences. None when the reference run's fixture is absent."""
+    if not os.path.exists(REFERENCE_RUN):
+        return None
+    from pyprop_gb300.workloads import run_steps
+    g = np.load(REFERENCE_RUN)
+    kw = dict(WORKLOAD, duration=50.0)
+    nsteps = run_steps(kw)
+    if np.max(np.abs(g["psi0"] - psi0)) > 1e-12:
+        raise RuntimeError("the reference run starts from another initial state")
+    out = {"bar": 1e-8, "steps": nsteps, "reference": "tests/golden/run_cayley_l40.npz (complex128, the "
+           "reference's own GMRES template, GMRES tolerance 1e-12)"}
+    for name, key in (("mixed", "fp32"), ("fp64", "fp64")):
+        prob = probs[key]
+        t, it, ps, _ = run(prob, nsteps, 0)
+        psi = prob.psi.numpy()
+        repr_ = prob.psi.GetRepresentation()
+        S = repr_.radial.BSplineObject.dense(repr_.overlap_rows)
+        Sp = psi @ S.T
+        r = psi - g["psi"] * (np.vdot(g["psi"], Sp) / np.vdot(g["psi"], g["psi"] @ S.T).real)
+        out[name] = {"gmres_tolerance": prob.Propagator.Tolerance, "pulse_steps_per_s": nsteps / t,
+                     "infidelity_vs_reference": float(np.vdot(r, r @ S.T).real / np.vdot(psi, Sp).real),
+                     "norm_error": abs(prob.psi.GetNorm() - float(g["norm"])),
+                     "energy_error": abs(prob.GetEnergyExpectationValue() - float(g["energy"])),
+                     "gmres_iterations_per_step": it, "refinement_passes_per_step": ps}
+    out["speedup"] = out["mixed"]["pulse_steps_per_s"] / out["fp64"]["pulse_steps_per_s"]
+    return out
 
 
 def run_ensemble(args, torch, flush):
@@ -780,7 +857,9 @@ def _oracle_setup():
     terms = [("_".join(g.GetStorageId() for g in p.GeometryList), p.PotentialData, p.GeometryList[0].GetBasisPairs(),
               p.TimeFunction) for p in bp.PotentialList]
     ham = OracleHamiltonian(terms, repr_.overlap_rows, nang, N)
-    cay = OracleCayley(ham, WORKLOAD["timestep"], [0], WORKLOAD["krylov_basis_size"], WORKLOAD["gmres_tolerance"])
+    from pyprop_gb300.workloads import EQUAL_ERROR_TOLERANCE
+    # complex128 like the plain FP64 path: the same equal-error GMRES tolerance
+    cay = OracleCayley(ham, WORKLOAD["timestep"], [0], WORKLOAD["krylov_basis_size"], EQUAL_ERROR_TOLERANCE["fp64"])
     psi0, _ = initial_state(prob)
     return cay, psi0
 
@@ -818,9 +897,11 @@ def cpu_baseline_sample(nsteps=20, procs=1):
     times = [q.get() for _ in ps]
     for p in ps:
         p.join()
+    from pyprop_gb300.workloads import EQUAL_ERROR_TOLERANCE
     return {"value": procs * nsteps / max(times), "unit": "steps/s", "cores": procs, "kind": "port",
             "sample": "%d Cayley steps from t=0 per process, numpy/scipy complex128 oracle of the reference "
-                      "algorithm (OPENBLAS_NUM_THREADS=1)" % nsteps}
+                      "algorithm at GMRES tolerance %g (the complex128 equal-error tolerance; "
+                      "OPENBLAS_NUM_THREADS=1)" % (nsteps, EQUAL_ERROR_TOLERANCE["fp64"])}
 
 
 def run_reference(args):
@@ -853,6 +934,8 @@ def main():
     ap.add_argument("--eager", action="store_true",
                     help="host-driven GMRES loops (same kernels, visible one by one to a profiler)")
     ap.add_argument("--ensemble", type=int, default=256, help="members of the batched leg (0 = skip)")
+    ap.add_argument("--pulse", type=int, default=1,
+                    help="whole-pulse leg against the reference run at equal error (0 = skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -327,6 +327,11 @@ int pg_cayley_advance(pg_cayley *c, void *psi, double dt, int nsteps, const doub
                       int nscales, pg_krylov_stats *stats);
 /* Statistics of the last completed step (waits for the stream). */
 int pg_cayley_last_stats(pg_cayley *c, pg_krylov_stats *stats);
+/* GMRES iterations and refinement passes summed over every step of this stepper so far
+ * (waits for the stream): totals of a run whose steps were enqueued without statistics. Same
+ * reference step as pg_cayley_step (CayleyPropagator.py:71-150; the reference keeps per-solve
+ * counters in GmresWrapper, gmreswrapper.h). */
+int pg_cayley_totals(pg_cayley *c, long long *iterations, long long *passes);
 /* FP64 mode: also compute ||(S + i dt/2 H) psi' - b|| every step (one extra matvec). */
 int pg_cayley_set_true_residual(pg_cayley *c, int on);
 /* Eager mode: the same kernels launched one by one with the GMRES/refinement loops driven

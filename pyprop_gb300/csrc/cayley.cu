@@ -104,6 +104,7 @@ __global__ void cay_gmres_init_kernel(GmresState *st, const double *__restrict__
         st->g[0] = b;
         st->g[1] = 0.0;
         st->stats.passes += 1;
+        st->stats.cum_passes += 1;
         st->stats.kernels += kernels;
         st->cont_inner = b > 0.0 ? 1 : 0;
         if (has_outer >= 0) cudaGraphSetConditional(inner, st->cont_inner ? 1u : 0u);
@@ -199,6 +200,7 @@ __global__ void cay_gmres_finalize_kernel(GmresState *st, double *h1, double *h2
     st->stats.k = J;
     st->stats.resid = resid;
     st->stats.iterations += 1;
+    st->stats.cum_iterations += 1;
     st->stats.kernels += kernels;
     st->beta_last = beta;
     const bool bad = !(resid == resid);
@@ -366,8 +368,10 @@ struct pg_cayley {
     cxd *b64 = nullptr, *r64 = nullptr, *d64 = nullptr, *e64 = nullptr;
     double *h1 = nullptr, *h2 = nullptr, *h3 = nullptr, *nrm = nullptr, *nrm2 = nullptr;
     GmresState *st = nullptr;
-    GmresStats *h_stats = nullptr;
-    int *h_err = nullptr;             // the context's device error word after the last step (pinned)
+    GmresStats *h_stats = nullptr;    // mapped pinned host memory (the single-kernel step writes it)
+    int *h_err = nullptr;             // the context's device error word after the last step (mapped)
+    GmresStats *dm_stats = nullptr;   // device-visible aliases of h_stats and h_err
+    int *dm_err = nullptr;
     StepParams *d_params = nullptr;
     StepParams *h_ring = nullptr;
     cudaEvent_t ring_ev[RING];
@@ -713,10 +717,12 @@ extern "C" int pg_cayley_create(pg_op *op64, pg_op *op_basis, pg_banded *prec64,
     for (double *z : {c->h1, c->h2, c->h3, c->nrm, c->nrm2}) PG_CUDA_TRY(cudaMemset(z, 0, cols));
     PG_CUDA_TRY(cudaMalloc(&c->st, sizeof(GmresState)));
     PG_CUDA_TRY(cudaMemset(c->st, 0, sizeof(GmresState)));
-    PG_CUDA_TRY(cudaMallocHost(&c->h_stats, sizeof(GmresStats)));
+    PG_CUDA_TRY(cudaHostAlloc(&c->h_stats, sizeof(GmresStats), cudaHostAllocMapped));
     memset(c->h_stats, 0, sizeof(GmresStats));
-    PG_CUDA_TRY(cudaMallocHost(&c->h_err, sizeof(int)));
+    PG_CUDA_TRY(cudaHostAlloc(&c->h_err, sizeof(int), cudaHostAllocMapped));
     *c->h_err = 0;
+    PG_CUDA_TRY(cudaHostGetDevicePointer((void **)&c->dm_stats, c->h_stats, 0));
+    PG_CUDA_TRY(cudaHostGetDevicePointer((void **)&c->dm_err, c->h_err, 0));
     PG_CUDA_TRY(cudaMalloc(&c->d_params, sizeof(StepParams)));
     c->params_dev = c->d_params;
     c->rctx.device = c->ctx->device;
@@ -779,6 +785,16 @@ static int cayley_launch(pg_cayley *c, cxd *psi, double dt, const double *scales
         ctx->launches = launches;
         PG_TRY(code);
     }
+    if (fused) {
+        // the step's parameters as kernel arguments; statistics and the error word come back
+        // through mapped host memory written by the kernel
+        StepParams p;
+        memset(&p, 0, sizeof(p));
+        p.dt = dt;
+        for (int k = 0; k < PG_MAX_SLOTS; ++k)
+            p.h[k] = mk<double>(k < nscales ? scales[2 * k] : 0.0, k < nscales ? scales[2 * k + 1] : 0.0);
+        return pg_cayley_fused_launch(c->fused, ctx->stream, p, psi, c->st, c->tol, ctx->d_err, c->dm_stats, c->dm_err);
+    }
     const int slot = c->ring_pos;
     c->ring_pos = (c->ring_pos + 1) % RING;
     if (c->ring_used[slot]) PG_CUDA_TRY(cudaEventSynchronize(c->ring_ev[slot]));
@@ -789,10 +805,7 @@ static int cayley_launch(pg_cayley *c, cxd *psi, double dt, const double *scales
     PG_CUDA_TRY(cudaMemcpyAsync(c->d_params, &p, sizeof(StepParams), cudaMemcpyHostToDevice, ctx->stream));
     PG_CUDA_TRY(cudaEventRecord(c->ring_ev[slot], ctx->stream));
     c->ring_used[slot] = true;
-    if (fused) {
-        PG_TRY(pg_cayley_fused_launch(c->fused, ctx->stream, c->d_params, psi, c->st, c->tol, ctx->d_err));
-        PG_CUDA_TRY(cudaMemcpyAsync(c->h_stats, &c->st->stats, sizeof(GmresStats), cudaMemcpyDeviceToHost, ctx->stream));
-    } else if (c->eager) {
+    if (c->eager) {
         c->rctx.stream = ctx->stream;
         const int code = (c->prec == PG_FP64) ? record_fp64(c, psi) : record_mixed(c, psi);
         ctx->launches = launches;
@@ -938,6 +951,15 @@ extern "C" int pg_cayley_last_stats(pg_cayley *c, pg_krylov_stats *st)
     if (!c || !st) return PG_ERR_ARG;
     PG_CUDA_TRY(cudaStreamSynchronize(c->ctx->stream));
     return fill_stats(c, st);
+}
+
+extern "C" int pg_cayley_totals(pg_cayley *c, long long *iterations, long long *passes)
+{
+    if (!c || !iterations || !passes) return PG_ERR_ARG;
+    PG_CUDA_TRY(cudaStreamSynchronize(c->ctx->stream));
+    *iterations = c->h_stats->cum_iterations;
+    *passes = c->h_stats->cum_passes;
+    return PG_OK;
 }
 
 // ------------------------------------------------------------------------------------

@@ -10,11 +10,15 @@
 //     Givens rotations and back-substitution in FP32 (the multi-kernel step's arithmetic)
 //     psi += e, r -= A e                             (FP64, rows spread over all CTAs)
 // Everything a GMRES iteration needs is local to the channel except the matvec (the dipole
-// couples neighbouring channels) and three scalar reductions (<V, w> twice, ||w||), so an
-// iteration costs three grid barriers instead of seven kernel launches, and a pass three more.
-// The Krylov vectors of channel a live in V[.][a] and are written only by CTA a; the vector
-// the next matvec reads is published unnormalised in a ping-pong buffer (wbuf) before the
-// barrier that completes its norm, and every reader scales it by 1/beta. Every CTA sums the
+// couples neighbouring channels) and two reductions: h1 = <V, w>, then h2 = <V, w'> of
+// w' = w - V h1 together with ||w'||^2. The norm of w'' = w' - V h2 follows by Pythagoras,
+// ||w''||^2 = ||w'||^2 - ||h2||^2 (w' is already orthogonal to V up to rounding, so there is
+// no cancellation), and an iteration costs two grid barriers instead of seven kernel launches.
+// The Krylov vectors of channel a live in V[.][a] and are written only by CTA a. The next
+// matvec's sources are published as w' in a ping-pong buffer (wbuf) before the second barrier;
+// a CTA staging a neighbour's fibre forms that neighbour's w'' = w' - V h2 itself (the same
+// arithmetic as the owner, from the neighbour's Krylov vectors, already visible) and scales it
+// by 1/beta, so the second correction needs no barrier of its own. Every CTA sums the
 // partials in the same order and runs the (tiny) Givens and back-substitution recurrences
 // itself, so all CTAs take identical decisions without another barrier. The FP64 parts
 // (residual rows, the correction e = V y) are spread over all CTAs: FP64 arithmetic is scarce
@@ -43,7 +47,7 @@ static const int FZ_MAXPASS = 4;             // refinement passes (as the multi-
 static const int FZ_PSTRIDE = 2 * (FZ_MAXM + 1);
 static const int FZ_MAXU = 4;                // distinct source channels per operator row (staged)
 static const unsigned int FZ_POLLS = 1u << 22;  // barrier polls (each an L2 round trip) before giving up
-enum { P_NRM = 0, P_H1 = 1, P_H2 = 2, P_H3 = 3, P_RES = 4, P_COUNT = 5 };
+enum { P_NRM = 0, P_H1 = 1, P_H2 = 2, P_RES = 3, P_COUNT = 4 };
 
 struct FzBarrier {
     unsigned int count;  // arrivals during the current launch
@@ -66,7 +70,9 @@ struct FzArgs {
     int nblk, w, fib_per_mat, g_in_smem;
     int nch, N, m;
     double tol;
-    const StepParams *params;
+    StepParams params;  // this step's dt and slot values (kernel argument)
+    GmresStats *hstats; // mapped host memory: the step's statistics at its end (or null)
+    int *herr;          // mapped host memory: the error word at the step's end (or null)
     cxd *psi;
     cxd *r64;        // [nch*N] FP64 residual (rows spread over the CTAs)
     cxd *e64;        // [nch*N] correction of the pass (read across channels by the FP64 rows)
@@ -106,7 +112,10 @@ __device__ __forceinline__ bool fz_grid_sync(FzBarrier *bar, unsigned int &targe
             if (++polls > FZ_POLLS) { ok = 0; break; }
             __nanosleep(32);
         }
-        if (!ok) atomicExch(err, 2);
+        if (!ok) {
+            atomicExch(err, 2);
+            if (a.herr) *(volatile int *)a.herr = 2;
+        }
         *s_ok = ok;
     }
     __syncthreads();
@@ -147,11 +156,28 @@ __device__ __forceinline__ void fz_reduce(const double *part, int nch, int nval,
     __syncthreads();
 }
 
-// Channel sums of the complex64 fibre xs: out[2q], out[2q+1] = <V_q, xs> for q < J (dots),
-// out[0] = ||xs||^2 (norm_only). Element sums in FP32 per thread and warp, CTA sums in FP64.
-__device__ __forceinline__ void fz_channel_sums(const cxf *Vc, long long ldv, int J, bool norm_only, const cxf *xs,
-                                                int N, double (*red)[2 * FZ_CB], double *out)
+// CTA sum of one FP64 value per thread into out[0] (FP64 throughout)
+__device__ __forceinline__ void fz_cta_sum64(double v, double (*red)[2 * FZ_CB], double *out)
 {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = fz_warp_sum(v);
+    if (lane == 0) red[warp][0] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double s = lane < FZ_NW ? red[lane][0] : 0.0;
+        s = fz_warp_sum(s);
+        if (lane == 0) out[0] = s;
+    }
+    __syncthreads();
+}
+
+// Channel sums of the complex64 fibre xs: out[2q], out[2q+1] = <V_q, xs> for q < J (dots),
+// out[0] = ||xs||^2 (norm_only); with_norm also out[2J] = ||xs||^2 beside the dots. Element
+// sums in FP32 per thread and warp, CTA sums in FP64.
+__device__ __forceinline__ void fz_channel_sums(const cxf *Vc, long long ldv, int J, bool norm_only, const cxf *xs,
+                                                int N, double (*red)[2 * FZ_CB], double *out, bool with_norm = false)
+{
+    float n2 = 0.f;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int ncol = norm_only ? 1 : J;
     for (int j0 = 0; j0 < ncol; j0 += FZ_CB) {
@@ -164,6 +190,10 @@ __device__ __forceinline__ void fz_channel_sums(const cxf *Vc, long long ldv, in
                 ax[0] = fmaf(b.x, b.x, ax[0]);
                 ax[0] = fmaf(b.y, b.y, ax[0]);
             } else {
+                if (with_norm && j0 == 0) {
+                    n2 = fmaf(b.x, b.x, n2);
+                    n2 = fmaf(b.y, b.y, n2);
+                }
 #pragma unroll
                 for (int q = 0; q < FZ_CB; ++q)
                     if (j0 + q < J) {
@@ -195,6 +225,33 @@ __device__ __forceinline__ void fz_channel_sums(const cxf *Vc, long long ldv, in
         }
         __syncthreads();
     }
+    if (with_norm && !norm_only) fz_cta_sum64((double)n2, red, out + 2 * J);
+}
+
+// acc -= sum_q V_q h_q over q < J (complex64, FMAs in a fixed order): the classical
+// Gram-Schmidt update of one element. The owner of a channel and the CTAs that stage its fibre
+// for their products run this same code on the same values, so they form the same vector.
+// CG: V is another CTA's global data, read through L2 (L1 may hold lines of an earlier pass).
+template <bool CG>
+__device__ __forceinline__ cxf fz_gs_update(cxf acc, const cxf *V, long long ldv, int J, const cxf *hs)
+{
+    for (int q0 = 0; q0 < J; q0 += FZ_CB) {
+        cxf v[FZ_CB];  // FZ_CB vectors' loads in flight together
+#pragma unroll
+        for (int q = 0; q < FZ_CB; ++q)
+            v[q] = q0 + q < J ? (CG ? fz_ldcg(V + (size_t)(q0 + q) * ldv) : V[(size_t)(q0 + q) * ldv])
+                              : mk<float>(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < FZ_CB; ++q) {
+            if (q0 + q >= J) break;
+            const cxf hc = hs[q0 + q];
+            acc.x = fmaf(-v[q].x, hc.x, acc.x);
+            acc.x = fmaf(v[q].y, hc.y, acc.x);
+            acc.y = fmaf(-v[q].x, hc.y, acc.y);
+            acc.y = fmaf(-v[q].y, hc.x, acc.y);
+        }
+    }
+    return acc;
 }
 
 // FP64 rows [lo, hi) of the flattened [Nang][N] operator applied to src (read through L2:
@@ -244,21 +301,6 @@ __device__ __forceinline__ double fz_rows64(const OpDev &op, const double *__res
     return nrm;
 }
 
-// CTA sum of one FP64 value per thread into out[0] (FP64 throughout)
-__device__ __forceinline__ void fz_cta_sum64(double v, double (*red)[2 * FZ_CB], double *out)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    v = fz_warp_sum(v);
-    if (lane == 0) red[warp][0] = v;
-    __syncthreads();
-    if (warp == 0) {
-        double s = lane < FZ_NW ? red[lane][0] : 0.0;
-        s = fz_warp_sum(s);
-        if (lane == 0) out[0] = s;
-    }
-    __syncthreads();
-}
-
 // Copy the real FP32 bands of operator row a ([entry][2kb+1][ld] in entry order) to shared
 // memory with asynchronous 16-byte copies (cp.async; waited for by fz_bands_wait).
 __device__ __forceinline__ void fz_bands_load(const FzArgs &A, int a, float *sband)
@@ -281,14 +323,16 @@ __device__ __forceinline__ void fz_bands_wait()
     __syncthreads();
 }
 
-// complex64 operator row a applied to the normalised vector wsrc * s: the row's distinct
-// source fibres are staged (scaled, with a zero halo of kb) in xsrc, then thread i forms
-// xs[i] = sum_e sc[slot_e] sum_d band_e[d][i] x_e[i + d - kb] from real bands (in shared
-// memory when sband is set, else read through L1); zero on the padding up to npad.
+// complex64 operator row a applied to the normalised vector (wsrc - V hs) * s: the row's
+// distinct source fibres are staged (the Gram-Schmidt correction by the first Jc Krylov
+// vectors of the source channel applied, scaled, with a zero halo of kb) in xsrc, then thread
+// i forms xs[i] = sum_e sc[slot_e] sum_d band_e[d][i] x_e[i + d - kb] from real bands (in
+// shared memory when sband is set, else read through L1); zero on the padding up to npad.
 template <int KB>
 __device__ __forceinline__ void fz_matvec32(const FzArgs &A, int a, const cxf *sc, const cxf *wsrc, float s, cxf *xs,
-                                            int npad, cxf *xsrc, const float *sband)
+                                            int npad, cxf *xsrc, const float *sband, int Jc, const cxf *hs)
 {
+    const long long nall = (long long)A.nch * A.N;
     const OpDev &op = A.opb;
     const int N = op.N, kb = KB >= 0 ? KB : op.kb, b = 2 * kb + 1, ld = op.ld, W = N + 2 * kb;
     const int nu = __ldg(A.nucol + a);
@@ -304,6 +348,15 @@ __device__ __forceinline__ void fz_matvec32(const FzArgs &A, int a, const cxf *s
             const int u = idx / W, q = idx - u * W, j = q - kb;
             v[k] = (idx < nu * W && j >= 0 && j < N) ? fz_ldcg(wsrc + (size_t)cols[u < FZ_MAXU ? u : 0] * N + j)
                                                      : mk<float>(0.f, 0.f);
+        }
+        if (Jc > 0) {
+#pragma unroll
+            for (int k = 0; k < FZ_MAXU; ++k) {
+                const int idx = base + threadIdx.x + k * FZ_THREADS;
+                const int u = idx / W, q = idx - u * W, j = q - kb;
+                if (idx < nu * W && j >= 0 && j < N)
+                    v[k] = fz_gs_update<true>(v[k], A.V + (size_t)cols[u < FZ_MAXU ? u : 0] * N + j, nall, Jc, hs);
+            }
         }
 #pragma unroll
         for (int k = 0; k < FZ_MAXU; ++k) {
@@ -458,7 +511,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
     __shared__ cxf sc_plus[PG_MAX_SLOTS];
     __shared__ double red[FZ_NW][2 * FZ_CB];
     __shared__ double hd[1];  // FP64 sums of the pass: ||d||^2, then ||r||^2
-    __shared__ float hf[3][FZ_PSTRIDE];  // the Gram-Schmidt sums h1, h2 and |w|^2 of this iteration
+    __shared__ float hf[2][FZ_PSTRIDE];  // the Gram-Schmidt sums h1 and h2 of this iteration
     __shared__ cxf hs[FZ_MAXM];
     __shared__ cxd ys[FZ_MAXM];
     __shared__ FzGivens G;
@@ -492,8 +545,8 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
     const bool lead = (ch == 0 && tid == 0);  // keeps the step statistics
 
     if (tid < PG_MAX_SLOTS) {
-        const double hdt = 0.5 * a.params->dt;
-        const cxd h = a.params->h[tid];
+        const double hdt = 0.5 * a.params.dt;
+        const cxd h = a.params.h[tid];
         cxd plus, diff;
         if (tid == 0) {
             plus = mk<double>(1.0, 0.0);
@@ -558,6 +611,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                 a.st->stats.beta0 = b;
                 a.st->stats.resid = b;
                 a.st->stats.passes = ctl.passes;
+                a.st->stats.cum_passes += 1;
             }
         }
         __syncthreads();
@@ -566,58 +620,51 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
             const int j = ctl.j, J = j + 1;
             const float s = ctl.s;
             if (owner) {
-                // V_j = w / beta (this channel), then xs = M^-1 A V_j (row ch)
+                // V_j = w'' / beta (this channel), then xs = M^-1 A V_j (row ch); the staged
+                // sources are the channels' w' with the previous iteration's second correction
+                // (hs = h2, j vectors) applied while staging
                 for (int i = tid; i < N; i += FZ_THREADS) {
                     const cxf v = xs[i];
                     const cxf vs = mk<float>(v.x * s, v.y * s);
                     Vc[(size_t)j * n + i] = vs;
                     if (sV) sV[(size_t)j * N + i] = vs;
                 }
-                fz_matvec32<KB>(a, ch, sc_plus, a.wbuf + (size_t)(j & 1) * n, s, xs, npad, xsrc, sband);
+                fz_matvec32<KB>(a, ch, sc_plus, a.wbuf + (size_t)(j & 1) * n, s, xs, npad, xsrc, sband, j, hs);
                 __syncthreads();
                 tri_solve_smem<float, cxf, FZ_NW>(nblk, w, mat, a.lo_inv, a.lo_g, a.lo_rb, a.up_inv, a.up_g, a.up_rb,
                                                   1, 1, a.g_in_smem, xs, sb, sg);
-                // classical Gram-Schmidt, twice: h1 = <V, w>, w -= V h1, h2 = <V, w>, w -= V h2
+                // classical Gram-Schmidt, twice: h1 = <V, w>, w' = w - V h1, h2 = <V, w'>, w'' = w' - V h2
                 fz_channel_sums(Vr, vld, J, false, xs, N, red, part_me + P_H1 * pstride);
             }
             if (!fz_grid_sync(a.bar, expect, ordinal, a, &ctl.ok)) return;
             fz_reduce(a.part + P_H1 * pstride, a.nch, 2 * J, hf[0]);
-            for (int rep = 0; rep < 2; ++rep) {
-                if (owner) {
-                    const float *h = hf[rep];
-                    if (tid < J) hs[tid] = mk<float>(h[2 * tid], h[2 * tid + 1]);
-                    __syncthreads();
-                    for (int i = tid; i < N; i += FZ_THREADS) {
-                        cxf acc = xs[i];
-                        for (int q0 = 0; q0 < J; q0 += FZ_CB) {
-                            // FZ_CB vectors' loads in flight together
-                            cxf v[FZ_CB];
-#pragma unroll
-                            for (int q = 0; q < FZ_CB; ++q)
-                                v[q] = q0 + q < J ? Vr[(size_t)(q0 + q) * vld + i] : mk<float>(0.f, 0.f);
-#pragma unroll
-                            for (int q = 0; q < FZ_CB; ++q) {
-                                if (q0 + q >= J) break;
-                                const cxf hc = hs[q0 + q];
-                                acc.x = fmaf(-v[q].x, hc.x, acc.x);
-                                acc.x = fmaf(v[q].y, hc.y, acc.x);
-                                acc.y = fmaf(-v[q].x, hc.y, acc.y);
-                                acc.y = fmaf(-v[q].y, hc.x, acc.y);
-                            }
-                        }
-                        xs[i] = acc;
-                        if (rep == 1) a.wbuf[(size_t)((j + 1) & 1) * n + (size_t)ch * N + i] = acc;
-                    }
-                    __syncthreads();
-                    fz_channel_sums(Vr, vld, J, rep == 1, xs, N, red, part_me + (rep == 0 ? P_H2 : P_H3) * pstride);
+            if (owner) {
+                if (tid < J) hs[tid] = mk<float>(hf[0][2 * tid], hf[0][2 * tid + 1]);
+                __syncthreads();
+                // w' = w - V h1, published for the next products; then h2 and ||w'||^2
+                for (int i = tid; i < N; i += FZ_THREADS) {
+                    const cxf acc = fz_gs_update<false>(xs[i], Vr + i, vld, J, hs);
+                    xs[i] = acc;
+                    a.wbuf[(size_t)((j + 1) & 1) * n + (size_t)ch * N + i] = acc;
                 }
-                if (!fz_grid_sync(a.bar, expect, ordinal, a, &ctl.ok)) return;
-                if (rep == 0) fz_reduce(a.part + P_H2 * pstride, a.nch, 2 * J, hf[1]);
-                else fz_reduce(a.part + P_H3 * pstride, a.nch, 1, hf[2]);
+                __syncthreads();
+                fz_channel_sums(Vr, vld, J, false, xs, N, red, part_me + P_H2 * pstride, true);
+            }
+            if (!fz_grid_sync(a.bar, expect, ordinal, a, &ctl.ok)) return;
+            fz_reduce(a.part + P_H2 * pstride, a.nch, 2 * J, hf[1]);
+            fz_reduce(a.part + P_H2 * pstride + 2 * J, a.nch, 1, hd);
+            if (owner) {
+                if (tid < J) hs[tid] = mk<float>(hf[1][2 * tid], hf[1][2 * tid + 1]);
+                __syncthreads();
+                // w'' = w' - V h2 (kept for the next iteration; the other CTAs form it themselves)
+                for (int i = tid; i < N; i += FZ_THREADS) xs[i] = fz_gs_update<false>(xs[i], Vr + i, vld, J, hs);
             }
             if (tid == 0) {
-                // |w| in FP32 (it enters the Hessenberg matrix and the next vector as FP32)
-                const float fb = sqrtf(fmaxf(hf[2][0], 0.f));
+                // ||w''||^2 = ||w'||^2 - ||h2||^2 (FP64), beta in FP32 (it enters the Hessenberg
+                // matrix and the next vector as FP32)
+                double b2 = hd[0];
+                for (int q = 0; q < J; ++q) b2 -= (double)hf[1][2 * q] * hf[1][2 * q] + (double)hf[1][2 * q + 1] * hf[1][2 * q + 1];
+                const float fb = (float)sqrt(fmax(b2, 0.0));
                 const float resid = fz_givens(G, j, hf[0], hf[1], fb);
                 const bool bad = !(resid == resid);
                 const bool conv = bad || resid <= ctl.tol_f || J >= a.m || !(fb > 0.f);
@@ -629,6 +676,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
                     a.st->stats.k = J;
                     a.st->stats.resid = resid;
                     a.st->stats.iterations += 1;
+                    a.st->stats.cum_iterations += 1;
                 }
             }
             __syncthreads();
@@ -669,6 +717,12 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
         }
         __syncthreads();
         if (!ctl.again) break;
+    }
+    // the step's statistics and the error word to the host (mapped memory): the last action
+    if (lead && a.hstats) {
+        *a.hstats = a.st->stats;
+        *(volatile int *)a.herr = *(volatile int *)a.err;
+        __threadfence_system();
     }
 }
 
@@ -851,11 +905,13 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
     return PG_OK;
 }
 
-int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams *params, cxd *psi, GmresState *st,
-                           double tol, int *err)
+int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams &params, cxd *psi, GmresState *st,
+                           double tol, int *err, GmresStats *host_stats, int *host_err)
 {
     FzArgs a = f->args;
     a.params = params;
+    a.hstats = host_stats;
+    a.herr = host_err;
     a.psi = psi;
     a.st = st;
     a.tol = tol;

@@ -14,6 +14,8 @@ struct GmresStats {
     double beta0;          // norm of the preconditioned right-hand side of the last solve
     long long kernels;     // kernels run by all steps so far (never reset; see the K_* counts)
     long long rejected;    // learned-preconditioner passes rejected by the true residual (cumulative)
+    long long cum_iterations;  // GMRES iterations of all steps so far (never reset)
+    long long cum_passes;      // refinement passes of all steps so far (never reset)
 };
 
 struct GmresState {
@@ -47,9 +49,12 @@ enum { SC_PLUS = 0, SC_MINUS = 1, SC_DIFF = 2, SC_NEGPLUS = 3, SC_COUNT = 4 };
 struct FusedCayley;
 // PG_OK and *out set when the operators qualify; an error code (and *out null) otherwise
 int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, FusedCayley **out);
-// one step on stream s: psi (complex128, device) advanced in place; st->stats updated
-int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams *params, cxd *psi, GmresState *st,
-                           double tol, int *err);
+// one step on stream s: psi (complex128, device) advanced in place; st->stats updated. The
+// step's parameters travel as kernel arguments; host_stats / host_err (device-visible aliases
+// of mapped host memory, or null) receive the step's statistics and the error word from the
+// kernel itself, so a step is one memset and one launch on the stream.
+int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams &params, cxd *psi, GmresState *st,
+                           double tol, int *err, GmresStats *host_stats, int *host_err);
 void pg_cayley_fused_free(FusedCayley *f);
 // test hook: arrivals that grid barrier number at_barrier (0 = the first of a step) of each
 // later step waits for in addition, which no CTA makes (0: none)

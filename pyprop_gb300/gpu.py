@@ -384,6 +384,13 @@ class CayleyStepper:
         check(self.lib.pg_cayley_last_stats(self.h, C.byref(self.stats)), "pg_cayley_last_stats")
         return self.stats
 
+    def totals(self):
+        """(GMRES iterations, refinement passes) summed over every step so far (waits)."""
+        it, ps = C.c_longlong(), C.c_longlong()
+        self.ctx.bind_stream()
+        check(self.lib.pg_cayley_totals(self.h, C.byref(it), C.byref(ps)), "pg_cayley_totals")
+        return it.value, ps.value
+
     def set_learned(self, net, coupling_slot):
         """Use the learned preconditioner ``net`` (MlpNet, or None to switch it off); its
         correction is scaled by i dt/2 times the scale of ``coupling_slot``."""

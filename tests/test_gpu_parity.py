@@ -46,7 +46,7 @@ def _run(prob, psi0, nsteps):
     return prob.psi.numpy()
 
 
-@pytest.mark.parametrize("precision,tol_inf,tol_norm", [("fp64", 1e-16, 1e-12), ("fp32", 1e-14, 1e-10)])
+@pytest.mark.parametrize("precision,tol_inf,tol_norm", [("fp64", 1e-22, 1e-11), ("fp32", 1e-18, 1e-10)])
 def test_cayley_l40_whole_pulse_against_reference(gpu, precision, tol_inf, tol_norm):
     """Hydrogen lmax 40, 600 B-splines, 5000 Crank-Nicolson steps through the 800 nm pulse
     (the benchmark's workload) at GMRES tolerance 1e-12: plain FP64, and mixed precision on
@@ -62,7 +62,7 @@ def test_cayley_l40_whole_pulse_against_reference(gpu, precision, tol_inf, tol_n
     assert abs(prob.GetEnergyExpectationValue() - float(g["energy"])) < 1e-9
 
 
-@pytest.mark.parametrize("precision,tol_inf", [("fp64", 1e-16), ("fp32", 1e-8)])
+@pytest.mark.parametrize("precision,tol_inf", [("fp64", 1e-22), ("fp32", 1e-9)])
 def test_pamp_l10_whole_pulse_against_reference(gpu, precision, tol_inf):
     """Hydrogen lmax 10, 150 B-splines, 1000 pAMP steps through a 10 a.u. 800 nm pulse from
     the field-free ground state with a converged Krylov basis (40 vectors): FP64, and the
@@ -79,7 +79,7 @@ def test_pamp_l10_whole_pulse_against_reference(gpu, precision, tol_inf):
     assert abs(prob.psi.GetNorm() - float(g["norm"])) < (1e-12 if precision == "fp64" else 1e-6)
 
 
-@pytest.mark.parametrize("precision,tol_inf", [("fp64", 1e-20), ("fp32", 1e-12)])
+@pytest.mark.parametrize("precision,tol_inf", [("fp64", 1e-18), ("fp32", 1e-11)])
 def test_pamp_l10_basis20_first_steps_against_reference(gpu, precision, tol_inf):
     """The same model with the workload's Krylov basis of 20: the first steps against the
     reference templates' state."""
@@ -117,7 +117,7 @@ def test_ensemble_members_against_reference(gpu):
     from pyprop_gb300.workloads import ENSEMBLE_MEMBER
     g = _fixture("run_members.npz")
     params = hydrogen_ensemble_params(256)
-    for kind, members, cls, tol, nsteps in (("pamp", g["members"], PamEnsembleGPU, 1e-12, int(g["pamp_steps"])),
+    for kind, members, cls, tol, nsteps in (("pamp", g["members"], PamEnsembleGPU, 1e-10, int(g["pamp_steps"])),
                                             ("cayley", g["cayley_members"], CayleyEnsembleGPU, 1e-12,
                                              int(g["cayley_steps"]))):
         prop = "PamPropagatorGPU" if kind == "pamp" else "CayleyPropagatorGPU"
@@ -132,3 +132,18 @@ def test_ensemble_members_against_reference(gpu):
             ref = g["%s%d_psi" % (kind, i)]
             assert infidelity(ref, p.psi.numpy(), _overlap(p)) < tol, (kind, int(i))
             assert abs(p.psi.GetNorm() - float(g["%s%d_norm" % (kind, i)])) < 1e-6, (kind, int(i))
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_cayley_l40_equal_error_operating_points(gpu, precision):
+    """The benchmark's operating points: mixed precision at GMRES tolerance 1e-7 and plain
+    FP64 at 1e-6 both end the 5000-step pulse within the spec bar (infidelity 1e-8)
+    of the reference run; mixed precision then needs one refinement pass per step."""
+    from pyprop_gb300.workloads import EQUAL_ERROR_TOLERANCE, HYDROGEN_L40_CAYLEY, run_steps
+    g = _fixture("run_cayley_l40.npz")
+    kw = dict(HYDROGEN_L40_CAYLEY, gmres_tolerance=EQUAL_ERROR_TOLERANCE[precision])
+    prob = _problem(kw, "CayleyPropagatorGPU", precision)
+    psi = _run(prob, g["psi0"], run_steps(kw))
+    assert infidelity(g["psi"], psi, _overlap(prob)) < 1e-8
+    if precision == "fp32":
+        assert prob.Propagator.LastStats.RestartCount == 1
