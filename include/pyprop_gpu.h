@@ -351,6 +351,17 @@ int pg_cayley_set_eager(pg_cayley *c, int on);
  * same reference step as
  * pg_cayley_step (CayleyPropagator.py:71-150). */
 int pg_cayley_set_fused(pg_cayley *c, int on);
+/* Layout of the single-kernel step (same reference step as pg_cayley_step,
+ * CayleyPropagator.py:71-150). variant 0 (default): each angular channel on a thread-block
+ * cluster of three CTAs, each holding a third of that channel's preconditioner factors in
+ * shared memory for the whole step, where the fibre length fits (about 700 B-splines of
+ * order 7) and all clusters can be resident at once, else one CTA per channel; 1: one CTA per
+ * channel; 2: the cluster layout (PG_ERR_SHAPE where it does not fit). Both give the same
+ * states to the GMRES tolerance. PG_ERR_STATE etc. as pg_cayley_set_fused when the stepper
+ * has no single-kernel step. pg_cayley_get_fused_variant: 1 or 2 for the layout the next
+ * step uses, 0 when the step is not the single-kernel one. */
+int pg_cayley_set_fused_variant(pg_cayley *c, int variant);
+int pg_cayley_get_fused_variant(pg_cayley *c, int *variant);
 /* Test hook for the bounded grid barriers of the single-kernel step (no counterpart in the
  * reference): with extra_arrivals > 0, grid barrier number at_barrier (0 = the first of a
  * step) of every later step waits for that many arrivals more than there are CTAs, so its

@@ -104,6 +104,8 @@ _SIGS = {
     "pg_cayley_set_fused": (_I, [_P, _I]),
     "pg_cayley_set_barrier_probe": (_I, [_P, _I, _I]),
     "pg_cayley_totals": (_I, [_P, C.POINTER(_LL), C.POINTER(_LL)]),
+    "pg_cayley_set_fused_variant": (_I, [_P, _I]),
+    "pg_cayley_get_fused_variant": (_I, [_P, _IP]),
     "pg_cayley_set_learned": (_I, [_P, _P, _I]),
     "pg_cayley_learned_rejected": (_I, [_P, C.POINTER(_LL)]),
     "pg_cayley_batch_create": (_I, [C.POINTER(_P), _I, C.POINTER(_P)]),

@@ -913,6 +913,20 @@ extern "C" int pg_cayley_set_fused(pg_cayley *c, int on)
     return PG_OK;
 }
 
+extern "C" int pg_cayley_set_fused_variant(pg_cayley *c, int variant)
+{
+    if (!c) return PG_ERR_ARG;
+    if (!c->fused) return c->fused_status != PG_OK ? c->fused_status : PG_ERR_STATE;
+    return pg_cayley_fused_select(c->fused, variant);
+}
+
+extern "C" int pg_cayley_get_fused_variant(pg_cayley *c, int *variant)
+{
+    if (!c || !variant) return PG_ERR_ARG;
+    *variant = (c->fused && c->use_fused && !c->mlp && !c->eager) ? pg_cayley_fused_which(c->fused) : 0;
+    return PG_OK;
+}
+
 extern "C" int pg_cayley_set_barrier_probe(pg_cayley *c, int extra_arrivals, int at_barrier)
 {
     if (!c || extra_arrivals < 0 || at_barrier < 0) return PG_ERR_ARG;

@@ -56,6 +56,11 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
 int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams &params, cxd *psi, GmresState *st,
                            double tol, int *err, GmresStats *host_stats, int *host_err);
 void pg_cayley_fused_free(FusedCayley *f);
+// 0: three CTAs per channel (a thread-block cluster) where the operator's shape fits, else
+// one CTA per channel; 1: one CTA per channel; 2: the cluster variant (PG_ERR_SHAPE if it
+// does not fit). pg_cayley_fused_which: the one selected (1 or 2).
+int pg_cayley_fused_select(FusedCayley *f, int variant);
+int pg_cayley_fused_which(const FusedCayley *f);
 // test hook: arrivals that grid barrier number at_barrier (0 = the first of a step) of each
 // later step waits for in addition, which no CTA makes (0: none)
 void pg_cayley_fused_set_probe(FusedCayley *f, unsigned int extra_arrivals, unsigned int at_barrier);

@@ -384,6 +384,17 @@ class CayleyStepper:
         check(self.lib.pg_cayley_last_stats(self.h, C.byref(self.stats)), "pg_cayley_last_stats")
         return self.stats
 
+    def set_fused_variant(self, variant):
+        """Layout of the single-kernel step: 0 the cluster layout where it fits (default), 1 one
+        CTA per channel, 2 the cluster layout (raises where it does not fit)."""
+        check(self.lib.pg_cayley_set_fused_variant(self.h, int(variant)), "pg_cayley_set_fused_variant")
+
+    def fused_variant(self):
+        """1 or 2: the layout of the next single-kernel step; 0 for the multi-kernel step."""
+        v = C.c_int()
+        check(self.lib.pg_cayley_get_fused_variant(self.h, C.byref(v)), "pg_cayley_get_fused_variant")
+        return v.value
+
     def totals(self):
         """(GMRES iterations, refinement passes) summed over every step so far (waits)."""
         it, ps = C.c_longlong(), C.c_longlong()

@@ -341,6 +341,8 @@ class CayleyPropagatorGPU(PropagatorBase):
         # mixed precision, rank-2 banded operator: the whole step as one kernel unless
         # gpu_fused_step = False
         self.FusedStep = bool(getattr(conf, "gpu_fused_step", True))
+        # its layout: 0 a cluster of three CTAs per channel where it fits, 1 one CTA per channel
+        self.FusedVariant = int(getattr(conf, "gpu_fused_variant", 0))
         # mixed precision: the FP64 residual operator computes its factorized (two-electron)
         # terms in double-float arithmetic unless gpu_fp64_emulation = False
         self.Fp64Emulation = bool(getattr(conf, "gpu_fp64_emulation", True))
@@ -372,6 +374,8 @@ class CayleyPropagatorGPU(PropagatorBase):
         if self.Eager:
             self.stepper.set_eager(True)
         self.Fused = self.stepper.set_fused(self.FusedStep and not self.Eager)
+        if self.Fused and self.FusedVariant:
+            self.stepper.set_fused_variant(self.FusedVariant)
 
     def AdvanceStep(self, t, dt):
         """One step at H(t + |dt|/2). With ``gpu_step_stats`` (default) the call waits for the

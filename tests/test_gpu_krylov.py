@@ -183,16 +183,19 @@ def test_cayley_single_kernel_step_full_size_properties(gpu):
     assert infidelity(out["fp64"], out["fp32"], S) < 1e-12
 
 
-def test_cayley_single_kernel_step_bounded_barrier_wait(gpu):
+@pytest.mark.parametrize("variant", [1, 2])
+def test_cayley_single_kernel_step_bounded_barrier_wait(gpu, variant):
     """A grid barrier of the single-kernel step whose arrivals never all come (the test hook
     adds one arrival that no CTA makes) gives up after its bounded polls: the step returns, the
     device error word reads 2, the step call reports it, psi is unchanged, and the next normal
-    step is correct."""
+    step is correct. Both layouts (one CTA per channel; three-CTA clusters)."""
     g = golden("hydrogen_small.npz")
     prob = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp32", gmres_tolerance=1e-12)
     prob.SetupStep(skipWavefunctionSetup=True)
     assert prob.Propagator.Fused
     stepper = prob.Propagator.stepper
+    stepper.set_fused_variant(variant)
+    assert stepper.fused_variant() == variant
     ctx = prob.Propagator.op64.ctx
     _set_psi(prob, g["psi"])
     scales = prob.Propagator.op64.scales(1.005)
@@ -215,17 +218,19 @@ def test_cayley_single_kernel_step_bounded_barrier_wait(gpu):
     assert relerr(prob.psi.numpy(), ref.psi.numpy()) < 1e-13
 
 
-def test_cayley_single_kernel_step_abandoned_after_first_pass_started(gpu):
-    """A bounded wait that runs out at a later grid barrier (barrier 4: the second Gram-Schmidt
-    sum of the first GMRES iteration, after the first refinement pass has started) is reported
-    too: the step call fails with PG_ERR_NOT_CONVERGED, the error word reads 2 and stays set,
-    so a step enqueued without statistics and read afterwards reports it as well; once the
-    word is cleared, steps from the original state are correct again."""
+@pytest.mark.parametrize("variant", [1, 2])
+def test_cayley_single_kernel_step_abandoned_after_first_pass_started(gpu, variant):
+    """A bounded wait that runs out at a later grid barrier (barrier 4, after the first
+    refinement pass and its first GMRES iteration have started) is reported too: the step call
+    fails with PG_ERR_NOT_CONVERGED, the error word reads 2 and stays set, so a step enqueued
+    without statistics and read afterwards reports it as well; once the word is cleared, steps
+    from the original state are correct again. Both layouts."""
     g = golden("hydrogen_small.npz")
     prob = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp32", gmres_tolerance=1e-12)
     prob.SetupStep(skipWavefunctionSetup=True)
     assert prob.Propagator.Fused
     stepper = prob.Propagator.stepper
+    stepper.set_fused_variant(variant)
     ctx = prob.Propagator.op64.ctx
     _set_psi(prob, g["psi"])
     scales = prob.Propagator.op64.scales(1.005)
@@ -250,6 +255,39 @@ def test_cayley_single_kernel_step_abandoned_after_first_pass_started(gpu):
     _set_psi(ref, g["psi"])
     ref.Propagator.stepper.step(ref.psi.GetData(), 0.01, scales)
     assert relerr(prob.psi.numpy(), ref.psi.numpy()) < 1e-13
+
+
+@pytest.mark.parametrize("lmax,nbsplines,rmax,nsteps", [(3, 40, 40.0, 10), (40, 600, 400.0, 40), (8, 267, 100.0, 20)])
+def test_cayley_cluster_layout_matches_one_cta_per_channel(gpu, lmax, nbsplines, rmax, nsteps):
+    """The single-kernel step with each channel on a three-CTA cluster (the solve factors in
+    shared memory, boundary values through distributed shared memory) and with one CTA per
+    channel: the same states to the GMRES tolerance after steps in the field, the FP64 true
+    residual bound every step, one kernel per step. Shapes: the small model (the third CTA of
+    each cluster owns no fibre block, only boundary rows), the benchmark's lmax 40 / 600
+    B-splines, and an ensemble member's lmax 8 / 267 B-splines."""
+    out = {}
+    for variant in (1, 2):
+        prob = hydrogen_problem(lmax=lmax, nbsplines=nbsplines, rmax=rmax, propagator="CayleyPropagatorGPU",
+                                precision="fp32", gmres_tolerance=1e-12, amplitude=0.05, pulse_duration=50.0)
+        prob.SetupStep(skipWavefunctionSetup=True)
+        assert prob.Propagator.Fused
+        prob.Propagator.stepper.set_fused_variant(variant)
+        assert prob.Propagator.stepper.fused_variant() == variant
+        shape = prob.psi.GetRepresentation().GetFullShape()
+        rng = np.random.default_rng(11)
+        psi = np.zeros(shape, complex)
+        i = np.arange(shape[1])
+        psi[0] = np.exp(-((i - shape[1] / 8.0) / (shape[1] / 20.0)) ** 2)
+        psi[1] = 0.3 * np.exp(-((i - shape[1] / 6.0) / (shape[1] / 15.0)) ** 2) * (1 + 0.1j * rng.normal(size=shape[1]))
+        _set_psi(prob, psi / np.linalg.norm(psi))
+        ctx = prob.Propagator.op64.ctx
+        k0 = ctx.launches()
+        for n in range(nsteps):
+            prob.Propagator.AdvanceStep(20.0 + 0.01 * n, 0.01)
+            assert prob.Propagator.LastStats.TrueResidual < 1e-12
+        assert ctx.launches() - k0 == nsteps and ctx.device_error() == 0
+        out[variant] = prob.psi.numpy()
+    assert relerr(out[2], out[1]) < 1e-10
 
 
 def test_cayley_single_kernel_step_other_spline_order(gpu):

@@ -48,7 +48,14 @@ def test_training_reduces_loss_on_a_linear_target(gpu):
     net = _net(d_in, h, d_out, seed=11)
     Xd = torch.as_tensor(X, dtype=torch.float32, device="cuda").to(torch.bfloat16)
     Td = torch.as_tensor(T, dtype=torch.float32, device="cuda")
+    # where a non-finite first loss would come from: the initial weights, the inputs, the output
+    W0 = net.get_weights()
+    Y0 = torch.zeros((B, d_out), dtype=torch.float32, device="cuda")
+    net.forward(Xd, Y0)
+    stages = {"weights": all(bool(np.isfinite(w).all()) for w in W0), "X": bool(torch.isfinite(Xd.float()).all()),
+              "T": bool(torch.isfinite(Td).all()), "Y": bool(torch.isfinite(Y0).all())}
     first = net.train_step(Xd, Td, 1e-3, want_loss=True)
+    assert np.isfinite(first), stages
     for _ in range(400):
         net.train_step(Xd, Td, 1e-3)
     last = net.train_step(Xd, Td, 1e-3, want_loss=True)
