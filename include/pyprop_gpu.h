@@ -457,6 +457,27 @@ int pg_mlp_train_step(pg_mlp *m, const void *X_bf16, const float *T, int batch, 
 int pg_mlp_block_features(pg_ctx *ctx, const void *y, int nblk, int N, int d_in, void *X_bf16);
 
 /* ---------------------------------------------------------------------------------- */
+/* analysis: projections on products of single-electron radial states                 */
+/* ---------------------------------------------------------------------------------- */
+/*
+ * For the angular indices `angular` [nidx] (distinct) of a two-electron wavefunction
+ * [nang][N1][N2] (complex128, device), with the radial states as columns of V1 [N1][n1] and
+ * V2 [N2][n2] (complex128, host, row-major):
+ *   pg_radial_products_project: proj[q][i1][i2] = sum_{r1,r2} conj(V1[r1][i1]) psi_w[a_q][r1][r2]
+ *       conj(V2[r2][i2]) into the host array proj [nidx][n1][n2] (complex128)
+ *       (CalculateProjectionRadialProductStates, examples/tensor/helium_stabilization/
+ *       analysis.cpp:39-81);
+ *   pg_radial_products_remove: the same projections of psi_w, then psi[a_q] -= V1 proj_q V2^T
+ *       (RemoveProjectionRadialProductStates, analysis.cpp:91-121).
+ * psi_w is the wavefunction with the integration weights (the overlap on both radial ranks)
+ * applied, as the reference's callers pass it. Both wait for the context's stream.
+ */
+int pg_radial_products_project(pg_ctx *ctx, const void *psi_w, int nang, int N1, int N2, const int *angular, int nidx,
+                               const double *V1, int n1, const double *V2, int n2, double *proj);
+int pg_radial_products_remove(pg_ctx *ctx, const void *psi_w, void *psi, int nang, int N1, int N2, const int *angular,
+                              int nidx, const double *V1, int n1, const double *V2, int n2);
+
+/* ---------------------------------------------------------------------------------- */
 /* allocation-free entry point                                                        */
 /* ---------------------------------------------------------------------------------- */
 /*

@@ -168,6 +168,32 @@ TIME_FUNCTIONS = {f.__name__: f for f in (
     LaserFunctionSimpleLength, LaserFunctionVelocity, LaserFunctionLength, LaserFunctionFlatTop)}
 
 
+class SingleIonizationBox(PotentialBase):
+    """1 where one electron is beyond ``inner_box_size`` and the other within ``width``, else 0
+    (examples/tensor/helium_stabilization/potential.cpp:190-218): its expectation value is the
+    probability of single ionization."""
+    _keys = ("radial_rank_1", "radial_rank_2", "inner_box_size", "width")
+    radial_rank_1 = 1
+    radial_rank_2 = 2
+    inner_box_size = 20.0
+    width = 20.0
+
+    def GetPotentialValue(self, pos):
+        r1, r2 = pos[self.radial_rank_1], pos[self.radial_rank_2]
+        inside = ((r1 > self.inner_box_size) & (r2 < self.width)) | ((r2 > self.inner_box_size) & (r1 < self.width))
+        return np.broadcast_to(inside.astype(np.float64), np.broadcast(*pos).shape)
+
+
+class DoubleIonizationBox(SingleIonizationBox):
+    """1 where both electrons are beyond ``inner_box_size``, else 0 (potential.cpp:220-247):
+    its expectation value is the probability of double ionization."""
+
+    def GetPotentialValue(self, pos):
+        r1, r2 = pos[self.radial_rank_1], pos[self.radial_rank_2]
+        inside = (r1 > self.inner_box_size) & (r2 > self.inner_box_size)
+        return np.broadcast_to(inside.astype(np.float64), np.broadcast(*pos).shape)
+
+
 def register_potential(cls):
     """Make a user evaluator class available to ``classname = "..."`` in configs."""
     POTENTIAL_CLASSES[cls.__name__] = cls
@@ -313,5 +339,5 @@ class CustomPotential_LaserLength(CoupledPotentialBase):
 
 
 for _cls in (CoupledSphericalCoulombPotential, CoupledSphericalKineticEnergyEvaluator, CustomPotentialEvaluationR12,
-             CustomPotential_LaserLength):
+             CustomPotential_LaserLength, SingleIonizationBox, DoubleIonizationBox):
     POTENTIAL_CLASSES[_cls.__name__] = _cls

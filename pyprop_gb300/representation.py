@@ -59,6 +59,11 @@ class CombinedRepresentation:
     def MultiplyOverlap(self, psi):
         self._radial(nat.PG_BAND_MUL_S, psi.GetData())
 
+    def MultiplyIntegrationWeights(self, psi):
+        """The integration weights of every rank (combinedrepresentation.cpp:93-130): the overlap
+        on the B-spline ranks, 1 on the angular basis ranks."""
+        self._radial(nat.PG_BAND_MUL_S, psi.GetData())
+
     def SolveOverlap(self, psi):
         self._radial(nat.PG_BAND_SOLVE_S, psi.GetData())
 

@@ -422,6 +422,31 @@ class TensorPotential:
     def GetTimeScaling(self, t):
         return float(self.TimeFunction(t)) if self.IsTimeDependent else 1.0
 
+    def _device_operator(self):
+        """This potential alone as a device operator (FP64), built on first use."""
+        if getattr(self, "_op", None) is None:
+            from . import _native as nat
+            from .gpu import Context, DeviceOperator
+            repr_ = self.psi.GetRepresentation()
+            if getattr(self, "BasisPairs", None) is None:
+                self.SetupStep(0.0)
+            self._op = DeviceOperator(Context.get(), [self], repr_.GetFullShape(), repr_.kb, nat.PG_FP64)
+        return self._op
+
+    def MultiplyPotential(self, srcPsi, destPsi, t, timeStep):
+        """destPsi += f(t) V srcPsi on the device (TensorPotential.py:92-112)."""
+        op = self._device_operator()
+        op.matvec(op.scales(t), srcPsi.GetData(), destPsi.GetData(), accumulate=True)
+
+    def GetExpectationValue(self, psi, tmpPsi, t, timeStep):
+        """<psi|V|psi>: tmpPsi = S^-1 V psi, then the S-weighted inner product with psi
+        (TensorPotential.py:117-125)."""
+        tmpPsi.Clear()
+        self.MultiplyPotential(psi, tmpPsi, t, timeStep)
+        repr_ = psi.GetRepresentation()
+        repr_.SolveOverlap(tmpPsi)
+        return psi.InnerProduct(tmpPsi)
+
     def CanConsolidate(self, other):
         """Same time dependence, same storage and basis pairs in every rank (``:128-163``)."""
         if self.Factors is not None or other.Factors is not None:
