@@ -457,6 +457,28 @@ int pg_mlp_train_step(pg_mlp *m, const void *X_bf16, const float *T, int batch, 
 int pg_mlp_block_features(pg_ctx *ctx, const void *y, int nblk, int N, int d_in, void *X_bf16);
 
 /* ---------------------------------------------------------------------------------- */
+/* operator construction: projection into B-spline band rows                          */
+/* ---------------------------------------------------------------------------------- */
+/*
+ * pg_bspline_band_project: for every batch row b < nbatch, the band rows of
+ *     M_b[i][j] = sum_{m < nint} sum_{p < q} w[m q + p] B[m][i - first[m]][p] B[m][j - first[m]][p]
+ *                 F[b * in_bstride + (m q + p) * in_qstride],   |i - j| < k,
+ * written to out[(b / bdiv) * ob1 + (b % bdiv) * ob2 + i * oi + d * od], d = (k - 1) + j - i
+ * (all pointers device, FP64). B [nint][k][q]: the k splines nonzero on quadrature interval m
+ * (first[m] + a, zero values outside [0, N)) at its q points; w [nint * q] the quadrature
+ * weights. This is the representation of a grid function in the B-spline basis that the
+ * tensor-potential generator performs on the host (TensorPotentialGenerator.py:80-274,
+ * core/tensorpotential/basis_bspline.h:11-47, BSplineGlobalOverlapIntegral in
+ * core/transform/bspline/bspline.cpp:373-466), without derivatives; two calls (along r2,
+ * then along r1 over the first result's columns) give a two-electron radial factor. The row
+ * and its band must fit in shared memory (PG_ERR_SHAPE otherwise).
+ */
+int pg_bspline_band_project(pg_ctx *ctx, const double *F, long long nbatch, int bdiv, long long in_bstride,
+                            long long in_qstride, int nint, int k, int q, const int *first, const double *B,
+                            const double *w, int N, double *out, long long ob1, long long ob2, long long oi,
+                            long long od);
+
+/* ---------------------------------------------------------------------------------- */
 /* analysis: projections on products of single-electron radial states                 */
 /* ---------------------------------------------------------------------------------- */
 /*

@@ -129,6 +129,8 @@ _SIGS = {
     "pg_mlp_train_step": (_I, [_P, _P, _P, _I, C.c_float, _DP]),
     "pg_mlp_block_features": (_I, [_P, _P, _I, _I, _I, _P]),
     "pg_vec_multidot_noalloc": (_I, [_I, _P, _LL, _I, _P, _LL, _P, _P]),
+    "pg_bspline_band_project": (_I, [_P, _P, _LL, _I, _LL, _LL, _I, _I, _I, _P, _P, _P, _I, _P, _LL, _LL, _LL,
+                                     _LL]),
     "pg_radial_products_project": (_I, [_P, _P, _I, _I, _I, _IP, _I, _DP, _I, _DP, _I, _DP]),
     "pg_radial_products_remove": (_I, [_P, _P, _P, _I, _I, _I, _IP, _I, _DP, _I, _DP, _I]),
 }

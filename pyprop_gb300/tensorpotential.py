@@ -314,6 +314,73 @@ def _radial_stencil(data2, pairs1, pairs2, N1, N2, kb):
     return R
 
 
+def _full_band(pairs, N, kb):
+    """True when the in-band pairs of a radial geometry are the whole band |i - j| <= kb
+    (the device projection writes every band entry)."""
+    p = np.asarray(pairs)
+    inside = p[np.abs(p[:, 1] - p[:, 0]) <= kb]
+    return len({(int(i), int(j)) for i, j in inside}) == N * (2 * kb + 1) - kb * (kb + 1)
+
+
+def gpu_setup_enabled():
+    """Radial factors of two-electron terms are projected on the GPU when a CUDA device is
+    present (PYPROP_GPU_SETUP=0 keeps the host projection, e.g. to compare the two)."""
+    import os
+    if os.environ.get("PYPROP_GPU_SETUP", "1") == "0":
+        return False
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def _device_tables(bs):
+    """Device copies of a B-spline basis's local tables: (first [nint] int32, values
+    [nint][k][q], weights [nint*q]) as torch tensors, cached on the basis object."""
+    import torch
+    tabs = getattr(bs, "_gpu_tables", None)
+    if tabs is None:
+        idx, valid, cols, loc = bs._local()
+        a0 = np.argmax(valid, axis=1)
+        first = (idx[np.arange(idx.shape[0]), a0] - a0).astype(np.int32)
+        tabs = (torch.as_tensor(first, device="cuda"), torch.as_tensor(np.ascontiguousarray(loc[0]), device="cuda"),
+                torch.as_tensor(np.ascontiguousarray(bs.weights), device="cuda"))
+        bs._gpu_tables = tabs
+    return tabs
+
+
+def radial_stencil_gpu(values, bs1, bs2):
+    """The stencil [N1][2k-1][2k-1][N2] of a real function values[q1][q2] on the two radial
+    quadrature grids (no derivatives), projected on the GPU by pg_bspline_band_project:
+    along r2 for every r1 point, then along r1 for every (i2, d2) column. Equals the host
+    ``_radial_stencil(_project(...))`` to rounding."""
+    import torch
+    from .gpu import Context, check, ptr
+    ctx = Context.get()
+    k = bs1.MaxSplineOrder
+    if bs2.MaxSplineOrder != k:
+        raise ValueError("both radial ranks need the same spline order")
+    bw = 2 * k - 1
+    N1, N2 = bs1.NumberOfBSplines, bs2.NumberOfBSplines
+    nq1, nq2 = len(bs1.grid), len(bs2.grid)
+    f1, B1, w1 = _device_tables(bs1)
+    f2, B2, w2 = _device_tables(bs2)
+    F = torch.as_tensor(np.ascontiguousarray(values, dtype=np.float64), device="cuda")
+    if tuple(F.shape) != (nq1, nq2):
+        raise ValueError("values must be given on the two quadrature grids")
+    G = torch.empty((nq1, N2, bw), dtype=torch.float64, device="cuda")
+    R = torch.empty((N1, bw, bw, N2), dtype=torch.float64, device="cuda")
+    lib = ctx.lib
+    ctx.bind_stream()
+    check(lib.pg_bspline_band_project(ctx.h, ptr(F), nq1, 1, nq2, 1, B2.shape[0], k, B2.shape[2], ptr(f2), ptr(B2),
+                                      ptr(w2), N2, ptr(G), N2 * bw, 0, bw, 1), "pg_bspline_band_project")
+    check(lib.pg_bspline_band_project(ctx.h, ptr(G), N2 * bw, bw, 1, N2 * bw, B1.shape[0], k, B1.shape[2], ptr(f1),
+                                      ptr(B1), ptr(w1), N1, ptr(R), 1, N2, bw * bw * N2, bw * N2),
+          "pg_bspline_band_project")
+    return R.cpu().numpy()
+
+
 def factorize_potential(bases, geoms, conf, evaluator, pos):
     """FactoredPotential for a rank-3 term on a coupled angular rank and two banded B-spline
     ranks, or None (then the term is stored per pair as in the reference).
@@ -351,17 +418,25 @@ def factorize_potential(bases, geoms, conf, evaluator, pos):
         return None
     shape = (1, len(bases[1].grid(geoms[1])), len(bases[2].grid(geoms[2])))
     N1, N2 = bases[1].size, bases[2].size
+    diffs = [conf.Get("differentiation%d" % r) if conf.Exists("differentiation%d" % r) else 0 for r in (1, 2)]
+    on_gpu = diffs == [0, 0] and all(_full_band(geoms[r].Pairs, bases[r].size, kb) for r in (1, 2)) \
+        and gpu_setup_enabled()
     stencils, coefs, weights = [], [], []
     for values, c in facs:
         c = np.asarray(c, dtype=np.float64).reshape(-1)
         if c.size != npairs or not np.any(c):
             continue
         v = np.broadcast_to(np.asarray(values, dtype=np.complex128), shape).copy()
-        data2 = _project(bases, geoms, conf, v, [1, 2])[0]
-        for part, w in ((data2.real, 1.0), (data2.imag, 1j)):
-            if not np.any(part):
-                continue
-            stencils.append(_radial_stencil(part, geoms[1].Pairs, geoms[2].Pairs, N1, N2, kb))
+        if on_gpu:
+            # projection on the GPU (pg_bspline_band_project), real and imaginary parts
+            bs1, bs2 = bases[1].BSplineObject, bases[2].BSplineObject
+            parts = [(radial_stencil_gpu(p, bs1, bs2), w) for p, w in ((v[0].real, 1.0), (v[0].imag, 1j)) if np.any(p)]
+        else:
+            data2 = _project(bases, geoms, conf, v, [1, 2])[0]
+            parts = [(_radial_stencil(p, geoms[1].Pairs, geoms[2].Pairs, N1, N2, kb), w)
+                     for p, w in ((data2.real, 1.0), (data2.imag, 1j)) if np.any(p)]
+        for stencil, w in parts:
+            stencils.append(stencil)
             coefs.append(c)
             weights.append(w)
     if not stencils:
