@@ -537,6 +537,9 @@ def run_ours(args):
     t_mt, it_mt, pass_mt, _ = run(probs["fp32_tight"], args.steps, args.warmup)
     t_dt, it_dt, _, _ = run(probs["fp64_tight"], args.steps, args.warmup)
     fused = bool(getattr(probs["fp32"].Propagator, "Fused", False))
+    # 2: the cluster variant (three CTAs per channel), 1: one CTA per channel
+    variant = probs["fp32"].Propagator.stepper.fused_variant() if fused else 0
+    kernel_name = {2: "cay_cluster_step_kernel<6>", 1: "cay_fused_step_kernel<6>"}.get(variant, "multi-kernel step")
     if dist:
         tt = torch.tensor([t_mixed, t_fp64], device="cuda", dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -602,8 +605,13 @@ def run_ours(args):
             # dominant kernel: the single-kernel step itself (one launch per step)
             "roofline": {"bound": "hbm", "achieved": bytes_step / (t_mixed / args.steps) / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": bytes_step / (t_mixed / args.steps) / 1e9 / peak,
+                         # ncu does not keep the cluster variant's launch shape (thread-block clusters in a
+                         # cooperative launch), so its DRAM bytes come from the one-CTA-per-channel
+                         # variant, which reads the same working set
                          "traffic": profile_traffic("cay_fused_step_kernel_lmax40_n600.md"),
-                         "kernel": "cay_fused_step_kernel<6>" if fused else "multi-kernel step",
+                         "traffic_source": "ncu capture of cay_fused_step_kernel<6> (same step, one CTA per "
+                                           "channel, same working set)" if variant == 2 else "ncu capture",
+                         "kernel": kernel_name,
                          "avg_launch_us": 1e6 * t_mixed / args.steps, "algorithmic_bytes": bytes_step,
                          "layout_bytes": layout_bytes_step, "peak_kind": peak_kind,
                          "bytes_rule": "per complex64/FP64 product s(sum P_t + 2 N_psi), per block solve the LAPACK "

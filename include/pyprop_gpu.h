@@ -61,8 +61,10 @@ int pg_ctx_use_own_stream(pg_ctx *ctx);
 long long pg_ctx_kernel_launches(pg_ctx *ctx);
 int pg_ctx_synchronize(pg_ctx *ctx);
 /* Device error word: non-zero when a kernel's bounded wait ran out (1: an asynchronous copy,
- * 2: a grid barrier of the single-kernel Cayley step); the kernel then skipped the rest of its
- * work. Waits for the context's stream. */
+ * 2: a grid barrier of the single-kernel Cayley step, 3: a factor copy of its cluster variant)
+ * or when a single-kernel Cayley step was launched with another shape than it was built for
+ * (4: a different grid, or the cluster variant without its thread-block clusters); the kernel
+ * then skipped the rest of its work. Waits for the context's stream. */
 int pg_ctx_device_error(pg_ctx *ctx, int *flag);
 /* Clear the device error word (stream-ordered). */
 int pg_ctx_clear_device_error(pg_ctx *ctx);
@@ -279,11 +281,20 @@ int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scales, int nsc
                  pg_krylov_stats *stats);
 /*
  * pAMP ensembles (no reference counterpart: the reference runs one wavefunction per process):
- * many pg_pamp members (each with its own operator, overlap and basis size) advanced by one
- * graph launch per ensemble step. The m x m exponential runs on the device (one CTA per
- * member, scaling and squaring of the order-6 Pade approximant, pamp.h:430-565) instead of
- * on the host. While a batch exists its members read their slot values from the batch;
- * pg_pamp_batch_destroy gives them back their own. scales: [nmembers][nscales] complex.
+ * many pg_pamp members (each with its own operator, overlap and basis size) advanced together,
+ * one launch per ensemble step. When every member has a complex64 basis (at most 24 vectors)
+ * and a rank-2 operator with real bands, the step is one persistent kernel: each CTA takes
+ * members from a device work list (largest first) and runs a member's whole pAMP step - psi
+ * <- U psi, the Arnoldi steps with CGS2 and FP64 sums, the m x m exponential (scaling and
+ * squaring of the order-6 Pade approximant, pamp.h:430-565) and psi = U^-1 V c. Its launch
+ * shape (threads per CTA, CTAs) is chosen at the first step by timing the candidates on the
+ * members themselves (their wavefunctions are saved and restored around the trials), and
+ * the graph of every member's kernels (all exponentials in one kernel) is timed beside it: the
+ * faster of the two is kept (a member runs on one SM in the persistent kernel and on the whole
+ * GPU in the graph, so small ensembles of large members can favour the graph). Members that do
+ * not qualify always take the graph. While a batch exists its members read their slot values
+ * from the batch; pg_pamp_batch_destroy gives them back their own.
+ * scales: [nmembers][nscales] complex.
  */
 typedef struct pg_pamp_batch pg_pamp_batch;
 int pg_pamp_batch_create(pg_pamp **members, int nmembers, pg_pamp_batch **out);
@@ -293,6 +304,14 @@ int pg_pamp_batch_step(pg_pamp_batch *b, void **psis, double dt, const double *s
  * basis size used (smaller after a happy breakdown). PG_ERR_BREAKDOWN if a Pade denominator
  * was singular. */
 int pg_pamp_batch_stats(pg_pamp_batch *b, pg_krylov_stats *stats);
+/* 1 = the persistent kernel (PG_ERR_STORAGE when a member does not qualify), 0 = the graph,
+ * -1 = the faster of the two, timed at the next step (the default) */
+int pg_pamp_batch_set_mode(pg_pamp_batch *b, int mode);
+/* the mode in use, the tuned launch shape (0 before the first timed step) and the timed
+ * ensemble steps in ms (graph_ms 0 when the graph was not timed); all outputs but mode may be
+ * null */
+int pg_pamp_batch_get_mode(pg_pamp_batch *b, int *mode, int *threads, int *ctas, float *persistent_ms,
+                           float *graph_ms);
 
 typedef struct pg_cayley pg_cayley;
 /*

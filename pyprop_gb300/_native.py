@@ -83,6 +83,9 @@ _SIGS = {
     "pg_pamp_batch_destroy": (_I, [_P]),
     "pg_pamp_batch_step": (_I, [_P, C.POINTER(_P), _D, _DP, _I]),
     "pg_pamp_batch_stats": (_I, [_P, C.POINTER(KrylovStats)]),
+    "pg_pamp_batch_set_mode": (_I, [_P, _I]),
+    "pg_pamp_batch_get_mode": (_I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_float),
+                                    C.POINTER(C.c_float)]),
     "pg_op_add_factored": (_I, [_P, _I, _DP, _DP, _IP, _LL, _IP, _IP, _IP, _DP]),
     "pg_op_factored_info": (_I, [_P, _DP]),
     "pg_op_set_fp64_emulation": (_I, [_P, _I]),

@@ -72,6 +72,7 @@ struct FzArgs {
     unsigned int probe_extra;    // test hook: arrivals barrier number probe_at waits for in addition (0)
     unsigned int probe_at;
     int cl_bpc, cl_rpc, cl_rbmax;  // cluster kernel: blocks and boundary rows per CTA, packed Rb entries
+    int nctas;                   // the grid the per-CTA tables are sized for
     const cxf *lo_inv, *lo_g, *lo_rb, *up_inv, *up_g, *up_rb;
     int nblk, w, fib_per_mat, g_in_smem;
     int nch, N, m;
@@ -509,9 +510,25 @@ struct FzCtl {
     float s;      // 1/beta for the next Krylov vector (formed once: FP64 division is slow here)
 };
 
+// A launch whose shape differs from the one the tables were built for (another grid size, or
+// the cluster kernel without its clusters) touches nothing: CTA 0 reports error word 4 in the
+// device word and the mapped host copies, and every CTA returns.
+__device__ __forceinline__ bool fz_bad_launch(const FzArgs &a, bool bad)
+{
+    if (!bad) return false;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicExch(a.err, 4);
+        if (a.herr) *(volatile int *)a.herr = 4;
+        if (a.hstats) *(volatile int *)&a.hstats->passes = 0;
+        __threadfence_system();
+    }
+    return true;
+}
+
 template <int KB>
 __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
 {
+    if (fz_bad_launch(a, gridDim.x != (unsigned)a.nctas || gridDim.y != 1 || gridDim.z != 1)) return;
     extern __shared__ __align__(16) unsigned char fz_smem[];
     __shared__ cxd sc_diff[PG_MAX_SLOTS], sc_negplus[PG_MAX_SLOTS];
     __shared__ cxf sc_plus[PG_MAX_SLOTS];
@@ -1012,6 +1029,9 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_cluster_step_kernel(FzArgs 
     __shared__ __align__(8) unsigned long long fbar;  // the factor copies' mbarrier
 
     cg::cluster_group cluster = cg::this_cluster();
+    if (fz_bad_launch(a, cluster.num_blocks() != CL_SIZE || gridDim.x != (unsigned)a.nctas || gridDim.y != 1 ||
+                             gridDim.z != 1))
+        return;
     const int cl = blockIdx.x / CL_SIZE;            // cluster: angular channel (when < nch)
     const int cr = (int)cluster.block_rank();       // this CTA's part of the channel
     const bool owner = cl < a.nch;
@@ -1497,6 +1517,7 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
     a.nch = nch;
     a.N = N;
     a.m = m;
+    a.nctas = nctas;
     const size_t n = (size_t)nch * N;
     int code = PG_OK;
     auto alloc = [&](void **p, size_t bytes) {
@@ -1550,6 +1571,7 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
         f->cnctas = cnctas;
         f->cargs = a;
         f->cargs.row_lo = (const int *)f->bufs[6];
+        f->cargs.nctas = cnctas;
         f->cargs.cl_bpc = bpc;
         f->cargs.cl_rpc = rpc;
         f->cargs.cl_rbmax = rbmax;

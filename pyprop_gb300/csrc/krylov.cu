@@ -12,6 +12,8 @@
 // DGKS test (0.717) only decides whether the second pass runs, which changes results at
 // the rounding level.
 #include "pg_internal.cuh"
+#include "pamp_expm.cuh"
+#include "pamp_persistent.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -564,183 +566,11 @@ extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scal
 // fork -> each member's psi = ||psi|| V c and overlap solve -> join.
 namespace {
 
-struct PampExpArgs {
-    const double *cols;  // the member's Hessenberg columns (ArnoldiBuf::d_cols)
-    const double *norm;  // [1] = ||psi||
-    double *c;           // out: [2m] coefficients of psi = V c
-    double *stats;       // out: [0] basis size used, [1] error estimate |c_(k-1)|^2 (before ||psi||), [2] 0 or -1 (singular)
-    int m, double_ortho;
-    double tol;
-};
-
-__device__ __forceinline__ cxd cdiv(cxd a, cxd b)
-{
-    const double d = b.x * b.x + b.y * b.y;
-    return mk<double>((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
-}
-
-// C = A B for k x k row-major matrices in shared memory (C distinct from A and B)
-__device__ void smem_matmul(int k, const cxd *A, const cxd *B, cxd *C)
-{
-    for (int t = threadIdx.x; t < k * k; t += blockDim.x) {
-        const int i = t / k, j = t - i * k;
-        cxd s = mk<double>(0.0, 0.0);
-        for (int q = 0; q < k; ++q) cfma(s, A[i * k + q], B[q * k + j]);
-        C[t] = s;
-    }
-    __syncthreads();
-}
-
 __global__ void __launch_bounds__(256) pamp_expm_kernel(const PampExpArgs *__restrict__ args,
                                                         const double *__restrict__ dt_dev)
 {
-    const PampExpArgs a = args[blockIdx.x];
-    const int m = a.m, tid = threadIdx.x, nt = blockDim.x;
     extern __shared__ __align__(16) unsigned char pe_smem[];
-    cxd *A = reinterpret_cast<cxd *>(pe_smem);
-    cxd *A2 = A + m * m, *P = A2 + m * m, *Q = P + m * m, *T = Q + m * m, *D = T + m * m;
-    __shared__ int k_sh, s_sh, piv_sh, bad_sh;
-    __shared__ double red[256];
-    const size_t cd = 2 * (size_t)(m + 2);
-    if (tid == 0) {  // happy breakdown (pamp.h:306-313): truncate at the first small subdiagonal
-        int k = m;
-        for (int j = 0; j + 1 < m; ++j)
-            if (a.cols[((size_t)j * 3 + 2) * cd + 2 * (j + 1) + 1] < a.tol) {
-                k = j + 1;
-                break;
-            }
-        k_sh = k;
-        bad_sh = 0;
-    }
-    __syncthreads();
-    const int k = k_sh;
-    const double dt = *dt_dev;
-    // A = -i dt H_k
-    double mx = 0.0;
-    for (int t = tid; t < k * k; t += nt) {
-        const int i = t / k, j = t - i * k;
-        cxd h = mk<double>(0.0, 0.0);
-        if (i <= j) {
-            const double *p0 = a.cols + ((size_t)j * 3 + 0) * cd;
-            h = mk<double>(p0[2 * i], p0[2 * i + 1]);
-            if (a.double_ortho) {
-                const double *p1 = a.cols + ((size_t)j * 3 + 1) * cd;
-                h = h + mk<double>(p1[2 * i], p1[2 * i + 1]);
-            }
-        } else if (i == j + 1) {
-            h = mk<double>(a.cols[((size_t)j * 3 + 2) * cd + 2 * (j + 1) + 1], 0.0);
-        }
-        A[t] = mk<double>(dt * h.y, -dt * h.x);
-        mx = fmax(mx, sqrt(A[t].x * A[t].x + A[t].y * A[t].y));
-    }
-    red[tid] = mx;
-    __syncthreads();
-    for (int w = nt / 2; w > 0; w >>= 1) {
-        if (tid < w) red[tid] = fmax(red[tid], red[tid + w]);
-        __syncthreads();
-    }
-    if (tid == 0) s_sh = red[0] > 0.0 ? max(0, (int)ceil(log2(red[0]))) : 0;
-    __syncthreads();
-    const int sq = s_sh;
-    const double scale = ldexp(1.0, -sq);
-    for (int t = tid; t < k * k; t += nt) A[t] = scale * A[t];
-    __syncthreads();
-    smem_matmul(k, A, A, A2);
-    // diagonal Pade approximant of order 6: c_0 = 1, c_(i+1) = c_i (p - i) / ((i + 1)(2p - i))
-    const int order = 6;
-    double c[order + 1];
-    c[0] = 1.0;
-    for (int i = 0; i < order; ++i) c[i + 1] = c[i] * (double)(order - i) / (double)((i + 1) * (2 * order - i));
-    for (int t = tid; t < k * k; t += nt) {
-        const bool dg = (t / k) == (t % k);
-        Q[t] = mk<double>(dg ? c[order] : 0.0, 0.0);
-        P[t] = mk<double>(dg ? c[order - 1] : 0.0, 0.0);
-    }
-    __syncthreads();
-    bool odd = true;
-    for (int i = order - 2; i >= 0; --i) {
-        cxd *M = odd ? Q : P;
-        smem_matmul(k, M, A2, T);
-        for (int t = tid; t < k * k; t += nt) M[t] = T[t] + mk<double>((t / k) == (t % k) ? c[i] : 0.0, 0.0);
-        __syncthreads();
-        odd = !odd;
-    }
-    {
-        cxd *M = odd ? Q : P;
-        smem_matmul(k, M, A, T);
-        for (int t = tid; t < k * k; t += nt) M[t] = T[t];
-        __syncthreads();
-    }
-    // solve (Q - P) X = P by LU with partial pivoting; X overwrites P
-    for (int t = tid; t < k * k; t += nt) D[t] = Q[t] - P[t];
-    __syncthreads();
-    for (int pc = 0; pc < k; ++pc) {
-        if (tid == 0) {
-            int r = pc;
-            double best = -1.0;
-            for (int i = pc; i < k; ++i) {
-                const double v = D[i * k + pc].x * D[i * k + pc].x + D[i * k + pc].y * D[i * k + pc].y;
-                if (v > best) { best = v; r = i; }
-            }
-            piv_sh = r;
-            if (best == 0.0) bad_sh = 1;
-        }
-        __syncthreads();
-        if (bad_sh) break;
-        const int r = piv_sh;
-        if (r != pc)
-            for (int j = tid; j < k; j += nt) {
-                cxd t0 = D[pc * k + j]; D[pc * k + j] = D[r * k + j]; D[r * k + j] = t0;
-                t0 = P[pc * k + j]; P[pc * k + j] = P[r * k + j]; P[r * k + j] = t0;
-            }
-        __syncthreads();
-        for (int i = pc + 1 + tid; i < k; i += nt) D[i * k + pc] = cdiv(D[i * k + pc], D[pc * k + pc]);
-        __syncthreads();
-        for (int t = tid; t < (k - pc - 1) * k; t += nt) {
-            const int i = pc + 1 + t / k, j = t % k;
-            const cxd l = D[i * k + pc];
-            if (j > pc) D[i * k + j] = D[i * k + j] - l * D[pc * k + j];
-            P[i * k + j] = P[i * k + j] - l * P[pc * k + j];
-        }
-        __syncthreads();
-    }
-    if (bad_sh) {
-        for (int t = tid; t < 2 * m; t += nt) a.c[t] = 0.0;
-        if (tid == 0) { a.stats[0] = k; a.stats[1] = 0.0; a.stats[2] = -1.0; }
-        return;
-    }
-    for (int j = tid; j < k; j += nt)
-        for (int i = k - 1; i >= 0; --i) {
-            cxd sum = P[i * k + j];
-            for (int q = i + 1; q < k; ++q) sum = sum - D[i * k + q] * P[q * k + j];
-            P[i * k + j] = cdiv(sum, D[i * k + i]);
-        }
-    __syncthreads();
-    // E = +-(I + 2 X), then squared sq times
-    cxd *E = P;
-    for (int t = tid; t < k * k; t += nt) {
-        cxd e = 2.0 * E[t];
-        if ((t / k) == (t % k)) e.x += 1.0;
-        E[t] = odd ? mk<double>(-e.x, -e.y) : e;
-    }
-    __syncthreads();
-    for (int q = 0; q < sq; ++q) {
-        smem_matmul(k, E, E, T);
-        for (int t = tid; t < k * k; t += nt) E[t] = T[t];
-        __syncthreads();
-    }
-    const double nrm = a.norm[1];
-    for (int i = tid; i < m; i += nt) {
-        const cxd v = i < k ? E[i * k] : mk<double>(0.0, 0.0);
-        a.c[2 * i] = v.x * nrm;
-        a.c[2 * i + 1] = v.y * nrm;
-    }
-    if (tid == 0) {
-        const cxd last = E[(k - 1) * k];
-        a.stats[0] = k;
-        a.stats[1] = last.x * last.x + last.y * last.y;
-        a.stats[2] = 0.0;
-    }
+    pamp_expm_block(args[blockIdx.x], *dt_dev, pe_smem);
 }
 
 }  // namespace
@@ -761,7 +591,216 @@ struct pg_pamp_batch {
     cudaGraphExec_t exec = nullptr;
     int mmax = 0;
     long long kernels_per_step = 0;
+    // the persistent step (pamp_persistent.cu): one launch for all members
+    int mode = 1;                    // 1 persistent (when pm_ok), 0 the graph of per-member kernels
+    bool auto_mode = true;           // the first step times both and keeps the faster
+    bool pm_ok = false;
+    std::vector<float *> pm_bands;   // real FP32 bands per member
+    std::vector<void *> pm_allocs;   // chunk tables and scratch of the members' solves
+    std::vector<PmMember> h_pm;
+    PmMember *d_pm = nullptr;
+    int *d_order = nullptr;
+    unsigned *d_queue = nullptr;
+    std::vector<void *> pm_psis;     // wavefunctions the uploaded descriptors point to
+    int pm_N = 0, pm_kb = 0, pm_m = 0, pm_nch = 0, pm_ent = 0;
+    bool pm_kb6 = false;
+    size_t pm_smem = 0;
+    int pm_threads = 0, pm_grid = 0; // autotuned at the first persistent step
+    bool pm_wide = false;
+    bool tuned = false;
+    float pm_best_ms = 0.f, graph_ms = 0.f;
 };
+
+// Descriptors of the persistent step, when every member qualifies: a complex64 basis, a rank-2
+// operator with real bands and no dense or factorized part, an overlap factor of the operator's
+// band width, basis and band sizes within the kernel's limits. Otherwise pm_ok stays false and
+// the batch keeps the graph of per-member kernels.
+static int pm_prepare(pg_pamp_batch *b)
+{
+    const int n = (int)b->members.size();
+    b->pm_ok = false;
+    bool all6 = true;
+    for (int k = 0; k < n; ++k) {
+        const pg_pamp *p = b->members[k];
+        const pg_op *op = p->opb;
+        if (p->prec != PG_FP32 || op->rank != 2 || op->ndense_entries > 0 || op->fact.Q > 0) return PG_OK;
+        if (p->m > pm_max_basis() || op->kb < 1 || op->kb > pm_max_halfwidth()) return PG_OK;
+        if (p->ovlb->kind != 0 || p->ovl64->kind != 0 || p->ovlb->kb != op->kb || p->ovl64->kb != op->kb ||
+            p->ovlb->N != op->N || p->ovl64->N != op->N || !p->ovlb->d_U || !p->ovl64->d_U)
+            return PG_OK;
+        for (const auto &v : op->h_bands)
+            if (v.imag() != 0.0) return PG_OK;
+        all6 = all6 && op->kb == 6;
+    }
+    b->h_pm.assign(n, PmMember());
+    b->pm_bands.assign(n, nullptr);
+    std::vector<std::pair<long long, int>> cost(n);
+    for (int k = 0; k < n; ++k) {
+        pg_pamp *p = b->members[k];
+        pg_op *op = p->opb;
+        PG_TRY(pm_real_bands(op, &b->pm_bands[k]));
+        PmMember &M = b->h_pm[k];
+        M.nch = op->nrows;
+        M.N = op->N;
+        M.ld = op->ld;
+        M.kb = op->kb;
+        M.m = p->m;
+        M.double_ortho = p->double_ortho;
+        M.n = p->n;
+        M.nent = (int)op->nentries;
+        M.row_ptr = op->d_row_ptr;
+        M.ent_col = op->d_ent_col;
+        M.ent_band = op->d_ent_band;
+        M.ent_slot = op->d_ent_slot;
+        M.bands = b->pm_bands[k];
+        M.U32 = (const float *)p->ovlb->d_U;
+        M.U64 = (const double *)p->ovl64->d_U;
+        M.V = (cxf *)p->V;
+        M.w = (cxf *)p->w;
+        M.t = (cxf *)p->tmp;
+        M.scales = b->d_scales + (size_t)k * PG_MAX_SLOTS;
+        M.cols = p->ab.d_cols;
+        M.norm = p->d_norm;
+        M.ex.cols = p->ab.d_cols;
+        M.ex.norm = p->d_norm;
+        M.ex.c = p->d_c;
+        M.ex.stats = b->d_stats + 4 * k;
+        M.ex.m = p->m;
+        M.ex.double_ortho = p->double_ortho;
+        M.ex.tol = p->tolerance;
+        PG_TRY(pm_member_tables(M, b->pm_allocs));
+        b->pm_N = std::max(b->pm_N, M.N);
+        b->pm_kb = std::max(b->pm_kb, M.kb);
+        b->pm_m = std::max(b->pm_m, M.m);
+        b->pm_nch = std::max(b->pm_nch, M.nch);
+        b->pm_ent = std::max(b->pm_ent, M.nent);
+        // work list: the largest members first (their steps are the longest)
+        cost[k] = {-(long long)p->n * (long long)(op->h_row_ptr.empty() ? 1 : op->h_row_ptr.back() + op->nrows), k};
+    }
+    std::sort(cost.begin(), cost.end());
+    std::vector<int> order(n);
+    for (int k = 0; k < n; ++k) order[k] = cost[k].second;
+    PG_CUDA_TRY(cudaMalloc(&b->d_pm, sizeof(PmMember) * n));
+    PG_CUDA_TRY(cudaMalloc(&b->d_order, sizeof(int) * n));
+    PG_CUDA_TRY(cudaMemcpy(b->d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    PG_CUDA_TRY(cudaMalloc(&b->d_queue, sizeof(unsigned)));
+    b->pm_kb6 = all6;
+    b->pm_smem = pm_smem_bytes(b->pm_N, b->pm_kb, b->pm_m, b->pm_nch, b->pm_ent);
+    if (pm_occupancy(128, b->pm_smem, all6, false) < 1) return PG_OK;  // shared memory beyond the limit
+    b->pm_ok = true;
+    return PG_OK;
+}
+
+static int pm_set_psis(pg_pamp_batch *b, void **psis)
+{
+    const int n = (int)b->members.size();
+    bool same = (int)b->pm_psis.size() == n;
+    for (int k = 0; same && k < n; ++k) same = (b->pm_psis[k] == psis[k]);
+    if (same) return PG_OK;
+    for (int k = 0; k < n; ++k) b->h_pm[k].psi = (cxd *)psis[k];
+    PG_CUDA_TRY(cudaMemcpyAsync(b->d_pm, b->h_pm.data(), sizeof(PmMember) * n, cudaMemcpyHostToDevice, b->ctx->stream));
+    b->pm_psis.assign(psis, psis + n);
+    return PG_OK;
+}
+
+static int pm_run(pg_pamp_batch *b, int threads, int grid, bool wide)
+{
+    const int n = (int)b->members.size();
+    return pm_launch(b->d_pm, n, b->d_order, b->d_queue, (const double *)(b->d_scales + (size_t)n * PG_MAX_SLOTS),
+                     threads, grid, b->pm_smem, b->pm_kb6, wide, b->ctx->stream, b->pm_N, b->pm_kb, b->pm_m,
+                     b->pm_nch, b->pm_ent);
+}
+
+// The launch shape (register budget, threads per CTA, CTAs) is chosen by timing one ensemble
+// step of every candidate on the members' own data: each trial starts from a saved copy of the
+// wavefunctions, which are restored afterwards. More CTAs run more members at once; fewer keep
+// the working sets of the members in flight inside L2. With with_graph the graph of per-member
+// kernels is timed too (a member runs on one SM in the persistent kernel and on all of them in
+// the graph, so small ensembles of large members favour the graph) and the faster is kept.
+static int pamp_batch_build(pg_pamp_batch *b, void **psis);
+static int pm_tune(pg_pamp_batch *b, void **psis, bool with_graph)
+{
+    pg_ctx *ctx = b->ctx;
+    cudaStream_t s = ctx->stream;
+    const int n = (int)b->members.size();
+    std::vector<size_t> off(n + 1, 0);
+    for (int k = 0; k < n; ++k) off[k + 1] = off[k] + (size_t)b->members[k]->n * sizeof(cxd);
+    char *save = nullptr;
+    PG_CUDA_TRY(cudaMalloc(&save, std::max<size_t>(16, off[n])));
+    struct Guard {
+        char *p;
+        ~Guard() { cudaFree(p); }
+    } guard{save};
+    for (int k = 0; k < n; ++k)
+        PG_CUDA_TRY(cudaMemcpyAsync(save + off[k], psis[k], off[k + 1] - off[k], cudaMemcpyDeviceToDevice, s));
+    auto restore = [&]() -> int {
+        for (int k = 0; k < n; ++k)
+            PG_CUDA_TRY(cudaMemcpyAsync(psis[k], save + off[k], off[k + 1] - off[k], cudaMemcpyDeviceToDevice, s));
+        return PG_OK;
+    };
+    cudaEvent_t e0, e1;
+    PG_CUDA_TRY(cudaEventCreate(&e0));
+    PG_CUDA_TRY(cudaEventCreate(&e1));
+    struct EvGuard {
+        cudaEvent_t a, b;
+        ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
+    } eguard{e0, e1};
+    const int sms = std::max(1, ctx->num_sms);
+    float best = -1.f;
+    int bt = 0, bg = 0;
+    bool bw = false;
+    for (bool wide : {false, true}) {
+        for (int threads : {128, 256, 512}) {
+            const int occ = pm_occupancy(threads, b->pm_smem, b->pm_kb6, wide);
+            if (occ < 1) continue;
+            std::vector<int> grids;
+            for (int g : {sms / 2, sms, 2 * sms, 3 * sms, occ * sms}) {
+                g = std::min(std::min(g, occ * sms), n);
+                if (g >= 1 && std::find(grids.begin(), grids.end(), g) == grids.end()) grids.push_back(g);
+            }
+            for (int g : grids) {
+                PG_TRY(restore());
+                PG_TRY(pm_run(b, threads, g, wide));
+                PG_TRY(restore());
+                PG_CUDA_TRY(cudaEventRecord(e0, s));
+                PG_TRY(pm_run(b, threads, g, wide));
+                PG_CUDA_TRY(cudaEventRecord(e1, s));
+                PG_CUDA_TRY(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                PG_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+                if (best < 0.f || ms < best) {
+                    best = ms;
+                    bt = threads;
+                    bg = g;
+                    bw = wide;
+                }
+            }
+        }
+    }
+    float gms = 0.f;
+    if (with_graph) {
+        PG_TRY(pamp_batch_build(b, psis));
+        for (int rep = 0; rep < 2; ++rep) {
+            PG_TRY(restore());
+            PG_CUDA_TRY(cudaEventRecord(e0, s));
+            PG_CUDA_TRY(cudaGraphLaunch(b->exec, s));
+            PG_CUDA_TRY(cudaEventRecord(e1, s));
+            PG_CUDA_TRY(cudaEventSynchronize(e1));
+            PG_CUDA_TRY(cudaEventElapsedTime(&gms, e0, e1));
+        }
+    }
+    PG_TRY(restore());
+    PG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (bt == 0) return PG_ERR_SHAPE;
+    b->pm_threads = bt;
+    b->pm_grid = bg;
+    b->pm_wide = bw;
+    b->pm_best_ms = best;
+    b->graph_ms = gms;
+    if (with_graph) b->mode = (gms > 0.f && gms < best) ? 0 : 1;
+    b->tuned = true;
+    return PG_OK;
+}
 
 extern "C" int pg_pamp_batch_create(pg_pamp **members, int nmembers, pg_pamp_batch **out)
 {
@@ -813,6 +852,7 @@ extern "C" int pg_pamp_batch_create(pg_pamp **members, int nmembers, pg_pamp_bat
         members[k]->d_scales = b->d_scales + (size_t)k * PG_MAX_SLOTS;
         members[k]->built_psi = nullptr;
     }
+    PG_TRY(pm_prepare(b));
     *out = b;
     return PG_OK;
 }
@@ -839,6 +879,11 @@ extern "C" int pg_pamp_batch_destroy(pg_pamp_batch *b)
     cudaFree(b->d_stats);
     cudaFreeHost(b->h_stats);
     cudaFree(b->d_args);
+    for (float *q : b->pm_bands) cudaFree(q);
+    for (void *q : b->pm_allocs) cudaFree(q);
+    cudaFree(b->d_pm);
+    cudaFree(b->d_order);
+    cudaFree(b->d_queue);
     delete b;
     return PG_OK;
 }
@@ -915,9 +960,9 @@ extern "C" int pg_pamp_batch_step(pg_pamp_batch *b, void **psis, double dt, cons
 {
     if (!b || !psis || nscales < 0 || nscales > PG_MAX_SLOTS || (nscales > 0 && !scales)) return PG_ERR_ARG;
     const int n = (int)b->members.size();
-    bool same = b->exec && (int)b->psis.size() == n;
-    for (int k = 0; same && k < n; ++k) same = (b->psis[k] == psis[k]);
-    if (!same) PG_TRY(pamp_batch_build(b, psis));
+    for (int k = 0; k < n; ++k)
+        if (!psis[k]) return PG_ERR_ARG;
+    const bool tune = b->pm_ok && !b->tuned && (b->auto_mode || b->mode == 1);
     if (b->params_pending) PG_CUDA_TRY(cudaEventSynchronize(b->params_done));
     for (int k = 0; k < n; ++k)
         for (int q = 0; q < PG_MAX_SLOTS; ++q)
@@ -930,8 +975,42 @@ extern "C" int pg_pamp_batch_step(pg_pamp_batch *b, void **psis, double dt, cons
                                 cudaMemcpyHostToDevice, s));
     PG_CUDA_TRY(cudaEventRecord(b->params_done, s));
     b->params_pending = true;
+    if (b->pm_ok) PG_TRY(pm_set_psis(b, psis));
+    if (tune) PG_TRY(pm_tune(b, psis, b->auto_mode));
+    if (b->mode == 1 && b->pm_ok) {
+        PG_TRY(pm_run(b, b->pm_threads, b->pm_grid, b->pm_wide));
+        b->ctx->launches += 1;
+        return PG_OK;
+    }
+    bool same = b->exec && (int)b->psis.size() == n;
+    for (int k = 0; same && k < n; ++k) same = (b->psis[k] == psis[k]);
+    if (!same) PG_TRY(pamp_batch_build(b, psis));
     PG_CUDA_TRY(cudaGraphLaunch(b->exec, s));
     b->ctx->launches += b->kernels_per_step;
+    return PG_OK;
+}
+
+// 1: the persistent step (one launch per ensemble step), 0: the graph of per-member kernels
+extern "C" int pg_pamp_batch_set_mode(pg_pamp_batch *b, int mode)
+{
+    if (!b || mode < -1 || mode > 1) return PG_ERR_ARG;
+    if (mode == 1 && !b->pm_ok) return PG_ERR_STORAGE;
+    PG_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+    b->auto_mode = mode == -1;
+    b->mode = mode == 0 ? 0 : 1;
+    b->tuned = b->tuned && !b->auto_mode;  // automatic again: the next step times both once more
+    return PG_OK;
+}
+
+extern "C" int pg_pamp_batch_get_mode(pg_pamp_batch *b, int *mode, int *threads, int *ctas, float *persistent_ms,
+                                      float *graph_ms)
+{
+    if (!b || !mode) return PG_ERR_ARG;
+    *mode = (b->mode == 1 && b->pm_ok) ? 1 : 0;
+    if (threads) *threads = b->pm_threads;
+    if (ctas) *ctas = b->pm_grid;
+    if (persistent_ms) *persistent_ms = b->pm_best_ms;
+    if (graph_ms) *graph_ms = b->graph_ms;
     return PG_OK;
 }
 

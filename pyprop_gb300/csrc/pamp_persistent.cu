@@ -1,0 +1,662 @@
+// Persistent pAMP ensemble step (declarations and the algorithm in pamp_persistent.cuh).
+//
+// One CTA runs one member's step from start to end, so every wait is a CTA barrier: no CTA
+// waits on another, and a launch needs no co-residency. Per member and Arnoldi step j
+// (reference: core/krylov/pamp/pamp/pamp.h:270-351, the operator of
+// pyprop/propagator/BasisPropagator.py:116-159 MultiplyHamiltonianBalancedOverlap):
+//     w = H(t) t_j                         fused banded rows, real FP32 bands x slot values
+//     w <- U^-T w                          one thread per radial fibre (forward substitution)
+//     h1 = V^H w;  w -= V h1;  h2 = V^H w;  w -= V h2;  beta = ||w||     (CGS2, FP64 CTA sums)
+//     V[j+1] = w / beta;  t_(j+1) = U^-1 V[j+1]   one thread per fibre (back substitution)
+// with t_0 = U^-1 V[0], V[0] = U psi / ||U psi||, and at the end c = ||U psi|| exp(-i dt H_k) e_1
+// (pamp_expm_block) and psi = U^-1 (V c) in FP64. The Hessenberg columns, the coefficients and
+// the statistics land where the graph path puts them, so both paths share their readers.
+// The member's working set (bands, basis, scratch) is read from L2 or HBM; a fibre's overlap
+// factor sits in shared memory for the substitutions.
+#include "pamp_persistent.cuh"
+
+#include <algorithm>
+#include <mutex>
+
+namespace {
+
+constexpr int PM_MAXM = 20;     // Krylov basis sizes with per-thread column sums in registers
+constexpr int PM_MAXKB = 8;     // band half-width (at most the 8-row chunks of the FP64 solve)
+constexpr int PM_RED = 4 * PM_MAXM + 2;  // per-warp partials: two complex columns and one scalar
+constexpr int PM_WARPS = 16;    // at most 512 threads per CTA
+
+struct PmLayout {
+    size_t us = 0, uinv = 0, gu = 0, gl = 0, rp = 0, ent = 0, red = 0, h = 0, gram = 0, scal = 0, cc = 0, ex = 0;
+    size_t bytes = 0;
+};
+
+__host__ __device__ inline size_t pm_align16(size_t x) { return (x + 15) / 16 * 16; }
+
+// Nmax, kbmax, mmax: the members' largest radial size, band half-width and basis size; nchmax,
+// entmax: their largest channel and operator-entry counts
+__host__ __device__ inline PmLayout pm_layout(int Nmax, int kbmax, int mmax, int nchmax, int entmax)
+{
+    PmLayout L;
+    const size_t nck = (size_t)(Nmax + 31) / 32;
+    size_t o = 0;
+    L.us = o;   o = pm_align16(o + sizeof(float) * (size_t)Nmax * (kbmax + 1));
+    L.uinv = o; o = pm_align16(o + sizeof(float) * (size_t)Nmax);
+    L.gu = o;   o = pm_align16(o + sizeof(float) * nck * 32 * kbmax);
+    L.gl = o;   o = pm_align16(o + sizeof(float) * nck * 32 * kbmax);
+    L.rp = o;   o = pm_align16(o + sizeof(int) * (size_t)(nchmax + 1));
+    L.ent = o;  o = pm_align16(o + sizeof(int4) * (size_t)entmax);
+    L.red = o;  o = pm_align16(o + sizeof(double) * PM_WARPS * PM_RED);
+    L.h = o;    o = pm_align16(o + sizeof(cxd) * 3 * (PM_MAXM + 1));
+    L.gram = o; o = pm_align16(o + sizeof(cxd) * PM_MAXM * PM_MAXM);
+    L.scal = o; o = pm_align16(o + sizeof(cxf) * PG_MAX_SLOTS);
+    L.cc = o;   o = pm_align16(o + sizeof(cxd) * PM_MAXM);
+    L.ex = o;   o = pm_align16(o + sizeof(cxd) * 6 * (size_t)mmax * mmax);
+    L.bytes = o;
+    return L;
+}
+
+// Sums of per-thread FP32 column partials acc1[c] and (when two) acc2[c], c < J: warp sums in
+// FP32, CTA sums in FP64, into out1[c] and out2[c] (complex128). Ends after a CTA barrier, so the
+// results are visible to every thread.
+template <int MAXJ, bool TWO>
+__device__ __forceinline__ void pm_reduce(const cxf (&acc1)[MAXJ], const cxf (&acc2)[MAXJ], int J, double *red,
+                                          cxd *out1, cxd *out2)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int c = 0; c < MAXJ; ++c) {
+        if (c < J) {
+            float x = acc1[c].x, y = acc1[c].y, u = 0.f, v = 0.f;
+            if (TWO) {
+                u = acc2[c].x;
+                v = acc2[c].y;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                x += __shfl_xor_sync(0xffffffffu, x, o);
+                y += __shfl_xor_sync(0xffffffffu, y, o);
+                if (TWO) {
+                    u += __shfl_xor_sync(0xffffffffu, u, o);
+                    v += __shfl_xor_sync(0xffffffffu, v, o);
+                }
+            }
+            if (lane == 0) {
+                red[warp * PM_RED + 2 * c] = x;
+                red[warp * PM_RED + 2 * c + 1] = y;
+                if (TWO) {
+                    red[warp * PM_RED + 2 * MAXJ + 2 * c] = u;
+                    red[warp * PM_RED + 2 * MAXJ + 2 * c + 1] = v;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < (TWO ? 4 : 2) * J; q += blockDim.x) {
+        const int second = q >= 2 * J, v = second ? q - 2 * J : q;
+        double sum = 0.0;
+        for (int w = 0; w < nw; ++w) sum += red[w * PM_RED + (second ? 2 * MAXJ : 0) + v];
+        reinterpret_cast<double *>(second ? out2 : out1)[v] = sum;
+    }
+    __syncthreads();
+}
+
+// sum of one FP64 scalar over the CTA (every thread gets it)
+__device__ __forceinline__ double pm_sum1(double v, double *red, double *slot)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp * PM_RED + PM_RED - 1] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < nw; ++w) s += red[w * PM_RED + PM_RED - 1];
+        *slot = s;
+    }
+    __syncthreads();
+    return *slot;
+}
+
+// Banded triangular solves of every fibre of a member, parallel over chunks of CH rows: with z_c
+// the chunk's solution for zero values outside it and G_c (CH x kb, precomputed) its response to
+// the kb values that couple it to the neighbouring chunk (the first kb rows of chunk c+1 for
+// U x = b, the last kb rows of chunk c-1 for U^T x = b),
+//     x_c = z_c + G_c s,
+// and the coupling values s follow from a kb-wide recurrence over the chunks of each fibre.
+// Phase 1 (one thread per (fibre, chunk), the chunk in registers), phase 2 (one thread per
+// fibre), phase 3 (one thread per (fibre, chunk)), a CTA barrier after each. U(i, i+d) at
+// U[i (kb+1) + d]; Uinv (optional) holds 1 / U(i, i); sbuf: [nch][nchunks][kb] scratch.
+template <typename R> struct PmUT;
+template <> struct PmUT<float> { typedef float T; };
+template <> struct PmUT<double> { typedef double T; };
+
+template <int KB, int CH, bool LOWER, typename R>
+__device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x,
+                             int nch, int N, int kb_rt, const R *__restrict__ U, const R *__restrict__ Uinv,
+                             const R *__restrict__ G, cx<R> *__restrict__ sbuf)
+{
+    constexpr int KBC = KB > 0 ? KB : 1;
+    const int kb = KB > 0 ? KB : kb_rt, kw = kb + 1;
+    const int nck = (N + CH - 1) / CH, ntask = nch * nck, tid = threadIdx.x, T = blockDim.x;
+    // phase 1: z_c
+    for (int task = tid; task < ntask; task += T) {
+        const int a = task / nck, c = task - a * nck, r0 = c * CH, len = min(CH, N - r0);
+        const cx<R> *bb = b + (size_t)a * N + r0;
+        cx<R> z[CH];
+#pragma unroll
+        for (int r = 0; r < CH; ++r) {
+            z[r] = mk<R>((R)0, (R)0);
+            if (r < len) {
+                const cx<R> v = bb[r];
+                z[r] = (sc == 1.0) ? v : mk<R>((R)((double)v.x * sc), (R)((double)v.y * sc));
+                if (vout) vout[(size_t)a * N + r0 + r] = z[r];
+            }
+        }
+        if constexpr (LOWER) {
+#pragma unroll
+            for (int r = 0; r < CH; ++r) {
+                if (r < len) {
+                    cx<R> acc = z[r];
+                    if constexpr (KB > 0) {
+#pragma unroll
+                        for (int d = KB; d >= 1; --d)
+                            if (r - d >= 0) {
+                                const R u = U[(size_t)(r0 + r - d) * kw + d];
+                                acc.x -= u * z[r - d].x;
+                                acc.y -= u * z[r - d].y;
+                            }
+                    } else {
+                        for (int d = min(kb, r); d >= 1; --d) {
+                            const R u = U[(size_t)(r0 + r - d) * kw + d];
+                            acc.x -= u * z[r - d].x;
+                            acc.y -= u * z[r - d].y;
+                        }
+                    }
+                    const R inv = Uinv ? Uinv[r0 + r] : (R)1 / U[(size_t)(r0 + r) * kw];
+                    z[r] = mk<R>(acc.x * inv, acc.y * inv);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int r = CH - 1; r >= 0; --r) {
+                if (r < len) {
+                    cx<R> acc = z[r];
+                    if constexpr (KB > 0) {
+#pragma unroll
+                        for (int d = KB; d >= 1; --d)
+                            if (r + d < CH) {  // z past the chunk's (or the fibre's) end is zero
+                                const R u = U[(size_t)(r0 + r) * kw + d];
+                                acc.x -= u * z[r + d].x;
+                                acc.y -= u * z[r + d].y;
+                            }
+                    } else {
+                        for (int d = min(kb, CH - 1 - r); d >= 1; --d) {
+                            const R u = U[(size_t)(r0 + r) * kw + d];
+                            acc.x -= u * z[r + d].x;
+                            acc.y -= u * z[r + d].y;
+                        }
+                    }
+                    const R inv = Uinv ? Uinv[r0 + r] : (R)1 / U[(size_t)(r0 + r) * kw];
+                    z[r] = mk<R>(acc.x * inv, acc.y * inv);
+                }
+            }
+        }
+        cx<R> *xx = x + (size_t)a * N + r0;
+#pragma unroll
+        for (int r = 0; r < CH; ++r)
+            if (r < len) xx[r] = z[r];
+    }
+    __syncthreads();
+    // phase 2: the coupling values of every chunk, in chunk order
+    for (int a = tid; a < nch; a += T) {
+        const cx<R> *xa = x + (size_t)a * N;
+        cx<R> *sa = sbuf + (size_t)a * nck * kb;
+        cx<R> s[KB > 0 ? KB : 16];
+        if constexpr (LOWER) {
+            // s_c = last kb rows of chunk c (c < nck - 1, full chunks)
+            for (int c = 0; c + 1 < nck; ++c) {
+                const int rt = c * CH + CH - kb;
+                cx<R> sn[KB > 0 ? KB : 16];
+                for (int q = 0; q < kb; ++q) {
+                    cx<R> v = xa[rt + q];
+                    if (c > 0) {
+                        const R *g = G + ((size_t)c * CH + (CH - kb + q)) * kb;
+                        for (int p = 0; p < kb; ++p) {
+                            v.x += g[p] * s[p].x;
+                            v.y += g[p] * s[p].y;
+                        }
+                    }
+                    sn[q] = v;
+                }
+                for (int q = 0; q < kb; ++q) {
+                    s[q] = sn[q];
+                    sa[(size_t)c * kb + q] = sn[q];
+                }
+            }
+        } else {
+            // s_c = first kb rows of chunk c (c >= 1), from the last chunk down
+            for (int c = nck - 1; c >= 1; --c) {
+                const int r0 = c * CH;
+                cx<R> sn[KB > 0 ? KB : 16];
+                for (int q = 0; q < kb; ++q) {
+                    cx<R> v = (r0 + q < N) ? xa[r0 + q] : mk<R>((R)0, (R)0);
+                    if (c + 1 < nck) {
+                        const R *g = G + ((size_t)c * CH + q) * kb;
+                        for (int p = 0; p < kb; ++p) {
+                            v.x += g[p] * s[p].x;
+                            v.y += g[p] * s[p].y;
+                        }
+                    }
+                    sn[q] = v;
+                }
+                for (int q = 0; q < kb; ++q) {
+                    s[q] = sn[q];
+                    sa[(size_t)c * kb + q] = sn[q];
+                }
+            }
+        }
+        (void)KBC;
+    }
+    __syncthreads();
+    // phase 3: x_c = z_c + G_c s (the neighbouring chunk's coupling values)
+    for (int task = tid; task < ntask; task += T) {
+        const int a = task / nck, c = task - a * nck, r0 = c * CH, len = min(CH, N - r0);
+        const int cs = LOWER ? c - 1 : c + 1;
+        if (cs < 0 || cs >= nck) continue;
+        const cx<R> *sv = sbuf + ((size_t)a * nck + cs) * kb;
+        cx<R> s[KB > 0 ? KB : 16];
+        for (int q = 0; q < kb; ++q) s[q] = sv[q];
+        cx<R> *xx = x + (size_t)a * N + r0;
+        const R *g = G + (size_t)c * CH * kb;
+        for (int r = 0; r < len; ++r) {
+            cx<R> v = xx[r];
+            for (int q = 0; q < kb; ++q) {
+                const R gq = g[(size_t)r * kb + q];
+                v.x += gq * s[q].x;
+                v.y += gq * s[q].y;
+            }
+            xx[r] = v;
+        }
+    }
+    __syncthreads();
+}
+
+// (U psi)[e] in FP64 for element e = a N + i
+__device__ __forceinline__ cxd pm_upsi(const cxd *__restrict__ psi, const double *__restrict__ U, int N, int kb,
+                                       long long e)
+{
+    const int a = (int)(e / N), i = (int)(e - (long long)a * N);
+    const cxd *x = psi + (size_t)a * N;
+    const double *u = U + (size_t)i * (kb + 1);
+    cxd y = mk<double>(0.0, 0.0);
+    for (int d = 0; d <= kb && i + d < N; ++d) {
+        const double c = __ldg(u + d);
+        const cxd v = x[i + d];
+        y.x = fma(c, v.x, y.x);
+        y.y = fma(c, v.y, y.y);
+    }
+    return y;
+}
+
+template <int KB>
+__device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem, const PmLayout &L)
+{
+    float *Us = reinterpret_cast<float *>(smem + L.us);
+    float *Uinv = reinterpret_cast<float *>(smem + L.uinv);
+    float *Gu = reinterpret_cast<float *>(smem + L.gu);
+    float *Gl = reinterpret_cast<float *>(smem + L.gl);
+    int *rp = reinterpret_cast<int *>(smem + L.rp);
+    int4 *ent = reinterpret_cast<int4 *>(smem + L.ent);
+    double *red = reinterpret_cast<double *>(smem + L.red);
+    cxd *h1 = reinterpret_cast<cxd *>(smem + L.h);
+    cxd *h2 = h1 + (PM_MAXM + 1);
+    cxd *gcol = h2 + (PM_MAXM + 1);
+    cxd *gram = reinterpret_cast<cxd *>(smem + L.gram);
+    cxf *scal = reinterpret_cast<cxf *>(smem + L.scal);
+    cxd *cc = reinterpret_cast<cxd *>(smem + L.cc);
+    const int tid = threadIdx.x, T = blockDim.x;
+    const int N = M.N, nch = M.nch, m = M.m, ld = M.ld;
+    const int kb = (KB > 0) ? KB : M.kb, kw = kb + 1, bw = 2 * kb + 1;
+    const long long n = M.n;
+    const size_t cd = 2 * (size_t)(m + 2);
+    const int nck = (N + 31) / 32;
+    cxf *__restrict__ V = M.V;
+    cxf *__restrict__ w = M.w;
+    cxf *__restrict__ t = M.t;
+
+    // the member's overlap factor, chunk tables, operator rows and slot values in shared memory
+    for (int q = tid; q < N * kw; q += T) Us[q] = M.U32[q];
+    for (int i = tid; i < N; i += T) Uinv[i] = 1.0f / M.U32[(size_t)i * kw];
+    for (int q = tid; q < nck * 32 * kb; q += T) {
+        Gu[q] = M.G32u[q];
+        Gl[q] = M.G32l[q];
+    }
+    for (int r = tid; r <= nch; r += T) rp[r] = M.row_ptr[r];
+    for (int e = tid; e < M.nent; e += T) ent[e] = make_int4(M.ent_col[e], M.ent_band[e], M.ent_slot[e], 0);
+    for (int s = tid; s < PG_MAX_SLOTS; s += T) scal[s] = cvt<float>(M.scales[s]);
+
+    // V[0] = U psi / ||U psi|| (FP64 products and sum), ||U psi|| kept for the combination
+    double nrm = 0.0;
+    for (long long e = tid; e < n; e += T) {
+        const cxd y = pm_upsi(M.psi, M.U64, N, kb, e);
+        nrm = fma(y.x, y.x, fma(y.y, y.y, nrm));
+    }
+    nrm = pm_sum1(nrm, red, reinterpret_cast<double *>(cc));
+    {
+        const double b = sqrt(nrm), s = b > 0.0 ? 1.0 / b : 0.0;
+        if (tid == 0) {
+            M.norm[0] = nrm;
+            M.norm[1] = b;
+        }
+        for (long long e = tid; e < n; e += T) {
+            const cxd y = pm_upsi(M.psi, M.U64, N, kb, e);
+            V[e] = mk<float>((float)(y.x * s), (float)(y.y * s));
+        }
+    }
+    __syncthreads();
+    pm_solve_cta<KB, 32, false, float>(V, 1.0, nullptr, t, nch, N, kb, Us, Uinv, Gu, (cxf *)M.sbuf);
+
+    for (int j = 0; j < m; ++j) {
+        const int J = j + 1;
+        double *col0 = M.cols + ((size_t)j * 3 + 0) * cd;
+        double *col1 = M.cols + ((size_t)j * 3 + 1) * cd;
+        double *col2 = M.cols + ((size_t)j * 3 + 2) * cd;
+        // w = H(t) t_j
+        for (long long e = tid; e < n; e += T) {
+            const int a = (int)(e / N), i = (int)(e - (long long)a * N);
+            cxf acc = mk<float>(0.f, 0.f);
+            const int e1 = rp[a + 1];
+            for (int en = rp[a]; en < e1; ++en) {
+                const int4 E = ent[en];
+                const float *__restrict__ B = M.bands + (size_t)E.y * bw * ld + i;
+                const cxf *__restrict__ x = t + (size_t)E.x * N;
+                cxf tt = mk<float>(0.f, 0.f);
+                if constexpr (KB > 0) {
+                    float c[2 * KB + 1];
+#pragma unroll
+                    for (int d = 0; d < 2 * KB + 1; ++d) c[d] = __ldg(B + (size_t)d * ld);
+#pragma unroll
+                    for (int d = 0; d < 2 * KB + 1; ++d) {
+                        const int jj = i + d - KB;
+                        if (jj >= 0 && jj < N) {
+                            const cxf v = x[jj];
+                            tt.x = fmaf(c[d], v.x, tt.x);
+                            tt.y = fmaf(c[d], v.y, tt.y);
+                        }
+                    }
+                } else {
+                    for (int d = 0; d < bw; ++d) {
+                        const int jj = i + d - kb;
+                        if (jj >= 0 && jj < N) {
+                            const float c = __ldg(B + (size_t)d * ld);
+                            const cxf v = x[jj];
+                            tt.x = fmaf(c, v.x, tt.x);
+                            tt.y = fmaf(c, v.y, tt.y);
+                        }
+                    }
+                }
+                cfma(acc, scal[E.z], tt);
+            }
+            w[e] = acc;
+        }
+        __syncthreads();
+        pm_solve_cta<KB, 32, true, float>(w, 1.0, nullptr, w, nch, N, kb, Us, Uinv, Gl, (cxf *)M.sbuf);
+        // Gram-Schmidt, first pass: h1 = V^H w and the new Gram column V^H V[j] (one read of V)
+        {
+            cxf acc[PM_MAXM], gacc[PM_MAXM];
+#pragma unroll
+            for (int c = 0; c < PM_MAXM; ++c) {
+                acc[c] = mk<float>(0.f, 0.f);
+                gacc[c] = mk<float>(0.f, 0.f);
+            }
+            for (long long e = tid; e < n; e += T) {
+                const cxf we = w[e], vj = V[(size_t)j * n + e];
+#pragma unroll
+                for (int c = 0; c < PM_MAXM; ++c)
+                    if (c < J) {
+                        const cxf v = V[(size_t)c * n + e];
+                        cfma_conj(acc[c], v, we);
+                        cfma_conj(gacc[c], v, vj);
+                    }
+            }
+            pm_reduce<PM_MAXM, true>(acc, gacc, J, red, h1, gcol);
+        }
+        // second pass through the Gram matrix G = V^H V of the stored basis:
+        // h2 = V^H (w - V h1) = h1 - G h1, so that w - V (h1 + h2) needs one more read of V
+        for (int c = tid; c < J; c += T) {
+            gram[c * PM_MAXM + j] = gcol[c];
+            gram[j * PM_MAXM + c] = c == j ? mk<double>(gcol[c].x, 0.0) : mk<double>(gcol[c].x, -gcol[c].y);
+        }
+        __syncthreads();
+        for (int c = tid; c < J; c += T) {
+            cxd g = mk<double>(0.0, 0.0);
+            if (M.double_ortho)
+                for (int q = 0; q < J; ++q) cfma(g, gram[c * PM_MAXM + q], h1[q]);
+            const cxd hc = M.double_ortho ? h1[c] - g : mk<double>(0.0, 0.0);
+            h2[c] = hc;
+            col0[2 * c] = h1[c].x;
+            col0[2 * c + 1] = h1[c].y;
+            col1[2 * c] = hc.x;
+            col1[2 * c + 1] = hc.y;
+        }
+        __syncthreads();
+        // w - V (h1 + h2) into the slot of V[j+1] (unnormalised) and beta = its norm
+        {
+            cxf *dst = (J < m) ? V + (size_t)J * n : nullptr;
+            double nn = 0.0;
+            for (long long e = tid; e < n; e += T) {
+                cxf x = w[e];
+#pragma unroll
+                for (int c = 0; c < PM_MAXM; ++c)
+                    if (c < J) {
+                        const cxf v = V[(size_t)c * n + e];
+                        const cxf hc = cvt<float>(h1[c] + h2[c]);
+                        x.x = fmaf(-v.x, hc.x, x.x);
+                        x.x = fmaf(v.y, hc.y, x.x);
+                        x.y = fmaf(-v.x, hc.y, x.y);
+                        x.y = fmaf(-v.y, hc.x, x.y);
+                    }
+                if (dst) dst[e] = x;
+                nn = fma((double)x.x, (double)x.x, fma((double)x.y, (double)x.y, nn));
+            }
+            nn = pm_sum1(nn, red, reinterpret_cast<double *>(cc));
+            const double beta = sqrt(nn);
+            if (tid == 0) {
+                col2[2 * J] = nn;
+                col2[2 * J + 1] = beta;
+            }
+            // V[j+1] = (w - V h) / beta in place and t_(j+1) = U^-1 V[j+1]
+            if (dst) {
+                const double s = beta > 0.0 ? 1.0 / beta : 0.0;
+                pm_solve_cta<KB, 32, false, float>(dst, s, dst, t, nch, N, kb, Us, Uinv, Gu, (cxf *)M.sbuf);
+            }
+        }
+    }
+    __syncthreads();  // the columns written above are read by the exponential's threads
+    pamp_expm_block(M.ex, dt, smem + L.ex);
+    // psi = V c (c includes ||U psi||), then psi <- U^-1 psi in FP64
+    const int k = (int)M.ex.stats[0];
+    for (int c = tid; c < PM_MAXM; c += T) cc[c] = c < k ? mk<double>(M.ex.c[2 * c], M.ex.c[2 * c + 1]) : mk<double>(0.0, 0.0);
+    __syncthreads();
+    for (long long e = tid; e < n; e += T) {
+        double ax = 0.0, ay = 0.0;
+        for (int c = 0; c < k; ++c) {
+            const cxf v = V[(size_t)c * n + e];
+            const cxd q = cc[c];
+            ax = fma((double)v.x, q.x, ax);
+            ax = fma(-(double)v.y, q.y, ax);
+            ay = fma((double)v.x, q.y, ay);
+            ay = fma((double)v.y, q.x, ay);
+        }
+        M.psi[e] = mk<double>(ax, ay);
+    }
+    __syncthreads();
+    pm_solve_cta<KB, 8, false, double>(M.psi, 1.0, nullptr, M.psi, nch, N, kb, M.U64, nullptr, M.G64u,
+                                        (cxd *)M.sbuf);
+}
+
+// MAXT: the launch bound (512: 128 registers per thread, some spilled; 256: room for all of
+// them, fewer warps per SM) - the autotuner times both
+template <int KB, int MAXT>
+__global__ void __launch_bounds__(MAXT) pm_step_kernel(const PmMember *__restrict__ members, int nmembers,
+                                                       const int *__restrict__ order, unsigned *queue,
+                                                       const double *__restrict__ dt_dev, PmLayout L)
+{
+    extern __shared__ __align__(16) unsigned char pm_smem[];
+    __shared__ int s_pick;
+    const double dt = *dt_dev;
+    for (;;) {
+        if (threadIdx.x == 0) s_pick = (int)atomicAdd(queue, 1u);
+        __syncthreads();
+        const int q = s_pick;
+        __syncthreads();  // everyone has read the pick before thread 0 takes the next one
+        if (q >= nmembers) break;
+        pm_member_step<KB>(members[order[q]], dt, pm_smem, L);
+    }
+}
+
+const void *pm_kernel(bool kb6, bool wide)
+{
+    if (kb6) return wide ? (const void *)pm_step_kernel<6, 256> : (const void *)pm_step_kernel<6, 512>;
+    return wide ? (const void *)pm_step_kernel<-1, 256> : (const void *)pm_step_kernel<-1, 512>;
+}
+
+std::mutex g_pm_attr_mutex;
+size_t g_pm_attr[4] = {0, 0, 0, 0};
+
+// the dynamic shared-memory limit of an instance only ever rises
+cudaError_t pm_raise_smem(bool kb6, bool wide, size_t bytes)
+{
+    std::lock_guard<std::mutex> lock(g_pm_attr_mutex);
+    size_t &cur = g_pm_attr[(kb6 ? 1 : 0) + (wide ? 2 : 0)];
+    if (cur >= bytes) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(pm_kernel(kb6, wide), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
+
+}  // namespace
+
+int pm_real_bands(const pg_op *op, float **dev)
+{
+    const size_t rows = op->h_bands.size() / (size_t)std::max(1, op->N);
+    std::vector<float> out(std::max<size_t>(1, rows * (size_t)op->ld), 0.f);
+    for (size_t q = 0; q < rows; ++q)
+        for (int i = 0; i < op->N; ++i) {
+            const std::complex<double> v = op->h_bands[q * op->N + i];
+            if (v.imag() != 0.0) return PG_ERR_STORAGE;
+            out[q * op->ld + i] = (float)v.real();
+        }
+    PG_CUDA_TRY(cudaMalloc((void **)dev, out.size() * sizeof(float)));
+    PG_CUDA_TRY(cudaMemcpy(*dev, out.data(), out.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return PG_OK;
+}
+
+size_t pm_smem_bytes(int Nmax, int kbmax, int mmax, int nchmax, int entmax)
+{
+    return pm_layout(Nmax, kbmax, mmax, nchmax, entmax).bytes;
+}
+
+// Responses [nchunks][CH][kb] of CH-row chunks to their coupling values (see pm_solve_cta), in
+// FP64 from the FP64 factor: upper, the chunk's solution of U y = 0 with y = e_q on the first kb
+// rows after it; lower, of U^T y = 0 with y = e_q on the last kb rows before it.
+static std::vector<double> pm_chunk_tables(const std::vector<double> &U, int N, int kb, int CH, bool lower)
+{
+    const int kw = kb + 1, nck = (N + CH - 1) / CH;
+    std::vector<double> G((size_t)nck * CH * kb, 0.0), y(N, 0.0);
+    for (int c = 0; c < nck; ++c) {
+        const int r0 = c * CH, len = std::min(CH, N - r0);
+        if (lower ? c == 0 : c + 1 >= nck) continue;
+        for (int q = 0; q < kb; ++q) {
+            std::fill(y.begin(), y.end(), 0.0);
+            if (!lower) {
+                const int bi = r0 + CH + q;
+                if (bi >= N) continue;
+                y[bi] = 1.0;
+                for (int i = r0 + len - 1; i >= r0; --i) {
+                    double s = 0.0;
+                    for (int d = 1; d <= kb && i + d < N; ++d) s += U[(size_t)i * kw + d] * y[i + d];
+                    y[i] = -s / U[(size_t)i * kw];
+                }
+            } else {
+                y[r0 - kb + q] = 1.0;
+                for (int i = r0; i < r0 + len; ++i) {
+                    double s = 0.0;
+                    for (int d = 1; d <= kb && i - d >= 0; ++d) s += U[(size_t)(i - d) * kw + d] * y[i - d];
+                    y[i] = -s / U[(size_t)i * kw];
+                }
+            }
+            for (int r = 0; r < len; ++r) G[((size_t)c * CH + r) * kb + q] = y[r0 + r];
+        }
+    }
+    return G;
+}
+
+template <typename T>
+static int pm_upload(const std::vector<double> &v, const T **dst, std::vector<void *> &allocs)
+{
+    std::vector<T> t(v.begin(), v.end());
+    void *p = nullptr;
+    PG_CUDA_TRY(cudaMalloc(&p, std::max<size_t>(1, t.size()) * sizeof(T)));
+    allocs.push_back(p);
+    PG_CUDA_TRY(cudaMemcpy(p, t.data(), t.size() * sizeof(T), cudaMemcpyHostToDevice));
+    *dst = (const T *)p;
+    return PG_OK;
+}
+
+int pm_member_tables(PmMember &M, std::vector<void *> &allocs)
+{
+    if (M.kb < 1 || M.kb > PM_MAXKB || M.N < 1) return PG_ERR_SHAPE;
+    const int kw = M.kb + 1;
+    std::vector<double> U((size_t)M.N * kw);
+    PG_CUDA_TRY(cudaMemcpy(U.data(), M.U64, U.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    PG_TRY(pm_upload<float>(pm_chunk_tables(U, M.N, M.kb, 32, false), &M.G32u, allocs));
+    PG_TRY(pm_upload<float>(pm_chunk_tables(U, M.N, M.kb, 32, true), &M.G32l, allocs));
+    PG_TRY(pm_upload<double>(pm_chunk_tables(U, M.N, M.kb, 8, false), &M.G64u, allocs));
+    void *sb = nullptr;
+    PG_CUDA_TRY(cudaMalloc(&sb, sizeof(cxd) * (size_t)M.nch * ((M.N + 7) / 8) * M.kb + 16));
+    allocs.push_back(sb);
+    M.sbuf = sb;
+    return PG_OK;
+}
+
+int pm_occupancy(int threads, size_t smem, bool kb6, bool wide)
+{
+    if (threads > (wide ? 256 : 512)) return 0;
+    if (pm_raise_smem(kb6, wide, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pm_kernel(kb6, wide), threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return per_sm;
+}
+
+int pm_launch(const PmMember *d_members, int nmembers, const int *d_order, unsigned *d_queue, const double *d_dt,
+              int threads, int grid, size_t smem, bool kb6, bool wide, cudaStream_t s, int Nmax, int kbmax, int mmax,
+              int nchmax, int entmax)
+{
+    if (threads < 32 || threads > (wide ? 256 : 32 * PM_WARPS) || threads % 32 || grid < 1 || nmembers < 1)
+        return PG_ERR_ARG;
+    if (mmax > PM_MAXM || kbmax > PM_MAXKB) return PG_ERR_SHAPE;
+    const PmLayout L = pm_layout(Nmax, kbmax, mmax, nchmax, entmax);
+    if (L.bytes > smem) return PG_ERR_ARG;
+    PG_CUDA_TRY(pm_raise_smem(kb6, wide, smem));
+    PG_CUDA_TRY(cudaMemsetAsync(d_queue, 0, sizeof(unsigned), s));
+    if (kb6 && wide)
+        pm_step_kernel<6, 256><<<grid, threads, smem, s>>>(d_members, nmembers, d_order, d_queue, d_dt, L);
+    else if (kb6)
+        pm_step_kernel<6, 512><<<grid, threads, smem, s>>>(d_members, nmembers, d_order, d_queue, d_dt, L);
+    else if (wide)
+        pm_step_kernel<-1, 256><<<grid, threads, smem, s>>>(d_members, nmembers, d_order, d_queue, d_dt, L);
+    else
+        pm_step_kernel<-1, 512><<<grid, threads, smem, s>>>(d_members, nmembers, d_order, d_queue, d_dt, L);
+    PG_CUDA_TRY(cudaGetLastError());
+    return PG_OK;
+}
+
+int pm_max_basis() { return PM_MAXM; }
+int pm_max_halfwidth() { return PM_MAXKB; }

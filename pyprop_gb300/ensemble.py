@@ -180,6 +180,23 @@ class PamEnsembleGPU(CayleyEnsembleGPU):
         check(self.lib.pg_pamp_batch_stats(self.h, self.stats), "pg_pamp_batch_stats")
         return [s.as_dict() for s in self.stats]
 
+    def set_persistent(self, on=True):
+        """Force one persistent kernel per ensemble step (True; every member must qualify:
+        complex64 basis of at most 20 vectors, rank-2 operator with real bands, band half-width
+        at most 8), the graph of every member's kernels (False), or let the first step time both
+        and keep the faster (None, the default)."""
+        mode = -1 if on is None else (1 if on else 0)
+        check(self.lib.pg_pamp_batch_set_mode(self.h, mode), "pg_pamp_batch_set_mode")
+
+    def launch_shape(self):
+        """{"persistent", "threads", "ctas", "persistent_ms", "graph_ms"}: the step in use, the
+        autotuned launch shape and the timed ensemble steps (zeros before the first step)."""
+        mode, th, ct, ms, gms = C.c_int(), C.c_int(), C.c_int(), C.c_float(), C.c_float()
+        check(self.lib.pg_pamp_batch_get_mode(self.h, C.byref(mode), C.byref(th), C.byref(ct), C.byref(ms),
+                                              C.byref(gms)), "pg_pamp_batch_get_mode")
+        return {"persistent": bool(mode.value), "threads": th.value, "ctas": ct.value, "persistent_ms": ms.value,
+                "graph_ms": gms.value}
+
     def __del__(self):
         try:
             if getattr(self, "h", None):

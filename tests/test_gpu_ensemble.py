@@ -91,22 +91,129 @@ def test_pamp_ensemble_matches_single_members(gpu, precision):
     from pyprop_gb300.ensemble import PamEnsembleGPU
     alone = _pamp_members(precision)
     together = _pamp_members(precision)
+    exact = _pamp_members("fp64") if precision == "fp32" else []
     for _ in range(4):
-        for p in alone:
+        for p in alone + exact:
             p.AdvanceStep()
     ens = PamEnsembleGPU(together)
     for _ in range(4):
         ens.AdvanceStep()
     stats = ens.Stats()
     tol = 1e-11 if precision == "fp64" else 1e-6
-    for a, b, st in zip(alone, together, stats):
-        assert relerr(b.psi.numpy(), a.psi.numpy()) < tol, (precision, relerr(b.psi.numpy(), a.psi.numpy()))
+    for k, (a, b, st) in enumerate(zip(alone, together, stats)):
+        if precision == "fp64":
+            assert relerr(b.psi.numpy(), a.psi.numpy()) < tol, relerr(b.psi.numpy(), a.psi.numpy())
+        else:
+            # complex64 bases (the ensemble's persistent kernel, the lone member's kernels): both
+            # within the FP32 Krylov error of the complex128-basis result, which dt ||H_m|| scales
+            e_lone = relerr(a.psi.numpy(), exact[k].psi.numpy())
+            e_ens = relerr(b.psi.numpy(), exact[k].psi.numpy())
+            assert e_lone < 1e-5 and e_ens < 5 * e_lone + 1e-7, (e_ens, e_lone)
         assert st["Iterations"] == 20
         assert 0.0 <= st["ErrorEstimate"] < 1e-6
         assert abs(a.PropagatedTime - b.PropagatedTime) < 1e-12
     del ens
-    # members step alone again (their own slots back) and agree with the lone copies
+    # members step alone again (their own slots back) and agree with the lone copies (complex64:
+    # to the difference the two paths' rounding left after the ensemble steps)
     for p, q in zip(alone, together):
+        before = relerr(q.psi.numpy(), p.psi.numpy())
         p.AdvanceStep()
         q.AdvanceStep()
-        assert relerr(q.psi.numpy(), p.psi.numpy()) < tol
+        assert relerr(q.psi.numpy(), p.psi.numpy()) < (tol if precision == "fp64" else 2 * before + 1e-6)
+
+
+def _pamp_members_kw(precision, specs, seed):
+    probs = []
+    for k, sp in enumerate(specs):
+        p = hydrogen_problem(propagator="PamPropagatorGPU", precision=precision, **sp)
+        p.SetupStep(skipWavefunctionSetup=True)
+        rng = np.random.default_rng(seed + k)
+        shape = p.psi.GetRepresentation().GetFullShape()
+        psi = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+        p.psi.SetData(psi / np.linalg.norm(psi))
+        p.PropagatedTime = 1.0
+        probs.append(p)
+    return probs
+
+
+@pytest.mark.parametrize("order", [7, 5])
+def test_pamp_persistent_step_matches_graph_and_single_members(gpu, order):
+    """The persistent ensemble step (one CTA per member from a device work list, the whole pAMP
+    step in one launch; order 7: the kernel instance unrolled for 13-diagonal bands, order 5:
+    the generic one) against the graph of per-member kernels and the members stepped alone:
+    complex64 bases agree to the FP32 rounding of the Krylov vectors, the Hessenberg statistics
+    match, and the launch shape was autotuned. Both complex64 paths are judged against the same
+    members on a complex128 basis (their own rounding differs: substitutions here, block
+    inverses there)."""
+    from pyprop_gb300.ensemble import PamEnsembleGPU
+    specs = [dict(lmax=3, nbsplines=40, rmax=40.0, amplitude=0.05, order=order),
+             dict(lmax=5, nbsplines=33, rmax=30.0, amplitude=0.08, wavelength_nm=400.0, order=order),
+             dict(lmax=2, nbsplines=55, rmax=50.0, amplitude=0.02, wavelength_nm=1600.0, order=order),
+             dict(lmax=8, nbsplines=36, rmax=36.0, amplitude=0.1, wavelength_nm=600.0, order=order)]
+    alone = _pamp_members_kw("fp32", specs, 300)
+    graph = _pamp_members_kw("fp32", specs, 300)
+    pers = _pamp_members_kw("fp32", specs, 300)
+    exact = _pamp_members_kw("fp64", specs, 300)
+    eg = PamEnsembleGPU(graph)
+    eg.set_persistent(False)
+    ep = PamEnsembleGPU(pers)
+    ep.set_persistent(True)
+    for _ in range(5):
+        for p in alone + exact:
+            p.AdvanceStep()
+        eg.AdvanceStep()
+        ep.AdvanceStep()
+    shape = ep.launch_shape()
+    assert shape["persistent"] and shape["threads"] >= 128 and shape["ctas"] >= 1 and shape["persistent_ms"] > 0.0
+    assert not eg.launch_shape()["persistent"]
+    for a, g, q, x, sg, sq in zip(alone, graph, pers, exact, eg.Stats(), ep.Stats()):
+        e_graph = relerr(g.psi.numpy(), x.psi.numpy())
+        e_pers = relerr(q.psi.numpy(), x.psi.numpy())
+        assert e_graph < 1e-4 and e_pers < 5 * e_graph + 1e-7, (e_pers, e_graph)
+        assert relerr(q.psi.numpy(), a.psi.numpy()) < 3 * (e_graph + e_pers)
+        assert sq["Iterations"] == sg["Iterations"] == 20
+        assert 0.0 <= sq["ErrorEstimate"] < 1e-4
+        assert abs(np.log10(max(sq["ErrorEstimate"], 1e-300)) - np.log10(max(sg["ErrorEstimate"], 1e-300))) < 1.0
+        assert abs(q.PropagatedTime - a.PropagatedTime) < 1e-12
+
+
+def test_pamp_persistent_step_norm_and_fp64_members(gpu):
+    """Field-free members keep their norm under the persistent step (the exponential of a
+    Hermitian Hessenberg), and an ensemble with a complex128 basis stays on the graph (the
+    persistent kernel takes complex64 bases only)."""
+    from pyprop_gb300.ensemble import PamEnsembleGPU
+    specs = [dict(lmax=4, nbsplines=45, rmax=40.0, amplitude=0.0), dict(lmax=7, nbsplines=30, rmax=30.0, amplitude=0.0)]
+    pers = _pamp_members_kw("fp32", specs, 400)
+    ep = PamEnsembleGPU(pers)
+    ep.set_persistent(True)
+    n0 = [p.psi.GetNorm() for p in pers]
+    for _ in range(20):
+        ep.AdvanceStep()
+    assert ep.launch_shape()["persistent"]
+    for p, a in zip(pers, n0):
+        assert abs(p.psi.GetNorm() - a) < 1e-6
+    e64 = PamEnsembleGPU(_pamp_members_kw("fp64", specs, 400))
+    assert not e64.launch_shape()["persistent"]
+    with pytest.raises(RuntimeError):
+        e64.set_persistent(True)
+
+
+def test_pamp_batch_automatic_choice(gpu):
+    """By default the first ensemble step times the persistent kernel and the graph on the
+    members themselves (restoring their wavefunctions after each trial) and keeps the faster;
+    the step it runs continues from the unchanged start."""
+    from pyprop_gb300.ensemble import PamEnsembleGPU
+    specs = [dict(lmax=3, nbsplines=40, rmax=40.0, amplitude=0.05), dict(lmax=6, nbsplines=50, rmax=40.0, amplitude=0.05)]
+    auto = _pamp_members_kw("fp32", specs, 500)
+    ref = _pamp_members_kw("fp32", specs, 500)
+    ea = PamEnsembleGPU(auto)
+    er = PamEnsembleGPU(ref)
+    er.set_persistent(False)
+    for _ in range(3):
+        ea.AdvanceStep()
+        er.AdvanceStep()
+    shape = ea.launch_shape()
+    assert shape["persistent_ms"] > 0.0 and shape["graph_ms"] > 0.0
+    assert shape["persistent"] == (shape["persistent_ms"] <= shape["graph_ms"])
+    for a, r in zip(auto, ref):
+        assert relerr(a.psi.numpy(), r.psi.numpy()) < 1e-4
