@@ -138,6 +138,7 @@ __device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x,
     constexpr int KBC = KB > 0 ? KB : 1;
     const int kb = KB > 0 ? KB : kb_rt, kw = kb + 1;
     const int nck = (N + CH - 1) / CH, ntask = nch * nck, tid = threadIdx.x, T = blockDim.x;
+    const R scr = (R)sc;  // the scale in the vector's precision (FP64 arithmetic is slow here)
     // phase 1: z_c
     for (int task = tid; task < ntask; task += T) {
         const int a = task / nck, c = task - a * nck, r0 = c * CH, len = min(CH, N - r0);
@@ -148,7 +149,7 @@ __device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x,
             z[r] = mk<R>((R)0, (R)0);
             if (r < len) {
                 const cx<R> v = bb[r];
-                z[r] = (sc == 1.0) ? v : mk<R>((R)((double)v.x * sc), (R)((double)v.y * sc));
+                z[r] = (sc == 1.0) ? v : mk<R>(v.x * scr, v.y * scr);
                 if (vout) vout[(size_t)a * N + r0 + r] = z[r];
             }
         }
@@ -281,6 +282,19 @@ __device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x,
     __syncthreads();
 }
 
+// (h, l) += a (bh + bl) in double-float arithmetic: a bh exactly as ph + pl (FMA), a bl added to
+// the low part, the high parts summed by Knuth's two-sum
+__device__ __forceinline__ void df_madd(float &h, float &l, float a, float bh, float bl)
+{
+    const float ph = a * bh;
+    const float pl = fmaf(a, bh, -ph) + a * bl;
+    const float s = h + ph;
+    const float bb = s - h;
+    const float err = (h - (s - bb)) + (ph - bb);
+    h = s;
+    l += err + pl;
+}
+
 // (U psi)[e] in FP64 for element e = a N + i
 __device__ __forceinline__ cxd pm_upsi(const cxd *__restrict__ psi, const double *__restrict__ U, int N, int kb,
                                        long long e)
@@ -340,17 +354,19 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
     for (long long e = tid; e < n; e += T) {
         const cxd y = pm_upsi(M.psi, M.U64, N, kb, e);
         nrm = fma(y.x, y.x, fma(y.y, y.y, nrm));
+        V[e] = mk<float>((float)y.x, (float)y.y);
     }
     nrm = pm_sum1(nrm, red, reinterpret_cast<double *>(cc));
     {
-        const double b = sqrt(nrm), s = b > 0.0 ? 1.0 / b : 0.0;
+        const double b = sqrt(nrm);
+        const float s = b > 0.0 ? (float)(1.0 / b) : 0.f;
         if (tid == 0) {
             M.norm[0] = nrm;
             M.norm[1] = b;
         }
         for (long long e = tid; e < n; e += T) {
-            const cxd y = pm_upsi(M.psi, M.U64, N, kb, e);
-            V[e] = mk<float>((float)(y.x * s), (float)(y.y * s));
+            const cxf y = V[e];
+            V[e] = mk<float>(y.x * s, y.y * s);
         }
     }
     __syncthreads();
@@ -428,12 +444,14 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
             gram[j * PM_MAXM + c] = c == j ? mk<double>(gcol[c].x, 0.0) : mk<double>(gcol[c].x, -gcol[c].y);
         }
         __syncthreads();
+        cxf *hf = reinterpret_cast<cxf *>(cc);  // h1 + h2 in FP32 for the update
         for (int c = tid; c < J; c += T) {
             cxd g = mk<double>(0.0, 0.0);
             if (M.double_ortho)
                 for (int q = 0; q < J; ++q) cfma(g, gram[c * PM_MAXM + q], h1[q]);
             const cxd hc = M.double_ortho ? h1[c] - g : mk<double>(0.0, 0.0);
             h2[c] = hc;
+            hf[c] = cvt<float>(h1[c] + hc);
             col0[2 * c] = h1[c].x;
             col0[2 * c + 1] = h1[c].y;
             col1[2 * c] = hc.x;
@@ -443,23 +461,24 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
         // w - V (h1 + h2) into the slot of V[j+1] (unnormalised) and beta = its norm
         {
             cxf *dst = (J < m) ? V + (size_t)J * n : nullptr;
-            double nn = 0.0;
+            float nf = 0.f;  // per-thread sum in FP32 (as the graph path's column sums), CTA sum in FP64
             for (long long e = tid; e < n; e += T) {
                 cxf x = w[e];
 #pragma unroll
                 for (int c = 0; c < PM_MAXM; ++c)
                     if (c < J) {
                         const cxf v = V[(size_t)c * n + e];
-                        const cxf hc = cvt<float>(h1[c] + h2[c]);
+                        const cxf hc = hf[c];
                         x.x = fmaf(-v.x, hc.x, x.x);
                         x.x = fmaf(v.y, hc.y, x.x);
                         x.y = fmaf(-v.x, hc.y, x.y);
                         x.y = fmaf(-v.y, hc.x, x.y);
                     }
                 if (dst) dst[e] = x;
-                nn = fma((double)x.x, (double)x.x, fma((double)x.y, (double)x.y, nn));
+                nf = fmaf(x.x, x.x, fmaf(x.y, x.y, nf));
             }
-            nn = pm_sum1(nn, red, reinterpret_cast<double *>(cc));
+            __syncthreads();  // hf (in cc) is read above; pm_sum1 writes its slot there
+            double nn = pm_sum1((double)nf, red, reinterpret_cast<double *>(cc));
             const double beta = sqrt(nn);
             if (tid == 0) {
                 col2[2 * J] = nn;
@@ -478,17 +497,30 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
     const int k = (int)M.ex.stats[0];
     for (int c = tid; c < PM_MAXM; c += T) cc[c] = c < k ? mk<double>(M.ex.c[2 * c], M.ex.c[2 * c + 1]) : mk<double>(0.0, 0.0);
     __syncthreads();
+    // psi = V c in double-float arithmetic (FP32 pairs hi + lo: the coefficients split into two
+    // FP32 parts, each product made exact by an FMA, the sums by Knuth's two-sum), about 2^-44
+    // relative per sum - below the FP32 rounding of the Krylov vectors it combines - at FP32 rates
+    float *cq = reinterpret_cast<float *>(smem + L.ex);  // [k][4]: re hi, re lo, im hi, im lo
+    for (int c = tid; c < k; c += T) {
+        const cxd q = cc[c];
+        const float rh = (float)q.x, ih = (float)q.y;
+        cq[4 * c] = rh;
+        cq[4 * c + 1] = (float)(q.x - (double)rh);
+        cq[4 * c + 2] = ih;
+        cq[4 * c + 3] = (float)(q.y - (double)ih);
+    }
+    __syncthreads();
     for (long long e = tid; e < n; e += T) {
-        double ax = 0.0, ay = 0.0;
+        float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f;
         for (int c = 0; c < k; ++c) {
             const cxf v = V[(size_t)c * n + e];
-            const cxd q = cc[c];
-            ax = fma((double)v.x, q.x, ax);
-            ax = fma(-(double)v.y, q.y, ax);
-            ay = fma((double)v.x, q.y, ay);
-            ay = fma((double)v.y, q.x, ay);
+            const float rh = cq[4 * c], rl = cq[4 * c + 1], ih = cq[4 * c + 2], il = cq[4 * c + 3];
+            df_madd(xh, xl, v.x, rh, rl);
+            df_madd(xh, xl, -v.y, ih, il);
+            df_madd(yh, yl, v.x, ih, il);
+            df_madd(yh, yl, v.y, rh, rl);
         }
-        M.psi[e] = mk<double>(ax, ay);
+        M.psi[e] = mk<double>((double)xh + (double)xl, (double)yh + (double)yl);
     }
     __syncthreads();
     pm_solve_cta<KB, 8, false, double>(M.psi, 1.0, nullptr, M.psi, nch, N, kb, M.U64, nullptr, M.G64u,
