@@ -488,6 +488,7 @@ def run_ours(args):
         p.Propagator.StepStats = False  # steps only enqueue; stats are read after the end event
         p.Propagator.Eager = args.eager
         p.Propagator.FusedStep = fused
+        p.Propagator.FusedVariant = args.fused_variant
         p.SetupStep(skipWavefunctionSetup=True)
         probs[name] = p
     psi0, e0 = initial_state(probs["fp32"])
@@ -577,6 +578,7 @@ def run_ours(args):
 
     ens = run_ensemble(args, torch, flush) if args.ensemble > 0 else None
     ens_pamp = run_pamp_ensemble(args, torch, flush) if args.ensemble > 0 else None
+    two_e_large = time_two_electron_large(torch) if (args.two_electron_large and rank == 0) else None
     cpu = cpu_baseline_sample(nsteps=args.cpu_steps) if (rank == 0 and world == 1 and args.cpu_steps > 0) else None
     if rank == 0:
         steps_per_s = world * args.steps / t_mixed
@@ -650,6 +652,7 @@ def run_ours(args):
                             "repulsion multipoles + field-free terms), complex64, 5 launches back to back",
                 "info": two_e[2]},
             "two_electron_cayley": two_e_steps,
+            "two_electron_large": two_e_large,
             "cpu_baseline": cpu,
             "ensemble": ens,
             "ensemble_pamp": ens_pamp,
@@ -780,36 +783,38 @@ def run_ensemble(args, torch, flush):
             "setup_s": setup_s}
 
 
-def run_pamp_ensemble(args, torch, flush):
-    """The ensemble of run_ensemble with pAMP steps (Krylov basis 20, complex64 basis with FP64
-    Gram-Schmidt sums, the m x m exponentials of all members on the device), one graph launch
-    per ensemble step, against the same members stepped one at a time on the plain FP64 pAMP
-    path (host exponential)."""
-    import pyprop_gb300 as pp
-    from pyprop_gb300.ensemble import PamEnsembleGPU, job_throughput
-    from pyprop_gb300.workloads import hydrogen
-    t_setup = time.perf_counter()
-    params = _my_members(args.ensemble)
+def pamp_member_bytes(prob, m):
+    """Algorithmic bytes of one pAMP step of a member at complex64 (s = 8): m (B_mv + 2 B_S) +
+    sum_j B_GS(j), with B_mv = s (sum_t P_t + 2 N_psi) (P_t: stored elements of term t in the
+    reference's TensorPotential layout), B_S = 2 s N_psi per overlap solve (two per matvec in
+    the balanced form), B_GS(j) = 2 (2j + 2) s N_psi for CGS2 against j + 1 vectors."""
+    s = 8
+    n = int(np.prod(prob.psi.GetRepresentation().GetFullShape()))
+    P = sum(int(np.asarray(pot.PotentialData).size) for pot in prob.Propagator.BasePropagator.PotentialList)
+    b_mv = s * (P + 2 * n)
+    b_s = 2 * s * n
+    return m * (b_mv + 2 * b_s) + sum(2 * (2 * j + 2) * s * n for j in range(m))
 
-    def member(prm, precision):
+
+def _pamp_members(params, precision):
+    import pyprop_gb300 as pp
+    from pyprop_gb300.workloads import hydrogen
+    out = []
+    for prm in params:
         p = pp.Problem(pp.LoadString(hydrogen(propagator="PamPropagatorGPU", precision=precision, rmax=100.0,
                                               timestep=0.01, pulse_duration=10.0, duration=10.0,
                                               krylov_basis_size=20, **prm)))
         p.SetupStep(skipWavefunctionSetup=True)
         psi, _ = initial_state(p)
         p.psi.SetData(psi)
-        return p
+        out.append(p)
+    return out
 
-    probs = [member(prm, "fp32") for prm in params]
-    ens = PamEnsembleGPU(probs)
-    setup_s = time.perf_counter() - t_setup
-    for _ in range(args.warmup):
-        ens.AdvanceStep()
-    torch.cuda.synchronize()
-    K = max(1, min(args.steps, 20))
-    tables = []
-    for k in range(K):
-        tables.append(np.stack([p.Propagator.op64.scales(p.PropagatedTime + k * ens.dt) for p in probs]))
+
+def _time_ensemble(torch, flush, ens, probs, K):
+    """Device seconds of K ensemble steps (CUDA events around each, L2 flushed before each
+    outside the bracket), slot values of each step precomputed."""
+    tables = [np.stack([p.Propagator.op64.scales(p.PropagatedTime + k * ens.dt) for p in probs]) for k in range(K)]
     stream = torch.cuda.current_stream()
     total = 0.0
     for k in range(K):
@@ -820,35 +825,161 @@ def run_pamp_ensemble(args, torch, flush):
         e.record(stream)
         e.synchronize()
         total += s.elapsed_time(e) * 1e-3
+    return total
+
+
+def run_pamp_ensemble(args, torch, flush):
+    """The ensemble of run_ensemble with pAMP steps (Krylov basis 20, complex64 basis with FP64
+    Gram-Schmidt sums, the m x m exponentials of all members on the device). The step is the
+    faster of the persistent kernel (one launch per ensemble step, one CTA per member from a
+    device work list) and the graph of every member's kernels, as the batch's autotuner picks
+    it at its first step; both times are reported. Compared with the same members batched on a
+    complex128 basis (the graph: the persistent kernel takes complex64 bases) and one at a time
+    on the plain FP64 pAMP path (host exponential)."""
+    from pyprop_gb300.ensemble import PamEnsembleGPU, job_throughput
+    t_setup = time.perf_counter()
+    params = _my_members(args.ensemble)
+    probs = _pamp_members(params, "fp32")
+    ens = PamEnsembleGPU(probs)
+    setup_s = time.perf_counter() - t_setup
+    for _ in range(args.warmup):
+        ens.AdvanceStep()
+    torch.cuda.synchronize()
+    K = max(1, min(args.steps, 20))
+    total = _time_ensemble(torch, flush, ens, probs, K)
+    shape = ens.launch_shape()
     err = max(st["ErrorEstimate"] for st in ens.Stats())
     member_steps = K * len(probs)
+    bytes_step = sum(pamp_member_bytes(p, 20) for p in probs)
+    del ens
+    # the same members batched on a complex128 basis (one graph launch per ensemble step)
+    p64 = _pamp_members(params, "fp64")
+    e64 = PamEnsembleGPU(p64)
+    for _ in range(2):
+        e64.AdvanceStep()
+    torch.cuda.synchronize()
+    K64 = max(1, min(K, 5))
+    t64b = _time_ensemble(torch, flush, e64, p64, K64)
+    del e64
+    # and one member at a time on the plain FP64 path, on a sample of the members
     sample = list(range(0, len(params), max(1, len(params) // 16)))[:16]
+    stream = torch.cuda.current_stream()
     t64 = 0.0
     n64 = 0
     for i in sample:
-        p64 = member(params[i], "fp64")
+        q = p64[i]
         for _ in range(3):
-            p64.AdvanceStep()
+            q.AdvanceStep()
         torch.cuda.synchronize()
         for _ in range(5):
             flush.fill_(1.0)
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record(stream)
-            p64.AdvanceStep()
+            q.AdvanceStep()
             e.record(stream)
             e.synchronize()
             t64 += s.elapsed_time(e) * 1e-3
             n64 += 1
-        del p64
+    del p64
     fp64_rate = n64 / t64
-    rate, _, t_job = job_throughput(member_steps, total, _rank_world()[1])
-    del ens
+    world = _rank_world()[1]
+    rate, _, t_job = job_throughput(member_steps, total, world)
+    rate64b, _, _ = job_throughput(K64 * len(probs), t64b, world)
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_step / (total / K) / 1e9
     return {"members": args.ensemble, "member_steps_per_s": rate, "ms_per_ensemble_step": 1e3 * t_job / K,
-            "max_error_estimate": err, "plain_fp64_single_member_steps_per_s": fp64_rate,
-            "speedup_vs_plain_fp64": rate / fp64_rate,
-            "workload": "the members of `ensemble` with pAMP (m=20, complex64 basis, FP64 sums), one graph launch "
-                        "per ensemble step including the device Pade exponentials, L2 flushed between steps",
+            "step": "persistent kernel" if shape["persistent"] else "graph of per-member kernels",
+            "autotuned": shape, "max_error_estimate": err,
+            "batched_fp64_member_steps_per_s": rate64b, "speedup_vs_batched_fp64": rate / rate64b,
+            "plain_fp64_single_member_steps_per_s": fp64_rate, "speedup_vs_plain_fp64": rate / fp64_rate,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "algorithmic_bytes": bytes_step, "peak_kind": peak_kind,
+                         "traffic": profile_traffic("pm_step_kernel_pamp_ensemble256.md"),
+                         "kernel": "pm_step_kernel (persistent)" if shape["persistent"] else "graph",
+                         "bytes_rule": "per member m (B_mv + 2 B_S) + sum_j B_GS(j), complex64"},
+            "workload": "the members of `ensemble` with pAMP (m=20, complex64 basis, FP64 sums), one launch per "
+                        "ensemble step including the device Pade exponentials, L2 flushed between steps",
             "setup_s": setup_s}
+
+
+def time_two_electron_large(torch, steps=2):
+    """The largest two-electron model (coupled L <= 8, l1, l2 <= 16, 200 B-splines of order 7
+    per electron on r in [0, 200]: 1017 channels, 4.07e7 coefficients) end to end: operator
+    set-up (two-electron radial factors projected on the GPU), then mixed-precision Cayley
+    steps (complex64 factorized matvec, FP64 refinement in double-float, fast-diagonalization
+    radial preconditioner) in a length-gauge field; one untimed step first."""
+    import pyprop_gb300 as pp
+    from pyprop_gb300 import _native as nat
+    from pyprop_gb300.workloads import helium
+    t0 = time.perf_counter()
+    prob = pp.Problem(pp.LoadString(helium(propagator="CayleyPropagatorGPU", precision="fp32", amplitude=0.05,
+                                           frequency=0.5, pulse_duration=20.0, duration=20.0, timestep=0.01,
+                                           **TWO_ELECTRON_LARGE)))
+    prob.SetupStep(skipWavefunctionSetup=True)
+    setup_s = time.perf_counter() - t0
+    shape = prob.psi.GetRepresentation().GetFullShape()
+    rng = np.random.default_rng(1)
+    decay = np.exp(-0.05 * np.arange(shape[1]))
+    psi0 = np.zeros(shape, complex)
+    psi0[0] = rng.standard_normal(shape[1:]) * decay[:, None] * decay[None, :]
+    psi0 /= np.linalg.norm(psi0)
+    prob.psi.GetData().copy_(torch.as_tensor(psi0, device="cuda"))
+    prob.PropagatedTime = 1.0
+    prob.AdvanceStep()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    iters = 0
+    resid = 0.0
+    s_ev.record(stream)
+    for _ in range(steps):
+        prob.AdvanceStep()
+        st = prob.Propagator.LastStats
+        iters += st.Iterations
+        resid = max(resid, st.TrueResidual)
+    e_ev.record(stream)
+    e_ev.synchronize()
+    step_s = s_ev.elapsed_time(e_ev) * 1e-3 / steps
+    # the complex64 matvec of the factorized operator alone
+    op = prob.Propagator.BasePropagator.device_operator(nat.PG_FP32)
+    src = torch.randn(tuple(shape), dtype=torch.complex64, device="cuda")
+    dst = torch.zeros_like(src)
+    sc = op.scales(1.0)
+    op.matvec(sc, src, dst)
+    torch.cuda.synchronize()
+    s_ev.record(stream)
+    for _ in range(3):
+        op.matvec(sc, src, dst)
+    e_ev.record(stream)
+    e_ev.synchronize()
+    ms = s_ev.elapsed_time(e_ev) / 3
+    info = op.factored_info()
+    flops = info["flops_mix"] + info["flops_radial"]
+    peak = fp32_fma_peak_tflops()
+    return {"workload": "helium-like, coupled L<=8, l1,l2<=16, 200 B-splines order 7 per electron, r in [0,200] "
+                        "(1017 channels, %d coefficients), Cayley GMRES(20) mixed precision, fast-diagonalization "
+                        "preconditioner, dt=0.01, field on" % int(np.prod(shape)),
+            "setup_s": setup_s, "steps": steps, "steps_per_s": 1.0 / step_s, "s_per_step": step_s,
+            "gmres_iterations_per_step": iters / steps, "fp64_true_residual": resid,
+            "norm": prob.psi.GetNorm(),
+            "roofline_matvec": {"bound": "fma", "achieved": flops / ms / 1e9, "peak": peak, "unit": "TFLOP/s",
+                                "frac": flops / ms / 1e9 / peak, "ms_per_matvec": ms,
+                                "peak_kind": "nominal FP32 FMA peak at the maximum SM clock"},
+            "parity": "oracle comparison at reduced size with the same code path: tests/test_gpu_helium.py"}
+
+
+def profile_ensemble_pamp():
+    """Profiling entry point: the 256-member pAMP ensemble on the persistent kernel (forced),
+    its autotuning launches at the first step, then three steps."""
+    import torch
+    from pyprop_gb300.ensemble import PamEnsembleGPU, hydrogen_ensemble_params
+    probs = _pamp_members(hydrogen_ensemble_params(256), "fp32")
+    ens = PamEnsembleGPU(probs)
+    ens.set_persistent(True)
+    for _ in range(4):
+        ens.AdvanceStep()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "ensemble_pamp", "shape": ens.launch_shape()}))
 
 
 # ---------------------------------------------------------------------------------------
@@ -937,8 +1068,14 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=300,
                     help="oracle Cayley steps timed on one host core for cpu_baseline (0 = skip)")
     ap.add_argument("--two-electron", type=int, default=1, help="factorized two-electron matvec leg (0 = skip)")
-    ap.add_argument("--profile", choices=["matvec_hbm", "two_electron", "two_electron_large"], default=None,
-                    help="profiling entry point instead of the benchmark")
+    ap.add_argument("--profile", choices=["matvec_hbm", "two_electron", "two_electron_large", "ensemble_pamp"],
+                    default=None, help="profiling entry point instead of the benchmark")
+    ap.add_argument("--fused-variant", type=int, default=0, choices=[0, 1, 2],
+                    help="single-kernel Cayley step layout: 0 the cluster variant where it fits, 1 one CTA per "
+                         "channel (the layout to profile: ncu does not keep a cooperative launch's cluster shape), "
+                         "2 the cluster variant")
+    ap.add_argument("--two-electron-large", type=int, default=1,
+                    help="end-to-end leg of the largest two-electron model (0 = skip)")
     ap.add_argument("--eager", action="store_true",
                     help="host-driven GMRES loops (same kernels, visible one by one to a profiler)")
     ap.add_argument("--ensemble", type=int, default=256, help="members of the batched leg (0 = skip)")
@@ -959,6 +1096,10 @@ def main():
     if args.profile == "two_electron_large":
         build_native.build()
         profile_two_electron_large()
+        return
+    if args.profile == "ensemble_pamp":
+        build_native.build()
+        profile_ensemble_pamp()
         return
     if args.impl == "reference":
         run_reference(args)
