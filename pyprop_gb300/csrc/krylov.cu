@@ -602,7 +602,7 @@ struct pg_pamp_batch {
     int *d_order = nullptr;
     unsigned *d_queue = nullptr;
     std::vector<void *> pm_psis;     // wavefunctions the uploaded descriptors point to
-    int pm_N = 0, pm_kb = 0, pm_m = 0, pm_nch = 0, pm_ent = 0;
+    int pm_N = 0, pm_kb = 0, pm_m = 0, pm_nch = 0, pm_ent = 0, pm_basis = 0;
     bool pm_kb6 = false;
     size_t pm_smem = 0;
     int pm_threads = 0, pm_grid = 0; // autotuned at the first persistent step
@@ -669,11 +669,17 @@ static int pm_prepare(pg_pamp_batch *b)
         M.ex.double_ortho = p->double_ortho;
         M.ex.tol = p->tolerance;
         PG_TRY(pm_member_tables(M, b->pm_allocs));
+        // the bands as terms over a few basis bands staged in shared memory, when they allow it
+        // and the basis fits beside the rest (else the real bands are read from global memory)
+        PmMember T = M;
+        PG_TRY(pm_member_basis(op, T, b->pm_allocs));
+        if (T.nbasis > 0 && (size_t)T.nbasis * (2 * op->kb + 1) * op->N * sizeof(float) <= 96 * 1024) M = T;
         b->pm_N = std::max(b->pm_N, M.N);
         b->pm_kb = std::max(b->pm_kb, M.kb);
         b->pm_m = std::max(b->pm_m, M.m);
         b->pm_nch = std::max(b->pm_nch, M.nch);
         b->pm_ent = std::max(b->pm_ent, M.nent);
+        b->pm_basis = std::max(b->pm_basis, M.nbasis);
         // work list: the largest members first (their steps are the longest)
         cost[k] = {-(long long)p->n * (long long)(op->h_row_ptr.empty() ? 1 : op->h_row_ptr.back() + op->nrows), k};
     }
@@ -685,7 +691,7 @@ static int pm_prepare(pg_pamp_batch *b)
     PG_CUDA_TRY(cudaMemcpy(b->d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     PG_CUDA_TRY(cudaMalloc(&b->d_queue, sizeof(unsigned)));
     b->pm_kb6 = all6;
-    b->pm_smem = pm_smem_bytes(b->pm_N, b->pm_kb, b->pm_m, b->pm_nch, b->pm_ent);
+    b->pm_smem = pm_smem_bytes(b->pm_N, b->pm_kb, b->pm_m, b->pm_nch, b->pm_ent, b->pm_basis);
     if (pm_occupancy(128, b->pm_smem, all6, false) < 1) return PG_OK;  // shared memory beyond the limit
     b->pm_ok = true;
     return PG_OK;
@@ -708,7 +714,7 @@ static int pm_run(pg_pamp_batch *b, int threads, int grid, bool wide)
     const int n = (int)b->members.size();
     return pm_launch(b->d_pm, n, b->d_order, b->d_queue, (const double *)(b->d_scales + (size_t)n * PG_MAX_SLOTS),
                      threads, grid, b->pm_smem, b->pm_kb6, wide, b->ctx->stream, b->pm_N, b->pm_kb, b->pm_m,
-                     b->pm_nch, b->pm_ent);
+                     b->pm_nch, b->pm_ent, b->pm_basis);
 }
 
 // The launch shape (register budget, threads per CTA, CTAs) is chosen by timing one ensemble

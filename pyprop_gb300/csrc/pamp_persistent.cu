@@ -16,6 +16,7 @@
 #include "pamp_persistent.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 
 namespace {
@@ -24,17 +25,20 @@ constexpr int PM_MAXM = 20;     // Krylov basis sizes with per-thread column sum
 constexpr int PM_MAXKB = 8;     // band half-width (at most the 8-row chunks of the FP64 solve)
 constexpr int PM_RED = 4 * PM_MAXM + 2;  // per-warp partials: two complex columns and one scalar
 constexpr int PM_WARPS = 16;    // at most 512 threads per CTA
+constexpr int PM_MAXBASIS = 4;  // basis bands of an operator staged in shared memory
 
 struct PmLayout {
-    size_t us = 0, uinv = 0, gu = 0, gl = 0, rp = 0, ent = 0, red = 0, h = 0, gram = 0, scal = 0, cc = 0, ex = 0;
+    size_t us = 0, uinv = 0, gu = 0, gl = 0, rp = 0, ent = 0, bas = 0, red = 0, h = 0, gram = 0, scal = 0, cc = 0,
+           ex = 0;
     size_t bytes = 0;
 };
 
 __host__ __device__ inline size_t pm_align16(size_t x) { return (x + 15) / 16 * 16; }
 
 // Nmax, kbmax, mmax: the members' largest radial size, band half-width and basis size; nchmax,
-// entmax: their largest channel and operator-entry counts
-__host__ __device__ inline PmLayout pm_layout(int Nmax, int kbmax, int mmax, int nchmax, int entmax)
+// entmax: their largest channel and operator-entry (or term) counts; basismax: their largest
+// number of basis bands (0: every member reads its bands from global memory)
+__host__ __device__ inline PmLayout pm_layout(int Nmax, int kbmax, int mmax, int nchmax, int entmax, int basismax)
 {
     PmLayout L;
     const size_t nck = (size_t)(Nmax + 31) / 32;
@@ -45,6 +49,7 @@ __host__ __device__ inline PmLayout pm_layout(int Nmax, int kbmax, int mmax, int
     L.gl = o;   o = pm_align16(o + sizeof(float) * nck * 32 * kbmax);
     L.rp = o;   o = pm_align16(o + sizeof(int) * (size_t)(nchmax + 1));
     L.ent = o;  o = pm_align16(o + sizeof(int4) * (size_t)entmax);
+    L.bas = o;  o = pm_align16(o + sizeof(float) * (size_t)basismax * (2 * kbmax + 1) * Nmax);
     L.red = o;  o = pm_align16(o + sizeof(double) * PM_WARPS * PM_RED);
     L.h = o;    o = pm_align16(o + sizeof(cxd) * 3 * (PM_MAXM + 1));
     L.gram = o; o = pm_align16(o + sizeof(cxd) * PM_MAXM * PM_MAXM);
@@ -346,7 +351,11 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
         Gl[q] = M.G32l[q];
     }
     for (int r = tid; r <= nch; r += T) rp[r] = M.row_ptr[r];
-    for (int e = tid; e < M.nent; e += T) ent[e] = make_int4(M.ent_col[e], M.ent_band[e], M.ent_slot[e], 0);
+    for (int e = tid; e < M.nent; e += T)
+        ent[e] = make_int4(M.ent_col[e], M.ent_band[e], M.ent_slot[e], __float_as_int(M.ent_coef ? M.ent_coef[e] : 1.f));
+    float *Bs = reinterpret_cast<float *>(smem + L.bas);  // basis bands [k][d][N]
+    const int nbasis = M.nbasis;
+    for (int q = tid; q < nbasis * bw * N; q += T) Bs[q] = M.basis[q];
     for (int s = tid; s < PG_MAX_SLOTS; s += T) scal[s] = cvt<float>(M.scales[s]);
 
     // V[0] = U psi / ||U psi|| (FP64 products and sum), ||U psi|| kept for the combination
@@ -384,13 +393,19 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
             const int e1 = rp[a + 1];
             for (int en = rp[a]; en < e1; ++en) {
                 const int4 E = ent[en];
-                const float *__restrict__ B = M.bands + (size_t)E.y * bw * ld + i;
                 const cxf *__restrict__ x = t + (size_t)E.x * N;
                 cxf tt = mk<float>(0.f, 0.f);
                 if constexpr (KB > 0) {
                     float c[2 * KB + 1];
+                    if (nbasis) {  // basis band from shared memory
+                        const float *B = Bs + (size_t)E.y * bw * N + i;
 #pragma unroll
-                    for (int d = 0; d < 2 * KB + 1; ++d) c[d] = __ldg(B + (size_t)d * ld);
+                        for (int d = 0; d < 2 * KB + 1; ++d) c[d] = B[(size_t)d * N];
+                    } else {
+                        const float *__restrict__ B = M.bands + (size_t)E.y * bw * ld + i;
+#pragma unroll
+                        for (int d = 0; d < 2 * KB + 1; ++d) c[d] = __ldg(B + (size_t)d * ld);
+                    }
 #pragma unroll
                     for (int d = 0; d < 2 * KB + 1; ++d) {
                         const int jj = i + d - KB;
@@ -401,17 +416,21 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
                         }
                     }
                 } else {
+                    const float *B = nbasis ? Bs + (size_t)E.y * bw * N + i : M.bands + (size_t)E.y * bw * ld + i;
+                    const int bld = nbasis ? N : ld;
                     for (int d = 0; d < bw; ++d) {
                         const int jj = i + d - kb;
                         if (jj >= 0 && jj < N) {
-                            const float c = __ldg(B + (size_t)d * ld);
+                            const float c = B[(size_t)d * bld];
                             const cxf v = x[jj];
                             tt.x = fmaf(c, v.x, tt.x);
                             tt.y = fmaf(c, v.y, tt.y);
                         }
                     }
                 }
-                cfma(acc, scal[E.z], tt);
+                const float cf = __int_as_float(E.w);
+                const cxf sc = scal[E.z];
+                cfma(acc, mk<float>(sc.x * cf, sc.y * cf), tt);
             }
             w[e] = acc;
         }
@@ -584,9 +603,131 @@ int pm_real_bands(const pg_op *op, float **dev)
     return PG_OK;
 }
 
-size_t pm_smem_bytes(int Nmax, int kbmax, int mmax, int nchmax, int entmax)
+size_t pm_smem_bytes(int Nmax, int kbmax, int mmax, int nchmax, int entmax, int basismax)
 {
-    return pm_layout(Nmax, kbmax, mmax, nchmax, entmax).bytes;
+    return pm_layout(Nmax, kbmax, mmax, nchmax, entmax, basismax).bytes;
+}
+
+int pm_max_basis_bands() { return PM_MAXBASIS; }
+
+int pm_member_basis(const pg_op *op, PmMember &M, std::vector<void *> &allocs)
+{
+    M.nbasis = 0;
+    const int N = op->N, bw = 2 * op->kb + 1;
+    const size_t Lb = (size_t)bw * N;
+    if (N < 1 || op->h_bands.size() % Lb) return PG_OK;
+    const int nb = (int)(op->h_bands.size() / Lb);
+    std::vector<double> B((size_t)nb * Lb);
+    for (size_t x = 0; x < B.size(); ++x) B[x] = op->h_bands[x].real();
+    auto band = [&](int q) { return B.data() + (size_t)q * Lb; };
+    auto amax = [&](const double *v) {
+        double m = 0.0;
+        for (size_t x = 0; x < Lb; ++x) m = std::max(m, std::fabs(v[x]));
+        return m;
+    };
+    // bands that are multiples of one another: rep[q], band q = ratio[q] * band rep[q]
+    std::vector<int> rep(nb, -1), reps;
+    std::vector<double> ratio(nb, 0.0);
+    std::vector<size_t> piv(nb, 0);
+    for (int q = 0; q < nb; ++q) {
+        const double *v = band(q);
+        const double mq = amax(v);
+        for (size_t x = 0; x < Lb; ++x)
+            if (std::fabs(v[x]) == mq) { piv[q] = x; break; }
+        if (mq == 0.0) { rep[q] = -2; continue; }  // an all-zero band contributes nothing
+        for (int r : reps) {
+            const double *u = band(r);
+            const double rho = v[piv[r]] / u[piv[r]];
+            double dev = 0.0;
+            for (size_t x = 0; x < Lb && dev <= 1e-13 * mq; ++x) dev = std::max(dev, std::fabs(v[x] - rho * u[x]));
+            if (dev <= 1e-13 * mq) { rep[q] = r; ratio[q] = rho; break; }
+        }
+        if (rep[q] == -1) { rep[q] = q; ratio[q] = 1.0; reps.push_back(q); }
+    }
+    // representation of every representative over the basis: up to two (basis band, coefficient)
+    std::vector<std::vector<double>> basis;
+    std::vector<std::vector<std::pair<int, double>>> repr(nb);
+    if ((int)reps.size() <= PM_MAXBASIS) {
+        for (int r : reps) {
+            repr[r] = {{(int)basis.size(), 1.0}};
+            basis.emplace_back(band(r), band(r) + Lb);
+        }
+    } else {
+        // blocks on the diagonal: A + alpha D (a common field-free band plus a multiple of one more);
+        // the other blocks: one basis band each
+        std::vector<char> on_diag(nb, 0), off_diag(nb, 0);
+        for (int r = 0; r < op->nrows; ++r)
+            for (int e = op->h_row_ptr[r]; e < op->h_row_ptr[r + 1]; ++e) {
+                const int q = op->h_ent_band[e];
+                if (rep[q] < 0) continue;
+                (op->h_ent_col[e] == r ? on_diag : off_diag)[rep[q]] = 1;
+            }
+        std::vector<int> dreps, oreps;
+        for (int r : reps) {
+            if (on_diag[r] && off_diag[r]) return PG_OK;
+            (on_diag[r] ? dreps : oreps).push_back(r);
+        }
+        if (dreps.size() < 2 || (int)oreps.size() > PM_MAXBASIS - 2) return PG_OK;
+        const double *A = band(dreps[0]);
+        std::vector<double> D(Lb);
+        for (size_t x = 0; x < Lb; ++x) D[x] = band(dreps[1])[x] - A[x];
+        double dd = 0.0;
+        for (size_t x = 0; x < Lb; ++x) dd += D[x] * D[x];
+        if (dd == 0.0) return PG_OK;
+        basis.emplace_back(A, A + Lb);
+        basis.push_back(D);
+        repr[dreps[0]] = {{0, 1.0}};
+        for (size_t k = 1; k < dreps.size(); ++k) {
+            const double *v = band(dreps[k]);
+            double num = 0.0;
+            for (size_t x = 0; x < Lb; ++x) num += (v[x] - A[x]) * D[x];
+            const double alpha = num / dd;
+            double dev = 0.0;
+            for (size_t x = 0; x < Lb; ++x) dev = std::max(dev, std::fabs(v[x] - A[x] - alpha * D[x]));
+            if (dev > 1e-12 * std::max(amax(v), amax(A))) return PG_OK;
+            repr[dreps[k]] = {{0, 1.0}, {1, alpha}};
+        }
+        for (int r : oreps) {
+            repr[r] = {{(int)basis.size(), 1.0}};
+            basis.emplace_back(band(r), band(r) + Lb);
+        }
+    }
+    // terms per operator row, in the order of its entries
+    std::vector<int> rp(op->nrows + 1, 0), tcol, tbas, tslot;
+    std::vector<float> tcoef;
+    for (int r = 0; r < op->nrows; ++r) {
+        for (int e = op->h_row_ptr[r]; e < op->h_row_ptr[r + 1]; ++e) {
+            const int q = op->h_ent_band[e];
+            if (rep[q] < 0) continue;
+            for (const auto &kc : repr[rep[q]]) {
+                tcol.push_back(op->h_ent_col[e]);
+                tbas.push_back(kc.first);
+                tslot.push_back(op->h_ent_slot[e]);
+                tcoef.push_back((float)(ratio[q] * kc.second));
+            }
+        }
+        rp[r + 1] = (int)tcol.size();
+    }
+    std::vector<float> bas(basis.size() * Lb);
+    for (size_t k = 0; k < basis.size(); ++k)
+        for (size_t x = 0; x < Lb; ++x) bas[k * Lb + x] = (float)basis[k][x];
+    auto up = [&](const void *src, size_t bytes, const void **dst) -> int {
+        void *p = nullptr;
+        PG_CUDA_TRY(cudaMalloc(&p, std::max<size_t>(16, bytes)));
+        allocs.push_back(p);
+        if (bytes) PG_CUDA_TRY(cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice));
+        *dst = p;
+        return PG_OK;
+    };
+    PG_TRY(up(rp.data(), rp.size() * sizeof(int), (const void **)&M.row_ptr));
+    PG_TRY(up(tcol.data(), tcol.size() * sizeof(int), (const void **)&M.ent_col));
+    PG_TRY(up(tbas.data(), tbas.size() * sizeof(int), (const void **)&M.ent_band));
+    PG_TRY(up(tslot.data(), tslot.size() * sizeof(int), (const void **)&M.ent_slot));
+    PG_TRY(up(tcoef.data(), tcoef.size() * sizeof(float), (const void **)&M.ent_coef));
+    PG_TRY(up(bas.data(), bas.size() * sizeof(float), (const void **)&M.basis));
+    M.nent = (int)tcol.size();
+    M.nbasis = (int)basis.size();
+    return PG_OK;
 }
 
 // Responses [nchunks][CH][kb] of CH-row chunks to their coupling values (see pm_solve_cta), in
@@ -669,12 +810,12 @@ int pm_occupancy(int threads, size_t smem, bool kb6, bool wide)
 
 int pm_launch(const PmMember *d_members, int nmembers, const int *d_order, unsigned *d_queue, const double *d_dt,
               int threads, int grid, size_t smem, bool kb6, bool wide, cudaStream_t s, int Nmax, int kbmax, int mmax,
-              int nchmax, int entmax)
+              int nchmax, int entmax, int basismax)
 {
     if (threads < 32 || threads > (wide ? 256 : 32 * PM_WARPS) || threads % 32 || grid < 1 || nmembers < 1)
         return PG_ERR_ARG;
     if (mmax > PM_MAXM || kbmax > PM_MAXKB) return PG_ERR_SHAPE;
-    const PmLayout L = pm_layout(Nmax, kbmax, mmax, nchmax, entmax);
+    const PmLayout L = pm_layout(Nmax, kbmax, mmax, nchmax, entmax, basismax);
     if (L.bytes > smem) return PG_ERR_ARG;
     PG_CUDA_TRY(pm_raise_smem(kb6, wide, smem));
     PG_CUDA_TRY(cudaMemsetAsync(d_queue, 0, sizeof(unsigned), s));

@@ -23,6 +23,12 @@ struct PmMember {
     const cxd *scales = nullptr;              // its slot values [PG_MAX_SLOTS]
     double *cols = nullptr;                   // Hessenberg columns [m][3][2(m+2)] (ArnoldiBuf layout)
     double *norm = nullptr;                   // out: ||U psi||^2, ||U psi||
+    // nbasis > 0: the operator's bands are combinations of nbasis basis bands (basis [k][2kb+1][N],
+    // FP32), and row_ptr / ent_col / ent_band / ent_slot / ent_coef describe terms (column, basis
+    // band, slot, coefficient) instead of entries; the basis bands are staged in shared memory
+    int nbasis = 0;
+    const float *basis = nullptr;
+    const float *ent_coef = nullptr;
     const float *G32u = nullptr, *G32l = nullptr;  // chunk responses of the FP32 solves (32-row chunks)
     const double *G64u = nullptr;             // of the FP64 solve (16-row chunks)
     void *sbuf = nullptr;                     // coupling values of the chunks [nch][chunks][kb]
@@ -33,12 +39,19 @@ struct PmMember {
 // non-zero imaginary part
 int pm_real_bands(const pg_op *op, float **dev);
 
+// The operator as terms over at most pm_max_basis_bands() basis bands, when its bands allow it
+// (each a multiple of one basis band, or, for the blocks on the diagonal, of A + alpha D for a
+// common A and D: a per-channel field-free band plus a multiple of the centrifugal one); fills
+// M's term arrays and basis (appended to allocs) and sets M.nbasis, else leaves M.nbasis 0
+int pm_member_basis(const pg_op *op, PmMember &M, std::vector<void *> &allocs);
+int pm_max_basis_bands();
+
 // the chunk tables of the member's banded solves and its scratch (from M.U64, M.N, M.kb, M.nch);
 // the device allocations are appended to allocs (the caller frees them)
 int pm_member_tables(PmMember &M, std::vector<void *> &allocs);
 
 // the largest dynamic shared memory a launch for these members needs
-size_t pm_smem_bytes(int Nmax, int kbmax, int mmax, int nchmax, int entmax);
+size_t pm_smem_bytes(int Nmax, int kbmax, int mmax, int nchmax, int entmax, int basismax);
 
 // one ensemble step: queue (device counter) cleared, then `grid` CTAs of `threads` threads;
 // Nmax, kbmax, mmax, nchmax, entmax: the members' largest radial size, band half-width, basis
@@ -46,7 +59,7 @@ size_t pm_smem_bytes(int Nmax, int kbmax, int mmax, int nchmax, int entmax);
 // wide: the instance bounded at 256 threads (all registers it wants), else at 512
 int pm_launch(const PmMember *d_members, int nmembers, const int *d_order, unsigned *d_queue, const double *d_dt,
               int threads, int grid, size_t smem, bool kb6, bool wide, cudaStream_t s, int Nmax, int kbmax, int mmax,
-              int nchmax, int entmax);
+              int nchmax, int entmax, int basismax);
 
 // limits of the kernel: Krylov basis size and band half-width
 int pm_max_basis();
