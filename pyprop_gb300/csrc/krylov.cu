@@ -657,7 +657,7 @@ static int pm_prepare(pg_pamp_batch *b)
         M.U64 = (const double *)p->ovl64->d_U;
         M.V = (cxf *)p->V;
         M.w = (cxf *)p->w;
-        M.t = (cxf *)p->tmp;
+
         M.scales = b->d_scales + (size_t)k * PG_MAX_SLOTS;
         M.cols = p->ab.d_cols;
         M.norm = p->d_norm;

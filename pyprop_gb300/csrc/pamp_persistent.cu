@@ -4,15 +4,18 @@
 // waits on another, and a launch needs no co-residency. Per member and Arnoldi step j
 // (reference: core/krylov/pamp/pamp/pamp.h:270-351, the operator of
 // pyprop/propagator/BasisPropagator.py:116-159 MultiplyHamiltonianBalancedOverlap):
-//     w = H(t) t_j                         fused banded rows, real FP32 bands x slot values
-//     w <- U^-T w                          one thread per radial fibre (forward substitution)
-//     h1 = V^H w;  w -= V h1;  h2 = V^H w;  w -= V h2;  beta = ||w||     (CGS2, FP64 CTA sums)
-//     V[j+1] = w / beta;  t_(j+1) = U^-1 V[j+1]   one thread per fibre (back substitution)
+//     w = H(t) t_j                        banded rows: real FP32 bands (or basis bands in shared
+//                                         memory) x slot values
+//     w <- U^-T w                         banded solve by chunks (pm_solve_cta)
+//     h1 = V^H w, g = V^H V[j];  h2 = h1 - G h1;  w -= V (h1 + h2);  beta = ||w||
+//                                         CGS2 with its second projection through the Gram matrix
+//                                         G of the stored basis (FP32 per thread, FP64 CTA sums)
+//     V[j+1] = w / beta;  t_(j+1) = U^-1 V[j+1]
 // with t_0 = U^-1 V[0], V[0] = U psi / ||U psi||, and at the end c = ||U psi|| exp(-i dt H_k) e_1
-// (pamp_expm_block) and psi = U^-1 (V c) in FP64. The Hessenberg columns, the coefficients and
-// the statistics land where the graph path puts them, so both paths share their readers.
-// The member's working set (bands, basis, scratch) is read from L2 or HBM; a fibre's overlap
-// factor sits in shared memory for the substitutions.
+// (pamp_expm_block) and psi = U^-1 V c = sum_j c_j t_j in double-float arithmetic. The
+// Hessenberg columns, the coefficients and the statistics land where the graph path puts them,
+// so both paths share their readers. The member's basis and scratch are read from L2 or HBM;
+// its overlap factor, chunk tables and (where they allow it) basis bands sit in shared memory.
 #include "pamp_persistent.cuh"
 
 #include <algorithm>
@@ -49,13 +52,17 @@ __host__ __device__ inline PmLayout pm_layout(int Nmax, int kbmax, int mmax, int
     L.gl = o;   o = pm_align16(o + sizeof(float) * nck * 32 * kbmax);
     L.rp = o;   o = pm_align16(o + sizeof(int) * (size_t)(nchmax + 1));
     L.ent = o;  o = pm_align16(o + sizeof(int4) * (size_t)entmax);
-    L.bas = o;  o = pm_align16(o + sizeof(float) * (size_t)basismax * (2 * kbmax + 1) * Nmax);
+    // the basis bands are read in the Arnoldi steps only; the exponential's scratch, used after
+    // them, shares their region
+    L.bas = o;
+    L.ex = o;
+    o = pm_align16(o + std::max(sizeof(float) * (size_t)basismax * (2 * kbmax + 1) * Nmax,
+                                sizeof(cxd) * 6 * (size_t)mmax * mmax));
     L.red = o;  o = pm_align16(o + sizeof(double) * PM_WARPS * PM_RED);
     L.h = o;    o = pm_align16(o + sizeof(cxd) * 3 * (PM_MAXM + 1));
     L.gram = o; o = pm_align16(o + sizeof(cxd) * PM_MAXM * PM_MAXM);
     L.scal = o; o = pm_align16(o + sizeof(cxf) * PG_MAX_SLOTS);
     L.cc = o;   o = pm_align16(o + sizeof(cxd) * PM_MAXM);
-    L.ex = o;   o = pm_align16(o + sizeof(cxd) * 6 * (size_t)mmax * mmax);
     L.bytes = o;
     return L;
 }
@@ -341,7 +348,7 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
     const int nck = (N + 31) / 32;
     cxf *__restrict__ V = M.V;
     cxf *__restrict__ w = M.w;
-    cxf *__restrict__ t = M.t;
+    cxf *__restrict__ Tb = M.T;  // t_j = U^-1 V[j], all kept: psi = U^-1 V c = T c
 
     // the member's overlap factor, chunk tables, operator rows and slot values in shared memory
     for (int q = tid; q < N * kw; q += T) Us[q] = M.U32[q];
@@ -379,9 +386,10 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
         }
     }
     __syncthreads();
-    pm_solve_cta<KB, 32, false, float>(V, 1.0, nullptr, t, nch, N, kb, Us, Uinv, Gu, (cxf *)M.sbuf);
+    pm_solve_cta<KB, 32, false, float>(V, 1.0, nullptr, Tb, nch, N, kb, Us, Uinv, Gu, (cxf *)M.sbuf);
 
     for (int j = 0; j < m; ++j) {
+        const cxf *__restrict__ t = Tb + (size_t)j * n;
         const int J = j + 1;
         double *col0 = M.cols + ((size_t)j * 3 + 0) * cd;
         double *col1 = M.cols + ((size_t)j * 3 + 1) * cd;
@@ -506,19 +514,21 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
             // V[j+1] = (w - V h) / beta in place and t_(j+1) = U^-1 V[j+1]
             if (dst) {
                 const double s = beta > 0.0 ? 1.0 / beta : 0.0;
-                pm_solve_cta<KB, 32, false, float>(dst, s, dst, t, nch, N, kb, Us, Uinv, Gu, (cxf *)M.sbuf);
+                pm_solve_cta<KB, 32, false, float>(dst, s, dst, Tb + (size_t)J * n, nch, N, kb, Us, Uinv, Gu,
+                                                   (cxf *)M.sbuf);
             }
         }
     }
     __syncthreads();  // the columns written above are read by the exponential's threads
     pamp_expm_block(M.ex, dt, smem + L.ex);
-    // psi = V c (c includes ||U psi||), then psi <- U^-1 psi in FP64
+    // psi = U^-1 V c = T c (c includes ||U psi||): the combination of the t_j = U^-1 V[j] that the
+    // Arnoldi steps computed, so no banded solve of psi is needed
     const int k = (int)M.ex.stats[0];
     for (int c = tid; c < PM_MAXM; c += T) cc[c] = c < k ? mk<double>(M.ex.c[2 * c], M.ex.c[2 * c + 1]) : mk<double>(0.0, 0.0);
     __syncthreads();
-    // psi = V c in double-float arithmetic (FP32 pairs hi + lo: the coefficients split into two
-    // FP32 parts, each product made exact by an FMA, the sums by Knuth's two-sum), about 2^-44
-    // relative per sum - below the FP32 rounding of the Krylov vectors it combines - at FP32 rates
+    // in double-float arithmetic (FP32 pairs hi + lo: the coefficients split into two FP32 parts,
+    // each product made exact by an FMA, the sums by Knuth's two-sum), about 2^-44 relative per
+    // sum - below the FP32 rounding of the vectors it combines - at FP32 rates
     float *cq = reinterpret_cast<float *>(smem + L.ex);  // [k][4]: re hi, re lo, im hi, im lo
     for (int c = tid; c < k; c += T) {
         const cxd q = cc[c];
@@ -532,7 +542,7 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
     for (long long e = tid; e < n; e += T) {
         float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f;
         for (int c = 0; c < k; ++c) {
-            const cxf v = V[(size_t)c * n + e];
+            const cxf v = Tb[(size_t)c * n + e];
             const float rh = cq[4 * c], rl = cq[4 * c + 1], ih = cq[4 * c + 2], il = cq[4 * c + 3];
             df_madd(xh, xl, v.x, rh, rl);
             df_madd(xh, xl, -v.y, ih, il);
@@ -542,8 +552,6 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
         M.psi[e] = mk<double>((double)xh + (double)xl, (double)yh + (double)yl);
     }
     __syncthreads();
-    pm_solve_cta<KB, 8, false, double>(M.psi, 1.0, nullptr, M.psi, nch, N, kb, M.U64, nullptr, M.G64u,
-                                        (cxd *)M.sbuf);
 }
 
 // MAXT: the launch bound (512: 128 registers per thread, some spilled; 256: room for all of
@@ -785,11 +793,14 @@ int pm_member_tables(PmMember &M, std::vector<void *> &allocs)
     PG_CUDA_TRY(cudaMemcpy(U.data(), M.U64, U.size() * sizeof(double), cudaMemcpyDeviceToHost));
     PG_TRY(pm_upload<float>(pm_chunk_tables(U, M.N, M.kb, 32, false), &M.G32u, allocs));
     PG_TRY(pm_upload<float>(pm_chunk_tables(U, M.N, M.kb, 32, true), &M.G32l, allocs));
-    PG_TRY(pm_upload<double>(pm_chunk_tables(U, M.N, M.kb, 8, false), &M.G64u, allocs));
     void *sb = nullptr;
-    PG_CUDA_TRY(cudaMalloc(&sb, sizeof(cxd) * (size_t)M.nch * ((M.N + 7) / 8) * M.kb + 16));
+    PG_CUDA_TRY(cudaMalloc(&sb, sizeof(cxf) * (size_t)M.nch * ((M.N + 31) / 32) * M.kb + 16));
     allocs.push_back(sb);
     M.sbuf = sb;
+    void *tb = nullptr;
+    PG_CUDA_TRY(cudaMalloc(&tb, sizeof(cxf) * (size_t)M.m * M.n + 16));
+    allocs.push_back(tb);
+    M.T = (cxf *)tb;
     return PG_OK;
 }
 

@@ -3,7 +3,7 @@
 // sorted by size, largest first) and runs a member's whole step by itself: psi <- U psi, the
 // m Arnoldi steps on U^-H H(t) U^-1 (complex64 basis, classical Gram-Schmidt with a second
 // pass through the Gram matrix, FP64 CTA sums), the m x m exponential (pamp_expm_block) and
-// psi = ||psi|| U^-1 V c -
+// psi = ||psi|| U^-1 V c (as the combination of the U^-1 V[j] the Arnoldi steps computed) -
 // the same algorithm, layout and Hessenberg columns as the graph of per-member kernels in
 // krylov.cu, with no wait between CTAs. krylov.cu fills one PmMember per member from its
 // pg_pamp; pamp_persistent.cu holds the kernel, its launcher and the autotuned shape.
@@ -18,7 +18,8 @@ struct PmMember {
     const float *bands = nullptr;             // real FP32 bands [nbands][2kb+1][ld]
     const float *U32 = nullptr;               // overlap Cholesky factor U(i, i+d) at [i][d], FP32
     const double *U64 = nullptr;              // the same in FP64
-    cxf *V = nullptr, *w = nullptr, *t = nullptr;  // basis [m][n]; two scratch vectors [n]
+    cxf *V = nullptr, *w = nullptr;           // basis [m][n]; scratch [n]
+    cxf *T = nullptr;                         // t_j = U^-1 V[j] of every Arnoldi step [m][n]
     cxd *psi = nullptr;                       // the member's wavefunction (complex128)
     const cxd *scales = nullptr;              // its slot values [PG_MAX_SLOTS]
     double *cols = nullptr;                   // Hessenberg columns [m][3][2(m+2)] (ArnoldiBuf layout)
@@ -30,7 +31,6 @@ struct PmMember {
     const float *basis = nullptr;
     const float *ent_coef = nullptr;
     const float *G32u = nullptr, *G32l = nullptr;  // chunk responses of the FP32 solves (32-row chunks)
-    const double *G64u = nullptr;             // of the FP64 solve (16-row chunks)
     void *sbuf = nullptr;                     // coupling values of the chunks [nch][chunks][kb]
     PampExpArgs ex;                           // the exponential's arguments (cols, norm, c, stats)
 };
