@@ -31,8 +31,8 @@ constexpr int PM_WARPS = 16;    // at most 512 threads per CTA
 constexpr int PM_MAXBASIS = 4;  // basis bands of an operator staged in shared memory
 
 struct PmLayout {
-    size_t us = 0, uinv = 0, gu = 0, gl = 0, rp = 0, ent = 0, bas = 0, red = 0, h = 0, gram = 0, scal = 0, cc = 0,
-           ex = 0;
+    size_t us = 0, uinv = 0, gu = 0, gl = 0, zb = 0, rp = 0, ent = 0, bas = 0, red = 0, h = 0, gram = 0, scal = 0,
+           cc = 0, ex = 0;
     size_t bytes = 0;
 };
 
@@ -50,6 +50,7 @@ __host__ __device__ inline PmLayout pm_layout(int Nmax, int kbmax, int mmax, int
     L.uinv = o; o = pm_align16(o + sizeof(float) * (size_t)Nmax);
     L.gu = o;   o = pm_align16(o + sizeof(float) * nck * 32 * kbmax);
     L.gl = o;   o = pm_align16(o + sizeof(float) * nck * 32 * kbmax);
+    L.zb = o;   o = pm_align16(o + sizeof(cxf) * (size_t)nchmax * nck * kbmax);
     L.rp = o;   o = pm_align16(o + sizeof(int) * (size_t)(nchmax + 1));
     L.ent = o;  o = pm_align16(o + sizeof(int4) * (size_t)entmax);
     // the basis bands are read in the Arnoldi steps only; the exponential's scratch, used after
@@ -135,27 +136,23 @@ __device__ __forceinline__ double pm_sum1(double v, double *red, double *slot)
 // U x = b, the last kb rows of chunk c-1 for U^T x = b),
 //     x_c = z_c + G_c s,
 // and the coupling values s follow from a kb-wide recurrence over the chunks of each fibre.
-// Phase 1 (one thread per (fibre, chunk), the chunk in registers), phase 2 (one thread per
-// fibre), phase 3 (one thread per (fibre, chunk)), a CTA barrier after each. U(i, i+d) at
-// U[i (kb+1) + d]; Uinv (optional) holds 1 / U(i, i); sbuf: [nch][nchunks][kb] scratch.
-template <typename R> struct PmUT;
-template <> struct PmUT<float> { typedef float T; };
-template <> struct PmUT<double> { typedef double T; };
-
+// Phase 1 (one thread per (fibre, chunk), the chunk in registers) writes z_c to x and its kb
+// boundary values to shared memory (sb: [nch][nchunks][kb]); phase 2 (one thread per fibre)
+// turns them into the coupling values in place; phase 3 (one thread per (fibre, chunk)) adds
+// G_c s to x. A CTA barrier after each phase. (Keeping the chunk in registers from phase 1 to
+// phase 3 spills them.) U(i, i+d) at U[i (kb+1) + d]; Uinv holds 1 / U(i, i).
 template <int KB, int CH, bool LOWER, typename R>
-__device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x,
-                             int nch, int N, int kb_rt, const R *__restrict__ U, const R *__restrict__ Uinv,
-                             const R *__restrict__ G, cx<R> *__restrict__ sbuf)
+__device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x, int nch, int N, int kb_rt,
+                             const R *__restrict__ U, const R *__restrict__ Uinv, const R *__restrict__ G, cx<R> *sb)
 {
-    constexpr int KBC = KB > 0 ? KB : 1;
     const int kb = KB > 0 ? KB : kb_rt, kw = kb + 1;
     const int nck = (N + CH - 1) / CH, ntask = nch * nck, tid = threadIdx.x, T = blockDim.x;
     const R scr = (R)sc;  // the scale in the vector's precision (FP64 arithmetic is slow here)
-    // phase 1: z_c
+    // phase 1: z_c and its boundary values
     for (int task = tid; task < ntask; task += T) {
+        cx<R> z[CH];
         const int a = task / nck, c = task - a * nck, r0 = c * CH, len = min(CH, N - r0);
         const cx<R> *bb = b + (size_t)a * N + r0;
-        cx<R> z[CH];
 #pragma unroll
         for (int r = 0; r < CH; ++r) {
             z[r] = mk<R>((R)0, (R)0);
@@ -185,7 +182,7 @@ __device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x,
                             acc.y -= u * z[r - d].y;
                         }
                     }
-                    const R inv = Uinv ? Uinv[r0 + r] : (R)1 / U[(size_t)(r0 + r) * kw];
+                    const R inv = Uinv[r0 + r];
                     z[r] = mk<R>(acc.x * inv, acc.y * inv);
                 }
             }
@@ -209,8 +206,27 @@ __device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x,
                             acc.y -= u * z[r + d].y;
                         }
                     }
-                    const R inv = Uinv ? Uinv[r0 + r] : (R)1 / U[(size_t)(r0 + r) * kw];
+                    const R inv = Uinv[r0 + r];
                     z[r] = mk<R>(acc.x * inv, acc.y * inv);
+                }
+            }
+        }
+        cx<R> *zb = sb + ((size_t)a * nck + c) * kb;
+        if constexpr (KB > 0) {
+#pragma unroll
+            for (int q = 0; q < KB; ++q) {
+                if (LOWER) {
+                    if (c + 1 < nck) zb[q] = z[CH - KB + q];  // chunks before the last are full
+                } else {
+                    zb[q] = z[q];  // zero past the fibre's end
+                }
+            }
+        } else {
+            for (int q = 0; q < kb; ++q) {
+                if (LOWER) {
+                    if (c + 1 < nck) zb[q] = z[CH - kb + q];
+                } else {
+                    zb[q] = z[q];
                 }
             }
         }
@@ -220,18 +236,15 @@ __device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x,
             if (r < len) xx[r] = z[r];
     }
     __syncthreads();
-    // phase 2: the coupling values of every chunk, in chunk order
+    // phase 2: the coupling values of every chunk, in chunk order, in place of its boundary values
     for (int a = tid; a < nch; a += T) {
-        const cx<R> *xa = x + (size_t)a * N;
-        cx<R> *sa = sbuf + (size_t)a * nck * kb;
+        cx<R> *sa = sb + (size_t)a * nck * kb;
         cx<R> s[KB > 0 ? KB : 16];
+        cx<R> sn[KB > 0 ? KB : 16];
         if constexpr (LOWER) {
-            // s_c = last kb rows of chunk c (c < nck - 1, full chunks)
-            for (int c = 0; c + 1 < nck; ++c) {
-                const int rt = c * CH + CH - kb;
-                cx<R> sn[KB > 0 ? KB : 16];
+            for (int c = 0; c + 1 < nck; ++c) {  // s_c = the last kb rows of chunk c
                 for (int q = 0; q < kb; ++q) {
-                    cx<R> v = xa[rt + q];
+                    cx<R> v = sa[(size_t)c * kb + q];
                     if (c > 0) {
                         const R *g = G + ((size_t)c * CH + (CH - kb + q)) * kb;
                         for (int p = 0; p < kb; ++p) {
@@ -247,12 +260,9 @@ __device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x,
                 }
             }
         } else {
-            // s_c = first kb rows of chunk c (c >= 1), from the last chunk down
-            for (int c = nck - 1; c >= 1; --c) {
-                const int r0 = c * CH;
-                cx<R> sn[KB > 0 ? KB : 16];
+            for (int c = nck - 1; c >= 1; --c) {  // s_c = the first kb rows of chunk c
                 for (int q = 0; q < kb; ++q) {
-                    cx<R> v = (r0 + q < N) ? xa[r0 + q] : mk<R>((R)0, (R)0);
+                    cx<R> v = sa[(size_t)c * kb + q];
                     if (c + 1 < nck) {
                         const R *g = G + ((size_t)c * CH + q) * kb;
                         for (int p = 0; p < kb; ++p) {
@@ -268,27 +278,28 @@ __device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x,
                 }
             }
         }
-        (void)KBC;
     }
     __syncthreads();
     // phase 3: x_c = z_c + G_c s (the neighbouring chunk's coupling values)
-    for (int task = tid; task < ntask; task += T) {
-        const int a = task / nck, c = task - a * nck, r0 = c * CH, len = min(CH, N - r0);
-        const int cs = LOWER ? c - 1 : c + 1;
-        if (cs < 0 || cs >= nck) continue;
-        const cx<R> *sv = sbuf + ((size_t)a * nck + cs) * kb;
-        cx<R> s[KB > 0 ? KB : 16];
-        for (int q = 0; q < kb; ++q) s[q] = sv[q];
-        cx<R> *xx = x + (size_t)a * N + r0;
-        const R *g = G + (size_t)c * CH * kb;
-        for (int r = 0; r < len; ++r) {
-            cx<R> v = xx[r];
-            for (int q = 0; q < kb; ++q) {
-                const R gq = g[(size_t)r * kb + q];
-                v.x += gq * s[q].x;
-                v.y += gq * s[q].y;
+    {
+        for (int task = tid; task < ntask; task += T) {
+            const int a = task / nck, c = task - a * nck, r0 = c * CH, len = min(CH, N - r0);
+            const int cs = LOWER ? c - 1 : c + 1;
+            if (cs < 0 || cs >= nck) continue;
+            const cx<R> *sv = sb + ((size_t)a * nck + cs) * kb;
+            cx<R> s[KB > 0 ? KB : 16];
+            for (int q = 0; q < kb; ++q) s[q] = sv[q];
+            cx<R> *xx = x + (size_t)a * N + r0;
+            const R *g = G + (size_t)c * CH * kb;
+            for (int r = 0; r < len; ++r) {
+                cx<R> v = xx[r];
+                for (int q = 0; q < kb; ++q) {
+                    const R gq = g[(size_t)r * kb + q];
+                    v.x += gq * s[q].x;
+                    v.y += gq * s[q].y;
+                }
+                xx[r] = v;
             }
-            xx[r] = v;
         }
     }
     __syncthreads();
@@ -331,6 +342,7 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
     float *Uinv = reinterpret_cast<float *>(smem + L.uinv);
     float *Gu = reinterpret_cast<float *>(smem + L.gu);
     float *Gl = reinterpret_cast<float *>(smem + L.gl);
+    cxf *zb = reinterpret_cast<cxf *>(smem + L.zb);  // the solves' chunk boundary values
     int *rp = reinterpret_cast<int *>(smem + L.rp);
     int4 *ent = reinterpret_cast<int4 *>(smem + L.ent);
     double *red = reinterpret_cast<double *>(smem + L.red);
@@ -386,7 +398,7 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
         }
     }
     __syncthreads();
-    pm_solve_cta<KB, 32, false, float>(V, 1.0, nullptr, Tb, nch, N, kb, Us, Uinv, Gu, (cxf *)M.sbuf);
+    pm_solve_cta<KB, 32, false, float>(V, 1.0, nullptr, Tb, nch, N, kb, Us, Uinv, Gu, zb);
 
     for (int j = 0; j < m; ++j) {
         const cxf *__restrict__ t = Tb + (size_t)j * n;
@@ -443,7 +455,7 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
             w[e] = acc;
         }
         __syncthreads();
-        pm_solve_cta<KB, 32, true, float>(w, 1.0, nullptr, w, nch, N, kb, Us, Uinv, Gl, (cxf *)M.sbuf);
+        pm_solve_cta<KB, 32, true, float>(w, 1.0, nullptr, w, nch, N, kb, Us, Uinv, Gl, zb);
         // Gram-Schmidt, first pass: h1 = V^H w and the new Gram column V^H V[j] (one read of V)
         {
             cxf acc[PM_MAXM], gacc[PM_MAXM];
@@ -515,7 +527,7 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
             if (dst) {
                 const double s = beta > 0.0 ? 1.0 / beta : 0.0;
                 pm_solve_cta<KB, 32, false, float>(dst, s, dst, Tb + (size_t)J * n, nch, N, kb, Us, Uinv, Gu,
-                                                   (cxf *)M.sbuf);
+                                                   zb);
             }
         }
     }
@@ -793,10 +805,6 @@ int pm_member_tables(PmMember &M, std::vector<void *> &allocs)
     PG_CUDA_TRY(cudaMemcpy(U.data(), M.U64, U.size() * sizeof(double), cudaMemcpyDeviceToHost));
     PG_TRY(pm_upload<float>(pm_chunk_tables(U, M.N, M.kb, 32, false), &M.G32u, allocs));
     PG_TRY(pm_upload<float>(pm_chunk_tables(U, M.N, M.kb, 32, true), &M.G32l, allocs));
-    void *sb = nullptr;
-    PG_CUDA_TRY(cudaMalloc(&sb, sizeof(cxf) * (size_t)M.nch * ((M.N + 31) / 32) * M.kb + 16));
-    allocs.push_back(sb);
-    M.sbuf = sb;
     void *tb = nullptr;
     PG_CUDA_TRY(cudaMalloc(&tb, sizeof(cxf) * (size_t)M.m * M.n + 16));
     allocs.push_back(tb);

@@ -31,7 +31,6 @@ struct PmMember {
     const float *basis = nullptr;
     const float *ent_coef = nullptr;
     const float *G32u = nullptr, *G32l = nullptr;  // chunk responses of the FP32 solves (32-row chunks)
-    void *sbuf = nullptr;                     // coupling values of the chunks [nch][chunks][kb]
     PampExpArgs ex;                           // the exponential's arguments (cols, norm, c, stats)
 };
 
