@@ -28,11 +28,15 @@ static const int GT_LDA = GT_K + 8, GT_LDB = GT_N + 8, GT_LDC = GT_N + 4;
 enum { EPI_F32 = 0, EPI_RELU = 1, EPI_MASK = 2 };
 
 // C[M][N] = op(A)[M][K] op(B)[K][N]; A(i,k) = ta ? A[k*lda+i] : A[i*lda+k],
-// B(k,j) = tb ? B[j*ldb+k] : B[k*ldb+j].
+// B(k,j) = tb ? B[j*ldb+k] : B[k*ldb+j]. With Cacc (FP32 [M][N], zeroed before) the K range is
+// split over gridDim.z: each slice adds its partial product with atomics and the epilogue runs
+// in mlp_epilogue_kernel (products with few output tiles and a long K, such as the first
+// layer's 38400-wide input, would otherwise occupy a handful of SMs).
 template <int EPI>
 __global__ void __launch_bounds__(128) mlp_gemm_kernel(int M, int N, int K, const bf16 *__restrict__ A, int lda, int ta,
                                                        const bf16 *__restrict__ B, int ldb, int tb, float *C, int ldc,
-                                                       bf16 *Cb, int ldcb, const bf16 *__restrict__ mask, int ldm)
+                                                       bf16 *Cb, int ldcb, const bf16 *__restrict__ mask, int ldm,
+                                                       float *Cacc)
 {
     __shared__ __align__(32) bf16 As[GT_M * GT_LDA];
     __shared__ __align__(32) bf16 Bs[GT_K * GT_LDB];
@@ -46,19 +50,21 @@ __global__ void __launch_bounds__(128) mlp_gemm_kernel(int M, int N, int K, cons
 #pragma unroll
         for (int b = 0; b < 2; ++b) wmma::fill_fragment(acc[a][b], 0.0f);
     const bf16 zero = __float2bfloat16(0.0f);
-    for (int k0 = 0; k0 < K; k0 += GT_K) {
+    const int kper = ((K + (int)gridDim.z - 1) / (int)gridDim.z + GT_K - 1) / GT_K * GT_K;
+    const int kbeg = (int)blockIdx.z * kper, kend = min(K, kbeg + kper);
+    for (int k0 = kbeg; k0 < kend; k0 += GT_K) {
         for (int e = threadIdx.x; e < GT_M * GT_K; e += 128) {
             const int i = e / GT_K, k = e % GT_K;
             const int gi = m0 + i, gk = k0 + k;
             bf16 v = zero;
-            if (gi < M && gk < K) v = ta ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk];
+            if (gi < M && gk < kend) v = ta ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk];
             As[i * GT_LDA + k] = v;
         }
         for (int e = threadIdx.x; e < GT_K * GT_N; e += 128) {
             const int k = e / GT_N, j = e % GT_N;
             const int gk = k0 + k, gj = n0 + j;
             bf16 v = zero;
-            if (gk < K && gj < N) v = tb ? B[(size_t)gj * ldb + gk] : B[(size_t)gk * ldb + gj];
+            if (gk < kend && gj < N) v = tb ? B[(size_t)gj * ldb + gk] : B[(size_t)gk * ldb + gj];
             Bs[k * GT_LDB + j] = v;
         }
         __syncthreads();
@@ -88,6 +94,26 @@ __global__ void __launch_bounds__(128) mlp_gemm_kernel(int M, int N, int K, cons
         const int gi = m0 + i, gj = n0 + j;
         if (gi >= M || gj >= N) continue;
         float v = Cs[i * GT_LDC + j];
+        if (Cacc) {
+            atomicAdd(Cacc + (size_t)gi * N + gj, v);
+            continue;
+        }
+        if (EPI == EPI_RELU) v = fmaxf(v, 0.0f);
+        if (EPI == EPI_MASK && !(__bfloat162float(mask[(size_t)gi * ldm + gj]) > 0.0f)) v = 0.0f;
+        if (C) C[(size_t)gi * ldc + gj] = v;
+        if (EPI != EPI_F32) Cb[(size_t)gi * ldcb + gj] = __float2bfloat16(v);
+    }
+}
+
+// the epilogue of a K-split product on its summed FP32 result
+template <int EPI>
+__global__ void mlp_epilogue_kernel(int M, int N, const float *__restrict__ Cacc, float *C, int ldc, bf16 *Cb, int ldcb,
+                                    const bf16 *__restrict__ mask, int ldm)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)M * N;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int gi = (int)(e / N), gj = (int)(e - (long long)gi * N);
+        float v = Cacc[e];
         if (EPI == EPI_RELU) v = fmaxf(v, 0.0f);
         if (EPI == EPI_MASK && !(__bfloat162float(mask[(size_t)gi * ldm + gj]) > 0.0f)) v = 0.0f;
         if (C) C[(size_t)gi * ldc + gj] = v;
@@ -191,6 +217,7 @@ struct pg_mlp {
     int cap = 0;  // batch capacity of the activation buffers
     bf16 *h1 = nullptr, *h2 = nullptr, *dY = nullptr, *dh1 = nullptr, *dh2 = nullptr;
     float *y = nullptr;
+    float *acc = nullptr;  // [cap][h] FP32 sums of K-split products
     double *d_loss = nullptr, *h_loss = nullptr;
     long long n(int l) const { return (long long)rows[l] * cols[l]; }
 };
@@ -203,7 +230,25 @@ static int gemm(pg_mlp *m, int M, int N, int K, const bf16 *A, int lda, int ta, 
 {
     if (M <= 0 || N <= 0) return PG_OK;
     dim3 grid((N + GT_N - 1) / GT_N, (M + GT_M - 1) / GT_M);
-    mlp_gemm_kernel<EPI><<<grid, 128, 0, m->ctx->stream>>>(M, N, K, A, lda, ta, B, ldb, tb, C, ldc, Cb, ldcb, mask, ldm);
+    const int sms = std::max(1, m->ctx->num_sms);
+    const long long tiles = (long long)grid.x * grid.y;
+    int split = 1;
+    if (tiles < sms && K >= 16 * GT_K && (long long)M * N <= (long long)m->cap * m->h && m->acc)
+        split = (int)std::min<long long>((2LL * sms + tiles - 1) / tiles, K / (8 * GT_K));
+    if (split > 1) {
+        grid.z = split;
+        PG_CUDA_TRY(cudaMemsetAsync(m->acc, 0, sizeof(float) * (size_t)M * N, m->ctx->stream));
+        mlp_gemm_kernel<EPI><<<grid, 128, 0, m->ctx->stream>>>(M, N, K, A, lda, ta, B, ldb, tb, C, ldc, Cb, ldcb, mask,
+                                                               ldm, m->acc);
+        m->ctx->launches++;
+        PG_TRY(pg_check_launch(m->ctx));
+        mlp_epilogue_kernel<EPI><<<grid_for((long long)M * N), 256, 0, m->ctx->stream>>>(M, N, m->acc, C, ldc, Cb, ldcb,
+                                                                                        mask, ldm);
+        m->ctx->launches++;
+        return pg_check_launch(m->ctx);
+    }
+    mlp_gemm_kernel<EPI><<<grid, 128, 0, m->ctx->stream>>>(M, N, K, A, lda, ta, B, ldb, tb, C, ldc, Cb, ldcb, mask, ldm,
+                                                           nullptr);
     m->ctx->launches++;
     return pg_check_launch(m->ctx);
 }
@@ -212,8 +257,9 @@ static int ensure_cap(pg_mlp *m, int batch)
 {
     if (batch <= m->cap) return PG_OK;
     cudaFree(m->h1); cudaFree(m->h2); cudaFree(m->dY); cudaFree(m->dh1); cudaFree(m->dh2); cudaFree(m->y);
+    cudaFree(m->acc);
     m->h1 = m->h2 = m->dY = m->dh1 = m->dh2 = nullptr;
-    m->y = nullptr;
+    m->y = m->acc = nullptr;
     const size_t b = (size_t)batch;
     PG_CUDA_TRY(cudaMalloc(&m->h1, b * m->h * sizeof(bf16)));
     PG_CUDA_TRY(cudaMalloc(&m->h2, b * m->h * sizeof(bf16)));
@@ -221,6 +267,7 @@ static int ensure_cap(pg_mlp *m, int batch)
     PG_CUDA_TRY(cudaMalloc(&m->dh2, b * m->h * sizeof(bf16)));
     PG_CUDA_TRY(cudaMalloc(&m->dY, b * m->d_out * sizeof(bf16)));
     PG_CUDA_TRY(cudaMalloc(&m->y, b * m->d_out * sizeof(float)));
+    PG_CUDA_TRY(cudaMalloc(&m->acc, b * m->h * sizeof(float)));
     m->cap = batch;
     return PG_OK;
 }
@@ -304,6 +351,7 @@ extern "C" int pg_mlp_destroy(pg_mlp *m)
         cudaFree(m->W[l]); cudaFree(m->G[l]); cudaFree(m->M1[l]); cudaFree(m->M2[l]); cudaFree(m->Wb[l]);
     }
     cudaFree(m->h1); cudaFree(m->h2); cudaFree(m->dY); cudaFree(m->dh1); cudaFree(m->dh2); cudaFree(m->y);
+    cudaFree(m->acc);
     cudaFree(m->d_loss);
     if (m->h_loss) cudaFreeHost(m->h_loss);
     delete m;
