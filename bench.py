@@ -579,6 +579,7 @@ def run_ours(args):
     ens = run_ensemble(args, torch, flush) if args.ensemble > 0 else None
     ens_pamp = run_pamp_ensemble(args, torch, flush) if args.ensemble > 0 else None
     two_e_large = time_two_electron_large(torch) if (args.two_electron_large and rank == 0) else None
+    learned = time_learned_helium(torch) if (args.learned and rank == 0) else None
     cpu = cpu_baseline_sample(nsteps=args.cpu_steps) if (rank == 0 and world == 1 and args.cpu_steps > 0) else None
     if rank == 0:
         steps_per_s = world * args.steps / t_mixed
@@ -653,6 +654,7 @@ def run_ours(args):
                 "info": two_e[2]},
             "two_electron_cayley": two_e_steps,
             "two_electron_large": two_e_large,
+            "learned_helium": learned,
             "cpu_baseline": cpu,
             "ensemble": ens,
             "ensemble_pamp": ens_pamp,
@@ -968,6 +970,53 @@ def time_two_electron_large(torch, steps=2):
             "parity": "oracle comparison at reduced size with the same code path: tests/test_gpu_helium.py"}
 
 
+def time_learned_helium(torch):
+    """The learned preconditioner at the helium model of TWO_ELECTRON (coupled L <= 5, l1, l2
+    <= 10, 80 B-splines per electron: 291 angular blocks of 6400 coefficients), field free, on
+    top of the fast-diagonalization block preconditioner; the network learns the part of the
+    correction the blocks miss (the electron-electron repulsion). 172 harvested steps give
+    50 052 (residual, correction) block pairs (85% train, 15% held out); 3000 Adam steps on
+    the GPU; then 20 Cayley steps with and without the network from the same state."""
+    import pyprop_gb300 as pp
+    from pyprop_gb300.learned import LearnedPreconditioner
+    from pyprop_gb300.workloads import helium
+    prob = pp.Problem(pp.LoadString(helium(propagator="CayleyPropagatorGPU", precision="fp32", amplitude=0.0,
+                                           timestep=0.01, duration=20.0, gmres_tolerance=1e-10, **TWO_ELECTRON)))
+    prob.SetupStep(skipWavefunctionSetup=True)
+    shape = prob.psi.GetRepresentation().GetFullShape()
+    rng = np.random.default_rng(1)
+    decay = np.exp(-0.1 * np.arange(shape[1]))
+    psi0 = np.zeros(shape, complex)
+    psi0[0] = rng.standard_normal(shape[1:]) * decay[:, None] * decay[None, :]
+    psi0 /= np.linalg.norm(psi0)
+    prob.psi.GetData().copy_(torch.as_tensor(psi0, device="cuda"))
+    prob.PropagatedTime = 1.0
+    pots = prob.Propagator.BasePropagator.PotentialList
+    rep = [k for k, pot in enumerate(pots) if "ElectronicCoupling" in getattr(pot, "Name", "")][0]
+    lp = LearnedPreconditioner(prob.Propagator, hidden=256, coupling_potential=rep)
+    t0 = time.perf_counter()
+    lp.harvest(prob, 172)
+    ntr = int(0.85 * len(lp.pairs))
+    X, T = lp.training_set(lp.pairs[:ntr])
+    t1 = time.perf_counter()
+    losses = lp.train(X, T, steps=3000, lr=3e-4, batch=1024)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t1
+    rows = int(X.shape[0])
+    del X, T
+    held = lp.pairs[ntr:]
+    out = {"workload": "helium-like, coupled L<=5, l1,l2<=10, 80 B-splines per electron (291 blocks of 6400), "
+                       "field free, fast-diagonalization blocks + learned correction of the repulsion",
+           "network": "%d -> 256 -> 256 -> %d, %d parameters (BF16 weights, FP32 accumulate)" %
+                      (lp.d_in, lp.d_out, lp.net.parameter_count()),
+           "pairs": len(lp.pairs) * shape[0], "training_rows": rows, "train_s": t_train,
+           "harvest_s": t1 - t0, "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
+           "held_out_one_step_residual": {"block": lp.one_step_residual(held, learned=False),
+                                          "learned": lp.one_step_residual(held, learned=True)}}
+    out.update(lp.compare_steps(prob, 20))
+    return out
+
+
 def profile_ensemble_pamp():
     """Profiling entry point: the 256-member pAMP ensemble on the persistent kernel (forced),
     its autotuning launches at the first step, then three steps."""
@@ -1076,6 +1125,8 @@ def main():
                          "2 the cluster variant")
     ap.add_argument("--two-electron-large", type=int, default=1,
                     help="end-to-end leg of the largest two-electron model (0 = skip)")
+    ap.add_argument("--learned", type=int, default=1,
+                    help="learned-preconditioner leg at the L<=5, l<=10, 80-spline helium model (0 = skip)")
     ap.add_argument("--eager", action="store_true",
                     help="host-driven GMRES loops (same kernels, visible one by one to a profiler)")
     ap.add_argument("--ensemble", type=int, default=256, help="members of the batched leg (0 = skip)")

@@ -223,3 +223,41 @@ class LearnedPreconditioner:
     def attach(self, on=True):
         """Use (or stop using) the network inside the propagator's Cayley steps."""
         self.prop.stepper.set_learned(self.net if on else None, self.slot)
+
+    def compare_steps(self, prob, nsteps):
+        """nsteps Cayley steps from prob's current state without and with the network (each
+        after one untimed step from the same state, which the timed run restarts from):
+        {"block": ..., "learned": ...} with the GMRES iterations, the device time in ms, the
+        largest FP64 true residual and the passes the judge rejected, and "relerr" between
+        the two final states. prob ends in the learned run's final state, network detached."""
+        import torch
+        start = prob.psi.GetData().clone()
+        t0 = prob.PropagatedTime
+        out, psis = {}, {}
+        for on in (False, True):
+            self.attach(on)
+            rej0 = self.prop.stepper.learned_rejected() if on else 0
+            for timed in (False, True):
+                prob.psi.GetData().copy_(start)
+                prob.PropagatedTime = t0
+                if not timed:
+                    prob.AdvanceStep()
+                    continue
+                torch.cuda.synchronize()
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                it, res = 0, 0.0
+                s.record()
+                for _ in range(nsteps):
+                    prob.AdvanceStep()
+                    st = self.prop.LastStats
+                    it += st.Iterations
+                    res = max(res, st.TrueResidual)
+                e.record()
+                e.synchronize()
+                out["learned" if on else "block"] = {
+                    "gmres_iterations": int(it), "ms": s.elapsed_time(e), "max_true_residual": res,
+                    "rejected_passes": (self.prop.stepper.learned_rejected() - rej0) if on else 0}
+                psis[on] = prob.psi.GetData().clone()
+        self.attach(False)
+        out["relerr"] = float(torch.linalg.vector_norm(psis[True] - psis[False]) / torch.linalg.vector_norm(psis[False]))
+        return out

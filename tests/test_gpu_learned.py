@@ -187,3 +187,20 @@ def test_learned_preconditioner_on_the_two_electron_model(gpu):
     # conditioning of S x S + i dt/2 H
     assert relerr(out[True], out[False]) < 1e-7
     assert iters[True] <= iters[False]
+
+
+def test_learned_at_helium_l10_80_splines(gpu):
+    """The learned preconditioner at the size it is specified on: helium, coupled L <= 5,
+    l1, l2 <= 10, 80 B-splines per electron (291 angular blocks of 6400 coefficients), on top
+    of the fast-diagonalization blocks, learning the repulsion they omit from 50 052 harvested
+    block pairs. The network trains on the GPU (the loss falls), the flexible steps with it
+    meet the same true-residual tolerance, agree with the block-preconditioned steps to the
+    GMRES tolerance, and need no more GMRES iterations."""
+    import torch
+    import bench
+    out = bench.time_learned_helium(torch)
+    assert out["pairs"] == 50052 and out["training_rows"] > 40000
+    assert out["loss_last"] < out["loss_first"]
+    assert out["block"]["max_true_residual"] < 1e-10 and out["learned"]["max_true_residual"] < 1e-10
+    assert out["relerr"] < 1e-6
+    assert out["learned"]["gmres_iterations"] <= out["block"]["gmres_iterations"]
