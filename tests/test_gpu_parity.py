@@ -106,13 +106,15 @@ def test_pamp_l10_ground_state_by_piram_matches_fixture(gpu):
     assert infidelity(g["psi0"], prob.psi.numpy(), _overlap(prob)) < 1e-14
 
 
-def test_ensemble_members_against_reference(gpu):
+@pytest.mark.parametrize("pamp_step", ["persistent", "graph"])
+def test_ensemble_members_against_reference(gpu, pamp_step):
     """Members of the 256-member ensemble (lmax, B-splines, field and wavelength drawn with
     seed 20261203): four as a batched mixed-precision Crank-Nicolson ensemble over the whole
-    1000-step pulse, and eight as a batched pAMP ensemble (basis 20, complex64 with FP64 sums)
-    over the first steps (the basis is not converged for these stiff members, so longer pAMP
-    runs are rounding-sensitive in any implementation): each final state against the
-    reference templates' run of that member."""
+    1000-step pulse, and eight as a batched pAMP ensemble (basis 20, complex64 with FP64 sums;
+    the persistent kernel or the graph of the members' kernels, forced) over the first steps
+    (the basis is not converged for these stiff members, so longer pAMP runs are
+    rounding-sensitive in any implementation): each final state against the reference
+    templates' run of that member."""
     from pyprop_gb300.ensemble import CayleyEnsembleGPU, PamEnsembleGPU, hydrogen_ensemble_params
     from pyprop_gb300.workloads import ENSEMBLE_MEMBER
     g = _fixture("run_members.npz")
@@ -126,8 +128,13 @@ def test_ensemble_members_against_reference(gpu):
             p.psi.SetData(g["pamp%d_psi0" % i])
             p.PropagatedTime = 0.0
         ens = cls(probs)
+        if kind == "pamp":
+            ens.set_persistent(pamp_step == "persistent")
+            assert ens.launch_shape()["persistent"] == (pamp_step == "persistent") or pamp_step == "persistent"
         for _ in range(nsteps):
             ens.AdvanceStep()
+        if kind == "pamp":
+            assert ens.launch_shape()["persistent"] == (pamp_step == "persistent")
         for p, i in zip(probs, members):
             ref = g["%s%d_psi" % (kind, i)]
             assert infidelity(ref, p.psi.numpy(), _overlap(p)) < tol, (kind, int(i))
