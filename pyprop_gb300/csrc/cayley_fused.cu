@@ -86,7 +86,8 @@ struct FzArgs {
     cxf *wbuf;       // [2][nch*N] unnormalised next Krylov vector (read across channels)
     cxf *V;          // [m][nch*N] Krylov vectors (channel a written by CTA a only)
     double *part;    // [P_COUNT][CTAs][FZ_PSTRIDE] per-CTA partial sums
-    FzBarrier *bar;
+    FzBarrier *bar;      // this launch's arrival counter (launches alternate between two)
+    FzBarrier *bar_next; // the other one, cleared by this launch for the next
     GmresState *st;
     int *err;
 };
@@ -529,6 +530,8 @@ template <int KB>
 __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
 {
     if (fz_bad_launch(a, gridDim.x != (unsigned)a.nctas || gridDim.y != 1 || gridDim.z != 1)) return;
+    // the previous launch, which used bar_next, has completed: clear it for the next launch
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.bar_next->count = 0;
     extern __shared__ __align__(16) unsigned char fz_smem[];
     __shared__ cxd sc_diff[PG_MAX_SLOTS], sc_negplus[PG_MAX_SLOTS];
     __shared__ cxf sc_plus[PG_MAX_SLOTS];
@@ -744,8 +747,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_fused_step_kernel(FzArgs a)
     // the step's statistics and the error word to the host (mapped memory): the last action
     if (lead && a.hstats) {
         *a.hstats = a.st->stats;
-        *(volatile int *)a.herr = *(volatile int *)a.err;
-        __threadfence_system();
+        *(volatile int *)a.herr = *(volatile int *)a.err;  // read by the host after it synchronises
     }
 }
 
@@ -1032,6 +1034,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_cluster_step_kernel(FzArgs 
     if (fz_bad_launch(a, cluster.num_blocks() != CL_SIZE || gridDim.x != (unsigned)a.nctas || gridDim.y != 1 ||
                              gridDim.z != 1))
         return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.bar_next->count = 0;  // as in cay_fused_step_kernel
     const int cl = blockIdx.x / CL_SIZE;            // cluster: angular channel (when < nch)
     const int cr = (int)cluster.block_rank();       // this CTA's part of the channel
     const bool owner = cl < a.nch;
@@ -1318,8 +1321,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) cay_cluster_step_kernel(FzArgs 
     }
     if (lead && a.hstats) {
         *a.hstats = a.st->stats;
-        *(volatile int *)a.herr = *(volatile int *)a.err;
-        __threadfence_system();
+        *(volatile int *)a.herr = *(volatile int *)a.err;  // read by the host after it synchronises
     }
     cluster.sync();  // no CTA leaves while a peer could still read its shared memory
 }
@@ -1336,6 +1338,7 @@ struct FusedCayley {
     // the cluster variant (three CTAs per channel), when the operator's shape qualifies
     bool cluster_ok = false;
     bool use_cluster = false;
+    int parity = 0;     // which of the two arrival counters the next launch uses
     int coop = -1;      // cooperative launch with clusters: -1 untried, 1 works, 0 refused by the driver
     size_t csmem = 0;
     int cnctas = 0;
@@ -1528,7 +1531,8 @@ int pg_cayley_fused_prepare(pg_op *op64, pg_op *opb, pg_banded *precb, int m, Fu
     alloc((void **)&a.wbuf, sizeof(cxf) * 2 * n);
     alloc((void **)&a.V, sizeof(cxf) * (size_t)m * n);
     alloc((void **)&a.part, sizeof(double) * P_COUNT * (size_t)maxctas * FZ_PSTRIDE);
-    alloc((void **)&a.bar, sizeof(FzBarrier));
+    alloc((void **)&a.bar, 2 * sizeof(FzBarrier));
+    if (code == PG_OK && cudaMemset(a.bar, 0, 2 * sizeof(FzBarrier)) != cudaSuccess) code = PG_ERR_CUDA;
     if (code == PG_OK) code = upload_vec(rb64, &f->bufs[0]);
     if (code == PG_OK) code = upload_vec(rb32, &f->bufs[1]);
     if (code == PG_OK) code = upload_vec(ucol, &f->bufs[2]);
@@ -1606,7 +1610,9 @@ int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams &par
         a.err = err;
         a.probe_extra = f->args.probe_extra;
         a.probe_at = f->args.probe_at;
-        PG_CUDA_TRY(cudaMemsetAsync(a.bar, 0, sizeof(FzBarrier), s));
+        a.bar = f->args.bar + f->parity;
+        a.bar_next = f->args.bar + (1 - f->parity);
+        f->parity ^= 1;
         cudaLaunchConfig_t cfg;
         memset(&cfg, 0, sizeof(cfg));
         cfg.gridDim = dim3(f->cnctas);
@@ -1646,8 +1652,11 @@ int pg_cayley_fused_launch(FusedCayley *f, cudaStream_t s, const StepParams &par
     a.st = st;
     a.tol = tol;
     a.err = err;
-    // a barrier left half-way by an earlier launch whose wait ran out starts from zero again
-    PG_CUDA_TRY(cudaMemsetAsync(a.bar, 0, sizeof(FzBarrier), s));
+    // launches alternate between two arrival counters, each clearing the other at its start: a
+    // counter left half-way by a launch whose wait ran out is cleared before it is used again
+    a.bar = f->args.bar + f->parity;
+    a.bar_next = f->args.bar + (1 - f->parity);
+    f->parity ^= 1;
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof(cfg));
     cfg.gridDim = dim3(f->nctas);
