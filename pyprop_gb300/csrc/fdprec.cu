@@ -20,6 +20,32 @@
 
 namespace {
 
+// four consecutive entries of a shared-memory row (16-byte aligned: the row offset and the
+// column are multiples of 4) as 16-byte vector loads: fewer instructions and bank conflicts
+__device__ __forceinline__ void fd_ld4(const float *p, float (&v)[4])
+{
+    const float4 q = *reinterpret_cast<const float4 *>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+__device__ __forceinline__ void fd_ld4(const double *p, double (&v)[4])
+{
+    const double2 a = *reinterpret_cast<const double2 *>(p), b = *reinterpret_cast<const double2 *>(p + 2);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void fd_ld4(const cx<float> *p, cx<float> (&v)[4])
+{
+    const float4 a = *reinterpret_cast<const float4 *>(p), b = *reinterpret_cast<const float4 *>(p + 2);
+    v[0] = mk<float>(a.x, a.y); v[1] = mk<float>(a.z, a.w); v[2] = mk<float>(b.x, b.y); v[3] = mk<float>(b.z, b.w);
+}
+__device__ __forceinline__ void fd_ld4(const cx<double> *p, cx<double> (&v)[4])
+{
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        const double2 q = *reinterpret_cast<const double2 *>(p + w);
+        v[w] = mk<double>(q.x, q.y);
+    }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(1024) fd_solve_kernel(int N, int NP, const R *__restrict__ V,
                                                         const cx<R> *__restrict__ D, const int *__restrict__ lidx,
@@ -58,16 +84,17 @@ __global__ void __launch_bounds__(1024) fd_solve_kernel(int N, int NP, const R *
     zero();
     if (act)
         for (int k = 0; k < NP; ++k) {
+            R v[4];
+            cx<R> xv[4];
+            fd_ld4(V1 + (size_t)k * NP + i0, v);
+            fd_ld4(X + (size_t)k * NP + j0, xv);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const R v = V1[(size_t)k * NP + i0 + u];
+            for (int u = 0; u < 4; ++u)
 #pragma unroll
                 for (int w = 0; w < 4; ++w) {
-                    const cx<R> xv = X[(size_t)k * NP + j0 + w];
-                    acc[u][w].x = fma(v, xv.x, acc[u][w].x);
-                    acc[u][w].y = fma(v, xv.y, acc[u][w].y);
+                    acc[u][w].x = fma(v[u], xv[w].x, acc[u][w].x);
+                    acc[u][w].y = fma(v[u], xv[w].y, acc[u][w].y);
                 }
-            }
         }
     __syncthreads();
     if (act)
@@ -80,16 +107,18 @@ __global__ void __launch_bounds__(1024) fd_solve_kernel(int N, int NP, const R *
     zero();
     if (act)
         for (int k = 0; k < NP; ++k) {
+            R v[4];
+            fd_ld4(V2 + (size_t)k * NP + j0, v);
+            cx<R> tv[4];
 #pragma unroll
-            for (int w = 0; w < 4; ++w) {
-                const R v = V2[(size_t)k * NP + j0 + w];
+            for (int u = 0; u < 4; ++u) tv[u] = X[(size_t)(i0 + u) * NP + k];
+#pragma unroll
+            for (int w = 0; w < 4; ++w)
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
-                    const cx<R> tv = X[(size_t)(i0 + u) * NP + k];
-                    acc[u][w].x = fma(v, tv.x, acc[u][w].x);
-                    acc[u][w].y = fma(v, tv.y, acc[u][w].y);
+                    acc[u][w].x = fma(v[w], tv[u].x, acc[u][w].x);
+                    acc[u][w].y = fma(v[w], tv[u].y, acc[u][w].y);
                 }
-            }
         }
     __syncthreads();
     if (act) {
@@ -107,14 +136,15 @@ __global__ void __launch_bounds__(1024) fd_solve_kernel(int N, int NP, const R *
     zero();
     if (act)
         for (int k = 0; k < NP; ++k) {
+            cx<R> xv[4];
+            fd_ld4(X + (size_t)k * NP + j0, xv);
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const R v = V1[(size_t)(i0 + u) * NP + k];
 #pragma unroll
                 for (int w = 0; w < 4; ++w) {
-                    const cx<R> xv = X[(size_t)k * NP + j0 + w];
-                    acc[u][w].x = fma(v, xv.x, acc[u][w].x);
-                    acc[u][w].y = fma(v, xv.y, acc[u][w].y);
+                    acc[u][w].x = fma(v, xv[w].x, acc[u][w].x);
+                    acc[u][w].y = fma(v, xv[w].y, acc[u][w].y);
                 }
             }
         }
