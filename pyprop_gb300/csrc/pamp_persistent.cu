@@ -153,14 +153,19 @@ __device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x, i
         cx<R> z[CH];
         const int a = task / nck, c = task - a * nck, r0 = c * CH, len = min(CH, N - r0);
         const cx<R> *bb = b + (size_t)a * N + r0;
+        // all loads first: vout may be b itself (in-place normalisation), and a store between
+        // two loads would make each load wait for the previous one
 #pragma unroll
-        for (int r = 0; r < CH; ++r) {
-            z[r] = mk<R>((R)0, (R)0);
-            if (r < len) {
-                const cx<R> v = bb[r];
-                z[r] = (sc == 1.0) ? v : mk<R>(v.x * scr, v.y * scr);
-                if (vout) vout[(size_t)a * N + r0 + r] = z[r];
-            }
+        for (int r = 0; r < CH; ++r) z[r] = r < len ? bb[r] : mk<R>((R)0, (R)0);
+        if (sc != 1.0) {
+#pragma unroll
+            for (int r = 0; r < CH; ++r) z[r] = mk<R>(z[r].x * scr, z[r].y * scr);
+        }
+        if (vout) {
+            cx<R> *vo = vout + (size_t)a * N + r0;
+#pragma unroll
+            for (int r = 0; r < CH; ++r)
+                if (r < len) vo[r] = z[r];
         }
         if constexpr (LOWER) {
 #pragma unroll
@@ -291,14 +296,21 @@ __device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x, i
             for (int q = 0; q < kb; ++q) s[q] = sv[q];
             cx<R> *xx = x + (size_t)a * N + r0;
             const R *g = G + (size_t)c * CH * kb;
-            for (int r = 0; r < len; ++r) {
-                cx<R> v = xx[r];
-                for (int q = 0; q < kb; ++q) {
-                    const R gq = g[(size_t)r * kb + q];
-                    v.x += gq * s[q].x;
-                    v.y += gq * s[q].y;
+            // all loads of the chunk first, then the corrections and the stores
+            cx<R> z[CH];
+#pragma unroll
+            for (int r = 0; r < CH; ++r) z[r] = r < len ? xx[r] : mk<R>((R)0, (R)0);
+#pragma unroll
+            for (int r = 0; r < CH; ++r) {
+                if (r < len) {
+                    cx<R> v = z[r];
+                    for (int q = 0; q < kb; ++q) {
+                        const R gq = g[(size_t)r * kb + q];
+                        v.x += gq * s[q].x;
+                        v.y += gq * s[q].y;
+                    }
+                    xx[r] = v;
                 }
-                xx[r] = v;
             }
         }
     }
@@ -723,20 +735,24 @@ __device__ void pm_member_step(const PmMember &M, double dt, unsigned char *smem
         // w - V (h1 + h2) into the slot of V[j+1] (unnormalised) and beta = its norm
         {
             cxf *dst = (J < m) ? V + (size_t)J * n : nullptr;
+            // the columns read below (c < J) and the slot written (J) are disjoint: separate
+            // pointers let the next element's loads go ahead of this element's store
+            const cxf *__restrict__ Vr = V;
+            cxf *__restrict__ dstw = dst;
             float nf = 0.f;  // per-thread sum in FP32 (as the graph path's column sums), CTA sum in FP64
             for (long long e = tid; e < n; e += T) {
                 cxf x = w[e];
 #pragma unroll
                 for (int c = 0; c < PM_MAXM; ++c)
                     if (c < J) {
-                        const cxf v = V[(size_t)c * n + e];
+                        const cxf v = Vr[(size_t)c * n + e];
                         const cxf hc = hf[c];
                         x.x = fmaf(-v.x, hc.x, x.x);
                         x.x = fmaf(v.y, hc.y, x.x);
                         x.y = fmaf(-v.x, hc.y, x.y);
                         x.y = fmaf(-v.y, hc.x, x.y);
                     }
-                if (dst) dst[e] = x;
+                if (dstw) dstw[e] = x;
                 nf = fmaf(x.x, x.x, fmaf(x.y, x.y, nf));
             }
             __syncthreads();  // hf (in cc) is read above; pm_sum1 writes its slot there
