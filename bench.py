@@ -580,6 +580,7 @@ def run_ours(args):
     ens_pamp = run_pamp_ensemble(args, torch, flush) if args.ensemble > 0 else None
     two_e_large = time_two_electron_large(torch) if (args.two_electron_large and rank == 0) else None
     learned = time_learned_helium(torch) if (args.learned and rank == 0) else None
+    pamp_l10 = time_pamp_hydrogen_l10(torch, flush) if (args.pamp_l10 and rank == 0) else None
     cpu = cpu_baseline_sample(nsteps=args.cpu_steps) if (rank == 0 and world == 1 and args.cpu_steps > 0) else None
     if rank == 0:
         steps_per_s = world * args.steps / t_mixed
@@ -655,6 +656,7 @@ def run_ours(args):
             "two_electron_cayley": two_e_steps,
             "two_electron_large": two_e_large,
             "learned_helium": learned,
+            "pamp_hydrogen_l10": pamp_l10,
             "cpu_baseline": cpu,
             "ensemble": ens,
             "ensemble_pamp": ens_pamp,
@@ -970,6 +972,60 @@ def time_two_electron_large(torch, steps=2):
             "parity": "oracle comparison at reduced size with the same code path: tests/test_gpu_helium.py"}
 
 
+def time_pamp_hydrogen_l10(torch, flush, steps=1000, warmup=5):
+    """Hydrogen lmax 10, 150 B-splines, rmax 100, pAMP with 20 Krylov vectors, dt 0.01 through
+    the 10 a.u. 800 nm pulse (1000 steps), from the field-free 1s state: steps per second of the
+    single-wavefunction step: complex64 basis as one cooperative kernel per step (the default)
+    and as captured graphs; complex128 basis as graphs with the m x m exponential on the host
+    between them (the default: FP64 arithmetic is scarce on this GPU) and on the device. CUDA
+    events around each step on the launching stream, L2 flushed (256 MB write) before each,
+    outside the bracket."""
+    import pyprop_gb300 as pp
+    from pyprop_gb300.workloads import HYDROGEN_L10_PAMP, hydrogen
+    stream = torch.cuda.current_stream()
+    out = {"workload": "hydrogen lmax=10 N=150 rmax=100 pAMP(20), dt=0.01, 800nm sin2 pulse 0.05au, 1000 steps",
+           "timing": "CUDA events around each step, L2 flushed before each"}
+    psi0 = None
+    for name, prec, fused, dev in (("fp32", "fp32", True, False), ("fp32_graphs", "fp32", False, False),
+                                   ("fp64", "fp64", False, False), ("fp64_device_exp", "fp64", False, True)):
+        prob = pp.Problem(pp.LoadString(hydrogen(propagator="PamPropagatorGPU", precision=prec, **HYDROGEN_L10_PAMP)))
+        prob.SetupStep(skipWavefunctionSetup=True)
+        if prob.Propagator.stepper.set_fused(fused) != fused:
+            raise RuntimeError("pAMP leg: the single-kernel step does not take this workload")
+        prob.Propagator.stepper.set_device_exp(dev)
+        prob.Propagator.StepStats = False
+        if psi0 is None:
+            psi0, _ = initial_state(prob)
+        prob.psi.GetData().copy_(torch.as_tensor(psi0, device="cuda"))
+        prob.PropagatedTime = 0.0
+        ctx = prob.Propagator.op64.ctx
+        for _ in range(warmup):
+            prob.AdvanceStep()
+        torch.cuda.synchronize()
+        prob.PropagatedTime = 0.0
+        prob.psi.GetData().copy_(torch.as_tensor(psi0, device="cuda"))
+        l0 = ctx.launches()
+        events = []
+        for _ in range(steps):
+            flush.fill_(1.0)
+            s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s_ev.record(stream)
+            prob.AdvanceStep()
+            e_ev.record(stream)
+            events.append((s_ev, e_ev))
+        torch.cuda.synchronize()
+        total = sum(a.elapsed_time(b) for a, b in events) * 1e-3
+        st = prob.Propagator.LastStats
+        out[name] = {"steps_per_s": steps / total, "us_per_step": 1e6 * total / steps,
+                     "kernels_per_step": (ctx.launches() - l0) / steps, "norm_after_pulse": prob.psi.GetNorm(),
+                     "error_estimate_last_step": st.ErrorEstimate}
+    out["single_kernel_speedup_vs_graphs"] = out["fp32"]["steps_per_s"] / out["fp32_graphs"]["steps_per_s"]
+    out["speedup_vs_plain_fp64"] = out["fp32"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    out["parity"] = ("tests/test_gpu_parity.py: the whole pulse (40 vectors) and the first steps (20 vectors) against "
+                     "the reference templates' states")
+    return out
+
+
 def time_learned_helium(torch):
     """The learned preconditioner at the helium model of TWO_ELECTRON (coupled L <= 5, l1, l2
     <= 10, 80 B-splines per electron: 291 angular blocks of 6400 coefficients), field free, on
@@ -1125,6 +1181,8 @@ def main():
                          "2 the cluster variant")
     ap.add_argument("--two-electron-large", type=int, default=1,
                     help="end-to-end leg of the largest two-electron model (0 = skip)")
+    ap.add_argument("--pamp-l10", type=int, default=1,
+                    help="single-wavefunction pAMP leg: hydrogen lmax 10, 150 B-splines, 20 vectors (0 = skip)")
     ap.add_argument("--learned", type=int, default=1,
                     help="learned-preconditioner leg at the L<=5, l<=10, 80-spline helium model (0 = skip)")
     ap.add_argument("--eager", action="store_true",

@@ -276,9 +276,34 @@ typedef struct pg_pamp pg_pamp;
 int pg_pamp_create(pg_op *op64, pg_op *op_basis, pg_banded *ovl64, pg_banded *ovl_basis,
                    int basis_size, int basis_precision, int double_ortho, pg_pamp **out);
 int pg_pamp_destroy(pg_pamp *p);
-/* One step. scales: host complex128 [nscales], H(t) slot values. psi: device complex128. */
+/*
+ * One step. scales: host complex128 [nscales], H(t) slot values. psi: device complex128.
+ * By default (basis_size <= 48) the whole step, the m x m exponential included (one CTA, the
+ * scaled order-6 Pade of pamp.h:430-565), is one graph launch and the call returns without
+ * waiting; with stats != NULL it waits and fills them. A singular Pade denominator zeroes that
+ * step's coefficients and is reported (PG_ERR_BREAKDOWN) by the next call that reads
+ * statistics. Larger bases, or pg_pamp_set_device_exp(p, 0), compute the exponential on the
+ * host between two graphs (Hermitian tridiagonal H_m by implicit QL, otherwise the same
+ * Pade): the call then waits every step.
+ */
 int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scales, int nscales,
                  pg_krylov_stats *stats);
+int pg_pamp_set_device_exp(pg_pamp *p, int on); /* PG_ERR_STATE for on=1 when basis_size > 48 */
+int pg_pamp_last_stats(pg_pamp *p, pg_krylov_stats *stats); /* waits for the last step */
+/*
+ * Single-kernel step (complex64 basis; the default where it qualifies: a rank-2 operator with
+ * real bands, at most 4 source channels per row, basis_size <= 32, one resident CTA per
+ * channel): one cooperative launch runs the Arnoldi recurrence on T_j = U^-1 V_j (S-orthonormal,
+ * the same Krylov space and Hessenberg matrix as the balanced form), the m x m exponential in
+ * double-float arithmetic in every CTA, and psi = ||psi||_S sum_j c_j T_j. Two grid barriers
+ * per Arnoldi step, each a bounded wait: one that runs out sets the context's error word to 2,
+ * leaves psi unchanged, and the next call that reads statistics returns PG_ERR_NOT_CONVERGED.
+ * pg_pamp_set_fused(p, 0) selects the graphs; on=1 returns PG_ERR_STORAGE/SHAPE/STATE when the
+ * stepper does not qualify. pg_pamp_set_barrier_probe is a test hook: grid barrier number
+ * at_barrier of later steps waits for extra_arrivals arrivals that never come.
+ */
+int pg_pamp_set_fused(pg_pamp *p, int on);
+int pg_pamp_set_barrier_probe(pg_pamp *p, int extra_arrivals, int at_barrier);
 /*
  * pAMP ensembles (no reference counterpart: the reference runs one wavefunction per process):
  * many pg_pamp members (each with its own operator, overlap and basis size) advanced together,

@@ -25,6 +25,7 @@ PG_BAND_SOLVE_S = 5
 PG_BAND_PREC_SOLVE = 6
 PG_ERR_STORAGE = -3
 PG_ERR_SHAPE = -4
+PG_ERR_NOT_CONVERGED = -7
 PG_ERR_STATE = -9
 
 ERRORS = {
@@ -97,6 +98,10 @@ _SIGS = {
     "pg_pamp_create": (_I, [_P, _P, _P, _P, _I, _I, _I, C.POINTER(_P)]),
     "pg_pamp_destroy": (_I, [_P]),
     "pg_pamp_step": (_I, [_P, _P, _D, _DP, _I, C.POINTER(KrylovStats)]),
+    "pg_pamp_set_device_exp": (_I, [_P, _I]),
+    "pg_pamp_last_stats": (_I, [_P, C.POINTER(KrylovStats)]),
+    "pg_pamp_set_fused": (_I, [_P, _I]),
+    "pg_pamp_set_barrier_probe": (_I, [_P, _I, _I]),
     "pg_cayley_create": (_I, [_P, _P, _P, _P, _I, _I, _D, C.POINTER(_P)]),
     "pg_cayley_destroy": (_I, [_P]),
     "pg_cayley_step": (_I, [_P, _P, _D, _DP, _I, C.POINTER(KrylovStats)]),

@@ -14,12 +14,14 @@
 #include "pg_internal.cuh"
 #include "pamp_expm.cuh"
 #include "pamp_persistent.cuh"
+#include "pamp_fused.cuh"
 
 #include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstring>
 #include <limits>
+#include <mutex>
 
 typedef std::complex<double> zd;
 
@@ -206,11 +208,14 @@ static pg_scales to_scales(const double *s, int n)
 // ------------------------------------------------------------------------------------
 // pAMP
 // ------------------------------------------------------------------------------------
-// A step is two CUDA graphs and one host round trip:
-//   graph 1: psi <- U psi, ||psi||, V[0] = psi/||psi||, then m Arnoldi steps on
-//            U^-H H(t) U^-1 (solve, matvec, solve, CGS2), Hessenberg columns to pinned memory;
+// A step is one CUDA graph with no host round trip (the default, basis <= PAMP_DEV_EXP_MAXM):
+//   psi <- U psi, ||psi||, V[0] = psi/||psi||, then m Arnoldi steps on U^-H H(t) U^-1
+//   (solve, matvec, solve, CGS2); c = ||psi|| exp(-i dt H_m) e1 by one CTA (the reference's
+//   scaled Pade of order 6, pamp_expm.cuh); psi = V c, psi <- U^-1 psi.
+// or (pg_pamp_set_device_exp(p, 0)) two graphs and one host round trip:
+//   graph 1: the Arnoldi steps, Hessenberg columns to pinned memory;
 //   host:    exp(-i dt H_m) e1 in FP64 (Hermitian tridiagonal H_m: eigen-decomposition by
-//            implicit QL; otherwise the reference's scaled Pade of order 6);
+//            implicit QL; otherwise the same Pade);
 //   graph 2: coefficients to the device, psi = ||psi|| V c, psi <- U^-1 psi.
 // A happy breakdown (beta < sqrt(eps), pamp.h:306-313) truncates the basis on the host; the
 // device normalisation maps a zero norm to a zero vector, so the extra rows stay finite and
@@ -315,6 +320,48 @@ bool expm_first_column(int k, const std::vector<zd> &H, double dt, std::vector<z
 
 }  // namespace dense
 
+namespace {
+
+__global__ void __launch_bounds__(256) pamp_expm_kernel(const PampExpArgs *__restrict__ args,
+                                                        const double *__restrict__ dt_dev)
+{
+    extern __shared__ __align__(16) unsigned char pe_smem[];
+    pamp_expm_block(args[blockIdx.x], *dt_dev, pe_smem);
+}
+
+// One wavefunction's exponential; stats[3] is a sticky flag (1 after any singular Pade
+// denominator) that the host clears when it reads the statistics.
+__global__ void __launch_bounds__(256) pamp_expm_one_kernel(const PampExpArgs *__restrict__ args,
+                                                            const double *__restrict__ dt_dev)
+{
+    extern __shared__ __align__(16) unsigned char pe_smem[];
+    const PampExpArgs a = *args;
+    pamp_expm_block(a, *dt_dev, pe_smem);
+    if (threadIdx.x == 0 && a.stats[2] != 0.0) a.stats[3] = 1.0;
+}
+
+// Largest basis whose exponential fits one CTA's shared memory (6 m^2 complex doubles).
+const int PAMP_DEV_EXP_MAXM = 48;
+
+size_t pamp_expm_smem(int m) { return 6 * sizeof(cxd) * (size_t)m * m; }
+
+// Raise (never lower) the dynamic shared-memory limit of both exponential kernels.
+int pamp_expm_raise_smem(size_t bytes)
+{
+    static std::mutex mu;
+    static size_t raised = 48 * 1024;
+    std::lock_guard<std::mutex> lock(mu);
+    if (bytes <= raised) return PG_OK;
+    PG_CUDA_TRY(cudaFuncSetAttribute(pamp_expm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    PG_CUDA_TRY(cudaFuncSetAttribute(pamp_expm_one_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    raised = bytes;
+    return PG_OK;
+}
+
+}  // namespace
+
+const int PAMP_RING = 4;  // pinned parameter slots of the steps in flight
+
 struct pg_pamp {
     pg_op *op64 = nullptr, *opb = nullptr;
     pg_banded *ovl64 = nullptr, *ovlb = nullptr;
@@ -338,6 +385,26 @@ struct pg_pamp {
     bool last_hermitian = false;
     long long kernels_per_step = 0;  // kernel nodes of the two graphs
     pg_krylov_stats last_stats = {};  // of the last step (ensemble steps read it per member)
+    // device exponential (the default where m <= PAMP_DEV_EXP_MAXM): the whole step is one
+    // graph - Arnoldi, the m x m exponential in one CTA, psi = ||psi|| V c - so a step never
+    // waits for the host; statistics are read back only when asked for.
+    bool device_exp = false;
+    int built_mode = -1;                // device_exp of the graphs built for built_psi
+    cudaGraphExec_t gd = nullptr;
+    long long kernels_device = 0;
+    PampExpArgs *d_exargs = nullptr;
+    double *d_ex = nullptr;             // [0..3] exponential statistics (pamp_expm_one_kernel), [4] dt
+    double *h_ex = nullptr;             // pinned [4] statistics read back
+    cxd *h_ring = nullptr;              // pinned [PAMP_RING][PG_MAX_SLOTS + 1]: slot values, then dt
+    cudaEvent_t ring_ev[PAMP_RING] = {};
+    bool ring_used[PAMP_RING] = {};
+    int ring_pos = 0;
+    bool stats_pending = false;         // a device step ran since the statistics were last read
+    // the single-kernel step (pamp_fused.cu; complex64 basis): the default where it qualifies
+    FusedPamp *fused = nullptr;
+    int fused_status = PG_ERR_STATE;    // why it does not qualify (PG_OK when it does)
+    bool use_fused = false;
+    bool fused_pending = false;         // a single-kernel step ran since the error word was last read
 };
 
 extern "C" int pg_pamp_create(pg_op *op64, pg_op *op_basis, pg_banded *ovl64, pg_banded *ovl_basis, int basis_size,
@@ -373,6 +440,30 @@ extern "C" int pg_pamp_create(pg_op *op64, pg_op *op_basis, pg_banded *ovl64, pg
     p->rctx.num_sms = p->ctx->num_sms;
     PG_TRY(pg_ctx_ensure_reduction(&p->rctx));
     PG_CUDA_TRY(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking));
+    PG_CUDA_TRY(cudaMalloc(&p->d_ex, sizeof(double) * 8));
+    PG_CUDA_TRY(cudaMemset(p->d_ex, 0, sizeof(double) * 8));
+    PG_CUDA_TRY(cudaMallocHost(&p->h_ex, sizeof(double) * 6));
+    PG_CUDA_TRY(cudaMallocHost(&p->h_ring, sizeof(cxd) * PAMP_RING * (PG_MAX_SLOTS + 1)));
+    for (int k = 0; k < PAMP_RING; ++k) PG_CUDA_TRY(cudaEventCreateWithFlags(&p->ring_ev[k], cudaEventDisableTiming));
+    if (p->m <= PAMP_DEV_EXP_MAXM) {
+        PampExpArgs a;
+        a.cols = p->ab.d_cols;
+        a.norm = p->d_norm;
+        a.c = p->d_c;
+        a.stats = p->d_ex;
+        a.m = p->m;
+        a.double_ortho = p->double_ortho;
+        a.tol = p->tolerance;
+        PG_CUDA_TRY(cudaMalloc(&p->d_exargs, sizeof(PampExpArgs)));
+        PG_CUDA_TRY(cudaMemcpy(p->d_exargs, &a, sizeof(PampExpArgs), cudaMemcpyHostToDevice));
+        PG_TRY(pamp_expm_raise_smem(pamp_expm_smem(p->m)));
+        p->device_exp = false;  // FP64 arithmetic is scarce on this GPU: the host is faster for this m x m work
+    }
+    if (basis_precision == PG_FP32) {
+        p->fused_status = pg_pamp_fused_prepare(op_basis, ovl64, ovl_basis, p->V, p->m, p->tolerance, &p->fused);
+        if (p->fused_status == PG_OK) p->use_fused = true;
+        cudaGetLastError();  // a shape the single-kernel step refuses leaves no error behind
+    }
     *out = p;
     return PG_OK;
 }
@@ -383,7 +474,15 @@ extern "C" int pg_pamp_destroy(pg_pamp *p)
     cudaStreamSynchronize(p->ctx->stream);
     if (p->g1) cudaGraphExecDestroy(p->g1);
     if (p->g2) cudaGraphExecDestroy(p->g2);
+    if (p->gd) cudaGraphExecDestroy(p->gd);
     if (p->cap) cudaStreamDestroy(p->cap);
+    for (int k = 0; k < PAMP_RING; ++k)
+        if (p->ring_ev[k]) cudaEventDestroy(p->ring_ev[k]);
+    pg_pamp_fused_free(p->fused);
+    cudaFree(p->d_exargs);
+    cudaFree(p->d_ex);
+    if (p->h_ex) cudaFreeHost(p->h_ex);
+    if (p->h_ring) cudaFreeHost(p->h_ring);
     cudaFree(p->V);
     cudaFree(p->w);
     cudaFree(p->tmp);
@@ -442,7 +541,20 @@ static int pamp_record_finish(pg_pamp *p, cxd *x, bool upload = true)
     return pg_banded_apply_dev(p->ovl64, PG_BAND_SOLVE_U, x);
 }
 
-static int pamp_capture(pg_pamp *p, cxd *x, bool first, cudaGraphExec_t *out)
+// The whole step on the device: Arnoldi, the exponential, psi = ||psi|| V c, psi <- U^-1 psi.
+template <typename R>
+static int pamp_record_device(pg_pamp *p, cxd *x)
+{
+    PG_TRY(pamp_record_arnoldi<R>(p, x, false));
+    pamp_expm_one_kernel<<<1, 256, pamp_expm_smem(p->m), p->ctx->stream>>>(p->d_exargs, p->d_ex + 4);
+    PG_CUDA_TRY(cudaGetLastError());
+    p->ctx->launches += 1;
+    return pamp_record_finish<R>(p, x, false);
+}
+
+enum { PAMP_PART_ARNOLDI = 0, PAMP_PART_FINISH = 1, PAMP_PART_DEVICE = 2 };
+
+static int pamp_capture(pg_pamp *p, cxd *x, int part, cudaGraphExec_t *out, long long *kernels)
 {
     pg_ctx *ctx = p->ctx;
     cudaStream_t saved = ctx->stream;
@@ -450,11 +562,13 @@ static int pamp_capture(pg_pamp *p, cxd *x, bool first, cudaGraphExec_t *out)
     const long long l0 = ctx->launches, r0 = p->rctx.launches;
     PG_CUDA_TRY(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
     ctx->stream = p->cap;
+    const bool f64 = p->prec == PG_FP64;
     int code;
-    if (first) code = (p->prec == PG_FP64) ? pamp_record_arnoldi<double>(p, x) : pamp_record_arnoldi<float>(p, x);
-    else code = (p->prec == PG_FP64) ? pamp_record_finish<double>(p, x) : pamp_record_finish<float>(p, x);
+    if (part == PAMP_PART_ARNOLDI) code = f64 ? pamp_record_arnoldi<double>(p, x) : pamp_record_arnoldi<float>(p, x);
+    else if (part == PAMP_PART_FINISH) code = f64 ? pamp_record_finish<double>(p, x) : pamp_record_finish<float>(p, x);
+    else code = f64 ? pamp_record_device<double>(p, x) : pamp_record_device<float>(p, x);
     ctx->stream = saved;
-    p->kernels_per_step += (ctx->launches - l0) + (p->rctx.launches - r0);
+    *kernels += (ctx->launches - l0) + (p->rctx.launches - r0);
     ctx->launches = l0;
     p->rctx.launches = r0;
     cudaGraph_t g = nullptr;
@@ -478,20 +592,29 @@ static int pamp_capture(pg_pamp *p, cxd *x, bool first, cudaGraphExec_t *out)
 
 static int pamp_build(pg_pamp *p, cxd *x)
 {
-    if (p->built_psi == x) return PG_OK;
+    const int mode = p->device_exp ? 1 : 0;
+    if (p->built_psi == x && p->built_mode == mode) return PG_OK;
     if (p->g1) { cudaGraphExecDestroy(p->g1); p->g1 = nullptr; }
     if (p->g2) { cudaGraphExecDestroy(p->g2); p->g2 = nullptr; }
+    if (p->gd) { cudaGraphExecDestroy(p->gd); p->gd = nullptr; }
+    p->built_psi = nullptr;
     p->kernels_per_step = 0;
-    PG_TRY(pamp_capture(p, x, true, &p->g1));
-    PG_TRY(pamp_capture(p, x, false, &p->g2));
+    p->kernels_device = 0;
+    if (mode) {
+        PG_TRY(pamp_capture(p, x, PAMP_PART_DEVICE, &p->gd, &p->kernels_device));
+    } else {
+        PG_TRY(pamp_capture(p, x, PAMP_PART_ARNOLDI, &p->g1, &p->kernels_per_step));
+        PG_TRY(pamp_capture(p, x, PAMP_PART_FINISH, &p->g2, &p->kernels_per_step));
+    }
     p->built_psi = x;
+    p->built_mode = mode;
     return PG_OK;
 }
 
-static void pamp_set_scales(pg_pamp *p, const double *scales, int nscales)
+static void pamp_set_scales(cxd *dst, const double *scales, int nscales)
 {
     for (int k = 0; k < PG_MAX_SLOTS; ++k)
-        p->h_scales[k] = mk<double>(k < nscales ? scales[2 * k] : 0.0, k < nscales ? scales[2 * k + 1] : 0.0);
+        dst[k] = mk<double>(k < nscales ? scales[2 * k] : 0.0, k < nscales ? scales[2 * k + 1] : 0.0);
 }
 
 // After the Arnoldi graph has completed: the m x m Hessenberg from the downloaded columns
@@ -537,19 +660,135 @@ static int pamp_host_exp(pg_pamp *p, double dt, pg_krylov_stats *st)
     return PG_OK;
 }
 
+// Waits for the last device step and copies its basis size and error estimate into
+// last_stats (and st). A singular Pade denominator in any device step since the last read
+// gives PG_ERR_BREAKDOWN (that step's coefficients were zeroed).
+static int pamp_read_stats(pg_pamp *p, pg_krylov_stats *st)
+{
+    pg_ctx *ctx = p->ctx;
+    if (p->stats_pending) {
+        PG_CUDA_TRY(cudaMemcpyAsync(p->h_ex, p->d_ex, sizeof(double) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        if (p->fused_pending)
+            PG_CUDA_TRY(cudaMemcpyAsync(p->h_ex + 4, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        p->stats_pending = false;
+        if (p->fused_pending) {
+            p->fused_pending = false;
+            int word = 0;
+            memcpy(&word, p->h_ex + 4, sizeof(int));
+            if (word != 0) return PG_ERR_NOT_CONVERGED;  // a grid barrier's bounded wait ran out (error word)
+        }
+        p->last_stats.Iterations = (long long)p->h_ex[0];
+        p->last_stats.ErrorEstimate = p->h_ex[1];
+        if (p->h_ex[3] != 0.0) {
+            PG_CUDA_TRY(cudaMemsetAsync(p->d_ex + 3, 0, sizeof(double), ctx->stream));
+            if (st) { st->Iterations = p->last_stats.Iterations; st->ErrorEstimate = p->last_stats.ErrorEstimate; }
+            return PG_ERR_BREAKDOWN;
+        }
+    }
+    if (st) { st->Iterations = p->last_stats.Iterations; st->ErrorEstimate = p->last_stats.ErrorEstimate; }
+    return PG_OK;
+}
+
 extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scales, int nscales, pg_krylov_stats *st)
 {
     if (!p || !psi || nscales < 0 || nscales > PG_MAX_SLOTS || (nscales > 0 && !scales)) return PG_ERR_ARG;
     pg_ctx *ctx = p->ctx;
+    const int m = p->m;
+    const long long ip = (long long)(p->double_ortho ? 2 : 1) * m, ro = p->double_ortho ? m : 0;
+    if (p->use_fused) {
+        cxd h[PG_MAX_SLOTS];
+        pamp_set_scales(h, scales, nscales);
+        PG_TRY(pg_pamp_fused_launch(p->fused, ctx->stream, (cxd *)psi, dt, h, p->d_ex, ctx->d_err));
+        ctx->launches += 1;
+        p->stats_pending = true;
+        p->fused_pending = true;
+        p->last_stats.OpCount += m;
+        p->last_stats.InnerProductCount += 2 * m;
+        p->last_stats.ReOrthoCount += m;
+        if (!st) return PG_OK;
+        st->OpCount += m;
+        st->InnerProductCount += 2 * m;
+        st->ReOrthoCount += m;
+        return pamp_read_stats(p, st);
+    }
     PG_TRY(pamp_build(p, (cxd *)psi));
-    pamp_set_scales(p, scales, nscales);
-    PG_CUDA_TRY(cudaMemcpyAsync(p->d_scales, p->h_scales, sizeof(cxd) * PG_MAX_SLOTS, cudaMemcpyHostToDevice, ctx->stream));
-    PG_CUDA_TRY(cudaGraphLaunch(p->g1, ctx->stream));
-    PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    PG_TRY(pamp_host_exp(p, dt, st));
-    PG_CUDA_TRY(cudaGraphLaunch(p->g2, ctx->stream));
-    ctx->launches += p->kernels_per_step;
+    if (!p->device_exp) {
+        pamp_set_scales(p->h_scales, scales, nscales);
+        PG_CUDA_TRY(cudaMemcpyAsync(p->d_scales, p->h_scales, sizeof(cxd) * PG_MAX_SLOTS, cudaMemcpyHostToDevice,
+                                    ctx->stream));
+        PG_CUDA_TRY(cudaGraphLaunch(p->g1, ctx->stream));
+        PG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        PG_TRY(pamp_host_exp(p, dt, st));
+        PG_CUDA_TRY(cudaGraphLaunch(p->g2, ctx->stream));
+        ctx->launches += p->kernels_per_step;
+        return PG_OK;
+    }
+    // the slot values and dt go through a ring of pinned buffers: the host refills a slot only
+    // after the copy that read it has run
+    const int slot = p->ring_pos;
+    p->ring_pos = (p->ring_pos + 1) % PAMP_RING;
+    if (p->ring_used[slot]) PG_CUDA_TRY(cudaEventSynchronize(p->ring_ev[slot]));
+    cxd *hp = p->h_ring + (size_t)slot * (PG_MAX_SLOTS + 1);
+    pamp_set_scales(hp, scales, nscales);
+    hp[PG_MAX_SLOTS] = mk<double>(dt, 0.0);
+    PG_CUDA_TRY(cudaMemcpyAsync(p->d_scales, hp, sizeof(cxd) * PG_MAX_SLOTS, cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA_TRY(cudaMemcpyAsync(p->d_ex + 4, hp + PG_MAX_SLOTS, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA_TRY(cudaEventRecord(p->ring_ev[slot], ctx->stream));
+    p->ring_used[slot] = true;
+    PG_CUDA_TRY(cudaGraphLaunch(p->gd, ctx->stream));
+    ctx->launches += p->kernels_device;
+    p->stats_pending = true;
+    p->last_stats.OpCount += m;
+    p->last_stats.InnerProductCount += ip;
+    p->last_stats.ReOrthoCount += ro;
+    if (!st) return PG_OK;
+    st->OpCount += m;
+    st->InnerProductCount += ip;
+    st->ReOrthoCount += ro;
+    return pamp_read_stats(p, st);
+}
+
+// 1: the m x m exponential on the device, no host round trip (default where the basis has at
+// most PAMP_DEV_EXP_MAXM vectors); 0: on the host between two graphs (Hermitian tridiagonal
+// H_m by implicit QL, otherwise the same Pade).
+extern "C" int pg_pamp_set_device_exp(pg_pamp *p, int on)
+{
+    if (!p) return PG_ERR_ARG;
+    if (on && !p->d_exargs) return PG_ERR_STATE;
+    if (p->device_exp != (on != 0)) {
+        PG_CUDA_TRY(cudaStreamSynchronize(p->ctx->stream));
+        p->device_exp = on != 0;
+    }
     return PG_OK;
+}
+
+// 1: the single-kernel step (complex64 basis; the default where it qualifies), 0: the graphs.
+extern "C" int pg_pamp_set_fused(pg_pamp *p, int on)
+{
+    if (!p) return PG_ERR_ARG;
+    if (on && !p->fused) return p->fused_status != PG_OK ? p->fused_status : PG_ERR_STATE;
+    p->use_fused = on != 0;
+    return PG_OK;
+}
+
+// Test hook of the single-kernel step: grid barrier number at_barrier of later steps waits for
+// extra_arrivals arrivals that never come (its bounded wait runs out: error word 2).
+extern "C" int pg_pamp_set_barrier_probe(pg_pamp *p, int extra_arrivals, int at_barrier)
+{
+    if (!p || extra_arrivals < 0 || at_barrier < 0) return PG_ERR_ARG;
+    if (!p->fused) return PG_ERR_STATE;
+    pg_pamp_fused_set_probe(p->fused, (unsigned)extra_arrivals, (unsigned)at_barrier);
+    return PG_OK;
+}
+
+// Statistics of the last step (waits for it when the exponential ran on the device).
+extern "C" int pg_pamp_last_stats(pg_pamp *p, pg_krylov_stats *st)
+{
+    if (!p || !st) return PG_ERR_ARG;
+    const int code = pamp_read_stats(p, nullptr);
+    *st = p->last_stats;
+    return code;
 }
 
 // ------------------------------------------------------------------------------------
@@ -558,22 +797,11 @@ extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scal
 // ------------------------------------------------------------------------------------
 // pAMP ensembles: one graph launch per ensemble step
 // ------------------------------------------------------------------------------------
-// The single-wavefunction step computes exp(-i dt H_m) e1 on the host between its two graphs;
-// an ensemble cannot stop for the host once per member. Here the m x m exponential runs on the
-// device, one CTA per member, with the reference's method (pamp.h:430-565: scaling and squaring
-// of the diagonal Pade approximant of order 6, the formulation of dense::expm_pade above), so the
-// graph is: fork -> each member's Arnoldi steps -> join -> all exponentials in one kernel ->
-// fork -> each member's psi = ||psi|| V c and overlap solve -> join.
-namespace {
-
-__global__ void __launch_bounds__(256) pamp_expm_kernel(const PampExpArgs *__restrict__ args,
-                                                        const double *__restrict__ dt_dev)
-{
-    extern __shared__ __align__(16) unsigned char pe_smem[];
-    pamp_expm_block(args[blockIdx.x], *dt_dev, pe_smem);
-}
-
-}  // namespace
+// The m x m exponential runs on the device, one CTA per member, with the reference's method
+// (pamp.h:430-565: scaling and squaring of the diagonal Pade approximant of order 6, the
+// formulation of dense::expm_pade above), so the graph is: fork -> each member's Arnoldi steps
+// -> join -> all exponentials in one kernel -> fork -> each member's psi = ||psi|| V c and
+// overlap solve -> join.
 
 struct pg_pamp_batch {
     std::vector<pg_pamp *> members;
@@ -815,6 +1043,7 @@ extern "C" int pg_pamp_batch_create(pg_pamp **members, int nmembers, pg_pamp_bat
     b->ctx = members[0]->ctx;
     for (int k = 0; k < nmembers; ++k) {
         if (!members[k] || members[k]->ctx != b->ctx) { delete b; return PG_ERR_ARG; }
+        if (members[k]->m > PAMP_DEV_EXP_MAXM) { delete b; return PG_ERR_SHAPE; }  // exponential on the device
         for (int q = 0; q < k; ++q)
             if (members[q] == members[k]) { delete b; return PG_ERR_ARG; }
         b->members.push_back(members[k]);
@@ -841,8 +1070,7 @@ extern "C" int pg_pamp_batch_create(pg_pamp **members, int nmembers, pg_pamp_bat
     }
     PG_CUDA_TRY(cudaMalloc(&b->d_args, sizeof(PampExpArgs) * nmembers));
     PG_CUDA_TRY(cudaMemcpy(b->d_args, args.data(), sizeof(PampExpArgs) * nmembers, cudaMemcpyHostToDevice));
-    const size_t smem = 6 * sizeof(cxd) * (size_t)b->mmax * b->mmax;
-    PG_CUDA_TRY(cudaFuncSetAttribute(pamp_expm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PG_TRY(pamp_expm_raise_smem(pamp_expm_smem(b->mmax)));
     PG_CUDA_TRY(cudaEventCreateWithFlags(&b->params_done, cudaEventDisableTiming));
     PG_CUDA_TRY(cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking));
     PG_CUDA_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
@@ -879,6 +1107,7 @@ extern "C" int pg_pamp_batch_destroy(pg_pamp_batch *b)
         b->members[k]->built_psi = nullptr;  // its own graphs captured the batch's slot pointer
         if (b->members[k]->g1) { cudaGraphExecDestroy(b->members[k]->g1); b->members[k]->g1 = nullptr; }
         if (b->members[k]->g2) { cudaGraphExecDestroy(b->members[k]->g2); b->members[k]->g2 = nullptr; }
+        if (b->members[k]->gd) { cudaGraphExecDestroy(b->members[k]->gd); b->members[k]->gd = nullptr; }
     }
     cudaFree(b->d_scales);
     cudaFreeHost(b->h_scales);
@@ -920,7 +1149,7 @@ static int pamp_batch_build(pg_pamp_batch *b, void **psis)
             code = PG_ERR_CUDA;
     }
     if (code == PG_OK) {
-        const size_t smem = 6 * sizeof(cxd) * (size_t)b->mmax * b->mmax;
+        const size_t smem = pamp_expm_smem(b->mmax);
         pamp_expm_kernel<<<n, 256, smem, b->origin>>>(b->d_args, (const double *)(b->d_scales + (size_t)n * PG_MAX_SLOTS));
         kernels += 1;
         if (cudaGetLastError() != cudaSuccess || cudaEventRecord(b->mid, b->origin) != cudaSuccess) code = PG_ERR_CUDA;

@@ -317,229 +317,6 @@ __device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x, i
     __syncthreads();
 }
 
-// ---- the m x m exponential in double-float arithmetic ----------------------------------------
-// The same method as pamp_expm_block (scaling and squaring of the diagonal Pade approximant of
-// order 6, Horner in A^2, (Q - P) X = P by LU with partial pivoting, E = +-(I + 2X)) with the
-// matrices as complex double-float values (FP32 pairs hi + lo per real part, about 2^-44
-// relative): the FP64 matrix products of that routine take a few hundred microseconds per
-// member on one SM of this GPU. Divisions (2m^2 of them) and the final coefficients go
-// through FP64.
-struct dff {
-    float h, l;
-};
-__device__ __forceinline__ dff df_make(double x)
-{
-    const float h = (float)x;
-    return {h, (float)(x - (double)h)};
-}
-__device__ __forceinline__ double df_val(dff a) { return (double)a.h + (double)a.l; }
-__device__ __forceinline__ dff df_add(dff a, dff b)
-{
-    const float s = a.h + b.h;
-    const float bb = s - a.h;
-    const float e = ((a.h - (s - bb)) + (b.h - bb)) + (a.l + b.l);
-    const float h = s + e;
-    return {h, e - (h - s)};
-}
-__device__ __forceinline__ dff df_mul(dff a, dff b)
-{
-    const float p = a.h * b.h;
-    const float e = fmaf(a.h, b.l, fmaf(a.l, b.h, fmaf(a.h, b.h, -p)));
-    const float h = p + e;
-    return {h, e - (h - p)};
-}
-__device__ __forceinline__ dff df_neg(dff a) { return {-a.h, -a.l}; }
-
-typedef float4 zdf;  // (re hi, re lo, im hi, im lo)
-__device__ __forceinline__ zdf zdf_make(cxd v)
-{
-    const dff r = df_make(v.x), i = df_make(v.y);
-    return make_float4(r.h, r.l, i.h, i.l);
-}
-__device__ __forceinline__ cxd zdf_val(zdf a) { return mk<double>((double)a.x + (double)a.y, (double)a.z + (double)a.w); }
-__device__ __forceinline__ zdf zdf_add(zdf a, zdf b)
-{
-    const dff r = df_add({a.x, a.y}, {b.x, b.y}), i = df_add({a.z, a.w}, {b.z, b.w});
-    return make_float4(r.h, r.l, i.h, i.l);
-}
-__device__ __forceinline__ zdf zdf_sub(zdf a, zdf b) { return zdf_add(a, make_float4(-b.x, -b.y, -b.z, -b.w)); }
-__device__ __forceinline__ zdf zdf_mul(zdf a, zdf b)
-{
-    const dff ar{a.x, a.y}, ai{a.z, a.w}, br{b.x, b.y}, bi{b.z, b.w};
-    const dff r = df_add(df_mul(ar, br), df_neg(df_mul(ai, bi)));
-    const dff i = df_add(df_mul(ar, bi), df_mul(ai, br));
-    return make_float4(r.h, r.l, i.h, i.l);
-}
-
-// C = A B for k x k row-major matrices in shared memory (C distinct from A and B)
-__device__ void zdf_matmul(int k, const zdf *A, const zdf *B, zdf *C)
-{
-    for (int t = threadIdx.x; t < k * k; t += blockDim.x) {
-        const int i = t / k, j = t - i * k;
-        zdf s = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int q = 0; q < k; ++q) s = zdf_add(s, zdf_mul(A[i * k + q], B[q * k + j]));
-        C[t] = s;
-    }
-    __syncthreads();
-}
-
-// c = ||psi|| exp(-i dt H_k) e_1 as pamp_expm_block computes it (same arguments and outputs)
-__device__ void pamp_expm_block_df(const PampExpArgs &a, double dt, unsigned char *pe_smem)
-{
-    const int m = a.m, tid = threadIdx.x, nt = blockDim.x;
-    zdf *A = reinterpret_cast<zdf *>(pe_smem);
-    zdf *A2 = A + m * m, *P = A2 + m * m, *Q = P + m * m, *T = Q + m * m, *D = T + m * m;
-    __shared__ int k_sh, s_sh, piv_sh, bad_sh;
-    __shared__ double red[32];
-    const size_t cd = 2 * (size_t)(m + 2);
-    if (tid == 0) {  // happy breakdown (pamp.h:306-313): truncate at the first small subdiagonal
-        int k = m;
-        for (int j = 0; j + 1 < m; ++j)
-            if (a.cols[((size_t)j * 3 + 2) * cd + 2 * (j + 1) + 1] < a.tol) {
-                k = j + 1;
-                break;
-            }
-        k_sh = k;
-        bad_sh = 0;
-    }
-    __syncthreads();
-    const int k = k_sh;
-    // -i dt H_k in FP64: its largest magnitude sets the scaling
-    double mx = 0.0;
-    for (int t = tid; t < k * k; t += nt) {
-        const int i = t / k, j = t - i * k;
-        cxd h = mk<double>(0.0, 0.0);
-        if (i <= j) {
-            const double *p0 = a.cols + ((size_t)j * 3 + 0) * cd;
-            h = mk<double>(p0[2 * i], p0[2 * i + 1]);
-            if (a.double_ortho) {
-                const double *p1 = a.cols + ((size_t)j * 3 + 1) * cd;
-                h = h + mk<double>(p1[2 * i], p1[2 * i + 1]);
-            }
-        } else if (i == j + 1) {
-            h = mk<double>(a.cols[((size_t)j * 3 + 2) * cd + 2 * (j + 1) + 1], 0.0);
-        }
-        const cxd v = mk<double>(dt * h.y, -dt * h.x);
-        mx = fmax(mx, sqrt(v.x * v.x + v.y * v.y));
-        T[t] = zdf_make(v);  // unscaled, scaled below
-    }
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if ((tid & 31) == 0) red[tid >> 5] = mx;
-    __syncthreads();
-    if (tid == 0) {
-        double r = 0.0;
-        for (int w = 0; w < (nt + 31) / 32; ++w) r = fmax(r, red[w]);
-        s_sh = r > 0.0 ? max(0, (int)ceil(log2(r))) : 0;
-    }
-    __syncthreads();
-    const int sq = s_sh;
-    const float scale = ldexpf(1.0f, -sq);  // a power of two: exact on both parts
-    for (int t = tid; t < k * k; t += nt) {
-        const zdf v = T[t];
-        A[t] = make_float4(v.x * scale, v.y * scale, v.z * scale, v.w * scale);
-    }
-    __syncthreads();
-    zdf_matmul(k, A, A, A2);
-    const int order = 6;
-    double c[order + 1];
-    c[0] = 1.0;
-    for (int i = 0; i < order; ++i) c[i + 1] = c[i] * (double)(order - i) / (double)((i + 1) * (2 * order - i));
-    for (int t = tid; t < k * k; t += nt) {
-        const bool dg = (t / k) == (t % k);
-        Q[t] = zdf_make(mk<double>(dg ? c[order] : 0.0, 0.0));
-        P[t] = zdf_make(mk<double>(dg ? c[order - 1] : 0.0, 0.0));
-    }
-    __syncthreads();
-    bool odd = true;
-    for (int i = order - 2; i >= 0; --i) {
-        zdf *M = odd ? Q : P;
-        zdf_matmul(k, M, A2, T);
-        const zdf ci = zdf_make(mk<double>(c[i], 0.0));
-        for (int t = tid; t < k * k; t += nt) M[t] = (t / k) == (t % k) ? zdf_add(T[t], ci) : T[t];
-        __syncthreads();
-        odd = !odd;
-    }
-    {
-        zdf *M = odd ? Q : P;
-        zdf_matmul(k, M, A, T);
-        for (int t = tid; t < k * k; t += nt) M[t] = T[t];
-        __syncthreads();
-    }
-    for (int t = tid; t < k * k; t += nt) D[t] = zdf_sub(Q[t], P[t]);
-    __syncthreads();
-    for (int pc = 0; pc < k; ++pc) {
-        if (tid == 0) {
-            int r = pc;
-            double best = -1.0;
-            for (int i = pc; i < k; ++i) {
-                const cxd v = zdf_val(D[i * k + pc]);
-                const double mag = v.x * v.x + v.y * v.y;
-                if (mag > best) { best = mag; r = i; }
-            }
-            piv_sh = r;
-            if (best == 0.0) bad_sh = 1;
-        }
-        __syncthreads();
-        if (bad_sh) break;
-        const int r = piv_sh;
-        if (r != pc)
-            for (int j = tid; j < k; j += nt) {
-                zdf t0 = D[pc * k + j]; D[pc * k + j] = D[r * k + j]; D[r * k + j] = t0;
-                t0 = P[pc * k + j]; P[pc * k + j] = P[r * k + j]; P[r * k + j] = t0;
-            }
-        __syncthreads();
-        for (int i = pc + 1 + tid; i < k; i += nt)
-            D[i * k + pc] = zdf_make(cdiv(zdf_val(D[i * k + pc]), zdf_val(D[pc * k + pc])));
-        __syncthreads();
-        for (int t = tid; t < (k - pc - 1) * k; t += nt) {
-            const int i = pc + 1 + t / k, j = t % k;
-            const zdf l = D[i * k + pc];
-            if (j > pc) D[i * k + j] = zdf_sub(D[i * k + j], zdf_mul(l, D[pc * k + j]));
-            P[i * k + j] = zdf_sub(P[i * k + j], zdf_mul(l, P[pc * k + j]));
-        }
-        __syncthreads();
-    }
-    if (bad_sh) {
-        for (int t = tid; t < 2 * m; t += nt) a.c[t] = 0.0;
-        if (tid == 0) { a.stats[0] = k; a.stats[1] = 0.0; a.stats[2] = -1.0; }
-        __syncthreads();
-        return;
-    }
-    for (int j = tid; j < k; j += nt)
-        for (int i = k - 1; i >= 0; --i) {
-            zdf sum = P[i * k + j];
-            for (int q = i + 1; q < k; ++q) sum = zdf_sub(sum, zdf_mul(D[i * k + q], P[q * k + j]));
-            P[i * k + j] = zdf_make(cdiv(zdf_val(sum), zdf_val(D[i * k + i])));
-        }
-    __syncthreads();
-    zdf *E = P;  // +-(I + 2 X), then squared sq times
-    for (int t = tid; t < k * k; t += nt) {
-        zdf e = E[t];
-        e = make_float4(2.f * e.x, 2.f * e.y, 2.f * e.z, 2.f * e.w);
-        if ((t / k) == (t % k)) e = zdf_add(e, make_float4(1.f, 0.f, 0.f, 0.f));
-        E[t] = odd ? make_float4(-e.x, -e.y, -e.z, -e.w) : e;
-    }
-    __syncthreads();
-    for (int q = 0; q < sq; ++q) {
-        zdf_matmul(k, E, E, T);
-        for (int t = tid; t < k * k; t += nt) E[t] = T[t];
-        __syncthreads();
-    }
-    const double nrm = a.norm[1];
-    for (int i = tid; i < m; i += nt) {
-        const cxd v = i < k ? zdf_val(E[i * k]) : mk<double>(0.0, 0.0);
-        a.c[2 * i] = v.x * nrm;
-        a.c[2 * i + 1] = v.y * nrm;
-    }
-    if (tid == 0) {
-        const cxd last = zdf_val(E[(k - 1) * k]);
-        a.stats[0] = k;
-        a.stats[1] = last.x * last.x + last.y * last.y;
-        a.stats[2] = 0.0;
-    }
-    __syncthreads();
-}
-
 // (h, l) += a (bh + bl) in double-float arithmetic: a bh exactly as ph + pl (FMA), a bl added to
 // the low part, the high parts summed by Knuth's two-sum
 __device__ __forceinline__ void df_madd(float &h, float &l, float a, float bh, float bl)

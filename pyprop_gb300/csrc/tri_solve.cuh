@@ -38,6 +38,13 @@ __device__ __forceinline__ cx<double> tri_ld(const cx<double> *p)
     const double2 v = __ldcg((const double2 *)p);
     return mk<double>(v.x, v.y);
 }
+// factor loads from global memory (through L2) or, with SMEM_TAB, from tables the caller
+// staged in shared memory
+template <bool SMEM_TAB, typename C> __device__ __forceinline__ C tri_ldt(const C *p)
+{
+    if constexpr (SMEM_TAB) return *p;
+    else return tri_ld(p);
+}
 
 // Blocked triangular solves, parallel over the blocks of a fibre. With T_b the 32x32 diagonal
 // block of block b and C_b its coupling to the w boundary values s of the neighbouring block
@@ -56,7 +63,8 @@ __device__ __forceinline__ cx<double> tri_ld(const cx<double> *p)
 // tri_solve_smem runs both sweeps with the CTA's NW warps on xs ([nblk*32], zero past the
 // fibre's end) for factor m; sb ([nblk*w]) and sg ([nblk][w][32], when g_in_smem) are shared
 // scratch. Callers synchronise the CTA before the call; it returns after a CTA barrier.
-template <typename R, typename C, int NW>
+// SMEM_TAB: the factor tables (inv, g, rb) are in shared memory (g_in_smem is then 0).
+template <typename R, typename C, int NW, bool SMEM_TAB = false>
 __device__ __forceinline__ void tri_solve_smem(int nblk, int w, size_t m, const C *__restrict__ lo_inv,
                                                const C *__restrict__ lo_g, const C *__restrict__ lo_rb,
                                                const C *__restrict__ up_inv, const C *__restrict__ up_g,
@@ -77,12 +85,12 @@ __device__ __forceinline__ void tri_solve_smem(int nblk, int w, size_t m, const 
 #pragma unroll 1
         for (int q0 = 0; q0 < 32; q0 += 16) {
 #pragma unroll
-            for (int q = 0; q < 16; ++q) coef_fma(acc[q & 3], tri_ld(ib + (q0 + q) * 32 + lane), shfl_cx(r, q0 + q));
+            for (int q = 0; q < 16; ++q) coef_fma(acc[q & 3], tri_ldt<SMEM_TAB>(ib + (q0 + q) * 32 + lane), shfl_cx(r, q0 + q));
         }
         xs[blk * 32 + lane] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
         if (g_in_smem) {
             const C *gb = g + (m * nblk + blk) * gstride;
-            for (int c = 0; c < w; ++c) sg[((size_t)blk * w + c) * 32 + lane] = tri_ld(gb + c * 32 + lane);
+            for (int c = 0; c < w; ++c) sg[((size_t)blk * w + c) * 32 + lane] = tri_ldt<SMEM_TAB>(gb + c * 32 + lane);
         }
     };
     // s = Rb z[boundary rows]: each warp takes BRW consecutive output rows at a time, lanes
@@ -107,8 +115,8 @@ __device__ __forceinline__ void tri_solve_smem(int nblk, int w, size_t m, const 
                     const int row = row0 + q, bo = row / w;
                     const bool nza = ca < c_hi && row < nb && (lower ? bca <= bo : bca >= bo);
                     const bool nzb = cb < c_hi && row < nb && (lower ? bcb <= bo : bcb >= bo);
-                    va[q] = nza ? tri_ld(Rm + (size_t)row * nb + ca) : C();
-                    vb[q] = nzb ? tri_ld(Rm + (size_t)row * nb + cb) : C();
+                    va[q] = nza ? tri_ldt<SMEM_TAB>(Rm + (size_t)row * nb + ca) : C();
+                    vb[q] = nzb ? tri_ldt<SMEM_TAB>(Rm + (size_t)row * nb + cb) : C();
                 }
                 const cx<R> za = ca < c_hi ? xs[bca * 32 + r0 + (ca - bca * w)] : mk<R>((R)0, (R)0);
                 const cx<R> zb = cb < c_hi ? xs[bcb * 32 + r0 + (cb - bcb * w)] : mk<R>((R)0, (R)0);
@@ -139,7 +147,7 @@ __device__ __forceinline__ void tri_solve_smem(int nblk, int w, size_t m, const 
                 for (int c = 0; c < w; ++c) coef_fms(y, gb[c * 32 + lane], sb[nbk * w + c]);
             } else {
                 const C *gb = g + (m * nblk + blk) * gstride;
-                for (int c = 0; c < w; ++c) coef_fms(y, tri_ld(gb + c * 32 + lane), sb[nbk * w + c]);
+                for (int c = 0; c < w; ++c) coef_fms(y, tri_ldt<SMEM_TAB>(gb + c * 32 + lane), sb[nbk * w + c]);
             }
         }
         return y;

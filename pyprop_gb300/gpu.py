@@ -341,12 +341,41 @@ class PampStepper:
         self.h = h
         self.stats = nat.KrylovStats()
 
-    def step(self, psi, dt, scales):
+    def step(self, psi, dt, scales, want_stats=True):
+        """One step; with ``want_stats`` the call waits for it and returns the statistics,
+        otherwise it only enqueues (where the exponential runs on the device) and returns None."""
         sc = np.ascontiguousarray(scales, dtype=np.complex128)
         _, sp = nat.dptr(sc.view(np.float64))
         self.ctx.bind_stream()
-        check(self.lib.pg_pamp_step(self.h, ptr(psi), float(dt), sp, len(sc), C.byref(self.stats)), "pg_pamp_step")
+        check(self.lib.pg_pamp_step(self.h, ptr(psi), float(dt), sp, len(sc),
+                                    C.byref(self.stats) if want_stats else None), "pg_pamp_step")
+        return self.stats if want_stats else None
+
+    def last_stats(self):
+        self.ctx.bind_stream()
+        check(self.lib.pg_pamp_last_stats(self.h, C.byref(self.stats)), "pg_pamp_last_stats")
         return self.stats
+
+    def set_fused(self, on):
+        """Single-kernel step (complex64 basis; the default where the operators qualify) or the
+        graphs. Returns whether the single-kernel step is now selected."""
+        code = self.lib.pg_pamp_set_fused(self.h, int(bool(on)))
+        if on and code in (nat.PG_ERR_STATE, nat.PG_ERR_STORAGE, nat.PG_ERR_SHAPE):
+            return False
+        check(code, "pg_pamp_set_fused")
+        return bool(on)
+
+    def set_barrier_probe(self, extra_arrivals, at_barrier=0):
+        """Test hook: grid barrier number ``at_barrier`` of later single-kernel steps waits for
+        arrivals that never come (its bounded polls run out; error word 2)."""
+        check(self.lib.pg_pamp_set_barrier_probe(self.h, int(extra_arrivals), int(at_barrier)),
+              "pg_pamp_set_barrier_probe")
+
+    def set_device_exp(self, on):
+        """Graph path: True runs the m x m exponential on the device (basis of at most 48
+        vectors; a step never waits for the host), False (default) on the host between two
+        graphs (faster on this GPU, whose FP64 arithmetic is scarce)."""
+        check(self.lib.pg_pamp_set_device_exp(self.h, int(bool(on))), "pg_pamp_set_device_exp")
 
     def __del__(self):
         try:

@@ -12,8 +12,11 @@ A config switches to these by naming them: ``propagator = PamPropagatorGPU`` or
 ``CayleyPropagatorGPU``, ``base_propagator = BasisPropagatorGPU`` (``BasisPropagator`` is
 accepted as the same class). GPU-only keys in [Propagation]: ``gpu_precision``
 ("fp64" or "fp32": precision of the Krylov basis and of the operator it multiplies);
-``gpu_fused_step`` (default True: a mixed-precision Cayley step of a one-electron banded
-operator runs as one cooperative kernel; False keeps the captured multi-kernel step).
+``gpu_fused_step`` (default True: a mixed-precision Cayley or pAMP step of a one-electron
+banded operator runs as one cooperative kernel; False keeps the captured multi-kernel step);
+``gpu_step_stats`` (default True: each step waits and keeps its statistics; False only
+enqueues, and the statistics are read when asked for); ``gpu_device_exponential`` (pAMP graph
+path, default False: the m x m exponential on the host between two graphs; True on the device).
 """
 from __future__ import annotations
 
@@ -154,6 +157,9 @@ class PamPropagatorGPU(PropagatorBase):
         method = getattr(conf, "krylov_exponentiation_method", 0)
         if method not in (0, "pade", "Pade"):
             _log.warning("krylov_exponentiation_method=%r: the GPU path uses the Pade exponential", method)
+        self.StepStats = bool(getattr(conf, "gpu_step_stats", True))
+        self.DeviceExponential = bool(getattr(conf, "gpu_device_exponential", False))
+        self.FusedStep = bool(getattr(conf, "gpu_fused_step", True))
 
     def SetupStep(self, dt):
         self.BasePropagator.SetupStep(dt)
@@ -165,10 +171,29 @@ class PamPropagatorGPU(PropagatorBase):
         self.ovlb = self.ovl64 if self.Precision == nat.PG_FP64 else Banded.overlap(self.opb, repr_.overlap_rows)
         self.stepper = PampStepper(self.op64, self.opb, self.ovl64, self.ovlb, self.BasisSize, self.Precision,
                                    self.DoubleOrthogonalization)
+        if self.DeviceExponential and self.BasisSize <= 48:
+            self.stepper.set_device_exp(True)
+        # the single-kernel step (complex64 basis) where it qualifies
+        self.Fused = self.stepper.set_fused(self.FusedStep and self.Precision == nat.PG_FP32)
 
     def AdvanceStep(self, t, dt):
+        """One step at H(t). With ``gpu_step_stats`` (default) the call waits for the step and
+        keeps its statistics; otherwise it only enqueues and ``GetErrorEstimate`` waits."""
         scales = self.op64.scales(t)
-        self.LastStats = self.stepper.step(self.psi.GetData(), dt, scales)
+        self._last_stats = None
+        st = self.stepper.step(self.psi.GetData(), dt, scales, want_stats=self.StepStats)
+        if st is not None:
+            self.LastStats = st
+
+    @property
+    def LastStats(self):
+        if getattr(self, "_last_stats", None) is None:
+            self._last_stats = self.stepper.last_stats()
+        return self._last_stats
+
+    @LastStats.setter
+    def LastStats(self, value):
+        self._last_stats = value
 
     def MultiplyHamiltonian(self, srcPsi, destPsi, t, dt):
         self.BasePropagator.MultiplyHamiltonian(srcPsi, destPsi, t, dt)

@@ -104,11 +104,12 @@ def test_pamp_ensemble_matches_single_members(gpu, precision):
         if precision == "fp64":
             assert relerr(b.psi.numpy(), a.psi.numpy()) < tol, relerr(b.psi.numpy(), a.psi.numpy())
         else:
-            # complex64 bases (the ensemble's persistent kernel, the lone member's kernels): both
-            # within the FP32 Krylov error of the complex128-basis result, which dt ||H_m|| scales
+            # complex64 bases (the ensemble's step; the lone member's single-kernel step, whose
+            # Krylov vectors are U^-1 V in complex64): both within the FP32 Krylov error of the
+            # complex128-basis result, which dt ||H_m|| scales
             e_lone = relerr(a.psi.numpy(), exact[k].psi.numpy())
             e_ens = relerr(b.psi.numpy(), exact[k].psi.numpy())
-            assert e_lone < 1e-5 and e_ens < 5 * e_lone + 1e-7, (e_ens, e_lone)
+            assert e_lone < 5e-5 and e_ens < 5 * e_lone + 1e-7, (e_ens, e_lone)
         assert st["Iterations"] == 20
         assert 0.0 <= st["ErrorEstimate"] < 1e-6
         assert abs(a.PropagatedTime - b.PropagatedTime) < 1e-12

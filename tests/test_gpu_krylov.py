@@ -53,6 +53,108 @@ def test_pamp_steps_against_oracle_fp64_and_fp32(gpu):
         assert abs(ham.norm(out) - ham.norm(psi_ref)) < 10 * tol_rel
 
 
+def test_pamp_device_exponential_matches_host_exponential(gpu):
+    """The step with the m x m exponential on the device (one graph, no wait) against the step
+    that computes it on the host between two graphs: same states, same statistics, read on
+    demand after steps that did not wait."""
+    g = golden("hydrogen_small.npz")
+    t0, dt, nsteps = 1.0, 0.01, 10
+    outs, stats = {}, {}
+    for dev in (True, False):
+        prob = hydrogen_problem(propagator="PamPropagatorGPU", precision="fp64")
+        prob.SetupStep(skipWavefunctionSetup=True)
+        prob.Propagator.stepper.set_device_exp(dev)
+        prob.Propagator.StepStats = False
+        _set_psi(prob, g["psi"])
+        for n in range(nsteps):
+            prob.Propagator.AdvanceStep(t0 + n * dt, dt)
+        st = prob.Propagator.LastStats
+        stats[dev] = (st.OpCount, st.Iterations, st.ErrorEstimate)
+        outs[dev] = prob.psi.numpy()
+    # the host takes the Hermitian tridiagonal H_m by implicit QL, the device the scaled Pade:
+    # both within rounding of the exact exponential
+    assert relerr(outs[True], outs[False]) < 1e-11
+    assert stats[True][:2] == stats[False][:2] == (20 * nsteps, 20)
+    assert stats[True][2] < 1e-20 and stats[False][2] < 1e-20
+    # a basis above the device exponential's limit keeps the host path
+    big = hydrogen_problem(propagator="PamPropagatorGPU", precision="fp64", krylov_basis_size=60)
+    big.SetupStep(skipWavefunctionSetup=True)
+    with pytest.raises(nat.PygpuError):
+        big.Propagator.stepper.set_device_exp(True)
+
+
+def test_pamp_single_kernel_step_matches_graphs_and_oracle(gpu):
+    """The single-kernel complex64-basis pAMP step (Arnoldi on T_j = U^-1 V_j, the exponential
+    in every CTA, one launch per step) against the oracle's complex128 steps and against the
+    captured graphs with the same complex64 basis, over 10 steps enqueued without waiting."""
+    from oracle.propagators import OraclePam
+    g = golden("hydrogen_small.npz")
+    ref = hydrogen_problem()
+    ham = oracle_hamiltonian(ref)
+    pam = OraclePam(ham, 20, True)
+    psi_ref = g["psi"].copy()
+    t0, dt, nsteps = 1.0, 0.01, 10
+    for n in range(nsteps):
+        psi_ref = pam.step(psi_ref, t0 + n * dt, dt)
+    S = ham.overlap.S
+    outs = {}
+    for fused in (True, False):
+        prob = hydrogen_problem(propagator="PamPropagatorGPU", precision="fp32")
+        prob.SetupStep(skipWavefunctionSetup=True)
+        assert prob.Propagator.Fused
+        if not fused:
+            assert not prob.Propagator.stepper.set_fused(False)
+        prob.Propagator.StepStats = False
+        ctx = prob.Propagator.op64.ctx
+        _set_psi(prob, g["psi"])
+        l0 = ctx.launches()
+        for n in range(nsteps):
+            prob.Propagator.AdvanceStep(t0 + n * dt, dt)
+        st = prob.Propagator.LastStats
+        assert st.Iterations == 20 and 0.0 <= st.ErrorEstimate < 1e-10
+        if fused:
+            assert ctx.launches() - l0 == nsteps
+        outs[fused] = prob.psi.numpy()
+    for fused, out in outs.items():
+        assert relerr(out, psi_ref) < 5e-5, fused
+        assert infidelity(psi_ref, out, S) < 1e-9, fused
+        assert abs(ham.norm(out) - ham.norm(psi_ref)) < 5e-6, fused
+    assert relerr(outs[True], outs[False]) < 5e-5
+
+
+@pytest.mark.parametrize("at_barrier", [0, 5])
+def test_pamp_single_kernel_step_bounded_barrier_wait(gpu, at_barrier):
+    """A grid barrier of the single-kernel pAMP step whose arrivals never all come (the test
+    hook adds one that no CTA makes; barrier 0 is the norm's, barrier 5 the third Arnoldi
+    step's first) gives up after its bounded polls: the call reports PG_ERR_NOT_CONVERGED, the
+    device error word reads 2, psi is unchanged, and once the word is cleared the next step
+    equals a fresh stepper's."""
+    g = golden("hydrogen_small.npz")
+    prob = hydrogen_problem(propagator="PamPropagatorGPU", precision="fp32")
+    prob.SetupStep(skipWavefunctionSetup=True)
+    assert prob.Propagator.Fused
+    stepper = prob.Propagator.stepper
+    ctx = prob.Propagator.op64.ctx
+    _set_psi(prob, g["psi"])
+    scales = prob.Propagator.op64.scales(1.0)
+    ctx.clear_device_error()
+    stepper.set_barrier_probe(1, at_barrier)
+    with pytest.raises(nat.PygpuError) as exc:
+        stepper.step(prob.psi.GetData(), 0.01, scales)
+    assert exc.value.code == nat.PG_ERR_NOT_CONVERGED
+    assert ctx.device_error() == 2
+    assert relerr(prob.psi.numpy(), g["psi"]) == 0.0
+    stepper.set_barrier_probe(0, 0)
+    ctx.clear_device_error()
+    stepper.step(prob.psi.GetData(), 0.01, scales)
+    assert ctx.device_error() == 0
+    ref = hydrogen_problem(propagator="PamPropagatorGPU", precision="fp32")
+    ref.SetupStep(skipWavefunctionSetup=True)
+    _set_psi(ref, g["psi"])
+    ref.Propagator.stepper.step(ref.psi.GetData(), 0.01, scales)
+    assert relerr(prob.psi.numpy(), ref.psi.numpy()) < 1e-13
+
+
 def test_cayley_step_fp64_matches_golden(gpu):
     g = golden("hydrogen_small.npz")
     prob = hydrogen_problem(propagator="CayleyPropagatorGPU", precision="fp64", gmres_tolerance=1e-13)
