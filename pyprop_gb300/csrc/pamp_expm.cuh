@@ -220,14 +220,23 @@ static __device__ __forceinline__ dff df_add(dff a, dff b)
     const float h = s + e;
     return {h, e - (h - s)};
 }
+// (products whose rounded value enters a two-sum are formed with __fmul_rn, which the
+// compiler never contracts into an FMA with a following addition)
 static __device__ __forceinline__ dff df_mul(dff a, dff b)
 {
-    const float p = a.h * b.h;
+    const float p = __fmul_rn(a.h, b.h);
     const float e = fmaf(a.h, b.l, fmaf(a.l, b.h, fmaf(a.h, b.h, -p)));
     const float h = p + e;
     return {h, e - (h - p)};
 }
 static __device__ __forceinline__ dff df_neg(dff a) { return {-a.h, -a.l}; }
+// 1 / a: the FP32 reciprocal refined by one Newton step in double-float arithmetic
+static __device__ __forceinline__ dff df_recip(dff a)
+{
+    const dff x{1.0f / a.h, 0.f};
+    const dff r = df_add({1.0f, 0.f}, df_neg(df_mul(a, x)));  // 1 - a x
+    return df_add(x, df_mul(x, r));
+}
 
 typedef float4 zdf;  // (re hi, re lo, im hi, im lo)
 static const int PE_DF_MAXM = 64;  // largest basis of the double-float exponential
@@ -251,24 +260,79 @@ static __device__ __forceinline__ zdf zdf_mul(zdf a, zdf b)
     return make_float4(r.h, r.l, i.h, i.l);
 }
 
-// C = A B for k x k row-major matrices in shared memory (C distinct from A and B); each
-// element's sum runs as four independent chains (the double-float additions are long
-// dependent sequences, so one chain per element would leave the SM waiting on latency)
+// 1 / d = conj(d) / |d|^2 in double-float arithmetic; false when |d|^2 is zero or not finite
+static __device__ __forceinline__ bool zdf_recip(zdf d, zdf &out)
+{
+    const dff re{d.x, d.y}, im{d.z, d.w};
+    const dff n2 = df_add(df_mul(re, re), df_mul(im, im));
+    if (!(n2.h > 0.f && n2.h < 3e38f)) return false;
+    const dff inv = df_recip(n2);
+    const dff r = df_mul(re, inv), i = df_neg(df_mul(im, inv));
+    out = make_float4(r.h, r.l, i.h, i.l);
+    return true;
+}
+
+// Accumulated real product in double-float arithmetic, in the manner of the compensated dot
+// product (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26,
+// 2005): s + c += a b with a, b double-float; the high product split exactly by an FMA, the
+// cross terms and the two-sum error gathered in c, renormalised once at the end.
+struct dacc {
+    float s, c;
+};
+static __device__ __forceinline__ void dacc_madd(dacc &u, float ah, float al, float bh, float bl)
+{
+    const float p = __fmul_rn(ah, bh);
+    const float e = fmaf(ah, bl, fmaf(al, bh, fmaf(ah, bh, -p)));
+    const float t = u.s + p;
+    const float bb = t - u.s;
+    u.c += ((u.s - (t - bb)) + (p - bb)) + e;
+    u.s = t;
+}
+static __device__ __forceinline__ void dacc_merge(dacc &u, const dacc &v)
+{
+    const float t = u.s + v.s;
+    const float bb = t - u.s;
+    u.c += ((u.s - (t - bb)) + (v.s - bb)) + v.c;
+    u.s = t;
+}
+static __device__ __forceinline__ float2 dacc_val(const dacc &u)
+{
+    const float h = u.s + u.c;
+    return make_float2(h, u.c - (h - u.s));
+}
+
+// C = A B for k x k row-major matrices in shared memory (C distinct from A and B): each
+// element's real and imaginary sums as two compensated chains over alternate terms (four
+// chains in flight per thread)
 static __device__ void zdf_matmul(int k, const zdf *A, const zdf *B, zdf *C)
 {
     for (int t = threadIdx.x; t < k * k; t += blockDim.x) {
         const int i = t / k, j = t - i * k;
-        const zdf z = make_float4(0.f, 0.f, 0.f, 0.f);
-        zdf s0 = z, s1 = z, s2 = z, s3 = z;
+        dacc r0{0.f, 0.f}, r1{0.f, 0.f}, i0{0.f, 0.f}, i1{0.f, 0.f};
         int q = 0;
-        for (; q + 3 < k; q += 4) {
-            s0 = zdf_add(s0, zdf_mul(A[i * k + q], B[q * k + j]));
-            s1 = zdf_add(s1, zdf_mul(A[i * k + q + 1], B[(q + 1) * k + j]));
-            s2 = zdf_add(s2, zdf_mul(A[i * k + q + 2], B[(q + 2) * k + j]));
-            s3 = zdf_add(s3, zdf_mul(A[i * k + q + 3], B[(q + 3) * k + j]));
+        for (; q + 1 < k; q += 2) {
+            const zdf a0 = A[i * k + q], b0 = B[q * k + j];
+            const zdf a1 = A[i * k + q + 1], b1 = B[(q + 1) * k + j];
+            dacc_madd(r0, a0.x, a0.y, b0.x, b0.y);
+            dacc_madd(r0, -a0.z, -a0.w, b0.z, b0.w);
+            dacc_madd(i0, a0.x, a0.y, b0.z, b0.w);
+            dacc_madd(i0, a0.z, a0.w, b0.x, b0.y);
+            dacc_madd(r1, a1.x, a1.y, b1.x, b1.y);
+            dacc_madd(r1, -a1.z, -a1.w, b1.z, b1.w);
+            dacc_madd(i1, a1.x, a1.y, b1.z, b1.w);
+            dacc_madd(i1, a1.z, a1.w, b1.x, b1.y);
         }
-        for (; q < k; ++q) s0 = zdf_add(s0, zdf_mul(A[i * k + q], B[q * k + j]));
-        C[t] = zdf_add(zdf_add(s0, s1), zdf_add(s2, s3));
+        if (q < k) {
+            const zdf a0 = A[i * k + q], b0 = B[q * k + j];
+            dacc_madd(r0, a0.x, a0.y, b0.x, b0.y);
+            dacc_madd(r0, -a0.z, -a0.w, b0.z, b0.w);
+            dacc_madd(i0, a0.x, a0.y, b0.z, b0.w);
+            dacc_madd(i0, a0.z, a0.w, b0.x, b0.y);
+        }
+        dacc_merge(r0, r1);
+        dacc_merge(i0, i1);
+        const float2 re = dacc_val(r0), im = dacc_val(i0);
+        C[t] = make_float4(re.x, re.y, im.x, im.y);
     }
     __syncthreads();
 }
@@ -377,8 +441,8 @@ static __device__ void pamp_expm_block_df(const PampExpArgs &a, double dt, unsig
     __syncthreads();
     // LU with partial pivoting, two CTA barriers per column: warp 0 finds the pivot (largest
     // magnitude, the first on ties; high parts in FP32), swaps the rows and forms the pivot's
-    // reciprocal (one FP64 division); then every thread eliminates its elements of the rows
-    // below with its own multiplier D[i][pc] / pivot (no FP64 division per element)
+    // reciprocal (double-float Newton step); then every thread eliminates its elements of the
+    // rows below with its own multiplier D[i][pc] / pivot (no division per element)
     for (int pc = 0; pc < k; ++pc) {
         if (tid < 32) {
             float best = -1.f;
@@ -400,9 +464,8 @@ static __device__ void pamp_expm_block_df(const PampExpArgs &a, double dt, unsig
                 }
             __syncwarp();
             if (tid == 0) {
-                const cxd d = zdf_val(D[pc * k + pc]);
-                const double den = d.x * d.x + d.y * d.y;
-                if (den > 0.0 && den < 1e300) rinv[pc] = zdf_make(mk<double>(d.x / den, -d.y / den));
+                zdf r;
+                if (zdf_recip(D[pc * k + pc], r)) rinv[pc] = r;
                 else bad_sh = 1;
             }
         }

@@ -62,17 +62,20 @@ __device__ __forceinline__ void pf_acc(float &h, float &l, float ph, float pl)
 // (h, l) += a b, the product split exactly by an FMA
 __device__ __forceinline__ void pf_madd(float &h, float &l, float a, float b)
 {
-    const float q = a * b;
+    const float q = __fmul_rn(a, b);  // never contracted into an FMA with the two-sum
     pf_acc(h, l, q, fmaf(a, b, -q));
 }
 
 // out[2q], out[2q+1] = <T_q, y> for q < J (T_q at Tr + q tld) and, with zx, out[2J] =
-// Re <zx, y>: warp w takes the columns w, w + FZ_NW, ...; its lanes stride over the N elements
-// and the 32 lane sums are combined by shuffles, all in double-float arithmetic on the
-// complex64 products. No CTA barrier inside (the grid barrier that follows has one).
+// Re <zx, y>, each as a double-float pair (high, low) in the 8-byte slot: warp w takes the
+// columns w, w + FZ_NW, ...; its lanes stride over the N elements and the 32 lane sums are
+// combined by shuffles, all in double-float arithmetic on the complex64 products (the FP64
+// pipe of this GPU is too narrow for per-element FP64 sums). No CTA barrier inside (the grid
+// barrier that follows has one).
 __device__ __forceinline__ void pf_dots(const cxf *Tr, long long tld, int J, const cxf *y, const cxf *zx, int N,
-                                        double *out)
+                                        double *outd)
 {
+    float2 *out = reinterpret_cast<float2 *>(outd);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int ncol = J + (zx ? 1 : 0);
     for (int q = warp; q < ncol; q += FZ_NW) {
@@ -93,10 +96,45 @@ __device__ __forceinline__ void pf_dots(const cxf *Tr, long long tld, int J, con
             pf_acc(yh, yl, oyh, oyl);
         }
         if (lane == 0) {
-            out[2 * q] = (double)xh + (double)xl;
-            if (q < J) out[2 * q + 1] = (double)yh + (double)yl;
+            out[2 * q] = make_float2(xh, xl);
+            if (q < J) out[2 * q + 1] = make_float2(yh, yl);
         }
     }
+}
+
+// out[t] = sum over the channels a < nch of the double-float partials part[a][t], t < nval:
+// one warp per value (two values' loads in flight together), the channels over the lanes,
+// double-float shuffles in a fixed order (the same in every CTA), one FP64 sum at the end.
+// Ends with a CTA barrier.
+__device__ __forceinline__ void pf_reduce(const double *part, int nch, int nval, double *out)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int t0 = warp; t0 < nval; t0 += 2 * FZ_NW) {
+        float h[2] = {0.f, 0.f}, l[2] = {0.f, 0.f};
+        for (int a = lane; a < nch; a += 32) {
+            float2 v[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int t = t0 + u * FZ_NW;
+                v[u] = t < nval ? __ldcg(reinterpret_cast<const float2 *>(part + (size_t)a * FZ_PSTRIDE + t))
+                                : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) pf_acc(h[u], l[u], v[u].x, v[u].y);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const float oh = __shfl_xor_sync(0xffffffffu, h[u], o), ol = __shfl_xor_sync(0xffffffffu, l[u], o);
+                pf_acc(h[u], l[u], oh, ol);
+            }
+        if (lane == 0)
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+                if (t0 + u * FZ_NW < nval) out[t0 + u * FZ_NW] = (double)h[u] + (double)l[u];
+    }
+    __syncthreads();
 }
 
 // Stage bytes (a multiple of 4) at src into shared memory at dst with asynchronous copies of
@@ -238,7 +276,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) pamp_fused_step_kernel(PfArgs p
         // h1 = T^H y
         pf_dots(Tr, tld, J, ys, nullptr, N, part_me + P_H1 * pstride);
         if (!fz_grid_sync(a.bar, expect, ordinal, a, &s_ok)) return;
-        fz_reduce(a.part + P_H1 * pstride, a.nch, 2 * J, h1d);
+        pf_reduce(a.part + P_H1 * pstride, a.nch, 2 * J, h1d);
         if (tid < J) hs[tid] = mk<float>((float)h1d[2 * tid], (float)h1d[2 * tid + 1]);
         __syncthreads();
         // z' = z - T h1, published for the next products
@@ -265,28 +303,33 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) pamp_fused_step_kernel(PfArgs p
         __syncthreads();
         pf_dots(Tr, tld, J, ys, xs, N, part_me + P_H2 * pstride);
         if (!fz_grid_sync(a.bar, expect, ordinal, a, &s_ok)) return;
-        fz_reduce(a.part + P_H2 * pstride, a.nch, 2 * J + 1, h2d);
+        pf_reduce(a.part + P_H2 * pstride, a.nch, 2 * J + 1, h2d);
         if (tid < J) hs[tid] = mk<float>((float)h2d[2 * tid], (float)h2d[2 * tid + 1]);
         __syncthreads();
         // z'' = z' - T h2 (the next T_j; the other CTAs form it themselves)
         for (int i = tid; i < N; i += FZ_THREADS) xs[i] = fz_gs_update<false>(xs[i], Tr + i, tld, J, hs);
-        if (tid == 0) {
-            double b2 = h2d[2 * J];
-            for (int q = 0; q < J; ++q) b2 -= h2d[2 * q] * h2d[2 * q] + h2d[2 * q + 1] * h2d[2 * q + 1];
-            double beta = sqrt(fmax(b2, 0.0));
-            if (!(beta == beta)) beta = 0.0;
+        if (tid < 32) {
             // Hessenberg column j in the layout the exponential reads (pass 0 h1, pass 1 h2,
-            // pass 2 the subdiagonal beta at 2J + 1)
-            for (int q = 0; q < J; ++q) {
+            // pass 2 the subdiagonal beta at 2J + 1); beta^2 = ||z'||_S^2 - |h2|^2
+            double sq = 0.0;
+            for (int q = tid; q < J; q += 32) {
+                sq = fma(h2d[2 * q], h2d[2 * q], sq);
+                sq = fma(h2d[2 * q + 1], h2d[2 * q + 1], sq);
                 hc[((size_t)j * 3 + 0) * cd + 2 * q] = h1d[2 * q];
                 hc[((size_t)j * 3 + 0) * cd + 2 * q + 1] = h1d[2 * q + 1];
                 hc[((size_t)j * 3 + 1) * cd + 2 * q] = h2d[2 * q];
                 hc[((size_t)j * 3 + 1) * cd + 2 * q + 1] = h2d[2 * q + 1];
             }
-            hc[((size_t)j * 3 + 2) * cd + 2 * J + 1] = beta;
-            s_k = J;
-            s_inv = (float)(beta > 0.0 ? 1.0 / beta : 0.0);
-            s_cont = (J < m && beta >= p.tol) ? 1 : 0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+            if (tid == 0) {
+                double beta = sqrt(fmax(h2d[2 * J] - sq, 0.0));
+                if (!(beta == beta)) beta = 0.0;
+                hc[((size_t)j * 3 + 2) * cd + 2 * J + 1] = beta;
+                s_k = J;
+                s_inv = beta > 0.0 ? 1.0f / (float)beta : 0.f;
+                s_cont = (J < m && beta >= p.tol) ? 1 : 0;
+            }
         }
         __syncthreads();
     }

@@ -321,7 +321,7 @@ __device__ void pm_solve_cta(const cx<R> *b, double sc, cx<R> *vout, cx<R> *x, i
 // the low part, the high parts summed by Knuth's two-sum
 __device__ __forceinline__ void df_madd(float &h, float &l, float a, float bh, float bl)
 {
-    const float ph = a * bh;
+    const float ph = __fmul_rn(a, bh);  // never contracted into an FMA with the two-sum below
     const float pl = fmaf(a, bh, -ph) + a * bl;
     const float s = h + ph;
     const float bb = s - h;
