@@ -347,15 +347,21 @@ static __device__ void pamp_expm_block_df(const PampExpArgs &a, double dt, unsig
     __shared__ float red[32];
     __shared__ zdf rinv[PE_DF_MAXM];  // reciprocals of the LU pivots
     const size_t cd = 2 * (size_t)(m + 2);
-    if (tid == 0) {  // happy breakdown (pamp.h:306-313): truncate at the first small subdiagonal
+    if (tid < 32) {  // happy breakdown (pamp.h:306-313): truncate at the first small subdiagonal
         int k = m;
-        for (int j = 0; j + 1 < m; ++j)
-            if (a.cols[((size_t)j * 3 + 2) * cd + 2 * (j + 1) + 1] < a.tol) {
-                k = j + 1;
+        for (int j0 = 0; j0 + 1 < m; j0 += 32) {  // the subdiagonals loaded together, a ballot finds the first
+            const int j = j0 + tid;
+            const bool small = j + 1 < m && a.cols[((size_t)j * 3 + 2) * cd + 2 * (j + 1) + 1] < a.tol;
+            const unsigned bal = __ballot_sync(0xffffffffu, small);
+            if (bal) {
+                k = j0 + __ffs(bal);
                 break;
             }
-        k_sh = k;
-        bad_sh = 0;
+        }
+        if (tid == 0) {
+            k_sh = k;
+            bad_sh = 0;
+        }
     }
     __syncthreads();
     const int k = k_sh;
@@ -486,12 +492,33 @@ static __device__ void pamp_expm_block_df(const PampExpArgs &a, double dt, unsig
         __syncthreads();
         return;
     }
-    for (int j = tid; j < k; j += nt)
+    // back substitution, one warp per column of X: row i's sum over q > i by the lanes (a
+    // compensated product each, merged by shuffles in a fixed order), then lane 0 forms X[i][j]
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    for (int j = warp; j < k; j += nw) {
         for (int i = k - 1; i >= 0; --i) {
-            zdf sum = P[i * k + j];
-            for (int q = i + 1; q < k; ++q) sum = zdf_sub(sum, zdf_mul(D[i * k + q], P[q * k + j]));
-            P[i * k + j] = zdf_mul(sum, rinv[i]);
+            dacc sr{0.f, 0.f}, si{0.f, 0.f};
+            for (int q = i + 1 + lane; q < k; q += 32) {
+                const zdf d = D[i * k + q], x = P[q * k + j];
+                dacc_madd(sr, d.x, d.y, x.x, x.y);
+                dacc_madd(sr, -d.z, -d.w, x.z, x.w);
+                dacc_madd(si, d.x, d.y, x.z, x.w);
+                dacc_madd(si, d.z, d.w, x.x, x.y);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const dacc orr{__shfl_xor_sync(0xffffffffu, sr.s, o), __shfl_xor_sync(0xffffffffu, sr.c, o)};
+                const dacc oi{__shfl_xor_sync(0xffffffffu, si.s, o), __shfl_xor_sync(0xffffffffu, si.c, o)};
+                dacc_merge(sr, orr);
+                dacc_merge(si, oi);
+            }
+            if (lane == 0) {
+                const float2 r = dacc_val(sr), im = dacc_val(si);
+                P[i * k + j] = zdf_mul(zdf_sub(P[i * k + j], make_float4(r.x, r.y, im.x, im.y)), rinv[i]);
+            }
+            __syncwarp();
         }
+    }
     __syncthreads();
     zdf *E = P;  // +-(I + 2 X), then squared sq times
     for (int t = tid; t < k * k; t += nt) {
@@ -501,19 +528,51 @@ static __device__ void pamp_expm_block_df(const PampExpArgs &a, double dt, unsig
         E[t] = odd ? make_float4(-e.x, -e.y, -e.z, -e.w) : e;
     }
     __syncthreads();
-    for (int q = 0; q < sq; ++q) {
-        zdf_matmul(k, E, E, T);
-        for (int t = tid; t < k * k; t += nt) E[t] = T[t];
+    // all but the last rs squarings as matrix products (ping-pong between E and T); the first
+    // column of E^(2^rs) then by 2^rs - 1 products of E with its first column (one warp per
+    // row, compensated sums merged by shuffles)
+    const int rs = min(sq, 4);
+    zdf *F = T;
+    for (int q = 0; q < sq - rs; ++q) {
+        zdf_matmul(k, E, E, F);
+        zdf *tmp = E; E = F; F = tmp;
+    }
+    zdf *v = F, *w = F + k;  // F is free: two vectors of k
+    for (int i = tid; i < k; i += nt) v[i] = E[i * k];
+    __syncthreads();
+    for (int it = 0; it < (1 << rs) - 1; ++it) {
+        for (int i = warp; i < k; i += nw) {
+            dacc sr{0.f, 0.f}, si{0.f, 0.f};
+            for (int q = lane; q < k; q += 32) {
+                const zdf e = E[i * k + q], x = v[q];
+                dacc_madd(sr, e.x, e.y, x.x, x.y);
+                dacc_madd(sr, -e.z, -e.w, x.z, x.w);
+                dacc_madd(si, e.x, e.y, x.z, x.w);
+                dacc_madd(si, e.z, e.w, x.x, x.y);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const dacc orr{__shfl_xor_sync(0xffffffffu, sr.s, o), __shfl_xor_sync(0xffffffffu, sr.c, o)};
+                const dacc oi{__shfl_xor_sync(0xffffffffu, si.s, o), __shfl_xor_sync(0xffffffffu, si.c, o)};
+                dacc_merge(sr, orr);
+                dacc_merge(si, oi);
+            }
+            if (lane == 0) {
+                const float2 r = dacc_val(sr), im = dacc_val(si);
+                w[i] = make_float4(r.x, r.y, im.x, im.y);
+            }
+        }
         __syncthreads();
+        zdf *tmp = v; v = w; w = tmp;
     }
     const double nrm = a.norm[1];
     for (int i = tid; i < m; i += nt) {
-        const cxd v = i < k ? zdf_val(E[i * k]) : mk<double>(0.0, 0.0);
-        a.c[2 * i] = v.x * nrm;
-        a.c[2 * i + 1] = v.y * nrm;
+        const cxd val = i < k ? zdf_val(v[i]) : mk<double>(0.0, 0.0);
+        a.c[2 * i] = val.x * nrm;
+        a.c[2 * i + 1] = val.y * nrm;
     }
     if (tid == 0) {
-        const cxd last = zdf_val(E[(k - 1) * k]);
+        const cxd last = zdf_val(v[k - 1]);
         a.stats[0] = k;
         a.stats[1] = last.x * last.x + last.y * last.y;
         a.stats[2] = 0.0;

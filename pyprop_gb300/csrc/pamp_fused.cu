@@ -323,7 +323,11 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) pamp_fused_step_kernel(PfArgs p
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
             if (tid == 0) {
-                double beta = sqrt(fmax(h2d[2 * J] - sq, 0.0));
+                // sqrt from the FP32 reciprocal square root and one Newton step (few FP64 operations)
+                const double b2 = fmax(h2d[2 * J] - sq, 0.0);
+                const float r = b2 > 0.0 ? rsqrtf((float)b2) : 0.f;
+                const double x = (double)((float)b2 * r);
+                double beta = x + (b2 - x * x) * (0.5 * (double)r);
                 if (!(beta == beta)) beta = 0.0;
                 hc[((size_t)j * 3 + 2) * cd + 2 * J + 1] = beta;
                 s_k = J;
