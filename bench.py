@@ -1016,9 +1016,20 @@ def time_pamp_hydrogen_l10(torch, flush, steps=1000, warmup=5):
         torch.cuda.synchronize()
         total = sum(a.elapsed_time(b) for a, b in events) * 1e-3
         st = prob.Propagator.LastStats
+        if name == "fp32":
+            prob_fused = prob
         out[name] = {"steps_per_s": steps / total, "us_per_step": 1e6 * total / steps,
                      "kernels_per_step": (ctx.launches() - l0) / steps, "norm_after_pulse": prob.psi.GetNorm(),
                      "error_estimate_last_step": st.ErrorEstimate}
+    # the single-kernel step's roofline: algorithmic bytes of one complex64-basis step
+    peak, peak_kind = measured_peaks()
+    nbytes = pamp_member_bytes(prob_fused, 20)
+    ach = nbytes / (out["fp32"]["us_per_step"] * 1e-6) / 1e9
+    out["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                       "traffic": profile_traffic("pamp_fused_step_kernel_hydrogen_l10_n150.md"),
+                       "kernel": "pamp_fused_step_kernel<6,true>", "algorithmic_bytes": nbytes, "peak_kind": peak_kind,
+                       "note": "1.3 MB working set resident in L2 and shared memory: latency-bound (grid and CTA "
+                               "barriers)"}
     out["single_kernel_speedup_vs_graphs"] = out["fp32"]["steps_per_s"] / out["fp32_graphs"]["steps_per_s"]
     out["speedup_vs_plain_fp64"] = out["fp32"]["steps_per_s"] / out["fp64"]["steps_per_s"]
     out["parity"] = ("tests/test_gpu_parity.py: the whole pulse (40 vectors) and the first steps (20 vectors) against "
@@ -1085,6 +1096,23 @@ def profile_ensemble_pamp():
         ens.AdvanceStep()
     torch.cuda.synchronize()
     print(json.dumps({"profile": "ensemble_pamp", "shape": ens.launch_shape()}))
+
+
+def profile_pamp_l10():
+    """Profiling entry point: the single-wavefunction pAMP workload (hydrogen lmax 10, 150
+    B-splines, basis 20, complex64) on the single-kernel step, 7 steps from the 1s state."""
+    import torch
+    import pyprop_gb300 as pp
+    from pyprop_gb300.workloads import HYDROGEN_L10_PAMP, hydrogen
+    prob = pp.Problem(pp.LoadString(hydrogen(propagator="PamPropagatorGPU", precision="fp32", **HYDROGEN_L10_PAMP)))
+    prob.SetupStep(skipWavefunctionSetup=True)
+    prob.Propagator.StepStats = False
+    psi0, _ = initial_state(prob)
+    prob.psi.GetData().copy_(torch.as_tensor(psi0, device="cuda"))
+    for _ in range(7):
+        prob.AdvanceStep()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "pamp_l10", "fused": bool(prob.Propagator.Fused), "norm": prob.psi.GetNorm()}))
 
 
 # ---------------------------------------------------------------------------------------
@@ -1173,7 +1201,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=300,
                     help="oracle Cayley steps timed on one host core for cpu_baseline (0 = skip)")
     ap.add_argument("--two-electron", type=int, default=1, help="factorized two-electron matvec leg (0 = skip)")
-    ap.add_argument("--profile", choices=["matvec_hbm", "two_electron", "two_electron_large", "ensemble_pamp"],
+    ap.add_argument("--profile", choices=["matvec_hbm", "two_electron", "two_electron_large", "ensemble_pamp", "pamp_l10"],
                     default=None, help="profiling entry point instead of the benchmark")
     ap.add_argument("--fused-variant", type=int, default=0, choices=[0, 1, 2],
                     help="single-kernel Cayley step layout: 0 the cluster variant where it fits, 1 one CTA per "
@@ -1205,6 +1233,10 @@ def main():
     if args.profile == "two_electron_large":
         build_native.build()
         profile_two_electron_large()
+        return
+    if args.profile == "pamp_l10":
+        build_native.build()
+        profile_pamp_l10()
         return
     if args.profile == "ensemble_pamp":
         build_native.build()

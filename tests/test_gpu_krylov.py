@@ -122,6 +122,36 @@ def test_pamp_single_kernel_step_matches_graphs_and_oracle(gpu):
     assert relerr(outs[True], outs[False]) < 5e-5
 
 
+@pytest.mark.parametrize("kw", [dict(lmax=3, nbsplines=40, rmax=40.0, order=5),
+                                dict(lmax=5, nbsplines=600, rmax=300.0)])
+def test_pamp_single_kernel_step_other_layouts(gpu, kw):
+    """The single-kernel pAMP step on the generic band-width instance (B-splines of order 5) and
+    on a fibre whose solve factors do not fit in shared memory (600 B-splines: read through L2)
+    against the graphs with the same complex64 basis and the complex128-basis step: both
+    complex64 paths within the FP32 Krylov error of the complex128 result."""
+    t0, dt, nsteps = 1.0, 0.01, 5
+    rng = np.random.default_rng(7)
+    out = {}
+    psi0 = None
+    for name, prec, fused in (("fused", "fp32", True), ("graphs", "fp32", False), ("exact", "fp64", False)):
+        prob = hydrogen_problem(propagator="PamPropagatorGPU", precision=prec, amplitude=0.05, **kw)
+        prob.SetupStep(skipWavefunctionSetup=True)
+        if prec == "fp32":
+            assert prob.Propagator.stepper.set_fused(fused) == fused
+        if psi0 is None:
+            shape = prob.psi.GetRepresentation().GetFullShape()
+            psi0 = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+            psi0 *= np.exp(-np.arange(shape[1]) * (10.0 / shape[1]))[None, :]  # weight on the inner splines
+            psi0 /= np.linalg.norm(psi0)
+        _set_psi(prob, psi0)
+        for n in range(nsteps):
+            prob.Propagator.AdvanceStep(t0 + n * dt, dt)
+        out[name] = prob.psi.numpy()
+    e_graph = relerr(out["graphs"], out["exact"])
+    e_fused = relerr(out["fused"], out["exact"])
+    assert e_graph < 1e-4 and e_fused < 5 * e_graph + 1e-7, (e_fused, e_graph)
+
+
 @pytest.mark.parametrize("at_barrier", [0, 5])
 def test_pamp_single_kernel_step_bounded_barrier_wait(gpu, at_barrier):
     """A grid barrier of the single-kernel pAMP step whose arrivals never all come (the test
