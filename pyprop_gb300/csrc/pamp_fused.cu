@@ -33,7 +33,8 @@
 
 #include <cstring>
 
-static const int PF_PE = 2 * FZ_MAXM + 8;  // per CTA: c [2m], ||psi||_S^2 and ||psi||_S, statistics [4]
+static const int PF_PE = 2 * FZ_MAXM + 8;
+static const int PF_DENSE_MAXN = 176;  // longest fibre whose dense S^-1 is staged in shared memory  // per CTA: c [2m], ||psi||_S^2 and ||psi||_S, statistics [4]
 
 struct PfArgs {
     FzArgs z;                 // channel tables, bands, scratch, barrier, error word, psi
@@ -41,6 +42,8 @@ struct PfArgs {
     const float *S32;         // [N][2ks+1] overlap rows
     const double *S64;        // [N][2ks+1]
     int ks;                   // overlap half-bandwidth
+    const float *sinv;        // [N][sld] S^-1 in FP32 (dense solve mode)
+    int sld;
     int off_ys, off_sb, off_sg, off_xsrc, off_band, off_tab, off_T;  // shared-memory layout (bytes)
     double dt;
     double tol;               // beta below it truncates the basis
@@ -151,9 +154,13 @@ __device__ __forceinline__ void pf_stage(void *dst, const void *src, size_t byte
     }
 }
 
-template <int KB, bool STAB>
+// The overlap solve z = S^-1 y: SOLVE 0 the blocked triangular solves with factors read through
+// L2, 1 the same with the factors staged in shared memory, 2 a product with the dense S^-1 (FP32,
+// formed in FP64 on the host) staged in shared memory, for fibres short enough to hold it.
+template <int KB, int SOLVE>
 __global__ void __launch_bounds__(FZ_THREADS, 1) pamp_fused_step_kernel(PfArgs p)
 {
+    constexpr bool STAB = SOLVE == 1;
     const FzArgs &a = p.z;
     if (fz_bad_launch(a, gridDim.x != (unsigned)a.nctas || gridDim.y != 1 || gridDim.z != 1)) return;
     // the previous launch, which used bar_next, has completed: clear it for the next launch
@@ -204,6 +211,10 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) pamp_fused_step_kernel(PfArgs p
 
     if (tid < PG_MAX_SLOTS) sc[tid] = cvt<float>(p.h[tid]);
     // this channel's FP32 bands (and the solve factors) to shared memory, in flight during the norm
+    if (SOLVE == 2) {
+        pf_stage(tab, p.sinv, sizeof(float) * (size_t)N * p.sld);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
     if (STAB) {
         pf_stage((void *)lo_inv, p.slo_inv + mat * nblk * 1024, sizeof(float) * nblk * 1024);
         pf_stage((void *)up_inv, p.sup_inv + mat * nblk * 1024, sizeof(float) * nblk * 1024);
@@ -241,7 +252,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) pamp_fused_step_kernel(PfArgs p
         }
         fz_cta_sum64(nrm, red, part_me + P_NRM * pstride);
     }
-    if (sband || STAB) fz_bands_wait();  // before any exit: no copy outlives the CTA
+    if (sband || SOLVE != 0) fz_bands_wait();  // before any exit: no copy outlives the CTA
     if (!fz_grid_sync(a.bar, expect, ordinal, a, &s_ok)) return;
     fz_reduce(a.part + P_NRM * pstride, a.nch, 1, hd);
     if (tid == 0) {
@@ -268,11 +279,35 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) pamp_fused_step_kernel(PfArgs p
         // second correction (hs = h2, j vectors) applied, scaled by s
         fz_matvec32<KB>(a, ch, sc, a.wbuf + (size_t)(j & 1) * n, s, ys, npad, xsrc, sband, j, hs);
         __syncthreads();
-        for (int i = tid; i < npad; i += FZ_THREADS) xs[i] = ys[i];
-        __syncthreads();
-        // z = S^-1 y = U^-1 U^-T y
-        tri_solve_smem<float, float, FZ_NW, STAB>(nblk, w, tmat, lo_inv, lo_g, lo_rb, up_inv, up_g, up_rb, 1, 1,
-                                                  STAB ? 0 : a.g_in_smem, xs, sb, sg);
+        if constexpr (SOLVE == 2) {
+            // z = S^-1 y: row i by a group of 8 lanes (columns strided by 8), summed by shuffles
+            for (int i0 = 0; i0 < npad; i0 += FZ_THREADS / 8) {
+                const int i = i0 + (tid >> 3), g = tid & 7;
+                float zx = 0.f, zy = 0.f;
+                if (i < N) {
+                    const float *row = tab + (size_t)i * p.sld;
+                    for (int c = g; c < N; c += 8) {
+                        const float sv = row[c];
+                        const cxf v = ys[c];
+                        zx = fmaf(sv, v.x, zx);
+                        zy = fmaf(sv, v.y, zy);
+                    }
+                }
+#pragma unroll
+                for (int o = 4; o > 0; o >>= 1) {
+                    zx += __shfl_xor_sync(0xffffffffu, zx, o);
+                    zy += __shfl_xor_sync(0xffffffffu, zy, o);
+                }
+                if (g == 0 && i < npad) xs[i] = mk<float>(zx, zy);
+            }
+            __syncthreads();
+        } else {
+            for (int i = tid; i < npad; i += FZ_THREADS) xs[i] = ys[i];
+            __syncthreads();
+            // z = S^-1 y = U^-1 U^-T y
+            tri_solve_smem<float, float, FZ_NW, STAB>(nblk, w, tmat, lo_inv, lo_g, lo_rb, up_inv, up_g, up_rb, 1, 1,
+                                                      STAB ? 0 : a.g_in_smem, xs, sb, sg);
+        }
         // h1 = T^H y
         pf_dots(Tr, tld, J, ys, nullptr, N, part_me + P_H1 * pstride);
         if (!fz_grid_sync(a.bar, expect, ordinal, a, &s_ok)) return;
@@ -382,11 +417,55 @@ struct FusedPamp {
     PfArgs args;
     size_t smem = 0;
     int nctas = 0;
-    bool kb6 = false;
-    bool stab = false;  // the solve factors staged in shared memory
+    void (*kern)(PfArgs) = nullptr;  // the instance for the band width and solve mode
+    int solve = 0;                     // 0 factors through L2, 1 factors in shared memory, 2 dense S^-1
     int parity = 0;
-    void *bufs[4] = {nullptr, nullptr, nullptr, nullptr};  // real bands, source tables
+    void *bufs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // real bands, source tables, S^-1
 };
+
+// S^-1 in FP32 rows of sld floats (zero past N): S from the FP64 overlap rows on the device,
+// Cholesky S = L L^T and the inverse column by column in FP64 on the host (set-up only)
+static bool dense_inverse(pg_banded *ovl64, int N, int sld, std::vector<float> &out)
+{
+    const int kb = ovl64->kb, b = 2 * kb + 1;
+    std::vector<double> rows((size_t)N * b);
+    if (cudaMemcpy(rows.data(), ovl64->d_S, sizeof(double) * rows.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return false;
+    std::vector<double> L((size_t)N * N, 0.0);
+    for (int i = 0; i < N; ++i)
+        for (int d = 0; d < b; ++d) {
+            const int j = i + d - kb;
+            if (j >= 0 && j <= i) L[(size_t)i * N + j] = rows[(size_t)i * b + d];
+        }
+    for (int j = 0; j < N; ++j) {  // in place: lower triangle of S -> L
+        double djj = L[(size_t)j * N + j];
+        for (int q = std::max(0, j - 2 * kb); q < j; ++q) djj -= L[(size_t)j * N + q] * L[(size_t)j * N + q];
+        if (!(djj > 0.0)) return false;
+        djj = std::sqrt(djj);
+        L[(size_t)j * N + j] = djj;
+        for (int i = j + 1; i < std::min(N, j + kb + 1); ++i) {
+            double v = L[(size_t)i * N + j];
+            for (int q = std::max(0, i - 2 * kb); q < j; ++q) v -= L[(size_t)i * N + q] * L[(size_t)j * N + q];
+            L[(size_t)i * N + j] = v / djj;
+        }
+    }
+    out.assign((size_t)N * sld, 0.f);
+    std::vector<double> x(N);
+    for (int c = 0; c < N; ++c) {
+        for (int i = 0; i < N; ++i) {  // L y = e_c
+            double v = i == c ? 1.0 : 0.0;
+            for (int q = std::max(0, i - kb); q < i; ++q) v -= L[(size_t)i * N + q] * x[q];
+            x[i] = v / L[(size_t)i * N + i];
+        }
+        for (int i = N - 1; i >= 0; --i) {  // L^T z = y
+            double v = x[i];
+            for (int q = i + 1; q < std::min(N, i + kb + 1); ++q) v -= L[(size_t)q * N + i] * x[q];
+            x[i] = v / L[(size_t)i * N + i];
+        }
+        for (int i = 0; i < N; ++i) out[(size_t)i * sld + c] = (float)x[i];
+    }
+    return true;
+}
 
 int pg_pamp_fused_prepare(pg_op *opb, pg_banded *ovl64, pg_banded *ovlb, void *T, int m, double tol,
                           FusedPamp **out)
@@ -420,9 +499,13 @@ int pg_pamp_fused_prepare(pg_op *opb, pg_banded *ovl64, pg_banded *ovlb, void *T
     // shared memory: xs | ys sb sg xsrc [bands] [solve factors] (the exponential's scratch over
     // ys...) | [T]
     const size_t nbw = (size_t)nblk * w;
-    const size_t tab_bytes = sizeof(float) * (2 * (size_t)nblk * 1024 + 2 * nbw * 32 + 2 * nbw * nbw);
+    const size_t fac_bytes = sizeof(float) * (2 * (size_t)nblk * 1024 + 2 * nbw * 32 + 2 * nbw * nbw);
+    // the dense inverse's rows padded to 8 banks past a multiple of 32 words: the four rows a
+    // warp reads at once fall in distinct banks
+    const int sld = ((N + 23) / 32) * 32 + 8;
+    const size_t dense_bytes = sizeof(float) * (size_t)N * sld;
     struct Lay { size_t ys, sb, sg, xsrc, band, tab, T, total; };
-    auto layout = [&](int g_in_smem, int bands_smem, int v_smem, int stab) {
+    auto layout = [&](int g_in_smem, int bands_smem, int v_smem, int solve) {
         Lay L;
         L.ys = npad * sizeof(cxf);
         L.sb = L.ys + npad * sizeof(cxf);
@@ -430,26 +513,31 @@ int pg_pamp_fused_prepare(pg_op *opb, pg_banded *ovl64, pg_banded *ovlb, void *T
         L.xsrc = L.sg + (g_in_smem ? (size_t)nblk * w * 32 * sizeof(float) : 0);
         L.band = a16(L.xsrc + (size_t)FZ_MAXU * (N + 2 * kb) * sizeof(cxf));
         L.tab = a16(L.band + (bands_smem ? band_bytes : 0));
-        const size_t work_end = L.tab + (stab ? tab_bytes : 0);
+        const size_t work_end = L.tab + (solve == 2 ? dense_bytes : solve == 1 ? fac_bytes : 0);
         const size_t ex_end = L.ys + 6 * sizeof(float4) * (size_t)m * m;
         L.T = a16(std::max(work_end, ex_end));
         L.total = L.T + (v_smem ? (size_t)m * N * sizeof(cxf) : 0);
         return L;
     };
     const size_t limit = 200 * 1024;
-    // everything in shared memory where it fits; then without the bands, without the solve
-    // factors, without the Krylov vectors, without the couplings
-    int g_in_smem = 0, bands_smem = 1, v_smem = 1, stab = 1;
-    Lay L = layout(0, 1, 1, 1);
-    if (L.total > limit) { bands_smem = 0; L = layout(0, 0, 1, 1); }
-    if (L.total > limit) { stab = 0; g_in_smem = 1; L = layout(1, 0, 1, 0); }
+    // everything in shared memory where it fits (short fibres: the dense inverse; else the
+    // blocked solve's factors); then without the bands, the factors, the Krylov vectors, the
+    // couplings
+    int g_in_smem = 0, bands_smem = 1, v_smem = 1, solve = N <= PF_DENSE_MAXN ? 2 : 1;
+    Lay L = layout(0, 1, 1, solve);
+    if (L.total > limit) { bands_smem = 0; L = layout(0, 0, 1, solve); }
+    if (L.total > limit && solve == 2) { solve = 1; L = layout(0, 0, 1, 1); }
+    if (L.total > limit) { solve = 0; g_in_smem = 1; L = layout(1, 0, 1, 0); }
     if (L.total > limit) { v_smem = 0; L = layout(1, 0, 0, 0); }
     if (L.total > limit) { g_in_smem = 0; L = layout(0, 0, 0, 0); }
     if (L.total > limit) return PG_ERR_SHAPE;
-    const void *kern = kb6 ? (stab ? (const void *)pamp_fused_step_kernel<6, true> : (const void *)pamp_fused_step_kernel<6, false>)
-                           : (stab ? (const void *)pamp_fused_step_kernel<-1, true>
-                                   : (const void *)pamp_fused_step_kernel<-1, false>);
-    PG_CUDA_TRY(raise_smem_limit(kern, L.total));
+    void (*kern)(PfArgs) = kb6 ? (solve == 2 ? pamp_fused_step_kernel<6, 2> : solve == 1 ? pamp_fused_step_kernel<6, 1>
+                                                                                        : pamp_fused_step_kernel<6, 0>)
+                               : (solve == 2 ? pamp_fused_step_kernel<-1, 2>
+                                             : solve == 1 ? pamp_fused_step_kernel<-1, 1> : pamp_fused_step_kernel<-1, 0>);
+    std::vector<float> sinv;
+    if (solve == 2 && !dense_inverse(ovl64, N, sld, sinv)) return PG_ERR_STORAGE;
+    PG_CUDA_TRY(raise_smem_limit((const void *)kern, L.total));
     int per_sm = 0;
     PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FZ_THREADS, L.total));
     if (per_sm < 1 || nch > per_sm * std::max(1, ctx->num_sms)) return PG_ERR_SHAPE;  // all CTAs resident
@@ -504,6 +592,7 @@ int pg_pamp_fused_prepare(pg_op *opb, pg_banded *ovl64, pg_banded *ovlb, void *T
     if (code == PG_OK) code = upload_vec(ucol, &f->bufs[1]);
     if (code == PG_OK) code = upload_vec(nucol, &f->bufs[2]);
     if (code == PG_OK) code = upload_vec(ent_u, &f->bufs[3]);
+    if (code == PG_OK && solve == 2) code = upload_vec(sinv, &f->bufs[4]);
     if (code != PG_OK) {
         pg_pamp_fused_free(f);
         return code;
@@ -512,10 +601,12 @@ int pg_pamp_fused_prepare(pg_op *opb, pg_banded *ovl64, pg_banded *ovlb, void *T
     a.ucol = (const int *)f->bufs[1];
     a.nucol = (const int *)f->bufs[2];
     a.ent_u = (const unsigned char *)f->bufs[3];
+    p.sinv = (const float *)f->bufs[4];
+    p.sld = sld;
     f->smem = L.total;
     f->nctas = nch;
-    f->kb6 = kb6;
-    f->stab = stab != 0;
+    f->kern = kern;
+    f->solve = solve;
     *out = f;
     return PG_OK;
 }
@@ -543,10 +634,7 @@ int pg_pamp_fused_launch(FusedPamp *f, cudaStream_t s, cxd *psi, double dt, cons
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (f->kb6 && f->stab) PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, pamp_fused_step_kernel<6, true>, p));
-    else if (f->kb6) PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, pamp_fused_step_kernel<6, false>, p));
-    else if (f->stab) PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, pamp_fused_step_kernel<-1, true>, p));
-    else PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, pamp_fused_step_kernel<-1, false>, p));
+    PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, f->kern, p));
     return PG_OK;
 }
 

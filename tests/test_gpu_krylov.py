@@ -123,12 +123,14 @@ def test_pamp_single_kernel_step_matches_graphs_and_oracle(gpu):
 
 
 @pytest.mark.parametrize("kw", [dict(lmax=3, nbsplines=40, rmax=40.0, order=5),
+                                dict(lmax=3, nbsplines=300, rmax=150.0),
                                 dict(lmax=5, nbsplines=600, rmax=300.0)])
 def test_pamp_single_kernel_step_other_layouts(gpu, kw):
-    """The single-kernel pAMP step on the generic band-width instance (B-splines of order 5) and
-    on a fibre whose solve factors do not fit in shared memory (600 B-splines: read through L2)
-    against the graphs with the same complex64 basis and the complex128-basis step: both
-    complex64 paths within the FP32 Krylov error of the complex128 result."""
+    """The single-kernel pAMP step on the generic band-width instance (B-splines of order 5, the
+    dense S^-1 of a short fibre), with the blocked solve's factors in shared memory (300
+    B-splines) and read through L2 (600 B-splines), against the graphs with the same complex64
+    basis and the complex128-basis step: both complex64 paths within the FP32 Krylov error of
+    the complex128 result."""
     t0, dt, nsteps = 1.0, 0.01, 5
     rng = np.random.default_rng(7)
     out = {}
