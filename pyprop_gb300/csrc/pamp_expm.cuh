@@ -1,7 +1,9 @@
 // The m x m exponential of pAMP on the device: c = ||psi|| exp(-i dt H_k) e_1 with the
 // reference's method (core/krylov/pamp/pamp/pamp.h:430-565: scaling and squaring of the
 // diagonal Pade approximant of order 6, coefficients c_0 = 1, c_(i+1) = c_i (p-i)/((i+1)(2p-i)),
-// Horner in A^2, N/D = I + 2 (E - O)^-1 O), run by one CTA per member. Shared by the ensemble
+// N/D = I + 2 (E - O)^-1 O with the even and odd parts E, O of the numerator; the reference
+// evaluates them by Horner in A^2, here from the powers A^2, A^4, A^6 - the same approximant in
+// four matrix products instead of seven), run by one CTA per member. Shared by the ensemble
 // graph (one kernel for all members) and the persistent ensemble kernel.
 #pragma once
 #include "pg_internal.cuh"
@@ -108,19 +110,20 @@ static __device__ void pamp_expm_block(const PampExpArgs &a, double dt, unsigned
         P[t] = mk<double>(dg ? c[order - 1] : 0.0, 0.0);
     }
     __syncthreads();
-    bool odd = true;
-    for (int i = order - 2; i >= 0; --i) {
-        cxd *M = odd ? Q : P;
-        smem_matmul(k, M, A2, T);
-        for (int t = tid; t < k * k; t += nt) M[t] = T[t] + mk<double>((t / k) == (t % k) ? c[i] : 0.0, 0.0);
-        __syncthreads();
-        odd = !odd;
+    // even part Q = c0 + c2 B + c4 B^2 + c6 B^3 and odd part P = A (c1 + c3 B + c5 B^2) of the
+    // numerator, B = A^2: four matrix products in all (B, B^2, B^3, A P')
+    const bool odd = false;
+    smem_matmul(k, A2, A2, T);  // B^2
+    smem_matmul(k, T, A2, D);   // B^3
+    for (int t = tid; t < k * k; t += nt) {
+        const double dg = (t / k) == (t % k) ? 1.0 : 0.0;
+        Q[t] = c[6] * D[t] + c[4] * T[t] + c[2] * A2[t] + mk<double>(c[0] * dg, 0.0);
+        P[t] = c[5] * T[t] + c[3] * A2[t] + mk<double>(c[1] * dg, 0.0);
     }
+    __syncthreads();
+    smem_matmul(k, P, A, T);
     {
-        cxd *M = odd ? Q : P;
-        smem_matmul(k, M, A, T);
-        for (int t = tid; t < k * k; t += nt) M[t] = T[t];
-        __syncthreads();
+        cxd *tmp = P; P = T; T = tmp;
     }
     // solve (Q - P) X = P by LU with partial pivoting; X overwrites P
     for (int t = tid; t < k * k; t += nt) D[t] = Q[t] - P[t];
@@ -198,7 +201,7 @@ static __device__ void pamp_expm_block(const PampExpArgs &a, double dt, unsigned
 
 // ---- the same exponential in double-float arithmetic -----------------------------------------
 // The same method as pamp_expm_block (scaling and squaring of the diagonal Pade approximant of
-// order 6, Horner in A^2, (Q - P) X = P by LU with partial pivoting, E = +-(I + 2X)) with the
+// order 6 from the powers of A^2, (Q - P) X = P by LU with partial pivoting, E = I + 2X) with the
 // matrices as complex double-float values (FP32 pairs hi + lo per real part, about 2^-44
 // relative): the FP64 matrix products of that routine take a few hundred microseconds per
 // member on one SM of this GPU. Divisions (2m^2 of them) and the final coefficients go
@@ -428,20 +431,34 @@ static __device__ void pamp_expm_block_df(const PampExpArgs &a, double dt, unsig
         P[t] = zdf_make(mk<double>(dg ? c[order - 1] : 0.0, 0.0));
     }
     __syncthreads();
-    bool odd = true;
-    for (int i = order - 2; i >= 0; --i) {
-        zdf *M = odd ? Q : P;
-        zdf_matmul(k, M, A2, T);
-        const zdf ci = zdf_make(mk<double>(c[i], 0.0));
-        for (int t = tid; t < k * k; t += nt) M[t] = (t / k) == (t % k) ? zdf_add(T[t], ci) : T[t];
-        __syncthreads();
-        odd = !odd;
-    }
+    // even part Q = c0 + c2 B + c4 B^2 + c6 B^3 and odd part P = A (c1 + c3 B + c5 B^2) of the
+    // numerator, B = A^2: four matrix products in all (B, B^2, B^3, A P')
+    const bool odd = false;
+    zdf_matmul(k, A2, A2, T);  // B^2
+    zdf_matmul(k, T, A2, D);   // B^3
     {
-        zdf *M = odd ? Q : P;
-        zdf_matmul(k, M, A, T);
-        for (int t = tid; t < k * k; t += nt) M[t] = T[t];
-        __syncthreads();
+        const dff c0 = df_make(c[0]), c1 = df_make(c[1]), c2 = df_make(c[2]), c3 = df_make(c[3]), c4 = df_make(c[4]),
+                  c5 = df_make(c[5]), c6 = df_make(c[6]);
+        auto scl = [](dff s, zdf v) {
+            const dff r = df_mul(s, {v.x, v.y}), i = df_mul(s, {v.z, v.w});
+            return make_float4(r.h, r.l, i.h, i.l);
+        };
+        for (int t = tid; t < k * k; t += nt) {
+            const bool dg = (t / k) == (t % k);
+            zdf q = zdf_add(zdf_add(scl(c6, D[t]), scl(c4, T[t])), scl(c2, A2[t]));
+            zdf p = zdf_add(scl(c5, T[t]), scl(c3, A2[t]));
+            if (dg) {
+                q = zdf_add(q, make_float4(c0.h, c0.l, 0.f, 0.f));
+                p = zdf_add(p, make_float4(c1.h, c1.l, 0.f, 0.f));
+            }
+            Q[t] = q;
+            P[t] = p;
+        }
+    }
+    __syncthreads();
+    zdf_matmul(k, P, A, T);
+    {
+        zdf *tmp = P; P = T; T = tmp;
     }
     for (int t = tid; t < k * k; t += nt) D[t] = zdf_sub(Q[t], P[t]);
     __syncthreads();
