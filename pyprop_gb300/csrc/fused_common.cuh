@@ -304,6 +304,10 @@ __device__ __forceinline__ void fz_bands_wait()
 // i forms xs[i] = sum_e sc[slot_e] sum_d band_e[d][i] x_e[i + d - kb] from real bands (in
 // shared memory when sband is set, else read through L1); zero on the padding up to npad.
 template <int KB>
+__device__ __forceinline__ void fz_rowprod32(const FzArgs &A, int a, const cxf *sc, cxf *xs, int npad,
+                                             const cxf *xsrc, const float *sband);
+
+template <int KB>
 __device__ __forceinline__ void fz_matvec32(const FzArgs &A, int a, const cxf *sc, const cxf *wsrc, float s, cxf *xs,
                                             int npad, cxf *xsrc, const float *sband, int Jc, const cxf *hs)
 {
@@ -340,6 +344,18 @@ __device__ __forceinline__ void fz_matvec32(const FzArgs &A, int a, const cxf *s
         }
     }
     __syncthreads();
+    fz_rowprod32<KB>(A, a, sc, xs, npad, xsrc, sband);
+}
+
+// The row product of fz_matvec32 from source fibres already staged in xsrc ([nu][N + 2kb],
+// zero halo of kb; callers synchronise the CTA after staging): thread i forms
+// xs[i] = sum_e sc[slot_e] sum_d band_e[d][i] x_e[i + d - kb], zero on the padding up to npad.
+template <int KB>
+__device__ __forceinline__ void fz_rowprod32(const FzArgs &A, int a, const cxf *sc, cxf *xs, int npad,
+                                             const cxf *xsrc, const float *sband)
+{
+    const OpDev &op = A.opb;
+    const int N = op.N, kb = KB >= 0 ? KB : op.kb, b = 2 * kb + 1, ld = op.ld, W = N + 2 * kb;
     const int e0 = __ldg(op.row_ptr + a), e1 = __ldg(op.row_ptr + a + 1);
     for (int i = threadIdx.x; i < npad; i += FZ_THREADS) {
         cxf acc = mk<float>(0.f, 0.f);

@@ -44,6 +44,8 @@ struct PfArgs {
     int ks;                   // overlap half-bandwidth
     const float *sinv;        // [N][sld] S^-1 in FP32 (dense solve mode)
     int sld;
+    const signed char *uslot; // [Nang][FZ_MAXU] cache slot of each source channel of a row (-1: the row's own)
+    int ncache, off_cache;    // neighbour Krylov vectors kept in shared memory: slots (0: none), offset
     int off_ys, off_sb, off_sg, off_xsrc, off_band, off_tab, off_T;  // shared-memory layout (bytes)
     double dt;
     double tol;               // beta below it truncates the basis
@@ -154,6 +156,32 @@ __device__ __forceinline__ void pf_stage(void *dst, const void *src, size_t byte
     }
 }
 
+// Stage the row's source fibres T_j[col] = (z'[col] - sum_q<j T_q[col] h2_q) s into xsrc
+// ([nu][N + 2kb], zero halo), with the Gram-Schmidt correction read from shared memory: the
+// CTA's own channel from its Krylov vectors sT, each neighbour from the copies of its T_q this
+// CTA formed while staging in earlier Arnoldi steps (cache [slot][m][N]); the new T_j of each
+// neighbour joins its copies. The same arithmetic as the owner's, so the copies are the
+// owner's vectors bit for bit. Only z' is read from global memory (one L2 round trip).
+__device__ __forceinline__ void pf_sources(const FzArgs &A, int a, const cxf *wsrc, float s, int j, const cxf *hs,
+                                           cxf *xsrc, int kb, const cxf *sT, cxf *cache, const signed char *slot)
+{
+    const int N = A.N, m = A.m, W = N + 2 * kb, nu = __ldg(A.nucol + a);
+    for (int idx = threadIdx.x; idx < nu * W; idx += FZ_THREADS) {
+        const int u = idx / W, jj = idx - u * W - kb;
+        cxf x = mk<float>(0.f, 0.f);
+        if (jj >= 0 && jj < N) {
+            const int col = __ldg(A.ucol + (size_t)a * FZ_MAXU + u);
+            const int sl = __ldg(slot + u);
+            const cxf *Tq = sl < 0 ? sT + jj : cache + (size_t)sl * m * N + jj;
+            const cxf v = fz_gs_update<false>(fz_ldcg(wsrc + (size_t)col * N + jj), Tq, N, j, hs);
+            x = mk<float>(v.x * s, v.y * s);
+            if (sl >= 0) cache[((size_t)sl * m + j) * N + jj] = x;
+        }
+        xsrc[idx] = x;
+    }
+    __syncthreads();
+}
+
 // The overlap solve z = S^-1 y: SOLVE 0 the blocked triangular solves with factors read through
 // L2, 1 the same with the factors staged in shared memory, 2 a product with the dense S^-1 (FP32,
 // formed in FP64 on the host) staged in shared memory, for fibres short enough to hold it.
@@ -187,6 +215,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) pamp_fused_step_kernel(PfArgs p
     cxf *xsrc = (cxf *)(pf_smem + p.off_xsrc);              // [FZ_MAXU][N + 2kb] staged sources
     float *sband = a.bands_smem ? (float *)(pf_smem + p.off_band) : nullptr;
     cxf *sT = a.v_smem ? (cxf *)(pf_smem + p.off_T) : nullptr;  // [m][N] this channel's T_q
+    cxf *cache = p.ncache ? (cxf *)(pf_smem + p.off_cache) : nullptr;  // [slots][m][N] neighbours' T_q
     unsigned char *exs = pf_smem + p.off_ys;                // the exponential's scratch, after the loop
     cxf *Tc = a.V + (size_t)ch * N;                         // T_q[ch] at Tc + q n
     const cxf *Tr = sT ? sT : Tc;
@@ -277,7 +306,13 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) pamp_fused_step_kernel(PfArgs p
         }
         // y = H T_j (row ch); the staged sources are the channels' z' with the last step's
         // second correction (hs = h2, j vectors) applied, scaled by s
-        fz_matvec32<KB>(a, ch, sc, a.wbuf + (size_t)(j & 1) * n, s, ys, npad, xsrc, sband, j, hs);
+        if (cache) {
+            pf_sources(a, ch, a.wbuf + (size_t)(j & 1) * n, s, j, hs, xsrc, KB >= 0 ? KB : a.opb.kb, sT, cache,
+                       p.uslot + (size_t)ch * FZ_MAXU);
+            fz_rowprod32<KB>(a, ch, sc, ys, npad, xsrc, sband);
+        } else {
+            fz_matvec32<KB>(a, ch, sc, a.wbuf + (size_t)(j & 1) * n, s, ys, npad, xsrc, sband, j, hs);
+        }
         __syncthreads();
         if constexpr (SOLVE == 2) {
             // z = S^-1 y: row i by a group of 8 lanes (columns strided by 8), summed by shuffles
@@ -420,7 +455,7 @@ struct FusedPamp {
     void (*kern)(PfArgs) = nullptr;  // the instance for the band width and solve mode
     int solve = 0;                     // 0 factors through L2, 1 factors in shared memory, 2 dense S^-1
     int parity = 0;
-    void *bufs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // real bands, source tables, S^-1
+    void *bufs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // bands, source tables, S^-1, slots
 };
 
 // S^-1 in FP32 rows of sld floats (zero past N): S from the FP64 overlap rows on the device,
@@ -504,8 +539,18 @@ int pg_pamp_fused_prepare(pg_op *opb, pg_banded *ovl64, pg_banded *ovlb, void *T
     // warp reads at once fall in distinct banks
     const int sld = ((N + 23) / 32) * 32 + 8;
     const size_t dense_bytes = sizeof(float) * (size_t)N * sld;
-    struct Lay { size_t ys, sb, sg, xsrc, band, tab, T, total; };
-    auto layout = [&](int g_in_smem, int bands_smem, int v_smem, int solve) {
+    // neighbour channels per row (the cache slots of the staged sources)
+    std::vector<signed char> uslot((size_t)nch * FZ_MAXU, -1);
+    int ncache = 0;
+    for (int r = 0; r < nch; ++r) {
+        int c = 0;
+        for (int u = 0; u < nucol[r]; ++u)
+            if (ucol[(size_t)r * FZ_MAXU + u] != r) uslot[(size_t)r * FZ_MAXU + u] = (signed char)c++;
+        ncache = std::max(ncache, c);
+    }
+    const size_t cache_bytes = (size_t)ncache * m * N * sizeof(cxf);
+    struct Lay { size_t ys, sb, sg, xsrc, band, tab, T, cache, total; };
+    auto layout = [&](int g_in_smem, int bands_smem, int v_smem, int solve, int cache) {
         Lay L;
         L.ys = npad * sizeof(cxf);
         L.sb = L.ys + npad * sizeof(cxf);
@@ -516,20 +561,25 @@ int pg_pamp_fused_prepare(pg_op *opb, pg_banded *ovl64, pg_banded *ovlb, void *T
         const size_t work_end = L.tab + (solve == 2 ? dense_bytes : solve == 1 ? fac_bytes : 0);
         const size_t ex_end = L.ys + 6 * sizeof(float4) * (size_t)m * m;
         L.T = a16(std::max(work_end, ex_end));
-        L.total = L.T + (v_smem ? (size_t)m * N * sizeof(cxf) : 0);
+        L.cache = a16(L.T + (v_smem ? (size_t)m * N * sizeof(cxf) : 0));
+        L.total = L.cache + (cache ? cache_bytes : 0);
         return L;
     };
-    const size_t limit = 200 * 1024;
+    // the opt-in shared memory of a CTA less room for the kernel's static arrays
+    int optin = 0;
+    PG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    const size_t limit = std::min<size_t>((size_t)std::max(optin, 48 * 1024) - 8 * 1024, 224 * 1024);
     // everything in shared memory where it fits (short fibres: the dense inverse; else the
     // blocked solve's factors); then without the bands, the factors, the Krylov vectors, the
     // couplings
-    int g_in_smem = 0, bands_smem = 1, v_smem = 1, solve = N <= PF_DENSE_MAXN ? 2 : 1;
-    Lay L = layout(0, 1, 1, solve);
-    if (L.total > limit) { bands_smem = 0; L = layout(0, 0, 1, solve); }
-    if (L.total > limit && solve == 2) { solve = 1; L = layout(0, 0, 1, 1); }
-    if (L.total > limit) { solve = 0; g_in_smem = 1; L = layout(1, 0, 1, 0); }
-    if (L.total > limit) { v_smem = 0; L = layout(1, 0, 0, 0); }
-    if (L.total > limit) { g_in_smem = 0; L = layout(0, 0, 0, 0); }
+    int g_in_smem = 0, bands_smem = 1, v_smem = 1, solve = N <= PF_DENSE_MAXN ? 2 : 1, use_cache = ncache > 0;
+    Lay L = layout(0, 1, 1, solve, use_cache);
+    if (L.total > limit && use_cache) { use_cache = 0; L = layout(0, 1, 1, solve, 0); }
+    if (L.total > limit) { bands_smem = 0; L = layout(0, 0, 1, solve, 0); }
+    if (L.total > limit && solve == 2) { solve = 1; L = layout(0, 0, 1, 1, 0); }
+    if (L.total > limit) { solve = 0; g_in_smem = 1; L = layout(1, 0, 1, 0, 0); }
+    if (L.total > limit) { v_smem = 0; L = layout(1, 0, 0, 0, 0); }
+    if (L.total > limit) { g_in_smem = 0; L = layout(0, 0, 0, 0, 0); }
     if (L.total > limit) return PG_ERR_SHAPE;
     void (*kern)(PfArgs) = kb6 ? (solve == 2 ? pamp_fused_step_kernel<6, 2> : solve == 1 ? pamp_fused_step_kernel<6, 1>
                                                                                         : pamp_fused_step_kernel<6, 0>)
@@ -593,6 +643,7 @@ int pg_pamp_fused_prepare(pg_op *opb, pg_banded *ovl64, pg_banded *ovlb, void *T
     if (code == PG_OK) code = upload_vec(nucol, &f->bufs[2]);
     if (code == PG_OK) code = upload_vec(ent_u, &f->bufs[3]);
     if (code == PG_OK && solve == 2) code = upload_vec(sinv, &f->bufs[4]);
+    if (code == PG_OK && use_cache) code = upload_vec(uslot, &f->bufs[5]);
     if (code != PG_OK) {
         pg_pamp_fused_free(f);
         return code;
@@ -603,6 +654,9 @@ int pg_pamp_fused_prepare(pg_op *opb, pg_banded *ovl64, pg_banded *ovlb, void *T
     a.ent_u = (const unsigned char *)f->bufs[3];
     p.sinv = (const float *)f->bufs[4];
     p.sld = sld;
+    p.uslot = (const signed char *)f->bufs[5];
+    p.ncache = use_cache ? ncache : 0;
+    p.off_cache = (int)L.cache;
     f->smem = L.total;
     f->nctas = nch;
     f->kern = kern;
