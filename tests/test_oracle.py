@@ -97,3 +97,53 @@ def test_shift_invert_ground_state_config1():
     assert abs(lam[0] + 0.5) < 1e-10
     psi = vecs[0].reshape(nang, N)
     assert abs(ham.energy(psi) + 0.5) < 1e-10
+
+
+def test_pamp_arnoldi_on_u_inverse_basis_equals_balanced_form():
+    """The recurrence the single-kernel pAMP step runs: Arnoldi on T_j = U^-1 V_j (S = U^T U)
+    with y = H T_j, z = S^-1 y, h1 = T^H y, h2 = T^H S z', beta^2 = ||z'||_S^2 - |h2|^2 gives the
+    Hessenberg matrix of the balanced form (Arnoldi on U^-T H U^-1 with CGS2) and the same
+    psi(t + dt) = U^-1 ||U psi|| V c = ||psi||_S sum_j c_j T_j (complex128, random banded S > 0
+    and Hermitian H)."""
+    rng = np.random.default_rng(11)
+    n, m, dt, kb = 48, 10, 0.05, 3
+    S = np.zeros((n, n))
+    for d in range(-kb, kb + 1):
+        S += np.diag(rng.uniform(-0.2, 0.2, n - abs(d)), d) if d else 0.0
+    S = (S + S.T) / 2 + 2.0 * np.eye(n)
+    Hh = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    H = (Hh + Hh.conj().T) / 2
+    psi = rng.normal(size=n) + 1j * rng.normal(size=n)
+    U = sl.cholesky(S)
+    Ui = np.linalg.inv(U)
+    A = Ui.T @ H @ Ui
+    x = U @ psi
+    nrm = np.linalg.norm(x)
+    V, Hm = [x / nrm], np.zeros((m, m), complex)
+    for j in range(m):
+        w = A @ V[j]
+        for _ in range(2):
+            h = np.array([v.conj() @ w for v in V])
+            w = w - sum(hh * v for hh, v in zip(h, V))
+            Hm[:j + 1, j] += h
+        if j + 1 < m:
+            Hm[j + 1, j] = np.linalg.norm(w)
+        V.append(w / np.linalg.norm(w))
+    ref = Ui @ (np.array(V[:m]).T @ (sl.expm(-1j * dt * Hm)[:, 0] * nrm))
+    nrm_s = np.sqrt((psi.conj() @ S @ psi).real)
+    T, Ht = [psi / nrm_s], np.zeros((m, m), complex)
+    for j in range(m):
+        y = H @ T[j]
+        z = np.linalg.solve(S, y)
+        h1 = np.array([t.conj() @ y for t in T])
+        z1 = z - sum(hh * t for hh, t in zip(h1, T))
+        u = S @ z1
+        h2 = np.array([t.conj() @ u for t in T])
+        beta = np.sqrt((z1.conj() @ u).real - np.sum(np.abs(h2) ** 2))
+        Ht[:j + 1, j] = h1 + h2
+        if j + 1 < m:
+            Ht[j + 1, j] = beta
+        T.append((z1 - sum(hh * t for hh, t in zip(h2, T))) / beta)
+    out = np.array(T[:m]).T @ (sl.expm(-1j * dt * Ht)[:, 0] * nrm_s)
+    assert np.abs(Hm - Ht).max() < 1e-12 * np.abs(Hm).max()
+    assert np.linalg.norm(out - ref) < 1e-13 * np.linalg.norm(ref)
