@@ -25,7 +25,7 @@
 // that runs out sets the context's error word (2) and the CTAs return with psi unchanged.
 //
 // Qualifying steppers (pg_pamp_fused_prepare): complex64 basis, a rank-2 operator with real
-// bands and at most FZ_MAXU distinct source channels per row, basis size <= FZ_MAXM, and no
+// bands and at most FZ_MAXU distinct source channels per row, basis size <= PF_MAXM, and no
 // more channels than resident CTAs of 768 threads.
 #include "fused_common.cuh"
 #include "pamp_expm.cuh"
@@ -33,7 +33,9 @@
 
 #include <cstring>
 
-static const int PF_PE = 2 * FZ_MAXM + 8;
+static const int PF_MAXM = 48;                 // Krylov basis bound of the single-kernel pAMP step
+static const int PF_PSTRIDE = 2 * (PF_MAXM + 1);  // doubles per CTA and phase in the partials
+static const int PF_PE = 2 * PF_MAXM + 8;
 static const int PF_DENSE_MAXN = 176;  // longest fibre whose dense S^-1 is staged in shared memory  // per CTA: c [2m], ||psi||_S^2 and ||psi||_S, statistics [4]
 
 struct PfArgs {
@@ -121,7 +123,7 @@ __device__ __forceinline__ void pf_reduce(const double *part, int nch, int nval,
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
                 const int t = t0 + u * FZ_NW;
-                v[u] = t < nval ? __ldcg(reinterpret_cast<const float2 *>(part + (size_t)a * FZ_PSTRIDE + t))
+                v[u] = t < nval ? __ldcg(reinterpret_cast<const float2 *>(part + (size_t)a * PF_PSTRIDE + t))
                                 : make_float2(0.f, 0.f);
             }
 #pragma unroll
@@ -196,10 +198,10 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) pamp_fused_step_kernel(PfArgs p
     extern __shared__ __align__(16) unsigned char pf_smem[];
     __shared__ cxf sc[PG_MAX_SLOTS];
     __shared__ double red[FZ_NW][2 * FZ_CB];
-    __shared__ double h1d[FZ_PSTRIDE], h2d[FZ_PSTRIDE];
+    __shared__ double h1d[PF_PSTRIDE], h2d[PF_PSTRIDE];
     __shared__ double hd[1];
-    __shared__ cxf hs[FZ_MAXM];
-    __shared__ double cs[2 * FZ_MAXM];
+    __shared__ cxf hs[PF_MAXM];
+    __shared__ double cs[2 * PF_MAXM];
     __shared__ int s_ok, s_k, s_cont;
     __shared__ float s_inv;  // 1/beta (first 1/||psi||_S) of the Krylov vector formed next
 
@@ -221,8 +223,8 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) pamp_fused_step_kernel(PfArgs p
     const cxf *Tr = sT ? sT : Tc;
     const long long tld = sT ? (long long)N : n;
     const size_t mat = (size_t)(ch / a.fib_per_mat);
-    const size_t pstride = (size_t)gridDim.x * FZ_PSTRIDE;
-    double *part_me = a.part + (size_t)ch * FZ_PSTRIDE;
+    const size_t pstride = (size_t)gridDim.x * PF_PSTRIDE;
+    double *part_me = a.part + (size_t)ch * PF_PSTRIDE;
     double *hc = p.hcols + (size_t)ch * m * 3 * cd;
     double *pe = p.pe + (size_t)ch * PF_PE;
     unsigned int expect = 0, ordinal = 0;
@@ -283,7 +285,13 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) pamp_fused_step_kernel(PfArgs p
     }
     if (sband || SOLVE != 0) fz_bands_wait();  // before any exit: no copy outlives the CTA
     if (!fz_grid_sync(a.bar, expect, ordinal, a, &s_ok)) return;
-    fz_reduce(a.part + P_NRM * pstride, a.nch, 1, hd);
+    if (tid < 32) {  // ||psi||_S^2: the channels' FP64 partials over the lanes, a fixed order
+        double v = 0.0;
+        for (int c = tid; c < a.nch; c += 32) v += __ldcg(a.part + P_NRM * pstride + (size_t)c * PF_PSTRIDE);
+        v = fz_warp_sum(v);
+        if (tid == 0) hd[0] = v;
+    }
+    __syncthreads();
     if (tid == 0) {
         const double nrm = sqrt(fmax(hd[0], 0.0));
         pe[2 * m] = hd[0];
@@ -508,7 +516,7 @@ int pg_pamp_fused_prepare(pg_op *opb, pg_banded *ovl64, pg_banded *ovlb, void *T
     if (!out) return PG_ERR_ARG;
     *out = nullptr;
     if (!opb || !ovl64 || !ovlb || !T) return PG_ERR_ARG;
-    if (m < 2 || m > FZ_MAXM) return PG_ERR_SHAPE;
+    if (m < 2 || m > PF_MAXM) return PG_ERR_SHAPE;
     if (opb->rank != 2 || opb->precision != PG_FP32 || !opb->finalized) return PG_ERR_STORAGE;
     if (opb->ndense_entries > 0 || opb->fact.Q > 0) return PG_ERR_STORAGE;
     if (ovlb->kind != 0 || !ovlb->op || ovlb->op->precision != PG_FP32 || ovl64->kind != 0 || !ovl64->op ||
@@ -631,7 +639,7 @@ int pg_pamp_fused_prepare(pg_op *opb, pg_banded *ovl64, pg_banded *ovlb, void *T
         if (code == PG_OK && cudaMalloc(q, bytes) != cudaSuccess) code = PG_ERR_CUDA;
     };
     alloc((void **)&a.wbuf, sizeof(cxf) * 2 * n);
-    alloc((void **)&a.part, sizeof(double) * P_COUNT * (size_t)nch * FZ_PSTRIDE);
+    alloc((void **)&a.part, sizeof(double) * P_COUNT * (size_t)nch * PF_PSTRIDE);
     alloc((void **)&a.bar, 2 * sizeof(FzBarrier));
     alloc((void **)&p.hcols, sizeof(double) * (size_t)nch * m * 3 * 2 * (m + 2));
     alloc((void **)&p.pe, sizeof(double) * (size_t)nch * PF_PE);

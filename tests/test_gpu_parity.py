@@ -62,21 +62,27 @@ def test_cayley_l40_whole_pulse_against_reference(gpu, precision, tol_inf, tol_n
     assert abs(prob.GetEnergyExpectationValue() - float(g["energy"])) < 1e-9
 
 
-@pytest.mark.parametrize("precision,tol_inf", [("fp64", 1e-22), ("fp32", 1e-9)])
-def test_pamp_l10_whole_pulse_against_reference(gpu, precision, tol_inf):
+@pytest.mark.parametrize("precision,fused,tol_inf,tol_norm", [("fp64", False, 1e-22, 1e-12), ("fp32", True, 1e-9, 3e-6),
+                                                           ("fp32", False, 1e-9, 1e-6)])
+def test_pamp_l10_whole_pulse_against_reference(gpu, precision, fused, tol_inf, tol_norm):
     """Hydrogen lmax 10, 150 B-splines, 1000 pAMP steps through a 10 a.u. 800 nm pulse from
     the field-free ground state with a converged Krylov basis (40 vectors): FP64, and the
-    complex64 basis with FP64 sums, against the reference templates' final state. With the
+    complex64 basis with FP64 sums on the single-kernel step and on the graphs, against the
+    reference templates' final state. The single-kernel step's norm drifts more (about 1e-6
+    over the pulse against 1e-7: its FP32 overlap solve and FP32 overlap products are not exact
+    inverses of each other); its state matches the reference to the same infidelity. With the
     workload's 20 vectors the step is not converged for this model and its trajectory is
     sensitive to rounding in any implementation, so that basis is compared over the first
     steps (next test)."""
     from pyprop_gb300.workloads import HYDROGEN_L10_PAMP, run_steps
     g = _fixture("run_pamp_l10.npz")
     prob = _problem(dict(HYDROGEN_L10_PAMP, krylov_basis_size=40), "PamPropagatorGPU", precision)
+    if precision == "fp32":
+        assert prob.Propagator.stepper.set_fused(fused) == fused
     psi = _run(prob, g["psi0"], run_steps(HYDROGEN_L10_PAMP))
     S = _overlap(prob)
     assert infidelity(g["psi"], psi, S) < tol_inf
-    assert abs(prob.psi.GetNorm() - float(g["norm"])) < (1e-12 if precision == "fp64" else 1e-6)
+    assert abs(prob.psi.GetNorm() - float(g["norm"])) < tol_norm
 
 
 @pytest.mark.parametrize("precision,tol_inf", [("fp64", 1e-18), ("fp32", 1e-11)])
