@@ -5,8 +5,8 @@ reference's own pAMP / GMRES templates (and, beside them, by the numpy oracle; t
 check that the two agree). Each test starts the GPU path from the fixture's initial state,
 runs the same number of steps through the public Problem / ensemble API and compares the
 final state: the S-weighted infidelity 1 - |<psi_ref|psi>|^2 / (<psi_ref|psi_ref><psi|psi>),
-the S-norm and the energy <H(t_end)>. Tolerances are written per test; the spec bar is
-an infidelity of 1e-8.
+the S-norm and the energy <H(t_end)>. Tolerances are written per test; the accuracy target of
+the mixed-precision paths is an infidelity of 1e-8.
 """
 import os
 
@@ -149,7 +149,7 @@ def test_ensemble_members_against_reference(gpu, pamp_step):
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
 def test_cayley_l40_equal_error_operating_points(gpu, precision):
     """The benchmark's operating points: mixed precision at GMRES tolerance 1e-7 and plain
-    FP64 at 1e-6 both end the 5000-step pulse within the spec bar (infidelity 1e-8)
+    FP64 at 1e-6 both end the 5000-step pulse within the accuracy target (infidelity 1e-8)
     of the reference run; mixed precision then needs one refinement pass per step."""
     from pyprop_gb300.workloads import EQUAL_ERROR_TOLERANCE, HYDROGEN_L40_CAYLEY, run_steps
     g = _fixture("run_cayley_l40.npz")
