@@ -231,47 +231,62 @@ __device__ __forceinline__ cxf fz_gs_update(cxf acc, const cxf *V, long long ldv
 
 // FP64 rows [lo, hi) of the flattened [Nang][N] operator applied to src (read through L2:
 // other CTAs write it): r[o] (+)= sum_e sc[slot_e] sum_d band_e[d][i] src[col_e][i + d - kb],
-// o = a N + i, real bands. Returns this thread's share of ||r||^2 over its rows.
+// o = a N + i, real bands. A row's entries are spread over FZ_RG neighbouring lanes (entry
+// e0 + g, e0 + g + FZ_RG, ... on lane g of the group) and summed by shuffles in a fixed order,
+// so a CTA's rows (a few hundred) keep all its warps' loads in flight at once. Returns this
+// thread's share of ||r||^2 over its rows.
+static const int FZ_RG = 4;
 template <int KB>
 __device__ __forceinline__ double fz_rows64(const OpDev &op, const double *__restrict__ rb, long long lo, long long hi,
                                             const cxd *sc, const cxd *src, cxd *r, bool accumulate)
 {
     const int N = op.N, kb = KB >= 0 ? KB : op.kb, b = 2 * kb + 1, ld = op.ld;
+    const int g = threadIdx.x & (FZ_RG - 1);
     double nrm = 0.0;
-    for (long long o = lo + threadIdx.x; o < hi; o += FZ_THREADS) {
-        const int a = (int)(o / N), i = (int)(o - (long long)a * N);
-        const int e0 = __ldg(op.row_ptr + a), e1 = __ldg(op.row_ptr + a + 1);
+    for (long long base = lo; base < hi; base += FZ_THREADS / FZ_RG) {  // uniform over the CTA
+        const long long o = base + threadIdx.x / FZ_RG;
         cxd acc = mk<double>(0.0, 0.0);
-        for (int e = e0; e < e1; ++e) {
-            const cxd se = sc[__ldg(op.ent_slot + e)];
-            if (se.x == 0.0 && se.y == 0.0) continue;  // e.g. the overlap in -i dt H psi
-            const double *B = rb + (size_t)__ldg(op.ent_band + e) * b * ld + i;
-            const cxd *x = src + (size_t)__ldg(op.ent_col + e) * N + i - kb;
-            double tx = 0.0, ty = 0.0;
-            if (KB >= 0) {
+        if (o < hi) {
+            const int a = (int)(o / N), i = (int)(o - (long long)a * N);
+            const int e0 = __ldg(op.row_ptr + a), e1 = __ldg(op.row_ptr + a + 1);
+            for (int e = e0 + g; e < e1; e += FZ_RG) {
+                const cxd se = sc[__ldg(op.ent_slot + e)];
+                if (se.x == 0.0 && se.y == 0.0) continue;  // e.g. the overlap in -i dt H psi
+                const double *B = rb + (size_t)__ldg(op.ent_band + e) * b * ld + i;
+                const cxd *x = src + (size_t)__ldg(op.ent_col + e) * N + i - kb;
+                double tx = 0.0, ty = 0.0;
+                if (KB >= 0) {
 #pragma unroll
-                for (int d = 0; d < 2 * KB + 1; ++d)
-                    if (i + d - kb >= 0 && i + d - kb < N) {
-                        const double c = __ldg(B + (size_t)d * ld);
-                        const cxd v = fz_ldcg(x + d);
-                        tx = fma(c, v.x, tx);
-                        ty = fma(c, v.y, ty);
-                    }
-            } else {
-                for (int d = 0; d < b; ++d)
-                    if (i + d - kb >= 0 && i + d - kb < N) {
-                        const double c = __ldg(B + (size_t)d * ld);
-                        const cxd v = fz_ldcg(x + d);
-                        tx = fma(c, v.x, tx);
-                        ty = fma(c, v.y, ty);
-                    }
+                    for (int d = 0; d < 2 * KB + 1; ++d)
+                        if (i + d - kb >= 0 && i + d - kb < N) {
+                            const double c = __ldg(B + (size_t)d * ld);
+                            const cxd v = fz_ldcg(x + d);
+                            tx = fma(c, v.x, tx);
+                            ty = fma(c, v.y, ty);
+                        }
+                } else {
+                    for (int d = 0; d < b; ++d)
+                        if (i + d - kb >= 0 && i + d - kb < N) {
+                            const double c = __ldg(B + (size_t)d * ld);
+                            const cxd v = fz_ldcg(x + d);
+                            tx = fma(c, v.x, tx);
+                            ty = fma(c, v.y, ty);
+                        }
+                }
+                cfma(acc, se, mk<double>(tx, ty));
             }
-            cfma(acc, se, mk<double>(tx, ty));
         }
-        if (accumulate) acc = acc + fz_ldcg(r + o);
-        r[o] = acc;
-        nrm = fma(acc.x, acc.x, nrm);
-        nrm = fma(acc.y, acc.y, nrm);
+#pragma unroll
+        for (int off = 1; off < FZ_RG; off <<= 1) {
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, off);
+            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, off);
+        }
+        if (o < hi && g == 0) {
+            if (accumulate) acc = acc + fz_ldcg(r + o);
+            r[o] = acc;
+            nrm = fma(acc.x, acc.x, nrm);
+            nrm = fma(acc.y, acc.y, nrm);
+        }
     }
     return nrm;
 }
