@@ -291,9 +291,9 @@ int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scales, int nsc
 int pg_pamp_set_device_exp(pg_pamp *p, int on); /* PG_ERR_STATE for on=1 when basis_size > 48 */
 int pg_pamp_last_stats(pg_pamp *p, pg_krylov_stats *stats); /* waits for the last step */
 /*
- * Single-kernel step (complex64 basis; the default where it qualifies: a rank-2 operator with
- * real bands, at most 4 source channels per row, basis_size <= 48 and its working set within a
- * CTA's shared memory, one resident CTA per channel): one cooperative launch runs the Arnoldi recurrence on T_j = U^-1 V_j (S-orthonormal,
+ * Single-kernel step (complex64 basis with double_ortho = 1; the default where it qualifies: a
+ * rank-2 operator with real bands, at most 4 source channels per row, basis_size <= 48 and its
+ * working set within a CTA's shared memory, one resident CTA per channel): one cooperative launch runs the Arnoldi recurrence on T_j = U^-1 V_j (S-orthonormal,
  * the same Krylov space and Hessenberg matrix as the balanced form), the m x m exponential in
  * double-float arithmetic in every CTA, and psi = ||psi||_S sum_j c_j T_j. Two grid barriers
  * per Arnoldi step, each a bounded wait: one that runs out sets the context's error word to 2,

@@ -459,7 +459,7 @@ extern "C" int pg_pamp_create(pg_op *op64, pg_op *op_basis, pg_banded *ovl64, pg
         PG_TRY(pamp_expm_raise_smem(pamp_expm_smem(p->m)));
         p->device_exp = false;  // FP64 arithmetic is scarce on this GPU: the host is faster for this m x m work
     }
-    if (basis_precision == PG_FP32) {
+    if (basis_precision == PG_FP32 && p->double_ortho) {  // the single-kernel step always runs CGS2
         p->fused_status = pg_pamp_fused_prepare(op_basis, ovl64, ovl_basis, p->V, p->m, p->tolerance, &p->fused);
         if (p->fused_status == PG_OK) p->use_fused = true;
         cudaGetLastError();  // a shape the single-kernel step refuses leaves no error behind
