@@ -1027,7 +1027,7 @@ def time_pamp_hydrogen_l10(torch, flush, steps=1000, warmup=5):
     ach = nbytes / (out["fp32"]["us_per_step"] * 1e-6) / 1e9
     out["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                        "traffic": profile_traffic("pamp_fused_step_kernel_hydrogen_l10_n150.md"),
-                       "kernel": "pamp_fused_step_kernel<6,true>", "algorithmic_bytes": nbytes, "peak_kind": peak_kind,
+                       "kernel": "pamp_fused_step_kernel<6,2>", "algorithmic_bytes": nbytes, "peak_kind": peak_kind,
                        "note": "1.3 MB working set resident in L2 and shared memory: latency-bound (grid and CTA "
                                "barriers)"}
     out["single_kernel_speedup_vs_graphs"] = out["fp32"]["steps_per_s"] / out["fp32_graphs"]["steps_per_s"]
