@@ -57,7 +57,11 @@ class Context:
         return ctx
 
     def bind_stream(self):
-        s = torch().cuda.current_stream(self.device).cuda_stream
+        """Bind the context to torch's current stream on its device (called before every
+        launch; the raw-handle query avoids building a Stream object each time)."""
+        t = torch()
+        raw = getattr(t._C, "_cuda_getCurrentRawStream", None)
+        s = raw(self.device) if raw is not None else t.cuda.current_stream(self.device).cuda_stream
         check(self.lib.pg_ctx_set_stream(self.h, C.c_void_p(s)), "pg_ctx_set_stream")
 
     def launches(self):
@@ -344,10 +348,9 @@ class PampStepper:
     def step(self, psi, dt, scales, want_stats=True):
         """One step; with ``want_stats`` the call waits for it and returns the statistics,
         otherwise it only enqueues (where the exponential runs on the device) and returns None."""
-        sc = np.ascontiguousarray(scales, dtype=np.complex128)
-        _, sp = nat.dptr(sc.view(np.float64))
+        sc = np.ascontiguousarray(scales, dtype=np.complex128)  # kept alive across the call
         self.ctx.bind_stream()
-        check(self.lib.pg_pamp_step(self.h, ptr(psi), float(dt), sp, len(sc),
+        check(self.lib.pg_pamp_step(self.h, ptr(psi), float(dt), sc.ctypes.data_as(nat._DP), len(sc),
                                     C.byref(self.stats) if want_stats else None), "pg_pamp_step")
         return self.stats if want_stats else None
 
@@ -401,10 +404,9 @@ class CayleyStepper:
         self.stats = nat.KrylovStats()
 
     def step(self, psi, dt, scales, want_stats=True):
-        sc = np.ascontiguousarray(scales, dtype=np.complex128)
-        _, sp = nat.dptr(sc.view(np.float64))
+        sc = np.ascontiguousarray(scales, dtype=np.complex128)  # kept alive across the call
         self.ctx.bind_stream()
-        check(self.lib.pg_cayley_step(self.h, ptr(psi), float(dt), sp, len(sc),
+        check(self.lib.pg_cayley_step(self.h, ptr(psi), float(dt), sc.ctypes.data_as(nat._DP), len(sc),
                                       C.byref(self.stats) if want_stats else None), "pg_cayley_step")
         return self.stats if want_stats else None
 
