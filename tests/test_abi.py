@@ -42,6 +42,12 @@ def test_null_arguments_rejected_without_device():
     assert lib.pg_op_destroy(None) == -1
     assert lib.pg_banded_apply(None, 0, None) == -1
     assert lib.pg_tensor_multiply_diag_bandnh(None, 1, 13, 1.0, None, 1, 1, None, 1, 1, 6, None) == -1
+    # the pAMP step's switches and statistics
+    assert lib.pg_pamp_step(None, None, 0.01, None, 0, None) == -1
+    assert lib.pg_pamp_set_fused(None, 1) == -1
+    assert lib.pg_pamp_set_device_exp(None, 1) == -1
+    assert lib.pg_pamp_set_barrier_probe(None, 1, 0) == -1
+    assert lib.pg_pamp_last_stats(None, None) == -1
 
 
 def test_header_compiles_as_c():
