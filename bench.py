@@ -581,6 +581,9 @@ def run_ours(args):
     two_e_large = time_two_electron_large(torch) if (args.two_electron_large and rank == 0) else None
     learned = time_learned_helium(torch) if (args.learned and rank == 0) else None
     pamp_l10 = time_pamp_hydrogen_l10(torch, flush) if (args.pamp_l10 and rank == 0) else None
+    if pamp_l10 is not None and world == 1 and args.cpu_steps > 0:
+        pamp_l10["cpu_baseline"] = cpu_pamp_sample()
+        pamp_l10["speedup_vs_cpu_port"] = pamp_l10["fp32"]["steps_per_s"] / pamp_l10["cpu_baseline"]["value"]
     cpu = cpu_baseline_sample(nsteps=args.cpu_steps) if (rank == 0 and world == 1 and args.cpu_steps > 0) else None
     if rank == 0:
         steps_per_s = world * args.steps / t_mixed
@@ -1174,6 +1177,51 @@ def cpu_baseline_sample(nsteps=20, procs=1):
             "sample": "%d Cayley steps from t=0 per process, numpy/scipy complex128 oracle of the reference "
                       "algorithm at GMRES tolerance %g (the complex128 equal-error tolerance; "
                       "OPENBLAS_NUM_THREADS=1)" % (nsteps, EQUAL_ERROR_TOLERANCE["fp64"])}
+
+
+def _oracle_pamp_worker(nsteps, q):
+    """Oracle pAMP steps (complex128, basis 20, CGS2) of the single-wavefunction pAMP workload."""
+    import pyprop_gb300 as pp
+    from oracle.propagators import OracleHamiltonian, OraclePam
+    from pyprop_gb300.workloads import HYDROGEN_L10_PAMP, hydrogen
+    prob = pp.Problem(pp.LoadString(hydrogen(propagator="PamPropagatorGPU", precision="fp64", **HYDROGEN_L10_PAMP)))
+    repr_ = prob.psi.GetRepresentation()
+    nang, N = repr_.GetFullShape()
+    bp = prob.Propagator.BasePropagator
+    terms = [("_".join(g.GetStorageId() for g in p.GeometryList), p.PotentialData, p.GeometryList[0].GetBasisPairs(),
+              p.TimeFunction) for p in bp.PotentialList]
+    pam = OraclePam(OracleHamiltonian(terms, repr_.overlap_rows, nang, N), HYDROGEN_L10_PAMP["krylov_basis_size"], True)
+    psi, _ = initial_state(prob)
+    dt = HYDROGEN_L10_PAMP["timestep"]
+    t0 = time.perf_counter()
+    for n in range(nsteps):
+        psi = pam.step(psi, n * dt, dt)
+    q.put(time.perf_counter() - t0)
+
+
+def cpu_pamp_sample(nsteps=100):
+    """The oracle port of the reference's pAMP step on one host core (spawned process, one BLAS
+    thread) for the single-wavefunction pAMP workload."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    saved = {k: os.environ.get(k) for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")}
+    for k in saved:
+        os.environ[k] = "1"
+    try:
+        proc = ctx.Process(target=_oracle_pamp_worker, args=(nsteps, q))
+        proc.start()
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    elapsed = q.get()
+    proc.join()
+    return {"value": nsteps / elapsed, "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": "%d pAMP steps from the field-free 1s state, numpy/scipy complex128 oracle of the reference "
+                      "algorithm (basis 20, CGS2; OPENBLAS_NUM_THREADS=1)" % nsteps}
 
 
 def run_reference(args):
