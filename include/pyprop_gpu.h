@@ -278,13 +278,16 @@ int pg_pamp_create(pg_op *op64, pg_op *op_basis, pg_banded *ovl64, pg_banded *ov
 int pg_pamp_destroy(pg_pamp *p);
 /*
  * One step. scales: host complex128 [nscales], H(t) slot values. psi: device complex128.
- * By default (basis_size <= 48) the whole step, the m x m exponential included (one CTA, the
- * scaled order-6 Pade of pamp.h:430-565), is one graph launch and the call returns without
- * waiting; with stats != NULL it waits and fills them. A singular Pade denominator zeroes that
- * step's coefficients and is reported (PG_ERR_BREAKDOWN) by the next call that reads
- * statistics. Larger bases, or pg_pamp_set_device_exp(p, 0), compute the exponential on the
- * host between two graphs (Hermitian tridiagonal H_m by implicit QL, otherwise the same
- * Pade): the call then waits every step.
+ * Three forms, all with the reference's order-6 Pade exponential (pamp.h:430-565) or, on the
+ * host, the same for a Hermitian tridiagonal H_m by implicit QL:
+ *  - complex64 basis: the single-kernel step below (the default where it qualifies);
+ *  - otherwise, by default: two captured graphs with the m x m exponential on the host between
+ *    them (the call waits every step; faster on this GPU than its FP64 Pade);
+ *  - pg_pamp_set_device_exp(p, 1) (basis_size <= 48): one graph launch with the exponential in
+ *    one CTA on the device; the call returns without waiting.
+ * With stats != NULL the call waits and fills them. On the device forms a singular Pade
+ * denominator zeroes that step's coefficients and is reported (PG_ERR_BREAKDOWN) by the next
+ * call that reads statistics.
  */
 int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scales, int nscales,
                  pg_krylov_stats *stats);
@@ -293,8 +296,9 @@ int pg_pamp_last_stats(pg_pamp *p, pg_krylov_stats *stats); /* waits for the las
 /*
  * Single-kernel step (complex64 basis with double_ortho = 1; the default where it qualifies: a
  * rank-2 operator with real bands, at most 4 source channels per row, basis_size <= 48 and its
- * working set within a CTA's shared memory, one resident CTA per channel): one cooperative launch runs the Arnoldi recurrence on T_j = U^-1 V_j (S-orthonormal,
- * the same Krylov space and Hessenberg matrix as the balanced form), the m x m exponential in
+ * working set within a CTA's shared memory, one resident CTA per channel): one cooperative
+ * launch runs the Arnoldi recurrence on T_j = U^-1 V_j (S-orthonormal, the same Krylov space
+ * and Hessenberg matrix as the balanced form), the m x m exponential in
  * double-float arithmetic in every CTA, and psi = ||psi||_S sum_j c_j T_j. Two grid barriers
  * per Arnoldi step, each a bounded wait: one that runs out sets the context's error word to 2,
  * leaves psi unchanged, and the next call that reads statistics returns PG_ERR_NOT_CONVERGED.
