@@ -208,15 +208,17 @@ static pg_scales to_scales(const double *s, int n)
 // ------------------------------------------------------------------------------------
 // pAMP
 // ------------------------------------------------------------------------------------
-// A step is one CUDA graph with no host round trip (the default, basis <= PAMP_DEV_EXP_MAXM):
-//   psi <- U psi, ||psi||, V[0] = psi/||psi||, then m Arnoldi steps on U^-H H(t) U^-1
-//   (solve, matvec, solve, CGS2); c = ||psi|| exp(-i dt H_m) e1 by one CTA (the reference's
-//   scaled Pade of order 6, pamp_expm.cuh); psi = V c, psi <- U^-1 psi.
-// or (pg_pamp_set_device_exp(p, 0)) two graphs and one host round trip:
-//   graph 1: the Arnoldi steps, Hessenberg columns to pinned memory;
+// A complex64-basis step with double orthogonalization runs as one cooperative kernel where it
+// qualifies (pamp_fused.cu). Otherwise a step is two CUDA graphs and one host round trip (the
+// default: the host computes this m x m exponential faster than this GPU's FP64 pipe):
+//   graph 1: psi <- U psi, ||psi||, V[0] = psi/||psi||, then m Arnoldi steps on
+//            U^-H H(t) U^-1 (solve, matvec, solve, CGS2), Hessenberg columns to pinned memory;
 //   host:    exp(-i dt H_m) e1 in FP64 (Hermitian tridiagonal H_m: eigen-decomposition by
 //            implicit QL; otherwise the same Pade);
 //   graph 2: coefficients to the device, psi = ||psi|| V c, psi <- U^-1 psi.
+// or (pg_pamp_set_device_exp(p, 1), basis <= PAMP_DEV_EXP_MAXM) one graph with no host round
+// trip: the same Arnoldi steps, c = ||psi|| exp(-i dt H_m) e1 by one CTA (the reference's scaled
+// Pade of order 6, pamp_expm.cuh), psi = V c, psi <- U^-1 psi.
 // A happy breakdown (beta < sqrt(eps), pamp.h:306-313) truncates the basis on the host; the
 // device normalisation maps a zero norm to a zero vector, so the extra rows stay finite and
 // get zero coefficients.
@@ -385,7 +387,7 @@ struct pg_pamp {
     bool last_hermitian = false;
     long long kernels_per_step = 0;  // kernel nodes of the two graphs
     pg_krylov_stats last_stats = {};  // of the last step (ensemble steps read it per member)
-    // device exponential (the default where m <= PAMP_DEV_EXP_MAXM): the whole step is one
+    // device exponential (pg_pamp_set_device_exp; m <= PAMP_DEV_EXP_MAXM): the whole step is one
     // graph - Arnoldi, the m x m exponential in one CTA, psi = ||psi|| V c - so a step never
     // waits for the host; statistics are read back only when asked for.
     bool device_exp = false;
@@ -749,9 +751,9 @@ extern "C" int pg_pamp_step(pg_pamp *p, void *psi, double dt, const double *scal
     return pamp_read_stats(p, st);
 }
 
-// 1: the m x m exponential on the device, no host round trip (default where the basis has at
-// most PAMP_DEV_EXP_MAXM vectors); 0: on the host between two graphs (Hermitian tridiagonal
-// H_m by implicit QL, otherwise the same Pade).
+// 1: the m x m exponential on the device, no host round trip (bases of at most
+// PAMP_DEV_EXP_MAXM vectors); 0 (the default): on the host between two graphs (Hermitian
+// tridiagonal H_m by implicit QL, otherwise the same Pade).
 extern "C" int pg_pamp_set_device_exp(pg_pamp *p, int on)
 {
     if (!p) return PG_ERR_ARG;
