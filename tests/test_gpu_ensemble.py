@@ -84,10 +84,10 @@ def _pamp_members(precision, with_field=True):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_pamp_ensemble_matches_single_members(gpu, precision):
-    """pAMP members of different sizes and fields advanced by one graph launch per step (the
-    m x m exponentials on the device, Pade of order 6) against the same members stepped alone
-    (host exponential), and a second batch built on the same members after the first is
-    destroyed."""
+    """pAMP members of different sizes and fields advanced by one launch per step (the m x m
+    exponentials on the device, Pade of order 6) against the same members stepped alone
+    (complex128: the graphs with the host exponential; complex64: the single-kernel step), and a
+    second batch built on the same members after the first is destroyed."""
     from pyprop_gb300.ensemble import PamEnsembleGPU
     alone = _pamp_members(precision)
     together = _pamp_members(precision)
